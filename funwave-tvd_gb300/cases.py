@@ -1,0 +1,100 @@
+"""Seeded synthetic cases with the shapes of the benchmark configurations.
+
+The reference measures on no public dataset; these generators stand in for
+its input decks.  Each returns ``(params, depth, phases)``: an input.txt-style
+dictionary, the interior depth (Mglob x Nglob, x = cross-shore first, metres,
+positive down) and the JON_2D phases (or None).
+
+  planar_beach   2-D planar beach with a regular wavemaker and a west
+                 sponge, periodic in y (the 250 x 500 configuration)
+  shoal_jonswap  1:50 slope from 20 m with an elliptic shoal and a
+                 directional JONSWAP wavemaker (the 2048 x 2048 configuration)
+"""
+import numpy as np
+
+
+def _smooth(noise, sigma_cells, periodic_y):
+    from scipy.ndimage import gaussian_filter
+    return gaussian_filter(noise, sigma=sigma_cells, mode=("nearest", "wrap" if periodic_y else "nearest"))
+
+
+def planar_beach(Mglob=250, Nglob=500, dx=1.0, seed=0, noise_std=0.02, noise_sigma=5.0,
+                 **overrides):
+    """Depth 5 m for x < 100 m, then a 1:20 slope up to 2 m above still water,
+    plus a seeded N(0, noise_std) field smoothed by a Gaussian of standard
+    deviation noise_sigma metres and rescaled back to noise_std.  WK_REG
+    H = 0.3 m, T = 6 s at x = 50 m (Time_ramp = 1 period), 30 m west sponge,
+    periodic in y, MinDepth 0.01 m, other keys at their reference defaults."""
+    x = np.arange(Mglob) * dx
+    h = np.where(x < 100.0, 5.0, 5.0 - (x - 100.0) / 20.0)
+    h = np.maximum(h, -2.0)
+    depth = np.repeat(h[:, None], Nglob, axis=1)
+    if noise_std > 0:
+        rng = np.random.default_rng(seed)
+        n = rng.normal(0.0, noise_std, size=(Mglob, Nglob))
+        n = _smooth(n, noise_sigma / dx, True)
+        s = n.std()
+        if s > 0:
+            n = n * (noise_std / s)
+        depth = depth + n
+    p = {
+        "Mglob": Mglob, "Nglob": Nglob, "DX": dx, "DY": dx,
+        "PERIODIC": True, "WAVEMAKER": "WK_REG",
+        "AMP_WK": 0.15, "Tperiod": 6.0, "DEP_WK": 5.0, "Xc_WK": 50.0,
+        "Theta_WK": 0.0, "Delta_WK": 0.5, "Time_ramp": 1.0,
+        "DIRECT_SPONGE": True, "Sponge_west_width": 30.0,
+        "R_sponge": 0.85, "A_sponge": 5.0,
+        "DISPERSION": True, "Gamma1": 1.0, "Gamma2": 1.0, "Gamma3": 1.0,
+        "Beta_ref": -0.531, "VISCOSITY_BREAKING": True, "SHOW_BREAKING": True,
+        "Cbrk1": 0.65, "Cbrk2": 0.35, "CFL": 0.5,
+        "MinDepth": 0.01, "MinDepthFrc": 0.1, "TOTAL_TIME": 300.0,
+    }
+    p.update(overrides)
+    return p, np.asfortranarray(depth), None
+
+
+def shoal_jonswap(Mglob=2048, Nglob=2048, dx=2.0, seed=0, **overrides):
+    """20 m flat offshore, then a 1:50 slope through the shoreline (which
+    lies 200 m from the east wall); an elliptic shoal cap
+    8*sqrt(1-(dx/200)^2-(dy/150)^2) m high centred 1.5 km offshore of the
+    shoreline and mid-domain alongshore.  JON_2D Hs = 1 m, Tp = 10 s,
+    gamma = 3.3, 0.05-0.30 Hz in 50 frequencies x 30 directions, cos^2s
+    spreading with s = 10, phases uniform on [0, 2pi) from the seed;
+    wavemaker at x = 200 m, 100 m west sponge, walls elsewhere."""
+    x = np.arange(Mglob) * dx
+    y = np.arange(Nglob) * dx
+    L = Mglob * dx
+    x_shore = L - 200.0
+    x_toe = x_shore - 20.0 * 50.0
+    h = np.where(x < x_toe, 20.0, 20.0 - (x - x_toe) / 50.0)
+    depth = np.repeat(h[:, None], Nglob, axis=1)
+    xc, yc = x_shore - 1500.0, y.mean()
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    r2 = ((X - xc) / 200.0) ** 2 + ((Y - yc) / 150.0) ** 2
+    depth = depth - 8.0 * np.sqrt(np.maximum(0.0, 1.0 - r2))
+    nf, nt = 50, 30
+    rng = np.random.default_rng(seed)
+    phases = np.asfortranarray(rng.uniform(0.0, 2.0 * np.pi, size=(nf, nt)))
+    p = {
+        "Mglob": Mglob, "Nglob": Nglob, "DX": dx, "DY": dx,
+        "PERIODIC": False, "WAVEMAKER": "JON_2D",
+        "Hmo": 1.0, "FreqPeak": 0.1, "FreqMin": 0.05, "FreqMax": 0.30, "GammaTMA": 3.3,
+        "Nfreq": nf, "Ntheta": nt, "ThetaPeak": 0.0, "SPREADING": "COS2S", "SPREADING_S": 10.0,
+        "DEP_WK": 20.0, "Xc_WK": 200.0, "Delta_WK": 0.5, "Time_ramp": 1.0,
+        "DIRECT_SPONGE": True, "Sponge_west_width": 100.0,
+        "DISPERSION": True, "VISCOSITY_BREAKING": True, "SHOW_BREAKING": True,
+        "CFL": 0.5, "MinDepth": 0.01, "MinDepthFrc": 0.1, "TOTAL_TIME": 600.0,
+    }
+    p.update(overrides)
+    return p, np.asfortranarray(depth), phases
+
+
+def random_state(Mglob, Nglob, seed=0, eta_amp=0.05, u_amp=0.1, smooth=3.0):
+    """Smooth random interior eta, u, v (for unit parity cases)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for amp in (eta_amp, u_amp, u_amp):
+        f = _smooth(rng.normal(size=(Mglob, Nglob)), smooth, False)
+        s = np.abs(f).max()
+        out.append(np.asfortranarray(f * (amp / s if s > 0 else 0.0)))
+    return tuple(out)

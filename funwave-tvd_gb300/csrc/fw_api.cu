@@ -1,0 +1,637 @@
+// fw_api.cu -- the C ABI of include/funwave_gpu.h: context creation, one
+// device arena for all state, Fortran-layout field transfer, the stepping
+// entry points and the CUDA-graph replay of whole steps.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fw_init.h"
+#include "fw_internal.h"
+
+using namespace fw;
+
+namespace {
+
+const char *kErrText[] = {"ok",
+                          "CUDA runtime error",
+                          "device allocation failed",
+                          "invalid argument",
+                          "blow-up: max|eta| exceeds EtaBlowVal",
+                          "non-finite eta",
+                          "option not supported by this build",
+                          "call out of order (context not initialised)",
+                          "no usable CUDA device"};
+
+int cuda_status(fw_ctx *c, cudaError_t e) {
+    if (e == cudaSuccess && c && c->sticky_error == 0) return FW_OK;
+    if (c && !c->sticky_error && e != cudaSuccess) c->sticky_error = (int)e;
+    return FW_ERR_CUDA;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// field table: name -> device pointer, element kind and layout
+enum Kind { CELL = 0, XFACE = 1, YFACE = 2 };
+struct FieldRef {
+    void *ptr;
+    int kind;
+    int is_mask;  // uint8 on the device, int32 on the host
+};
+
+template <typename T> bool find_field(fw_ctx *c, const char *name, FieldRef &r) {
+    Fields<T> &f = c->F<T>();
+    struct E {
+        const char *n;
+        void *p;
+        int k;
+        int m;
+    } tab[] = {
+        {"Eta", f.Eta, CELL, 0}, {"U", f.U, CELL, 0}, {"V", f.V, CELL, 0}, {"Ubar", f.Ubar, CELL, 0},
+        {"Vbar", f.Vbar, CELL, 0}, {"HU", f.HU, CELL, 0}, {"HV", f.HV, CELL, 0}, {"H", f.H, CELL, 0},
+        {"Eta0", f.Eta0, CELL, 0}, {"Ubar0", f.Ubar0, CELL, 0}, {"Vbar0", f.Vbar0, CELL, 0}, {"U0", f.U0, CELL, 0},
+        {"V0", f.V0, CELL, 0}, {"Depth", f.Depth, CELL, 0}, {"Cd", f.Cd, CELL, 0}, {"SPONGE", f.SPONGE, CELL, 0},
+        {"CD_4_SPONGE", f.CD4, CELL, 0}, {"U4", f.U4, CELL, 0}, {"V4", f.V4, CELL, 0}, {"U1p", f.U1p, CELL, 0},
+        {"V1p", f.V1p, CELL, 0}, {"Udisp", f.Udisp, CELL, 0}, {"Vdisp", f.Vdisp, CELL, 0},
+        {"ETAx", f.ETAx, CELL, 0}, {"ETAy", f.ETAy, CELL, 0}, {"ETAT", f.ETAT, CELL, 0}, {"AGE", f.AGE, CELL, 0},
+        {"nu_break", f.nu, CELL, 0}, {"SourceX", f.SourceX, CELL, 0}, {"SourceY", f.SourceY, CELL, 0},
+        {"WaveMaker_Mass", f.WM, CELL, 0}, {"HeightMax", f.Hmax, CELL, 0}, {"Depthx", f.Depthx, XFACE, 0},
+        {"P", f.P, XFACE, 0}, {"Fx", f.Fx, XFACE, 0}, {"Gx", f.Gx, XFACE, 0}, {"Depthy", f.Depthy, YFACE, 0},
+        {"Q", f.Q, YFACE, 0}, {"Fy", f.Fy, YFACE, 0}, {"Gy", f.Gy, YFACE, 0}, {"MASK", f.MASK, CELL, 1},
+        {"MASK9", f.MASK9, CELL, 1}, {"MASK_STRUC", f.MASK_STRUC, CELL, 1},
+    };
+    for (auto &e : tab)
+        if (std::strcmp(e.n, name) == 0) {
+            r.ptr = e.p;
+            r.kind = e.k;
+            r.is_mask = e.m;
+            return true;
+        }
+    return false;
+}
+
+void extent(const fw_ctx *c, int kind, int &w, int &h) {
+    w = c->g.Mloc + (kind == XFACE ? 1 : 0);
+    h = c->g.Nloc + (kind == YFACE ? 1 : 0);
+}
+
+// host (Fortran, double/int32, w x h) <-> device (pitched, T/uint8)
+template <typename T> int put_field(fw_ctx *c, const FieldRef &r, const void *host) {
+    int w, h;
+    extent(c, r.kind, w, h);
+    const size_t n = (size_t)w * h;
+    cudaError_t e;
+    if (r.is_mask) {
+        std::vector<uint8_t> tmp(n);
+        const int *src = (const int *)host;
+        for (size_t k = 0; k < n; k++) tmp[k] = (uint8_t)(src[k] != 0 ? (src[k] > 0 ? 1 : 0) : 0);
+        e = cudaMemcpy2DAsync(r.ptr, (size_t)c->g.pitch, tmp.data(), (size_t)w, (size_t)w, (size_t)h,
+                              cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    } else {
+        std::vector<T> tmp(n);
+        const double *src = (const double *)host;
+        for (size_t k = 0; k < n; k++) tmp[k] = (T)src[k];
+        e = cudaMemcpy2DAsync(r.ptr, (size_t)c->g.pitch * sizeof(T), tmp.data(), (size_t)w * sizeof(T),
+                              (size_t)w * sizeof(T), (size_t)h, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    }
+    return cuda_status(c, e);
+}
+
+template <typename T> int get_field(fw_ctx *c, const FieldRef &r, void *host) {
+    int w, h;
+    extent(c, r.kind, w, h);
+    const size_t n = (size_t)w * h;
+    cudaError_t e;
+    if (r.is_mask) {
+        std::vector<uint8_t> tmp(n);
+        e = cudaMemcpy2DAsync(tmp.data(), (size_t)w, r.ptr, (size_t)c->g.pitch, (size_t)w, (size_t)h,
+                              cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        int *dst = (int *)host;
+        for (size_t k = 0; k < n; k++) dst[k] = tmp[k];
+    } else {
+        std::vector<T> tmp(n);
+        e = cudaMemcpy2DAsync(tmp.data(), (size_t)w * sizeof(T), r.ptr, (size_t)c->g.pitch * sizeof(T),
+                              (size_t)w * sizeof(T), (size_t)h, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        double *dst = (double *)host;
+        for (size_t k = 0; k < n; k++) dst[k] = (double)tmp[k];
+    }
+    return cuda_status(c, e);
+}
+
+int put_named(fw_ctx *c, const char *name, const void *host) {
+    FieldRef r;
+    if (c->p.precision == FW_PREC_FP64) {
+        if (!find_field<double>(c, name, r)) return FW_ERR_BAD_PARAM;
+        return put_field<double>(c, r, host);
+    }
+    if (!find_field<float>(c, name, r)) return FW_ERR_BAD_PARAM;
+    return put_field<float>(c, r, host);
+}
+
+LinePart make_part(int L, int nlines) {
+    LinePart lp;
+    lp.L = L;
+    lp.nlines = nlines;
+    lp.m = 16;
+    if (L < 2 * lp.m) {
+        lp.m = L;
+        lp.P = 1;
+    } else {
+        lp.P = L / lp.m;
+    }
+    return lp;
+}
+
+// carve the arena: T fields, masks, double scratch, small tables
+template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
+    const Grid &g = c->g;
+    const size_t plane = (size_t)g.pitch * (size_t)(g.Nloc + 1);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off = align256(off + bytes);
+        return base + o;
+    };
+    Fields<T> f{};
+    T **tf[] = {&f.Eta,   &f.U,     &f.V,     &f.Ubar,   &f.Vbar,  &f.HU,   &f.HV,    &f.H,     &f.Eta0,
+                &f.Ubar0, &f.Vbar0, &f.U0,    &f.V0,     &f.Depth, &f.Depthx, &f.Depthy, &f.Cd, &f.SPONGE,
+                &f.CD4,   &f.P,     &f.Q,     &f.Fx,     &f.Fy,    &f.Gx,   &f.Gy,    &f.A,     &f.B,
+                &f.C,     &f.E,     &f.U4,    &f.V4,     &f.U1p,   &f.V1p,  &f.Udisp, &f.Vdisp, &f.ETAx,
+                &f.ETAy,  &f.ETAT,  &f.AGE,   &f.AGEn,   &f.nu,    &f.SourceX, &f.SourceY, &f.WM, &f.Hmax};
+    for (T **p : tf) *p = (T *)take(plane * sizeof(T));
+    uint8_t **mf[] = {&f.MASK, &f.MASKn, &f.MASK9, &f.MASK_STRUC};
+    for (uint8_t **p : mf) *p = (uint8_t *)take(plane);
+    double **df[] = {&f.rhs_x, &f.rhs_y, &f.ty, &f.tp, &f.tq};
+    for (double **p : df) *p = (double *)take(plane * sizeof(double));
+    const size_t nred = std::max((size_t)c->px.nlines * 2 * c->px.P, (size_t)c->py.nlines * 2 * c->py.P);
+    f.red = (double *)take(nred * 6 * sizeof(double));
+    f.dsc = (double *)take(S_NSLOT * sizeof(double));
+    f.dtmin_bits = (unsigned long long *)take(sizeof(unsigned long long));
+    f.etamax_bits = (unsigned long long *)take(sizeof(unsigned long long));
+    f.ncand = (int *)take(sizeof(int));
+    f.cand = (int *)take((size_t)c->ncand_cap * sizeof(int));
+    const int nf = c->p.wavemaker == FW_WK_JON_2D ? (c->p.nfreq > 0 ? c->p.nfreq : 1) : 1;
+    f.omega = (double *)take((size_t)nf * sizeof(double));
+    f.wmcs = (double *)take((size_t)nf * 2 * sizeof(double));
+    f.Cm = f.Sm = nullptr;  // band tables are allocated by fw_init
+    if (assign) c->F<T>() = f;
+    return off;
+}
+
+int upload_array(fw_ctx *c, void *dst, const void *src, size_t bytes) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return cuda_status(c, e);
+}
+
+double *dsc_ptr(fw_ctx *c) { return c->p.precision == FW_PREC_FP64 ? c->fd.dsc : c->ff.dsc; }
+
+template <typename T> void dispatch_stage(fw_ctx *c, int istage) { launch_stage<T>(c, istage); }
+
+// one whole step on the stream (main.F:284-535 minus OUTPUT)
+template <typename T> void enqueue_step(fw_ctx *c) {
+    launch_begin_step<T>(c);
+    for (int s = 1; s <= 3; s++) launch_stage<T>(c, s);
+    launch_end_step<T>(c);
+}
+
+int check_ready(fw_ctx *c) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    if (!c->initialized) return FW_ERR_NOT_READY;
+    if (c->sticky_error) return FW_ERR_CUDA;
+    return FW_OK;
+}
+
+int finish(fw_ctx *c) {
+    cudaError_t e = cudaGetLastError();
+    return cuda_status(c, e);
+}
+
+unsigned long long *etamax_ptr(fw_ctx *c) {
+    return c->p.precision == FW_PREC_FP64 ? c->fd.etamax_bits : c->ff.etamax_bits;
+}
+
+// host pointer state that a captured graph bakes in
+long long swap_state(fw_ctx *c) {
+    if (c->p.precision == FW_PREC_FP64) return (long long)((uintptr_t)c->fd.MASK ^ ((uintptr_t)c->fd.AGE << 1));
+    return (long long)((uintptr_t)c->ff.MASK ^ ((uintptr_t)c->ff.AGE << 1));
+}
+
+int read_status(fw_ctx *c, int *status) {
+    unsigned long long bits = 0;
+    cudaError_t e = cudaMemcpyAsync(&bits, etamax_ptr(c), sizeof(bits), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    double mx;
+    std::memcpy(&mx, &bits, sizeof(mx));
+    int st = FW_OK;
+    if (!(mx == mx) || std::isinf(mx)) st = FW_ERR_NAN;
+    else if (mx > c->EtaBlowVal) st = FW_ERR_BLOWUP;
+    if (status) *status = st;
+    return FW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void fw_params_default(fw_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->Mglob = 0;
+    p->Nglob = 0;
+    p->DX = 1.0;
+    p->DY = 1.0;
+    p->periodic = 0;
+    p->dispersion = 1;
+    p->gamma1 = 1.0;
+    p->gamma2 = 1.0;
+    p->gamma3 = 1.0;
+    p->beta_ref = -0.531;
+    p->viscosity_breaking = 1;
+    p->show_breaking = 1;
+    p->cbrk1 = 0.65;
+    p->cbrk2 = 0.35;
+    p->wavemaker_cbrk = 1.0;
+    p->nu_bkg = 0.0;
+    p->swe_eta_dep = 0.80;
+    p->cfl = 0.5;
+    p->froude_cap = 3.0;
+    p->min_depth = 0.1;
+    p->min_depth_frc = 0.1;
+    p->trough_limit = -999999.0;
+    p->crest_limit = 999999.0;
+    p->r_sponge = 0.85;
+    p->a_sponge = 5.0;
+    p->wavemaker = FW_WK_NONE;
+    p->delta_wk = 0.5;
+    p->time_ramp = 0.0;
+    p->ywidth_wk = 999999.0;
+    p->sigma_theta = 10.0;
+    p->spreading = FW_SPREAD_WRAPPED_NORMAL;
+    p->precision = FW_PREC_FP64;
+    p->device = 0;
+}
+
+const char *fw_strerror(int s) {
+    if (s > 0 || s < -8) return "unknown status";
+    return kErrText[-s];
+}
+
+int fw_create(const fw_params *p, fw_ctx **out) {
+    if (!p || !out) return FW_ERR_BAD_PARAM;
+    *out = nullptr;
+    if (p->Mglob < 2 || p->Nglob < 2 || !(p->DX > 0) || !(p->DY > 0) || !(p->cfl > 0) ||
+        (p->precision != FW_PREC_FP64 && p->precision != FW_PREC_MIXED) ||
+        (p->wavemaker < FW_WK_NONE || p->wavemaker > FW_WK_JON_2D) || !(p->min_depth_frc > 0))
+        return FW_ERR_BAD_PARAM;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p->device) {
+        cudaGetLastError();
+        return FW_ERR_NO_DEVICE;
+    }
+    if (cudaSetDevice(p->device) != cudaSuccess) return FW_ERR_NO_DEVICE;
+    fw_ctx *c = new (std::nothrow) fw_ctx();
+    if (!c) return FW_ERR_OOM;
+    c->p = *p;
+    Grid &g = c->g;
+    std::memset(&g, 0, sizeof(g));
+    g.Mglob = p->Mglob;
+    g.Nglob = p->Nglob;
+    g.Mloc = p->Mglob + 2 * NG;
+    g.Nloc = p->Nglob + 2 * NG;
+    g.pitch = ((g.Mloc + 1) + 31) / 32 * 32;
+    g.ib = NG;
+    g.ie = g.Mloc - NG - 1;
+    g.jb = NG;
+    g.je = g.Nloc - NG - 1;
+    g.periodic = p->periodic;
+    g.dispersion = p->dispersion;
+    g.visc_breaking = p->viscosity_breaking;
+    g.show_breaking = p->show_breaking;
+    g.direct_sponge = p->direct_sponge;
+    g.friction_sponge = p->friction_sponge;
+    g.eta_limiter = p->eta_limiter;
+    g.wavemaker = p->wavemaker;
+    g.nfreq = p->wavemaker == FW_WK_JON_2D ? p->nfreq : 0;
+    g.DX = p->DX;
+    g.DY = p->DY;
+    // dispersion coefficients (init.F:656-664); Gamma1/2 off without dispersion
+    g.gamma1 = p->dispersion ? p->gamma1 : 0.0;
+    g.gamma2 = p->dispersion ? p->gamma2 : 0.0;
+    g.gamma3 = p->gamma3;
+    g.b1 = p->beta_ref * p->beta_ref;
+    g.b2 = p->beta_ref;
+    g.Beta_1 = p->beta_ref + 1.0;
+    g.Beta_2 = (1.0 / 5.0) * (1.0 / 5.0) / 1.0;
+    g.cbrk1 = p->cbrk1;
+    g.cbrk2 = p->cbrk2;
+    g.wavemaker_cbrk = p->wavemaker_cbrk;
+    g.nu_bkg = p->nu_bkg;
+    g.swe_eta_dep = p->swe_eta_dep;
+    g.froude_cap = p->froude_cap;
+    g.min_depth_frc = p->min_depth_frc;
+    g.cfl = p->cfl;
+    g.fixed_dt = p->fixed_dt;
+    g.dt_fixed = p->dt_fixed;
+    g.trough = p->trough_limit;
+    g.crest = p->crest_limit;
+    g.xc_wk = p->xc_wk;
+    g.yc_wk = p->yc_wk;
+    g.ywidth_wk = p->ywidth_wk;
+    g.tperiod = p->tperiod;
+    g.time_ramp = p->time_ramp;
+    g.freq_peak = p->freq_peak;
+    g.ilo = 1;
+    g.ihi = 0;
+    g.jlo = 1;
+    g.jhi = 0;
+    c->px = make_part(p->Mglob, p->Nglob);
+    c->py = make_part(p->Nglob, p->Mglob);
+    c->ncand_cap = (p->Mglob + 2) * (p->Nglob + 2);
+    const bool fp64 = p->precision == FW_PREC_FP64;
+    const size_t bytes = fp64 ? carve<double>(c, nullptr, false) : carve<float>(c, nullptr, false);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return FW_ERR_CUDA;
+    }
+    if (cudaMalloc(&c->arena, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return FW_ERR_OOM;
+    }
+    c->arena_bytes = bytes;
+    if (fp64) carve<double>(c, (char *)c->arena, true);
+    else carve<float>(c, (char *)c->arena, true);
+    cudaError_t e = cudaMemsetAsync(c->arena, 0, bytes, c->stream);
+    const unsigned long long inf_bits = 0x7ff0000000000000ull;
+    unsigned long long *dtb = fp64 ? c->fd.dtmin_bits : c->ff.dtmin_bits;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dtb, &inf_bits, sizeof(inf_bits), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fw_destroy(c);
+        return FW_ERR_CUDA;
+    }
+    *out = c;
+    return FW_OK;
+}
+
+int fw_destroy(fw_ctx *c) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    void *band[4] = {c->fd.Cm, c->fd.Sm, c->ff.Cm, c->ff.Sm};
+    for (void *b : band)
+        if (b) cudaFree(b);
+    if (c->arena) cudaFree(c->arena);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return FW_OK;
+}
+
+int fw_init(fw_ctx *c, const double *depth, const double *eta, const double *u, const double *v,
+            const double *phases) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    HostCase hc;
+    std::string err;
+    int rc = build_case(c->p, depth, eta, u, v, phases, hc, err);
+    if (rc != FW_OK) return rc;
+    Grid &g = c->g;
+    g.T_brk = hc.T_brk;
+    g.width_wk = hc.Width_WK;
+    g.D_gen = hc.D_gen;
+    g.beta_gen = hc.beta_gen;
+    g.rlamda = hc.rlamda;
+    c->EtaBlowVal = hc.EtaBlowVal;
+    if (hc.ilo <= hc.ihi && hc.jlo <= hc.jhi) {
+        g.ilo = hc.ilo - 1;
+        g.ihi = hc.ihi - 1;
+        g.jlo = hc.jlo - 1;
+        g.jhi = hc.jhi - 1;
+    } else {
+        g.ilo = 1;
+        g.ihi = 0;
+        g.jlo = 1;
+        g.jhi = 0;
+    }
+    struct {
+        const char *n;
+        const void *d;
+    } up[] = {{"Depth", hc.Depth.data()}, {"Depthx", hc.Depthx.data()}, {"Depthy", hc.Depthy.data()},
+              {"Eta", hc.Eta.data()},     {"U", hc.U.data()},           {"V", hc.V.data()},
+              {"H", hc.H.data()},         {"HU", hc.HU.data()},         {"HV", hc.HV.data()},
+              {"Ubar", hc.Ubar.data()},   {"Vbar", hc.Vbar.data()},     {"Cd", hc.Cd.data()},
+              {"SPONGE", hc.SPONGE.data()}, {"nu_break", hc.nu.data()}, {"MASK", hc.MASK.data()},
+              {"MASK9", hc.MASK9.data()}, {"MASK_STRUC", hc.MASK_STRUC.data()}};
+    for (auto &x : up) {
+        rc = put_named(c, x.n, x.d);
+        if (rc != FW_OK) return rc;
+    }
+    // JON_2D band tables
+    if (c->p.wavemaker == FW_WK_JON_2D && !hc.Cm.empty()) {
+        const size_t nb = hc.Cm.size() * sizeof(double);
+        double *Cm = nullptr, *Sm = nullptr;
+        if (cudaMalloc(&Cm, nb) != cudaSuccess || cudaMalloc(&Sm, nb) != cudaSuccess) {
+            cudaGetLastError();
+            if (Cm) cudaFree(Cm);
+            return FW_ERR_OOM;
+        }
+        double **dCm = c->p.precision == FW_PREC_FP64 ? &c->fd.Cm : &c->ff.Cm;
+        double **dSm = c->p.precision == FW_PREC_FP64 ? &c->fd.Sm : &c->ff.Sm;
+        if (*dCm) cudaFree(*dCm);
+        if (*dSm) cudaFree(*dSm);
+        *dCm = Cm;
+        *dSm = Sm;
+        if ((rc = upload_array(c, Cm, hc.Cm.data(), nb)) != FW_OK) return rc;
+        if ((rc = upload_array(c, Sm, hc.Sm.data(), nb)) != FW_OK) return rc;
+        double *om = c->p.precision == FW_PREC_FP64 ? c->fd.omega : c->ff.omega;
+        if ((rc = upload_array(c, om, hc.omega.data(), hc.omega.size() * sizeof(double))) != FW_OK) return rc;
+    }
+    double sc[S_NSLOT] = {0};
+    if ((rc = upload_array(c, dsc_ptr(c), sc, sizeof(sc))) != FW_OK) return rc;
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    c->graph_ready = 0;
+    c->initialized = 1;
+    return FW_OK;
+}
+
+int fw_get_field(fw_ctx *c, const char *name, void *host) {
+    if (!c || !name || !host) return FW_ERR_BAD_PARAM;
+    FieldRef r;
+    if (c->p.precision == FW_PREC_FP64) {
+        if (!find_field<double>(c, name, r)) return FW_ERR_BAD_PARAM;
+        return get_field<double>(c, r, host);
+    }
+    if (!find_field<float>(c, name, r)) return FW_ERR_BAD_PARAM;
+    return get_field<float>(c, r, host);
+}
+
+int fw_set_field(fw_ctx *c, const char *name, const void *host) {
+    if (!c || !name || !host) return FW_ERR_BAD_PARAM;
+    return put_named(c, name, host);
+}
+
+int fw_get_scalar(fw_ctx *c, const char *name, double *v) {
+    if (!c || !name || !v) return FW_ERR_BAD_PARAM;
+    if (!std::strcmp(name, "TIME") || !std::strcmp(name, "DT")) {
+        double sc[S_NSLOT];
+        cudaError_t e = cudaMemcpyAsync(sc, dsc_ptr(c), sizeof(sc), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_status(c, e);
+        *v = !std::strcmp(name, "TIME") ? sc[S_TIME] : sc[S_DT];
+        return FW_OK;
+    }
+    if (!std::strcmp(name, "EtaBlowVal")) *v = c->EtaBlowVal;
+    else if (!std::strcmp(name, "T_brk")) *v = c->g.T_brk;
+    else if (!std::strcmp(name, "Width_WK")) *v = c->g.width_wk;
+    else if (!std::strcmp(name, "D_gen")) *v = c->g.D_gen;
+    else if (!std::strcmp(name, "beta_gen")) *v = c->g.beta_gen;
+    else if (!std::strcmp(name, "rlamda")) *v = c->g.rlamda;
+    else if (!std::strcmp(name, "ilo")) *v = c->g.ilo + 1;
+    else if (!std::strcmp(name, "ihi")) *v = c->g.ihi + 1;
+    else if (!std::strcmp(name, "jlo")) *v = c->g.jlo + 1;
+    else if (!std::strcmp(name, "jhi")) *v = c->g.jhi + 1;
+    else if (!std::strcmp(name, "pitch")) *v = c->g.pitch;
+    else return FW_ERR_BAD_PARAM;
+    return FW_OK;
+}
+
+int fw_set_scalar(fw_ctx *c, const char *name, double v) {
+    if (!c || !name) return FW_ERR_BAD_PARAM;
+    if (!std::strcmp(name, "TIME") || !std::strcmp(name, "DT")) {
+        const int slot = !std::strcmp(name, "TIME") ? S_TIME : S_DT;
+        cudaError_t e = cudaMemcpyAsync(dsc_ptr(c) + slot, &v, sizeof(double), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        return cuda_status(c, e);
+    }
+    if (!std::strcmp(name, "EtaBlowVal")) c->EtaBlowVal = v;
+    else if (!std::strcmp(name, "T_brk")) c->g.T_brk = v;
+    else return FW_ERR_BAD_PARAM;
+    c->graph_ready = 0;
+    return FW_OK;
+}
+
+#define DISPATCH(fn)                                                           \
+    do {                                                                       \
+        int rc_ = check_ready(c);                                              \
+        if (rc_ != FW_OK) return rc_;                                          \
+        if (c->p.precision == FW_PREC_FP64) fn<double>(c); else fn<float>(c);  \
+        return finish(c);                                                      \
+    } while (0)
+
+int fw_begin_step(fw_ctx *c) { DISPATCH(launch_begin_step); }
+int fw_exchange(fw_ctx *c) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    if (c->p.precision == FW_PREC_FP64) launch_exchange<double>(c, false);
+    else launch_exchange<float>(c, false);
+    return finish(c);
+}
+int fw_estimate_dt(fw_ctx *c) { DISPATCH(launch_estimate_dt); }
+int fw_cal_dispersion(fw_ctx *c) { DISPATCH(launch_dispersion); }
+int fw_fluxes(fw_ctx *c) { DISPATCH(launch_fluxes); }
+int fw_source_terms(fw_ctx *c) { DISPATCH(launch_sources_debug); }
+int fw_update_mask(fw_ctx *c) { DISPATCH(launch_update_mask); }
+int fw_wave_breaking(fw_ctx *c) { DISPATCH(launch_breaking); }
+int fw_sponge_damping(fw_ctx *c) { DISPATCH(launch_sponge); }
+
+int fw_estimate_huv(fw_ctx *c, int istage) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    if (istage < 1 || istage > 3) return FW_ERR_BAD_PARAM;
+    if (c->p.precision == FW_PREC_FP64) launch_estimate_huv<double>(c, istage);
+    else launch_estimate_huv<float>(c, istage);
+    return finish(c);
+}
+
+int fw_stage(fw_ctx *c, int istage) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    if (istage < 1 || istage > 3) return FW_ERR_BAD_PARAM;
+    if (c->p.precision == FW_PREC_FP64) launch_stage<double>(c, istage);
+    else launch_stage<float>(c, istage);
+    return finish(c);
+}
+
+int fw_end_step(fw_ctx *c, int *status) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    cudaError_t e = cudaMemsetAsync(etamax_ptr(c), 0, sizeof(unsigned long long), c->stream);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    if (c->p.precision == FW_PREC_FP64) launch_end_step<double>(c);
+    else launch_end_step<float>(c);
+    if ((rc = finish(c)) != FW_OK) return rc;
+    return read_status(c, status);
+}
+
+int fw_step(fw_ctx *c, int nsteps, int *status) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    if (nsteps < 0) return FW_ERR_BAD_PARAM;
+    if (status) *status = FW_OK;
+    if (nsteps == 0) return FW_OK;
+    cudaError_t e = cudaMemsetAsync(etamax_ptr(c), 0, sizeof(unsigned long long), c->stream);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    const bool fp64 = c->p.precision == FW_PREC_FP64;
+    int left = nsteps;
+    // a graph holds two steps, after which every ping-pong buffer is back in
+    // its place; it is (re)captured whenever the host-side buffer state
+    // differs from the one it was captured with
+    while (left >= 2) {
+        if (!c->graph_ready || c->graph_state != swap_state(c)) {
+            if (c->graph) {
+                cudaGraphExecDestroy(c->graph);
+                c->graph = nullptr;
+            }
+            const long long st = swap_state(c);
+            cudaGraph_t graph;
+            e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return cuda_status(c, e);
+            for (int k = 0; k < 2; k++) {
+                if (fp64) enqueue_step<double>(c);
+                else enqueue_step<float>(c);
+            }
+            e = cudaStreamEndCapture(c->stream, &graph);
+            if (e != cudaSuccess) return cuda_status(c, e);
+            e = cudaGraphInstantiate(&c->graph, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_status(c, e);
+            c->graph_ready = 1;
+            c->graph_state = st;
+        }
+        e = cudaGraphLaunch(c->graph, c->stream);
+        if (e != cudaSuccess) return cuda_status(c, e);
+        left -= 2;
+    }
+    if (left == 1) {
+        if (fp64) enqueue_step<double>(c);
+        else enqueue_step<float>(c);
+        c->graph_ready = 0;
+    }
+    if ((rc = finish(c)) != FW_OK) return rc;
+    return read_status(c, status);
+}
+
+int fw_sync(fw_ctx *c) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    return cuda_status(c, cudaStreamSynchronize(c->stream));
+}
+
+long long fw_launch_count(fw_ctx *c) { return c ? c->launches : -1; }
+void *fw_stream(fw_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+}  // extern "C"

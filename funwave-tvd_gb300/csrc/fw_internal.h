@@ -1,0 +1,111 @@
+// fw_internal.h -- device state and launch interface of the GB300 solver.
+//
+// Device layout: every 2-D field (cells, x-faces, y-faces) is stored
+// x-fastest with one common pitch (elements) >= Mloc+1, rounded up to 32
+// elements, and Nloc+1 rows; index (i, j) -> i + j*pitch with 0-based i, j
+// (Fortran I = i+1).  Bulk fields are T (double in FP64 mode, float in mixed
+// mode); masks are uint8; the tridiagonal u/v recovery works in double.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include "funwave_gpu.h"
+
+namespace fw {
+
+constexpr int NG = 3;  // Nghost (mod_global.F:129)
+
+// Scalars every kernel needs, passed by value.
+struct Grid {
+    int Mloc, Nloc, pitch;
+    int ib, ie, jb, je;      // 0-based interior bounds, inclusive
+    int Mglob, Nglob;
+    int periodic, dispersion, visc_breaking, show_breaking;
+    int direct_sponge, friction_sponge, eta_limiter, wavemaker;
+    int ilo, ihi, jlo, jhi;  // 0-based wavemaker band (empty when ilo > ihi)
+    int nfreq;
+    double DX, DY;
+    double gamma1, gamma2, gamma3, b1, b2, Beta_1, Beta_2;
+    double cbrk1, cbrk2, wavemaker_cbrk, nu_bkg, T_brk;
+    double swe_eta_dep, froude_cap, min_depth_frc, cfl, dt_fixed;
+    int fixed_dt;
+    double trough, crest;
+    double xc_wk, yc_wk, ywidth_wk, width_wk;
+    double D_gen, beta_gen, rlamda, tperiod, time_ramp, freq_peak;
+};
+
+// device scalar slots (double array)
+enum : int { S_TIME = 0, S_DT = 1, S_DTMIN = 2, S_ETAMAX = 3, S_NSLOT = 8 };
+
+template <typename T>
+struct Fields {
+    T *Eta, *U, *V, *Ubar, *Vbar, *HU, *HV, *H;
+    T *Eta0, *Ubar0, *Vbar0, *U0, *V0;
+    T *Depth, *Depthx, *Depthy, *Cd, *SPONGE, *CD4;
+    T *P, *Q, *Fx, *Fy, *Gx, *Gy;
+    T *A, *B, *C, *E;                 // exchanged Uxx+Vxy, DUxx+DVxy, Uxy+Vyy, DUxy+DVyy
+    T *U4, *V4, *U1p, *V1p, *Udisp, *Vdisp;  // Udisp = U1pp+U2+U3
+    T *ETAx, *ETAy, *ETAT;
+    T *AGE, *AGEn, *nu;               // AGE ping-pong (old / new)
+    T *SourceX, *SourceY, *WM;        // materialised only by the unit entry points
+    T *Hmax;
+    uint8_t *MASK, *MASKn, *MASK9, *MASK_STRUC;
+    double *rhs_x, *rhs_y;            // tmp4 of GET_Eta_U_V_HU_HV
+    double *ty, *tp, *tq;             // chunked line-solver scratch
+    double *red;                      // reduced systems
+    double *Cm, *Sm, *omega, *wmcs;   // JON_2D band tables and cos/sin(omega t)
+    double *dsc;                      // device scalars (S_*)
+    int *cand, *ncand;                // breaking candidates
+    unsigned long long *dtmin_bits;
+    unsigned long long *etamax_bits;
+};
+
+// line-solver partition of one direction
+struct LinePart {
+    int L;       // line length (interior rows)
+    int nlines;  // number of lines
+    int m;       // rows per chunk (the last chunk takes the remainder)
+    int P;       // chunks per line
+};
+
+// launchers (fw_kernels.cu), all asynchronous on the context stream
+template <typename T> void launch_begin_step(fw_ctx *c);
+template <typename T> void launch_exchange(fw_ctx *c, bool with_sponge);
+template <typename T> void launch_estimate_dt(fw_ctx *c);
+template <typename T> void launch_dispersion(fw_ctx *c);
+template <typename T> void launch_fluxes(fw_ctx *c);
+template <typename T> void launch_sources_debug(fw_ctx *c);
+template <typename T> void launch_estimate_huv(fw_ctx *c, int istage);
+template <typename T> void launch_update_mask(fw_ctx *c);
+template <typename T> void launch_breaking(fw_ctx *c);
+template <typename T> void launch_sponge(fw_ctx *c);
+template <typename T> void launch_end_step(fw_ctx *c);
+template <typename T> void launch_stage(fw_ctx *c, int istage);
+
+}  // namespace fw
+
+#include <cuda_runtime.h>
+
+// Host context behind the opaque C handle.
+struct fw_ctx {
+    fw_params p;
+    fw::Grid g;
+    cudaStream_t stream = nullptr;
+    fw::Fields<double> fd{};
+    fw::Fields<float> ff{};
+    fw::LinePart px{}, py{};
+    void *arena = nullptr;       // one device allocation holds every field
+    size_t arena_bytes = 0;
+    int ncand_cap = 0;
+    long long launches = 0;
+    int initialized = 0;
+    int sticky_error = 0;        // first CUDA error seen by a launcher
+    double EtaBlowVal = 0.0;
+    cudaGraphExec_t graph = nullptr;
+    int graph_ready = 0;
+    long long graph_state = 0;   // host buffer state the graph was captured with
+    template <typename T> fw::Fields<T> &F();
+};
+template <> inline fw::Fields<double> &fw_ctx::F<double>() { return fd; }
+template <> inline fw::Fields<float> &fw_ctx::F<float>() { return ff; }

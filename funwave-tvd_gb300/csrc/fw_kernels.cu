@@ -1,0 +1,1579 @@
+// fw_kernels.cu -- sm_103a kernels of the FUNWAVE-TVD SSP-RK3 stage.
+//
+// Every kernel reproduces one or more of the reference's Fortran units on
+// the device-resident state (layout in fw_internal.h).  Index ranges,
+// in-place update orders and stale-value semantics follow the reference:
+//   - ghost cells hold exactly what EXCHANGE / EXCHANGE_DISPERSION leave
+//     (PHI_COLL order: periodic copy, x mirror on interior rows, y mirror on
+//     all columns; bc.F:631-1272), including the periodic corner cells that
+//     keep the value of the x-ghost cell they copy from before that cell is
+//     refilled;
+//   - BOUNDARY_CONDITION's overlapping dry-face writes (bc.F:214-293) are
+//     resolved per face by the write that comes last in the reference's loop;
+//   - UPDATE_MASK is a Jacobi update (masks.F:75-143) with the order-
+//     dependent Depthx/Depthy reset (masks.F:152-161) resolved per face;
+//   - the breaking AGE sweep (breaker.F:149-229) is an in-place Gauss-Seidel
+//     sweep; it is reproduced exactly by evaluating every cell whose result
+//     does not depend on its neighbours in parallel, then iterating the rest
+//     (cells with AGE = 0 and Cbrk2 <= ETAt < Cbrk1) to the fixed point of
+//     the sweep's acyclic dependency graph.
+// T is the storage and arithmetic type of the bulk fields (double or
+// float); the tridiagonal u/v recovery always runs in double.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "fw_internal.h"
+
+namespace fw {
+
+#define IDX(i, j) ((size_t)(i) + (size_t)(j) * (size_t)g.pitch)
+
+// pi as the reference stores it: a default-REAL literal (mod_param.F:71)
+constexpr double PI_SP = (double)(float)3.141592653;
+constexpr double GRAV = 9.81;
+constexpr double SMALL = 0.000001;
+constexpr double LARGE = 999999.0;
+
+__device__ __forceinline__ double fsqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float fsqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double fabs_(double x) { return fabs(x); }
+__device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
+__device__ __forceinline__ double fcopysign(double a, double b) { return copysign(a, b); }
+__device__ __forceinline__ float fcopysign(float a, float b) { return copysignf(a, b); }
+__device__ __forceinline__ double fexp(double x) { return exp(x); }
+__device__ __forceinline__ float fexp(float x) { return expf(x); }
+__device__ __forceinline__ double fsin(double x) { return sin(x); }
+__device__ __forceinline__ float fsin(float x) { return sinf(x); }
+__device__ __forceinline__ double fcos(double x) { return cos(x); }
+__device__ __forceinline__ float fcos(float x) { return cosf(x); }
+__device__ __forceinline__ double ftanh(double x) { return tanh(x); }
+__device__ __forceinline__ float ftanh(float x) { return tanhf(x); }
+__device__ __forceinline__ double fatan2(double y, double x) { return atan2(y, x); }
+__device__ __forceinline__ float fatan2(float y, float x) { return atan2f(y, x); }
+
+template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
+template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
+
+// ---------------------------------------------------------------------------
+// exchange source of a ghost cell (PHI_COLL, serial branches)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int mirror_x(const Grid &g, int i) {
+    return i < g.ib ? 2 * g.ib - 1 - i : (i > g.ie ? 2 * g.ie + 1 - i : i);
+}
+__device__ __forceinline__ int mirror_y(const Grid &g, int j) {
+    return j < g.jb ? 2 * g.jb - 1 - j : (j > g.je ? 2 * g.je + 1 - j : j);
+}
+// periodic-y source row of a ghost row (bc.F:735-740)
+__device__ __forceinline__ int period_y(const Grid &g, int j) {
+    return j < g.jb ? j + g.je - 2 : (j > g.je ? j - g.je + 2 : j);
+}
+
+// ---------------------------------------------------------------------------
+// CAL_DISPERSION, part 1 (dispersion.F:62-289): masked derivatives at the
+// exchange source of every cell, combined into the four sums the rest of
+// the unit uses, plus ETAx/ETAy (exchanged) and ETAT.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    const T DX = (T)g.DX, DY = (T)g.DY, mdf = (T)g.min_depth_frc;
+    const size_t id = IDX(i, j);
+    // ETAT from the previous stage's face fluxes (dispersion.F:103-119)
+    if (i <= g.Mloc - 2 && j <= g.Nloc - 2)
+        f.ETAT[id] = -(f.P[IDX(i + 1, j)] - f.P[id]) / DX - (f.Q[IDX(i, j + 1)] - f.Q[id]) / DY;
+
+    const bool gx = (i < g.ib) || (i > g.ie);
+    const bool gy = (j < g.jb) || (j > g.je);
+    const int si = mirror_x(g, i);
+    int sj = j;
+    T sy3 = (T)1;  // sign of VTYPE 3 fields in a y ghost
+    bool stale = false;
+    if (gy) {
+        if (g.periodic) {
+            sj = period_y(g, j);
+            stale = gx;  // periodic corner: keeps the pre-exchange value
+        } else {
+            sj = mirror_y(g, j);
+            sy3 = (T)-1;
+        }
+    }
+    const T sx2 = gx ? (T)-1 : (T)1;  // sign of VTYPE 2 fields in an x ghost
+
+    const T m9 = (T)f.MASK9[IDX(si, sj)];
+    const bool wall = (si == g.ib) || (si == g.ie) || (sj == g.jb) || (sj == g.je);
+#define LU(a, b) f.U[IDX(si + (a), sj + (b))]
+#define LV(a, b) f.V[IDX(si + (a), sj + (b))]
+#define LDU(a, b) (tmax(f.Depth[IDX(si + (a), sj + (b))], mdf) * LU(a, b))
+#define LDV(a, b) (tmax(f.Depth[IDX(si + (a), sj + (b))], mdf) * LV(a, b))
+#define DXX(F) (((F(1, 0) - (T)2 * F(0, 0) + F(-1, 0)) / DX / DX) * m9)
+#define DYY(F) (((F(0, 1) - (T)2 * F(0, 0) + F(0, -1)) / DY / DY) * m9)
+#define DXY(F)                                                                              \
+    (wall ? (T)0                                                                            \
+          : ((((F(1, 1) - F(1, -1)) / (T)2 / DY) - ((F(-1, 1) - F(-1, -1)) / (T)2 / DY)) / (T)2 / \
+             DX) * m9)
+    const T Uxx = DXX(LU), Vyy = DYY(LV), Uxy = DXY(LU), Vxy = DXY(LV);
+    const T DUxx = DXX(LDU), DVyy = DYY(LDV), DUxy = DXY(LDU), DVxy = DXY(LDV);
+#undef LU
+#undef LV
+#undef LDU
+#undef LDV
+#undef DXX
+#undef DYY
+#undef DXY
+    f.A[id] = sx2 * Uxx + Vxy;
+    f.B[id] = sx2 * DUxx + DVxy;
+    f.C[id] = Uxy + sy3 * Vyy;
+    f.E[id] = DUxy + sy3 * DVyy;
+    if (!stale && (g.gamma2 > 0.0 || g.show_breaking)) {
+        const T ex = (f.Eta[IDX(si + 1, sj)] - f.Eta[IDX(si - 1, sj)]) / DX / (T)2 * m9;
+        const T ey = (f.Eta[IDX(si, sj + 1)] - f.Eta[IDX(si, sj - 1)]) / DY / (T)2 * m9;
+        f.ETAx[id] = sx2 * ex;
+        f.ETAy[id] = sy3 * ey;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// CAL_DISPERSION, part 2 (dispersion.F:293-503): U4, V4 on every cell;
+// U1p, V1p and U1pp+U2+U3, V1pp+V2+V3 on the interior.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    const size_t id = IDX(i, j);
+    const T DX = (T)g.DX, DY = (T)g.DY, mdf = (T)g.min_depth_frc;
+    const T B1 = (T)g.Beta_1, B2 = (T)g.Beta_2, g2 = (T)g.gamma2, b2 = (T)g.b2;
+    const T one = (T)1, two = (T)2, half = (T)0.5;
+    const T D = f.Depth[id], reta = f.Eta[id], m9 = (T)f.MASK9[id];
+    const T a = f.A[id], b = f.B[id], c = f.C[id], e = f.E[id];
+    T u4 = (one / (T)3 - B1 + half * B1 * B1) * D * D * a + (B1 - one / two) * D * b;
+    T v4 = (one / (T)3 - B1 + half * B1 * B1) * D * D * c + (B1 - one / two) * D * e;
+    if (g.gamma2 > 0.0) {
+        const T ken1 = (one / (T)6 - B1 + B1 * B1) * D * reta * B2 +
+                       (one / two * B1 * B1 - one / (T)6) * reta * reta * B2 * B2;
+        const T ken2 = (B1 - one / two) * reta * B2;
+        u4 = u4 + g2 * m9 * (ken1 * a + ken2 * b);
+        v4 = v4 + g2 * m9 * (ken1 * c + ken2 * e);
+    }
+    f.U4[id] = u4;
+    f.V4[id] = v4;
+    if (i < g.ib || i > g.ie || j < g.jb || j > g.je) return;
+
+    f.U1p[id] = half * (one - B1) * (one - B1) * D * D * a + (B1 - one) * D * b;
+    f.V1p[id] = half * (one - B1) * (one - B1) * D * D * c + (B1 - one) * D * e;
+    if (!(g.gamma2 > 0.0)) return;
+
+    const T DT = (T)f.dsc[S_DT];
+    const bool wall = (i == g.ib) || (i == g.ie) || (j == g.jb) || (j == g.je);
+#define AT(F, a_, b_) f.F[IDX(i + (a_), j + (b_))]
+    const T UxxVxy = a, UxyVyy = c, HUxxHVxy = b, HUxyHVyy = e;
+    const T UxxVxy_x = (AT(A, 1, 0) - AT(A, -1, 0)) / two / DX;
+    const T UxxVxy_y = (AT(A, 0, 1) - AT(A, 0, -1)) / two / DY;
+    const T UxyVyy_x = (AT(C, 1, 0) - AT(C, -1, 0)) / two / DX;
+    const T UxyVyy_y = (AT(C, 0, 1) - AT(C, 0, -1)) / two / DY;
+    const T HUxxHVxy_x = (AT(B, 1, 0) - AT(B, -1, 0)) / two / DX;
+    const T HUxxHVxy_y = (AT(B, 0, 1) - AT(B, 0, -1)) / two / DY;
+    const T HUxyHVyy_x = (AT(E, 1, 0) - AT(E, -1, 0)) / two / DX;
+    const T HUxyHVyy_y = (AT(E, 0, 1) - AT(E, 0, -1)) / two / DY;
+    const T rh = D;
+    const T rhx = (AT(Depth, 1, 0) - AT(Depth, -1, 0)) / two / DX;
+    const T rhy = (AT(Depth, 0, 1) - AT(Depth, 0, -1)) / two / DY;
+    const T ETAx = f.ETAx[id], ETAy = f.ETAy[id], ETAT = f.ETAT[id];
+    // first derivatives of U, V, DU, DV (derivatives.F:123-162)
+    const T Ux = (AT(U, 1, 0) - AT(U, -1, 0)) / DX / two * m9;
+    const T Vx = (AT(V, 1, 0) - AT(V, -1, 0)) / DX / two * m9;
+    const T Uy = (AT(U, 0, 1) - AT(U, 0, -1)) / DY / two * m9;
+    const T Vy = (AT(V, 0, 1) - AT(V, 0, -1)) / DY / two * m9;
+#define DUP(a_, b_) (tmax(AT(Depth, a_, b_), mdf) * AT(U, a_, b_))
+#define DVP(a_, b_) (tmax(AT(Depth, a_, b_), mdf) * AT(V, a_, b_))
+    const T DUx = (DUP(1, 0) - DUP(-1, 0)) / DX / two * m9;
+    const T DVy = (DVP(0, 1) - DVP(0, -1)) / DY / two * m9;
+    // time derivatives Ut=(U-U0)/DT (dispersion.F:133-141) and their
+    // derivatives; the cross derivatives are zero on the wall rows
+#define UT(a_, b_) ((AT(U, a_, b_) - AT(U0, a_, b_)) / DT)
+#define VT(a_, b_) ((AT(V, a_, b_) - AT(V0, a_, b_)) / DT)
+#define DUT(a_, b_) (tmax(AT(Depth, a_, b_), mdf) * UT(a_, b_))
+#define DVT(a_, b_) (tmax(AT(Depth, a_, b_), mdf) * VT(a_, b_))
+#define D1X(F) (((F(1, 0) - F(-1, 0)) / DX / two) * m9)
+#define D1Y(F) (((F(0, 1) - F(0, -1)) / DY / two) * m9)
+#define D2X(F) (((F(1, 0) - two * F(0, 0) + F(-1, 0)) / DX / DX) * m9)
+#define D2Y(F) (((F(0, 1) - two * F(0, 0) + F(0, -1)) / DY / DY) * m9)
+#define D2XY(F) \
+    (wall ? (T)0 : ((((F(1, 1) - F(1, -1)) / two / DY) - ((F(-1, 1) - F(-1, -1)) / two / DY)) / two / DX) * m9)
+    const T Utx = D1X(UT), Vty = D1Y(VT);
+    const T Utxx = D2X(UT), Vtyy = D2Y(VT);
+    const T Utxy = D2XY(UT), Vtxy = D2XY(VT);
+    const T DUtx = D1X(DUT), DVty = D1Y(DVT);
+    const T DUtxx = D2X(DUT), DVtyy = D2Y(DVT);
+    const T DUtxy = D2XY(DUT), DVtxy = D2XY(DVT);
+#undef D1X
+#undef D1Y
+#undef D2X
+#undef D2Y
+#undef D2XY
+#undef UT
+#undef VT
+#undef DUT
+#undef DVT
+#undef DUP
+#undef DVP
+    const T Uc = f.U[id], Vc = f.V[id];
+#undef AT
+    T U1pp = -reta * B2 * ETAx * B2 * (Utx + Vty) - half * reta * reta * B2 * B2 * (Utxx + Vtxy) -
+             ETAx * B2 * (DUtx + DVty) - reta * B2 * (DUtxx + DVtxy);
+    T V1pp = -reta * B2 * ETAy * B2 * (Utx + Vty) - half * reta * reta * B2 * B2 * (Utxy + Vtyy) -
+             ETAy * B2 * (DUtx + DVty) - reta * B2 * (DUtxy + DVtyy);
+    T ken1 = B1 * (one - B1) * rh * ETAT * B2 - B1 * B1 * reta * B2 * ETAT * B2;
+    T ken2 = B1 * (one - B1) * rh * reta * B2 - half * B1 * B1 * reta * reta * B2 * B2;
+    T ken3 = B1 * ETAT * B2;
+    T ken4 = B1 * reta * B2;
+    U1pp = U1pp - ken1 * UxxVxy - ken2 * (Utxx + Vtxy) + ken3 * HUxxHVxy + ken4 * (DUtxx + DVtxy);
+    V1pp = V1pp - ken1 * UxyVyy - ken2 * (Utxy + Vtyy) + ken3 * HUxyHVyy + ken4 * (DUtxy + DVtyy);
+
+    ken1 = (B1 - one) * (rhx + ETAx) * B2;
+    ken2 = (B1 - one) * (rh + reta) * B2;
+    ken3 = ((one - B1) * (one - B1) * rh * rhx * B2 * B2 - B1 * (one - B1) * (rhx * reta * B2 + rh * ETAx * B2) +
+            (B1 * B1 - one) * reta * ETAx * B2 * B2);
+    ken4 = (half * (one - B1) * (one - B1) * rh * rh * B2 * B2 - B1 * (one - B1) * rh * reta * B2 +
+            half * (B1 * B1 - one) * reta * reta * B2 * B2);
+    const T ken5 = ((one - B1) * (one - B1) * rh * rhy * B2 * B2 -
+                    B1 * (one - B1) * (rhy * reta * B2 + rh * ETAy * B2) + (B1 * B1 - one) * reta * ETAy * B2 * B2);
+    const T U2 = ken1 * (Uc * HUxxHVxy + Vc * HUxyHVyy) +
+                 ken2 * (Ux * HUxxHVxy + Uc * HUxxHVxy_x + Vx * HUxyHVyy + Vc * HUxyHVyy_x) +
+                 ken3 * (Uc * UxxVxy + Vc * UxyVyy) + ken4 * (Ux * UxxVxy + Uc * UxxVxy_x + Vx * UxyVyy + Vc * UxyVyy_x) +
+                 B2 * B2 * (DUx + DVy + reta * B2 * (Ux + Vy)) * (HUxxHVxy + ETAx * B2 * (Ux + Vy) + reta * B2 * UxxVxy);
+    ken1 = (B1 - one) * (rhy + ETAy) * B2;
+    const T V2 = ken1 * (Uc * HUxxHVxy + Vc * HUxyHVyy) +
+                 ken2 * (Uy * HUxxHVxy + Uc * HUxxHVxy_y + Vy * HUxyHVyy + Vc * HUxyHVyy_y) +
+                 ken5 * (Uc * UxxVxy + Vc * UxyVyy) + ken4 * (Uy * UxxVxy + Uc * UxxVxy_y + Vy * UxyVyy + Vc * UxyVyy_y) +
+                 B2 * B2 * (DUx + DVy + reta * B2 * (Ux + Vy)) * (HUxyHVyy + ETAy * B2 * (Ux + Vy) + reta * B2 * UxyVyy);
+    const T omega_0 = Vx - Uy;
+    const T omega_1 = (b2 * rhx + B1 * ETAx) * B2 * (HUxyHVyy + (b2 * rh + B1 * reta) * B2 * UxyVyy) -
+                      (b2 * rhy + B1 * ETAy) * B2 * (HUxxHVxy + (b2 * rh + B1 * reta) * B2 * UxxVxy);
+    ken1 = ((B1 - one / two) * (reta + rh) * B2);
+    ken2 = (one / (T)3 - B1 + half * B1 * B1) * rh * rh * B2 * B2 + (one / (T)6 - B1 + B1 * B1) * rh * reta * B2 +
+           (one / two * B1 * B1 - one / (T)6) * reta * reta * B2 * B2;
+    const T U3 = -Vc * omega_1 - omega_0 * (ken1 * HUxyHVyy + ken2 * UxyVyy);
+    const T V3 = Uc * omega_1 + omega_0 * (ken1 * HUxxHVxy + ken2 * UxxVxy);
+    f.Udisp[id] = U1pp + U2 + U3;
+    f.Vdisp[id] = V1pp + V2 + V3;
+}
+
+// ---------------------------------------------------------------------------
+// FLUXES (fluxes.F:52-117): 4th-order MUSCL-TVD (CONSTRUCT_HO_X/Y
+// :1531-1754), Zhou wave speeds (:352-439), HLL (:171-194) and
+// BOUNDARY_CONDITION (bc.F:53-295), fused per face.
+// ---------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ T lim3(T a, T b, T c) {
+    if (a >= (T)0) return tmax((T)0, tmin(tmin(a, (T)2 * b), (T)2 * c));
+    return tmin((T)0, tmax(tmax(a, (T)2 * b), (T)2 * c));
+}
+// Din(p) from v[0..3] = Vin(p-2..p+1), m[0..3] = MASK(p-2..p+1)
+template <typename T> __device__ __forceinline__ T ho_din(const T *v, const int *m) {
+    T TXP1 = v[1] - v[0], TXP2 = v[2] - v[1], TXP3 = v[3] - v[2];
+    T DVP1 = lim3(TXP1, TXP2, TXP3), DVP2 = lim3(TXP2, TXP3, TXP1), DVP3 = lim3(TXP3, TXP1, TXP2);
+    if (m[0] == 0 || m[3] == 0) {
+        TXP1 = TXP2;
+        TXP3 = TXP2;
+        DVP1 = lim3(TXP1, TXP2, TXP3);
+        DVP2 = lim3(TXP2, TXP3, TXP1);
+        DVP3 = lim3(TXP3, TXP1, TXP2);
+    }
+    if (m[1] == 0 || m[2] == 0) {
+        DVP1 = (T)0;
+        DVP2 = (T)0;
+        DVP3 = (T)0;
+    }
+    return TXP2 - (T)1 / (T)6 * (DVP3 - (T)2 * DVP2 + DVP1);
+}
+template <typename T> __device__ __forceinline__ T vl_guard(T t) {
+    if (fabs_(t) <= (T)SMALL) t = (T)SMALL * fcopysign((T)1, t);
+    return t;
+}
+template <typename T> __device__ __forceinline__ T vl_phi(T rat) {
+    T van = (T)0;
+    if (fabs_((T)1 + rat) > (T)SMALL) van = (rat + fabs_(rat)) / ((T)1 + rat);
+    return van;
+}
+// face values of one field at face p: v[0..5] = Vin(p-3..p+2)
+template <typename T>
+__device__ __forceinline__ void ho_face(const T *v, const int *m, T &L, T &R) {
+    const T d0 = ho_din(v + 0, m + 0), d1 = ho_din(v + 1, m + 1), d2 = ho_din(v + 2, m + 2);
+    T t1 = vl_guard(d0), t2 = vl_guard(d1);
+    T van1 = vl_phi(t2 / t1), van2 = vl_phi(t1 / t2);
+    L = v[2] + ((T)1 / (T)6) * (van1 * t1 + (T)2 * van2 * t2);
+    t1 = vl_guard(d1);
+    t2 = vl_guard(d2);
+    van1 = vl_phi(t2 / t1);
+    van2 = vl_phi(t1 / t2);
+    R = v[3] - ((T)1 / (T)6) * ((T)2 * van1 * t1 + van2 * t2);
+}
+template <typename T> __device__ __forceinline__ T hll(T SL, T SR, T FL, T FR, T UL, T UR) {
+    if (SL >= (T)0) return FL;
+    if (SR <= (T)0) return FR;
+    T f = SR * FL - SL * FR + SL * SR * (UR - UL);
+    if (fabs_(SR - SL) < (T)SMALL) return f / (T)SMALL;
+    return f / (SR - SL);
+}
+template <typename T> __device__ __forceinline__ T press(T Xi, T Deps, T g3) {
+    return (T)0.5 * (T)GRAV * (Xi * Xi * g3 + (T)2 * Xi * Deps);
+}
+
+// One face of direction DIR (0: x-faces, 1: y-faces).  Normal velocity is
+// U for x and V for y; the tangential one the other.
+template <typename T, int DIR>
+__global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (DIR == 0) {
+        if (i < g.ib || i > g.ie + 1 || j < g.jb || j > g.je) return;
+    } else {
+        if (i < g.ib || i > g.ie || j < g.jb || j > g.je + 1) return;
+    }
+    const int di = DIR == 0 ? 1 : 0, dj = DIR == 0 ? 0 : 1;
+    const T g1 = (T)g.gamma1, g3 = (T)g.gamma3;
+    T vu[6], vv[6], vhu[6], vhv[6], ve[6], vu4[6], vv4[6];
+    int mk[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const size_t q = IDX(i + (k - 3) * di, j + (k - 3) * dj);
+        vu[k] = f.U[q];
+        vv[k] = f.V[q];
+        vhu[k] = f.HU[q];
+        vhv[k] = f.HV[q];
+        ve[k] = f.Eta[q];
+        vu4[k] = f.U4[q];
+        vv4[k] = f.V4[q];
+        mk[k] = f.MASK[q];
+    }
+    T UL, UR, VL, VR, HUL, HUR, HVL, HVR, EL, ER, U4L = 0, U4R = 0, V4L = 0, V4R = 0;
+    ho_face(vu, mk, UL, UR);
+    ho_face(vv, mk, VL, VR);
+    ho_face(vhu, mk, HUL, HUR);
+    ho_face(vhv, mk, HVL, HVR);
+    ho_face(ve, mk, EL, ER);
+    if (g.dispersion) {
+        ho_face(vu4, mk, U4L, U4R);
+        ho_face(vv4, mk, V4L, V4R);
+    }
+    const size_t fid = IDX(i, j);
+    const T Dd = DIR == 0 ? f.Depthx[fid] : f.Depthy[fid];
+    const T HL = EL + Dd, HR = ER + Dd;
+    // MASK9u(Mloc1,:) = MASK9(Mloc,:) (fluxes.F:1333); the faces computed
+    // here never reach that column
+    const T m9 = (T)f.MASK9[fid];
+    // normal (n) and tangential (t) components
+    const T nL = DIR == 0 ? UL : VL, nR = DIR == 0 ? UR : VR;
+    const T tL = DIR == 0 ? VL : UL, tR = DIR == 0 ? VR : UR;
+    const T n4L = DIR == 0 ? U4L : V4L, n4R = DIR == 0 ? U4R : V4R;
+    const T t4L = DIR == 0 ? V4L : U4L, t4R = DIR == 0 ? V4R : U4R;
+    const T qnL = DIR == 0 ? HUL : HVL, qnR = DIR == 0 ? HUR : HVR;  // HU for x, HV for y
+    const T qtL = DIR == 0 ? HVL : HUL, qtR = DIR == 0 ? HVR : HUR;
+    // mass flux PL/QL, normal momentum flux FxL/GyL, tangential GxL/FyL
+    const T ML = qnL + g1 * m9 * HL * n4L;
+    const T MR = qnR + g1 * m9 * HR * n4R;
+    const T NL = g3 * ML * (nL + g1 * m9 * n4L) + (T)0.5 * (T)GRAV * ((EL) * (EL)*g3 + (T)2 * (EL) * (Dd));
+    const T NR = g3 * MR * (nR + g1 * m9 * n4R) + (T)0.5 * (T)GRAV * ((ER) * (ER)*g3 + (T)2 * (ER) * (Dd));
+    T TL, TR;
+    if (DIR == 0) {
+        TL = HL * (nL + g1 * m9 * n4L) * (tL + g1 * m9 * t4L) * g3;
+        TR = HR * (nR + g1 * m9 * n4R) * (tR + g1 * m9 * t4R) * g3;
+    } else {
+        TL = HL * (tL + g1 * m9 * t4L) * (nL + g1 * m9 * n4L) * g3;
+        TR = HR * (tR + g1 * m9 * t4R) * (nR + g1 * m9 * n4R) * g3;
+    }
+    // WAVE_SPEED (Zhou et al. 2001)
+    const T SQR_PHI_L = fsqrt((T)GRAV * fabs_(HL));
+    const T SQR_PHI_R = fsqrt((T)GRAV * fabs_(HR));
+    const T SQR_PHI_S = (T)0.5 * (SQR_PHI_L + SQR_PHI_R) + (T)0.25 * (nL - nR);
+    const T U_S = (T)0.5 * (nL + nR) + SQR_PHI_L - SQR_PHI_R;
+    const T SL = tmin(nL - SQR_PHI_L, U_S - SQR_PHI_S);
+    const T SR = tmax(nR + SQR_PHI_R, U_S + SQR_PHI_S);
+    T Pm = hll(SL, SR, ML, MR, EL, ER);
+    T Nm = hll(SL, SR, NL, NR, qnL, qnR);
+    T Tm = hll(SL, SR, TL, TR, qtL, qtR);
+    // BOUNDARY_CONDITION: walls, then the dry-cell loop (last write wins)
+    const int lo = DIR == 0 ? g.ib : g.jb, hi = DIR == 0 ? g.ie : g.je;
+    const int pos = DIR == 0 ? i : j;
+    const bool wall_on = DIR == 0 || !g.periodic;
+    if (wall_on && pos == lo) {
+        Pm = (T)0;
+        Nm = press(ER, Dd, g3);
+        Tm = (T)0;
+    }
+    if (wall_on && pos == hi + 1) {
+        Pm = (T)0;
+        Nm = press(EL, Dd, g3);
+        Tm = (T)0;
+    }
+    const int mL = mk[2], mR = mk[3];  // cells pos-1 and pos
+    if (mL < 1) {
+        Pm = (T)0;
+        Nm = (pos - 1 != hi) ? press(ER, Dd, g3) * (T)mR : (T)0;
+        Tm = (T)0;
+    }
+    if (mR < 1) {
+        Pm = (T)0;
+        Nm = (pos != lo) ? press(EL, Dd, g3) * (T)mL : (T)0;
+        Tm = (T)0;
+    }
+    if (DIR == 0) {
+        f.P[fid] = Pm;
+        f.Fx[fid] = Nm;
+        f.Gx[fid] = Tm;
+    } else {
+        f.Q[fid] = Pm;
+        f.Gy[fid] = Nm;
+        f.Fy[fid] = Tm;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// SourceTerms (sources.F:56-548) at one interior cell, with the wavemaker
+// mass of WK_REG / JON_2D (sources.F:109-134).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T wavemaker_mass(const Grid &g, const Fields<T> &f, int i, int j, double TIME) {
+    if (i < g.ilo || i > g.ihi || j < g.jlo || j > g.jhi) return (T)0;
+    if (g.wavemaker == FW_WK_REG) {
+        const T AA = ftanh((T)PI_SP / ((T)g.time_ramp * (T)g.tperiod) * (T)TIME) * (T)g.D_gen;
+        const T xmk = (T)(i - g.ib) * (T)g.DX, ymk = (T)(j - g.jb) * (T)g.DY;
+        const T dxm = xmk - (T)g.xc_wk;
+        return AA * fexp(-(T)g.beta_gen * (dxm * dxm)) *
+               fsin((T)g.rlamda * (ymk - (T)0) - (T)2 * (T)PI_SP / (T)g.tperiod * (T)TIME);
+    }
+    if (g.wavemaker == FW_WK_JON_2D) {
+        const T AA = ftanh((T)PI_SP / ((T)g.time_ramp / (T)g.freq_peak) * (T)TIME);
+        const int bw = g.ihi - g.ilo + 1, bh = g.jhi - g.jlo + 1;
+        const size_t b = (size_t)(i - g.ilo) + (size_t)(j - g.jlo) * bw;
+        T s = (T)0;
+        for (int k = 0; k < g.nfreq; k++)
+            s = s + AA * ((T)f.Cm[b + (size_t)k * bw * bh] * (T)f.wmcs[2 * k] +
+                          (T)f.Sm[b + (size_t)k * bw * bh] * (T)f.wmcs[2 * k + 1]);
+        return s;
+    }
+    return (T)0;
+}
+
+template <typename T>
+__device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, int i, int j, T wm, T &SX,
+                                             T &SY) {
+    const T DX = (T)g.DX, DY = (T)g.DY, mdf = (T)g.min_depth_frc;
+    const T g1 = (T)g.gamma1, g2 = (T)g.gamma2;
+    const size_t id = IDX(i, j);
+    const size_t ie_ = IDX(i + 1, j), iw = IDX(i - 1, j), in_ = IDX(i, j + 1), is = IDX(i, j - 1);
+    const T U = f.U[id], V = f.V[id];
+    const T spd = fsqrt(U * U + V * V);
+    const T m9 = (T)f.MASK9[id];
+    const T mk = (T)f.MASK[id];
+    const T Hm = tmax(f.H[id], mdf);
+    const T Eta = f.Eta[id];
+    const T U4 = f.U4[id], V4 = f.V4[id];
+    const T dPQ = (f.P[ie_] - f.P[id]) / DX + (f.Q[in_] - f.Q[id]) / DY;
+    const T FrcInsX = -f.Cd[id] * U * spd;
+    T sx = (T)GRAV * (Eta) / DX * (f.Depthx[ie_] - f.Depthx[id]) * mk + FrcInsX +
+           g1 * m9 * Hm *
+               (U * (T)0.5 * (f.U4[ie_] - f.U4[iw]) / DX + V * (T)0.5 * (f.U4[in_] - f.U4[is]) / DY +
+                U4 * (T)0.5 * (f.U[ie_] - f.U[iw]) / DX + V4 * (T)0.5 * (f.U[in_] - f.U[is]) / DY -
+                g2 * m9 * f.Udisp[id]) +
+           g1 * m9 * dPQ * (U4 - f.U1p[id]) + wm * U;
+    const T FrcInsY = -f.Cd[id] * V * spd;
+    T sy = (T)GRAV * (Eta) / DY * (f.Depthy[in_] - f.Depthy[id]) * mk + FrcInsY +
+           g1 * m9 * Hm *
+               (U * (T)0.5 * (f.V4[ie_] - f.V4[iw]) / DX + V * (T)0.5 * (f.V4[in_] - f.V4[is]) / DY +
+                U4 * (T)0.5 * (f.V[ie_] - f.V[iw]) / DX + V4 * (T)0.5 * (f.V[in_] - f.V[is]) / DY -
+                g2 * m9 * f.Vdisp[id]) +
+           g1 * m9 * dPQ * (V4 - f.V1p[id]) + wm * V;
+    if (g.friction_sponge) {
+        sx = sx - f.CD4[id] * U * spd * f.Depth[id];
+        sy = sy - f.CD4[id] * V * spd * f.Depth[id];
+    }
+    if (g.visc_breaking) {
+        // nu_vis is a float array (sources.F:69): the face sums are float sums
+        const float nc = (float)f.nu[id];
+        const T nxp = (T)((float)f.nu[ie_] + nc), nxm = (T)((float)f.nu[iw] + nc);
+        const T nyp = (T)((float)f.nu[in_] + nc), nym = (T)((float)f.nu[is] + nc);
+        const T HUc = f.HU[id], HVc = f.HV[id];
+        const T bx = (T)0.5 / DX * (nxp * (T)1 / DX * (f.HU[ie_] - HUc) - nxm * (T)1 / DX * (HUc - f.HU[iw])) +
+                     (T)0.5 / DY * (nyp * (T)1 / DY * (f.HU[in_] - HUc) - nym * (T)1 / DY * (HUc - f.HU[is]));
+        sx = sx + bx;
+        const T by = (T)0.5 / DX * (nxp * (T)1 / DX * (f.HV[ie_] - HVc) - nxm * (T)1 / DX * (HVc - f.HV[iw])) +
+                     (T)0.5 / DY * (nyp * (T)1 / DY * (f.HV[in_] - HVc) - nym * (T)1 / DY * (HVc - f.HV[is]));
+        sy = sy + by;
+    }
+    SX = sx;
+    SY = sy;
+}
+
+// SourceTerms alone (materialises SourceX, SourceY, WaveMaker_Mass)
+template <typename T>
+__global__ void __launch_bounds__(256) k_sources(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + g.ib;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + g.jb;
+    if (i > g.ie || j > g.je) return;
+    const T wm = wavemaker_mass(g, f, i, j, f.dsc[S_TIME]);
+    T sx, sy;
+    source_terms(g, f, i, j, wm, sx, sy);
+    f.SourceX[IDX(i, j)] = sx;
+    f.SourceY[IDX(i, j)] = sy;
+    f.WM[IDX(i, j)] = wm;
+}
+
+// ---------------------------------------------------------------------------
+// ESTIMATE_HUV (etauv_solver.F:53-351) fused with SourceTerms, plus the H
+// update and the right-hand sides of the tridiagonal systems of
+// GET_Eta_U_V_HU_HV (etauv_solver.F:365-539).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(Grid g, Fields<T> f, T al, T be) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    const size_t id = IDX(i, j);
+    const T g3 = (T)g.gamma3;
+    if (i < g.ib || i > g.ie || j < g.jb || j > g.je) {
+        f.H[id] = f.Eta[id] * g3 + f.Depth[id];  // H = Eta*Gamma3+Depth on all cells
+        return;
+    }
+    const T DX = (T)g.DX, DY = (T)g.DY;
+    const T DT = (T)f.dsc[S_DT];
+    const double TIME = f.dsc[S_TIME];
+    const T wm = wavemaker_mass(g, f, i, j, TIME);
+    T SX, SY;
+    source_terms(g, f, i, j, wm, SX, SY);
+
+    const size_t ie_ = IDX(i + 1, j), in_ = IDX(i, j + 1);
+    T R1 = -(T)1 / DX * (f.P[ie_] * (T)1 + f.P[id] * (T)-1) - (T)1 / DY * (f.Q[in_] * (T)1 + f.Q[id] * (T)-1);
+    if (g.wavemaker != FW_WK_NONE) {
+        const T xmk = (T)(i - g.ib) * DX, ymk = (T)(j - g.jb) * DY;
+        if (fabs_(xmk - (T)g.xc_wk) < (T)g.width_wk && fabs_(ymk - (T)g.yc_wk) < (T)g.ywidth_wk / (T)2)
+            R1 = R1 + wm;
+    }
+    T eta = al * f.Eta0[id] + be * (f.Eta[id] + DT * R1);
+    if (g.eta_limiter) {
+        if (eta < (T)g.trough) eta = (T)g.trough;
+        if (eta > (T)g.crest) eta = (T)g.crest;
+    }
+    const T R2 = -(T)1 / DX * (f.Fx[ie_] * (T)1 + f.Fx[id] * (T)-1) -
+                 (T)1 / DY * (f.Fy[in_] * (T)1 + f.Fy[id] * (T)-1) + SX;
+    const T ubar = al * f.Ubar0[id] + be * (f.Ubar[id] + DT * R2);
+    const T R3 = -(T)1 / DX * (f.Gx[ie_] * (T)1 + f.Gx[id] * (T)-1) -
+                 (T)1 / DY * (f.Gy[in_] * (T)1 + f.Gy[id] * (T)-1) + SY;
+    const T vbar = al * f.Vbar0[id] + be * (f.Vbar[id] + DT * R3);
+    f.Eta[id] = eta;
+    f.Ubar[id] = ubar;
+    f.Vbar[id] = vbar;
+    const T H = eta * g3 + f.Depth[id];
+    f.H[id] = H;
+    if (!g.dispersion) return;
+
+    // tmp4 of the x and y systems, in double (etauv_solver.F:410-411, 508-509)
+    const double ddx = g.DX, ddy = g.DY, mdf = g.min_depth_frc;
+    const double g1 = g.gamma1, b1 = g.b1, b2 = g.b2;
+    const double m9 = (double)f.MASK9[id];
+    const double mk = (double)f.MASK[id];
+    const double dep = tmax((double)f.Depth[id], mdf);
+    const bool wall = (i == g.ib) || (i == g.ie) || (j == g.jb) || (j == g.je);
+    double Vxy = 0.0, DVxy = 0.0, Uxy = 0.0, DUxy = 0.0;
+    if (!wall) {
+#define XY(F)                                                                                 \
+    ((((F(1, 1) - F(1, -1)) / 2.0 / ddy) - ((F(-1, 1) - F(-1, -1)) / 2.0 / ddy)) / 2.0 / ddx * m9)
+#define LV(a, b) ((double)f.V[IDX(i + (a), j + (b))])
+#define LU(a, b) ((double)f.U[IDX(i + (a), j + (b))])
+#define LDV(a, b) (tmax((double)f.Depth[IDX(i + (a), j + (b))], mdf) * LV(a, b))
+#define LDU(a, b) (tmax((double)f.Depth[IDX(i + (a), j + (b))], mdf) * LU(a, b))
+        Vxy = XY(LV);
+        DVxy = XY(LDV);
+        Uxy = XY(LU);
+        DUxy = XY(LDU);
+#undef XY
+#undef LV
+#undef LU
+#undef LDV
+#undef LDU
+    }
+    const double Hm = tmax((double)H, mdf);
+    f.rhs_x[id] = (double)ubar * mk / Hm + g1 * m9 * (-b1 / 2.0 * dep * dep * Vxy - b2 * dep * DVxy);
+    f.rhs_y[id] = (double)vbar * mk / Hm + g1 * m9 * (-b1 / 2.0 * dep * dep * Uxy - b2 * dep * DUxy);
+}
+
+// ---------------------------------------------------------------------------
+// Tridiagonal u/v recovery (TRIDx_ser / TRIDy_ser / TRIDy_periodic,
+// tridiagnal.F:59-398) as a partitioned line solver in double:
+//   A: every chunk of m rows eliminates its interior rows for three right-
+//      hand sides and emits two rows of a reduced tridiagonal system;
+//   B: one thread per line solves the reduced system (two right-hand sides
+//      and the Sherman-Morrison combination for periodic y);
+//   C: every chunk back-substitutes its interior rows.
+// Rows are the reference's normalised rows a x(k-1) + x(k) + c x(k+1) = d.
+// ---------------------------------------------------------------------------
+template <typename T, int DIR>
+__device__ __forceinline__ void tri_coef(const Grid &g, const Fields<T> &f, int i, int j, double &a, double &c,
+                                         double &d) {
+    const double h = DIR == 0 ? g.DX : g.DY;
+    const double mdf = g.min_depth_frc, g1 = g.gamma1, b1 = g.b1, b2 = g.b2;
+    const size_t id = IDX(i, j);
+    const double dep = tmax((double)f.Depth[id], mdf);
+    const double depl = tmax((double)f.Depth[DIR == 0 ? IDX(i - 1, j) : IDX(i, j - 1)], mdf);
+    const double depr = tmax((double)f.Depth[DIR == 0 ? IDX(i + 1, j) : IDX(i, j + 1)], mdf);
+    const double m9 = (double)f.MASK9[id];
+    const double tmp1 = g1 * m9 * (b1 / 2.0 / h / h * dep * dep + b2 / h / h * depl * dep);
+    const double tmp2 = 1.0 + g1 * m9 * (-b1 / h / h * dep * dep - 2.0 * b2 / h / h * dep * dep);
+    const double tmp3 = g1 * m9 * (b1 / 2.0 / h / h * dep * dep + b2 / h / h * dep * depr);
+    const double tmp4 = DIR == 0 ? f.rhs_x[id] : f.rhs_y[id];
+    if (tmp2 != 0.0 || f.MASK[id] > 0) {
+        a = tmp1 / tmp2;
+        c = tmp3 / tmp2;
+        d = tmp4 / tmp2;
+    } else {
+        a = 0.0;
+        c = 0.0;
+        d = 0.0;
+    }
+}
+
+// row k (0..L-1) of line l -> cell
+template <int DIR> __device__ __forceinline__ void line_cell(const Grid &g, int l, int k, int &i, int &j) {
+    if (DIR == 0) {
+        i = g.ib + k;
+        j = g.jb + l;
+    } else {
+        i = g.ib + l;
+        j = g.jb + k;
+    }
+}
+
+// coefficients of row k of line l, with the periodic end-row scaling of
+// TRIDy_periodic (tridiagnal.F:168-173) when PER
+template <typename T, int DIR, bool PER>
+__device__ __forceinline__ void row_coef(const Grid &g, const Fields<T> &f, const LinePart &lp, int l, int k,
+                                         double &a, double &c, double &d) {
+    int i, j;
+    line_cell<DIR>(g, l, k, i, j);
+    tri_coef<T, DIR>(g, f, i, j, a, c, d);
+    if (PER) {
+        if (k == 0) {
+            double a2, c2, d2;
+            int ie2, je2;
+            line_cell<DIR>(g, l, lp.L - 1, ie2, je2);
+            tri_coef<T, DIR>(g, f, ie2, je2, a2, c2, d2);  // c_end
+            c = c / (1 + c2);
+            d = d / (1 + c2);
+        } else if (k == lp.L - 1) {
+            double a2, c2, d2;
+            int ib2, jb2;
+            line_cell<DIR>(g, l, 0, ib2, jb2);
+            tri_coef<T, DIR>(g, f, ib2, jb2, a2, c2, d2);  // a_beg
+            a = a / (1 + a2);
+            d = d / (1 + a2);
+        }
+    }
+}
+
+template <int DIR>
+__device__ __forceinline__ void chunk_of(const LinePart &lp, int t, int &l, int &ch) {
+    // x lines: consecutive threads walk the chunks of one line;
+    // y lines: consecutive threads walk neighbouring lines (coalesced)
+    if (DIR == 0) {
+        l = t / lp.P;
+        ch = t % lp.P;
+    } else {
+        ch = t / lp.nlines;
+        l = t % lp.nlines;
+    }
+}
+
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(128) k_tri_a(Grid g, Fields<T> f, LinePart lp) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= lp.nlines * lp.P) return;
+    int l, ch;
+    chunk_of<DIR>(lp, t, l, ch);
+    const int s = ch * lp.m;
+    const int e = (ch == lp.P - 1) ? lp.L - 1 : s + lp.m - 1;
+    double as, cs, ds, ae, ce, de;
+    row_coef<T, DIR, PER>(g, f, lp, l, s, as, cs, ds);
+    row_coef<T, DIR, PER>(g, f, lp, l, e, ae, ce, de);
+    if (s == 0) as = 0.0;           // first row: no lower neighbour
+    if (e == lp.L - 1) ce = 0.0;    // last row: no upper neighbour
+    double lo_s, di_s, up_s, r_s, lo_e, di_e, up_e, r_e;
+    if (e - s >= 2) {
+        // interior rows s+1..e-1: forward sweep with three right-hand sides
+        double cp = 0.0, yp = 0.0, pp = 0.0, qp = 0.0;
+        for (int k = s + 1; k <= e - 1; k++) {
+            double a, c, d;
+            row_coef<T, DIR, PER>(g, f, lp, l, k, a, c, d);
+            const double lower = (k > s + 1) ? a : 0.0;
+            const double r = 1.0 - lower * cp;
+            const double upper = (k < e - 1) ? c : 0.0;
+            cp = upper / r;
+            yp = (d - lower * yp) / r;
+            pp = ((k == s + 1 ? a : 0.0) - lower * pp) / r;
+            qp = ((k == e - 1 ? c : 0.0) - lower * qp) / r;
+            int ii, jj;
+            line_cell<DIR>(g, l, k, ii, jj);
+            const size_t q = IDX(ii, jj);
+            f.ty[q] = yp;
+            f.tp[q] = pp;
+            f.tq[q] = qp;
+            // keep c' for the backward sweep in rhs_x/rhs_y of this row
+            (DIR == 0 ? f.rhs_x : f.rhs_y)[q] = cp;
+        }
+        // backward sweep
+        double yn = 0.0, pn = 0.0, qn = 0.0;
+        double y1 = 0, p1 = 0, q1 = 0, yl = 0, pl = 0, ql = 0;
+        for (int k = e - 1; k >= s + 1; k--) {
+            int ii, jj;
+            line_cell<DIR>(g, l, k, ii, jj);
+            const size_t q = IDX(ii, jj);
+            const double cpk = (DIR == 0 ? f.rhs_x : f.rhs_y)[q];
+            const double yk = f.ty[q] - cpk * yn;
+            const double pk = f.tp[q] - cpk * pn;
+            const double qk = f.tq[q] - cpk * qn;
+            f.ty[q] = yk;
+            f.tp[q] = pk;
+            f.tq[q] = qk;
+            yn = yk;
+            pn = pk;
+            qn = qk;
+            if (k == e - 1) {
+                yl = yk;
+                pl = pk;
+                ql = qk;
+            }
+            if (k == s + 1) {
+                y1 = yk;
+                p1 = pk;
+                q1 = qk;
+            }
+        }
+        lo_s = as;
+        di_s = 1.0 - cs * p1;
+        up_s = -cs * q1;
+        r_s = ds - cs * y1;
+        lo_e = -ae * pl;
+        di_e = 1.0 - ae * ql;
+        up_e = ce;
+        r_e = de - ae * yl;
+    } else {
+        lo_s = as;
+        di_s = 1.0;
+        up_s = cs;
+        r_s = ds;
+        lo_e = ae;
+        di_e = 1.0;
+        up_e = ce;
+        r_e = de;
+    }
+    double *red = f.red + ((size_t)l * 2 * lp.P + 2 * ch) * 6;
+    red[0] = lo_s;
+    red[1] = di_s;
+    red[2] = up_s;
+    red[3] = r_s;
+    red[4] = (PER && s == 0) ? 1.0 : 0.0;  // second right-hand side (scaled below)
+    red[6 + 0] = lo_e;
+    red[6 + 1] = di_e;
+    red[6 + 2] = up_e;
+    red[6 + 3] = r_e;
+    red[6 + 4] = (PER && e == lp.L - 1) ? 1.0 : 0.0;
+}
+
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(128) k_tri_b(Grid g, Fields<T> f, LinePart lp) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= lp.nlines) return;
+    const int n = 2 * lp.P;
+    double *red = f.red + (size_t)l * n * 6;
+    double a_beg = 0.0, c_end = 0.0;
+    if (PER) {
+        double a, c, d;
+        int i, j;
+        line_cell<DIR>(g, l, 0, i, j);
+        tri_coef<T, DIR>(g, f, i, j, a, c, d);
+        a_beg = a;
+        line_cell<DIR>(g, l, lp.L - 1, i, j);
+        tri_coef<T, DIR>(g, f, i, j, a, c, d);
+        c_end = c;
+        // e = [1/(1+c_end), 0, ..., 0, -1/(1+a_beg)] (tridiagnal.F:207-215)
+        red[4] = 1.0 / (1.0 + c_end);
+        red[(size_t)(n - 1) * 6 + 4] = -1.0 / (1.0 + a_beg);
+    }
+    // Thomas on the reduced rows: slot 5 keeps c', slots 3/4 the rhs
+    double cp = 0.0, r1 = 0.0, r2 = 0.0;
+    for (int k = 0; k < n; k++) {
+        double *row = red + (size_t)k * 6;
+        const double lo = (k > 0) ? row[0] : 0.0;
+        const double den = row[1] - lo * cp;
+        cp = (k < n - 1 ? row[2] : 0.0) / den;
+        r1 = (row[3] - lo * r1) / den;
+        row[5] = cp;
+        row[3] = r1;
+        if (PER) {
+            r2 = (row[4] - lo * r2) / den;
+            row[4] = r2;
+        }
+    }
+    double x1 = 0.0, x2 = 0.0;
+    for (int k = n - 1; k >= 0; k--) {
+        double *row = red + (size_t)k * 6;
+        x1 = row[3] - row[5] * x1;
+        row[3] = x1;
+        if (PER) {
+            x2 = row[4] - row[5] * x2;
+            row[4] = x2;
+        }
+    }
+    if (PER) {
+        const double y1b = red[3], y1e = red[(size_t)(n - 1) * 6 + 3];
+        const double y2b = red[4], y2e = red[(size_t)(n - 1) * 6 + 4];
+        const double beta = (c_end * y1b - a_beg * y1e) / (1.0 - (c_end * y2b - a_beg * y2e));
+        for (int k = 0; k < n; k++) {
+            double *row = red + (size_t)k * 6;
+            row[3] = row[3] + beta * row[4];
+        }
+    }
+}
+
+template <typename T, int DIR>
+__global__ void __launch_bounds__(128) k_tri_c(Grid g, Fields<T> f, LinePart lp) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= lp.nlines * lp.P) return;
+    int l, ch;
+    chunk_of<DIR>(lp, t, l, ch);
+    const int s = ch * lp.m;
+    const int e = (ch == lp.P - 1) ? lp.L - 1 : s + lp.m - 1;
+    const double *red = f.red + ((size_t)l * 2 * lp.P + 2 * ch) * 6;
+    const double xs = red[3], xe = red[6 + 3];
+    T *out = DIR == 0 ? f.U : f.V;
+    int i, j;
+    line_cell<DIR>(g, l, s, i, j);
+    out[IDX(i, j)] = (T)xs;
+    line_cell<DIR>(g, l, e, i, j);
+    out[IDX(i, j)] = (T)xe;
+    for (int k = s + 1; k <= e - 1; k++) {
+        line_cell<DIR>(g, l, k, i, j);
+        const size_t q = IDX(i, j);
+        out[q] = (T)(f.ty[q] - f.tp[q] * xs - f.tq[q] * xe);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// GET_Eta_U_V_HU_HV tail (etauv_solver.F:558-600): dry zeroing, HU/HV and
+// the Froude cap, with the MASK of the start of the stage.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_post(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    const size_t id = IDX(i, j);
+    const T mdf = (T)g.min_depth_frc;
+    const bool interior = !(i < g.ib || i > g.ie || j < g.jb || j > g.je);
+    if (interior) {
+        if (!g.dispersion) {
+            const T Hm = tmax(f.H[id], mdf);
+            f.U[id] = f.Ubar[id] / Hm;
+            f.V[id] = f.Vbar[id] / Hm;
+        }
+        if (f.MASK[id] < 1) {
+            f.Ubar[id] = (T)0;
+            f.Vbar[id] = (T)0;
+            f.U[id] = (T)0;
+            f.V[id] = (T)0;
+            f.HU[id] = (T)0;
+            f.HV[id] = (T)0;
+        } else {
+            const T Hm = tmax(f.H[id], mdf);
+            const T u = f.U[id], v = f.V[id];
+            f.HU[id] = Hm * u;
+            f.HV[id] = Hm * v;
+            const T Utotal = fsqrt(u * u + v * v);
+            const T Fr = fsqrt((T)GRAV * Hm);
+            if (Utotal / Fr > (T)g.froude_cap) {
+                const T th = fatan2(v, u);
+                const T un = (T)g.froude_cap * Fr * fcos(th);
+                const T vn = (T)g.froude_cap * Fr * fsin(th);
+                f.U[id] = un;
+                f.V[id] = vn;
+                f.HU[id] = un * Hm;
+                f.HV[id] = vn * Hm;
+            }
+        }
+    }
+}
+
+// Ubar = HU, Vbar = HV on every cell when DISPERSION is off (etauv_solver.F:596-600)
+template <typename T>
+__global__ void k_nodisp_copy(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    const size_t id = IDX(i, j);
+    f.Ubar[id] = f.HU[id];
+    f.Vbar[id] = f.HV[id];
+}
+
+// ---------------------------------------------------------------------------
+// UPDATE_MASK (masks.F:51-205): MASK (Jacobi into MASKn), the Depthx/
+// Depthy reset at old-dry cells, MASK9.  Launched over (Mloc+1) x (Nloc+1)
+// so that every face has a thread.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ bool in_mask_range(const Grid &g, int a, int b) {
+    return a >= g.ib - 2 && a <= g.ie + 2 && b >= g.jb - 2 && b <= g.je + 2;
+}
+template <typename T>
+__device__ __forceinline__ int new_mask(const Grid &g, const Fields<T> &f, int a, int b) {
+    const size_t q = IDX(a, b);
+    const int m = f.MASK[q];
+    if (!in_mask_range<T>(g, a, b) || f.MASK_STRUC[q] != 1) return m;
+    // the total-depth tests run in double in both precisions
+    const double eta = (double)f.Eta[q];
+    if (m < 1) {
+        int r = m;
+        if (eta > -(double)f.Depth[q]) r = 1;
+        if (f.MASK[IDX(a - 1, b)] == 1 && (double)f.Eta[IDX(a - 1, b)] > eta) r = 1;
+        if (f.MASK[IDX(a + 1, b)] == 1 && (double)f.Eta[IDX(a + 1, b)] > eta) r = 1;
+        if (f.MASK[IDX(a, b - 1)] == 1 && (double)f.Eta[IDX(a, b - 1)] > eta) r = 1;
+        if (f.MASK[IDX(a, b + 1)] == 1 && (double)f.Eta[IDX(a, b + 1)] > eta) r = 1;
+        return r;
+    }
+    return (eta < -(double)f.Depth[q]) ? 0 : m;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_mask(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i > g.Mloc || j > g.Nloc) return;
+    // Depthx at x-face i of row j
+    if (j < g.Nloc && j >= g.jb - 2 && j <= g.je + 2) {
+        const bool rin = (i >= g.ib - 2 && i <= g.ie + 2);
+        const bool lin = (i - 1 >= g.ib - 2 && i - 1 <= g.ie + 2);
+        if (rin && f.MASK[IDX(i, j)] < 1) f.Depthx[IDX(i, j)] = f.Depth[IDX(i - 1, j)];
+        else if (lin && f.MASK[IDX(i - 1, j)] < 1) f.Depthx[IDX(i, j)] = f.Depth[IDX(i, j)];
+    }
+    // Depthy at y-face j of column i
+    if (i < g.Mloc && i >= g.ib - 2 && i <= g.ie + 2) {
+        const bool tin = (j >= g.jb - 2 && j <= g.je + 2);
+        const bool bin = (j - 1 >= g.jb - 2 && j - 1 <= g.je + 2);
+        if (tin && f.MASK[IDX(i, j)] < 1) f.Depthy[IDX(i, j)] = f.Depth[IDX(i, j - 1)];
+        else if (bin && f.MASK[IDX(i, j - 1)] < 1) f.Depthy[IDX(i, j)] = f.Depth[IDX(i, j)];
+    }
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    const size_t id = IDX(i, j);
+    f.MASKn[id] = (uint8_t)new_mask(g, f, i, j);
+    // MASK9 on Ibeg-1..Iend+1 x Jbeg-1..Jend+1; 0 elsewhere (never written
+    // in the reference, whose temporary is fresh memory)
+    uint8_t m9 = 0;
+    if (i >= g.ib - 1 && i <= g.ie + 1 && j >= g.jb - 1 && j <= g.je + 1) {
+        if (g.visc_breaking) {
+            m9 = 1;
+        } else {
+            int p = 1;
+            for (int b = -1; b <= 1; b++)
+                for (int a = -1; a <= 1; a++) p *= new_mask(g, f, i + a, j + b);
+            if (fabs((double)f.Eta[id]) / tmax((double)f.Depth[id], g.min_depth_frc) > g.swe_eta_dep) p = 0;
+            m9 = (uint8_t)p;
+        }
+    }
+    f.MASK9[id] = m9;
+}
+
+// ---------------------------------------------------------------------------
+// BREAKING (breaker.F:87-353), default branch
+// ---------------------------------------------------------------------------
+template <typename T> struct BrkLocal {
+    T tmp1, tmp2, tmp3, et;
+};
+template <typename T>
+__device__ __forceinline__ BrkLocal<T> brk_local(const Grid &g, const Fields<T> &f, size_t id) {
+    BrkLocal<T> b;
+    b.tmp3 = fsqrt((T)GRAV * tmax((T)g.min_depth_frc, f.H[id]));
+    b.tmp1 = (T)g.cbrk1 * b.tmp3;
+    b.tmp2 = (T)g.cbrk2 * b.tmp3;
+    b.et = f.ETAT[id];
+    return b;
+}
+template <typename T>
+__device__ __forceinline__ bool in_wk_zone(const Grid &g, int i, int j) {
+    const T xmk = (T)(i - g.ib) * (T)g.DX, ymk = (T)(j - g.jb) * (T)g.DY;
+    return fabs_(xmk - (T)g.xc_wk) < (T)g.width_wk && fabs_(ymk - (T)g.yc_wk) < (T)g.ywidth_wk / (T)2;
+}
+template <typename T>
+__device__ __forceinline__ T nu_value(const Grid &g, const Fields<T> &f, size_t id, const BrkLocal<T> &b, T age,
+                                      bool zone) {
+    const T mdf = (T)g.min_depth_frc;
+    if (zone) {
+        if (b.et > tmin(b.tmp2, (T)g.wavemaker_cbrk * b.tmp3)) {
+            const T cap1 = (T)1 * (tmax(f.Depth[id], mdf) + f.Eta[id]);
+            return cap1 * (T)g.wavemaker_cbrk * b.tmp3 + (T)g.nu_bkg;
+        }
+        return (T)0 + (T)g.nu_bkg;
+    }
+    if (age > (T)0 && age < (T)g.T_brk && b.et > b.tmp2) {
+        const T cap1 = (T)1 * (tmax(f.Depth[id], mdf) + f.Eta[id]);
+        return cap1 * b.tmp2 + (T)g.nu_bkg;
+    }
+    return (T)0 + (T)g.nu_bkg;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_break_a(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    const size_t id = IDX(i, j);
+    const T age = f.AGE[id];
+    if (i < g.ib - 1 || i > g.ie + 1 || j < g.jb - 1 || j > g.je + 1) {
+        f.AGEn[id] = age;
+        return;
+    }
+    const T DT = (T)f.dsc[S_DT];
+    const BrkLocal<T> b = brk_local(g, f, id);
+    T an = age;
+    bool cand = false;
+    if (b.et >= b.tmp1 && (age == (T)0 || age > (T)g.T_brk)) an = DT;
+    else if (age > (T)0) an = age + DT;
+    else if (b.et >= b.tmp2) cand = true;
+    f.AGEn[id] = an;
+    const bool zone = in_wk_zone<T>(g, i, j);
+    if (cand) {
+        const int slot = atomicAdd(f.ncand, 1);
+        f.cand[slot] = i + j * g.pitch;
+    }
+    if (zone || !cand) f.nu[id] = nu_value(g, f, id, b, an, zone);
+}
+
+// the neighbour test of one candidate (breaker.F:182-224); N = new values
+template <typename T>
+__device__ __forceinline__ bool brk_neigh(const Grid &g, const Fields<T> &f, const volatile T *N, int i, int j,
+                                          T DT) {
+    const size_t id = IDX(i, j);
+    const T ex = f.ETAx[id], ey = f.ETAy[id];
+    const T ANGLE = fatan2(-ey, -ex) * (T)180 / (T)PI_SP;
+    const T tmp4 = tmax(fsqrt(ex * ex + ey * ey), (T)SMALL);
+    const T Hc = f.H[id];
+    const T C = tmin(fabs_(f.ETAT[id]) / tmp4, fsqrt((T)GRAV * fabs_(Hc)));
+    const T DX = (T)g.DX, DY = (T)g.DY;
+    const T propxy = fsqrt(DX * DX + DY * DY) / tmax(C, (T)SMALL);
+    const T propx = fsqrt(DX * DX) / tmax(C, (T)SMALL);
+    const T propy = fsqrt(DY * DY) / tmax(C, (T)SMALL);
+    const T *O = f.AGE;  // values before the sweep
+#define NW(a, b) N[IDX(i + (a), j + (b))]
+#define OL(a, b) O[IDX(i + (a), j + (b))]
+    bool hit = false;
+    T A1, A2, A3;
+    if (ANGLE >= (T)0 && ANGLE < (T)90) {
+        A1 = NW(-1, 0);
+        A2 = NW(-1, -1);
+        A3 = NW(0, -1);
+        if ((A1 >= DT && A1 > propx) || (A2 >= DT && A2 > propxy) || (A3 >= DT && A3 > propy)) hit = true;
+    }
+    if (ANGLE >= (T)90 && ANGLE < (T)180) {
+        A1 = OL(1, 0);
+        A2 = NW(1, -1);
+        A3 = NW(0, -1);
+        if ((A1 >= DT && A1 > propx) || (A2 >= DT && A2 > propxy) || (A3 >= DT && A3 > propy)) hit = true;
+    }
+    if (ANGLE >= (T)-180 && ANGLE < (T)-90) {
+        A1 = OL(1, 0);
+        A2 = OL(1, 1);
+        A3 = OL(0, 1);
+        if ((A1 >= DT && A1 > propx) || (A2 >= DT && A2 > propxy) || (A3 >= DT && A3 > propy)) hit = true;
+    }
+    if (ANGLE >= (T)-90 && ANGLE < (T)0) {
+        A1 = OL(0, 1);
+        A2 = OL(-1, 1);
+        A3 = NW(-1, 0);
+        if ((A1 >= DT && A1 > propy) || (A2 >= DT && A2 > propxy) || (A3 >= DT && A3 > propx)) hit = true;
+    }
+#undef NW
+#undef OL
+    return hit;
+}
+
+// Candidates of the sweep: iterate to the fixed point, then set nu.  One
+// block; every pass either turns at least one candidate from 0 to DT or
+// ends the loop, so it runs at most ncand+1 passes.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_break_b(Grid g, Fields<T> f) {
+    __shared__ int changed;
+    const int n = *f.ncand;
+    const T DT = (T)f.dsc[S_DT];
+    volatile T *N = f.AGEn;
+    for (int pass = 0; pass <= n; pass++) {
+        if (threadIdx.x == 0) changed = 0;
+        __syncthreads();
+        for (int c = threadIdx.x; c < n; c += blockDim.x) {
+            const int code = f.cand[c];
+            const int i = code % g.pitch, j = code / g.pitch;
+            const size_t id = IDX(i, j);
+            if (N[id] != (T)0) continue;
+            if (brk_neigh(g, f, N, i, j, DT)) {
+                N[id] = DT;
+                changed = 1;
+            }
+        }
+        __syncthreads();
+        const int ch = changed;
+        __syncthreads();
+        if (!ch) break;
+    }
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        const int code = f.cand[c];
+        const int i = code % g.pitch, j = code / g.pitch;
+        const size_t id = IDX(i, j);
+        if (in_wk_zone<T>(g, i, j)) continue;
+        const BrkLocal<T> b = brk_local(g, f, id);
+        f.nu[id] = nu_value(g, f, id, b, (T)N[id], false);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *f.ncand = 0;
+}
+
+// ---------------------------------------------------------------------------
+// EXCHANGE ghost fill (bc.F:426-529 with PHI_COLL / PHI_COLL_VARIABLE_LENGTH)
+// in place.  One thread per ghost cell; in periodic mode the thread of an
+// x-ghost cell also moves its pre-fill value into the corner cell that
+// copies it (bc.F:735-740 runs before the x mirror).
+// ---------------------------------------------------------------------------
+struct GhostSet {
+    int n;  // number of fields
+};
+
+template <typename T>
+__device__ __forceinline__ void ghost_x_cell(const Grid &g, T *phi, int i, int j, int vtype) {
+    // i is an x-ghost column, j an interior row
+    const int si = mirror_x(g, i);
+    const T v = phi[IDX(si, j)];
+    if (g.periodic) {
+        if (j >= g.je - 2) phi[IDX(i, j - (g.je - 2))] = phi[IDX(i, j)];
+        else if (j <= g.jb + 2) phi[IDX(i, j + g.je - 2)] = phi[IDX(i, j)];
+    }
+    phi[IDX(i, j)] = (vtype == 2) ? -v : v;
+}
+template <typename T>
+__device__ __forceinline__ void ghost_y_cell(const Grid &g, T *phi, int i, int j, int vtype) {
+    // j is a y-ghost row, any column
+    const bool gx = (i < g.ib) || (i > g.ie);
+    if (g.periodic) {
+        if (gx) return;  // corner: written by the x-ghost thread
+        phi[IDX(i, j)] = phi[IDX(i, period_y(g, j))];
+        return;
+    }
+    const T v = phi[IDX(mirror_x(g, i), mirror_y(g, j))];
+    T r = v;
+    if (vtype == 2 && gx) r = -r;
+    if (vtype == 3) r = -r;
+    phi[IDX(i, j)] = r;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_ghost(Grid g, Fields<T> f, int with_age) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nX = 6 * g.Nglob;
+    const int nY = 6 * g.Mloc;
+    const int ncell = nX + nY;
+    if (t < ncell) {
+        if (t < nX) {
+            const int col = t % 6;
+            const int i = col < 3 ? col : g.ie + 1 + (col - 3);
+            const int j = g.jb + t / 6;
+            ghost_x_cell(g, f.Eta, i, j, 1);
+            ghost_x_cell(g, f.U, i, j, 2);
+            ghost_x_cell(g, f.HU, i, j, 2);
+            ghost_x_cell(g, f.V, i, j, 3);
+            ghost_x_cell(g, f.HV, i, j, 3);
+            ghost_x_cell(g, f.MASK, i, j, 1);
+            if (with_age) {
+                ghost_x_cell(g, f.AGE, i, j, 1);
+                ghost_x_cell(g, f.nu, i, j, 1);
+            }
+        } else {
+            const int u = t - nX;
+            const int row = u / g.Mloc;
+            const int i = u % g.Mloc;
+            const int j = row < 3 ? row : g.je + 1 + (row - 3);
+            ghost_y_cell(g, f.Eta, i, j, 1);
+            ghost_y_cell(g, f.U, i, j, 2);
+            ghost_y_cell(g, f.HU, i, j, 2);
+            ghost_y_cell(g, f.V, i, j, 3);
+            ghost_y_cell(g, f.HV, i, j, 3);
+            ghost_y_cell(g, f.MASK, i, j, 1);
+            if (with_age) {
+                ghost_y_cell(g, f.AGE, i, j, 1);
+                ghost_y_cell(g, f.nu, i, j, 1);
+            }
+        }
+        return;
+    }
+    if (!with_age) return;
+    // P on x-faces and Q on y-faces: plain mirror on all four sides
+    // (PHI_COLL_VARIABLE_LENGTH, periodic ignored), last index Iend1 / Jend1
+    int u = t - ncell;
+    const int nPX = 6 * g.Nglob, nPY = 6 * (g.Mloc + 1);
+    if (u < nPX + nPY) {
+        const int ie1 = g.ie + 1;
+        int i, j;
+        if (u < nPX) {
+            const int col = u % 6;
+            i = col < 3 ? col : ie1 + 1 + (col - 3);
+            j = g.jb + u / 6;
+        } else {
+            u -= nPX;
+            const int row = u / (g.Mloc + 1);
+            i = u % (g.Mloc + 1);
+            j = row < 3 ? row : g.je + 1 + (row - 3);
+        }
+        const int si = i < g.ib ? 2 * g.ib - 1 - i : (i > ie1 ? 2 * ie1 + 1 - i : i);
+        const int sj = mirror_y(g, j);
+        f.P[IDX(i, j)] = f.P[IDX(si, sj)];
+        return;
+    }
+    u -= nPX + nPY;
+    const int nQX = 6 * (g.Nglob + 1), nQY = 6 * g.Mloc;
+    if (u < nQX + nQY) {
+        const int je1 = g.je + 1;
+        int i, j;
+        if (u < nQX) {
+            const int col = u % 6;
+            i = col < 3 ? col : g.ie + 1 + (col - 3);
+            j = g.jb + u / 6;
+        } else {
+            u -= nQX;
+            const int row = u / g.Mloc;
+            i = u % g.Mloc;
+            j = row < 3 ? row : je1 + 1 + (row - 3);
+        }
+        const int si = mirror_x(g, i);
+        const int sj = j < g.jb ? 2 * g.jb - 1 - j : (j > je1 ? 2 * je1 + 1 - j : j);
+        f.Q[IDX(i, j)] = f.Q[IDX(si, sj)];
+    }
+}
+
+// U,V,HU,HV *= MASK (bc.F:491-494) and, optionally, SPONGE_DAMPING
+// (sponge.F:52-66), on every cell
+template <typename T>
+__global__ void __launch_bounds__(256) k_maskmul(Grid g, Fields<T> f, int sponge) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    const size_t id = IDX(i, j);
+    const uint8_t mi = f.MASK[id];
+    const T m = (T)mi;
+    T u = f.U[id] * m, v = f.V[id] * m;
+    f.HU[id] = f.HU[id] * m;
+    f.HV[id] = f.HV[id] * m;
+    if (sponge) {
+        const T s = f.SPONGE[id];
+        if (mi > 0) f.Eta[id] = f.Eta[id] / s;
+        u = u / s;
+        v = v / s;
+    }
+    f.U[id] = u;
+    f.V[id] = v;
+}
+
+// SPONGE_DAMPING alone
+template <typename T>
+__global__ void k_sponge(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    const size_t id = IDX(i, j);
+    const T s = f.SPONGE[id];
+    if (f.MASK[id] > 0) f.Eta[id] = f.Eta[id] / s;
+    f.U[id] = f.U[id] / s;
+    f.V[id] = f.V[id] / s;
+}
+
+// ---------------------------------------------------------------------------
+// ESTIMATE_DT (misc.F:216-296): CFL minimum over every cell, then DT and
+// TIME on the device.  Positive doubles order like their bit patterns.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ double dt_cell(const Grid &g, const Fields<T> &f, size_t id) {
+    const T c = fsqrt((T)GRAV * tmax(f.H[id], (T)g.min_depth_frc));
+    T t1 = fabs_(f.U[id]) + c;
+    T t2 = (t1 < (T)SMALL) ? (T)g.DX / (T)SMALL : (T)g.DX / t1;
+    T m = t2;
+    t1 = fabs_(f.V[id]) + c;
+    t2 = (t1 < (T)SMALL) ? (T)g.DY / (T)SMALL : (T)g.DY / t1;
+    if (t2 < m) m = t2;
+    return (double)m;
+}
+
+__device__ __forceinline__ void block_min_to_global(double v, unsigned long long *dst) {
+    __shared__ double sm[32];
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
+    const int warp = (threadIdx.x + threadIdx.y * blockDim.x) >> 5;
+    const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+    if (lane == 0) sm[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = lane < nw ? sm[lane] : 1.0e300;
+        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) atomicMin(dst, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+// begin of a step: U,V,HU,HV *= MASK after the ghost fill, the Eta0/Ubar0/
+// Vbar0/U0/V0 copies (main.F:295-297,331) and the CFL minimum
+template <typename T>
+__global__ void __launch_bounds__(256) k_begin(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double v = 1.0e300;
+    if (i < g.Mloc && j < g.Nloc) {
+        const size_t id = IDX(i, j);
+        const T m = (T)f.MASK[id];
+        const T u = f.U[id] * m, vv = f.V[id] * m;
+        f.U[id] = u;
+        f.V[id] = vv;
+        f.HU[id] = f.HU[id] * m;
+        f.HV[id] = f.HV[id] * m;
+        f.Eta0[id] = f.Eta[id];
+        f.Ubar0[id] = f.Ubar[id];
+        f.Vbar0[id] = f.Vbar[id];
+        f.U0[id] = u;
+        f.V0[id] = vv;
+        v = dt_cell(g, f, id);
+    }
+    block_min_to_global(v, f.dtmin_bits);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dt_only(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double v = 1.0e300;
+    if (i < g.Mloc && j < g.Nloc) v = dt_cell(g, f, IDX(i, j));
+    block_min_to_global(v, f.dtmin_bits);
+}
+
+// DT = CFL*min (with DT_fixed halving), TIME += DT, and the JON_2D
+// cos/sin(omega_k TIME) table of this step (sources.F:121-124)
+__global__ void k_dt_final(Grid g, double *dsc, unsigned long long *bits, double *omega, double *wmcs, int nfreq) {
+    __shared__ double time_s;
+    if (threadIdx.x == 0) {
+        double tmp3 = __longlong_as_double((long long)*bits);
+        if (!(tmp3 < LARGE)) tmp3 = LARGE;
+        const double dt_tmp = g.cfl * tmp3;
+        double dt;
+        if (g.fixed_dt) {
+            dt = g.dt_fixed;
+            for (int k = 0; k < 4096 && dt > dt_tmp; k++) dt = dt / 2.0;
+        } else {
+            dt = dt_tmp;
+        }
+        dsc[S_DT] = dt;
+        dsc[S_TIME] = dsc[S_TIME] + dt;
+        time_s = dsc[S_TIME];
+        *bits = 0x7ff0000000000000ull;  // +inf for the next minimum
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nfreq; k += blockDim.x) {
+        wmcs[2 * k] = cos(omega[k] * time_s);
+        wmcs[2 * k + 1] = sin(omega[k] * time_s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// end of a step: MAX_MIN_PROPERTY (Hmax, misc.F:307-383) and the
+// CHECK_BLOWUP maximum (misc.F:394-433)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_end(Grid g, Fields<T> f, int track_hmax) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double v = 0.0;
+    if (i < g.Mloc && j < g.Nloc) {
+        const size_t id = IDX(i, j);
+        const T eta = f.Eta[id];
+        if (track_hmax && f.MASK[id] > 0 && eta > f.Hmax[id]) f.Hmax[id] = eta;
+        if (i >= g.ib && i <= g.ie && j >= g.jb && j <= g.je) {
+            const double a = fabs((double)eta);
+            v = (a == a) ? a : 1.0e308 * 10.0;  // NaN -> +inf
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (((threadIdx.x + threadIdx.y * blockDim.x) & 31) == 0)
+        atomicMax(f.etamax_bits, (unsigned long long)__double_as_longlong(v));
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline dim3 grid2(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
+static const dim3 B2D(32, 8);
+
+static inline void note(fw_ctx *c, int n = 1) {
+    c->launches += n;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess && !c->sticky_error) c->sticky_error = (int)e;
+}
+
+template <typename T> void launch_ghost(fw_ctx *c, bool full) {
+    const Grid &g = c->g;
+    int n = 6 * g.Nglob + 6 * g.Mloc;
+    if (full) n += 6 * g.Nglob + 6 * (g.Mloc + 1) + 6 * (g.Nglob + 1) + 6 * g.Mloc;
+    k_ghost<T><<<(n + 255) / 256, 256, 0, c->stream>>>(g, c->F<T>(), full ? 1 : 0);
+    note(c);
+}
+
+template <typename T> void launch_exchange(fw_ctx *c, bool with_sponge) {
+    const Grid &g = c->g;
+    launch_ghost<T>(c, g.visc_breaking != 0);
+    k_maskmul<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>(), with_sponge ? 1 : 0);
+    note(c);
+}
+
+template <typename T> void launch_sponge(fw_ctx *c) {
+    const Grid &g = c->g;
+    k_sponge<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+}
+
+static void launch_dt_final(fw_ctx *c) {
+    auto &fd = c->fd;
+    double *dsc = c->p.precision == FW_PREC_FP64 ? c->fd.dsc : c->ff.dsc;
+    unsigned long long *bits = c->p.precision == FW_PREC_FP64 ? c->fd.dtmin_bits : c->ff.dtmin_bits;
+    double *om = c->p.precision == FW_PREC_FP64 ? c->fd.omega : c->ff.omega;
+    double *cs = c->p.precision == FW_PREC_FP64 ? c->fd.wmcs : c->ff.wmcs;
+    (void)fd;
+    k_dt_final<<<1, 128, 0, c->stream>>>(c->g, dsc, bits, om, cs, c->g.wavemaker == FW_WK_JON_2D ? c->g.nfreq : 0);
+    note(c);
+}
+
+template <typename T> void launch_estimate_dt(fw_ctx *c) {
+    const Grid &g = c->g;
+    k_dt_only<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+    launch_dt_final(c);
+}
+
+template <typename T> void launch_begin_step(fw_ctx *c) {
+    const Grid &g = c->g;
+    launch_ghost<T>(c, g.visc_breaking != 0);
+    k_begin<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+    launch_dt_final(c);
+}
+
+template <typename T> void launch_dispersion(fw_ctx *c) {
+    const Grid &g = c->g;
+    k_disp_a<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+    k_disp_b<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+}
+
+template <typename T> void launch_fluxes(fw_ctx *c) {
+    const Grid &g = c->g;
+    k_flux<T, 0><<<grid2(g.Mloc + 1, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+    k_flux<T, 1><<<grid2(g.Mloc, g.Nloc + 1, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+}
+
+template <typename T> void launch_sources_debug(fw_ctx *c) {
+    const Grid &g = c->g;
+    k_sources<T><<<grid2(g.Mglob, g.Nglob, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+}
+
+template <typename T, int DIR, bool PER> static void launch_tri(fw_ctx *c, const LinePart &lp) {
+    const Grid &g = c->g;
+    const int nt = lp.nlines * lp.P;
+    k_tri_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+    note(c);
+    k_tri_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+    note(c);
+    k_tri_c<T, DIR><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+    note(c);
+}
+
+template <typename T> void launch_estimate_huv(fw_ctx *c, int istage) {
+    const Grid &g = c->g;
+    static const double AL[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0};
+    static const double BE[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
+    const T al = (T)AL[istage - 1], be = (T)BE[istage - 1];
+    k_update<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>(), al, be);
+    note(c);
+    if (g.dispersion) {
+        launch_tri<T, 0, false>(c, c->px);
+        if (g.periodic) launch_tri<T, 1, true>(c, c->py);
+        else launch_tri<T, 1, false>(c, c->py);
+    }
+    k_post<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+    if (!g.dispersion) {
+        k_nodisp_copy<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+        note(c);
+    }
+}
+
+template <typename T> void launch_update_mask(fw_ctx *c) {
+    const Grid &g = c->g;
+    k_mask<T><<<grid2(g.Mloc + 1, g.Nloc + 1, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+    auto &F = c->F<T>();
+    uint8_t *t = F.MASK;
+    F.MASK = F.MASKn;
+    F.MASKn = t;
+}
+
+template <typename T> void launch_breaking(fw_ctx *c) {
+    const Grid &g = c->g;
+    if (!g.show_breaking) return;
+    k_break_a<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+    k_break_b<T><<<1, 1024, 0, c->stream>>>(g, c->F<T>());
+    note(c);
+    auto &F = c->F<T>();
+    T *t = F.AGE;
+    F.AGE = F.AGEn;
+    F.AGEn = t;
+}
+
+template <typename T> void launch_end_step(fw_ctx *c) {
+    const Grid &g = c->g;
+    k_end<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>(), c->p.track_hmax);
+    note(c);
+}
+
+template <typename T> void launch_stage(fw_ctx *c, int istage) {
+    const Grid &g = c->g;
+    if (g.dispersion) launch_dispersion<T>(c);
+    launch_fluxes<T>(c);
+    launch_estimate_huv<T>(c, istage);
+    launch_update_mask<T>(c);
+    launch_breaking<T>(c);
+    launch_exchange<T>(c, g.direct_sponge != 0);
+}
+
+#define INST(T)                                                  \
+    template void launch_begin_step<T>(fw_ctx *);                \
+    template void launch_exchange<T>(fw_ctx *, bool);            \
+    template void launch_estimate_dt<T>(fw_ctx *);               \
+    template void launch_dispersion<T>(fw_ctx *);                \
+    template void launch_fluxes<T>(fw_ctx *);                    \
+    template void launch_sources_debug<T>(fw_ctx *);             \
+    template void launch_estimate_huv<T>(fw_ctx *, int);         \
+    template void launch_update_mask<T>(fw_ctx *);               \
+    template void launch_breaking<T>(fw_ctx *);                  \
+    template void launch_sponge<T>(fw_ctx *);                    \
+    template void launch_end_step<T>(fw_ctx *);                  \
+    template void launch_stage<T>(fw_ctx *, int);
+INST(double)
+INST(float)
+#undef INST
+
+}  // namespace fw

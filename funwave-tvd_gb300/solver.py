@@ -1,0 +1,346 @@
+"""ctypes binding of ``libfunwave_gpu.so`` (include/funwave_gpu.h).
+
+:class:`Solver` mirrors the reference's driver interface for the hot path:
+the unit calls keep the Fortran subroutine names (``cal_dispersion``,
+``fluxes``, ``source_terms``, ``estimate_huv``, ``update_mask``,
+``wave_breaking``, ``exchange``, ``sponge_damping``, ``estimate_dt``) and
+fields are read and written by their MODULE GLOBAL names as Fortran-ordered
+numpy arrays with ghost cells.  Errors raise :class:`FwError` carrying the
+library status, where the reference would STOP.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+
+from .params import with_defaults
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_ROOT = os.path.dirname(_HERE)
+_CSRC = os.path.join(_HERE, "csrc")
+_BUILD = os.path.join(_HERE, "_build")
+_HEADER = os.path.join(_ROOT, "include", "funwave_gpu.h")
+_SOURCES = ["fw_kernels.cu", "fw_api.cu", "fw_init.cpp"]
+
+FW_ERRORS = {0: "FW_OK", -1: "FW_ERR_CUDA", -2: "FW_ERR_OOM", -3: "FW_ERR_BAD_PARAM",
+             -4: "FW_ERR_BLOWUP", -5: "FW_ERR_NAN", -6: "FW_ERR_UNSUPPORTED",
+             -7: "FW_ERR_NOT_READY", -8: "FW_ERR_NO_DEVICE"}
+
+
+class FwError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        super().__init__("%s (%d)%s" % (FW_ERRORS.get(status, "?"), status,
+                                        (": " + what) if what else ""))
+
+
+def lib_path():
+    return os.path.join(_BUILD, "libfunwave_gpu.so")
+
+
+def build(verbose=False):
+    """Compile the CUDA library for sm_103a with nvcc (no GPU needed).
+
+    Each translation unit is compiled in parallel, then linked into
+    ``_build/libfunwave_gpu.so``.  Rebuilds only when a source is newer."""
+    os.makedirs(_BUILD, exist_ok=True)
+    out = lib_path()
+    srcs = [os.path.join(_CSRC, s) for s in _SOURCES]
+    deps = srcs + [os.path.join(_CSRC, h) for h in os.listdir(_CSRC) if h.endswith(".h")] + [_HEADER]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+        return out
+    nvcc = os.environ.get("NVCC", "nvcc")
+    common = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-I" + os.path.join(_ROOT, "include")]
+    arch = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo"]
+    objs, procs = [], []
+    for s in srcs:
+        o = os.path.join(_BUILD, os.path.basename(s) + ".o")
+        objs.append(o)
+        cmd = [nvcc] + common + arch + ["-c", s, "-o", o]
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    for cmd, p in procs:
+        txt = p.communicate()[0].decode(errors="replace")
+        if p.returncode != 0:
+            raise RuntimeError("nvcc failed: %s\n%s" % (" ".join(cmd), txt))
+        if verbose and txt.strip():
+            print(txt)
+    link = [nvcc] + arch + ["-shared", "-o", out + ".tmp"] + objs
+    subprocess.run(link, check=True)
+    os.replace(out + ".tmp", out)
+    return out
+
+
+class FwParams(ctypes.Structure):
+    _fields_ = [
+        ("Mglob", ctypes.c_int), ("Nglob", ctypes.c_int),
+        ("DX", ctypes.c_double), ("DY", ctypes.c_double),
+        ("periodic", ctypes.c_int), ("dispersion", ctypes.c_int),
+        ("gamma1", ctypes.c_double), ("gamma2", ctypes.c_double),
+        ("gamma3", ctypes.c_double), ("beta_ref", ctypes.c_double),
+        ("viscosity_breaking", ctypes.c_int), ("show_breaking", ctypes.c_int),
+        ("cbrk1", ctypes.c_double), ("cbrk2", ctypes.c_double),
+        ("wavemaker_cbrk", ctypes.c_double), ("nu_bkg", ctypes.c_double),
+        ("swe_eta_dep", ctypes.c_double), ("cfl", ctypes.c_double),
+        ("fixed_dt", ctypes.c_int), ("dt_fixed", ctypes.c_double),
+        ("froude_cap", ctypes.c_double), ("min_depth", ctypes.c_double),
+        ("min_depth_frc", ctypes.c_double), ("eta_limiter", ctypes.c_int),
+        ("trough_limit", ctypes.c_double), ("crest_limit", ctypes.c_double),
+        ("direct_sponge", ctypes.c_int),
+        ("sponge_west", ctypes.c_double), ("sponge_east", ctypes.c_double),
+        ("sponge_south", ctypes.c_double), ("sponge_north", ctypes.c_double),
+        ("r_sponge", ctypes.c_double), ("a_sponge", ctypes.c_double),
+        ("friction_sponge", ctypes.c_int), ("cd_fixed", ctypes.c_double),
+        ("wavemaker", ctypes.c_int),
+        ("amp_wk", ctypes.c_double), ("tperiod", ctypes.c_double),
+        ("dep_wk", ctypes.c_double), ("xc_wk", ctypes.c_double),
+        ("yc_wk", ctypes.c_double), ("theta_wk", ctypes.c_double),
+        ("delta_wk", ctypes.c_double), ("time_ramp", ctypes.c_double),
+        ("ywidth_wk", ctypes.c_double),
+        ("freq_peak", ctypes.c_double), ("freq_min", ctypes.c_double),
+        ("freq_max", ctypes.c_double), ("gamma_tma", ctypes.c_double),
+        ("hmo", ctypes.c_double), ("theta_peak", ctypes.c_double),
+        ("sigma_theta", ctypes.c_double),
+        ("nfreq", ctypes.c_int), ("ntheta", ctypes.c_int),
+        ("spreading", ctypes.c_int), ("spread_s", ctypes.c_double),
+        ("precision", ctypes.c_int), ("device", ctypes.c_int),
+        ("track_hmax", ctypes.c_int),
+    ]
+
+
+_KEYS = {
+    "Mglob": "Mglob", "Nglob": "Nglob", "DX": "DX", "DY": "DY",
+    "PERIODIC": "periodic", "DISPERSION": "dispersion", "Gamma1": "gamma1",
+    "Gamma2": "gamma2", "Gamma3": "gamma3", "Beta_ref": "beta_ref",
+    "VISCOSITY_BREAKING": "viscosity_breaking", "SHOW_BREAKING": "show_breaking",
+    "Cbrk1": "cbrk1", "Cbrk2": "cbrk2", "WAVEMAKER_Cbrk": "wavemaker_cbrk",
+    "nu_bkg": "nu_bkg", "SWE_ETA_DEP": "swe_eta_dep", "CFL": "cfl",
+    "DT_fixed": "dt_fixed", "FroudeCap": "froude_cap", "MinDepth": "min_depth",
+    "MinDepthFrc": "min_depth_frc", "ETA_LIMITER": "eta_limiter",
+    "TroughLimit": "trough_limit", "CrestLimit": "crest_limit",
+    "DIRECT_SPONGE": "direct_sponge", "Sponge_west_width": "sponge_west",
+    "Sponge_east_width": "sponge_east", "Sponge_south_width": "sponge_south",
+    "Sponge_north_width": "sponge_north", "R_sponge": "r_sponge",
+    "A_sponge": "a_sponge", "FRICTION_SPONGE": "friction_sponge", "Cd": "cd_fixed",
+    "AMP_WK": "amp_wk", "Tperiod": "tperiod", "DEP_WK": "dep_wk", "Xc_WK": "xc_wk",
+    "Yc_WK": "yc_wk", "Theta_WK": "theta_wk", "Delta_WK": "delta_wk",
+    "Time_ramp": "time_ramp", "Ywidth_WK": "ywidth_wk", "FreqPeak": "freq_peak",
+    "FreqMin": "freq_min", "FreqMax": "freq_max", "GammaTMA": "gamma_tma",
+    "Hmo": "hmo", "ThetaPeak": "theta_peak", "Sigma_Theta": "sigma_theta",
+    "Nfreq": "nfreq", "Ntheta": "ntheta", "SPREADING_S": "spread_s",
+    "OUT_Hmax": "track_hmax",
+}
+_WK = {"NONE": 0, "WK_REG": 1, "JON_2D": 2}
+
+
+def params_struct(p, precision=None, device=0):
+    """Fill FwParams from an input.txt-style dictionary."""
+    p = with_defaults(p)
+    s = FwParams()
+    for k, name in _KEYS.items():
+        if k in p:
+            t = dict(FwParams._fields_)[name]
+            setattr(s, name, int(p[k]) if t is ctypes.c_int else float(p[k]))
+    s.fixed_dt = 1 if p.get("DT_fixed", 0) else 0
+    if p["WAVEMAKER"] not in _WK:
+        raise FwError(-6, "WAVEMAKER=%s is outside the built hot path" % p["WAVEMAKER"])
+    s.wavemaker = _WK[p["WAVEMAKER"]]
+    s.spreading = 1 if p.get("SPREADING", "WRAPPED_NORMAL") == "COS2S" else 0
+    prec = precision or p.get("PRECISION", "FP64")
+    s.precision = {"FP64": 0, "MIXED": 1}[prec.upper()]
+    s.device = int(device)
+    return s
+
+
+_lib = None
+
+
+def declared_symbols():
+    """Function names declared in include/funwave_gpu.h."""
+    txt = open(_HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(fw_[a-z_0-9]+)\s*\(", txt)))
+
+
+def load_library(path=None):
+    """Load the library (building it first if needed) and declare its ABI."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    path = path or lib_path()
+    if not os.path.exists(path):
+        build()
+    L = ctypes.CDLL(path)
+    vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    L.fw_params_default.argtypes = [ctypes.POINTER(FwParams)]
+    L.fw_params_default.restype = None
+    L.fw_create.argtypes = [ctypes.POINTER(FwParams), ctypes.POINTER(vp)]
+    L.fw_destroy.argtypes = [vp]
+    L.fw_init.argtypes = [vp] + [ctypes.POINTER(dp)] * 5
+    L.fw_get_field.argtypes = [vp, ctypes.c_char_p, vp]
+    L.fw_set_field.argtypes = [vp, ctypes.c_char_p, vp]
+    L.fw_get_scalar.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(dp)]
+    L.fw_set_scalar.argtypes = [vp, ctypes.c_char_p, dp]
+    for n in ("begin_step", "exchange", "estimate_dt", "cal_dispersion", "fluxes",
+              "source_terms", "update_mask", "wave_breaking", "sponge_damping", "sync"):
+        getattr(L, "fw_" + n).argtypes = [vp]
+    L.fw_stage.argtypes = [vp, ip]
+    L.fw_estimate_huv.argtypes = [vp, ip]
+    L.fw_end_step.argtypes = [vp, ctypes.POINTER(ip)]
+    L.fw_step.argtypes = [vp, ip, ctypes.POINTER(ip)]
+    L.fw_launch_count.argtypes = [vp]
+    L.fw_launch_count.restype = ctypes.c_longlong
+    L.fw_stream.argtypes = [vp]
+    L.fw_stream.restype = vp
+    L.fw_strerror.argtypes = [ip]
+    L.fw_strerror.restype = ctypes.c_char_p
+    if path == lib_path():
+        _lib = L
+    return L
+
+
+_MASKS = {"MASK", "MASK9", "MASK_STRUC"}
+_XFACE = {"Depthx", "P", "Fx", "Gx"}
+_YFACE = {"Depthy", "Q", "Fy", "Gy"}
+
+
+def _dptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Solver:
+    """One device-resident FUNWAVE-TVD case."""
+
+    def __init__(self, params, precision=None, device=0):
+        self.params = with_defaults(params)
+        self.L = load_library()
+        self._p = params_struct(self.params, precision, device)
+        h = ctypes.c_void_p()
+        self._check(self.L.fw_create(ctypes.byref(self._p), ctypes.byref(h)), "fw_create")
+        self.ctx = h
+        self.Mloc = self._p.Mglob + 6
+        self.Nloc = self._p.Nglob + 6
+        self.precision = "FP64" if self._p.precision == 0 else "MIXED"
+
+    def _check(self, rc, what=""):
+        if rc != 0:
+            raise FwError(rc, what)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.fw_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # --- set-up ---------------------------------------------------------
+    def init(self, depth, eta=None, u=None, v=None, phases=None):
+        """INITIALIZATION from interior arrays (Mglob x Nglob, x first)."""
+        def f(a):
+            return None if a is None else np.asfortranarray(np.asarray(a, dtype=np.float64))
+        d, e, uu, vv = f(depth), f(eta), f(u), f(v)
+        ph = f(phases)
+        self._keep = (d, e, uu, vv, ph)
+        self._check(self.L.fw_init(self.ctx, _dptr(d), _dptr(e), _dptr(uu), _dptr(vv), _dptr(ph)),
+                    "fw_init")
+
+    # --- fields ---------------------------------------------------------
+    def shape(self, name):
+        if name in _XFACE:
+            return (self.Mloc + 1, self.Nloc)
+        if name in _YFACE:
+            return (self.Mloc, self.Nloc + 1)
+        return (self.Mloc, self.Nloc)
+
+    def get(self, name):
+        dt = np.int32 if name in _MASKS else np.float64
+        a = np.zeros(self.shape(name), dtype=dt, order="F")
+        self._check(self.L.fw_get_field(self.ctx, name.encode(), a.ctypes.data), "get " + name)
+        return a
+
+    def set(self, name, arr):
+        dt = np.int32 if name in _MASKS else np.float64
+        a = np.asfortranarray(np.asarray(arr, dtype=dt))
+        if a.shape != self.shape(name):
+            raise FwError(-3, "%s must have shape %s" % (name, self.shape(name)))
+        self._check(self.L.fw_set_field(self.ctx, name.encode(), a.ctypes.data), "set " + name)
+
+    def __getitem__(self, name):
+        return self.get(name)
+
+    def scalar(self, name):
+        v = ctypes.c_double()
+        self._check(self.L.fw_get_scalar(self.ctx, name.encode(), ctypes.byref(v)), name)
+        return v.value
+
+    def set_scalar(self, name, value):
+        self._check(self.L.fw_set_scalar(self.ctx, name.encode(), float(value)), name)
+
+    # --- time stepping (main.F:284-535) ---------------------------------
+    def step(self, nsteps=1, check=True):
+        st = ctypes.c_int()
+        self._check(self.L.fw_step(self.ctx, int(nsteps), ctypes.byref(st)), "fw_step")
+        if check and st.value != 0:
+            raise FwError(st.value, "after %d steps" % nsteps)
+        return st.value
+
+    def begin_step(self):
+        self._check(self.L.fw_begin_step(self.ctx), "fw_begin_step")
+
+    def stage(self, istage):
+        self._check(self.L.fw_stage(self.ctx, int(istage)), "fw_stage")
+
+    def end_step(self):
+        st = ctypes.c_int()
+        self._check(self.L.fw_end_step(self.ctx, ctypes.byref(st)), "fw_end_step")
+        return st.value
+
+    def sync(self):
+        self._check(self.L.fw_sync(self.ctx), "fw_sync")
+
+    # --- the reference's units ------------------------------------------
+    def exchange(self):
+        self._check(self.L.fw_exchange(self.ctx), "EXCHANGE")
+
+    def estimate_dt(self):
+        self._check(self.L.fw_estimate_dt(self.ctx), "ESTIMATE_DT")
+
+    def cal_dispersion(self):
+        self._check(self.L.fw_cal_dispersion(self.ctx), "CAL_DISPERSION")
+
+    def fluxes(self):
+        self._check(self.L.fw_fluxes(self.ctx), "FLUXES")
+
+    def source_terms(self):
+        self._check(self.L.fw_source_terms(self.ctx), "SourceTerms")
+
+    def estimate_huv(self, istage):
+        self._check(self.L.fw_estimate_huv(self.ctx, int(istage)), "ESTIMATE_HUV")
+
+    def update_mask(self):
+        self._check(self.L.fw_update_mask(self.ctx), "UPDATE_MASK")
+
+    def wave_breaking(self):
+        self._check(self.L.fw_wave_breaking(self.ctx), "WAVE_BREAKING")
+
+    def sponge_damping(self):
+        self._check(self.L.fw_sponge_damping(self.ctx), "SPONGE_DAMPING")
+
+    def launch_count(self):
+        return int(self.L.fw_launch_count(self.ctx))
+
+    def stream(self):
+        return self.L.fw_stream(self.ctx)

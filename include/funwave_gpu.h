@@ -1,0 +1,165 @@
+/*
+ * funwave_gpu.h -- C ABI of the GB300 (sm_103a) FUNWAVE-TVD solver stage.
+ *
+ * The reference (mayhl/FUNWAVE-TVD) has no plugin API: its hot path is a set
+ * of argument-less Fortran subroutines called from the time loop of
+ * src/main.F:284-535 on shared MODULE GLOBAL state (src/mod_global.F).  This
+ * library replaces that loop body.  A Fortran host binds these functions with
+ * ISO_C_BINDING; every entry point takes plain pointers,
+ * sizes and a POD parameter block, returns an int status (0 = OK, negative =
+ * FW_ERR_*), never exits, aborts or traps, and keeps all solver state
+ * resident on one GPU between calls.
+ *
+ * Host arrays are Fortran column-major with the reference's extents and ghost
+ * cells (Nghost = 3):  cell arrays Mloc x Nloc, x-face arrays (Mloc+1) x
+ * Nloc, y-face arrays Mloc x (Nloc+1), Mloc = Mglob + 6, Nloc = Nglob + 6;
+ * reals are double (REAL(SP) of the FP64 build), masks int32 (default
+ * INTEGER).  The device layout is private.
+ */
+#ifndef FUNWAVE_GPU_H
+#define FUNWAVE_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FW_OK               0
+#define FW_ERR_CUDA        -1   /* a CUDA runtime call failed */
+#define FW_ERR_OOM         -2   /* device allocation failed */
+#define FW_ERR_BAD_PARAM   -3   /* invalid argument or parameter block */
+#define FW_ERR_BLOWUP      -4   /* CHECK_BLOWUP: max|eta| > EtaBlowVal */
+#define FW_ERR_NAN         -5   /* non-finite eta */
+#define FW_ERR_UNSUPPORTED -6   /* option not built into this library */
+#define FW_ERR_NOT_READY   -7   /* call order violated (e.g. step before init) */
+#define FW_ERR_NO_DEVICE   -8   /* no usable CUDA device */
+
+/* precision of the bulk arithmetic */
+#define FW_PREC_FP64  0   /* every field and operation in double */
+#define FW_PREC_MIXED 1   /* fields and fluxes in float; tridiagonal u/v
+                             recovery and total-depth tests in double */
+
+/* wavemaker kinds (WAVEMAKER key) */
+#define FW_WK_NONE   0
+#define FW_WK_REG    1    /* WK_REG   (wavemaker.F:67-194, 2369-2405) */
+#define FW_WK_JON_2D 2    /* JON_2D   (wavemaker.F:370-413, 2128-2357) */
+
+/* directional spreading of JON_2D */
+#define FW_SPREAD_WRAPPED_NORMAL 0   /* the reference's Sigma_Theta form */
+#define FW_SPREAD_COS2S          1   /* cos^2s((theta-theta_p)/2), s = spread_s */
+
+/* Parameter block: the input.txt keys of the hot path with the reference's
+ * names in the comments and defaults of src/io.F.  fw_params_default()
+ * fills the defaults. */
+typedef struct fw_params {
+    int    Mglob, Nglob;          /* Mglob, Nglob */
+    double DX, DY;                /* DX, DY */
+    int    periodic;              /* PERIODIC          (F) */
+    int    dispersion;            /* DISPERSION        (T) */
+    double gamma1, gamma2, gamma3, beta_ref;  /* Gamma1..3 (1), Beta_ref (-0.531) */
+    int    viscosity_breaking;    /* VISCOSITY_BREAKING (T) */
+    int    show_breaking;         /* SHOW_BREAKING     (T) */
+    double cbrk1, cbrk2;          /* Cbrk1 (0.65), Cbrk2 (0.35) */
+    double wavemaker_cbrk;        /* WAVEMAKER_Cbrk    (1.0) */
+    double nu_bkg;                /* nu_bkg            (0) */
+    double swe_eta_dep;           /* SWE_ETA_DEP       (0.8) */
+    double cfl;                   /* CFL               (0.5) */
+    int    fixed_dt;              /* 1 when DT_fixed is given */
+    double dt_fixed;              /* DT_fixed */
+    double froude_cap;            /* FroudeCap         (3.0) */
+    double min_depth;             /* MinDepth          (0.1) */
+    double min_depth_frc;         /* MinDepthFrc       (0.1) */
+    int    eta_limiter;           /* ETA_LIMITER       (F) */
+    double trough_limit, crest_limit;  /* TroughLimit, CrestLimit */
+    int    direct_sponge;         /* DIRECT_SPONGE     (F) */
+    double sponge_west, sponge_east, sponge_south, sponge_north; /* Sponge_*_width (0) */
+    double r_sponge, a_sponge;    /* R_sponge (0.85), A_sponge (5.0) */
+    int    friction_sponge;       /* FRICTION_SPONGE   (F); CD_4_SPONGE uploaded */
+    double cd_fixed;              /* Cd                (0) */
+    int    wavemaker;             /* FW_WK_* */
+    double amp_wk, tperiod, dep_wk, xc_wk, yc_wk, theta_wk, delta_wk; /* AMP_WK.. Delta_WK (0.5) */
+    double time_ramp, ywidth_wk;  /* Time_ramp (0), Ywidth_WK (LARGE) */
+    double freq_peak, freq_min, freq_max;      /* FreqPeak, FreqMin, FreqMax */
+    double gamma_tma, hmo, theta_peak, sigma_theta; /* GammaTMA, Hmo, ThetaPeak, Sigma_Theta (10) */
+    int    nfreq, ntheta;         /* Nfreq, Ntheta */
+    int    spreading;             /* FW_SPREAD_* */
+    double spread_s;              /* s of cos^2s */
+    /* build-side options (not input.txt keys) */
+    int    precision;             /* FW_PREC_FP64 or FW_PREC_MIXED */
+    int    device;                /* CUDA device ordinal */
+    int    track_hmax;            /* OUT_Hmax: keep the running max of eta */
+} fw_params;
+
+typedef struct fw_ctx fw_ctx;
+
+/* Fill p with the reference's input.txt defaults (src/io.F READ_* sites). */
+void fw_params_default(fw_params *p);
+
+/* Create a context and allocate its device state (no kernel runs yet).
+ * Replaces ALLOCATE_VARIABLES (init.F:54-269) and INDEX (misc.F:54-178). */
+int fw_create(const fw_params *p, fw_ctx **out);
+int fw_destroy(fw_ctx *ctx);
+
+/* Host-side INITIALIZATION (init.F:280-1272): depth ghosts and face depths,
+ * EtaBlowVal, Cd, wavemaker coefficients (WK_REG; JON_2D spectrum and the
+ * band Cm/Sm of CALCULATE_Cm_Sm), the direct sponge, MASK/dry eta, H, HU,
+ * HV, Ubar, Vbar, MASK9 and the wavemaker band, then uploads everything.
+ *   depth  interior depth, Mglob x Nglob column-major (DEPTH_TYPE=DATA)
+ *   eta,u,v  optional interior initial state (INI_UVZ), NULL for zero
+ *   phases optional JON_2D phases phi1(kf,ktheta), Nfreq x Ntheta column-
+ *          major; the reference draws them from rand(0)
+ *          (wavemaker.F:2342-2352), so a caller supplies them. */
+int fw_init(fw_ctx *ctx, const double *depth, const double *eta, const double *u,
+            const double *v, const double *phases);
+
+/* Whole-field transfer by reference name ("Eta","U","V","Ubar","Vbar","HU",
+ * "HV","H","MASK","MASK9","Depth","Depthx","Depthy","P","Q","Fx","Fy","Gx",
+ * "Gy","U4","V4","U1p","V1p","Udisp","Vdisp","ETAx","ETAy","ETAT","AGE",
+ * "nu_break","SPONGE","Cd","CD_4_SPONGE","MASK_STRUC","Eta0","Ubar0",
+ * "Vbar0","U0","V0","SourceX","SourceY","WaveMaker_Mass","HeightMax").
+ * host points to a Fortran-ordered array of the field's full extent
+ * (double, or int32 for MASK/MASK9/MASK_STRUC).  Synchronous. */
+int fw_get_field(fw_ctx *ctx, const char *name, void *host);
+int fw_set_field(fw_ctx *ctx, const char *name, const void *host);
+/* scalars "TIME","DT","EtaBlowVal","T_brk","Width_WK","ilo","ihi","jlo","jhi" */
+int fw_get_scalar(fw_ctx *ctx, const char *name, double *value);
+int fw_set_scalar(fw_ctx *ctx, const char *name, double value);
+
+/* --- time stepping (main.F:284-535) ------------------------------------ */
+/* Eta0/Ubar0/Vbar0 copies, EXCHANGE, ESTIMATE_DT (TIME += DT), U0/V0
+ * copies: main.F:295-331.  DT and TIME stay on the device. */
+int fw_begin_step(fw_ctx *ctx);
+/* One SSP-RK stage, istage = 1..3: main.F:382-485. */
+int fw_stage(fw_ctx *ctx, int istage);
+/* MAX_MIN_PROPERTY (Hmax) and CHECK_BLOWUP: main.F:509-512. *status gets
+ * FW_OK, FW_ERR_BLOWUP or FW_ERR_NAN. */
+int fw_end_step(fw_ctx *ctx, int *status);
+/* nsteps whole steps (fw_begin_step + 3 fw_stage + fw_end_step), replayed
+ * from a CUDA graph; *status as fw_end_step for the last step, checked
+ * once at the end. */
+int fw_step(fw_ctx *ctx, int nsteps, int *status);
+/* Synchronise the context's stream. */
+int fw_sync(fw_ctx *ctx);
+
+/* --- the reference's units, one call each (for coupling and parity) ---- */
+int fw_exchange(fw_ctx *ctx);            /* EXCHANGE        bc.F:426 */
+int fw_estimate_dt(fw_ctx *ctx);         /* ESTIMATE_DT     misc.F:216 */
+int fw_cal_dispersion(fw_ctx *ctx);      /* CAL_DISPERSION  dispersion.F:62 */
+int fw_fluxes(fw_ctx *ctx);              /* FLUXES          fluxes.F:52 */
+int fw_source_terms(fw_ctx *ctx);        /* SourceTerms     sources.F:56 (materialises SourceX/Y) */
+int fw_estimate_huv(fw_ctx *ctx, int istage); /* ESTIMATE_HUV etauv_solver.F:53 */
+int fw_update_mask(fw_ctx *ctx);         /* UPDATE_MASK     masks.F:51 */
+int fw_wave_breaking(fw_ctx *ctx);       /* WAVE_BREAKING   breaker.F:60 */
+int fw_sponge_damping(fw_ctx *ctx);      /* SPONGE_DAMPING  sponge.F:52 */
+
+/* Kernel launches issued by this context since creation (diagnostics). */
+long long fw_launch_count(fw_ctx *ctx);
+/* CUDA stream of the context, as a void* (cudaStream_t). */
+void *fw_stream(fw_ctx *ctx);
+/* Human-readable text of a status code. */
+const char *fw_strerror(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
