@@ -1,0 +1,374 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 FUNWAVE-TVD SSP-RK3 step on the 2048 x 2048
+elliptic-shoal / directional-JONSWAP workload.
+
+Metric: cell-steps/s (interior cells x whole SSP-RK3 steps per second) on
+one GB300, mixed-FP32 (float fields, FP64 tridiagonal u/v recovery and
+total-depth tests) as ``value``, with the all-FP64 path and the eta error of
+the mixed path against it beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One process per GPU (torchrun for N > 1): every rank advances its own
+replica of the workload (runs are independent; no collective on the data
+path), the step time is the maximum over ranks and value sums all ranks'
+cell-steps.  The reference arm times the CPU restatement of the reference's
+algorithm (the Fortran reference has no compiler here or on the GPU host)
+on all host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import __graft_entry__  # noqa: E402
+
+METRIC = "cell-steps/s (1 GB300) mixed-FP32 vs FP64 at stated eta error; ensemble runs/hr"
+UNIT = "cell-steps/s"
+WORKLOAD = ("2048x2048 1:50 slope + elliptic shoal, JON_2D Hs=1 m Tp=10 s 50x30 cos^2s, "
+            "dx=2 m, walls, west sponge (configs[1] shape, synthetic)")
+
+# Algorithmic bytes per launch unit of each kernel: every distinct array the
+# kernel must read once plus every array it must write once (T = bytes of a
+# bulk field element, masks 1 byte, tridiagonal right-hand sides 8 bytes).
+# Unit: one cell (one face for flux_x / flux_y).
+KERNEL_BYTES = {
+    "disp_a": lambda T: 13 * T + 1,       # U V Eta Depth P Q + MASK9 -> A B C E ETAx ETAy ETAT
+    "disp_b": lambda T: 19 * T + 1,       # A B C E U V U0 V0 Eta Depth ETAx ETAy ETAT + MASK9 -> U4 V4 U1p V1p Udisp Vdisp
+    "flux_x": lambda T: 11 * T + 2,       # U V HU HV Eta U4 V4 Depthx + MASK MASK9 -> P Fx Gx
+    "flux_y": lambda T: 11 * T + 2,
+    "update": lambda T: 32 * T + 2 + 16,  # 28 fields + MASK MASK9 -> Eta Ubar Vbar H + rhs_x rhs_y
+    "tri_x": lambda T: 2 * T + 10,        # Depth MASK9 MASK rhs_x -> U
+    "tri_y": lambda T: 2 * T + 10,
+    "post": lambda T: 7 * T + 1 + 6 * T,  # U V H Ubar Vbar HU HV + MASK -> U V HU HV Ubar Vbar
+    "mask": lambda T: 4 * T + 4 + 2 * T,  # Eta Depth Depthx Depthy + MASK MASK_STRUC -> MASKn MASK9 Depthx Depthy
+    "break_a": lambda T: 8 * T + 2 * T,   # H ETAx ETAy ETAT Depth Eta AGE nu -> AGEn nu
+    "maskmul": lambda T: 6 * T + 1 + 5 * T,
+    "begin": lambda T: 8 * T + 1 + 9 * T,
+}
+# kernel launches per stage (tri_* count the partitioned solve as one)
+PER_STAGE = ["disp_a", "disp_b", "flux_x", "flux_y", "update", "tri_x", "tri_y", "post",
+             "mask", "break_a", "maskmul"]
+# whole-step algorithmic bytes per cell-step: the cross-stage state each of
+# the three stages must read and write once (61 reals + 6 mask bytes)
+STEP_BYTES = {"fp64": 61 * 8 + 6, "mixed": 61 * 4 + 6}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p is not None:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                out = self.p.communicate(timeout=5)[0]
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                out = self.p.communicate()[0]
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cuda_timer(solver):
+    import torch
+    ext = torch.cuda.ExternalStream(solver.stream())
+    return ext, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def barrier(pg):
+    if pg:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, pg):
+    if not pg:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_precision(fw, params, depth, phases, precision, K, W, local, pg):
+    import torch
+    s = fw.Solver(params, precision=precision, device=local)
+    s.init(depth, phases=phases)
+    n0 = s.launch_count()
+    s.step(2)                       # captures the two-step graph
+    per_step = (s.launch_count() - n0) // 2
+    if W > 2:
+        s.step(W - 2)
+    ext, e0, e1 = cuda_timer(s)
+    barrier(pg)
+    s.sync()
+    with ClockSampler(local) as clk:
+        e0.record(ext)
+        st = s.step(K, check=False)
+        e1.record(ext)
+        e1.synchronize()
+    s.sync()
+    barrier(pg)
+    ms = e0.elapsed_time(e1)
+    return s, {"ms": ms, "status": st, "launches_per_step": per_step, "clocks": clk.summary()}
+
+
+def kernel_profile(s, T, cells, faces_x, faces_y, hbm):
+    """Average duration of each kernel of a stage (CUDA events on the
+    library stream) and its achieved algorithmic bandwidth."""
+    out = {}
+    for name in PER_STAGE:
+        try:
+            ms = s.time_kernel(name, nrep=10)
+        except Exception:
+            continue
+        unit = faces_x if name == "flux_x" else faces_y if name == "flux_y" else cells
+        b = KERNEL_BYTES[name](T) * unit
+        out[name] = {"ms": ms, "bytes": b, "gbs": b / (ms * 1e-3) / 1e9, "frac": b / (ms * 1e-3) / 1e9 / hbm}
+    return out
+
+
+def e2e_run(fw, s, K):
+    """Per step through the C ABI with pinned host buffers: upload Eta, U,
+    V, Ubar, Vbar, one fw_step, read back Eta, U, V."""
+    import numpy as np
+    import torch
+    shp = (s.Mloc, s.Nloc)
+    bufs = {}
+    for n in ("Eta", "U", "V", "Ubar", "Vbar"):
+        t = torch.empty((s.Nloc, s.Mloc), dtype=torch.float64, pin_memory=True)
+        a = t.numpy().T  # Fortran-ordered (Mloc, Nloc) view of pinned memory
+        a[...] = s.get(n)
+        bufs[n] = (t, a)
+    import ctypes
+    L = s.L
+    s.sync()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        for n in ("Eta", "U", "V", "Ubar", "Vbar"):
+            rc = L.fw_set_field(s.ctx, n.encode(), bufs[n][1].ctypes.data)
+            assert rc == 0
+        s.step(1, check=False)
+        for n in ("Eta", "U", "V"):
+            rc = L.fw_get_field(s.ctx, n.encode(), bufs[n][1].ctypes.data)
+            assert rc == 0
+    s.sync()
+    dt = time.perf_counter() - t0
+    nb = s.Mloc * s.Nloc * 8
+    return dt, 5 * nb, 3 * nb
+
+
+def cpu_baseline(fw, params, depth, phases, max_seconds=20.0, max_steps=5):
+    """The oracle (C restatement, all host threads) on the same workload:
+    init, one untimed step, then whole steps until max_seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fw_oracle
+    fw_oracle.build()
+    o = fw_oracle.Oracle(params)
+    o["Depth"][3:-3, 3:-3] = depth
+    if phases is not None:
+        o.set_phases(phases)
+    o.init()
+    o.step()
+    n, t0 = 0, time.perf_counter()
+    while n < max_steps:
+        o.step()
+        n += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    dt = time.perf_counter() - t0
+    cores = fw_oracle.lib().ofw_get_threads()
+    cells = params["Mglob"] * params["Nglob"]
+    o.close()
+    return {"value": cells * n / dt, "unit": UNIT, "cores": int(cores), "kind": "port",
+            "sample": "%d whole steps of the %dx%d workload after init and one warm-up step (%.1f s)"
+                      % (n, params["Mglob"], params["Nglob"], dt)}
+
+
+def reference_arm(args, fw, params, depth, phases):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fw_oracle
+    fw_oracle.build()
+    o = fw_oracle.Oracle(params)
+    o["Depth"][3:-3, 3:-3] = depth
+    if phases is not None:
+        o.set_phases(phases)
+    o.init()
+    for _ in range(args.warmup):
+        o.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step()
+    dt = time.perf_counter() - t0
+    cells = params["Mglob"] * params["Nglob"]
+    v = cells * args.steps / dt
+    cores = int(fw_oracle.lib().ofw_get_threads())
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "precision": "FP64"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d whole FP64 steps of the %dx%d workload after %d warm-up steps; the "
+                                   "Fortran reference cannot be compiled (no Fortran compiler on either "
+                                   "host), so its C restatement (oracle/) runs on %d OpenMP threads"
+                                   % (args.steps, params["Mglob"], params["Nglob"], args.warmup, cores)},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=2048, help="grid edge (2048 for the benchmark)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    fw = __graft_entry__.load_package()
+    params, depth, phases = fw.cases.shoal_jonswap(Mglob=args.size, Nglob=args.size, seed=2024)
+    params = fw.with_defaults(params)
+    if args.impl == "reference":
+        return reference_arm(args, fw, params, depth, phases)
+
+    ws, rank, local = dist_env()
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = True
+    import torch
+    torch.cuda.set_device(local)
+    fw.load_library()
+    K, W = args.steps, max(args.warmup, 3)
+    cells = params["Mglob"] * params["Nglob"]
+    hbm, peak_kind = peaks()
+
+    sm, rm = run_precision(fw, params, depth, phases, "MIXED", K, W, local, pg)
+    ms_mixed = max_over_ranks(rm["ms"], pg)
+    res64 = None
+    if not args.no_fp64:
+        s64, r64 = run_precision(fw, params, depth, phases, "FP64", K, W, local, pg)
+        ms64 = max_over_ranks(r64["ms"], pg)
+        import numpy as np
+        e_m = sm.get("Eta")[3:-3, 3:-3]
+        e_d = s64.get("Eta")[3:-3, 3:-3]
+        wet = (s64.get("MASK")[3:-3, 3:-3] > 0)
+        rms = float(np.sqrt(np.mean((e_m - e_d)[wet] ** 2)))
+        mask_mis = int(np.sum(sm.get("MASK") != s64.get("MASK")))
+        res64 = {"value": cells * K * ws / (ms64 * 1e-3), "ms_per_step": ms64 / K, "dtype": "f64",
+                 "step_roofline_frac_hbm": STEP_BYTES["fp64"] * cells / (ms64 / K * 1e-3) / 1e9 / hbm,
+                 "eta_rms_mixed_vs_fp64_m": rms, "mask_mismatch_cells": mask_mis,
+                 "time_mixed_s": sm.scalar("TIME"), "time_fp64_s": s64.scalar("TIME"),
+                 "status": r64["status"]}
+        prof64 = kernel_profile(s64, 8, cells, (params["Mglob"] + 1) * params["Nglob"],
+                                params["Mglob"] * (params["Nglob"] + 1), hbm)
+        res64["kernels"] = {k: round(v["ms"], 4) for k, v in prof64.items()}
+        s64.close()
+    e2e_steps = min(K, 10)
+    e2e_dt, h2d, d2h = e2e_run(fw, sm, e2e_steps)
+    # per-kernel timing last: some kernels update the state in place
+    prof = kernel_profile(sm, 4, cells, (params["Mglob"] + 1) * params["Nglob"],
+                          params["Mglob"] * (params["Nglob"] + 1), hbm)
+    dom = max(prof, key=lambda k: prof[k]["ms"]) if prof else None
+    sm.close()
+    if rank != 0:
+        return 0
+    value = cells * K * ws / (ms_mixed * 1e-3)
+    step_s = ms_mixed / K * 1e-3
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+        "ms_per_step": ms_mixed / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 tridiagonal and depth tests)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [params["Mglob"], params["Nglob"]], "dx_m": params["DX"],
+                   "precision": "MIXED", "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "state (~0.8 GB mixed, ~1.6 GB FP64) exceeds the 129 MB L2; no flush"},
+        "gpu_launches": rm["launches_per_step"] * K,
+        "clocks": rm["clocks"],
+        "status": rm["status"],
+        "step_roofline": {"bound": "hbm", "bytes_per_cell_step": STEP_BYTES["mixed"],
+                          "achieved": STEP_BYTES["mixed"] * cells / step_s / 1e9, "peak": hbm, "unit": "GB/s",
+                          "frac": STEP_BYTES["mixed"] * cells / step_s / 1e9 / hbm, "peak_kind": peak_kind},
+        "e2e": {"value": cells * e2e_steps / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "what": "per step: Eta,U,V,Ubar,Vbar uploaded from pinned host memory, fw_step, Eta,U,V read back"},
+        "fp64": res64,
+        "kernels_ms": {k: round(v["ms"], 4) for k, v in prof.items()},
+    }
+    if dom:
+        d = prof[dom]
+        line["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": d["gbs"], "peak": hbm, "unit": "GB/s",
+                            "frac": d["frac"], "traffic": None, "peak_kind": peak_kind,
+                            "algorithmic_bytes_per_launch": d["bytes"], "ms_per_launch": d["ms"]}
+    if not args.no_cpu_baseline and ws == 1:
+        line["cpu_baseline"] = cpu_baseline(fw, params, depth, phases)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

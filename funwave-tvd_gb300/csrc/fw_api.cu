@@ -79,50 +79,38 @@ void extent(const fw_ctx *c, int kind, int &w, int &h) {
     h = c->g.Nloc + (kind == YFACE ? 1 : 0);
 }
 
-// host (Fortran, double/int32, w x h) <-> device (pitched, T/uint8)
+// host (Fortran, double/int32, w x h) <-> device (pitched, T/uint8).
+// double fields of the FP64 build move with one 2-D copy; float fields and
+// masks go through a device staging plane and a conversion kernel.
 template <typename T> int put_field(fw_ctx *c, const FieldRef &r, const void *host) {
     int w, h;
     extent(c, r.kind, w, h);
-    const size_t n = (size_t)w * h;
     cudaError_t e;
-    if (r.is_mask) {
-        std::vector<uint8_t> tmp(n);
-        const int *src = (const int *)host;
-        for (size_t k = 0; k < n; k++) tmp[k] = (uint8_t)(src[k] != 0 ? (src[k] > 0 ? 1 : 0) : 0);
-        e = cudaMemcpy2DAsync(r.ptr, (size_t)c->g.pitch, tmp.data(), (size_t)w, (size_t)w, (size_t)h,
-                              cudaMemcpyHostToDevice, c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (!r.is_mask && sizeof(T) == sizeof(double)) {
+        e = cudaMemcpy2DAsync(r.ptr, (size_t)c->g.pitch * sizeof(T), host, (size_t)w * sizeof(double),
+                              (size_t)w * sizeof(double), (size_t)h, cudaMemcpyHostToDevice, c->stream);
     } else {
-        std::vector<T> tmp(n);
-        const double *src = (const double *)host;
-        for (size_t k = 0; k < n; k++) tmp[k] = (T)src[k];
-        e = cudaMemcpy2DAsync(r.ptr, (size_t)c->g.pitch * sizeof(T), tmp.data(), (size_t)w * sizeof(T),
-                              (size_t)w * sizeof(T), (size_t)h, cudaMemcpyHostToDevice, c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        const size_t esz = r.is_mask ? sizeof(int) : sizeof(double);
+        e = cudaMemcpyAsync(c->staging, host, (size_t)w * h * esz, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) convert_in(c, c->staging, r.is_mask, r.ptr, w, h);
     }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return cuda_status(c, e);
 }
 
 template <typename T> int get_field(fw_ctx *c, const FieldRef &r, void *host) {
     int w, h;
     extent(c, r.kind, w, h);
-    const size_t n = (size_t)w * h;
     cudaError_t e;
-    if (r.is_mask) {
-        std::vector<uint8_t> tmp(n);
-        e = cudaMemcpy2DAsync(tmp.data(), (size_t)w, r.ptr, (size_t)c->g.pitch, (size_t)w, (size_t)h,
-                              cudaMemcpyDeviceToHost, c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-        int *dst = (int *)host;
-        for (size_t k = 0; k < n; k++) dst[k] = tmp[k];
+    if (!r.is_mask && sizeof(T) == sizeof(double)) {
+        e = cudaMemcpy2DAsync(host, (size_t)w * sizeof(double), r.ptr, (size_t)c->g.pitch * sizeof(T),
+                              (size_t)w * sizeof(double), (size_t)h, cudaMemcpyDeviceToHost, c->stream);
     } else {
-        std::vector<T> tmp(n);
-        e = cudaMemcpy2DAsync(tmp.data(), (size_t)w * sizeof(T), r.ptr, (size_t)c->g.pitch * sizeof(T),
-                              (size_t)w * sizeof(T), (size_t)h, cudaMemcpyDeviceToHost, c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-        double *dst = (double *)host;
-        for (size_t k = 0; k < n; k++) dst[k] = (double)tmp[k];
+        const size_t esz = r.is_mask ? sizeof(int) : sizeof(double);
+        convert_out(c, r.ptr, r.is_mask, c->staging, w, h);
+        e = cudaMemcpyAsync(host, c->staging, (size_t)w * h * esz, cudaMemcpyDeviceToHost, c->stream);
     }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return cuda_status(c, e);
 }
 
@@ -182,7 +170,11 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
     f.omega = (double *)take((size_t)nf * sizeof(double));
     f.wmcs = (double *)take((size_t)nf * 2 * sizeof(double));
     f.Cm = f.Sm = nullptr;  // band tables are allocated by fw_init
-    if (assign) c->F<T>() = f;
+    void *stg = take((size_t)(g.Mloc + 1) * (size_t)(g.Nloc + 1) * sizeof(double));
+    if (assign) {
+        c->F<T>() = f;
+        c->staging = stg;
+    }
     return off;
 }
 
@@ -632,6 +624,35 @@ int fw_sync(fw_ctx *c) {
 }
 
 long long fw_launch_count(fw_ctx *c) { return c ? c->launches : -1; }
+
+int fw_time_kernel(fw_ctx *c, const char *name, int nrep, double *ms_per_launch) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    if (!name || nrep < 1 || !ms_per_launch) return FW_ERR_BAD_PARAM;
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return cuda_status(c, cudaGetLastError());
+    const bool fp64 = c->p.precision == FW_PREC_FP64;
+    // one untimed launch validates the name and warms the caches
+    if ((fp64 ? launch_by_name<double>(c, name) : launch_by_name<float>(c, name)) != 0) {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return FW_ERR_BAD_PARAM;
+    }
+    cudaError_t e = cudaEventRecord(a, c->stream);
+    for (int k = 0; k < nrep && e == cudaSuccess; k++) {
+        if (fp64) launch_by_name<double>(c, name);
+        else launch_by_name<float>(c, name);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    *ms_per_launch = (double)ms / nrep;
+    return finish(c);
+}
 void *fw_stream(fw_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 }  // extern "C"

@@ -82,6 +82,10 @@ template <typename T> void launch_breaking(fw_ctx *c);
 template <typename T> void launch_sponge(fw_ctx *c);
 template <typename T> void launch_end_step(fw_ctx *c);
 template <typename T> void launch_stage(fw_ctx *c, int istage);
+template <typename T> int launch_by_name(fw_ctx *c, const char *name);
+// staging buffer <-> field (double <-> float fields, int32 <-> uint8 masks)
+void convert_in(fw_ctx *c, const void *staging, int is_mask, void *field, int w, int h);
+void convert_out(fw_ctx *c, const void *field, int is_mask, void *staging, int w, int h);
 
 }  // namespace fw
 
@@ -96,6 +100,7 @@ struct fw_ctx {
     fw::Fields<float> ff{};
     fw::LinePart px{}, py{};
     void *arena = nullptr;       // one device allocation holds every field
+    void *staging = nullptr;     // one host-layout plane for field transfers
     size_t arena_bytes = 0;
     int ncand_cap = 0;
     long long launches = 0;

@@ -23,6 +23,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 
 #include "fw_internal.h"
 
@@ -128,11 +129,28 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
     f.B[id] = sx2 * DUxx + DVxy;
     f.C[id] = Uxy + sy3 * Vyy;
     f.E[id] = DUxy + sy3 * DVyy;
-    if (!stale && (g.gamma2 > 0.0 || g.show_breaking)) {
+    // ETAx, ETAy: computed on the interior and exchanged only when Gamma2 > 0
+    // (bc.F:395-398); without Gamma2 the ghosts keep their old values
+    const bool exch = g.gamma2 > 0.0;
+    if (exch || (g.show_breaking && !gx && !gy)) {
         const T ex = (f.Eta[IDX(si + 1, sj)] - f.Eta[IDX(si - 1, sj)]) / DX / (T)2 * m9;
         const T ey = (f.Eta[IDX(si, sj + 1)] - f.Eta[IDX(si, sj - 1)]) / DY / (T)2 * m9;
-        f.ETAx[id] = sx2 * ex;
-        f.ETAy[id] = sy3 * ey;
+        if (!stale) {
+            if (exch && g.periodic && gx && !gy) {
+                // the periodic copy (bc.F:735-740) runs before the x mirror:
+                // a corner cell receives this x-ghost cell's previous value
+                if (j >= g.je - 2) {
+                    f.ETAx[IDX(i, j - (g.je - 2))] = f.ETAx[id];
+                    f.ETAy[IDX(i, j - (g.je - 2))] = f.ETAy[id];
+                }
+                if (j <= g.jb + 2) {
+                    f.ETAx[IDX(i, j + g.je - 2)] = f.ETAx[id];
+                    f.ETAy[IDX(i, j + g.je - 2)] = f.ETAy[id];
+                }
+            }
+            f.ETAx[id] = sx2 * ex;
+            f.ETAy[id] = sy3 * ey;
+        }
     }
 }
 
@@ -1154,7 +1172,7 @@ __device__ __forceinline__ void ghost_x_cell(const Grid &g, T *phi, int i, int j
     const T v = phi[IDX(si, j)];
     if (g.periodic) {
         if (j >= g.je - 2) phi[IDX(i, j - (g.je - 2))] = phi[IDX(i, j)];
-        else if (j <= g.jb + 2) phi[IDX(i, j + g.je - 2)] = phi[IDX(i, j)];
+        if (j <= g.jb + 2) phi[IDX(i, j + g.je - 2)] = phi[IDX(i, j)];
     }
     phi[IDX(i, j)] = (vtype == 2) ? -v : v;
 }
@@ -1558,6 +1576,75 @@ template <typename T> void launch_stage(fw_ctx *c, int istage) {
     launch_breaking<T>(c);
     launch_exchange<T>(c, g.direct_sponge != 0);
 }
+
+// ---------------------------------------------------------------------------
+// host-layout conversion: a Fortran (w x h, leading dimension w) array in a
+// device staging buffer <-> a pitched field
+// ---------------------------------------------------------------------------
+template <typename S, typename D>
+__global__ void k_unpack(const S *src, int w, int h, D *dst, int pitch) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= w || j >= h) return;
+    dst[(size_t)i + (size_t)j * pitch] = (D)src[(size_t)i + (size_t)j * w];
+}
+template <typename S, typename D>
+__global__ void k_pack(const S *src, int pitch, int w, int h, D *dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= w || j >= h) return;
+    dst[(size_t)i + (size_t)j * w] = (D)src[(size_t)i + (size_t)j * pitch];
+}
+__global__ void k_unpack_mask(const int *src, int w, int h, uint8_t *dst, int pitch) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= w || j >= h) return;
+    const int v = src[(size_t)i + (size_t)j * w];
+    dst[(size_t)i + (size_t)j * pitch] = (uint8_t)(v > 0 ? 1 : 0);
+}
+
+void convert_in(fw_ctx *c, const void *staging, int is_mask, void *field, int w, int h) {
+    const dim3 b(32, 8), gr((w + 31) / 32, (h + 7) / 8);
+    if (is_mask) k_unpack_mask<<<gr, b, 0, c->stream>>>((const int *)staging, w, h, (uint8_t *)field, c->g.pitch);
+    else k_unpack<double, float><<<gr, b, 0, c->stream>>>((const double *)staging, w, h, (float *)field, c->g.pitch);
+    note(c);
+}
+void convert_out(fw_ctx *c, const void *field, int is_mask, void *staging, int w, int h) {
+    const dim3 b(32, 8), gr((w + 31) / 32, (h + 7) / 8);
+    if (is_mask) k_pack<uint8_t, int><<<gr, b, 0, c->stream>>>((const uint8_t *)field, c->g.pitch, w, h, (int *)staging);
+    else k_pack<float, double><<<gr, b, 0, c->stream>>>((const float *)field, c->g.pitch, w, h, (double *)staging);
+    note(c);
+}
+
+// one kernel of the step by name, for timing (fw_time_kernel)
+template <typename T> int launch_by_name(fw_ctx *c, const char *name) {
+    const Grid &g = c->g;
+    Fields<T> &f = c->F<T>();
+    const dim3 gc = grid2(g.Mloc, g.Nloc, B2D);
+    auto is = [&](const char *n) { return std::strcmp(name, n) == 0; };
+    if (is("disp_a")) k_disp_a<T><<<gc, B2D, 0, c->stream>>>(g, f);
+    else if (is("disp_b")) k_disp_b<T><<<gc, B2D, 0, c->stream>>>(g, f);
+    else if (is("flux_x")) k_flux<T, 0><<<grid2(g.Mloc + 1, g.Nloc, B2D), B2D, 0, c->stream>>>(g, f);
+    else if (is("flux_y")) k_flux<T, 1><<<grid2(g.Mloc, g.Nloc + 1, B2D), B2D, 0, c->stream>>>(g, f);
+    else if (is("update")) k_update<T><<<gc, B2D, 0, c->stream>>>(g, f, (T)0.75, (T)0.25);
+    else if (is("tri_x")) { launch_tri<T, 0, false>(c, c->px); return 0; }
+    else if (is("tri_y")) {
+        if (g.periodic) launch_tri<T, 1, true>(c, c->py);
+        else launch_tri<T, 1, false>(c, c->py);
+        return 0;
+    }
+    else if (is("post")) k_post<T><<<gc, B2D, 0, c->stream>>>(g, f);
+    else if (is("mask")) k_mask<T><<<grid2(g.Mloc + 1, g.Nloc + 1, B2D), B2D, 0, c->stream>>>(g, f);
+    else if (is("break_a")) k_break_a<T><<<gc, B2D, 0, c->stream>>>(g, f);
+    else if (is("ghost")) { launch_ghost<T>(c, g.visc_breaking != 0); return 0; }
+    else if (is("maskmul")) k_maskmul<T><<<gc, B2D, 0, c->stream>>>(g, f, g.direct_sponge);
+    else if (is("begin")) k_begin<T><<<gc, B2D, 0, c->stream>>>(g, f);
+    else return -1;
+    note(c);
+    return 0;
+}
+template int launch_by_name<double>(fw_ctx *, const char *);
+template int launch_by_name<float>(fw_ctx *, const char *);
 
 #define INST(T)                                                  \
     template void launch_begin_step<T>(fw_ctx *);                \

@@ -193,6 +193,7 @@ def load_library(path=None):
     L.fw_launch_count.restype = ctypes.c_longlong
     L.fw_stream.argtypes = [vp]
     L.fw_stream.restype = vp
+    L.fw_time_kernel.argtypes = [vp, ctypes.c_char_p, ip, ctypes.POINTER(dp)]
     L.fw_strerror.argtypes = [ip]
     L.fw_strerror.restype = ctypes.c_char_p
     if path == lib_path():
@@ -338,6 +339,12 @@ class Solver:
 
     def sponge_damping(self):
         self._check(self.L.fw_sponge_damping(self.ctx), "SPONGE_DAMPING")
+
+    def time_kernel(self, name, nrep=20):
+        """Average duration (ms) of one kernel of the step, CUDA events."""
+        ms = ctypes.c_double()
+        self._check(self.L.fw_time_kernel(self.ctx, name.encode(), int(nrep), ctypes.byref(ms)), name)
+        return ms.value
 
     def launch_count(self):
         return int(self.L.fw_launch_count(self.ctx))

@@ -152,8 +152,16 @@ int fw_update_mask(fw_ctx *ctx);         /* UPDATE_MASK     masks.F:51 */
 int fw_wave_breaking(fw_ctx *ctx);       /* WAVE_BREAKING   breaker.F:60 */
 int fw_sponge_damping(fw_ctx *ctx);      /* SPONGE_DAMPING  sponge.F:52 */
 
-/* Kernel launches issued by this context since creation (diagnostics). */
+/* Kernel launches issued by this context since creation (diagnostics;
+ * launches recorded into a CUDA graph are counted once, at capture). */
 long long fw_launch_count(fw_ctx *ctx);
+/* Time nrep back-to-back launches of one kernel of the step with CUDA events
+ * on the context stream; *ms_per_launch = average duration.  Names:
+ * "disp_a","disp_b","flux_x","flux_y","update","tri_x","tri_y","post",
+ * "mask","break_a","ghost","maskmul","begin".  Kernels that update state in
+ * place (update, post, mask, maskmul, begin) change the state: time them on
+ * a context whose state is disposable.  No reference counterpart. */
+int fw_time_kernel(fw_ctx *ctx, const char *name, int nrep, double *ms_per_launch);
 /* CUDA stream of the context, as a void* (cudaStream_t). */
 void *fw_stream(fw_ctx *ctx);
 /* Human-readable text of a status code. */
