@@ -152,7 +152,8 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
     T **tf[] = {&f.Eta,   &f.U,     &f.V,     &f.Ubar,   &f.Vbar,  &f.HU,   &f.HV,    &f.H,     &f.Eta0,
                 &f.Ubar0, &f.Vbar0, &f.U0,    &f.V0,     &f.Depth, &f.Depthx, &f.Depthy, &f.Cd, &f.SPONGE,
                 &f.CD4,   &f.P,     &f.Q,     &f.Fx,     &f.Fy,    &f.Gx,   &f.Gy,    &f.A,     &f.B,
-                &f.C,     &f.E,     &f.U4,    &f.V4,     &f.U1p,   &f.V1p,  &f.Udisp, &f.Vdisp, &f.ETAx,
+                &f.C,     &f.E,     &f.Uxx,   &f.Vxy,   &f.Uxy,   &f.Vyy,   &f.DUxx,  &f.DVxy,
+                &f.DUxy,  &f.DVyy,  &f.U4,    &f.V4,     &f.U1p,   &f.V1p,  &f.Udisp, &f.Vdisp, &f.ETAx,
                 &f.ETAy,  &f.ETAT,  &f.AGE,   &f.AGEn,   &f.nu,    &f.SourceX, &f.SourceY, &f.WM, &f.Hmax};
     for (T **p : tf) *p = (T *)take(plane * sizeof(T));
     uint8_t **mf[] = {&f.MASK, &f.MASKn, &f.MASK9, &f.MASK_STRUC};
@@ -346,6 +347,14 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     g.ihi = 0;
     g.jlo = 1;
     g.jhi = 0;
+    for (int d = 0; d < 2; d++) {
+        const double h = d == 0 ? p->DX : p->DY;
+        g.cA[d] = g.b1 / 2.0 / (h * h);
+        g.cB[d] = g.b2 / (h * h);
+        g.cC[d] = (-g.b1 - 2.0 * g.b2) / (h * h);
+    }
+    g.rdx = 1.0 / p->DX;
+    g.rdy = 1.0 / p->DY;
     c->px = make_part(p->Mglob, p->Nglob);
     c->py = make_part(p->Nglob, p->Mglob);
     c->ncand_cap = (p->Mglob + 2) * (p->Nglob + 2);

@@ -33,6 +33,10 @@ struct Grid {
     double trough, crest;
     double xc_wk, yc_wk, ywidth_wk, width_wk;
     double D_gen, beta_gen, rlamda, tperiod, time_ramp, freq_peak;
+    // constants of the mixed path: tridiagonal coefficient factors per
+    // direction (b1/2/h^2, b2/h^2, (-b1-2*b2)/h^2) and 1/DX, 1/DY
+    double cA[2], cB[2], cC[2];
+    double rdx, rdy;
 };
 
 // device scalar slots (double array)
@@ -44,7 +48,8 @@ struct Fields {
     T *Eta0, *Ubar0, *Vbar0, *U0, *V0;
     T *Depth, *Depthx, *Depthy, *Cd, *SPONGE, *CD4;
     T *P, *Q, *Fx, *Fy, *Gx, *Gy;
-    T *A, *B, *C, *E;                 // exchanged Uxx+Vxy, DUxx+DVxy, Uxy+Vyy, DUxy+DVyy
+    T *A, *B, *C, *E;                 // mixed: exchanged Uxx+Vxy, DUxx+DVxy, Uxy+Vyy, DUxy+DVyy
+    T *Uxx, *Vxy, *Uxy, *Vyy, *DUxx, *DVxy, *DUxy, *DVyy;  // FP64: the exchanged terms themselves
     T *U4, *V4, *U1p, *V1p, *Udisp, *Vdisp;  // Udisp = U1pp+U2+U3
     T *ETAx, *ETAy, *ETAT;
     T *AGE, *AGEn, *nu;               // AGE ping-pong (old / new)

@@ -125,10 +125,23 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
 #undef DXX
 #undef DYY
 #undef DXY
-    f.A[id] = sx2 * Uxx + Vxy;
-    f.B[id] = sx2 * DUxx + DVxy;
-    f.C[id] = Uxy + sy3 * Vyy;
-    f.E[id] = DUxy + sy3 * DVyy;
+    if constexpr (sizeof(T) == sizeof(double)) {
+        // FP64: keep every exchanged term (VTYPE 2: Uxx DUxx; 3: Vyy DVyy;
+        // 1: the cross derivatives), as EXCHANGE_DISPERSION leaves them
+        f.Uxx[id] = sx2 * Uxx;
+        f.DUxx[id] = sx2 * DUxx;
+        f.Vyy[id] = sy3 * Vyy;
+        f.DVyy[id] = sy3 * DVyy;
+        f.Uxy[id] = Uxy;
+        f.Vxy[id] = Vxy;
+        f.DUxy[id] = DUxy;
+        f.DVxy[id] = DVxy;
+    } else {
+        f.A[id] = sx2 * Uxx + Vxy;
+        f.B[id] = sx2 * DUxx + DVxy;
+        f.C[id] = Uxy + sy3 * Vyy;
+        f.E[id] = DUxy + sy3 * DVyy;
+    }
     // ETAx, ETAy: computed on the interior and exchanged only when Gamma2 > 0
     // (bc.F:395-398); without Gamma2 the ghosts keep their old values
     const bool exch = g.gamma2 > 0.0;
@@ -168,7 +181,19 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
     const T B1 = (T)g.Beta_1, B2 = (T)g.Beta_2, g2 = (T)g.gamma2, b2 = (T)g.b2;
     const T one = (T)1, two = (T)2, half = (T)0.5;
     const T D = f.Depth[id], reta = f.Eta[id], m9 = (T)f.MASK9[id];
-    const T a = f.A[id], b = f.B[id], c = f.C[id], e = f.E[id];
+    constexpr bool EXACT = sizeof(T) == sizeof(double);
+    T a, b, c, e;
+    if constexpr (EXACT) {
+        a = f.Uxx[id] + f.Vxy[id];
+        b = f.DUxx[id] + f.DVxy[id];
+        c = f.Uxy[id] + f.Vyy[id];
+        e = f.DUxy[id] + f.DVyy[id];
+    } else {
+        a = f.A[id];
+        b = f.B[id];
+        c = f.C[id];
+        e = f.E[id];
+    }
     T u4 = (one / (T)3 - B1 + half * B1 * B1) * D * D * a + (B1 - one / two) * D * b;
     T v4 = (one / (T)3 - B1 + half * B1 * B1) * D * D * c + (B1 - one / two) * D * e;
     if (g.gamma2 > 0.0) {
@@ -190,14 +215,31 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
     const bool wall = (i == g.ib) || (i == g.ie) || (j == g.jb) || (j == g.je);
 #define AT(F, a_, b_) f.F[IDX(i + (a_), j + (b_))]
     const T UxxVxy = a, UxyVyy = c, HUxxHVxy = b, HUxyHVyy = e;
-    const T UxxVxy_x = (AT(A, 1, 0) - AT(A, -1, 0)) / two / DX;
-    const T UxxVxy_y = (AT(A, 0, 1) - AT(A, 0, -1)) / two / DY;
-    const T UxyVyy_x = (AT(C, 1, 0) - AT(C, -1, 0)) / two / DX;
-    const T UxyVyy_y = (AT(C, 0, 1) - AT(C, 0, -1)) / two / DY;
-    const T HUxxHVxy_x = (AT(B, 1, 0) - AT(B, -1, 0)) / two / DX;
-    const T HUxxHVxy_y = (AT(B, 0, 1) - AT(B, 0, -1)) / two / DY;
-    const T HUxyHVyy_x = (AT(E, 1, 0) - AT(E, -1, 0)) / two / DX;
-    const T HUxyHVyy_y = (AT(E, 0, 1) - AT(E, 0, -1)) / two / DY;
+    T UxxVxy_x, UxxVxy_y, UxyVyy_x, UxyVyy_y, HUxxHVxy_x, HUxxHVxy_y, HUxyHVyy_x, HUxyHVyy_y;
+    if constexpr (EXACT) {
+        // (F1(I+1)+F2(I+1)-F1(I-1)-F2(I-1))/2/DX, evaluated left to right
+#define DIFF(F1, F2, a1, b1, a2, b2, H) \
+    ((AT(F1, a1, b1) + AT(F2, a1, b1) - AT(F1, a2, b2) - AT(F2, a2, b2)) / two / H)
+        UxxVxy_x = DIFF(Uxx, Vxy, 1, 0, -1, 0, DX);
+        UxxVxy_y = DIFF(Uxx, Vxy, 0, 1, 0, -1, DY);
+        UxyVyy_x = DIFF(Uxy, Vyy, 1, 0, -1, 0, DX);
+        UxyVyy_y = DIFF(Uxy, Vyy, 0, 1, 0, -1, DY);
+        HUxxHVxy_x = DIFF(DUxx, DVxy, 1, 0, -1, 0, DX);
+        HUxxHVxy_y = DIFF(DUxx, DVxy, 0, 1, 0, -1, DY);
+        HUxyHVyy_x = DIFF(DUxy, DVyy, 1, 0, -1, 0, DX);
+        HUxyHVyy_y = DIFF(DUxy, DVyy, 0, 1, 0, -1, DY);
+#undef DIFF
+    } else {
+        const T hx = (T)(0.5 * g.rdx), hy = (T)(0.5 * g.rdy);
+        UxxVxy_x = (AT(A, 1, 0) - AT(A, -1, 0)) * hx;
+        UxxVxy_y = (AT(A, 0, 1) - AT(A, 0, -1)) * hy;
+        UxyVyy_x = (AT(C, 1, 0) - AT(C, -1, 0)) * hx;
+        UxyVyy_y = (AT(C, 0, 1) - AT(C, 0, -1)) * hy;
+        HUxxHVxy_x = (AT(B, 1, 0) - AT(B, -1, 0)) * hx;
+        HUxxHVxy_y = (AT(B, 0, 1) - AT(B, 0, -1)) * hy;
+        HUxyHVyy_x = (AT(E, 1, 0) - AT(E, -1, 0)) * hx;
+        HUxyHVyy_y = (AT(E, 0, 1) - AT(E, 0, -1)) * hy;
+    }
     const T rh = D;
     const T rhx = (AT(Depth, 1, 0) - AT(Depth, -1, 0)) / two / DX;
     const T rhy = (AT(Depth, 0, 1) - AT(Depth, 0, -1)) / two / DY;
@@ -590,34 +632,45 @@ __global__ void __launch_bounds__(256) k_update(Grid g, Fields<T> f, T al, T be)
     f.H[id] = H;
     if (!g.dispersion) return;
 
-    // tmp4 of the x and y systems, in double (etauv_solver.F:410-411, 508-509)
-    const double ddx = g.DX, ddy = g.DY, mdf = g.min_depth_frc;
+    // tmp4 of the x and y systems (etauv_solver.F:410-411, 508-509)
+    const double mdf = g.min_depth_frc;
     const double g1 = g.gamma1, b1 = g.b1, b2 = g.b2;
     const double m9 = (double)f.MASK9[id];
     const double mk = (double)f.MASK[id];
     const double dep = tmax((double)f.Depth[id], mdf);
-    const bool wall = (i == g.ib) || (i == g.ie) || (j == g.jb) || (j == g.je);
-    double Vxy = 0.0, DVxy = 0.0, Uxy = 0.0, DUxy = 0.0;
-    if (!wall) {
-#define XY(F)                                                                                 \
-    ((((F(1, 1) - F(1, -1)) / 2.0 / ddy) - ((F(-1, 1) - F(-1, -1)) / 2.0 / ddy)) / 2.0 / ddx * m9)
-#define LV(a, b) ((double)f.V[IDX(i + (a), j + (b))])
-#define LU(a, b) ((double)f.U[IDX(i + (a), j + (b))])
-#define LDV(a, b) (tmax((double)f.Depth[IDX(i + (a), j + (b))], mdf) * LV(a, b))
-#define LDU(a, b) (tmax((double)f.Depth[IDX(i + (a), j + (b))], mdf) * LU(a, b))
-        Vxy = XY(LV);
-        DVxy = XY(LDV);
-        Uxy = XY(LU);
-        DUxy = XY(LDU);
+    const double Hm = tmax((double)H, mdf);
+    if constexpr (sizeof(T) == sizeof(double)) {
+        // the cross derivatives CAL_DISPERSION left at the start of the stage
+        const double Vxy = f.Vxy[id], DVxy = f.DVxy[id], Uxy = f.Uxy[id], DUxy = f.DUxy[id];
+        f.rhs_x[id] = (double)ubar * mk / Hm + g1 * m9 * (-b1 / 2.0 * dep * dep * Vxy - b2 * dep * DVxy);
+        f.rhs_y[id] = (double)vbar * mk / Hm + g1 * m9 * (-b1 / 2.0 * dep * dep * Uxy - b2 * dep * DUxy);
+    } else {
+        // mixed: cross derivatives of the stage-start U, V in float
+        const bool wall = (i == g.ib) || (i == g.ie) || (j == g.jb) || (j == g.je);
+        T Vxy = (T)0, DVxy = (T)0, Uxy = (T)0, DUxy = (T)0;
+        if (!wall) {
+            const T q = (T)(0.25 * g.rdx * g.rdy) * (T)m9;
+            const T mf = (T)mdf;
+#define XY(F) (((F(1, 1) - F(1, -1)) - (F(-1, 1) - F(-1, -1))) * q)
+#define LV(a, b) (f.V[IDX(i + (a), j + (b))])
+#define LU(a, b) (f.U[IDX(i + (a), j + (b))])
+#define LDV(a, b) (tmax(f.Depth[IDX(i + (a), j + (b))], mf) * LV(a, b))
+#define LDU(a, b) (tmax(f.Depth[IDX(i + (a), j + (b))], mf) * LU(a, b))
+            Vxy = XY(LV);
+            DVxy = XY(LDV);
+            Uxy = XY(LU);
+            DUxy = XY(LDU);
 #undef XY
 #undef LV
 #undef LU
 #undef LDV
 #undef LDU
+        }
+        const T fd = (T)dep, fg = (T)(g1 * m9), rH = (T)1 / (T)Hm;
+        const T hb1 = (T)(-0.5 * b1), fb2 = (T)b2;
+        f.rhs_x[id] = (double)(ubar * (T)mk * rH + fg * (hb1 * fd * fd * Vxy - fb2 * fd * DVxy));
+        f.rhs_y[id] = (double)(vbar * (T)mk * rH + fg * (hb1 * fd * fd * Uxy - fb2 * fd * DUxy));
     }
-    const double Hm = tmax((double)H, mdf);
-    f.rhs_x[id] = (double)ubar * mk / Hm + g1 * m9 * (-b1 / 2.0 * dep * dep * Vxy - b2 * dep * DVxy);
-    f.rhs_y[id] = (double)vbar * mk / Hm + g1 * m9 * (-b1 / 2.0 * dep * dep * Uxy - b2 * dep * DUxy);
 }
 
 // ---------------------------------------------------------------------------
@@ -633,25 +686,46 @@ __global__ void __launch_bounds__(256) k_update(Grid g, Fields<T> f, T al, T be)
 template <typename T, int DIR>
 __device__ __forceinline__ void tri_coef(const Grid &g, const Fields<T> &f, int i, int j, double &a, double &c,
                                          double &d) {
-    const double h = DIR == 0 ? g.DX : g.DY;
-    const double mdf = g.min_depth_frc, g1 = g.gamma1, b1 = g.b1, b2 = g.b2;
+    const double mdf = g.min_depth_frc, g1 = g.gamma1;
     const size_t id = IDX(i, j);
     const double dep = tmax((double)f.Depth[id], mdf);
     const double depl = tmax((double)f.Depth[DIR == 0 ? IDX(i - 1, j) : IDX(i, j - 1)], mdf);
     const double depr = tmax((double)f.Depth[DIR == 0 ? IDX(i + 1, j) : IDX(i, j + 1)], mdf);
     const double m9 = (double)f.MASK9[id];
-    const double tmp1 = g1 * m9 * (b1 / 2.0 / h / h * dep * dep + b2 / h / h * depl * dep);
-    const double tmp2 = 1.0 + g1 * m9 * (-b1 / h / h * dep * dep - 2.0 * b2 / h / h * dep * dep);
-    const double tmp3 = g1 * m9 * (b1 / 2.0 / h / h * dep * dep + b2 / h / h * dep * depr);
     const double tmp4 = DIR == 0 ? f.rhs_x[id] : f.rhs_y[id];
-    if (tmp2 != 0.0 || f.MASK[id] > 0) {
-        a = tmp1 / tmp2;
-        c = tmp3 / tmp2;
-        d = tmp4 / tmp2;
+    double tmp1, tmp2, tmp3;
+    if constexpr (sizeof(T) == sizeof(double)) {
+        // the reference's expressions (etauv_solver.F:406-409, 504-507)
+        const double h = DIR == 0 ? g.DX : g.DY, b1 = g.b1, b2 = g.b2;
+        tmp1 = g1 * m9 * (b1 / 2.0 / h / h * dep * dep + b2 / h / h * depl * dep);
+        tmp2 = 1.0 + g1 * m9 * (-b1 / h / h * dep * dep - 2.0 * b2 / h / h * dep * dep);
+        tmp3 = g1 * m9 * (b1 / 2.0 / h / h * dep * dep + b2 / h / h * dep * depr);
+        if (tmp2 != 0.0 || f.MASK[id] > 0) {
+            a = tmp1 / tmp2;
+            c = tmp3 / tmp2;
+            d = tmp4 / tmp2;
+        } else {
+            a = 0.0;
+            c = 0.0;
+            d = 0.0;
+        }
     } else {
-        a = 0.0;
-        c = 0.0;
-        d = 0.0;
+        // mixed: the same coefficients from per-direction constants and one
+        // reciprocal
+        const double gm = g1 * m9;
+        tmp1 = gm * dep * (g.cA[DIR] * dep + g.cB[DIR] * depl);
+        tmp2 = 1.0 + gm * g.cC[DIR] * dep * dep;
+        tmp3 = gm * dep * (g.cA[DIR] * dep + g.cB[DIR] * depr);
+        if (tmp2 != 0.0 || f.MASK[id] > 0) {
+            const double r = 1.0 / tmp2;
+            a = tmp1 * r;
+            c = tmp3 * r;
+            d = tmp4 * r;
+        } else {
+            a = 0.0;
+            c = 0.0;
+            d = 0.0;
+        }
     }
 }
 
@@ -727,12 +801,12 @@ __global__ void __launch_bounds__(128) k_tri_a(Grid g, Fields<T> f, LinePart lp)
             double a, c, d;
             row_coef<T, DIR, PER>(g, f, lp, l, k, a, c, d);
             const double lower = (k > s + 1) ? a : 0.0;
-            const double r = 1.0 - lower * cp;
+            const double r = 1.0 / (1.0 - lower * cp);
             const double upper = (k < e - 1) ? c : 0.0;
-            cp = upper / r;
-            yp = (d - lower * yp) / r;
-            pp = ((k == s + 1 ? a : 0.0) - lower * pp) / r;
-            qp = ((k == e - 1 ? c : 0.0) - lower * qp) / r;
+            cp = upper * r;
+            yp = (d - lower * yp) * r;
+            pp = ((k == s + 1 ? a : 0.0) - lower * pp) * r;
+            qp = ((k == e - 1 ? c : 0.0) - lower * qp) * r;
             int ii, jj;
             line_cell<DIR>(g, l, k, ii, jj);
             const size_t q = IDX(ii, jj);
@@ -877,6 +951,92 @@ __global__ void __launch_bounds__(128) k_tri_c(Grid g, Fields<T> f, LinePart lp)
         line_cell<DIR>(g, l, k, i, j);
         const size_t q = IDX(i, j);
         out[q] = (T)(f.ty[q] - f.tp[q] * xs - f.tq[q] * xe);
+    }
+}
+
+// FP64: one thread per line, the reference's Thomas recurrence in its own
+// operation order (TRIDx_ser / TRIDy_ser, tridiagnal.F:338-398) and, for
+// periodic y, TRIDy_periodic's two solves and combination
+// (tridiagnal.F:59-325).  c' and d' (and e' for the second periodic
+// solve) are kept in the solver scratch.
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(128) k_thomas(Grid g, Fields<T> f, LinePart lp) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= lp.nlines) return;
+    const int L = lp.L;
+    double a_beg = 0.0, c_end = 0.0;
+    int i, j;
+    if (PER) {
+        double a, c, d;
+        line_cell<DIR>(g, l, 0, i, j);
+        tri_coef<T, DIR>(g, f, i, j, a, c, d);
+        a_beg = a;
+        line_cell<DIR>(g, l, L - 1, i, j);
+        tri_coef<T, DIR>(g, f, i, j, a, c, d);
+        c_end = c;
+    }
+    double cp = 0.0, dp = 0.0, ep = 0.0;
+    for (int k = 0; k < L; k++) {
+        double a, c, d;
+        line_cell<DIR>(g, l, k, i, j);
+        tri_coef<T, DIR>(g, f, i, j, a, c, d);
+        double e = 0.0;
+        if (PER) {
+            if (k == 0) {
+                c = c / (1 + c_end);
+                d = d / (1 + c_end);
+                e = 1.0 / (1.0 + c_end);
+            }
+            if (k == L - 1) {
+                a = a / (1 + a_beg);
+                d = d / (1 + a_beg);
+                e = -1.0 / (1.0 + a_beg);
+            }
+        }
+        if (k > 0 && a != 0.0) {
+            const double den = 1.0 / a - cp;
+            c = c / a / den;
+            d = (d / a - dp) / den;
+            if (PER) e = (e / a - ep) / den;
+        }
+        cp = c;
+        dp = d;
+        ep = e;
+        const size_t q = IDX(i, j);
+        f.tp[q] = c;
+        f.ty[q] = d;
+        if (PER) f.tq[q] = e;
+    }
+    // back substitution; y1 into ty, y2 into tq
+    double z1 = 0.0, z2 = 0.0;
+    for (int k = L - 1; k >= 0; k--) {
+        line_cell<DIR>(g, l, k, i, j);
+        const size_t q = IDX(i, j);
+        if (k == L - 1) {
+            z1 = f.ty[q];
+            if (PER) z2 = f.tq[q];
+        } else {
+            z1 = f.ty[q] - f.tp[q] * z1;
+            if (PER) z2 = f.tq[q] - f.tp[q] * z2;
+        }
+        if (PER) {
+            f.ty[q] = z1;
+            f.tq[q] = z2;
+        } else {
+            (DIR == 0 ? f.U : f.V)[q] = (T)z1;
+        }
+    }
+    if (PER) {
+        line_cell<DIR>(g, l, 0, i, j);
+        const size_t q0 = IDX(i, j);
+        line_cell<DIR>(g, l, L - 1, i, j);
+        const size_t q1 = IDX(i, j);
+        const double beta = (c_end * f.ty[q0] - a_beg * f.ty[q1]) / (1.0 - (c_end * f.tq[q0] - a_beg * f.tq[q1]));
+        for (int k = 0; k < L; k++) {
+            line_cell<DIR>(g, l, k, i, j);
+            const size_t q = IDX(i, j);
+            (DIR == 0 ? f.U : f.V)[q] = (T)(f.ty[q] + beta * f.tq[q]);
+        }
     }
 }
 
@@ -1378,7 +1538,7 @@ __global__ void __launch_bounds__(256) k_dt_only(Grid g, Fields<T> f) {
 
 // DT = CFL*min (with DT_fixed halving), TIME += DT, and the JON_2D
 // cos/sin(omega_k TIME) table of this step (sources.F:121-124)
-__global__ void k_dt_final(Grid g, double *dsc, unsigned long long *bits, double *omega, double *wmcs, int nfreq) {
+static __global__ void k_dt_final(Grid g, double *dsc, unsigned long long *bits, double *omega, double *wmcs, int nfreq) {
     __shared__ double time_s;
     if (threadIdx.x == 0) {
         double tmp3 = __longlong_as_double((long long)*bits);
@@ -1509,6 +1669,11 @@ template <typename T> void launch_sources_debug(fw_ctx *c) {
 
 template <typename T, int DIR, bool PER> static void launch_tri(fw_ctx *c, const LinePart &lp) {
     const Grid &g = c->g;
+    if constexpr (sizeof(T) == sizeof(double)) {
+        k_thomas<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        note(c);
+        return;
+    }
     const int nt = lp.nlines * lp.P;
     k_tri_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
     note(c);
@@ -1577,6 +1742,7 @@ template <typename T> void launch_stage(fw_ctx *c, int istage) {
     launch_exchange<T>(c, g.direct_sponge != 0);
 }
 
+#ifdef FW_SHARED_DEFS
 // ---------------------------------------------------------------------------
 // host-layout conversion: a Fortran (w x h, leading dimension w) array in a
 // device staging buffer <-> a pitched field
@@ -1616,6 +1782,8 @@ void convert_out(fw_ctx *c, const void *field, int is_mask, void *staging, int w
     note(c);
 }
 
+#endif  // FW_SHARED_DEFS
+
 // one kernel of the step by name, for timing (fw_time_kernel)
 template <typename T> int launch_by_name(fw_ctx *c, const char *name) {
     const Grid &g = c->g;
@@ -1643,8 +1811,6 @@ template <typename T> int launch_by_name(fw_ctx *c, const char *name) {
     note(c);
     return 0;
 }
-template int launch_by_name<double>(fw_ctx *, const char *);
-template int launch_by_name<float>(fw_ctx *, const char *);
 
 #define INST(T)                                                  \
     template void launch_begin_step<T>(fw_ctx *);                \
@@ -1658,9 +1824,7 @@ template int launch_by_name<float>(fw_ctx *, const char *);
     template void launch_breaking<T>(fw_ctx *);                  \
     template void launch_sponge<T>(fw_ctx *);                    \
     template void launch_end_step<T>(fw_ctx *);                  \
-    template void launch_stage<T>(fw_ctx *, int);
-INST(double)
-INST(float)
-#undef INST
+    template void launch_stage<T>(fw_ctx *, int);     \
+    template int launch_by_name<T>(fw_ctx *, const char *);
 
 }  // namespace fw

@@ -22,7 +22,15 @@ _ROOT = os.path.dirname(_HERE)
 _CSRC = os.path.join(_HERE, "csrc")
 _BUILD = os.path.join(_HERE, "_build")
 _HEADER = os.path.join(_ROOT, "include", "funwave_gpu.h")
-_SOURCES = ["fw_kernels.cu", "fw_api.cu", "fw_init.cpp"]
+# translation units and their extra flags: the FP64 kernels and the host
+# initialisation keep every multiply and add separately rounded (the
+# reference's operation order); the mixed-precision kernels may contract
+_SOURCES = {
+    "fw_kernels_f64.cu": ["-fmad=false"],
+    "fw_kernels_f32.cu": [],
+    "fw_api.cu": [],
+    "fw_init.cpp": ["-Xcompiler", "-ffp-contract=off"],
+}
 
 FW_ERRORS = {0: "FW_OK", -1: "FW_ERR_CUDA", -2: "FW_ERR_OOM", -3: "FW_ERR_BAD_PARAM",
              -4: "FW_ERR_BLOWUP", -5: "FW_ERR_NAN", -6: "FW_ERR_UNSUPPORTED",
@@ -48,7 +56,8 @@ def build(verbose=False):
     os.makedirs(_BUILD, exist_ok=True)
     out = lib_path()
     srcs = [os.path.join(_CSRC, s) for s in _SOURCES]
-    deps = srcs + [os.path.join(_CSRC, h) for h in os.listdir(_CSRC) if h.endswith(".h")] + [_HEADER]
+    deps = srcs + [os.path.join(_CSRC, h) for h in os.listdir(_CSRC)
+                   if h.endswith(".h") or h.endswith(".cuh")] + [_HEADER]
     if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
         return out
     nvcc = os.environ.get("NVCC", "nvcc")
@@ -58,7 +67,7 @@ def build(verbose=False):
     for s in srcs:
         o = os.path.join(_BUILD, os.path.basename(s) + ".o")
         objs.append(o)
-        cmd = [nvcc] + common + arch + ["-c", s, "-o", o]
+        cmd = [nvcc] + common + arch + _SOURCES[os.path.basename(s)] + ["-c", s, "-o", o]
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     for cmd, p in procs:
         txt = p.communicate()[0].decode(errors="replace")

@@ -1,9 +1,11 @@
 """GPU parity with the CPU oracle, unit by unit and over whole steps.
 
-FP64: every compared field within 1e-9 of its scale per unit (the kernels
-round differently from the oracle only through fused multiply-adds, the
-partitioned tridiagonal elimination and CUDA's libm), MASK and MASK9
-bit-exact.  Mixed precision: eta within 1e-4 m of the FP64 oracle after the
+FP64: the kernels keep the reference's operation order without fused
+multiply-adds and solve the tridiagonal systems with the reference's Thomas
+recurrence, so they differ from the oracle only where CUDA's libm (exp, sin,
+cos, tanh, atan2 in the wavemaker, breaking and Froude cap) rounds its last
+bit differently from glibc: every field within 1e-11 of its scale per unit,
+MASK and MASK9 bit-exact.  Mixed precision: eta within 1e-4 m of the FP64 oracle after the
 stated steps, MASK mismatches counted.
 """
 import numpy as np
@@ -13,8 +15,8 @@ from helpers import G, interior, make_pair, maxrel, sloped_beach
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-9
-ATOL = 1e-12  # absolute floor: fields of physical size O(0.01-10) in SI units
+TOL = 1e-11
+ATOL = 1e-14  # absolute floor for values that are exact zeros in one of the two
 
 
 def _regions(s):
@@ -170,7 +172,7 @@ def test_whole_steps_fp64(fw, oracle_mod, periodic):
         assert np.array_equal(s.get("MASK"), o["MASK"]), "MASK after %d steps" % (4 * (k + 1))
         for name in ("Eta", "U", "V"):
             e = maxrel(interior(s.get(name)), interior(o[name]))
-            assert e <= 1e-7, "%s after %d steps: %.3e" % (name, 4 * (k + 1), e)
+            assert e <= 1e-9, "%s after %d steps: %.3e" % (name, 4 * (k + 1), e)
     assert abs(s.scalar("TIME") - o.scalar("TIME")) <= 1e-10 * o.scalar("TIME")
 
 
