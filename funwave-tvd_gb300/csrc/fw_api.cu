@@ -160,6 +160,17 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
     for (uint8_t **p : mf) *p = (uint8_t *)take(plane);
     double **df[] = {&f.rhs_x, &f.rhs_y, &f.ty, &f.tp, &f.tq};
     for (double **p : df) *p = (double *)take(plane * sizeof(double));
+    f.m9_dirty = (int *)take(sizeof(int));
+    if (sizeof(T) == sizeof(float)) {
+        for (int d = 0; d < 2; d++) {
+            double **ff[] = {&f.fac_it[d], &f.fac_r[d], &f.fac_lr[d], &f.fac_cp[d], &f.fac_p[d], &f.fac_q[d]};
+            for (double **p : ff) *p = (double *)take(plane * sizeof(double));
+            const LinePart &lp = d == 0 ? c->px : c->py;
+            // per line: 2P reduced rows x 3 + P chunks x 2 + 2P second solution + 3
+            const size_t per_line = (size_t)2 * lp.P * 3 + (size_t)lp.P * 2 + (size_t)2 * lp.P + 3;
+            f.fac_red[d] = (double *)take((size_t)lp.nlines * per_line * sizeof(double));
+        }
+    }
     const size_t nred = std::max((size_t)c->px.nlines * 2 * c->px.P, (size_t)c->py.nlines * 2 * c->py.P);
     f.red = (double *)take(nred * 6 * sizeof(double));
     f.dsc = (double *)take(S_NSLOT * sizeof(double));
@@ -358,6 +369,9 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     c->px = make_part(p->Mglob, p->Nglob);
     c->py = make_part(p->Nglob, p->Mglob);
     c->ncand_cap = (p->Mglob + 2) * (p->Nglob + 2);
+    // the factored solve assumes tmp2 = 1 + Gamma1*MASK9*(-b1-2*b2)/h^2*dep^2
+    // never vanishes, which holds for -b1-2*b2 >= 0 (Beta_ref in [-2, 0])
+    c->factored = (p->precision == FW_PREC_MIXED) && (-g.b1 - 2.0 * g.b2 >= 0.0) ? 1 : 0;
     const bool fp64 = p->precision == FW_PREC_FP64;
     const size_t bytes = fp64 ? carve<double>(c, nullptr, false) : carve<float>(c, nullptr, false);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -461,6 +475,9 @@ int fw_init(fw_ctx *c, const double *depth, const double *eta, const double *u, 
     }
     double sc[S_NSLOT] = {0};
     if ((rc = upload_array(c, dsc_ptr(c), sc, sizeof(sc))) != FW_OK) return rc;
+    const int one = 1;  // factor the tridiagonal matrices at the first stage
+    int *dirty = c->p.precision == FW_PREC_FP64 ? c->fd.m9_dirty : c->ff.m9_dirty;
+    if ((rc = upload_array(c, dirty, &one, sizeof(one))) != FW_OK) return rc;
     if (c->graph) {
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;

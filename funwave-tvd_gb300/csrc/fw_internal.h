@@ -59,6 +59,13 @@ struct Fields {
     double *rhs_x, *rhs_y;            // tmp4 of GET_Eta_U_V_HU_HV
     double *ty, *tp, *tq;             // chunked line-solver scratch
     double *red;                      // reduced systems
+    // mixed path: constant factorisation of the tridiagonal matrices, per
+    // direction d: per row 1/tmp2, r, lower*r, c', p, q; per reduced row
+    // lo, 1/den, c'; per chunk c_s, a_e; per line (periodic) the second
+    // solution, c_end, a_beg and the Sherman-Morrison denominator
+    double *fac_it[2], *fac_r[2], *fac_lr[2], *fac_cp[2], *fac_p[2], *fac_q[2];
+    double *fac_red[2];
+    int *m9_dirty;                    // MASK9 changed since the last factorisation
     double *Cm, *Sm, *omega, *wmcs;   // JON_2D band tables and cos/sin(omega t)
     double *dsc;                      // device scalars (S_*)
     int *cand, *ncand;                // breaking candidates
@@ -114,6 +121,7 @@ struct fw_ctx {
     double EtaBlowVal = 0.0;
     cudaGraphExec_t graph = nullptr;
     int graph_ready = 0;
+    int factored = 0;            // mixed path solves with the constant factorisation
     long long graph_state = 0;   // host buffer state the graph was captured with
     template <typename T> fw::Fields<T> &F();
 };

@@ -84,8 +84,12 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
     const T DX = (T)g.DX, DY = (T)g.DY, mdf = (T)g.min_depth_frc;
     const size_t id = IDX(i, j);
     // ETAT from the previous stage's face fluxes (dispersion.F:103-119)
-    if (i <= g.Mloc - 2 && j <= g.Nloc - 2)
-        f.ETAT[id] = -(f.P[IDX(i + 1, j)] - f.P[id]) / DX - (f.Q[IDX(i, j + 1)] - f.Q[id]) / DY;
+    if (i <= g.Mloc - 2 && j <= g.Nloc - 2) {
+        if constexpr (sizeof(T) == sizeof(double))
+            f.ETAT[id] = -(f.P[IDX(i + 1, j)] - f.P[id]) / DX - (f.Q[IDX(i, j + 1)] - f.Q[id]) / DY;
+        else
+            f.ETAT[id] = -(f.P[IDX(i + 1, j)] - f.P[id]) * (T)g.rdx - (f.Q[IDX(i, j + 1)] - f.Q[id]) * (T)g.rdy;
+    }
 
     const bool gx = (i < g.ib) || (i > g.ie);
     const bool gy = (j < g.jb) || (j > g.je);
@@ -110,12 +114,18 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
 #define LV(a, b) f.V[IDX(si + (a), sj + (b))]
 #define LDU(a, b) (tmax(f.Depth[IDX(si + (a), sj + (b))], mdf) * LU(a, b))
 #define LDV(a, b) (tmax(f.Depth[IDX(si + (a), sj + (b))], mdf) * LV(a, b))
-#define DXX(F) (((F(1, 0) - (T)2 * F(0, 0) + F(-1, 0)) / DX / DX) * m9)
-#define DYY(F) (((F(0, 1) - (T)2 * F(0, 0) + F(0, -1)) / DY / DY) * m9)
-#define DXY(F)                                                                              \
-    (wall ? (T)0                                                                            \
-          : ((((F(1, 1) - F(1, -1)) / (T)2 / DY) - ((F(-1, 1) - F(-1, -1)) / (T)2 / DY)) / (T)2 / \
-             DX) * m9)
+    // FP64: the reference's divisions; mixed: reciprocal constants
+    constexpr bool EXACT = sizeof(T) == sizeof(double);
+    const T rdx2 = (T)(g.rdx * g.rdx), rdy2 = (T)(g.rdy * g.rdy), rdxy4 = (T)(0.25 * g.rdx * g.rdy);
+#define DXX(F) (EXACT ? (((F(1, 0) - (T)2 * F(0, 0) + F(-1, 0)) / DX / DX) * m9) \
+                      : ((F(1, 0) - (T)2 * F(0, 0) + F(-1, 0)) * rdx2 * m9))
+#define DYY(F) (EXACT ? (((F(0, 1) - (T)2 * F(0, 0) + F(0, -1)) / DY / DY) * m9) \
+                      : ((F(0, 1) - (T)2 * F(0, 0) + F(0, -1)) * rdy2 * m9))
+#define DXY(F)                                                                                      \
+    (wall ? (T)0                                                                                    \
+          : (EXACT ? ((((F(1, 1) - F(1, -1)) / (T)2 / DY) - ((F(-1, 1) - F(-1, -1)) / (T)2 / DY)) / \
+                      (T)2 / DX) * m9                                                               \
+                   : (((F(1, 1) - F(1, -1)) - (F(-1, 1) - F(-1, -1))) * rdxy4 * m9)))
     const T Uxx = DXX(LU), Vyy = DYY(LV), Uxy = DXY(LU), Vxy = DXY(LV);
     const T DUxx = DXX(LDU), DVyy = DYY(LDV), DUxy = DXY(LDU), DVxy = DXY(LDV);
 #undef LU
@@ -146,8 +156,10 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
     // (bc.F:395-398); without Gamma2 the ghosts keep their old values
     const bool exch = g.gamma2 > 0.0;
     if (exch || (g.show_breaking && !gx && !gy)) {
-        const T ex = (f.Eta[IDX(si + 1, sj)] - f.Eta[IDX(si - 1, sj)]) / DX / (T)2 * m9;
-        const T ey = (f.Eta[IDX(si, sj + 1)] - f.Eta[IDX(si, sj - 1)]) / DY / (T)2 * m9;
+        const T dex = f.Eta[IDX(si + 1, sj)] - f.Eta[IDX(si - 1, sj)];
+        const T dey = f.Eta[IDX(si, sj + 1)] - f.Eta[IDX(si, sj - 1)];
+        const T ex = EXACT ? dex / DX / (T)2 * m9 : dex * (T)(0.5 * g.rdx) * m9;
+        const T ey = EXACT ? dey / DY / (T)2 * m9 : dey * (T)(0.5 * g.rdy) * m9;
         if (!stale) {
             if (exch && g.periodic && gx && !gy) {
                 // the periodic copy (bc.F:735-740) runs before the x mirror:
@@ -212,6 +224,9 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
     if (!(g.gamma2 > 0.0)) return;
 
     const T DT = (T)f.dsc[S_DT];
+    const T rDT = (T)(1.0 / f.dsc[S_DT]);
+    const T hdx = (T)(0.5 * g.rdx), hdy = (T)(0.5 * g.rdy);
+    const T rdx2 = (T)(g.rdx * g.rdx), rdy2 = (T)(g.rdy * g.rdy), rdxy4 = (T)(0.25 * g.rdx * g.rdy);
     const bool wall = (i == g.ib) || (i == g.ie) || (j == g.jb) || (j == g.je);
 #define AT(F, a_, b_) f.F[IDX(i + (a_), j + (b_))]
     const T UxxVxy = a, UxyVyy = c, HUxxHVxy = b, HUxyHVyy = e;
@@ -241,30 +256,40 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
         HUxyHVyy_y = (AT(E, 0, 1) - AT(E, 0, -1)) * hy;
     }
     const T rh = D;
-    const T rhx = (AT(Depth, 1, 0) - AT(Depth, -1, 0)) / two / DX;
-    const T rhy = (AT(Depth, 0, 1) - AT(Depth, 0, -1)) / two / DY;
+    const T rhx = EXACT ? (AT(Depth, 1, 0) - AT(Depth, -1, 0)) / two / DX : (AT(Depth, 1, 0) - AT(Depth, -1, 0)) * hdx;
+    const T rhy = EXACT ? (AT(Depth, 0, 1) - AT(Depth, 0, -1)) / two / DY : (AT(Depth, 0, 1) - AT(Depth, 0, -1)) * hdy;
     const T ETAx = f.ETAx[id], ETAy = f.ETAy[id], ETAT = f.ETAT[id];
     // first derivatives of U, V, DU, DV (derivatives.F:123-162)
-    const T Ux = (AT(U, 1, 0) - AT(U, -1, 0)) / DX / two * m9;
-    const T Vx = (AT(V, 1, 0) - AT(V, -1, 0)) / DX / two * m9;
-    const T Uy = (AT(U, 0, 1) - AT(U, 0, -1)) / DY / two * m9;
-    const T Vy = (AT(V, 0, 1) - AT(V, 0, -1)) / DY / two * m9;
+#define FD1X(F) (EXACT ? ((F(1, 0) - F(-1, 0)) / DX / two) * m9 : ((F(1, 0) - F(-1, 0)) * hdx) * m9)
+#define FD1Y(F) (EXACT ? ((F(0, 1) - F(0, -1)) / DY / two) * m9 : ((F(0, 1) - F(0, -1)) * hdy) * m9)
+#define LU_(a_, b_) AT(U, a_, b_)
+#define LV_(a_, b_) AT(V, a_, b_)
+    const T Ux = FD1X(LU_);
+    const T Vx = FD1X(LV_);
+    const T Uy = FD1Y(LU_);
+    const T Vy = FD1Y(LV_);
+#undef LU_
+#undef LV_
 #define DUP(a_, b_) (tmax(AT(Depth, a_, b_), mdf) * AT(U, a_, b_))
 #define DVP(a_, b_) (tmax(AT(Depth, a_, b_), mdf) * AT(V, a_, b_))
-    const T DUx = (DUP(1, 0) - DUP(-1, 0)) / DX / two * m9;
-    const T DVy = (DVP(0, 1) - DVP(0, -1)) / DY / two * m9;
+    const T DUx = FD1X(DUP);
+    const T DVy = FD1Y(DVP);
     // time derivatives Ut=(U-U0)/DT (dispersion.F:133-141) and their
     // derivatives; the cross derivatives are zero on the wall rows
-#define UT(a_, b_) ((AT(U, a_, b_) - AT(U0, a_, b_)) / DT)
-#define VT(a_, b_) ((AT(V, a_, b_) - AT(V0, a_, b_)) / DT)
+#define UT(a_, b_) (EXACT ? ((AT(U, a_, b_) - AT(U0, a_, b_)) / DT) : ((AT(U, a_, b_) - AT(U0, a_, b_)) * rDT))
+#define VT(a_, b_) (EXACT ? ((AT(V, a_, b_) - AT(V0, a_, b_)) / DT) : ((AT(V, a_, b_) - AT(V0, a_, b_)) * rDT))
 #define DUT(a_, b_) (tmax(AT(Depth, a_, b_), mdf) * UT(a_, b_))
 #define DVT(a_, b_) (tmax(AT(Depth, a_, b_), mdf) * VT(a_, b_))
-#define D1X(F) (((F(1, 0) - F(-1, 0)) / DX / two) * m9)
-#define D1Y(F) (((F(0, 1) - F(0, -1)) / DY / two) * m9)
-#define D2X(F) (((F(1, 0) - two * F(0, 0) + F(-1, 0)) / DX / DX) * m9)
-#define D2Y(F) (((F(0, 1) - two * F(0, 0) + F(0, -1)) / DY / DY) * m9)
-#define D2XY(F) \
-    (wall ? (T)0 : ((((F(1, 1) - F(1, -1)) / two / DY) - ((F(-1, 1) - F(-1, -1)) / two / DY)) / two / DX) * m9)
+#define D1X(F) FD1X(F)
+#define D1Y(F) FD1Y(F)
+#define D2X(F) (EXACT ? (((F(1, 0) - two * F(0, 0) + F(-1, 0)) / DX / DX) * m9) \
+                      : ((F(1, 0) - two * F(0, 0) + F(-1, 0)) * rdx2 * m9))
+#define D2Y(F) (EXACT ? (((F(0, 1) - two * F(0, 0) + F(0, -1)) / DY / DY) * m9) \
+                      : ((F(0, 1) - two * F(0, 0) + F(0, -1)) * rdy2 * m9))
+#define D2XY(F)                                                                                          \
+    (wall ? (T)0                                                                                         \
+          : (EXACT ? ((((F(1, 1) - F(1, -1)) / two / DY) - ((F(-1, 1) - F(-1, -1)) / two / DY)) / two / DX) * m9 \
+                   : (((F(1, 1) - F(1, -1)) - (F(-1, 1) - F(-1, -1))) * rdxy4 * m9)))
     const T Utx = D1X(UT), Vty = D1Y(VT);
     const T Utxx = D2X(UT), Vtyy = D2Y(VT);
     const T Utxy = D2XY(UT), Vtxy = D2XY(VT);
@@ -282,6 +307,8 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
 #undef DVT
 #undef DUP
 #undef DVP
+#undef FD1X
+#undef FD1Y
     const T Uc = f.U[id], Vc = f.V[id];
 #undef AT
     T U1pp = -reta * B2 * ETAx * B2 * (Utx + Vty) - half * reta * reta * B2 * B2 * (Utxx + Vtxy) -
@@ -360,19 +387,6 @@ template <typename T> __device__ __forceinline__ T vl_phi(T rat) {
     if (fabs_((T)1 + rat) > (T)SMALL) van = (rat + fabs_(rat)) / ((T)1 + rat);
     return van;
 }
-// face values of one field at face p: v[0..5] = Vin(p-3..p+2)
-template <typename T>
-__device__ __forceinline__ void ho_face(const T *v, const int *m, T &L, T &R) {
-    const T d0 = ho_din(v + 0, m + 0), d1 = ho_din(v + 1, m + 1), d2 = ho_din(v + 2, m + 2);
-    T t1 = vl_guard(d0), t2 = vl_guard(d1);
-    T van1 = vl_phi(t2 / t1), van2 = vl_phi(t1 / t2);
-    L = v[2] + ((T)1 / (T)6) * (van1 * t1 + (T)2 * van2 * t2);
-    t1 = vl_guard(d1);
-    t2 = vl_guard(d2);
-    van1 = vl_phi(t2 / t1);
-    van2 = vl_phi(t1 / t2);
-    R = v[3] - ((T)1 / (T)6) * ((T)2 * van1 * t1 + van2 * t2);
-}
 template <typename T> __device__ __forceinline__ T hll(T SL, T SR, T FL, T FR, T UL, T UR) {
     if (SL >= (T)0) return FL;
     if (SR <= (T)0) return FR;
@@ -384,50 +398,96 @@ template <typename T> __device__ __forceinline__ T press(T Xi, T Deps, T g3) {
     return (T)0.5 * (T)GRAV * (Xi * Xi * g3 + (T)2 * Xi * Deps);
 }
 
-// One face of direction DIR (0: x-faces, 1: y-faces).  Normal velocity is
-// U for x and V for y; the tangential one the other.
+// Limited face values of one field from Din(p-1), Din(p), Din(p+1) and the
+// cells p-1, p.  FP64 evaluates the reference's van Leer expressions
+// (fluxes.F:1602-1630); the mixed path uses the equal closed form
+// VAN1*TMP1 = VAN2*TMP2 = 2*TMP1*TMP2/(TMP1+TMP2) for TMP1*TMP2 > 0, else 0.
+template <typename T>
+__device__ __forceinline__ void ho_lr(T vm1, T v0, T d0, T d1, T d2, T &L, T &R) {
+    if constexpr (sizeof(T) == sizeof(double)) {
+        T t1 = vl_guard(d0), t2 = vl_guard(d1);
+        T van1 = vl_phi(t2 / t1), van2 = vl_phi(t1 / t2);
+        L = vm1 + ((T)1 / (T)6) * (van1 * t1 + (T)2 * van2 * t2);
+        t1 = vl_guard(d1);
+        t2 = vl_guard(d2);
+        van1 = vl_phi(t2 / t1);
+        van2 = vl_phi(t1 / t2);
+        R = v0 - ((T)1 / (T)6) * ((T)2 * van1 * t1 + van2 * t2);
+    } else {
+        T t1 = vl_guard(d0), t2 = vl_guard(d1), t3 = vl_guard(d2);
+        const T hl = (t1 * t2 > (T)0) ? (T)2 * t1 * t2 / (t1 + t2) : (T)0;
+        const T hr = (t2 * t3 > (T)0) ? (T)2 * t2 * t3 / (t2 + t3) : (T)0;
+        L = vm1 + (T)0.5 * hl;
+        R = v0 - (T)0.5 * hr;
+    }
+}
+
+// Faces of direction DIR (0: x-faces, 1: y-faces) on a 32 x 8 tile.  Din of
+// the seven reconstructed fields is computed once per cell position into
+// shared memory; each thread then finishes one face: face values, Zhou wave
+// speeds, HLL and the boundary/dry-face rules.  Normal velocity is U for x
+// and V for y.
 template <typename T, int DIR>
 __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (DIR == 0) {
-        if (i < g.ib || i > g.ie + 1 || j < g.jb || j > g.je) return;
-    } else {
-        if (i < g.ib || i > g.ie || j < g.jb || j > g.je + 1) return;
-    }
+    constexpr int BX = 32, BY = 8;
+    constexpr int NB = DIR == 0 ? BX : BY;        // faces per tile line
+    constexpr int NTL = DIR == 0 ? BY : BX;       // tile lines
+    constexpr int NP = DIR == 0 ? BX + 2 : BY + 3;  // Din positions per line (+1 pad for y)
+    __shared__ T din[7][NTL][NP];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i = g.ib + blockIdx.x * BX + tx;
+    const int j = g.jb + blockIdx.y * BY + ty;
+    const int own = DIR == 0 ? tx : ty;
+    const int line = DIR == 0 ? ty : tx;
+    const int lo = DIR == 0 ? g.ib : g.jb, hi = DIR == 0 ? g.ie : g.je;
+    const int base = (DIR == 0 ? g.ib + blockIdx.x * BX : g.jb + blockIdx.y * BY) - 1;
+    const bool line_ok = DIR == 0 ? (j <= g.je) : (i <= g.ie);
     const int di = DIR == 0 ? 1 : 0, dj = DIR == 0 ? 0 : 1;
-    const T g1 = (T)g.gamma1, g3 = (T)g.gamma3;
-    T vu[6], vv[6], vhu[6], vhv[6], ve[6], vu4[6], vv4[6];
-    int mk[6];
+    const T *src[7] = {f.U, f.V, f.HU, f.HV, f.Eta, f.U4, f.V4};
+    const int nvar = g.dispersion ? 7 : 5;
+    for (int k = own; k < NB + 2; k += NB) {
+        const int p = base + k;
+        if (line_ok && p >= lo - 1 && p <= hi + 2) {
+            const int ci = DIR == 0 ? p : i, cj = DIR == 0 ? j : p;
+            int m[4];
 #pragma unroll
-    for (int k = 0; k < 6; k++) {
-        const size_t q = IDX(i + (k - 3) * di, j + (k - 3) * dj);
-        vu[k] = f.U[q];
-        vv[k] = f.V[q];
-        vhu[k] = f.HU[q];
-        vhv[k] = f.HV[q];
-        ve[k] = f.Eta[q];
-        vu4[k] = f.U4[q];
-        vv4[k] = f.V4[q];
-        mk[k] = f.MASK[q];
+            for (int q = 0; q < 4; q++) m[q] = f.MASK[IDX(ci + (q - 2) * di, cj + (q - 2) * dj)];
+            for (int vv = 0; vv < nvar; vv++) {
+                T v[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) v[q] = src[vv][IDX(ci + (q - 2) * di, cj + (q - 2) * dj)];
+                din[vv][line][k] = ho_din(v, m);
+            }
+        }
     }
-    T UL, UR, VL, VR, HUL, HUR, HVL, HVR, EL, ER, U4L = 0, U4R = 0, V4L = 0, V4R = 0;
-    ho_face(vu, mk, UL, UR);
-    ho_face(vv, mk, VL, VR);
-    ho_face(vhu, mk, HUL, HUR);
-    ho_face(vhv, mk, HVL, HVR);
-    ho_face(ve, mk, EL, ER);
-    if (g.dispersion) {
-        ho_face(vu4, mk, U4L, U4R);
-        ho_face(vv4, mk, V4L, V4R);
+    __syncthreads();
+    if (DIR == 0) {
+        if (i > g.ie + 1 || j > g.je) return;
+    } else {
+        if (i > g.ie || j > g.je + 1) return;
     }
+    const T g1 = (T)g.gamma1, g3 = (T)g.gamma3;
     const size_t fid = IDX(i, j);
+    const size_t cm = DIR == 0 ? IDX(i - 1, j) : IDX(i, j - 1);  // cell pos-1 (cell pos is fid)
+    const int kf = own + 1;
+    T Lv[7], Rv[7];
+    for (int vv = 0; vv < 7; vv++) {
+        if (vv >= nvar) {
+            Lv[vv] = (T)0;
+            Rv[vv] = (T)0;
+            continue;
+        }
+        ho_lr(src[vv][cm], src[vv][fid], din[vv][line][kf - 1], din[vv][line][kf], din[vv][line][kf + 1], Lv[vv],
+              Rv[vv]);
+    }
+    const T UL = Lv[0], UR = Rv[0], VL = Lv[1], VR = Rv[1], HUL = Lv[2], HUR = Rv[2];
+    const T HVL = Lv[3], HVR = Rv[3], EL = Lv[4], ER = Rv[4];
+    const T U4L = Lv[5], U4R = Rv[5], V4L = Lv[6], V4R = Rv[6];
     const T Dd = DIR == 0 ? f.Depthx[fid] : f.Depthy[fid];
     const T HL = EL + Dd, HR = ER + Dd;
     // MASK9u(Mloc1,:) = MASK9(Mloc,:) (fluxes.F:1333); the faces computed
     // here never reach that column
     const T m9 = (T)f.MASK9[fid];
-    // normal (n) and tangential (t) components
     const T nL = DIR == 0 ? UL : VL, nR = DIR == 0 ? UR : VR;
     const T tL = DIR == 0 ? VL : UL, tR = DIR == 0 ? VR : UR;
     const T n4L = DIR == 0 ? U4L : V4L, n4R = DIR == 0 ? U4R : V4R;
@@ -458,7 +518,6 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
     T Nm = hll(SL, SR, NL, NR, qnL, qnR);
     T Tm = hll(SL, SR, TL, TR, qtL, qtR);
     // BOUNDARY_CONDITION: walls, then the dry-cell loop (last write wins)
-    const int lo = DIR == 0 ? g.ib : g.jb, hi = DIR == 0 ? g.ie : g.je;
     const int pos = DIR == 0 ? i : j;
     const bool wall_on = DIR == 0 || !g.periodic;
     if (wall_on && pos == lo) {
@@ -471,7 +530,7 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
         Nm = press(EL, Dd, g3);
         Tm = (T)0;
     }
-    const int mL = mk[2], mR = mk[3];  // cells pos-1 and pos
+    const int mL = f.MASK[cm], mR = f.MASK[fid];  // cells pos-1 and pos
     if (mL < 1) {
         Pm = (T)0;
         Nm = (pos - 1 != hi) ? press(ER, Dd, g3) * (T)mR : (T)0;
@@ -523,7 +582,12 @@ __device__ __forceinline__ T wavemaker_mass(const Grid &g, const Fields<T> &f, i
 template <typename T>
 __device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, int i, int j, T wm, T &SX,
                                              T &SY) {
+    constexpr bool EXACT = sizeof(T) == sizeof(double);
     const T DX = (T)g.DX, DY = (T)g.DY, mdf = (T)g.min_depth_frc;
+    const T rdx = (T)g.rdx, rdy = (T)g.rdy;
+    // x/DX: the reference's division in FP64, a reciprocal in the mixed path
+#define OX(x) (EXACT ? (x) / DX : (x) * rdx)
+#define OY(x) (EXACT ? (x) / DY : (x) * rdy)
     const T g1 = (T)g.gamma1, g2 = (T)g.gamma2;
     const size_t id = IDX(i, j);
     const size_t ie_ = IDX(i + 1, j), iw = IDX(i - 1, j), in_ = IDX(i, j + 1), is = IDX(i, j - 1);
@@ -534,19 +598,19 @@ __device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, 
     const T Hm = tmax(f.H[id], mdf);
     const T Eta = f.Eta[id];
     const T U4 = f.U4[id], V4 = f.V4[id];
-    const T dPQ = (f.P[ie_] - f.P[id]) / DX + (f.Q[in_] - f.Q[id]) / DY;
+    const T dPQ = OX(f.P[ie_] - f.P[id]) + OY(f.Q[in_] - f.Q[id]);
     const T FrcInsX = -f.Cd[id] * U * spd;
-    T sx = (T)GRAV * (Eta) / DX * (f.Depthx[ie_] - f.Depthx[id]) * mk + FrcInsX +
+    T sx = OX((T)GRAV * (Eta)) * (f.Depthx[ie_] - f.Depthx[id]) * mk + FrcInsX +
            g1 * m9 * Hm *
-               (U * (T)0.5 * (f.U4[ie_] - f.U4[iw]) / DX + V * (T)0.5 * (f.U4[in_] - f.U4[is]) / DY +
-                U4 * (T)0.5 * (f.U[ie_] - f.U[iw]) / DX + V4 * (T)0.5 * (f.U[in_] - f.U[is]) / DY -
+               (OX(U * (T)0.5 * (f.U4[ie_] - f.U4[iw])) + OY(V * (T)0.5 * (f.U4[in_] - f.U4[is])) +
+                OX(U4 * (T)0.5 * (f.U[ie_] - f.U[iw])) + OY(V4 * (T)0.5 * (f.U[in_] - f.U[is])) -
                 g2 * m9 * f.Udisp[id]) +
            g1 * m9 * dPQ * (U4 - f.U1p[id]) + wm * U;
     const T FrcInsY = -f.Cd[id] * V * spd;
-    T sy = (T)GRAV * (Eta) / DY * (f.Depthy[in_] - f.Depthy[id]) * mk + FrcInsY +
+    T sy = OY((T)GRAV * (Eta)) * (f.Depthy[in_] - f.Depthy[id]) * mk + FrcInsY +
            g1 * m9 * Hm *
-               (U * (T)0.5 * (f.V4[ie_] - f.V4[iw]) / DX + V * (T)0.5 * (f.V4[in_] - f.V4[is]) / DY +
-                U4 * (T)0.5 * (f.V[ie_] - f.V[iw]) / DX + V4 * (T)0.5 * (f.V[in_] - f.V[is]) / DY -
+               (OX(U * (T)0.5 * (f.V4[ie_] - f.V4[iw])) + OY(V * (T)0.5 * (f.V4[in_] - f.V4[is])) +
+                OX(U4 * (T)0.5 * (f.V[ie_] - f.V[iw])) + OY(V4 * (T)0.5 * (f.V[in_] - f.V[is])) -
                 g2 * m9 * f.Vdisp[id]) +
            g1 * m9 * dPQ * (V4 - f.V1p[id]) + wm * V;
     if (g.friction_sponge) {
@@ -559,13 +623,24 @@ __device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, 
         const T nxp = (T)((float)f.nu[ie_] + nc), nxm = (T)((float)f.nu[iw] + nc);
         const T nyp = (T)((float)f.nu[in_] + nc), nym = (T)((float)f.nu[is] + nc);
         const T HUc = f.HU[id], HVc = f.HV[id];
-        const T bx = (T)0.5 / DX * (nxp * (T)1 / DX * (f.HU[ie_] - HUc) - nxm * (T)1 / DX * (HUc - f.HU[iw])) +
-                     (T)0.5 / DY * (nyp * (T)1 / DY * (f.HU[in_] - HUc) - nym * (T)1 / DY * (HUc - f.HU[is]));
+        T bx, by;
+        if constexpr (EXACT) {
+            bx = (T)0.5 / DX * (nxp * (T)1 / DX * (f.HU[ie_] - HUc) - nxm * (T)1 / DX * (HUc - f.HU[iw])) +
+                 (T)0.5 / DY * (nyp * (T)1 / DY * (f.HU[in_] - HUc) - nym * (T)1 / DY * (HUc - f.HU[is]));
+            by = (T)0.5 / DX * (nxp * (T)1 / DX * (f.HV[ie_] - HVc) - nxm * (T)1 / DX * (HVc - f.HV[iw])) +
+                 (T)0.5 / DY * (nyp * (T)1 / DY * (f.HV[in_] - HVc) - nym * (T)1 / DY * (HVc - f.HV[is]));
+        } else {
+            const T cx = (T)(0.5 * g.rdx * g.rdx), cy = (T)(0.5 * g.rdy * g.rdy);
+            bx = cx * (nxp * (f.HU[ie_] - HUc) - nxm * (HUc - f.HU[iw])) +
+                 cy * (nyp * (f.HU[in_] - HUc) - nym * (HUc - f.HU[is]));
+            by = cx * (nxp * (f.HV[ie_] - HVc) - nxm * (HVc - f.HV[iw])) +
+                 cy * (nyp * (f.HV[in_] - HVc) - nym * (HVc - f.HV[is]));
+        }
         sx = sx + bx;
-        const T by = (T)0.5 / DX * (nxp * (T)1 / DX * (f.HV[ie_] - HVc) - nxm * (T)1 / DX * (HVc - f.HV[iw])) +
-                     (T)0.5 / DY * (nyp * (T)1 / DY * (f.HV[in_] - HVc) - nym * (T)1 / DY * (HVc - f.HV[is]));
         sy = sy + by;
     }
+#undef OX
+#undef OY
     SX = sx;
     SY = sy;
 }
@@ -608,7 +683,9 @@ __global__ void __launch_bounds__(256) k_update(Grid g, Fields<T> f, T al, T be)
     source_terms(g, f, i, j, wm, SX, SY);
 
     const size_t ie_ = IDX(i + 1, j), in_ = IDX(i, j + 1);
-    T R1 = -(T)1 / DX * (f.P[ie_] * (T)1 + f.P[id] * (T)-1) - (T)1 / DY * (f.Q[in_] * (T)1 + f.Q[id] * (T)-1);
+    constexpr bool EXACT = sizeof(T) == sizeof(double);
+    const T cdx = EXACT ? (T)1 / DX : (T)g.rdx, cdy = EXACT ? (T)1 / DY : (T)g.rdy;
+    T R1 = -cdx * (f.P[ie_] * (T)1 + f.P[id] * (T)-1) - cdy * (f.Q[in_] * (T)1 + f.Q[id] * (T)-1);
     if (g.wavemaker != FW_WK_NONE) {
         const T xmk = (T)(i - g.ib) * DX, ymk = (T)(j - g.jb) * DY;
         if (fabs_(xmk - (T)g.xc_wk) < (T)g.width_wk && fabs_(ymk - (T)g.yc_wk) < (T)g.ywidth_wk / (T)2)
@@ -619,11 +696,9 @@ __global__ void __launch_bounds__(256) k_update(Grid g, Fields<T> f, T al, T be)
         if (eta < (T)g.trough) eta = (T)g.trough;
         if (eta > (T)g.crest) eta = (T)g.crest;
     }
-    const T R2 = -(T)1 / DX * (f.Fx[ie_] * (T)1 + f.Fx[id] * (T)-1) -
-                 (T)1 / DY * (f.Fy[in_] * (T)1 + f.Fy[id] * (T)-1) + SX;
+    const T R2 = -cdx * (f.Fx[ie_] * (T)1 + f.Fx[id] * (T)-1) - cdy * (f.Fy[in_] * (T)1 + f.Fy[id] * (T)-1) + SX;
     const T ubar = al * f.Ubar0[id] + be * (f.Ubar[id] + DT * R2);
-    const T R3 = -(T)1 / DX * (f.Gx[ie_] * (T)1 + f.Gx[id] * (T)-1) -
-                 (T)1 / DY * (f.Gy[in_] * (T)1 + f.Gy[id] * (T)-1) + SY;
+    const T R3 = -cdx * (f.Gx[ie_] * (T)1 + f.Gx[id] * (T)-1) - cdy * (f.Gy[in_] * (T)1 + f.Gy[id] * (T)-1) + SY;
     const T vbar = al * f.Vbar0[id] + be * (f.Vbar[id] + DT * R3);
     f.Eta[id] = eta;
     f.Ubar[id] = ubar;
@@ -1040,6 +1115,298 @@ __global__ void __launch_bounds__(128) k_thomas(Grid g, Fields<T> f, LinePart lp
     }
 }
 
+// Mixed path: the tridiagonal matrices depend on Depth and MASK9 only, so
+// their partitioned factorisation is computed when MASK9 has changed (never
+// again once viscosity breaking has set MASK9 = 1 on the ring) and each
+// stage runs only the substitutions for its right-hand side.
+struct FacLine {
+    double *lo, *invden, *cpr, *cs, *ae, *x2, *tail;  // tail: c_end, a_beg, den_beta
+};
+__device__ __forceinline__ FacLine fac_line(double *base, const LinePart &lp, int l) {
+    const int n = 2 * lp.P;
+    double *b = base + (size_t)l * (size_t)(4 * n + 2 * lp.P + 3);
+    FacLine f;
+    f.lo = b;
+    f.invden = b + n;
+    f.cpr = b + 2 * n;
+    f.cs = b + 3 * n;
+    f.ae = b + 3 * n + lp.P;
+    f.x2 = b + 3 * n + 2 * lp.P;
+    f.tail = b + 4 * n + 2 * lp.P;
+    return f;
+}
+
+// coefficients a, c and 1/tmp2 of one row (no right-hand side)
+template <typename T, int DIR>
+__device__ __forceinline__ void tri_ac(const Grid &g, const Fields<T> &f, int i, int j, double &a, double &c,
+                                       double &it) {
+    const double mdf = g.min_depth_frc;
+    const size_t id = IDX(i, j);
+    const double dep = tmax((double)f.Depth[id], mdf);
+    const double depl = tmax((double)f.Depth[DIR == 0 ? IDX(i - 1, j) : IDX(i, j - 1)], mdf);
+    const double depr = tmax((double)f.Depth[DIR == 0 ? IDX(i + 1, j) : IDX(i, j + 1)], mdf);
+    const double gm = g.gamma1 * (double)f.MASK9[id];
+    const double tmp1 = gm * dep * (g.cA[DIR] * dep + g.cB[DIR] * depl);
+    const double tmp2 = 1.0 + gm * g.cC[DIR] * dep * dep;
+    const double tmp3 = gm * dep * (g.cA[DIR] * dep + g.cB[DIR] * depr);
+    it = 1.0 / tmp2;
+    a = tmp1 * it;
+    c = tmp3 * it;
+}
+
+template <typename T, int DIR, bool PER>
+__device__ __forceinline__ void tri_ac_row(const Grid &g, const Fields<T> &f, const LinePart &lp, int l, int k,
+                                           double &a, double &c, double &it) {
+    int i, j;
+    line_cell<DIR>(g, l, k, i, j);
+    tri_ac<T, DIR>(g, f, i, j, a, c, it);
+    if (PER && (k == 0 || k == lp.L - 1)) {
+        double a2, c2, it2;
+        int i2, j2;
+        line_cell<DIR>(g, l, k == 0 ? lp.L - 1 : 0, i2, j2);
+        tri_ac<T, DIR>(g, f, i2, j2, a2, c2, it2);
+        if (k == 0) c = c / (1 + c2);        // c_end
+        else a = a / (1 + a2);                // a_beg
+    }
+}
+
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp) {
+    if (!*f.m9_dirty) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= lp.nlines * lp.P) return;
+    int l, ch;
+    chunk_of<DIR>(lp, t, l, ch);
+    const int s = ch * lp.m;
+    const int e = (ch == lp.P - 1) ? lp.L - 1 : s + lp.m - 1;
+    double *it_ = f.fac_it[DIR], *r_ = f.fac_r[DIR], *lr_ = f.fac_lr[DIR], *cp_ = f.fac_cp[DIR];
+    double *p_ = f.fac_p[DIR], *q_ = f.fac_q[DIR];
+    double as, cs, its, ae, ce, ite;
+    tri_ac_row<T, DIR, PER>(g, f, lp, l, s, as, cs, its);
+    tri_ac_row<T, DIR, PER>(g, f, lp, l, e, ae, ce, ite);
+    int i, j;
+    line_cell<DIR>(g, l, s, i, j);
+    it_[IDX(i, j)] = its;
+    line_cell<DIR>(g, l, e, i, j);
+    it_[IDX(i, j)] = ite;
+    if (s == 0) as = 0.0;
+    if (e == lp.L - 1) ce = 0.0;
+    double lo_s, di_s, up_s, lo_e, di_e, up_e;
+    if (e - s >= 2) {
+        double cp = 0.0, pp = 0.0, qp = 0.0;
+        for (int k = s + 1; k <= e - 1; k++) {
+            double a, c, it;
+            tri_ac_row<T, DIR, PER>(g, f, lp, l, k, a, c, it);
+            const double lower = (k > s + 1) ? a : 0.0;
+            const double r = 1.0 / (1.0 - lower * cp);
+            const double upper = (k < e - 1) ? c : 0.0;
+            cp = upper * r;
+            pp = ((k == s + 1 ? a : 0.0) - lower * pp) * r;
+            qp = ((k == e - 1 ? c : 0.0) - lower * qp) * r;
+            line_cell<DIR>(g, l, k, i, j);
+            const size_t q = IDX(i, j);
+            it_[q] = it;
+            r_[q] = r;
+            lr_[q] = lower * r;
+            cp_[q] = cp;
+            p_[q] = pp;
+            q_[q] = qp;
+        }
+        double pn = 0.0, qn = 0.0, p1 = 0.0, q1 = 0.0, pl = 0.0, ql = 0.0;
+        for (int k = e - 1; k >= s + 1; k--) {
+            line_cell<DIR>(g, l, k, i, j);
+            const size_t q = IDX(i, j);
+            const double cpk = cp_[q];
+            const double pk = p_[q] - cpk * pn, qk = q_[q] - cpk * qn;
+            p_[q] = pk;
+            q_[q] = qk;
+            pn = pk;
+            qn = qk;
+            if (k == e - 1) {
+                pl = pk;
+                ql = qk;
+            }
+            if (k == s + 1) {
+                p1 = pk;
+                q1 = qk;
+            }
+        }
+        lo_s = as;
+        di_s = 1.0 - cs * p1;
+        up_s = -cs * q1;
+        lo_e = -ae * pl;
+        di_e = 1.0 - ae * ql;
+        up_e = ce;
+    } else {
+        lo_s = as;
+        di_s = 1.0;
+        up_s = cs;
+        lo_e = ae;
+        di_e = 1.0;
+        up_e = ce;
+    }
+    // reduced rows go to the reduced-system scratch; k_fac_b factors them
+    double *red = f.red + ((size_t)l * 2 * lp.P + 2 * ch) * 6;
+    red[0] = lo_s;
+    red[1] = di_s;
+    red[2] = up_s;
+    red[6] = lo_e;
+    red[7] = di_e;
+    red[8] = up_e;
+    FacLine fl = fac_line(f.fac_red[DIR], lp, l);
+    fl.cs[ch] = (e - s >= 2) ? cs : 0.0;
+    fl.ae[ch] = (e - s >= 2) ? ae : 0.0;
+}
+
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(128) k_fac_b(Grid g, Fields<T> f, LinePart lp) {
+    if (!*f.m9_dirty) return;
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= lp.nlines) return;
+    const int n = 2 * lp.P;
+    const double *red = f.red + (size_t)l * n * 6;
+    FacLine fl = fac_line(f.fac_red[DIR], lp, l);
+    double cpr = 0.0;
+    for (int k = 0; k < n; k++) {
+        const double lo = (k > 0) ? red[k * 6 + 0] : 0.0;
+        const double id = 1.0 / (red[k * 6 + 1] - lo * cpr);
+        cpr = (k < n - 1 ? red[k * 6 + 2] : 0.0) * id;
+        fl.lo[k] = lo;
+        fl.invden[k] = id;
+        fl.cpr[k] = cpr;
+    }
+    if (PER) {
+        // the second periodic solution (right-hand side e of TRIDy_periodic,
+        // tridiagnal.F:207-215) and the constant denominator of beta
+        double a, c, it;
+        int i, j;
+        line_cell<DIR>(g, l, 0, i, j);
+        tri_ac<T, DIR>(g, f, i, j, a, c, it);
+        const double a_beg = a;
+        line_cell<DIR>(g, l, lp.L - 1, i, j);
+        tri_ac<T, DIR>(g, f, i, j, a, c, it);
+        const double c_end = c;
+        double z = 0.0;
+        for (int k = 0; k < n; k++) {
+            const double rhs = k == 0 ? 1.0 / (1.0 + c_end) : (k == n - 1 ? -1.0 / (1.0 + a_beg) : 0.0);
+            z = (rhs - fl.lo[k] * z) * fl.invden[k];
+            fl.x2[k] = z;
+        }
+        double x = 0.0;
+        for (int k = n - 1; k >= 0; k--) {
+            x = fl.x2[k] - fl.cpr[k] * x;
+            fl.x2[k] = x;
+        }
+        fl.tail[0] = c_end;
+        fl.tail[1] = a_beg;
+        fl.tail[2] = 1.0 - (c_end * fl.x2[0] - a_beg * fl.x2[n - 1]);
+    }
+}
+
+static __global__ void k_fac_clear(int *dirty) { *dirty = 0; }
+
+// per stage: right-hand side, chunk forward/backward substitution
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(128) k_sol_a(Grid g, Fields<T> f, LinePart lp) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= lp.nlines * lp.P) return;
+    int l, ch;
+    chunk_of<DIR>(lp, t, l, ch);
+    const int s = ch * lp.m;
+    const int e = (ch == lp.P - 1) ? lp.L - 1 : s + lp.m - 1;
+    const double *rhs = DIR == 0 ? f.rhs_x : f.rhs_y;
+    const double *it_ = f.fac_it[DIR], *r_ = f.fac_r[DIR], *lr_ = f.fac_lr[DIR], *cp_ = f.fac_cp[DIR];
+    FacLine fl = fac_line(f.fac_red[DIR], lp, l);
+    double sc0 = 1.0, sc1 = 1.0;
+    if (PER) {
+        sc0 = 1.0 / (1.0 + fl.tail[0]);  // row 0: d / (1 + c_end)
+        sc1 = 1.0 / (1.0 + fl.tail[1]);  // row L-1: d / (1 + a_beg)
+    }
+    auto dval = [&](int k, size_t q) {
+        double d = rhs[q] * it_[q];
+        if (PER && k == 0) d *= sc0;
+        if (PER && k == lp.L - 1) d *= sc1;
+        return d;
+    };
+    int i, j;
+    line_cell<DIR>(g, l, s, i, j);
+    const double ds = dval(s, IDX(i, j));
+    line_cell<DIR>(g, l, e, i, j);
+    const double de = dval(e, IDX(i, j));
+    double rs = ds, re = de;
+    if (e - s >= 2) {
+        double yp = 0.0;
+        for (int k = s + 1; k <= e - 1; k++) {
+            line_cell<DIR>(g, l, k, i, j);
+            const size_t q = IDX(i, j);
+            yp = dval(k, q) * r_[q] - lr_[q] * yp;
+            f.ty[q] = yp;
+        }
+        double yn = 0.0, y1 = 0.0, yl = 0.0;
+        for (int k = e - 1; k >= s + 1; k--) {
+            line_cell<DIR>(g, l, k, i, j);
+            const size_t q = IDX(i, j);
+            const double yk = f.ty[q] - cp_[q] * yn;
+            f.ty[q] = yk;
+            yn = yk;
+            if (k == e - 1) yl = yk;
+            if (k == s + 1) y1 = yk;
+        }
+        rs = ds - fl.cs[ch] * y1;
+        re = de - fl.ae[ch] * yl;
+    }
+    double *red = f.red + ((size_t)l * 2 * lp.P + 2 * ch) * 6;
+    red[3] = rs;
+    red[9] = re;
+}
+
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(128) k_sol_b(Grid g, Fields<T> f, LinePart lp) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= lp.nlines) return;
+    const int n = 2 * lp.P;
+    double *red = f.red + (size_t)l * n * 6;
+    FacLine fl = fac_line(f.fac_red[DIR], lp, l);
+    double z = 0.0;
+    for (int k = 0; k < n; k++) {
+        z = (red[k * 6 + 3] - fl.lo[k] * z) * fl.invden[k];
+        red[k * 6 + 3] = z;
+    }
+    double x = 0.0;
+    for (int k = n - 1; k >= 0; k--) {
+        x = red[k * 6 + 3] - fl.cpr[k] * x;
+        red[k * 6 + 3] = x;
+    }
+    if (PER) {
+        const double beta = (fl.tail[0] * red[3] - fl.tail[1] * red[(size_t)(n - 1) * 6 + 3]) / fl.tail[2];
+        for (int k = 0; k < n; k++) red[k * 6 + 3] += beta * fl.x2[k];
+    }
+}
+
+template <typename T, int DIR>
+__global__ void __launch_bounds__(128) k_sol_c(Grid g, Fields<T> f, LinePart lp) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= lp.nlines * lp.P) return;
+    int l, ch;
+    chunk_of<DIR>(lp, t, l, ch);
+    const int s = ch * lp.m;
+    const int e = (ch == lp.P - 1) ? lp.L - 1 : s + lp.m - 1;
+    const double *red = f.red + ((size_t)l * 2 * lp.P + 2 * ch) * 6;
+    const double xs = red[3], xe = red[9];
+    const double *p_ = f.fac_p[DIR], *q_ = f.fac_q[DIR];
+    T *out = DIR == 0 ? f.U : f.V;
+    int i, j;
+    line_cell<DIR>(g, l, s, i, j);
+    out[IDX(i, j)] = (T)xs;
+    line_cell<DIR>(g, l, e, i, j);
+    out[IDX(i, j)] = (T)xe;
+    for (int k = s + 1; k <= e - 1; k++) {
+        line_cell<DIR>(g, l, k, i, j);
+        const size_t q = IDX(i, j);
+        out[q] = (T)(f.ty[q] - p_[q] * xs - q_[q] * xe);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // GET_Eta_U_V_HU_HV tail (etauv_solver.F:558-600): dry zeroing, HU/HV and
 // the Froude cap, with the MASK of the start of the stage.
@@ -1160,6 +1527,7 @@ __global__ void __launch_bounds__(256) k_mask(Grid g, Fields<T> f) {
             m9 = (uint8_t)p;
         }
     }
+    if (f.MASK9[id] != m9) *f.m9_dirty = 1;  // the tridiagonal matrices change
     f.MASK9[id] = m9;
 }
 
@@ -1655,9 +2023,9 @@ template <typename T> void launch_dispersion(fw_ctx *c) {
 
 template <typename T> void launch_fluxes(fw_ctx *c) {
     const Grid &g = c->g;
-    k_flux<T, 0><<<grid2(g.Mloc + 1, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    k_flux<T, 0><<<grid2(g.Mglob + 1, g.Nglob, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
     note(c);
-    k_flux<T, 1><<<grid2(g.Mloc, g.Nloc + 1, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    k_flux<T, 1><<<grid2(g.Mglob, g.Nglob + 1, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
     note(c);
 }
 
@@ -1675,6 +2043,15 @@ template <typename T, int DIR, bool PER> static void launch_tri(fw_ctx *c, const
         return;
     }
     const int nt = lp.nlines * lp.P;
+    if (c->factored) {
+        k_fac_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        k_fac_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        k_sol_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        k_sol_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        k_sol_c<T, DIR><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        note(c, 5);
+        return;
+    }
     k_tri_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
     note(c);
     k_tri_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
@@ -1694,6 +2071,10 @@ template <typename T> void launch_estimate_huv(fw_ctx *c, int istage) {
         launch_tri<T, 0, false>(c, c->px);
         if (g.periodic) launch_tri<T, 1, true>(c, c->py);
         else launch_tri<T, 1, false>(c, c->py);
+        if (sizeof(T) == sizeof(float) && c->factored) {
+            k_fac_clear<<<1, 1, 0, c->stream>>>(c->F<T>().m9_dirty);
+            note(c);
+        }
     }
     k_post<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
     note(c);
@@ -1792,8 +2173,8 @@ template <typename T> int launch_by_name(fw_ctx *c, const char *name) {
     auto is = [&](const char *n) { return std::strcmp(name, n) == 0; };
     if (is("disp_a")) k_disp_a<T><<<gc, B2D, 0, c->stream>>>(g, f);
     else if (is("disp_b")) k_disp_b<T><<<gc, B2D, 0, c->stream>>>(g, f);
-    else if (is("flux_x")) k_flux<T, 0><<<grid2(g.Mloc + 1, g.Nloc, B2D), B2D, 0, c->stream>>>(g, f);
-    else if (is("flux_y")) k_flux<T, 1><<<grid2(g.Mloc, g.Nloc + 1, B2D), B2D, 0, c->stream>>>(g, f);
+    else if (is("flux_x")) k_flux<T, 0><<<grid2(g.Mglob + 1, g.Nglob, B2D), B2D, 0, c->stream>>>(g, f);
+    else if (is("flux_y")) k_flux<T, 1><<<grid2(g.Mglob, g.Nglob + 1, B2D), B2D, 0, c->stream>>>(g, f);
     else if (is("update")) k_update<T><<<gc, B2D, 0, c->stream>>>(g, f, (T)0.75, (T)0.25);
     else if (is("tri_x")) { launch_tri<T, 0, false>(c, c->px); return 0; }
     else if (is("tri_y")) {
