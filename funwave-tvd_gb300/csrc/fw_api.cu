@@ -3,6 +3,7 @@
 // entry points and the CUDA-graph replay of whole steps.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -128,7 +129,9 @@ LinePart make_part(int L, int nlines) {
     LinePart lp;
     lp.L = L;
     lp.nlines = nlines;
-    lp.m = 16;
+    // chunks of at least 16 rows and at most 64 chunks per line, so that the
+    // sequential reduced solve per line stays short
+    lp.m = std::max(16, (L + 63) / 64);
     if (L < 2 * lp.m) {
         lp.m = L;
         lp.P = 1;

@@ -1367,15 +1367,42 @@ __global__ void __launch_bounds__(128) k_sol_b(Grid g, Fields<T> f, LinePart lp)
     const int n = 2 * lp.P;
     double *red = f.red + (size_t)l * n * 6;
     FacLine fl = fac_line(f.fac_red[DIR], lp, l);
+    // n = 2P is even; batches of up to 8 rows load before they compute
+    constexpr int B = 8;
     double z = 0.0;
-    for (int k = 0; k < n; k++) {
-        z = (red[k * 6 + 3] - fl.lo[k] * z) * fl.invden[k];
-        red[k * 6 + 3] = z;
+    for (int k0 = 0; k0 < n; k0 += B) {
+        double rb[B], lb[B], ib[B];
+        const int nb = min(B, n - k0);
+#pragma unroll
+        for (int u = 0; u < B; u++)
+            if (u < nb) {
+                rb[u] = red[(k0 + u) * 6 + 3];
+                lb[u] = fl.lo[k0 + u];
+                ib[u] = fl.invden[k0 + u];
+            }
+#pragma unroll
+        for (int u = 0; u < B; u++)
+            if (u < nb) {
+                z = (rb[u] - lb[u] * z) * ib[u];
+                red[(k0 + u) * 6 + 3] = z;
+            }
     }
     double x = 0.0;
-    for (int k = n - 1; k >= 0; k--) {
-        x = red[k * 6 + 3] - fl.cpr[k] * x;
-        red[k * 6 + 3] = x;
+    for (int k1 = n; k1 > 0; k1 -= B) {
+        double zb[B], cb[B];
+        const int nb = min(B, k1);
+#pragma unroll
+        for (int u = 0; u < B; u++)
+            if (u < nb) {
+                zb[u] = red[(k1 - 1 - u) * 6 + 3];
+                cb[u] = fl.cpr[k1 - 1 - u];
+            }
+#pragma unroll
+        for (int u = 0; u < B; u++)
+            if (u < nb) {
+                x = zb[u] - cb[u] * x;
+                red[(k1 - 1 - u) * 6 + 3] = x;
+            }
     }
     if (PER) {
         const double beta = (fl.tail[0] * red[3] - fl.tail[1] * red[(size_t)(n - 1) * 6 + 3]) / fl.tail[2];
