@@ -288,6 +288,8 @@ def main():
     ap.add_argument("--size", type=int, default=2048, help="grid edge (2048 for the benchmark)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-kernel-profile", action="store_true",
+                    help="skip the per-kernel timing (e.g. for an ncu launch list of the stepping only)")
     args = ap.parse_args()
     fw = __graft_entry__.load_package()
     params, depth, phases = fw.cases.shoal_jonswap(Mglob=args.size, Nglob=args.size, seed=2024)
@@ -325,15 +327,15 @@ def main():
                  "eta_rms_mixed_vs_fp64_m": rms, "mask_mismatch_cells": mask_mis,
                  "time_mixed_s": sm.scalar("TIME"), "time_fp64_s": s64.scalar("TIME"),
                  "status": r64["status"]}
-        prof64 = kernel_profile(s64, 8, cells, (params["Mglob"] + 1) * params["Nglob"],
-                                params["Mglob"] * (params["Nglob"] + 1), hbm)
+        prof64 = {} if args.no_kernel_profile else kernel_profile(
+            s64, 8, cells, (params["Mglob"] + 1) * params["Nglob"], params["Mglob"] * (params["Nglob"] + 1), hbm)
         res64["kernels"] = {k: round(v["ms"], 4) for k, v in prof64.items()}
         s64.close()
     e2e_steps = min(K, 10)
     e2e_dt, h2d, d2h = e2e_run(fw, sm, e2e_steps)
     # per-kernel timing last: some kernels update the state in place
-    prof = kernel_profile(sm, 4, cells, (params["Mglob"] + 1) * params["Nglob"],
-                          params["Mglob"] * (params["Nglob"] + 1), hbm)
+    prof = {} if args.no_kernel_profile else kernel_profile(
+        sm, 4, cells, (params["Mglob"] + 1) * params["Nglob"], params["Mglob"] * (params["Nglob"] + 1), hbm)
     dom = max(prof, key=lambda k: prof[k]["ms"]) if prof else None
     sm.close()
     if rank != 0:

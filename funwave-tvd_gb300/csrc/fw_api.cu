@@ -125,6 +125,45 @@ int put_named(fw_ctx *c, const char *name, const void *host) {
     return put_field<float>(c, r, host);
 }
 
+void fill_float_constants(Grid &g) {
+    g.f_DX = (float)g.DX;
+    g.f_DY = (float)g.DY;
+    g.f_rdx = (float)g.rdx;
+    g.f_rdy = (float)g.rdy;
+    g.f_hdx = (float)(0.5 * g.rdx);
+    g.f_hdy = (float)(0.5 * g.rdy);
+    g.f_rdx2 = (float)(g.rdx * g.rdx);
+    g.f_rdy2 = (float)(g.rdy * g.rdy);
+    g.f_rdxy4 = (float)(0.25 * g.rdx * g.rdy);
+    g.f_cx = (float)(0.5 * g.rdx * g.rdx);
+    g.f_cy = (float)(0.5 * g.rdy * g.rdy);
+    g.f_min_depth_frc = (float)g.min_depth_frc;
+    g.f_gamma1 = (float)g.gamma1;
+    g.f_gamma2 = (float)g.gamma2;
+    g.f_gamma3 = (float)g.gamma3;
+    g.f_Beta_1 = (float)g.Beta_1;
+    g.f_Beta_2 = (float)g.Beta_2;
+    g.f_b1 = (float)g.b1;
+    g.f_b2 = (float)g.b2;
+    g.f_hb1 = (float)(-0.5 * g.b1);
+    g.f_cbrk1 = (float)g.cbrk1;
+    g.f_cbrk2 = (float)g.cbrk2;
+    g.f_wavemaker_cbrk = (float)g.wavemaker_cbrk;
+    g.f_nu_bkg = (float)g.nu_bkg;
+    g.f_T_brk = (float)g.T_brk;
+    g.f_froude_cap = (float)g.froude_cap;
+    g.f_swe_eta_dep = (float)g.swe_eta_dep;
+    g.f_xc_wk = (float)g.xc_wk;
+    g.f_yc_wk = (float)g.yc_wk;
+    g.f_ywidth_wk = (float)g.ywidth_wk;
+    g.f_width_wk = (float)g.width_wk;
+    g.f_D_gen = (float)g.D_gen;
+    g.f_beta_gen = (float)g.beta_gen;
+    g.f_rlamda = (float)g.rlamda;
+    g.f_trough = (float)g.trough;
+    g.f_crest = (float)g.crest;
+}
+
 LinePart make_part(int L, int nlines) {
     LinePart lp;
     lp.L = L;
@@ -177,6 +216,7 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
     const size_t nred = std::max((size_t)c->px.nlines * 2 * c->px.P, (size_t)c->py.nlines * 2 * c->py.P);
     f.red = (double *)take(nred * 6 * sizeof(double));
     f.dsc = (double *)take(S_NSLOT * sizeof(double));
+    f.fsc = (float *)take(FS_NSLOT * sizeof(float));
     f.dtmin_bits = (unsigned long long *)take(sizeof(unsigned long long));
     f.etamax_bits = (unsigned long long *)take(sizeof(unsigned long long));
     f.ncand = (int *)take(sizeof(int));
@@ -184,6 +224,7 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
     const int nf = c->p.wavemaker == FW_WK_JON_2D ? (c->p.nfreq > 0 ? c->p.nfreq : 1) : 1;
     f.omega = (double *)take((size_t)nf * sizeof(double));
     f.wmcs = (double *)take((size_t)nf * 2 * sizeof(double));
+    f.wmcsf = (float *)take((size_t)nf * 2 * sizeof(float));
     f.Cm = f.Sm = nullptr;  // band tables are allocated by fw_init
     void *stg = take((size_t)(g.Mloc + 1) * (size_t)(g.Nloc + 1) * sizeof(double));
     if (assign) {
@@ -369,6 +410,7 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     }
     g.rdx = 1.0 / p->DX;
     g.rdy = 1.0 / p->DY;
+    fill_float_constants(g);
     c->px = make_part(p->Mglob, p->Nglob);
     c->py = make_part(p->Nglob, p->Mglob);
     c->ncand_cap = (p->Mglob + 2) * (p->Nglob + 2);
@@ -432,6 +474,7 @@ int fw_init(fw_ctx *c, const double *depth, const double *eta, const double *u, 
     g.beta_gen = hc.beta_gen;
     g.rlamda = hc.rlamda;
     c->EtaBlowVal = hc.EtaBlowVal;
+    fill_float_constants(g);
     if (hc.ilo <= hc.ihi && hc.jlo <= hc.jhi) {
         g.ilo = hc.ilo - 1;
         g.ihi = hc.ihi - 1;
@@ -540,8 +583,10 @@ int fw_set_scalar(fw_ctx *c, const char *name, double v) {
         return cuda_status(c, e);
     }
     if (!std::strcmp(name, "EtaBlowVal")) c->EtaBlowVal = v;
-    else if (!std::strcmp(name, "T_brk")) c->g.T_brk = v;
-    else return FW_ERR_BAD_PARAM;
+    else if (!std::strcmp(name, "T_brk")) {
+        c->g.T_brk = v;
+        fill_float_constants(c->g);
+    } else return FW_ERR_BAD_PARAM;
     c->graph_ready = 0;
     return FW_OK;
 }

@@ -37,7 +37,17 @@ struct Grid {
     // direction (b1/2/h^2, b2/h^2, (-b1-2*b2)/h^2) and 1/DX, 1/DY
     double cA[2], cB[2], cC[2];
     double rdx, rdy;
+    // float copies of the constants for the mixed path (no FP64 work per
+    // thread there): f_<name> = (float)<name>; f_hdx = 0.5/DX, f_rdx2 =
+    // 1/DX^2, f_rdxy4 = 0.25/(DX*DY), f_cx = 0.5/DX^2, f_hb1 = -0.5*b1
+    float f_DX, f_DY, f_rdx, f_rdy, f_hdx, f_hdy, f_rdx2, f_rdy2, f_rdxy4, f_cx, f_cy;
+    float f_min_depth_frc, f_gamma1, f_gamma2, f_gamma3, f_Beta_1, f_Beta_2, f_b1, f_b2, f_hb1;
+    float f_cbrk1, f_cbrk2, f_wavemaker_cbrk, f_nu_bkg, f_T_brk, f_froude_cap, f_swe_eta_dep;
+    float f_xc_wk, f_yc_wk, f_ywidth_wk, f_width_wk, f_D_gen, f_beta_gen, f_rlamda, f_trough, f_crest;
 };
+
+// float device scalars of the current step (mixed path)
+enum : int { FS_DT = 0, FS_RDT = 1, FS_WKAA = 2, FS_WKPH = 3, FS_NSLOT = 8 };
 
 // device scalar slots (double array)
 enum : int { S_TIME = 0, S_DT = 1, S_DTMIN = 2, S_ETAMAX = 3, S_NSLOT = 8 };
@@ -68,6 +78,8 @@ struct Fields {
     int *m9_dirty;                    // MASK9 changed since the last factorisation
     double *Cm, *Sm, *omega, *wmcs;   // JON_2D band tables and cos/sin(omega t)
     double *dsc;                      // device scalars (S_*)
+    float *fsc;                       // float device scalars (FS_*)
+    float *wmcsf;                     // float copy of wmcs
     int *cand, *ncand;                // breaking candidates
     unsigned long long *dtmin_bits;
     unsigned long long *etamax_bits;

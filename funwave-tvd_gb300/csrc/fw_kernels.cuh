@@ -54,6 +54,12 @@ __device__ __forceinline__ float ftanh(float x) { return tanhf(x); }
 __device__ __forceinline__ double fatan2(double y, double x) { return atan2(y, x); }
 __device__ __forceinline__ float fatan2(float y, float x) { return atan2f(y, x); }
 
+// a constant of the grid block in the kernel's precision: the double member
+// in FP64, its float copy f_<name> in the mixed path (no FP64 work there)
+#define GC(name) (sizeof(T) == sizeof(double) ? (T)g.name : (T)g.f_##name)
+// DT of the current step in the kernel's precision
+#define DTV (sizeof(T) == sizeof(double) ? (T)f.dsc[S_DT] : (T)f.fsc[FS_DT])
+
 template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
 template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
 
@@ -81,14 +87,14 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mloc || j >= g.Nloc) return;
-    const T DX = (T)g.DX, DY = (T)g.DY, mdf = (T)g.min_depth_frc;
+    const T DX = GC(DX), DY = GC(DY), mdf = GC(min_depth_frc);
     const size_t id = IDX(i, j);
     // ETAT from the previous stage's face fluxes (dispersion.F:103-119)
     if (i <= g.Mloc - 2 && j <= g.Nloc - 2) {
         if constexpr (sizeof(T) == sizeof(double))
             f.ETAT[id] = -(f.P[IDX(i + 1, j)] - f.P[id]) / DX - (f.Q[IDX(i, j + 1)] - f.Q[id]) / DY;
         else
-            f.ETAT[id] = -(f.P[IDX(i + 1, j)] - f.P[id]) * (T)g.rdx - (f.Q[IDX(i, j + 1)] - f.Q[id]) * (T)g.rdy;
+            f.ETAT[id] = -(f.P[IDX(i + 1, j)] - f.P[id]) * GC(rdx) - (f.Q[IDX(i, j + 1)] - f.Q[id]) * GC(rdy);
     }
 
     const bool gx = (i < g.ib) || (i > g.ie);
@@ -116,7 +122,7 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
 #define LDV(a, b) (tmax(f.Depth[IDX(si + (a), sj + (b))], mdf) * LV(a, b))
     // FP64: the reference's divisions; mixed: reciprocal constants
     constexpr bool EXACT = sizeof(T) == sizeof(double);
-    const T rdx2 = (T)(g.rdx * g.rdx), rdy2 = (T)(g.rdy * g.rdy), rdxy4 = (T)(0.25 * g.rdx * g.rdy);
+    const T rdx2 = (T)g.f_rdx2, rdy2 = (T)g.f_rdy2, rdxy4 = (T)g.f_rdxy4;
 #define DXX(F) (EXACT ? (((F(1, 0) - (T)2 * F(0, 0) + F(-1, 0)) / DX / DX) * m9) \
                       : ((F(1, 0) - (T)2 * F(0, 0) + F(-1, 0)) * rdx2 * m9))
 #define DYY(F) (EXACT ? (((F(0, 1) - (T)2 * F(0, 0) + F(0, -1)) / DY / DY) * m9) \
@@ -158,8 +164,8 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
     if (exch || (g.show_breaking && !gx && !gy)) {
         const T dex = f.Eta[IDX(si + 1, sj)] - f.Eta[IDX(si - 1, sj)];
         const T dey = f.Eta[IDX(si, sj + 1)] - f.Eta[IDX(si, sj - 1)];
-        const T ex = EXACT ? dex / DX / (T)2 * m9 : dex * (T)(0.5 * g.rdx) * m9;
-        const T ey = EXACT ? dey / DY / (T)2 * m9 : dey * (T)(0.5 * g.rdy) * m9;
+        const T ex = EXACT ? dex / DX / (T)2 * m9 : dex * (T)g.f_hdx * m9;
+        const T ey = EXACT ? dey / DY / (T)2 * m9 : dey * (T)g.f_hdy * m9;
         if (!stale) {
             if (exch && g.periodic && gx && !gy) {
                 // the periodic copy (bc.F:735-740) runs before the x mirror:
@@ -189,8 +195,8 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mloc || j >= g.Nloc) return;
     const size_t id = IDX(i, j);
-    const T DX = (T)g.DX, DY = (T)g.DY, mdf = (T)g.min_depth_frc;
-    const T B1 = (T)g.Beta_1, B2 = (T)g.Beta_2, g2 = (T)g.gamma2, b2 = (T)g.b2;
+    const T DX = GC(DX), DY = GC(DY), mdf = GC(min_depth_frc);
+    const T B1 = GC(Beta_1), B2 = GC(Beta_2), g2 = GC(gamma2), b2 = GC(b2);
     const T one = (T)1, two = (T)2, half = (T)0.5;
     const T D = f.Depth[id], reta = f.Eta[id], m9 = (T)f.MASK9[id];
     constexpr bool EXACT = sizeof(T) == sizeof(double);
@@ -223,10 +229,10 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
     f.V1p[id] = half * (one - B1) * (one - B1) * D * D * c + (B1 - one) * D * e;
     if (!(g.gamma2 > 0.0)) return;
 
-    const T DT = (T)f.dsc[S_DT];
-    const T rDT = (T)(1.0 / f.dsc[S_DT]);
-    const T hdx = (T)(0.5 * g.rdx), hdy = (T)(0.5 * g.rdy);
-    const T rdx2 = (T)(g.rdx * g.rdx), rdy2 = (T)(g.rdy * g.rdy), rdxy4 = (T)(0.25 * g.rdx * g.rdy);
+    const T DT = DTV;
+    const T rDT = (T)f.fsc[FS_RDT];
+    const T hdx = (T)g.f_hdx, hdy = (T)g.f_hdy;
+    const T rdx2 = (T)g.f_rdx2, rdy2 = (T)g.f_rdy2, rdxy4 = (T)g.f_rdxy4;
     const bool wall = (i == g.ib) || (i == g.ie) || (j == g.jb) || (j == g.je);
 #define AT(F, a_, b_) f.F[IDX(i + (a_), j + (b_))]
     const T UxxVxy = a, UxyVyy = c, HUxxHVxy = b, HUxyHVyy = e;
@@ -245,7 +251,7 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
         HUxyHVyy_y = DIFF(DUxy, DVyy, 0, 1, 0, -1, DY);
 #undef DIFF
     } else {
-        const T hx = (T)(0.5 * g.rdx), hy = (T)(0.5 * g.rdy);
+        const T hx = (T)g.f_hdx, hy = (T)g.f_hdy;
         UxxVxy_x = (AT(A, 1, 0) - AT(A, -1, 0)) * hx;
         UxxVxy_y = (AT(A, 0, 1) - AT(A, 0, -1)) * hy;
         UxyVyy_x = (AT(C, 1, 0) - AT(C, -1, 0)) * hx;
@@ -466,7 +472,7 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
     } else {
         if (i > g.ie || j > g.je + 1) return;
     }
-    const T g1 = (T)g.gamma1, g3 = (T)g.gamma3;
+    const T g1 = GC(gamma1), g3 = GC(gamma3);
     const size_t fid = IDX(i, j);
     const size_t cm = DIR == 0 ? IDX(i - 1, j) : IDX(i, j - 1);  // cell pos-1 (cell pos is fid)
     const int kf = own + 1;
@@ -559,22 +565,41 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
 template <typename T>
 __device__ __forceinline__ T wavemaker_mass(const Grid &g, const Fields<T> &f, int i, int j, double TIME) {
     if (i < g.ilo || i > g.ihi || j < g.jlo || j > g.jhi) return (T)0;
-    if (g.wavemaker == FW_WK_REG) {
-        const T AA = ftanh((T)PI_SP / ((T)g.time_ramp * (T)g.tperiod) * (T)TIME) * (T)g.D_gen;
-        const T xmk = (T)(i - g.ib) * (T)g.DX, ymk = (T)(j - g.jb) * (T)g.DY;
-        const T dxm = xmk - (T)g.xc_wk;
-        return AA * fexp(-(T)g.beta_gen * (dxm * dxm)) *
-               fsin((T)g.rlamda * (ymk - (T)0) - (T)2 * (T)PI_SP / (T)g.tperiod * (T)TIME);
-    }
-    if (g.wavemaker == FW_WK_JON_2D) {
-        const T AA = ftanh((T)PI_SP / ((T)g.time_ramp / (T)g.freq_peak) * (T)TIME);
-        const int bw = g.ihi - g.ilo + 1, bh = g.jhi - g.jlo + 1;
-        const size_t b = (size_t)(i - g.ilo) + (size_t)(j - g.jlo) * bw;
-        T s = (T)0;
-        for (int k = 0; k < g.nfreq; k++)
-            s = s + AA * ((T)f.Cm[b + (size_t)k * bw * bh] * (T)f.wmcs[2 * k] +
-                          (T)f.Sm[b + (size_t)k * bw * bh] * (T)f.wmcs[2 * k + 1]);
-        return s;
+    if constexpr (sizeof(T) == sizeof(double)) {
+        if (g.wavemaker == FW_WK_REG) {
+            const T AA = ftanh((T)PI_SP / ((T)g.time_ramp * (T)g.tperiod) * (T)TIME) * (T)g.D_gen;
+            const T xmk = (T)(i - g.ib) * (T)g.DX, ymk = (T)(j - g.jb) * (T)g.DY;
+            const T dxm = xmk - (T)g.xc_wk;
+            return AA * fexp(-(T)g.beta_gen * (dxm * dxm)) *
+                   fsin((T)g.rlamda * (ymk - (T)0) - (T)2 * (T)PI_SP / (T)g.tperiod * (T)TIME);
+        }
+        if (g.wavemaker == FW_WK_JON_2D) {
+            const T AA = ftanh((T)PI_SP / ((T)g.time_ramp / (T)g.freq_peak) * (T)TIME);
+            const int bw = g.ihi - g.ilo + 1, bh = g.jhi - g.jlo + 1;
+            const size_t b = (size_t)(i - g.ilo) + (size_t)(j - g.jlo) * bw;
+            T s = (T)0;
+            for (int k = 0; k < g.nfreq; k++)
+                s = s + AA * ((T)f.Cm[b + (size_t)k * bw * bh] * (T)f.wmcs[2 * k] +
+                              (T)f.Sm[b + (size_t)k * bw * bh] * (T)f.wmcs[2 * k + 1]);
+            return s;
+        }
+    } else {
+        // mixed: the ramp and phase of this step come from k_dt_final
+        const T AA = f.fsc[FS_WKAA];
+        if (g.wavemaker == FW_WK_REG) {
+            const T xmk = (T)(i - g.ib) * g.f_DX, ymk = (T)(j - g.jb) * g.f_DY;
+            const T dxm = xmk - g.f_xc_wk;
+            return AA * fexp(-g.f_beta_gen * (dxm * dxm)) * fsin(g.f_rlamda * ymk - f.fsc[FS_WKPH]);
+        }
+        if (g.wavemaker == FW_WK_JON_2D) {
+            const int bw = g.ihi - g.ilo + 1, bh = g.jhi - g.jlo + 1;
+            const size_t b = (size_t)(i - g.ilo) + (size_t)(j - g.jlo) * bw;
+            T s = (T)0;
+            for (int k = 0; k < g.nfreq; k++)
+                s = s + AA * ((T)f.Cm[b + (size_t)k * bw * bh] * f.wmcsf[2 * k] +
+                              (T)f.Sm[b + (size_t)k * bw * bh] * f.wmcsf[2 * k + 1]);
+            return s;
+        }
     }
     return (T)0;
 }
@@ -583,12 +608,12 @@ template <typename T>
 __device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, int i, int j, T wm, T &SX,
                                              T &SY) {
     constexpr bool EXACT = sizeof(T) == sizeof(double);
-    const T DX = (T)g.DX, DY = (T)g.DY, mdf = (T)g.min_depth_frc;
-    const T rdx = (T)g.rdx, rdy = (T)g.rdy;
+    const T DX = GC(DX), DY = GC(DY), mdf = GC(min_depth_frc);
+    const T rdx = GC(rdx), rdy = GC(rdy);
     // x/DX: the reference's division in FP64, a reciprocal in the mixed path
 #define OX(x) (EXACT ? (x) / DX : (x) * rdx)
 #define OY(x) (EXACT ? (x) / DY : (x) * rdy)
-    const T g1 = (T)g.gamma1, g2 = (T)g.gamma2;
+    const T g1 = GC(gamma1), g2 = GC(gamma2);
     const size_t id = IDX(i, j);
     const size_t ie_ = IDX(i + 1, j), iw = IDX(i - 1, j), in_ = IDX(i, j + 1), is = IDX(i, j - 1);
     const T U = f.U[id], V = f.V[id];
@@ -630,7 +655,7 @@ __device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, 
             by = (T)0.5 / DX * (nxp * (T)1 / DX * (f.HV[ie_] - HVc) - nxm * (T)1 / DX * (HVc - f.HV[iw])) +
                  (T)0.5 / DY * (nyp * (T)1 / DY * (f.HV[in_] - HVc) - nym * (T)1 / DY * (HVc - f.HV[is]));
         } else {
-            const T cx = (T)(0.5 * g.rdx * g.rdx), cy = (T)(0.5 * g.rdy * g.rdy);
+            const T cx = (T)g.f_cx, cy = (T)g.f_cy;
             bx = cx * (nxp * (f.HU[ie_] - HUc) - nxm * (HUc - f.HU[iw])) +
                  cy * (nyp * (f.HU[in_] - HUc) - nym * (HUc - f.HU[is]));
             by = cx * (nxp * (f.HV[ie_] - HVc) - nxm * (HVc - f.HV[iw])) +
@@ -670,13 +695,13 @@ __global__ void __launch_bounds__(256) k_update(Grid g, Fields<T> f, T al, T be)
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mloc || j >= g.Nloc) return;
     const size_t id = IDX(i, j);
-    const T g3 = (T)g.gamma3;
+    const T g3 = GC(gamma3);
     if (i < g.ib || i > g.ie || j < g.jb || j > g.je) {
         f.H[id] = f.Eta[id] * g3 + f.Depth[id];  // H = Eta*Gamma3+Depth on all cells
         return;
     }
-    const T DX = (T)g.DX, DY = (T)g.DY;
-    const T DT = (T)f.dsc[S_DT];
+    const T DX = GC(DX), DY = GC(DY);
+    const T DT = DTV;
     const double TIME = f.dsc[S_TIME];
     const T wm = wavemaker_mass(g, f, i, j, TIME);
     T SX, SY;
@@ -684,17 +709,17 @@ __global__ void __launch_bounds__(256) k_update(Grid g, Fields<T> f, T al, T be)
 
     const size_t ie_ = IDX(i + 1, j), in_ = IDX(i, j + 1);
     constexpr bool EXACT = sizeof(T) == sizeof(double);
-    const T cdx = EXACT ? (T)1 / DX : (T)g.rdx, cdy = EXACT ? (T)1 / DY : (T)g.rdy;
+    const T cdx = EXACT ? (T)1 / DX : GC(rdx), cdy = EXACT ? (T)1 / DY : GC(rdy);
     T R1 = -cdx * (f.P[ie_] * (T)1 + f.P[id] * (T)-1) - cdy * (f.Q[in_] * (T)1 + f.Q[id] * (T)-1);
     if (g.wavemaker != FW_WK_NONE) {
         const T xmk = (T)(i - g.ib) * DX, ymk = (T)(j - g.jb) * DY;
-        if (fabs_(xmk - (T)g.xc_wk) < (T)g.width_wk && fabs_(ymk - (T)g.yc_wk) < (T)g.ywidth_wk / (T)2)
+        if (fabs_(xmk - GC(xc_wk)) < GC(width_wk) && fabs_(ymk - GC(yc_wk)) < GC(ywidth_wk) / (T)2)
             R1 = R1 + wm;
     }
     T eta = al * f.Eta0[id] + be * (f.Eta[id] + DT * R1);
     if (g.eta_limiter) {
-        if (eta < (T)g.trough) eta = (T)g.trough;
-        if (eta > (T)g.crest) eta = (T)g.crest;
+        if (eta < GC(trough)) eta = GC(trough);
+        if (eta > GC(crest)) eta = GC(crest);
     }
     const T R2 = -cdx * (f.Fx[ie_] * (T)1 + f.Fx[id] * (T)-1) - cdy * (f.Fy[in_] * (T)1 + f.Fy[id] * (T)-1) + SX;
     const T ubar = al * f.Ubar0[id] + be * (f.Ubar[id] + DT * R2);
@@ -708,24 +733,27 @@ __global__ void __launch_bounds__(256) k_update(Grid g, Fields<T> f, T al, T be)
     if (!g.dispersion) return;
 
     // tmp4 of the x and y systems (etauv_solver.F:410-411, 508-509)
-    const double mdf = g.min_depth_frc;
-    const double g1 = g.gamma1, b1 = g.b1, b2 = g.b2;
-    const double m9 = (double)f.MASK9[id];
-    const double mk = (double)f.MASK[id];
-    const double dep = tmax((double)f.Depth[id], mdf);
-    const double Hm = tmax((double)H, mdf);
     if constexpr (sizeof(T) == sizeof(double)) {
+        const double mdf = g.min_depth_frc;
+        const double g1 = g.gamma1, b1 = g.b1, b2 = g.b2;
+        const double m9 = (double)f.MASK9[id];
+        const double mk = (double)f.MASK[id];
+        const double dep = tmax((double)f.Depth[id], mdf);
+        const double Hm = tmax((double)H, mdf);
         // the cross derivatives CAL_DISPERSION left at the start of the stage
         const double Vxy = f.Vxy[id], DVxy = f.DVxy[id], Uxy = f.Uxy[id], DUxy = f.DUxy[id];
         f.rhs_x[id] = (double)ubar * mk / Hm + g1 * m9 * (-b1 / 2.0 * dep * dep * Vxy - b2 * dep * DVxy);
         f.rhs_y[id] = (double)vbar * mk / Hm + g1 * m9 * (-b1 / 2.0 * dep * dep * Uxy - b2 * dep * DUxy);
     } else {
-        // mixed: cross derivatives of the stage-start U, V in float
+        // mixed: float arithmetic; the cross derivatives of the stage-start
+        // U, V are recomputed here
+        const T mf = g.f_min_depth_frc;
+        const T m9 = (T)f.MASK9[id], mk = (T)f.MASK[id];
+        const T dep = tmax(f.Depth[id], mf);
         const bool wall = (i == g.ib) || (i == g.ie) || (j == g.jb) || (j == g.je);
         T Vxy = (T)0, DVxy = (T)0, Uxy = (T)0, DUxy = (T)0;
         if (!wall) {
-            const T q = (T)(0.25 * g.rdx * g.rdy) * (T)m9;
-            const T mf = (T)mdf;
+            const T q = g.f_rdxy4 * m9;
 #define XY(F) (((F(1, 1) - F(1, -1)) - (F(-1, 1) - F(-1, -1))) * q)
 #define LV(a, b) (f.V[IDX(i + (a), j + (b))])
 #define LU(a, b) (f.U[IDX(i + (a), j + (b))])
@@ -741,10 +769,9 @@ __global__ void __launch_bounds__(256) k_update(Grid g, Fields<T> f, T al, T be)
 #undef LDV
 #undef LDU
         }
-        const T fd = (T)dep, fg = (T)(g1 * m9), rH = (T)1 / (T)Hm;
-        const T hb1 = (T)(-0.5 * b1), fb2 = (T)b2;
-        f.rhs_x[id] = (double)(ubar * (T)mk * rH + fg * (hb1 * fd * fd * Vxy - fb2 * fd * DVxy));
-        f.rhs_y[id] = (double)(vbar * (T)mk * rH + fg * (hb1 * fd * fd * Uxy - fb2 * fd * DUxy));
+        const T fg = g.f_gamma1 * m9, rH = (T)1 / tmax(H, mf);
+        f.rhs_x[id] = (double)(ubar * mk * rH + fg * (g.f_hb1 * dep * dep * Vxy - g.f_b2 * dep * DVxy));
+        f.rhs_y[id] = (double)(vbar * mk * rH + fg * (g.f_hb1 * dep * dep * Uxy - g.f_b2 * dep * DUxy));
     }
 }
 
@@ -1444,7 +1471,7 @@ __global__ void __launch_bounds__(256) k_post(Grid g, Fields<T> f) {
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mloc || j >= g.Nloc) return;
     const size_t id = IDX(i, j);
-    const T mdf = (T)g.min_depth_frc;
+    const T mdf = GC(min_depth_frc);
     const bool interior = !(i < g.ib || i > g.ie || j < g.jb || j > g.je);
     if (interior) {
         if (!g.dispersion) {
@@ -1466,10 +1493,10 @@ __global__ void __launch_bounds__(256) k_post(Grid g, Fields<T> f) {
             f.HV[id] = Hm * v;
             const T Utotal = fsqrt(u * u + v * v);
             const T Fr = fsqrt((T)GRAV * Hm);
-            if (Utotal / Fr > (T)g.froude_cap) {
+            if (Utotal / Fr > GC(froude_cap)) {
                 const T th = fatan2(v, u);
-                const T un = (T)g.froude_cap * Fr * fcos(th);
-                const T vn = (T)g.froude_cap * Fr * fsin(th);
+                const T un = GC(froude_cap) * Fr * fcos(th);
+                const T vn = GC(froude_cap) * Fr * fsin(th);
                 f.U[id] = un;
                 f.V[id] = vn;
                 f.HU[id] = un * Hm;
@@ -1504,18 +1531,19 @@ __device__ __forceinline__ int new_mask(const Grid &g, const Fields<T> &f, int a
     const size_t q = IDX(a, b);
     const int m = f.MASK[q];
     if (!in_mask_range<T>(g, a, b) || f.MASK_STRUC[q] != 1) return m;
-    // the total-depth tests run in double in both precisions
-    const double eta = (double)f.Eta[q];
+    // total-depth tests: comparing the stored values in T is exact (a
+    // float widened to double compares the same), so no FP64 work is needed
+    const T eta = f.Eta[q];
     if (m < 1) {
         int r = m;
-        if (eta > -(double)f.Depth[q]) r = 1;
-        if (f.MASK[IDX(a - 1, b)] == 1 && (double)f.Eta[IDX(a - 1, b)] > eta) r = 1;
-        if (f.MASK[IDX(a + 1, b)] == 1 && (double)f.Eta[IDX(a + 1, b)] > eta) r = 1;
-        if (f.MASK[IDX(a, b - 1)] == 1 && (double)f.Eta[IDX(a, b - 1)] > eta) r = 1;
-        if (f.MASK[IDX(a, b + 1)] == 1 && (double)f.Eta[IDX(a, b + 1)] > eta) r = 1;
+        if (eta > -f.Depth[q]) r = 1;
+        if (f.MASK[IDX(a - 1, b)] == 1 && f.Eta[IDX(a - 1, b)] > eta) r = 1;
+        if (f.MASK[IDX(a + 1, b)] == 1 && f.Eta[IDX(a + 1, b)] > eta) r = 1;
+        if (f.MASK[IDX(a, b - 1)] == 1 && f.Eta[IDX(a, b - 1)] > eta) r = 1;
+        if (f.MASK[IDX(a, b + 1)] == 1 && f.Eta[IDX(a, b + 1)] > eta) r = 1;
         return r;
     }
-    return (eta < -(double)f.Depth[q]) ? 0 : m;
+    return (eta < -f.Depth[q]) ? 0 : m;
 }
 
 template <typename T>
@@ -1550,7 +1578,7 @@ __global__ void __launch_bounds__(256) k_mask(Grid g, Fields<T> f) {
             int p = 1;
             for (int b = -1; b <= 1; b++)
                 for (int a = -1; a <= 1; a++) p *= new_mask(g, f, i + a, j + b);
-            if (fabs((double)f.Eta[id]) / tmax((double)f.Depth[id], g.min_depth_frc) > g.swe_eta_dep) p = 0;
+            if (fabs_(f.Eta[id]) / tmax(f.Depth[id], GC(min_depth_frc)) > GC(swe_eta_dep)) p = 0;
             m9 = (uint8_t)p;
         }
     }
@@ -1567,33 +1595,33 @@ template <typename T> struct BrkLocal {
 template <typename T>
 __device__ __forceinline__ BrkLocal<T> brk_local(const Grid &g, const Fields<T> &f, size_t id) {
     BrkLocal<T> b;
-    b.tmp3 = fsqrt((T)GRAV * tmax((T)g.min_depth_frc, f.H[id]));
-    b.tmp1 = (T)g.cbrk1 * b.tmp3;
-    b.tmp2 = (T)g.cbrk2 * b.tmp3;
+    b.tmp3 = fsqrt((T)GRAV * tmax(GC(min_depth_frc), f.H[id]));
+    b.tmp1 = GC(cbrk1) * b.tmp3;
+    b.tmp2 = GC(cbrk2) * b.tmp3;
     b.et = f.ETAT[id];
     return b;
 }
 template <typename T>
 __device__ __forceinline__ bool in_wk_zone(const Grid &g, int i, int j) {
-    const T xmk = (T)(i - g.ib) * (T)g.DX, ymk = (T)(j - g.jb) * (T)g.DY;
-    return fabs_(xmk - (T)g.xc_wk) < (T)g.width_wk && fabs_(ymk - (T)g.yc_wk) < (T)g.ywidth_wk / (T)2;
+    const T xmk = (T)(i - g.ib) * GC(DX), ymk = (T)(j - g.jb) * GC(DY);
+    return fabs_(xmk - GC(xc_wk)) < GC(width_wk) && fabs_(ymk - GC(yc_wk)) < GC(ywidth_wk) / (T)2;
 }
 template <typename T>
 __device__ __forceinline__ T nu_value(const Grid &g, const Fields<T> &f, size_t id, const BrkLocal<T> &b, T age,
                                       bool zone) {
-    const T mdf = (T)g.min_depth_frc;
+    const T mdf = GC(min_depth_frc);
     if (zone) {
-        if (b.et > tmin(b.tmp2, (T)g.wavemaker_cbrk * b.tmp3)) {
+        if (b.et > tmin(b.tmp2, GC(wavemaker_cbrk) * b.tmp3)) {
             const T cap1 = (T)1 * (tmax(f.Depth[id], mdf) + f.Eta[id]);
-            return cap1 * (T)g.wavemaker_cbrk * b.tmp3 + (T)g.nu_bkg;
+            return cap1 * GC(wavemaker_cbrk) * b.tmp3 + GC(nu_bkg);
         }
-        return (T)0 + (T)g.nu_bkg;
+        return (T)0 + GC(nu_bkg);
     }
-    if (age > (T)0 && age < (T)g.T_brk && b.et > b.tmp2) {
+    if (age > (T)0 && age < GC(T_brk) && b.et > b.tmp2) {
         const T cap1 = (T)1 * (tmax(f.Depth[id], mdf) + f.Eta[id]);
-        return cap1 * b.tmp2 + (T)g.nu_bkg;
+        return cap1 * b.tmp2 + GC(nu_bkg);
     }
-    return (T)0 + (T)g.nu_bkg;
+    return (T)0 + GC(nu_bkg);
 }
 
 template <typename T>
@@ -1607,11 +1635,11 @@ __global__ void __launch_bounds__(256) k_break_a(Grid g, Fields<T> f) {
         f.AGEn[id] = age;
         return;
     }
-    const T DT = (T)f.dsc[S_DT];
+    const T DT = DTV;
     const BrkLocal<T> b = brk_local(g, f, id);
     T an = age;
     bool cand = false;
-    if (b.et >= b.tmp1 && (age == (T)0 || age > (T)g.T_brk)) an = DT;
+    if (b.et >= b.tmp1 && (age == (T)0 || age > GC(T_brk))) an = DT;
     else if (age > (T)0) an = age + DT;
     else if (b.et >= b.tmp2) cand = true;
     f.AGEn[id] = an;
@@ -1633,7 +1661,7 @@ __device__ __forceinline__ bool brk_neigh(const Grid &g, const Fields<T> &f, con
     const T tmp4 = tmax(fsqrt(ex * ex + ey * ey), (T)SMALL);
     const T Hc = f.H[id];
     const T C = tmin(fabs_(f.ETAT[id]) / tmp4, fsqrt((T)GRAV * fabs_(Hc)));
-    const T DX = (T)g.DX, DY = (T)g.DY;
+    const T DX = GC(DX), DY = GC(DY);
     const T propxy = fsqrt(DX * DX + DY * DY) / tmax(C, (T)SMALL);
     const T propx = fsqrt(DX * DX) / tmax(C, (T)SMALL);
     const T propy = fsqrt(DY * DY) / tmax(C, (T)SMALL);
@@ -1678,7 +1706,7 @@ template <typename T>
 __global__ void __launch_bounds__(1024) k_break_b(Grid g, Fields<T> f) {
     __shared__ int changed;
     const int n = *f.ncand;
-    const T DT = (T)f.dsc[S_DT];
+    const T DT = DTV;
     volatile T *N = f.AGEn;
     for (int pass = 0; pass <= n; pass++) {
         if (threadIdx.x == 0) changed = 0;
@@ -1871,29 +1899,35 @@ __global__ void k_sponge(Grid g, Fields<T> f) {
 // TIME on the device.  Positive doubles order like their bit patterns.
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ __forceinline__ double dt_cell(const Grid &g, const Fields<T> &f, size_t id) {
-    const T c = fsqrt((T)GRAV * tmax(f.H[id], (T)g.min_depth_frc));
+__device__ __forceinline__ T dt_cell(const Grid &g, const Fields<T> &f, size_t id) {
+    const T c = fsqrt((T)GRAV * tmax(f.H[id], GC(min_depth_frc)));
     T t1 = fabs_(f.U[id]) + c;
-    T t2 = (t1 < (T)SMALL) ? (T)g.DX / (T)SMALL : (T)g.DX / t1;
+    T t2 = (t1 < (T)SMALL) ? GC(DX) / (T)SMALL : GC(DX) / t1;
     T m = t2;
     t1 = fabs_(f.V[id]) + c;
-    t2 = (t1 < (T)SMALL) ? (T)g.DY / (T)SMALL : (T)g.DY / t1;
+    t2 = (t1 < (T)SMALL) ? GC(DY) / (T)SMALL : GC(DY) / t1;
     if (t2 < m) m = t2;
-    return (double)m;
+    return m;
 }
 
-__device__ __forceinline__ void block_min_to_global(double v, unsigned long long *dst) {
-    __shared__ double sm[32];
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+__device__ __forceinline__ double tminr(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float tminr(float a, float b) { return fminf(a, b); }
+
+// block minimum in T, then one atomicMin on the (order-preserving) bits of
+// the positive double
+template <typename T>
+__device__ __forceinline__ void block_min_to_global(T v, unsigned long long *dst) {
+    __shared__ T sm[32];
+    for (int o = 16; o > 0; o >>= 1) v = tminr(v, __shfl_xor_sync(0xffffffffu, v, o));
     const int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
     const int warp = (threadIdx.x + threadIdx.y * blockDim.x) >> 5;
     const int nw = (blockDim.x * blockDim.y + 31) >> 5;
     if (lane == 0) sm[warp] = v;
     __syncthreads();
     if (warp == 0) {
-        v = lane < nw ? sm[lane] : 1.0e300;
-        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if (lane == 0) atomicMin(dst, (unsigned long long)__double_as_longlong(v));
+        v = lane < nw ? sm[lane] : (T)1.0e30;
+        for (int o = 16; o > 0; o >>= 1) v = tminr(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) atomicMin(dst, (unsigned long long)__double_as_longlong((double)v));
     }
 }
 
@@ -1903,7 +1937,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_begin(Grid g, Fields<T> f) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    double v = 1.0e300;
+    T v = (T)1.0e30;
     if (i < g.Mloc && j < g.Nloc) {
         const size_t id = IDX(i, j);
         const T m = (T)f.MASK[id];
@@ -1926,14 +1960,15 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_dt_only(Grid g, Fields<T> f) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    double v = 1.0e300;
+    T v = (T)1.0e30;
     if (i < g.Mloc && j < g.Nloc) v = dt_cell(g, f, IDX(i, j));
     block_min_to_global(v, f.dtmin_bits);
 }
 
 // DT = CFL*min (with DT_fixed halving), TIME += DT, and the JON_2D
 // cos/sin(omega_k TIME) table of this step (sources.F:121-124)
-static __global__ void k_dt_final(Grid g, double *dsc, unsigned long long *bits, double *omega, double *wmcs, int nfreq) {
+static __global__ void k_dt_final(Grid g, double *dsc, float *fsc, unsigned long long *bits, double *omega,
+                                  double *wmcs, float *wmcsf, int nfreq) {
     __shared__ double time_s;
     if (threadIdx.x == 0) {
         double tmp3 = __longlong_as_double((long long)*bits);
@@ -1950,11 +1985,25 @@ static __global__ void k_dt_final(Grid g, double *dsc, unsigned long long *bits,
         dsc[S_TIME] = dsc[S_TIME] + dt;
         time_s = dsc[S_TIME];
         *bits = 0x7ff0000000000000ull;  // +inf for the next minimum
+        // float scalars of the step for the mixed path: DT, 1/DT, the
+        // wavemaker ramp (sources.F:110,120) and the WK_REG phase
+        // 2*pi/Tperiod*TIME reduced modulo 2*pi
+        fsc[FS_DT] = (float)dt;
+        fsc[FS_RDT] = (float)(1.0 / dt);
+        if (g.wavemaker == FW_WK_REG) {
+            fsc[FS_WKAA] = (float)(tanh(PI_SP / (g.time_ramp * g.tperiod) * time_s) * g.D_gen);
+            const double ph = 2.0 * PI_SP / g.tperiod * time_s;
+            fsc[FS_WKPH] = (float)(ph - 2.0 * PI_SP * floor(ph / (2.0 * PI_SP)));
+        } else if (g.wavemaker == FW_WK_JON_2D) {
+            fsc[FS_WKAA] = (float)tanh(PI_SP / (g.time_ramp / g.freq_peak) * time_s);
+        }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < nfreq; k += blockDim.x) {
         wmcs[2 * k] = cos(omega[k] * time_s);
         wmcs[2 * k + 1] = sin(omega[k] * time_s);
+        wmcsf[2 * k] = (float)wmcs[2 * k];
+        wmcsf[2 * k + 1] = (float)wmcs[2 * k + 1];
     }
 }
 
@@ -1966,19 +2015,22 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_end(Grid g, Fields<T> f, int track_hmax) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    double v = 0.0;
+    T v = (T)0;
     if (i < g.Mloc && j < g.Nloc) {
         const size_t id = IDX(i, j);
         const T eta = f.Eta[id];
         if (track_hmax && f.MASK[id] > 0 && eta > f.Hmax[id]) f.Hmax[id] = eta;
         if (i >= g.ib && i <= g.ie && j >= g.jb && j <= g.je) {
-            const double a = fabs((double)eta);
-            v = (a == a) ? a : 1.0e308 * 10.0;  // NaN -> +inf
+            const T a = fabs_(eta);
+            v = (a == a) ? a : (T)INFINITY;  // NaN -> +inf
         }
     }
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) {
+        const T w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
     if (((threadIdx.x + threadIdx.y * blockDim.x) & 31) == 0)
-        atomicMax(f.etamax_bits, (unsigned long long)__double_as_longlong(v));
+        atomicMax(f.etamax_bits, (unsigned long long)__double_as_longlong((double)v));
 }
 
 // ---------------------------------------------------------------------------
@@ -2015,13 +2067,15 @@ template <typename T> void launch_sponge(fw_ctx *c) {
 }
 
 static void launch_dt_final(fw_ctx *c) {
-    auto &fd = c->fd;
-    double *dsc = c->p.precision == FW_PREC_FP64 ? c->fd.dsc : c->ff.dsc;
-    unsigned long long *bits = c->p.precision == FW_PREC_FP64 ? c->fd.dtmin_bits : c->ff.dtmin_bits;
-    double *om = c->p.precision == FW_PREC_FP64 ? c->fd.omega : c->ff.omega;
-    double *cs = c->p.precision == FW_PREC_FP64 ? c->fd.wmcs : c->ff.wmcs;
-    (void)fd;
-    k_dt_final<<<1, 128, 0, c->stream>>>(c->g, dsc, bits, om, cs, c->g.wavemaker == FW_WK_JON_2D ? c->g.nfreq : 0);
+    const bool d = c->p.precision == FW_PREC_FP64;
+    double *dsc = d ? c->fd.dsc : c->ff.dsc;
+    float *fsc = d ? c->fd.fsc : c->ff.fsc;
+    unsigned long long *bits = d ? c->fd.dtmin_bits : c->ff.dtmin_bits;
+    double *om = d ? c->fd.omega : c->ff.omega;
+    double *cs = d ? c->fd.wmcs : c->ff.wmcs;
+    float *csf = d ? c->fd.wmcsf : c->ff.wmcsf;
+    k_dt_final<<<1, 128, 0, c->stream>>>(c->g, dsc, fsc, bits, om, cs, csf,
+                                         c->g.wavemaker == FW_WK_JON_2D ? c->g.nfreq : 0);
     note(c);
 }
 
