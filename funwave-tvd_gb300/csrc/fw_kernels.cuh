@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(256) k_sources(Grid g, Fields<T> f) {
 // GET_Eta_U_V_HU_HV (etauv_solver.F:365-539).
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256) k_update(Grid g, Fields<T> f, T al, T be) {
+__global__ void __launch_bounds__(256, 3) k_update(Grid g, Fields<T> f, T al, T be) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mloc || j >= g.Nloc) return;
@@ -1214,8 +1214,10 @@ __global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp)
     int i, j;
     line_cell<DIR>(g, l, s, i, j);
     it_[IDX(i, j)] = its;
+    if (DIR == 0) r_[IDX(i, j)] = its;   // x lines: A = 1/tmp2 at chunk ends
     line_cell<DIR>(g, l, e, i, j);
     it_[IDX(i, j)] = ite;
+    if (DIR == 0) r_[IDX(i, j)] = ite;
     if (s == 0) as = 0.0;
     if (e == lp.L - 1) ce = 0.0;
     double lo_s, di_s, up_s, lo_e, di_e, up_e;
@@ -1233,7 +1235,7 @@ __global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp)
             line_cell<DIR>(g, l, k, i, j);
             const size_t q = IDX(i, j);
             it_[q] = it;
-            r_[q] = r;
+            r_[q] = DIR == 0 ? it * r : r;  // x lines: A = r/tmp2 (d*r in one product)
             lr_[q] = lower * r;
             cp_[q] = cp;
             p_[q] = pp;
@@ -1458,6 +1460,84 @@ __global__ void __launch_bounds__(128) k_sol_c(Grid g, Fields<T> f, LinePart lp)
         line_cell<DIR>(g, l, k, i, j);
         const size_t q = IDX(i, j);
         out[q] = (T)(f.ty[q] - p_[q] * xs - q_[q] * xe);
+    }
+}
+
+// x lines, one block per line: every global access is unit-stride across
+// the block; the right-hand side and the sweeps live in shared memory.
+//   y_k = rhs_k * A_k        (coalesced; A from k_fac_a)
+//   per chunk: forward  y_k -= lr_k * y_{k-1},  backward y_k -= c'_k * y_{k+1}
+//   reduced system (thread 0), then x_k = y_k - p_k x_s - q_k x_e (coalesced)
+template <typename T>
+__global__ void __launch_bounds__(128) k_linesolve_x(Grid g, Fields<T> f, LinePart lp) {
+    extern __shared__ double sh[];
+    const int l = blockIdx.x;
+    const int L = lp.L, P = lp.P, m = lp.m;
+    double *y = sh;            // L
+    double *bb = sh + L;       // L: lr, then c'
+    double *rr = sh + 2 * L;   // 2P reduced right-hand sides / solution
+    const int j = g.jb + l;
+    const size_t row = (size_t)j * g.pitch + g.ib;
+    const double *rhs = f.rhs_x + row, *A = f.fac_r[0] + row, *B = f.fac_lr[0] + row;
+    for (int k = threadIdx.x; k < L; k += blockDim.x) {
+        y[k] = rhs[k] * A[k];
+        bb[k] = B[k];
+    }
+    __syncthreads();
+    const int ch = threadIdx.x;
+    const int s = ch * m;
+    const int e = (ch == P - 1) ? L - 1 : s + m - 1;
+    if (ch < P && e - s >= 2) {
+        double yp = 0.0;
+        for (int k = s + 1; k <= e - 1; k++) {
+            yp = y[k] - bb[k] * yp;
+            y[k] = yp;
+        }
+    }
+    __syncthreads();
+    const double *CP = f.fac_cp[0] + row;
+    for (int k = threadIdx.x; k < L; k += blockDim.x) bb[k] = CP[k];
+    __syncthreads();
+    FacLine fl = fac_line(f.fac_red[0], lp, l);
+    if (ch < P) {
+        double rs = y[s], re = y[e];
+        if (e - s >= 2) {
+            double yn = 0.0;
+            for (int k = e - 1; k >= s + 1; k--) {
+                yn = y[k] - bb[k] * yn;
+                y[k] = yn;
+            }
+            rs = y[s] - fl.cs[ch] * y[s + 1];
+            re = y[e] - fl.ae[ch] * y[e - 1];
+        }
+        rr[2 * ch] = rs;
+        rr[2 * ch + 1] = re;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int n = 2 * P;
+        double z = 0.0;
+        for (int k = 0; k < n; k++) {
+            z = (rr[k] - fl.lo[k] * z) * fl.invden[k];
+            rr[k] = z;
+        }
+        double x = 0.0;
+        for (int k = n - 1; k >= 0; k--) {
+            x = rr[k] - fl.cpr[k] * x;
+            rr[k] = x;
+        }
+    }
+    __syncthreads();
+    const double *Pp = f.fac_p[0] + row, *Qq = f.fac_q[0] + row;
+    T *out = f.U + row;
+    for (int k = threadIdx.x; k < L; k += blockDim.x) {
+        const int c = min(k / m, P - 1);
+        const int cs = c * m, ce = (c == P - 1) ? L - 1 : cs + m - 1;
+        double x;
+        if (k == cs) x = rr[2 * c];
+        else if (k == ce) x = rr[2 * c + 1];
+        else x = y[k] - Pp[k] * rr[2 * c] - Qq[k] * rr[2 * c + 1];
+        out[k] = (T)x;
     }
 }
 
@@ -2127,6 +2207,14 @@ template <typename T, int DIR, bool PER> static void launch_tri(fw_ctx *c, const
     if (c->factored) {
         k_fac_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         k_fac_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        const size_t smem = (size_t)(2 * lp.L + 2 * lp.P) * sizeof(double);
+        if (DIR == 0 && !PER && lp.P <= 128 && smem <= 200 * 1024) {
+            if (smem > 48 * 1024)
+                cudaFuncSetAttribute(k_linesolve_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_linesolve_x<T><<<lp.nlines, 128, smem, c->stream>>>(g, c->F<T>(), lp);
+            note(c, 3);
+            return;
+        }
         k_sol_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         k_sol_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         k_sol_c<T, DIR><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);

@@ -24,10 +24,12 @@ _BUILD = os.path.join(_HERE, "_build")
 _HEADER = os.path.join(_ROOT, "include", "funwave_gpu.h")
 # translation units and their extra flags: the FP64 kernels and the host
 # initialisation keep every multiply and add separately rounded (the
-# reference's operation order); the mixed-precision kernels may contract
+# reference's operation order); the mixed-precision kernels may contract and
+# use the fast single-precision division and square root (the double
+# arithmetic of their line solver is not affected)
 _SOURCES = {
     "fw_kernels_f64.cu": ["-fmad=false"],
-    "fw_kernels_f32.cu": [],
+    "fw_kernels_f32.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
     "fw_api.cu": [],
     "fw_init.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
