@@ -200,17 +200,20 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
     for (T **p : tf) *p = (T *)take(plane * sizeof(T));
     uint8_t **mf[] = {&f.MASK, &f.MASKn, &f.MASK9, &f.MASK_STRUC};
     for (uint8_t **p : mf) *p = (uint8_t *)take(plane);
-    double **df[] = {&f.rhs_x, &f.rhs_y, &f.ty, &f.tp, &f.tq};
+    f.rhs_x = (T *)take(plane * sizeof(T));
+    f.rhs_y = (T *)take(plane * sizeof(T));
+    double **df[] = {&f.ty, &f.tp, &f.tq, &f.tc};
     for (double **p : df) *p = (double *)take(plane * sizeof(double));
     f.m9_dirty = (int *)take(sizeof(int));
     if (sizeof(T) == sizeof(float)) {
         for (int d = 0; d < 2; d++) {
-            double **ff[] = {&f.fac_it[d], &f.fac_r[d], &f.fac_lr[d], &f.fac_cp[d], &f.fac_p[d], &f.fac_q[d]};
-            for (double **p : ff) *p = (double *)take(plane * sizeof(double));
+            float **ff[] = {&f.fac_it[d], &f.fac_A[d], &f.fac_lr[d], &f.fac_cp[d], &f.fac_p[d],
+                            &f.fac_q[d], &f.fac_ah[d], &f.fac_al[d], &f.fac_ch[d], &f.fac_cl[d]};
+            for (float **p : ff) *p = (float *)take(plane * sizeof(float));
             const LinePart &lp = d == 0 ? c->px : c->py;
             // per line: 2P reduced rows x 3 + P chunks x 2 + 2P second solution + 3
             const size_t per_line = (size_t)2 * lp.P * 3 + (size_t)lp.P * 2 + (size_t)2 * lp.P + 3;
-            f.fac_red[d] = (double *)take((size_t)lp.nlines * per_line * sizeof(double));
+            f.fac_red[d] = (float *)take((size_t)lp.nlines * per_line * sizeof(float));
         }
     }
     const size_t nred = std::max((size_t)c->px.nlines * 2 * c->px.P, (size_t)c->py.nlines * 2 * c->py.P);

@@ -66,15 +66,18 @@ struct Fields {
     T *SourceX, *SourceY, *WM;        // materialised only by the unit entry points
     T *Hmax;
     uint8_t *MASK, *MASKn, *MASK9, *MASK_STRUC;
-    double *rhs_x, *rhs_y;            // tmp4 of GET_Eta_U_V_HU_HV
-    double *ty, *tp, *tq;             // chunked line-solver scratch
+    T *rhs_x, *rhs_y;                 // tmp4 of GET_Eta_U_V_HU_HV
+    double *ty, *tp, *tq, *tc;        // line-solver scratch
     double *red;                      // reduced systems
     // mixed path: constant factorisation of the tridiagonal matrices, per
-    // direction d: per row 1/tmp2, r, lower*r, c', p, q; per reduced row
-    // lo, 1/den, c'; per chunk c_s, a_e; per line (periodic) the second
+    // direction d, rounded to float: per row d-scale (1/tmp2, times r on
+    // chunk interiors), lower*r, c', p, q and the normalised coefficients a,
+    // c as float pairs (hi + lo) for the compensated residual; per reduced
+    // row lo, 1/den, c'; per chunk c_s, a_e; per line (periodic) the second
     // solution, c_end, a_beg and the Sherman-Morrison denominator
-    double *fac_it[2], *fac_r[2], *fac_lr[2], *fac_cp[2], *fac_p[2], *fac_q[2];
-    double *fac_red[2];
+    float *fac_it[2], *fac_A[2], *fac_lr[2], *fac_cp[2], *fac_p[2], *fac_q[2];
+    float *fac_ah[2], *fac_al[2], *fac_ch[2], *fac_cl[2];
+    float *fac_red[2];
     int *m9_dirty;                    // MASK9 changed since the last factorisation
     double *Cm, *Sm, *omega, *wmcs;   // JON_2D band tables and cos/sin(omega t)
     double *dsc;                      // device scalars (S_*)

@@ -367,21 +367,14 @@ template <typename T> __device__ __forceinline__ T lim3(T a, T b, T c) {
     return tmin((T)0, tmax(tmax(a, (T)2 * b), (T)2 * c));
 }
 // Din(p) from v[0..3] = Vin(p-2..p+1), m[0..3] = MASK(p-2..p+1)
+// (fluxes.F:1548-1598).  When any of the four cells is dry the reference
+// either limits three equal slopes, which returns TXP2 for each of them, or
+// zeroes the limited slopes; both give TXP2 - 1/6*(+0) = TXP2 exactly, so
+// the limiter is only evaluated for four wet cells.
 template <typename T> __device__ __forceinline__ T ho_din(const T *v, const int *m) {
-    T TXP1 = v[1] - v[0], TXP2 = v[2] - v[1], TXP3 = v[3] - v[2];
-    T DVP1 = lim3(TXP1, TXP2, TXP3), DVP2 = lim3(TXP2, TXP3, TXP1), DVP3 = lim3(TXP3, TXP1, TXP2);
-    if (m[0] == 0 || m[3] == 0) {
-        TXP1 = TXP2;
-        TXP3 = TXP2;
-        DVP1 = lim3(TXP1, TXP2, TXP3);
-        DVP2 = lim3(TXP2, TXP3, TXP1);
-        DVP3 = lim3(TXP3, TXP1, TXP2);
-    }
-    if (m[1] == 0 || m[2] == 0) {
-        DVP1 = (T)0;
-        DVP2 = (T)0;
-        DVP3 = (T)0;
-    }
+    const T TXP1 = v[1] - v[0], TXP2 = v[2] - v[1], TXP3 = v[3] - v[2];
+    if (!(m[0] && m[1] && m[2] && m[3])) return TXP2;
+    const T DVP1 = lim3(TXP1, TXP2, TXP3), DVP2 = lim3(TXP2, TXP3, TXP1), DVP3 = lim3(TXP3, TXP1, TXP2);
     return TXP2 - (T)1 / (T)6 * (DVP3 - (T)2 * DVP2 + DVP1);
 }
 template <typename T> __device__ __forceinline__ T vl_guard(T t) {
@@ -451,21 +444,29 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
     const int di = DIR == 0 ? 1 : 0, dj = DIR == 0 ? 0 : 1;
     const T *src[7] = {f.U, f.V, f.HU, f.HV, f.Eta, f.U4, f.V4};
     const int nvar = g.dispersion ? 7 : 5;
+    // 32-bit offsets: the arena planes hold fewer than 2^31 elements
+    const int stride = DIR == 0 ? 1 : g.pitch;
     for (int k = own; k < NB + 2; k += NB) {
         const int p = base + k;
         if (line_ok && p >= lo - 1 && p <= hi + 2) {
             const int ci = DIR == 0 ? p : i, cj = DIR == 0 ? j : p;
+            const int o0 = ci + cj * g.pitch - 2 * stride;
             int m[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) m[q] = f.MASK[IDX(ci + (q - 2) * di, cj + (q - 2) * dj)];
-            for (int vv = 0; vv < nvar; vv++) {
-                T v[4];
+            for (int q = 0; q < 4; q++) m[q] = f.MASK[o0 + q * stride];
 #pragma unroll
-                for (int q = 0; q < 4; q++) v[q] = src[vv][IDX(ci + (q - 2) * di, cj + (q - 2) * dj)];
-                din[vv][line][k] = ho_din(v, m);
+            for (int vv = 0; vv < 7; vv++) {
+                if (vv < nvar) {
+                    T v[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) v[q] = src[vv][o0 + q * stride];
+                    din[vv][line][k] = ho_din(v, m);
+                }
             }
         }
     }
+    (void)di;
+    (void)dj;
     __syncthreads();
     if (DIR == 0) {
         if (i > g.ie + 1 || j > g.je) return;
@@ -473,10 +474,11 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
         if (i > g.ie || j > g.je + 1) return;
     }
     const T g1 = GC(gamma1), g3 = GC(gamma3);
-    const size_t fid = IDX(i, j);
-    const size_t cm = DIR == 0 ? IDX(i - 1, j) : IDX(i, j - 1);  // cell pos-1 (cell pos is fid)
+    const int fid = i + j * g.pitch;
+    const int cm = fid - stride;  // cell pos-1 (cell pos is fid)
     const int kf = own + 1;
     T Lv[7], Rv[7];
+#pragma unroll
     for (int vv = 0; vv < 7; vv++) {
         if (vv >= nvar) {
             Lv[vv] = (T)0;
@@ -770,8 +772,8 @@ __global__ void __launch_bounds__(256, 3) k_update(Grid g, Fields<T> f, T al, T 
 #undef LDU
         }
         const T fg = g.f_gamma1 * m9, rH = (T)1 / tmax(H, mf);
-        f.rhs_x[id] = (double)(ubar * mk * rH + fg * (g.f_hb1 * dep * dep * Vxy - g.f_b2 * dep * DVxy));
-        f.rhs_y[id] = (double)(vbar * mk * rH + fg * (g.f_hb1 * dep * dep * Uxy - g.f_b2 * dep * DUxy));
+        f.rhs_x[id] = ubar * mk * rH + fg * (g.f_hb1 * dep * dep * Vxy - g.f_b2 * dep * DVxy);
+        f.rhs_y[id] = vbar * mk * rH + fg * (g.f_hb1 * dep * dep * Uxy - g.f_b2 * dep * DUxy);
     }
 }
 
@@ -915,8 +917,7 @@ __global__ void __launch_bounds__(128) k_tri_a(Grid g, Fields<T> f, LinePart lp)
             f.ty[q] = yp;
             f.tp[q] = pp;
             f.tq[q] = qp;
-            // keep c' for the backward sweep in rhs_x/rhs_y of this row
-            (DIR == 0 ? f.rhs_x : f.rhs_y)[q] = cp;
+            f.tc[q] = cp;  // c' for the backward sweep
         }
         // backward sweep
         double yn = 0.0, pn = 0.0, qn = 0.0;
@@ -925,7 +926,7 @@ __global__ void __launch_bounds__(128) k_tri_a(Grid g, Fields<T> f, LinePart lp)
             int ii, jj;
             line_cell<DIR>(g, l, k, ii, jj);
             const size_t q = IDX(ii, jj);
-            const double cpk = (DIR == 0 ? f.rhs_x : f.rhs_y)[q];
+            const double cpk = f.tc[q];
             const double yk = f.ty[q] - cpk * yn;
             const double pk = f.tp[q] - cpk * pn;
             const double qk = f.tq[q] - cpk * qn;
@@ -1143,15 +1144,23 @@ __global__ void __launch_bounds__(128) k_thomas(Grid g, Fields<T> f, LinePart lp
 }
 
 // Mixed path: the tridiagonal matrices depend on Depth and MASK9 only, so
-// their partitioned factorisation is computed when MASK9 has changed (never
-// again once viscosity breaking has set MASK9 = 1 on the ring) and each
-// stage runs only the substitutions for its right-hand side.
+// their partitioned factorisation is computed (in double) when MASK9 has
+// changed - never again once viscosity breaking has set MASK9 = 1 on the
+// ring - and stored rounded to float.  Each stage then solves in float and
+// refines once: x0 = S(d), r = d - T x0 with a compensated (float-pair)
+// residual, x = x0 + S(r).  S is the partitioned substitution: per chunk of
+// m rows a forward/backward sweep, a reduced system of two rows per chunk,
+// and the interior recovery x_k = y_k - p_k x_s - q_k x_e.  For periodic y,
+// S applies TRIDy_periodic's end-row scaling and Sherman-Morrison
+// combination, whose result solves the cyclic system
+// x0 + c0 x1 + a0 x(L-1) = d0, a(L-1) x(L-2) + x(L-1) + c(L-1) x0 = d(L-1)
+// (tridiagnal.F:59-325); the residual uses that cyclic operator.
 struct FacLine {
-    double *lo, *invden, *cpr, *cs, *ae, *x2, *tail;  // tail: c_end, a_beg, den_beta
+    float *lo, *invden, *cpr, *cs, *ae, *x2, *tail;  // tail: c_end, a_beg, den_beta
 };
-__device__ __forceinline__ FacLine fac_line(double *base, const LinePart &lp, int l) {
+__device__ __forceinline__ FacLine fac_line(float *base, const LinePart &lp, int l) {
     const int n = 2 * lp.P;
-    double *b = base + (size_t)l * (size_t)(4 * n + 2 * lp.P + 3);
+    float *b = base + (size_t)l * (size_t)(4 * n + 2 * lp.P + 3);
     FacLine f;
     f.lo = b;
     f.invden = b + n;
@@ -1163,7 +1172,7 @@ __device__ __forceinline__ FacLine fac_line(double *base, const LinePart &lp, in
     return f;
 }
 
-// coefficients a, c and 1/tmp2 of one row (no right-hand side)
+// normalised a, c and 1/tmp2 of one row, in double (no right-hand side)
 template <typename T, int DIR>
 __device__ __forceinline__ void tri_ac(const Grid &g, const Fields<T> &f, int i, int j, double &a, double &c,
                                        double &it) {
@@ -1181,6 +1190,7 @@ __device__ __forceinline__ void tri_ac(const Grid &g, const Fields<T> &f, int i,
     c = tmp3 * it;
 }
 
+// a, c of row k with the periodic end-row scaling (tridiagnal.F:168-173)
 template <typename T, int DIR, bool PER>
 __device__ __forceinline__ void tri_ac_row(const Grid &g, const Fields<T> &f, const LinePart &lp, int l, int k,
                                            double &a, double &c, double &it) {
@@ -1192,9 +1202,14 @@ __device__ __forceinline__ void tri_ac_row(const Grid &g, const Fields<T> &f, co
         int i2, j2;
         line_cell<DIR>(g, l, k == 0 ? lp.L - 1 : 0, i2, j2);
         tri_ac<T, DIR>(g, f, i2, j2, a2, c2, it2);
-        if (k == 0) c = c / (1 + c2);        // c_end
-        else a = a / (1 + a2);                // a_beg
+        if (k == 0) c = c / (1 + c2);   // c_end
+        else a = a / (1 + a2);           // a_beg
     }
+}
+
+__device__ __forceinline__ void split2(double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
 }
 
 template <typename T, int DIR, bool PER>
@@ -1206,23 +1221,35 @@ __global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp)
     chunk_of<DIR>(lp, t, l, ch);
     const int s = ch * lp.m;
     const int e = (ch == lp.P - 1) ? lp.L - 1 : s + lp.m - 1;
-    double *it_ = f.fac_it[DIR], *r_ = f.fac_r[DIR], *lr_ = f.fac_lr[DIR], *cp_ = f.fac_cp[DIR];
-    double *p_ = f.fac_p[DIR], *q_ = f.fac_q[DIR];
+    float *it_ = f.fac_it[DIR], *A_ = f.fac_A[DIR], *lr_ = f.fac_lr[DIR], *cp_ = f.fac_cp[DIR];
+    float *p_ = f.fac_p[DIR], *q_ = f.fac_q[DIR];
+    // the unscaled normalised coefficients of every row, for the residual
+    for (int k = s; k <= e; k++) {
+        double a, c, it;
+        int i, j;
+        line_cell<DIR>(g, l, k, i, j);
+        tri_ac<T, DIR>(g, f, i, j, a, c, it);
+        if (!PER && k == 0) a = 0.0;
+        if (!PER && k == lp.L - 1) c = 0.0;
+        const size_t q = IDX(i, j);
+        split2(a, f.fac_ah[DIR][q], f.fac_al[DIR][q]);
+        split2(c, f.fac_ch[DIR][q], f.fac_cl[DIR][q]);
+        it_[q] = (float)it;
+    }
     double as, cs, its, ae, ce, ite;
     tri_ac_row<T, DIR, PER>(g, f, lp, l, s, as, cs, its);
     tri_ac_row<T, DIR, PER>(g, f, lp, l, e, ae, ce, ite);
     int i, j;
     line_cell<DIR>(g, l, s, i, j);
-    it_[IDX(i, j)] = its;
-    if (DIR == 0) r_[IDX(i, j)] = its;   // x lines: A = 1/tmp2 at chunk ends
+    A_[IDX(i, j)] = 1.0f;
     line_cell<DIR>(g, l, e, i, j);
-    it_[IDX(i, j)] = ite;
-    if (DIR == 0) r_[IDX(i, j)] = ite;
+    A_[IDX(i, j)] = 1.0f;
     if (s == 0) as = 0.0;
     if (e == lp.L - 1) ce = 0.0;
     double lo_s, di_s, up_s, lo_e, di_e, up_e;
     if (e - s >= 2) {
         double cp = 0.0, pp = 0.0, qp = 0.0;
+        double *pbuf = f.tp, *qbuf = f.tq, *cbuf = f.tc;  // double scratch of the sweep
         for (int k = s + 1; k <= e - 1; k++) {
             double a, c, it;
             tri_ac_row<T, DIR, PER>(g, f, lp, l, k, a, c, it);
@@ -1234,21 +1261,21 @@ __global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp)
             qp = ((k == e - 1 ? c : 0.0) - lower * qp) * r;
             line_cell<DIR>(g, l, k, i, j);
             const size_t q = IDX(i, j);
-            it_[q] = it;
-            r_[q] = DIR == 0 ? it * r : r;  // x lines: A = r/tmp2 (d*r in one product)
-            lr_[q] = lower * r;
-            cp_[q] = cp;
-            p_[q] = pp;
-            q_[q] = qp;
+            A_[q] = (float)r;
+            lr_[q] = (float)(lower * r);
+            cp_[q] = (float)cp;
+            cbuf[q] = cp;
+            pbuf[q] = pp;
+            qbuf[q] = qp;
         }
         double pn = 0.0, qn = 0.0, p1 = 0.0, q1 = 0.0, pl = 0.0, ql = 0.0;
         for (int k = e - 1; k >= s + 1; k--) {
             line_cell<DIR>(g, l, k, i, j);
             const size_t q = IDX(i, j);
-            const double cpk = cp_[q];
-            const double pk = p_[q] - cpk * pn, qk = q_[q] - cpk * qn;
-            p_[q] = pk;
-            q_[q] = qk;
+            const double cpk = cbuf[q];
+            const double pk = pbuf[q] - cpk * pn, qk = qbuf[q] - cpk * qn;
+            p_[q] = (float)pk;
+            q_[q] = (float)qk;
             pn = pk;
             qn = qk;
             if (k == e - 1) {
@@ -1274,7 +1301,7 @@ __global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp)
         di_e = 1.0;
         up_e = ce;
     }
-    // reduced rows go to the reduced-system scratch; k_fac_b factors them
+    // reduced rows to the double scratch; k_fac_b factors them
     double *red = f.red + ((size_t)l * 2 * lp.P + 2 * ch) * 6;
     red[0] = lo_s;
     red[1] = di_s;
@@ -1283,8 +1310,8 @@ __global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp)
     red[7] = di_e;
     red[8] = up_e;
     FacLine fl = fac_line(f.fac_red[DIR], lp, l);
-    fl.cs[ch] = (e - s >= 2) ? cs : 0.0;
-    fl.ae[ch] = (e - s >= 2) ? ae : 0.0;
+    fl.cs[ch] = (e - s >= 2) ? (float)cs : 0.0f;
+    fl.ae[ch] = (e - s >= 2) ? (float)ae : 0.0f;
 }
 
 template <typename T, int DIR, bool PER>
@@ -1293,16 +1320,19 @@ __global__ void __launch_bounds__(128) k_fac_b(Grid g, Fields<T> f, LinePart lp)
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= lp.nlines) return;
     const int n = 2 * lp.P;
-    const double *red = f.red + (size_t)l * n * 6;
+    double *red = f.red + (size_t)l * n * 6;
     FacLine fl = fac_line(f.fac_red[DIR], lp, l);
     double cpr = 0.0;
     for (int k = 0; k < n; k++) {
         const double lo = (k > 0) ? red[k * 6 + 0] : 0.0;
         const double id = 1.0 / (red[k * 6 + 1] - lo * cpr);
         cpr = (k < n - 1 ? red[k * 6 + 2] : 0.0) * id;
-        fl.lo[k] = lo;
-        fl.invden[k] = id;
-        fl.cpr[k] = cpr;
+        fl.lo[k] = (float)lo;
+        fl.invden[k] = (float)id;
+        fl.cpr[k] = (float)cpr;
+        red[k * 6 + 3] = lo;   // double copies for the periodic solve below
+        red[k * 6 + 4] = id;
+        red[k * 6 + 5] = cpr;
     }
     if (PER) {
         // the second periodic solution (right-hand side e of TRIDy_periodic,
@@ -1318,24 +1348,48 @@ __global__ void __launch_bounds__(128) k_fac_b(Grid g, Fields<T> f, LinePart lp)
         double z = 0.0;
         for (int k = 0; k < n; k++) {
             const double rhs = k == 0 ? 1.0 / (1.0 + c_end) : (k == n - 1 ? -1.0 / (1.0 + a_beg) : 0.0);
-            z = (rhs - fl.lo[k] * z) * fl.invden[k];
-            fl.x2[k] = z;
+            z = (rhs - red[k * 6 + 3] * z) * red[k * 6 + 4];
+            red[k * 6 + 0] = z;
         }
-        double x = 0.0;
+        double x = 0.0, x0 = 0.0, xl = 0.0;
         for (int k = n - 1; k >= 0; k--) {
-            x = fl.x2[k] - fl.cpr[k] * x;
-            fl.x2[k] = x;
+            x = red[k * 6 + 0] - red[k * 6 + 5] * x;
+            fl.x2[k] = (float)x;
+            if (k == n - 1) xl = x;
+            if (k == 0) x0 = x;
         }
-        fl.tail[0] = c_end;
-        fl.tail[1] = a_beg;
-        fl.tail[2] = 1.0 - (c_end * fl.x2[0] - a_beg * fl.x2[n - 1]);
+        fl.tail[0] = (float)c_end;
+        fl.tail[1] = (float)a_beg;
+        fl.tail[2] = (float)(1.0 - (c_end * x0 - a_beg * xl));
     }
 }
 
 static __global__ void k_fac_clear(int *dirty) { *dirty = 0; }
 
-// per stage: right-hand side, chunk forward/backward substitution
-template <typename T, int DIR, bool PER>
+// compensated r = d - (a x(k-1) + x(k) + c x(k+1)) with a = ah + al, c = ch + cl
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+    p = a * b;
+    e = fmaf(a, b, -p);
+}
+__device__ __forceinline__ float residual(float d, float x, float xm, float xp, float ah, float al, float ch,
+                                          float cl) {
+    float t, e1, u, e2, v, e3, t2, e4, t3, e5;
+    two_sum(d, -x, t, e1);
+    two_prod(ah, xm, u, e2);
+    two_prod(ch, xp, v, e3);
+    two_sum(t, -u, t2, e4);
+    two_sum(t2, -v, t3, e5);
+    return t3 + ((((e1 + e4) + e5) - e2) - e3 - al * xm - cl * xp);
+}
+
+// y lines (and the periodic direction): per-chunk kernels, coalesced across
+// neighbouring lines.  PASS 0 solves d = rhs/tmp2, PASS 1 the residual.
+template <typename T, int DIR, bool PER, int PASS>
 __global__ void __launch_bounds__(128) k_sol_a(Grid g, Fields<T> f, LinePart lp) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= lp.nlines * lp.P) return;
@@ -1343,40 +1397,42 @@ __global__ void __launch_bounds__(128) k_sol_a(Grid g, Fields<T> f, LinePart lp)
     chunk_of<DIR>(lp, t, l, ch);
     const int s = ch * lp.m;
     const int e = (ch == lp.P - 1) ? lp.L - 1 : s + lp.m - 1;
-    const double *rhs = DIR == 0 ? f.rhs_x : f.rhs_y;
-    const double *it_ = f.fac_it[DIR], *r_ = f.fac_r[DIR], *lr_ = f.fac_lr[DIR], *cp_ = f.fac_cp[DIR];
+    const T *rhs = DIR == 0 ? f.rhs_x : f.rhs_y;
+    const float *it_ = f.fac_it[DIR], *A_ = f.fac_A[DIR], *lr_ = f.fac_lr[DIR], *cp_ = f.fac_cp[DIR];
+    float *ys = (float *)f.ty;   // y of this pass
+    const float *rr = (const float *)f.tq;  // residual (PASS 1)
     FacLine fl = fac_line(f.fac_red[DIR], lp, l);
-    double sc0 = 1.0, sc1 = 1.0;
+    float sc0 = 1.0f, sc1 = 1.0f;
     if (PER) {
-        sc0 = 1.0 / (1.0 + fl.tail[0]);  // row 0: d / (1 + c_end)
-        sc1 = 1.0 / (1.0 + fl.tail[1]);  // row L-1: d / (1 + a_beg)
+        sc0 = 1.0f / (1.0f + fl.tail[0]);  // row 0: d / (1 + c_end)
+        sc1 = 1.0f / (1.0f + fl.tail[1]);  // row L-1: d / (1 + a_beg)
     }
     auto dval = [&](int k, size_t q) {
-        double d = rhs[q] * it_[q];
+        float d = PASS == 0 ? (float)rhs[q] * it_[q] : rr[q];
         if (PER && k == 0) d *= sc0;
         if (PER && k == lp.L - 1) d *= sc1;
         return d;
     };
     int i, j;
     line_cell<DIR>(g, l, s, i, j);
-    const double ds = dval(s, IDX(i, j));
+    const float ds = dval(s, IDX(i, j));
     line_cell<DIR>(g, l, e, i, j);
-    const double de = dval(e, IDX(i, j));
-    double rs = ds, re = de;
+    const float de = dval(e, IDX(i, j));
+    float rs = ds, re = de;
     if (e - s >= 2) {
-        double yp = 0.0;
+        float yp = 0.0f;
         for (int k = s + 1; k <= e - 1; k++) {
             line_cell<DIR>(g, l, k, i, j);
             const size_t q = IDX(i, j);
-            yp = dval(k, q) * r_[q] - lr_[q] * yp;
-            f.ty[q] = yp;
+            yp = dval(k, q) * A_[q] - lr_[q] * yp;
+            ys[q] = yp;
         }
-        double yn = 0.0, y1 = 0.0, yl = 0.0;
+        float yn = 0.0f, y1 = 0.0f, yl = 0.0f;
         for (int k = e - 1; k >= s + 1; k--) {
             line_cell<DIR>(g, l, k, i, j);
             const size_t q = IDX(i, j);
-            const double yk = f.ty[q] - cp_[q] * yn;
-            f.ty[q] = yk;
+            const float yk = ys[q] - cp_[q] * yn;
+            ys[q] = yk;
             yn = yk;
             if (k == e - 1) yl = yk;
             if (k == s + 1) y1 = yk;
@@ -1384,9 +1440,9 @@ __global__ void __launch_bounds__(128) k_sol_a(Grid g, Fields<T> f, LinePart lp)
         rs = ds - fl.cs[ch] * y1;
         re = de - fl.ae[ch] * yl;
     }
-    double *red = f.red + ((size_t)l * 2 * lp.P + 2 * ch) * 6;
-    red[3] = rs;
-    red[9] = re;
+    float *red = (float *)f.red + ((size_t)l * 2 * lp.P + 2 * ch);
+    red[0] = rs;
+    red[1] = re;
 }
 
 template <typename T, int DIR, bool PER>
@@ -1394,18 +1450,17 @@ __global__ void __launch_bounds__(128) k_sol_b(Grid g, Fields<T> f, LinePart lp)
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= lp.nlines) return;
     const int n = 2 * lp.P;
-    double *red = f.red + (size_t)l * n * 6;
+    float *red = (float *)f.red + (size_t)l * n;
     FacLine fl = fac_line(f.fac_red[DIR], lp, l);
-    // n = 2P is even; batches of up to 8 rows load before they compute
     constexpr int B = 8;
-    double z = 0.0;
+    float z = 0.0f;
     for (int k0 = 0; k0 < n; k0 += B) {
-        double rb[B], lb[B], ib[B];
+        float rb[B], lb[B], ib[B];
         const int nb = min(B, n - k0);
 #pragma unroll
         for (int u = 0; u < B; u++)
             if (u < nb) {
-                rb[u] = red[(k0 + u) * 6 + 3];
+                rb[u] = red[k0 + u];
                 lb[u] = fl.lo[k0 + u];
                 ib[u] = fl.invden[k0 + u];
             }
@@ -1413,33 +1468,34 @@ __global__ void __launch_bounds__(128) k_sol_b(Grid g, Fields<T> f, LinePart lp)
         for (int u = 0; u < B; u++)
             if (u < nb) {
                 z = (rb[u] - lb[u] * z) * ib[u];
-                red[(k0 + u) * 6 + 3] = z;
+                red[k0 + u] = z;
             }
     }
-    double x = 0.0;
+    float x = 0.0f;
     for (int k1 = n; k1 > 0; k1 -= B) {
-        double zb[B], cb[B];
+        float zb[B], cb[B];
         const int nb = min(B, k1);
 #pragma unroll
         for (int u = 0; u < B; u++)
             if (u < nb) {
-                zb[u] = red[(k1 - 1 - u) * 6 + 3];
+                zb[u] = red[k1 - 1 - u];
                 cb[u] = fl.cpr[k1 - 1 - u];
             }
 #pragma unroll
         for (int u = 0; u < B; u++)
             if (u < nb) {
                 x = zb[u] - cb[u] * x;
-                red[(k1 - 1 - u) * 6 + 3] = x;
+                red[k1 - 1 - u] = x;
             }
     }
     if (PER) {
-        const double beta = (fl.tail[0] * red[3] - fl.tail[1] * red[(size_t)(n - 1) * 6 + 3]) / fl.tail[2];
-        for (int k = 0; k < n; k++) red[k * 6 + 3] += beta * fl.x2[k];
+        const float beta = (fl.tail[0] * red[0] - fl.tail[1] * red[n - 1]) / fl.tail[2];
+        for (int k = 0; k < n; k++) red[k] += beta * fl.x2[k];
     }
 }
 
-template <typename T, int DIR>
+// PASS 0: x0 -> tp scratch; PASS 1: out = x0 + correction
+template <typename T, int DIR, int PASS>
 __global__ void __launch_bounds__(128) k_sol_c(Grid g, Fields<T> f, LinePart lp) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= lp.nlines * lp.P) return;
@@ -1447,97 +1503,126 @@ __global__ void __launch_bounds__(128) k_sol_c(Grid g, Fields<T> f, LinePart lp)
     chunk_of<DIR>(lp, t, l, ch);
     const int s = ch * lp.m;
     const int e = (ch == lp.P - 1) ? lp.L - 1 : s + lp.m - 1;
-    const double *red = f.red + ((size_t)l * 2 * lp.P + 2 * ch) * 6;
-    const double xs = red[3], xe = red[9];
-    const double *p_ = f.fac_p[DIR], *q_ = f.fac_q[DIR];
+    const float *red = (const float *)f.red + ((size_t)l * 2 * lp.P + 2 * ch);
+    const float xs = red[0], xe = red[1];
+    const float *p_ = f.fac_p[DIR], *q_ = f.fac_q[DIR];
+    const float *ys = (const float *)f.ty;
+    float *x0 = (float *)f.tp;
     T *out = DIR == 0 ? f.U : f.V;
-    int i, j;
-    line_cell<DIR>(g, l, s, i, j);
-    out[IDX(i, j)] = (T)xs;
-    line_cell<DIR>(g, l, e, i, j);
-    out[IDX(i, j)] = (T)xe;
-    for (int k = s + 1; k <= e - 1; k++) {
+    for (int k = s; k <= e; k++) {
+        int i, j;
         line_cell<DIR>(g, l, k, i, j);
         const size_t q = IDX(i, j);
-        out[q] = (T)(f.ty[q] - p_[q] * xs - q_[q] * xe);
+        const float x = (k == s) ? xs : (k == e) ? xe : ys[q] - p_[q] * xs - q_[q] * xe;
+        if (PASS == 0) x0[q] = x;
+        else out[q] = (T)(x0[q] + x);
     }
 }
 
-// x lines, one block per line: every global access is unit-stride across
-// the block; the right-hand side and the sweeps live in shared memory.
-//   y_k = rhs_k * A_k        (coalesced; A from k_fac_a)
-//   per chunk: forward  y_k -= lr_k * y_{k-1},  backward y_k -= c'_k * y_{k+1}
-//   reduced system (thread 0), then x_k = y_k - p_k x_s - q_k x_e (coalesced)
+// compensated residual of the first solve on every interior cell
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(256) k_resid(Grid g, Fields<T> f, LinePart lp) {
+    const int i = g.ib + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = g.jb + blockIdx.y * blockDim.y + threadIdx.y;
+    if (i > g.ie || j > g.je) return;
+    const size_t q = IDX(i, j);
+    const int k = DIR == 0 ? i - g.ib : j - g.jb;
+    const size_t st = DIR == 0 ? 1 : (size_t)g.pitch;
+    const float *x0 = (const float *)f.tp;
+    const T *rhs = DIR == 0 ? f.rhs_x : f.rhs_y;
+    const float d = (float)rhs[q] * f.fac_it[DIR][q];
+    // neighbours along the line; the cyclic ends wrap in periodic y
+    float xm = 0.0f, xp = 0.0f;
+    if (k > 0) xm = x0[q - st];
+    else if (PER) xm = x0[q + (size_t)(lp.L - 1) * st];
+    if (k < lp.L - 1) xp = x0[q + st];
+    else if (PER) xp = x0[q - (size_t)(lp.L - 1) * st];
+    ((float *)f.tq)[q] = residual(d, x0[q], xm, xp, f.fac_ah[DIR][q], f.fac_al[DIR][q], f.fac_ch[DIR][q],
+                                  f.fac_cl[DIR][q]);
+}
+
+// x lines, one block per line, everything unit-stride: load d, solve, form
+// the compensated residual, solve again and write x0 + correction
 template <typename T>
 __global__ void __launch_bounds__(128) k_linesolve_x(Grid g, Fields<T> f, LinePart lp) {
-    extern __shared__ double sh[];
+    extern __shared__ float shf[];
     const int l = blockIdx.x;
     const int L = lp.L, P = lp.P, m = lp.m;
-    double *y = sh;            // L
-    double *bb = sh + L;       // L: lr, then c'
-    double *rr = sh + 2 * L;   // 2P reduced right-hand sides / solution
+    float *d = shf;            // L  right-hand side, then residual
+    float *y = shf + L;        // L  sweep values
+    float *x0 = shf + 2 * L;   // L  first solution
+    float *A = shf + 3 * L;    // L  sweep constants, staged with unit-stride loads
+    float *LR = shf + 4 * L;   // L
+    float *CP = shf + 5 * L;   // L
+    float *rr = shf + 6 * L;   // 2P reduced right-hand sides / solution
     const int j = g.jb + l;
     const size_t row = (size_t)j * g.pitch + g.ib;
-    const double *rhs = f.rhs_x + row, *A = f.fac_r[0] + row, *B = f.fac_lr[0] + row;
-    for (int k = threadIdx.x; k < L; k += blockDim.x) {
-        y[k] = rhs[k] * A[k];
-        bb[k] = B[k];
-    }
-    __syncthreads();
+    const T *rhs = f.rhs_x + row;
+    const float *IT = f.fac_it[0] + row, *Pp = f.fac_p[0] + row, *Qq = f.fac_q[0] + row;
+    FacLine fl = fac_line(f.fac_red[0], lp, l);
     const int ch = threadIdx.x;
     const int s = ch * m;
     const int e = (ch == P - 1) ? L - 1 : s + m - 1;
-    if (ch < P && e - s >= 2) {
-        double yp = 0.0;
-        for (int k = s + 1; k <= e - 1; k++) {
-            yp = y[k] - bb[k] * yp;
-            y[k] = yp;
-        }
-    }
-    __syncthreads();
-    const double *CP = f.fac_cp[0] + row;
-    for (int k = threadIdx.x; k < L; k += blockDim.x) bb[k] = CP[k];
-    __syncthreads();
-    FacLine fl = fac_line(f.fac_red[0], lp, l);
-    if (ch < P) {
-        double rs = y[s], re = y[e];
-        if (e - s >= 2) {
-            double yn = 0.0;
-            for (int k = e - 1; k >= s + 1; k--) {
-                yn = y[k] - bb[k] * yn;
-                y[k] = yn;
-            }
-            rs = y[s] - fl.cs[ch] * y[s + 1];
-            re = y[e] - fl.ae[ch] * y[e - 1];
-        }
-        rr[2 * ch] = rs;
-        rr[2 * ch + 1] = re;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const int n = 2 * P;
-        double z = 0.0;
-        for (int k = 0; k < n; k++) {
-            z = (rr[k] - fl.lo[k] * z) * fl.invden[k];
-            rr[k] = z;
-        }
-        double x = 0.0;
-        for (int k = n - 1; k >= 0; k--) {
-            x = rr[k] - fl.cpr[k] * x;
-            rr[k] = x;
-        }
-    }
-    __syncthreads();
-    const double *Pp = f.fac_p[0] + row, *Qq = f.fac_q[0] + row;
-    T *out = f.U + row;
     for (int k = threadIdx.x; k < L; k += blockDim.x) {
-        const int c = min(k / m, P - 1);
-        const int cs = c * m, ce = (c == P - 1) ? L - 1 : cs + m - 1;
-        double x;
-        if (k == cs) x = rr[2 * c];
-        else if (k == ce) x = rr[2 * c + 1];
-        else x = y[k] - Pp[k] * rr[2 * c] - Qq[k] * rr[2 * c + 1];
-        out[k] = (T)x;
+        d[k] = (float)rhs[k] * IT[k];
+        A[k] = f.fac_A[0][row + k];
+        LR[k] = f.fac_lr[0][row + k];
+        CP[k] = f.fac_cp[0][row + k];
+    }
+    __syncthreads();
+    for (int pass = 0; pass < 2; pass++) {
+        // chunk forward/backward sweeps; the constants stream from L1/L2
+        if (ch < P) {
+            float rs = d[s], re = d[e];
+            if (e - s >= 2) {
+                float yp = 0.0f;
+                for (int k = s + 1; k <= e - 1; k++) {
+                    yp = d[k] * A[k] - LR[k] * yp;
+                    y[k] = yp;
+                }
+                float yn = 0.0f;
+                for (int k = e - 1; k >= s + 1; k--) {
+                    yn = y[k] - CP[k] * yn;
+                    y[k] = yn;
+                }
+                rs = d[s] - fl.cs[ch] * y[s + 1];
+                re = d[e] - fl.ae[ch] * y[e - 1];
+            }
+            rr[2 * ch] = rs;
+            rr[2 * ch + 1] = re;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int n = 2 * P;
+            float z = 0.0f;
+            for (int k = 0; k < n; k++) {
+                z = (rr[k] - fl.lo[k] * z) * fl.invden[k];
+                rr[k] = z;
+            }
+            float x = 0.0f;
+            for (int k = n - 1; k >= 0; k--) {
+                x = rr[k] - fl.cpr[k] * x;
+                rr[k] = x;
+            }
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < L; k += blockDim.x) {
+            const int c = min(k / m, P - 1);
+            const int cs = c * m, ce = (c == P - 1) ? L - 1 : cs + m - 1;
+            const float x = (k == cs) ? rr[2 * c] : (k == ce) ? rr[2 * c + 1] : y[k] - Pp[k] * rr[2 * c] - Qq[k] * rr[2 * c + 1];
+            if (pass == 0) x0[k] = x;
+            else f.U[row + k] = (T)(x0[k] + x);
+        }
+        __syncthreads();
+        if (pass == 0) {
+            const float *AH = f.fac_ah[0] + row, *AL = f.fac_al[0] + row;
+            const float *CH = f.fac_ch[0] + row, *CL = f.fac_cl[0] + row;
+            for (int k = threadIdx.x; k < L; k += blockDim.x) {
+                const float xm = k > 0 ? x0[k - 1] : 0.0f, xp = k < L - 1 ? x0[k + 1] : 0.0f;
+                d[k] = residual((float)rhs[k] * IT[k], x0[k], xm, xp, AH[k], AL[k], CH[k], CL[k]);
+            }
+            __syncthreads();
+        }
     }
 }
 
@@ -2207,18 +2292,24 @@ template <typename T, int DIR, bool PER> static void launch_tri(fw_ctx *c, const
     if (c->factored) {
         k_fac_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         k_fac_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        const size_t smem = (size_t)(2 * lp.L + 2 * lp.P) * sizeof(double);
+        note(c, 2);
+        const size_t smem = (size_t)(6 * lp.L + 2 * lp.P) * sizeof(float);
         if (DIR == 0 && !PER && lp.P <= 128 && smem <= 200 * 1024) {
             if (smem > 48 * 1024)
                 cudaFuncSetAttribute(k_linesolve_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             k_linesolve_x<T><<<lp.nlines, 128, smem, c->stream>>>(g, c->F<T>(), lp);
-            note(c, 3);
+            note(c);
             return;
         }
-        k_sol_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        const dim3 gi = grid2(g.Mglob, g.Nglob, B2D);
+        k_sol_a<T, DIR, PER, 0><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         k_sol_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        k_sol_c<T, DIR><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        note(c, 5);
+        k_sol_c<T, DIR, 0><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        k_resid<T, DIR, PER><<<gi, B2D, 0, c->stream>>>(g, c->F<T>(), lp);
+        k_sol_a<T, DIR, PER, 1><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        k_sol_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        k_sol_c<T, DIR, 1><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        note(c, 7);
         return;
     }
     k_tri_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);

@@ -217,3 +217,22 @@ def test_units_mixed_precision(fw, oracle_mod, periodic):
         o.call("exchange")
         s.sponge_damping()
         o.call("sponge_damping")
+
+
+def test_mixed_vs_fp64_long_run(fw):
+    """The 250 x 500 planar beach for 300 steps (about 21 s of waves):
+    mixed precision (float fields, float line solve with one compensated
+    refinement step) against the FP64 path, which matches the oracle: eta
+    RMS over wet cells <= 1e-4 m, the benchmark spec's tolerance."""
+    p, depth, _ = fw.cases.planar_beach(seed=7)
+    d64 = fw.Solver(p, precision="FP64")
+    d64.init(depth)
+    mx = fw.Solver(p, precision="MIXED")
+    mx.init(depth)
+    d64.step(300)
+    mx.step(300)
+    e64, em = interior(d64.get("Eta")), interior(mx.get("Eta"))
+    wet = interior(d64.get("MASK")) > 0
+    rms = float(np.sqrt(np.mean((em - e64)[wet] ** 2)))
+    assert rms <= 1e-4, "eta rms %.3e" % rms
+    assert abs(d64.scalar("TIME") - mx.scalar("TIME")) < 1e-3 * d64.scalar("TIME")
