@@ -168,9 +168,9 @@ LinePart make_part(int L, int nlines) {
     LinePart lp;
     lp.L = L;
     lp.nlines = nlines;
-    // chunks of at least 16 rows and at most 64 chunks per line, so that the
-    // sequential reduced solve per line stays short
-    lp.m = std::max(16, (L + 63) / 64);
+    // chunks of at least 16 rows and at most 256 chunks per line (the
+    // reduced system of 2P rows is solved by one block)
+    lp.m = std::max(16, (L + 255) / 256);
     if (L < 2 * lp.m) {
         lp.m = L;
         lp.P = 1;

@@ -23,6 +23,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <algorithm>
 #include <cstring>
 
 #include "fw_internal.h"
@@ -1156,15 +1157,15 @@ __global__ void __launch_bounds__(128) k_thomas(Grid g, Fields<T> f, LinePart lp
 // x0 + c0 x1 + a0 x(L-1) = d0, a(L-1) x(L-2) + x(L-1) + c(L-1) x0 = d(L-1)
 // (tridiagnal.F:59-325); the residual uses that cyclic operator.
 struct FacLine {
-    float *lo, *invden, *cpr, *cs, *ae, *x2, *tail;  // tail: c_end, a_beg, den_beta
+    float *lo, *di, *up, *cs, *ae, *x2, *tail;  // reduced rows; tail: c_end, a_beg, den_beta
 };
 __device__ __forceinline__ FacLine fac_line(float *base, const LinePart &lp, int l) {
     const int n = 2 * lp.P;
     float *b = base + (size_t)l * (size_t)(4 * n + 2 * lp.P + 3);
     FacLine f;
     f.lo = b;
-    f.invden = b + n;
-    f.cpr = b + 2 * n;
+    f.di = b + n;
+    f.up = b + 2 * n;
     f.cs = b + 3 * n;
     f.ae = b + 3 * n + lp.P;
     f.x2 = b + 3 * n + 2 * lp.P;
@@ -1325,12 +1326,13 @@ __global__ void __launch_bounds__(128) k_fac_b(Grid g, Fields<T> f, LinePart lp)
     double cpr = 0.0;
     for (int k = 0; k < n; k++) {
         const double lo = (k > 0) ? red[k * 6 + 0] : 0.0;
+        const double up = (k < n - 1) ? red[k * 6 + 2] : 0.0;
         const double id = 1.0 / (red[k * 6 + 1] - lo * cpr);
-        cpr = (k < n - 1 ? red[k * 6 + 2] : 0.0) * id;
-        fl.lo[k] = (float)lo;
-        fl.invden[k] = (float)id;
-        fl.cpr[k] = (float)cpr;
-        red[k * 6 + 3] = lo;   // double copies for the periodic solve below
+        cpr = up * id;
+        fl.lo[k] = (float)lo;       // the reduced rows, solved per stage by
+        fl.di[k] = (float)red[k * 6 + 1];  // parallel cyclic reduction
+        fl.up[k] = (float)up;
+        red[k * 6 + 3] = lo;   // double factors for the periodic solve below
         red[k * 6 + 4] = id;
         red[k * 6 + 5] = cpr;
     }
@@ -1385,6 +1387,51 @@ __device__ __forceinline__ float residual(float d, float x, float xm, float xp, 
     two_sum(t, -u, t2, e4);
     two_sum(t2, -v, t3, e5);
     return t3 + ((((e1 + e4) + e5) - e2) - e3 - al * xm - cl * xp);
+}
+
+// Parallel cyclic reduction of n reduced rows lo x(k-1) + di x(k) +
+// up x(k+1) = r in shared memory by the whole block: log2(n) steps, each row
+// eliminating its neighbours at distance s; the solution replaces r.
+// Buffers: lo, di, up, r and their doubles lo2, di2, up2, r2 (n floats each).
+__device__ __forceinline__ void pcr_solve(float *lo, float *di, float *up, float *r, float *lo2, float *di2,
+                                          float *up2, float *r2, int n) {
+    for (int st = 1; st < n; st <<= 1) {
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const int km = k - st, kp = k + st;
+            float a = 0.0f, b = 0.0f, nlo = 0.0f, nup = 0.0f;
+            float nd = di[k], nr = r[k];
+            if (km >= 0) {
+                a = -lo[k] / di[km];
+                nlo = a * lo[km];
+                nd += a * up[km];
+                nr += a * r[km];
+            }
+            if (kp < n) {
+                b = -up[k] / di[kp];
+                nup = b * up[kp];
+                nd += b * lo[kp];
+                nr += b * r[kp];
+            }
+            lo2[k] = nlo;
+            di2[k] = nd;
+            up2[k] = nup;
+            r2[k] = nr;
+        }
+        __syncthreads();
+        float *t;
+        t = lo; lo = lo2; lo2 = t;
+        t = di; di = di2; di2 = t;
+        t = up; up = up2; up2 = t;
+        t = r; r = r2; r2 = t;
+    }
+    // after the last swap the current buffers may be the doubles: copy the
+    // solution into both
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const float x = r[k] / di[k];
+        r[k] = x;
+        r2[k] = x;
+    }
+    __syncthreads();
 }
 
 // y lines (and the periodic direction): per-chunk kernels, coalesced across
@@ -1446,52 +1493,24 @@ __global__ void __launch_bounds__(128) k_sol_a(Grid g, Fields<T> f, LinePart lp)
 }
 
 template <typename T, int DIR, bool PER>
-__global__ void __launch_bounds__(128) k_sol_b(Grid g, Fields<T> f, LinePart lp) {
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l >= lp.nlines) return;
+__global__ void __launch_bounds__(512) k_sol_b(Grid g, Fields<T> f, LinePart lp) {
+    extern __shared__ float shr[];
+    const int l = blockIdx.x;
     const int n = 2 * lp.P;
     float *red = (float *)f.red + (size_t)l * n;
     FacLine fl = fac_line(f.fac_red[DIR], lp, l);
-    constexpr int B = 8;
-    float z = 0.0f;
-    for (int k0 = 0; k0 < n; k0 += B) {
-        float rb[B], lb[B], ib[B];
-        const int nb = min(B, n - k0);
-#pragma unroll
-        for (int u = 0; u < B; u++)
-            if (u < nb) {
-                rb[u] = red[k0 + u];
-                lb[u] = fl.lo[k0 + u];
-                ib[u] = fl.invden[k0 + u];
-            }
-#pragma unroll
-        for (int u = 0; u < B; u++)
-            if (u < nb) {
-                z = (rb[u] - lb[u] * z) * ib[u];
-                red[k0 + u] = z;
-            }
+    float *lo = shr, *di = shr + n, *up = shr + 2 * n, *r = shr + 3 * n;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        lo[k] = fl.lo[k];
+        di[k] = fl.di[k];
+        up[k] = fl.up[k];
+        r[k] = red[k];
     }
-    float x = 0.0f;
-    for (int k1 = n; k1 > 0; k1 -= B) {
-        float zb[B], cb[B];
-        const int nb = min(B, k1);
-#pragma unroll
-        for (int u = 0; u < B; u++)
-            if (u < nb) {
-                zb[u] = red[k1 - 1 - u];
-                cb[u] = fl.cpr[k1 - 1 - u];
-            }
-#pragma unroll
-        for (int u = 0; u < B; u++)
-            if (u < nb) {
-                x = zb[u] - cb[u] * x;
-                red[k1 - 1 - u] = x;
-            }
-    }
-    if (PER) {
-        const float beta = (fl.tail[0] * red[0] - fl.tail[1] * red[n - 1]) / fl.tail[2];
-        for (int k = 0; k < n; k++) red[k] += beta * fl.x2[k];
-    }
+    __syncthreads();
+    pcr_solve(lo, di, up, r, shr + 4 * n, shr + 5 * n, shr + 6 * n, shr + 7 * n, n);
+    float beta = 0.0f;
+    if (PER) beta = (fl.tail[0] * r[0] - fl.tail[1] * r[n - 1]) / fl.tail[2];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) red[k] = PER ? r[k] + beta * fl.x2[k] : r[k];
 }
 
 // PASS 0: x0 -> tp scratch; PASS 1: out = x0 + correction
@@ -1544,7 +1563,7 @@ __global__ void __launch_bounds__(256) k_resid(Grid g, Fields<T> f, LinePart lp)
 // x lines, one block per line, everything unit-stride: load d, solve, form
 // the compensated residual, solve again and write x0 + correction
 template <typename T>
-__global__ void __launch_bounds__(128) k_linesolve_x(Grid g, Fields<T> f, LinePart lp) {
+__global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePart lp) {
     extern __shared__ float shf[];
     const int l = blockIdx.x;
     const int L = lp.L, P = lp.P, m = lp.m;
@@ -1555,6 +1574,7 @@ __global__ void __launch_bounds__(128) k_linesolve_x(Grid g, Fields<T> f, LinePa
     float *LR = shf + 4 * L;   // L
     float *CP = shf + 5 * L;   // L
     float *rr = shf + 6 * L;   // 2P reduced right-hand sides / solution
+    float *pb = shf + 6 * L + 2 * P;  // 7 x 2P PCR buffers
     const int j = g.jb + l;
     const size_t row = (size_t)j * g.pitch + g.ib;
     const T *rhs = f.rhs_x + row;
@@ -1591,21 +1611,14 @@ __global__ void __launch_bounds__(128) k_linesolve_x(Grid g, Fields<T> f, LinePa
             rr[2 * ch] = rs;
             rr[2 * ch + 1] = re;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            const int n = 2 * P;
-            float z = 0.0f;
-            for (int k = 0; k < n; k++) {
-                z = (rr[k] - fl.lo[k] * z) * fl.invden[k];
-                rr[k] = z;
-            }
-            float x = 0.0f;
-            for (int k = n - 1; k >= 0; k--) {
-                x = rr[k] - fl.cpr[k] * x;
-                rr[k] = x;
-            }
+        const int n = 2 * P;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            pb[k] = fl.lo[k];
+            pb[n + k] = fl.di[k];
+            pb[2 * n + k] = fl.up[k];
         }
         __syncthreads();
+        pcr_solve(pb, pb + n, pb + 2 * n, rr, pb + 3 * n, pb + 4 * n, pb + 5 * n, pb + 6 * n, n);
         for (int k = threadIdx.x; k < L; k += blockDim.x) {
             const int c = min(k / m, P - 1);
             const int cs = c * m, ce = (c == P - 1) ? L - 1 : cs + m - 1;
@@ -2293,21 +2306,23 @@ template <typename T, int DIR, bool PER> static void launch_tri(fw_ctx *c, const
         k_fac_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         k_fac_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         note(c, 2);
-        const size_t smem = (size_t)(6 * lp.L + 2 * lp.P) * sizeof(float);
-        if (DIR == 0 && !PER && lp.P <= 128 && smem <= 200 * 1024) {
+        const size_t smem = (size_t)(6 * lp.L + 2 * lp.P + 14 * lp.P) * sizeof(float);
+        if (DIR == 0 && !PER && lp.P <= 256 && smem <= 200 * 1024) {
             if (smem > 48 * 1024)
                 cudaFuncSetAttribute(k_linesolve_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_linesolve_x<T><<<lp.nlines, 128, smem, c->stream>>>(g, c->F<T>(), lp);
+            k_linesolve_x<T><<<lp.nlines, 256, smem, c->stream>>>(g, c->F<T>(), lp);
             note(c);
             return;
         }
         const dim3 gi = grid2(g.Mglob, g.Nglob, B2D);
         k_sol_a<T, DIR, PER, 0><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        k_sol_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        const int nb = std::min(512, ((2 * lp.P + 31) / 32) * 32);
+        const size_t sb = (size_t)16 * lp.P * sizeof(float);
+        k_sol_b<T, DIR, PER><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
         k_sol_c<T, DIR, 0><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         k_resid<T, DIR, PER><<<gi, B2D, 0, c->stream>>>(g, c->F<T>(), lp);
         k_sol_a<T, DIR, PER, 1><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        k_sol_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        k_sol_b<T, DIR, PER><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
         k_sol_c<T, DIR, 1><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         note(c, 7);
         return;
