@@ -32,6 +32,7 @@ _SOURCES = {
     "fw_kernels_f32.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
     "fw_api.cu": [],
     "fw_init.cpp": ["-Xcompiler", "-ffp-contract=off"],
+    "fw_noalloc.cu": ["-fmad=false"],
 }
 
 FW_ERRORS = {0: "FW_OK", -1: "FW_ERR_CUDA", -2: "FW_ERR_OOM", -3: "FW_ERR_BAD_PARAM",

@@ -164,6 +164,31 @@ long long fw_launch_count(fw_ctx *ctx);
 int fw_time_kernel(fw_ctx *ctx, const char *name, int nrep, double *ms_per_launch);
 /* CUDA stream of the context, as a void* (cudaStream_t). */
 void *fw_stream(fw_ctx *ctx);
+
+/* --- no device allocation ---------------------------------------------- */
+/* ESTIMATE_DT on device arrays the caller owns, allocating nothing: for
+ * callers that cannot call cudaMalloc (device arrays owned by an OpenACC or
+ * CUDA Fortran runtime, a fixed memory pool, a loop where allocation is
+ * forbidden).  No counterpart in the reference as an entry point; its
+ * arguments follow ESTIMATE_DT(M,N,DX,DY,U,V,H,MinDepthFrc,DT,CFL,TIME)
+ * (misc.F:216).
+ *   U, V, H    device pointers to contiguous Mloc x Nloc column-major double
+ *              arrays (ghost cells included, as the reference's loop covers
+ *              them), on the current CUDA device
+ *   dt_fixed   > 0 applies the DT_fixed halving, else 0
+ *   DT         device pointer, receives CFL * min(dx/(|u|+c), dy/(|v|+c))
+ *   TIME       device pointer (or NULL), TIME += DT
+ *   stream     cudaStream_t (NULL = legacy default stream)
+ * Mloc*Nloc may be at most FW_DT_DEVICE_MAX_CELLS; larger grids get
+ * FW_ERR_BAD_PARAM before anything runs.  The call's scratch is one static
+ * 512 KB device array per GPU: the first call on a device looks up its
+ * address (set-up; make that first call before any stream capture), and
+ * calls whose work overlaps on the GPU race on that array.  Asynchronous on
+ * stream; DT and TIME are valid once the stream reaches that point. */
+#define FW_DT_DEVICE_MAX_CELLS 134217728LL   /* 65536 blocks x 2048 cells */
+int fw_estimate_dt_device(int Mloc, int Nloc, double DX, double DY, const double *U, const double *V,
+                          const double *H, double MinDepthFrc, double CFL, double dt_fixed, double *DT,
+                          double *TIME, void *stream);
 /* Human-readable text of a status code. */
 const char *fw_strerror(int status);
 
