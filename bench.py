@@ -32,7 +32,7 @@ import __graft_entry__  # noqa: E402
 METRIC = "cell-steps/s (1 GB300) mixed-FP32 vs FP64 at stated eta error; ensemble runs/hr"
 UNIT = "cell-steps/s"
 WORKLOAD = ("2048x2048 1:50 slope + elliptic shoal, JON_2D Hs=1 m Tp=10 s 50x30 cos^2s, "
-            "dx=2 m, walls, west sponge (configs[1] shape, synthetic)")
+            "dx=2 m, walls, west sponge (synthetic)")
 
 # Algorithmic bytes per launch unit of each kernel: every distinct array the
 # kernel must read once plus every array it must write once (T = bytes of a
