@@ -168,6 +168,7 @@ LinePart make_part(int L, int nlines) {
     LinePart lp;
     lp.L = L;
     lp.nlines = nlines;
+    lp.red0 = 0;
     // chunks of at least 16 rows and at most 256 chunks per line (the
     // reduced system of 2P rows is solved by one block)
     lp.m = std::max(16, (L + 255) / 256);
@@ -205,7 +206,15 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
     double **df[] = {&f.ty, &f.tp, &f.tq, &f.tc};
     for (double **p : df) *p = (double *)take(plane * sizeof(double));
     f.m9_dirty = (int *)take(sizeof(int));
+    f.sw_p[0] = f.tp;
+    f.sw_q[0] = f.tq;
+    f.sw_c[0] = f.tc;
+    f.sw_p[1] = f.sw_q[1] = f.sw_c[1] = nullptr;
     if (sizeof(T) == sizeof(float)) {
+        // y factors in the same launch as x: a scratch of its own
+        f.sw_p[1] = (double *)take(plane * sizeof(double));
+        f.sw_q[1] = (double *)take(plane * sizeof(double));
+        f.sw_c[1] = (double *)take(plane * sizeof(double));
         for (int d = 0; d < 2; d++) {
             float **ff[] = {&f.fac_it[d], &f.fac_A[d], &f.fac_lr[d], &f.fac_cp[d], &f.fac_p[d],
                             &f.fac_q[d], &f.fac_ah[d], &f.fac_al[d], &f.fac_ch[d], &f.fac_cl[d]};
@@ -216,7 +225,9 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
             f.fac_red[d] = (float *)take((size_t)lp.nlines * per_line * sizeof(float));
         }
     }
-    const size_t nred = std::max((size_t)c->px.nlines * 2 * c->px.P, (size_t)c->py.nlines * 2 * c->py.P);
+    // the two directions' factorisation rows side by side (both directions
+    // are factored in one launch); the per-stage solves reuse the start
+    const size_t nred = (size_t)c->px.nlines * 2 * c->px.P + (size_t)c->py.nlines * 2 * c->py.P;
     f.red = (double *)take(nred * 6 * sizeof(double));
     f.dsc = (double *)take(S_NSLOT * sizeof(double));
     f.fsc = (float *)take(FS_NSLOT * sizeof(float));
@@ -378,6 +389,7 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     // dispersion coefficients (init.F:656-664); Gamma1/2 off without dispersion
     g.gamma1 = p->dispersion ? p->gamma1 : 0.0;
     g.gamma2 = p->dispersion ? p->gamma2 : 0.0;
+    g.has_g2 = g.gamma2 > 0.0 ? 1 : 0;
     g.gamma3 = p->gamma3;
     g.b1 = p->beta_ref * p->beta_ref;
     g.b2 = p->beta_ref;
@@ -416,6 +428,8 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     fill_float_constants(g);
     c->px = make_part(p->Mglob, p->Nglob);
     c->py = make_part(p->Nglob, p->Mglob);
+    c->px.red0 = 0;
+    c->py.red0 = (long long)c->px.nlines * 2 * c->px.P * 6;
     c->ncand_cap = (p->Mglob + 2) * (p->Nglob + 2);
     // the factored solve assumes tmp2 = 1 + Gamma1*MASK9*(-b1-2*b2)/h^2*dep^2
     // never vanishes, which holds for -b1-2*b2 >= 0 (Beta_ref in [-2, 0])
@@ -454,7 +468,7 @@ int fw_destroy(fw_ctx *c) {
     if (!c) return FW_ERR_BAD_PARAM;
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->graph) cudaGraphExecDestroy(c->graph);
-    void *band[4] = {c->fd.Cm, c->fd.Sm, c->ff.Cm, c->ff.Sm};
+    void *band[4] = {(void *)c->fd.Cm, (void *)c->fd.Sm, (void *)c->ff.Cm, (void *)c->ff.Sm};
     for (void *b : band)
         if (b) cudaFree(b);
     if (c->arena) cudaFree(c->arena);
@@ -504,21 +518,31 @@ int fw_init(fw_ctx *c, const double *depth, const double *eta, const double *u, 
     }
     // JON_2D band tables
     if (c->p.wavemaker == FW_WK_JON_2D && !hc.Cm.empty()) {
-        const size_t nb = hc.Cm.size() * sizeof(double);
-        double *Cm = nullptr, *Sm = nullptr;
+        // stored in the field precision: the mixed path sums them in float
+        const bool d = c->p.precision == FW_PREC_FP64;
+        const size_t es = d ? sizeof(double) : sizeof(float);
+        const size_t nb = hc.Cm.size() * es;
+        void *Cm = nullptr, *Sm = nullptr;
         if (cudaMalloc(&Cm, nb) != cudaSuccess || cudaMalloc(&Sm, nb) != cudaSuccess) {
             cudaGetLastError();
             if (Cm) cudaFree(Cm);
             return FW_ERR_OOM;
         }
-        double **dCm = c->p.precision == FW_PREC_FP64 ? &c->fd.Cm : &c->ff.Cm;
-        double **dSm = c->p.precision == FW_PREC_FP64 ? &c->fd.Sm : &c->ff.Sm;
-        if (*dCm) cudaFree(*dCm);
-        if (*dSm) cudaFree(*dSm);
-        *dCm = Cm;
-        *dSm = Sm;
-        if ((rc = upload_array(c, Cm, hc.Cm.data(), nb)) != FW_OK) return rc;
-        if ((rc = upload_array(c, Sm, hc.Sm.data(), nb)) != FW_OK) return rc;
+        void *oldc = d ? (void *)c->fd.Cm : (void *)c->ff.Cm, *olds = d ? (void *)c->fd.Sm : (void *)c->ff.Sm;
+        if (oldc) cudaFree(oldc);
+        if (olds) cudaFree(olds);
+        if (d) {
+            c->fd.Cm = (double *)Cm;
+            c->fd.Sm = (double *)Sm;
+            if ((rc = upload_array(c, Cm, hc.Cm.data(), nb)) != FW_OK) return rc;
+            if ((rc = upload_array(c, Sm, hc.Sm.data(), nb)) != FW_OK) return rc;
+        } else {
+            c->ff.Cm = (float *)Cm;
+            c->ff.Sm = (float *)Sm;
+            std::vector<float> tc(hc.Cm.begin(), hc.Cm.end()), ts(hc.Sm.begin(), hc.Sm.end());
+            if ((rc = upload_array(c, Cm, tc.data(), nb)) != FW_OK) return rc;
+            if ((rc = upload_array(c, Sm, ts.data(), nb)) != FW_OK) return rc;
+        }
         double *om = c->p.precision == FW_PREC_FP64 ? c->fd.omega : c->ff.omega;
         if ((rc = upload_array(c, om, hc.omega.data(), hc.omega.size() * sizeof(double))) != FW_OK) return rc;
     }

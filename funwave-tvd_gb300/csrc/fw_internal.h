@@ -25,6 +25,7 @@ struct Grid {
     int direct_sponge, friction_sponge, eta_limiter, wavemaker;
     int ilo, ihi, jlo, jhi;  // 0-based wavemaker band (empty when ilo > ihi)
     int nfreq;
+    int has_g2;              // Gamma2 > 0 (the dispersive ETAx/ETAy exchange)
     double DX, DY;
     double gamma1, gamma2, gamma3, b1, b2, Beta_1, Beta_2;
     double cbrk1, cbrk2, wavemaker_cbrk, nu_bkg, T_brk;
@@ -68,6 +69,7 @@ struct Fields {
     uint8_t *MASK, *MASKn, *MASK9, *MASK_STRUC;
     T *rhs_x, *rhs_y;                 // tmp4 of GET_Eta_U_V_HU_HV
     double *ty, *tp, *tq, *tc;        // line-solver scratch
+    double *sw_p[2], *sw_q[2], *sw_c[2];  // factorisation sweep scratch per direction (mixed)
     double *red;                      // reduced systems
     // mixed path: constant factorisation of the tridiagonal matrices, per
     // direction d, rounded to float: per row d-scale (1/tmp2, times r on
@@ -79,7 +81,8 @@ struct Fields {
     float *fac_ah[2], *fac_al[2], *fac_ch[2], *fac_cl[2];
     float *fac_red[2];
     int *m9_dirty;                    // MASK9 changed since the last factorisation
-    double *Cm, *Sm, *omega, *wmcs;   // JON_2D band tables and cos/sin(omega t)
+    T *Cm, *Sm;                       // JON_2D band tables (in the field precision)
+    double *omega, *wmcs;             // JON_2D frequencies and cos/sin(omega t)
     double *dsc;                      // device scalars (S_*)
     float *fsc;                       // float device scalars (FS_*)
     float *wmcsf;                     // float copy of wmcs
@@ -94,6 +97,7 @@ struct LinePart {
     int nlines;  // number of lines
     int m;       // rows per chunk (the last chunk takes the remainder)
     int P;       // chunks per line
+    long long red0;  // offset (doubles) of this direction's rows in the factorisation scratch
 };
 
 // launchers (fw_kernels.cu), all asynchronous on the context stream

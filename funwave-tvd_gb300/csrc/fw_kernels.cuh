@@ -61,6 +61,15 @@ __device__ __forceinline__ float fatan2(float y, float x) { return atan2f(y, x);
 // DT of the current step in the kernel's precision
 #define DTV (sizeof(T) == sizeof(double) ? (T)f.dsc[S_DT] : (T)f.fsc[FS_DT])
 
+// a 0/1 mask byte as a real, by a select instead of an integer-to-float
+// conversion instruction
+template <typename T> __device__ __forceinline__ T m2r(int m) { return m ? (T)1 : (T)0; }
+// a small integer (|k| < 2^22) as a real; in float exactly, by placing k in
+// the mantissa of 1.5*2^23 and subtracting that constant
+template <typename T> __device__ __forceinline__ T i2r(int k) {
+    if constexpr (sizeof(T) == sizeof(double)) return (T)k;
+    else return __int_as_float(0x4B400000 + k) - 12582912.0f;
+}
 template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
 template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
 
@@ -115,7 +124,7 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
     }
     const T sx2 = gx ? (T)-1 : (T)1;  // sign of VTYPE 2 fields in an x ghost
 
-    const T m9 = (T)f.MASK9[IDX(si, sj)];
+    const T m9 = m2r<T>(f.MASK9[IDX(si, sj)]);
     const bool wall = (si == g.ib) || (si == g.ie) || (sj == g.jb) || (sj == g.je);
 #define LU(a, b) f.U[IDX(si + (a), sj + (b))]
 #define LV(a, b) f.V[IDX(si + (a), sj + (b))]
@@ -161,7 +170,7 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
     }
     // ETAx, ETAy: computed on the interior and exchanged only when Gamma2 > 0
     // (bc.F:395-398); without Gamma2 the ghosts keep their old values
-    const bool exch = g.gamma2 > 0.0;
+    const bool exch = g.has_g2 != 0;
     if (exch || (g.show_breaking && !gx && !gy)) {
         const T dex = f.Eta[IDX(si + 1, sj)] - f.Eta[IDX(si - 1, sj)];
         const T dey = f.Eta[IDX(si, sj + 1)] - f.Eta[IDX(si, sj - 1)];
@@ -199,7 +208,7 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
     const T DX = GC(DX), DY = GC(DY), mdf = GC(min_depth_frc);
     const T B1 = GC(Beta_1), B2 = GC(Beta_2), g2 = GC(gamma2), b2 = GC(b2);
     const T one = (T)1, two = (T)2, half = (T)0.5;
-    const T D = f.Depth[id], reta = f.Eta[id], m9 = (T)f.MASK9[id];
+    const T D = f.Depth[id], reta = f.Eta[id], m9 = m2r<T>(f.MASK9[id]);
     constexpr bool EXACT = sizeof(T) == sizeof(double);
     T a, b, c, e;
     if constexpr (EXACT) {
@@ -215,7 +224,7 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
     }
     T u4 = (one / (T)3 - B1 + half * B1 * B1) * D * D * a + (B1 - one / two) * D * b;
     T v4 = (one / (T)3 - B1 + half * B1 * B1) * D * D * c + (B1 - one / two) * D * e;
-    if (g.gamma2 > 0.0) {
+    if (g.has_g2) {
         const T ken1 = (one / (T)6 - B1 + B1 * B1) * D * reta * B2 +
                        (one / two * B1 * B1 - one / (T)6) * reta * reta * B2 * B2;
         const T ken2 = (B1 - one / two) * reta * B2;
@@ -228,7 +237,7 @@ __global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
 
     f.U1p[id] = half * (one - B1) * (one - B1) * D * D * a + (B1 - one) * D * b;
     f.V1p[id] = half * (one - B1) * (one - B1) * D * D * c + (B1 - one) * D * e;
-    if (!(g.gamma2 > 0.0)) return;
+    if (!g.has_g2) return;
 
     const T DT = DTV;
     const T rDT = (T)f.fsc[FS_RDT];
@@ -422,35 +431,47 @@ __device__ __forceinline__ void ho_lr(T vm1, T v0, T d0, T d1, T d2, T &L, T &R)
     }
 }
 
-// Faces of direction DIR (0: x-faces, 1: y-faces) on a 32 x 8 tile.  Din of
-// the seven reconstructed fields is computed once per cell position into
-// shared memory; each thread then finishes one face: face values, Zhou wave
-// speeds, HLL and the boundary/dry-face rules.  Normal velocity is U for x
-// and V for y.
+// Faces of direction DIR (0: x-faces, 1: y-faces).  A tile is 32 x 8
+// x-faces or 32 x 32 y-faces (four per thread, so that the three-cell halo
+// along y is shared by 32 faces; 32 x 16 in FP64).  Din of the seven reconstructed fields is
+// computed once per cell position into shared memory; each thread then
+// finishes its faces: face values, Zhou wave speeds, HLL and the
+// boundary/dry-face rules.  Normal velocity is U for x and V for y.
+template <typename T, int DIR> struct FluxTile {
+    static constexpr int BX = 32, BY = 8;              // threads
+    // faces of a tile (y tiles of doubles are 16 high: 48 KB static shared memory)
+    static constexpr int FX = 32, FY = DIR == 0 ? 8 : (sizeof(T) == sizeof(double) ? 16 : 32);
+    static constexpr int FPT = FY / BY;                // faces per thread
+    static constexpr int NB = DIR == 0 ? FX : FY;      // faces per tile line
+    static constexpr int NTL = DIR == 0 ? FY : FX;     // tile lines
+    static constexpr int NPOS = NB + 2;                // Din positions per line
+    static constexpr int NP = DIR == 0 ? NPOS : NPOS + 1;  // odd row length for y
+};
+
 template <typename T, int DIR>
 __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
-    constexpr int BX = 32, BY = 8;
-    constexpr int NB = DIR == 0 ? BX : BY;        // faces per tile line
-    constexpr int NTL = DIR == 0 ? BY : BX;       // tile lines
-    constexpr int NP = DIR == 0 ? BX + 2 : BY + 3;  // Din positions per line (+1 pad for y)
+    using TL = FluxTile<T, DIR>;
+    constexpr int BX = TL::BX, BY = TL::BY, NTL = TL::NTL, NPOS = TL::NPOS, NP = TL::NP;
     __shared__ T din[7][NTL][NP];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int i = g.ib + blockIdx.x * BX + tx;
-    const int j = g.jb + blockIdx.y * BY + ty;
-    const int own = DIR == 0 ? tx : ty;
-    const int line = DIR == 0 ? ty : tx;
+    const int i0 = g.ib + blockIdx.x * TL::FX, j0 = g.jb + blockIdx.y * TL::FY;
     const int lo = DIR == 0 ? g.ib : g.jb, hi = DIR == 0 ? g.ie : g.je;
-    const int base = (DIR == 0 ? g.ib + blockIdx.x * BX : g.jb + blockIdx.y * BY) - 1;
-    const bool line_ok = DIR == 0 ? (j <= g.je) : (i <= g.ie);
-    const int di = DIR == 0 ? 1 : 0, dj = DIR == 0 ? 0 : 1;
+    const int base = (DIR == 0 ? i0 : j0) - 1;
     const T *src[7] = {f.U, f.V, f.HU, f.HV, f.Eta, f.U4, f.V4};
     const int nvar = g.dispersion ? 7 : 5;
     // 32-bit offsets: the arena planes hold fewer than 2^31 elements
     const int stride = DIR == 0 ? 1 : g.pitch;
-    for (int k = own; k < NB + 2; k += NB) {
+    // the NTL x NPOS Din positions of the tile, spread over all threads
+    // (consecutive threads on consecutive x for coalesced loads)
+    const int tid = tx + ty * BX;
+    for (int it = tid; it < NTL * NPOS; it += BX * BY) {
+        const int k = DIR == 0 ? it % NPOS : it / NTL;
+        const int ln = DIR == 0 ? it / NPOS : it % NTL;
         const int p = base + k;
-        if (line_ok && p >= lo - 1 && p <= hi + 2) {
-            const int ci = DIR == 0 ? p : i, cj = DIR == 0 ? j : p;
+        const int ci = DIR == 0 ? p : i0 + ln;
+        const int cj = DIR == 0 ? j0 + ln : p;
+        const bool lok = DIR == 0 ? (cj <= g.je) : (ci <= g.ie);
+        if (lok && p >= lo - 1 && p <= hi + 2) {
             const int o0 = ci + cj * g.pitch - 2 * stride;
             int m[4];
 #pragma unroll
@@ -461,20 +482,23 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
                     T v[4];
 #pragma unroll
                     for (int q = 0; q < 4; q++) v[q] = src[vv][o0 + q * stride];
-                    din[vv][line][k] = ho_din(v, m);
+                    din[vv][ln][k] = ho_din(v, m);
                 }
             }
         }
     }
-    (void)di;
-    (void)dj;
     __syncthreads();
-    if (DIR == 0) {
-        if (i > g.ie + 1 || j > g.je) return;
-    } else {
-        if (i > g.ie || j > g.je + 1) return;
-    }
     const T g1 = GC(gamma1), g3 = GC(gamma3);
+    for (int r = 0; r < TL::FPT; r++) {
+    const int i = i0 + tx;
+    const int j = j0 + ty + r * BY;
+    if (DIR == 0) {
+        if (i > g.ie + 1 || j > g.je) continue;
+    } else {
+        if (i > g.ie || j > g.je + 1) continue;
+    }
+    const int own = DIR == 0 ? tx : ty + r * BY;
+    const int line = DIR == 0 ? ty : tx;
     const int fid = i + j * g.pitch;
     const int cm = fid - stride;  // cell pos-1 (cell pos is fid)
     const int kf = own + 1;
@@ -496,7 +520,7 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
     const T HL = EL + Dd, HR = ER + Dd;
     // MASK9u(Mloc1,:) = MASK9(Mloc,:) (fluxes.F:1333); the faces computed
     // here never reach that column
-    const T m9 = (T)f.MASK9[fid];
+    const T m9 = m2r<T>(f.MASK9[fid]);
     const T nL = DIR == 0 ? UL : VL, nR = DIR == 0 ? UR : VR;
     const T tL = DIR == 0 ? VL : UL, tR = DIR == 0 ? VR : UR;
     const T n4L = DIR == 0 ? U4L : V4L, n4R = DIR == 0 ? U4R : V4R;
@@ -542,12 +566,12 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
     const int mL = f.MASK[cm], mR = f.MASK[fid];  // cells pos-1 and pos
     if (mL < 1) {
         Pm = (T)0;
-        Nm = (pos - 1 != hi) ? press(ER, Dd, g3) * (T)mR : (T)0;
+        Nm = (pos - 1 != hi) ? press(ER, Dd, g3) * m2r<T>(mR) : (T)0;
         Tm = (T)0;
     }
     if (mR < 1) {
         Pm = (T)0;
-        Nm = (pos != lo) ? press(EL, Dd, g3) * (T)mL : (T)0;
+        Nm = (pos != lo) ? press(EL, Dd, g3) * m2r<T>(mL) : (T)0;
         Tm = (T)0;
     }
     if (DIR == 0) {
@@ -558,6 +582,7 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
         f.Q[fid] = Pm;
         f.Gy[fid] = Nm;
         f.Fy[fid] = Tm;
+    }
     }
 }
 
@@ -590,7 +615,7 @@ __device__ __forceinline__ T wavemaker_mass(const Grid &g, const Fields<T> &f, i
         // mixed: the ramp and phase of this step come from k_dt_final
         const T AA = f.fsc[FS_WKAA];
         if (g.wavemaker == FW_WK_REG) {
-            const T xmk = (T)(i - g.ib) * g.f_DX, ymk = (T)(j - g.jb) * g.f_DY;
+            const T xmk = i2r<T>(i - g.ib) * g.f_DX, ymk = i2r<T>(j - g.jb) * g.f_DY;
             const T dxm = xmk - g.f_xc_wk;
             return AA * fexp(-g.f_beta_gen * (dxm * dxm)) * fsin(g.f_rlamda * ymk - f.fsc[FS_WKPH]);
         }
@@ -621,8 +646,8 @@ __device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, 
     const size_t ie_ = IDX(i + 1, j), iw = IDX(i - 1, j), in_ = IDX(i, j + 1), is = IDX(i, j - 1);
     const T U = f.U[id], V = f.V[id];
     const T spd = fsqrt(U * U + V * V);
-    const T m9 = (T)f.MASK9[id];
-    const T mk = (T)f.MASK[id];
+    const T m9 = m2r<T>(f.MASK9[id]);
+    const T mk = m2r<T>(f.MASK[id]);
     const T Hm = tmax(f.H[id], mdf);
     const T Eta = f.Eta[id];
     const T U4 = f.U4[id], V4 = f.V4[id];
@@ -715,7 +740,7 @@ __global__ void __launch_bounds__(256, 3) k_update(Grid g, Fields<T> f, T al, T 
     const T cdx = EXACT ? (T)1 / DX : GC(rdx), cdy = EXACT ? (T)1 / DY : GC(rdy);
     T R1 = -cdx * (f.P[ie_] * (T)1 + f.P[id] * (T)-1) - cdy * (f.Q[in_] * (T)1 + f.Q[id] * (T)-1);
     if (g.wavemaker != FW_WK_NONE) {
-        const T xmk = (T)(i - g.ib) * DX, ymk = (T)(j - g.jb) * DY;
+        const T xmk = i2r<T>(i - g.ib) * DX, ymk = i2r<T>(j - g.jb) * DY;
         if (fabs_(xmk - GC(xc_wk)) < GC(width_wk) && fabs_(ymk - GC(yc_wk)) < GC(ywidth_wk) / (T)2)
             R1 = R1 + wm;
     }
@@ -751,7 +776,7 @@ __global__ void __launch_bounds__(256, 3) k_update(Grid g, Fields<T> f, T al, T 
         // mixed: float arithmetic; the cross derivatives of the stage-start
         // U, V are recomputed here
         const T mf = g.f_min_depth_frc;
-        const T m9 = (T)f.MASK9[id], mk = (T)f.MASK[id];
+        const T m9 = m2r<T>(f.MASK9[id]), mk = m2r<T>(f.MASK[id]);
         const T dep = tmax(f.Depth[id], mf);
         const bool wall = (i == g.ib) || (i == g.ie) || (j == g.jb) || (j == g.je);
         T Vxy = (T)0, DVxy = (T)0, Uxy = (T)0, DUxy = (T)0;
@@ -1214,9 +1239,7 @@ __device__ __forceinline__ void split2(double v, float &hi, float &lo) {
 }
 
 template <typename T, int DIR, bool PER>
-__global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp) {
-    if (!*f.m9_dirty) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void fac_a_body(const Grid &g, const Fields<T> &f, const LinePart &lp, int t) {
     if (t >= lp.nlines * lp.P) return;
     int l, ch;
     chunk_of<DIR>(lp, t, l, ch);
@@ -1250,7 +1273,7 @@ __global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp)
     double lo_s, di_s, up_s, lo_e, di_e, up_e;
     if (e - s >= 2) {
         double cp = 0.0, pp = 0.0, qp = 0.0;
-        double *pbuf = f.tp, *qbuf = f.tq, *cbuf = f.tc;  // double scratch of the sweep
+        double *pbuf = f.sw_p[DIR], *qbuf = f.sw_q[DIR], *cbuf = f.sw_c[DIR];  // sweep scratch of this direction
         for (int k = s + 1; k <= e - 1; k++) {
             double a, c, it;
             tri_ac_row<T, DIR, PER>(g, f, lp, l, k, a, c, it);
@@ -1303,7 +1326,7 @@ __global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp)
         up_e = ce;
     }
     // reduced rows to the double scratch; k_fac_b factors them
-    double *red = f.red + ((size_t)l * 2 * lp.P + 2 * ch) * 6;
+    double *red = f.red + lp.red0 + ((size_t)l * 2 * lp.P + 2 * ch) * 6;
     red[0] = lo_s;
     red[1] = di_s;
     red[2] = up_s;
@@ -1316,12 +1339,16 @@ __global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp)
 }
 
 template <typename T, int DIR, bool PER>
-__global__ void __launch_bounds__(128) k_fac_b(Grid g, Fields<T> f, LinePart lp) {
+__global__ void __launch_bounds__(128) k_fac_a(Grid g, Fields<T> f, LinePart lp) {
     if (!*f.m9_dirty) return;
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    fac_a_body<T, DIR, PER>(g, f, lp, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <typename T, int DIR, bool PER>
+__device__ __forceinline__ void fac_b_body(const Grid &g, const Fields<T> &f, const LinePart &lp, int l) {
     if (l >= lp.nlines) return;
     const int n = 2 * lp.P;
-    double *red = f.red + (size_t)l * n * 6;
+    double *red = f.red + lp.red0 + (size_t)l * n * 6;
     FacLine fl = fac_line(f.fac_red[DIR], lp, l);
     double cpr = 0.0;
     for (int k = 0; k < n; k++) {
@@ -1364,6 +1391,26 @@ __global__ void __launch_bounds__(128) k_fac_b(Grid g, Fields<T> f, LinePart lp)
         fl.tail[1] = (float)a_beg;
         fl.tail[2] = (float)(1.0 - (c_end * x0 - a_beg * xl));
     }
+}
+
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(128) k_fac_b(Grid g, Fields<T> f, LinePart lp) {
+    if (!*f.m9_dirty) return;
+    fac_b_body<T, DIR, PER>(g, f, lp, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// both directions in one launch each: blocks [0, nbx) factor x, the rest y
+template <typename T, bool PERY>
+__global__ void __launch_bounds__(128) k_fac_a_xy(Grid g, Fields<T> f, LinePart px, LinePart py, int nbx) {
+    if (!*f.m9_dirty) return;
+    if ((int)blockIdx.x < nbx) fac_a_body<T, 0, false>(g, f, px, blockIdx.x * blockDim.x + threadIdx.x);
+    else fac_a_body<T, 1, PERY>(g, f, py, (blockIdx.x - nbx) * blockDim.x + threadIdx.x);
+}
+template <typename T, bool PERY>
+__global__ void __launch_bounds__(128) k_fac_b_xy(Grid g, Fields<T> f, LinePart px, LinePart py, int nbx) {
+    if (!*f.m9_dirty) return;
+    if ((int)blockIdx.x < nbx) fac_b_body<T, 0, false>(g, f, px, blockIdx.x * blockDim.x + threadIdx.x);
+    else fac_b_body<T, 1, PERY>(g, f, py, (blockIdx.x - nbx) * blockDim.x + threadIdx.x);
 }
 
 static __global__ void k_fac_clear(int *dirty) { *dirty = 0; }
@@ -1561,20 +1608,32 @@ __global__ void __launch_bounds__(256) k_resid(Grid g, Fields<T> f, LinePart lp)
 }
 
 // x lines, one block per line, everything unit-stride: load d, solve, form
-// the compensated residual, solve again and write x0 + correction
+// the compensated residual, solve again and write x0 + correction.  The
+// arrays that a thread walks along its own chunk are stored with one pad
+// float after every 16 (index k + k/16), so that the 32 chunks a warp walks
+// at once fall into different shared-memory banks.
+__host__ __device__ __forceinline__ int lsx_pad(int k) { return k + (k >> 4); }
+__host__ __device__ __forceinline__ size_t lsx_smem_floats(int L, int P) {
+    return (size_t)5 * (lsx_pad(L) + 1) + (size_t)L + 16 * (size_t)P;
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePart lp) {
+__global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePart lp, int clear_dirty) {
     extern __shared__ float shf[];
     const int l = blockIdx.x;
+    // the factorisation of this stage is complete: the MASK9 change flag
+    // can be reset for UPDATE_MASK to set again
+    if (clear_dirty && l == 0 && threadIdx.x == 0) *f.m9_dirty = 0;
     const int L = lp.L, P = lp.P, m = lp.m;
-    float *d = shf;            // L  right-hand side, then residual
-    float *y = shf + L;        // L  sweep values
-    float *x0 = shf + 2 * L;   // L  first solution
-    float *A = shf + 3 * L;    // L  sweep constants, staged with unit-stride loads
-    float *LR = shf + 4 * L;   // L
-    float *CP = shf + 5 * L;   // L
-    float *rr = shf + 6 * L;   // 2P reduced right-hand sides / solution
-    float *pb = shf + 6 * L + 2 * P;  // 7 x 2P PCR buffers
+    const int LP = lsx_pad(L) + 1;
+    float *d = shf;            // right-hand side, then residual (padded)
+    float *y = shf + LP;       // sweep values (padded)
+    float *A = shf + 2 * LP;   // sweep constants, staged with unit-stride loads (padded)
+    float *LR = shf + 3 * LP;
+    float *CP = shf + 4 * LP;
+    float *x0 = shf + 5 * LP;  // L  first solution (unpadded)
+    float *rr = x0 + L;        // 2P reduced right-hand sides / solution
+    float *pb = rr + 2 * P;    // 7 x 2P PCR buffers
     const int j = g.jb + l;
     const size_t row = (size_t)j * g.pitch + g.ib;
     const T *rhs = f.rhs_x + row;
@@ -1584,29 +1643,32 @@ __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePa
     const int s = ch * m;
     const int e = (ch == P - 1) ? L - 1 : s + m - 1;
     for (int k = threadIdx.x; k < L; k += blockDim.x) {
-        d[k] = (float)rhs[k] * IT[k];
-        A[k] = f.fac_A[0][row + k];
-        LR[k] = f.fac_lr[0][row + k];
-        CP[k] = f.fac_cp[0][row + k];
+        const int q = lsx_pad(k);
+        d[q] = (float)rhs[k] * IT[k];
+        A[q] = f.fac_A[0][row + k];
+        LR[q] = f.fac_lr[0][row + k];
+        CP[q] = f.fac_cp[0][row + k];
     }
     __syncthreads();
     for (int pass = 0; pass < 2; pass++) {
-        // chunk forward/backward sweeps; the constants stream from L1/L2
+        // chunk forward/backward sweeps
         if (ch < P) {
-            float rs = d[s], re = d[e];
+            float rs = d[lsx_pad(s)], re = d[lsx_pad(e)];
             if (e - s >= 2) {
                 float yp = 0.0f;
                 for (int k = s + 1; k <= e - 1; k++) {
-                    yp = d[k] * A[k] - LR[k] * yp;
-                    y[k] = yp;
+                    const int q = lsx_pad(k);
+                    yp = d[q] * A[q] - LR[q] * yp;
+                    y[q] = yp;
                 }
                 float yn = 0.0f;
                 for (int k = e - 1; k >= s + 1; k--) {
-                    yn = y[k] - CP[k] * yn;
-                    y[k] = yn;
+                    const int q = lsx_pad(k);
+                    yn = y[q] - CP[q] * yn;
+                    y[q] = yn;
                 }
-                rs = d[s] - fl.cs[ch] * y[s + 1];
-                re = d[e] - fl.ae[ch] * y[e - 1];
+                rs = rs - fl.cs[ch] * y[lsx_pad(s + 1)];
+                re = re - fl.ae[ch] * y[lsx_pad(e - 1)];
             }
             rr[2 * ch] = rs;
             rr[2 * ch + 1] = re;
@@ -1622,7 +1684,9 @@ __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePa
         for (int k = threadIdx.x; k < L; k += blockDim.x) {
             const int c = min(k / m, P - 1);
             const int cs = c * m, ce = (c == P - 1) ? L - 1 : cs + m - 1;
-            const float x = (k == cs) ? rr[2 * c] : (k == ce) ? rr[2 * c + 1] : y[k] - Pp[k] * rr[2 * c] - Qq[k] * rr[2 * c + 1];
+            const float x = (k == cs) ? rr[2 * c]
+                          : (k == ce) ? rr[2 * c + 1]
+                                      : y[lsx_pad(k)] - Pp[k] * rr[2 * c] - Qq[k] * rr[2 * c + 1];
             if (pass == 0) x0[k] = x;
             else f.U[row + k] = (T)(x0[k] + x);
         }
@@ -1632,7 +1696,7 @@ __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePa
             const float *CH = f.fac_ch[0] + row, *CL = f.fac_cl[0] + row;
             for (int k = threadIdx.x; k < L; k += blockDim.x) {
                 const float xm = k > 0 ? x0[k - 1] : 0.0f, xp = k < L - 1 ? x0[k + 1] : 0.0f;
-                d[k] = residual((float)rhs[k] * IT[k], x0[k], xm, xp, AH[k], AL[k], CH[k], CL[k]);
+                d[lsx_pad(k)] = residual((float)rhs[k] * IT[k], x0[k], xm, xp, AH[k], AL[k], CH[k], CL[k]);
             }
             __syncthreads();
         }
@@ -1644,10 +1708,7 @@ __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePa
 // the Froude cap, with the MASK of the start of the stage.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256) k_post(Grid g, Fields<T> f) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.Mloc || j >= g.Nloc) return;
+__device__ __forceinline__ void post_cell(const Grid &g, const Fields<T> &f, int i, int j) {
     const size_t id = IDX(i, j);
     const T mdf = GC(min_depth_frc);
     const bool interior = !(i < g.ib || i > g.ie || j < g.jb || j > g.je);
@@ -1682,6 +1743,14 @@ __global__ void __launch_bounds__(256) k_post(Grid g, Fields<T> f) {
             }
         }
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_post(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    post_cell(g, f, i, j);
 }
 
 // Ubar = HU, Vbar = HV on every cell when DISPERSION is off (etauv_solver.F:596-600)
@@ -1724,11 +1793,9 @@ __device__ __forceinline__ int new_mask(const Grid &g, const Fields<T> &f, int a
     return (eta < -f.Depth[q]) ? 0 : m;
 }
 
+// one thread of UPDATE_MASK at (i, j) in 0..Mloc x 0..Nloc
 template <typename T>
-__global__ void __launch_bounds__(256) k_mask(Grid g, Fields<T> f) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i > g.Mloc || j > g.Nloc) return;
+__device__ __forceinline__ void mask_cell(const Grid &g, const Fields<T> &f, int i, int j) {
     // Depthx at x-face i of row j
     if (j < g.Nloc && j >= g.jb - 2 && j <= g.je + 2) {
         const bool rin = (i >= g.ib - 2 && i <= g.ie + 2);
@@ -1764,6 +1831,14 @@ __global__ void __launch_bounds__(256) k_mask(Grid g, Fields<T> f) {
     f.MASK9[id] = m9;
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) k_mask(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i > g.Mloc || j > g.Nloc) return;
+    mask_cell(g, f, i, j);
+}
+
 // ---------------------------------------------------------------------------
 // BREAKING (breaker.F:87-353), default branch
 // ---------------------------------------------------------------------------
@@ -1781,7 +1856,7 @@ __device__ __forceinline__ BrkLocal<T> brk_local(const Grid &g, const Fields<T> 
 }
 template <typename T>
 __device__ __forceinline__ bool in_wk_zone(const Grid &g, int i, int j) {
-    const T xmk = (T)(i - g.ib) * GC(DX), ymk = (T)(j - g.jb) * GC(DY);
+    const T xmk = i2r<T>(i - g.ib) * GC(DX), ymk = i2r<T>(j - g.jb) * GC(DY);
     return fabs_(xmk - GC(xc_wk)) < GC(width_wk) && fabs_(ymk - GC(yc_wk)) < GC(ywidth_wk) / (T)2;
 }
 template <typename T>
@@ -1803,10 +1878,7 @@ __device__ __forceinline__ T nu_value(const Grid &g, const Fields<T> &f, size_t 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_break_a(Grid g, Fields<T> f) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.Mloc || j >= g.Nloc) return;
+__device__ __forceinline__ void break_cell(const Grid &g, const Fields<T> &f, int i, int j) {
     const size_t id = IDX(i, j);
     const T age = f.AGE[id];
     if (i < g.ib - 1 || i > g.ie + 1 || j < g.jb - 1 || j > g.je + 1) {
@@ -1827,6 +1899,31 @@ __global__ void __launch_bounds__(256) k_break_a(Grid g, Fields<T> f) {
         f.cand[slot] = i + j * g.pitch;
     }
     if (zone || !cand) f.nu[id] = nu_value(g, f, id, b, an, zone);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_break_a(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
+    break_cell(g, f, i, j);
+}
+
+// The stage's GET_Eta_U_V_HU_HV tail, UPDATE_MASK and the parallel part of
+// BREAKING in one pass: each reads only values that are final before it
+// starts (U, V from the line solves; Eta, H from ESTIMATE_HUV; the MASK of
+// the start of the stage; AGE of the previous stage) and writes disjoint
+// arrays, so one thread can do all three.  Launched over (Mloc+1) x (Nloc+1).
+template <typename T>
+__global__ void __launch_bounds__(256) k_post_mask_break(Grid g, Fields<T> f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i > g.Mloc || j > g.Nloc) return;
+    if (i < g.Mloc && j < g.Nloc) {
+        post_cell(g, f, i, j);
+        break_cell(g, f, i, j);
+    }
+    mask_cell(g, f, i, j);
 }
 
 // the neighbour test of one candidate (breaker.F:182-224); N = new values
@@ -2045,7 +2142,7 @@ __global__ void __launch_bounds__(256) k_maskmul(Grid g, Fields<T> f, int sponge
     if (i >= g.Mloc || j >= g.Nloc) return;
     const size_t id = IDX(i, j);
     const uint8_t mi = f.MASK[id];
-    const T m = (T)mi;
+    const T m = m2r<T>(mi);
     T u = f.U[id] * m, v = f.V[id] * m;
     f.HU[id] = f.HU[id] * m;
     f.HV[id] = f.HV[id] * m;
@@ -2118,7 +2215,7 @@ __global__ void __launch_bounds__(256) k_begin(Grid g, Fields<T> f) {
     T v = (T)1.0e30;
     if (i < g.Mloc && j < g.Nloc) {
         const size_t id = IDX(i, j);
-        const T m = (T)f.MASK[id];
+        const T m = m2r<T>(f.MASK[id]);
         const T u = f.U[id] * m, vv = f.V[id] * m;
         f.U[id] = u;
         f.V[id] = vv;
@@ -2216,6 +2313,13 @@ __global__ void __launch_bounds__(256) k_end(Grid g, Fields<T> f, int track_hmax
 // ---------------------------------------------------------------------------
 static inline dim3 grid2(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
 static const dim3 B2D(32, 8);
+// blocks of k_flux: tiles of FX x FY faces over (Mglob+1) x Nglob x-faces
+// or Mglob x (Nglob+1) y-faces
+template <typename T, int DIR> static dim3 flux_grid(const Grid &g) {
+    using TL = FluxTile<T, DIR>;
+    const int w = DIR == 0 ? g.Mglob + 1 : g.Mglob, h = DIR == 0 ? g.Nglob : g.Nglob + 1;
+    return dim3((w + TL::FX - 1) / TL::FX, (h + TL::FY - 1) / TL::FY);
+}
 
 static inline void note(fw_ctx *c, int n = 1) {
     c->launches += n;
@@ -2282,9 +2386,9 @@ template <typename T> void launch_dispersion(fw_ctx *c) {
 
 template <typename T> void launch_fluxes(fw_ctx *c) {
     const Grid &g = c->g;
-    k_flux<T, 0><<<grid2(g.Mglob + 1, g.Nglob, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    k_flux<T, 0><<<flux_grid<T, 0>(g), B2D, 0, c->stream>>>(g, c->F<T>());
     note(c);
-    k_flux<T, 1><<<grid2(g.Mglob, g.Nglob + 1, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    k_flux<T, 1><<<flux_grid<T, 1>(g), B2D, 0, c->stream>>>(g, c->F<T>());
     note(c);
 }
 
@@ -2294,25 +2398,28 @@ template <typename T> void launch_sources_debug(fw_ctx *c) {
     note(c);
 }
 
-template <typename T, int DIR, bool PER> static void launch_tri(fw_ctx *c, const LinePart &lp) {
+template <typename T, int DIR, bool PER>
+static bool launch_tri(fw_ctx *c, const LinePart &lp, bool fac = true, bool clear_dirty = false) {
     const Grid &g = c->g;
     if constexpr (sizeof(T) == sizeof(double)) {
         k_thomas<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         note(c);
-        return;
+        return false;
     }
     const int nt = lp.nlines * lp.P;
     if (c->factored) {
-        k_fac_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        k_fac_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        note(c, 2);
-        const size_t smem = (size_t)(6 * lp.L + 2 * lp.P + 14 * lp.P) * sizeof(float);
+        if (fac) {
+            k_fac_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_fac_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            note(c, 2);
+        }
+        const size_t smem = lsx_smem_floats(lp.L, lp.P) * sizeof(float);
         if (DIR == 0 && !PER && lp.P <= 256 && smem <= 200 * 1024) {
             if (smem > 48 * 1024)
                 cudaFuncSetAttribute(k_linesolve_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_linesolve_x<T><<<lp.nlines, 256, smem, c->stream>>>(g, c->F<T>(), lp);
+            k_linesolve_x<T><<<lp.nlines, 256, smem, c->stream>>>(g, c->F<T>(), lp, clear_dirty ? 1 : 0);
             note(c);
-            return;
+            return clear_dirty;
         }
         const dim3 gi = grid2(g.Mglob, g.Nglob, B2D);
         k_sol_a<T, DIR, PER, 0><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
@@ -2325,7 +2432,7 @@ template <typename T, int DIR, bool PER> static void launch_tri(fw_ctx *c, const
         k_sol_b<T, DIR, PER><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
         k_sol_c<T, DIR, 1><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         note(c, 7);
-        return;
+        return false;
     }
     k_tri_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
     note(c);
@@ -2333,9 +2440,12 @@ template <typename T, int DIR, bool PER> static void launch_tri(fw_ctx *c, const
     note(c);
     k_tri_c<T, DIR><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
     note(c);
+    return false;
 }
 
-template <typename T> void launch_estimate_huv(fw_ctx *c, int istage) {
+// ESTIMATE_HUV; with_post = false leaves the GET_Eta_U_V_HU_HV tail (k_post)
+// to the fused kernel of the stage
+template <typename T> static void launch_estimate_huv_opt(fw_ctx *c, int istage, bool with_post) {
     const Grid &g = c->g;
     static const double AL[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0};
     static const double BE[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
@@ -2343,14 +2453,34 @@ template <typename T> void launch_estimate_huv(fw_ctx *c, int istage) {
     k_update<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>(), al, be);
     note(c);
     if (g.dispersion) {
-        launch_tri<T, 0, false>(c, c->px);
-        if (g.periodic) launch_tri<T, 1, true>(c, c->py);
-        else launch_tri<T, 1, false>(c, c->py);
         if (sizeof(T) == sizeof(float) && c->factored) {
-            k_fac_clear<<<1, 1, 0, c->stream>>>(c->F<T>().m9_dirty);
-            note(c);
+            // factor both directions (when MASK9 changed) in one launch each,
+            // then solve; the x solve resets the change flag when it can
+            const int nbx = (c->px.nlines * c->px.P + 127) / 128;
+            const int nby = (c->py.nlines * c->py.P + 127) / 128;
+            const int lbx = (c->px.nlines + 127) / 128, lby = (c->py.nlines + 127) / 128;
+            if (g.periodic) {
+                k_fac_a_xy<T, true><<<nbx + nby, 128, 0, c->stream>>>(g, c->F<T>(), c->px, c->py, nbx);
+                k_fac_b_xy<T, true><<<lbx + lby, 128, 0, c->stream>>>(g, c->F<T>(), c->px, c->py, lbx);
+            } else {
+                k_fac_a_xy<T, false><<<nbx + nby, 128, 0, c->stream>>>(g, c->F<T>(), c->px, c->py, nbx);
+                k_fac_b_xy<T, false><<<lbx + lby, 128, 0, c->stream>>>(g, c->F<T>(), c->px, c->py, lbx);
+            }
+            note(c, 2);
+            const bool cleared = launch_tri<T, 0, false>(c, c->px, false, true);
+            if (g.periodic) launch_tri<T, 1, true>(c, c->py, false);
+            else launch_tri<T, 1, false>(c, c->py, false);
+            if (!cleared) {
+                k_fac_clear<<<1, 1, 0, c->stream>>>(c->F<T>().m9_dirty);
+                note(c);
+            }
+        } else {
+            launch_tri<T, 0, false>(c, c->px);
+            if (g.periodic) launch_tri<T, 1, true>(c, c->py);
+            else launch_tri<T, 1, false>(c, c->py);
         }
     }
+    if (!with_post) return;
     k_post<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
     note(c);
     if (!g.dispersion) {
@@ -2358,6 +2488,8 @@ template <typename T> void launch_estimate_huv(fw_ctx *c, int istage) {
         note(c);
     }
 }
+
+template <typename T> void launch_estimate_huv(fw_ctx *c, int istage) { launch_estimate_huv_opt<T>(c, istage, true); }
 
 template <typename T> void launch_update_mask(fw_ctx *c) {
     const Grid &g = c->g;
@@ -2392,9 +2524,26 @@ template <typename T> void launch_stage(fw_ctx *c, int istage) {
     const Grid &g = c->g;
     if (g.dispersion) launch_dispersion<T>(c);
     launch_fluxes<T>(c);
-    launch_estimate_huv<T>(c, istage);
-    launch_update_mask<T>(c);
-    launch_breaking<T>(c);
+    if (g.dispersion && g.show_breaking) {
+        // GET_Eta_U_V_HU_HV tail + UPDATE_MASK + BREAKING (parallel part)
+        // in one kernel, then the breaking sweep's candidates
+        launch_estimate_huv_opt<T>(c, istage, false);
+        k_post_mask_break<T><<<grid2(g.Mloc + 1, g.Nloc + 1, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+        note(c);
+        auto &F = c->F<T>();
+        uint8_t *t = F.MASK;
+        F.MASK = F.MASKn;
+        F.MASKn = t;
+        k_break_b<T><<<1, 1024, 0, c->stream>>>(g, F);
+        note(c);
+        T *a = F.AGE;
+        F.AGE = F.AGEn;
+        F.AGEn = a;
+    } else {
+        launch_estimate_huv<T>(c, istage);
+        launch_update_mask<T>(c);
+        launch_breaking<T>(c);
+    }
     launch_exchange<T>(c, g.direct_sponge != 0);
 }
 
@@ -2448,8 +2597,8 @@ template <typename T> int launch_by_name(fw_ctx *c, const char *name) {
     auto is = [&](const char *n) { return std::strcmp(name, n) == 0; };
     if (is("disp_a")) k_disp_a<T><<<gc, B2D, 0, c->stream>>>(g, f);
     else if (is("disp_b")) k_disp_b<T><<<gc, B2D, 0, c->stream>>>(g, f);
-    else if (is("flux_x")) k_flux<T, 0><<<grid2(g.Mglob + 1, g.Nglob, B2D), B2D, 0, c->stream>>>(g, f);
-    else if (is("flux_y")) k_flux<T, 1><<<grid2(g.Mglob, g.Nglob + 1, B2D), B2D, 0, c->stream>>>(g, f);
+    else if (is("flux_x")) k_flux<T, 0><<<flux_grid<T, 0>(g), B2D, 0, c->stream>>>(g, f);
+    else if (is("flux_y")) k_flux<T, 1><<<flux_grid<T, 1>(g), B2D, 0, c->stream>>>(g, f);
     else if (is("update")) k_update<T><<<gc, B2D, 0, c->stream>>>(g, f, (T)0.75, (T)0.25);
     else if (is("tri_x")) { launch_tri<T, 0, false>(c, c->px); return 0; }
     else if (is("tri_y")) {
