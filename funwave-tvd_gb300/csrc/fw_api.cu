@@ -64,9 +64,15 @@ template <typename T> bool find_field(fw_ctx *c, const char *name, FieldRef &r) 
         {"P", f.P, XFACE, 0}, {"Fx", f.Fx, XFACE, 0}, {"Gx", f.Gx, XFACE, 0}, {"Depthy", f.Depthy, YFACE, 0},
         {"Q", f.Q, YFACE, 0}, {"Fy", f.Fy, YFACE, 0}, {"Gy", f.Gy, YFACE, 0}, {"MASK", f.MASK, CELL, 1},
         {"MASK9", f.MASK9, CELL, 1}, {"MASK_STRUC", f.MASK_STRUC, CELL, 1},
+        {"HeightMin", f.Hmin, CELL, 0}, {"VelocityMax", f.Umax, CELL, 0}, {"MomentumFluxMax", f.MFmax, CELL, 0},
+        {"ETAmean", f.ETAmean, CELL, 0}, {"Umean", f.Umean, CELL, 0}, {"Vmean", f.Vmean, CELL, 0},
+        {"ETA2mean", f.ETA2mean, CELL, 0}, {"SigWaveHeight", f.SigWH, CELL, 0},
+        {"WaveHeightAve", f.WHave, CELL, 0}, {"WaveHeightRMS", f.WHrms, CELL, 0}, {"Emax", f.Emax, CELL, 0},
+        {"Emin", f.Emin, CELL, 0}, {"Num_Zero_Up", f.NZU, CELL, 0},
     };
     for (auto &e : tab)
         if (std::strcmp(e.n, name) == 0) {
+            if (!e.p) return false;  // a statistic that is switched off
             r.ptr = e.p;
             r.kind = e.k;
             r.is_mask = e.m;
@@ -199,6 +205,19 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
                 &f.DUxy,  &f.DVyy,  &f.U4,    &f.V4,     &f.U1p,   &f.V1p,  &f.Udisp, &f.Vdisp, &f.ETAx,
                 &f.ETAy,  &f.ETAT,  &f.AGE,   &f.AGEn,   &f.nu,    &f.SourceX, &f.SourceY, &f.WM, &f.Hmax};
     for (T **p : tf) *p = (T *)take(plane * sizeof(T));
+    // statistics planes only when switched on
+    if (g.track_hmin) f.Hmin = (T *)take(plane * sizeof(T));
+    if (g.track_umax) f.Umax = (T *)take(plane * sizeof(T));
+    if (g.track_mfmax) f.MFmax = (T *)take(plane * sizeof(T));
+    if (g.stats) {
+        T **sf[] = {&f.ETAmean, &f.Umean, &f.Vmean, &f.ETAsum, &f.Usum, &f.Vsum, &f.ETA2sum, &f.ETA2mean,
+                    &f.SigWH, &f.Emax, &f.Emin, &f.HavgSum, &f.HrmsSum, &f.WHave, &f.WHrms, &f.NZU};
+        for (T **p : sf) *p = (T *)take(plane * sizeof(T));
+        if (sizeof(T) == sizeof(float)) {
+            T **kf[] = {&f.kETAsum, &f.kUsum, &f.kVsum, &f.kETA2sum};
+            for (T **p : kf) *p = (T *)take(plane * sizeof(T));
+        }
+    }
     uint8_t **mf[] = {&f.MASK, &f.MASKn, &f.MASK9, &f.MASK_STRUC};
     for (uint8_t **p : mf) *p = (uint8_t *)take(plane);
     f.rhs_x = (T *)take(plane * sizeof(T));
@@ -341,6 +360,8 @@ void fw_params_default(fw_params *p) {
     p->spreading = FW_SPREAD_WRAPPED_NORMAL;
     p->precision = FW_PREC_FP64;
     p->device = 0;
+    p->steady_time = 999999.0;  // LARGE: no time means
+    p->t_intv_mean = 999999.0;
 }
 
 const char *fw_strerror(int s) {
@@ -390,6 +411,12 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     g.gamma1 = p->dispersion ? p->gamma1 : 0.0;
     g.gamma2 = p->dispersion ? p->gamma2 : 0.0;
     g.has_g2 = g.gamma2 > 0.0 ? 1 : 0;
+    g.track_hmin = p->track_hmin;
+    g.track_umax = p->track_umax;
+    g.track_mfmax = p->track_mfmax;
+    g.steady_time = p->steady_time;
+    g.t_intv_mean = p->t_intv_mean;
+    g.stats = p->steady_time < 999999.0 ? 1 : 0;  // MIXING_STUFF can run
     g.gamma3 = p->gamma3;
     g.b1 = p->beta_ref * p->beta_ref;
     g.b2 = p->beta_ref;
@@ -578,12 +605,12 @@ int fw_set_field(fw_ctx *c, const char *name, const void *host) {
 
 int fw_get_scalar(fw_ctx *c, const char *name, double *v) {
     if (!c || !name || !v) return FW_ERR_BAD_PARAM;
-    if (!std::strcmp(name, "TIME") || !std::strcmp(name, "DT")) {
+    if (!std::strcmp(name, "TIME") || !std::strcmp(name, "DT") || !std::strcmp(name, "T_sum")) {
         double sc[S_NSLOT];
         cudaError_t e = cudaMemcpyAsync(sc, dsc_ptr(c), sizeof(sc), cudaMemcpyDeviceToHost, c->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) return cuda_status(c, e);
-        *v = !std::strcmp(name, "TIME") ? sc[S_TIME] : sc[S_DT];
+        *v = !std::strcmp(name, "TIME") ? sc[S_TIME] : !std::strcmp(name, "DT") ? sc[S_DT] : sc[S_TSUM];
         return FW_OK;
     }
     if (!std::strcmp(name, "EtaBlowVal")) *v = c->EtaBlowVal;

@@ -26,6 +26,8 @@ struct Grid {
     int ilo, ihi, jlo, jhi;  // 0-based wavemaker band (empty when ilo > ihi)
     int nfreq;
     int has_g2;              // Gamma2 > 0 (the dispersive ETAx/ETAy exchange)
+    int track_hmin, track_umax, track_mfmax, stats;  // statistics switches
+    double steady_time, t_intv_mean;
     double DX, DY;
     double gamma1, gamma2, gamma3, b1, b2, Beta_1, Beta_2;
     double cbrk1, cbrk2, wavemaker_cbrk, nu_bkg, T_brk;
@@ -48,10 +50,12 @@ struct Grid {
 };
 
 // float device scalars of the current step (mixed path)
-enum : int { FS_DT = 0, FS_RDT = 1, FS_WKAA = 2, FS_WKPH = 3, FS_NSLOT = 8 };
+enum : int { FS_DT = 0, FS_RDT = 1, FS_WKAA = 2, FS_WKPH = 3, FS_TSUM = 4, FS_NSLOT = 8 };
 
 // device scalar slots (double array)
-enum : int { S_TIME = 0, S_DT = 1, S_DTMIN = 2, S_ETAMAX = 3, S_NSLOT = 8 };
+// S_TSUM: T_sum of MIXING_STUFF; S_TSUMU: the T_sum this step's means use;
+// S_MFLAG: 0 no statistics this step, 1 accumulate, 2 end of an interval
+enum : int { S_TIME = 0, S_DT = 1, S_DTMIN = 2, S_ETAMAX = 3, S_TSUM = 4, S_TSUMU = 5, S_MFLAG = 6, S_NSLOT = 8 };
 
 template <typename T>
 struct Fields {
@@ -66,6 +70,11 @@ struct Fields {
     T *AGE, *AGEn, *nu;               // AGE ping-pong (old / new)
     T *SourceX, *SourceY, *WM;        // materialised only by the unit entry points
     T *Hmax;
+    // statistics (null unless switched on): MAX_MIN_PROPERTY and CALCULATE_MEAN
+    T *Hmin, *Umax, *MFmax;
+    T *ETAmean, *Umean, *Vmean, *ETAsum, *Usum, *Vsum, *ETA2sum, *ETA2mean, *SigWH, *Emax, *Emin, *HavgSum,
+        *HrmsSum, *WHave, *WHrms, *NZU;
+    T *kETAsum, *kUsum, *kVsum, *kETA2sum;  // Kahan compensations of the mixed path
     uint8_t *MASK, *MASKn, *MASK9, *MASK_STRUC;
     T *rhs_x, *rhs_y;                 // tmp4 of GET_Eta_U_V_HU_HV
     double *ty, *tp, *tq, *tc;        // line-solver scratch

@@ -34,6 +34,8 @@ namespace fw {
 
 // pi as the reference stores it: a default-REAL literal (mod_param.F:71)
 constexpr double PI_SP = (double)(float)3.141592653;
+// the default-REAL literal 4.004 of SigWaveHeight (mixing.F:244)
+constexpr double C4004_SP = (double)(float)4.004;
 constexpr double GRAV = 9.81;
 constexpr double SMALL = 0.000001;
 constexpr double LARGE = 999999.0;
@@ -2206,8 +2208,32 @@ __device__ __forceinline__ void block_min_to_global(T v, unsigned long long *dst
     }
 }
 
-// begin of a step: U,V,HU,HV *= MASK after the ghost fill, the Eta0/Ubar0/
-// Vbar0/U0/V0 copies (main.F:295-297,331) and the CFL minimum
+// Eta0 = Eta on the ghost ring, before the step's EXCHANGE refills it
+// (main.F:295 comes before main.F:313): the ring still holds the previous
+// step's sponge-damped values.  6*Mloc + 6*Nglob cells, one thread each.
+template <typename T>
+__global__ void __launch_bounds__(256) k_eta0_ring(Grid g, Fields<T> f) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j;
+    if (t < 3 * g.Mloc) {
+        j = t / g.Mloc;
+        i = t - j * g.Mloc;
+    } else if ((t -= 3 * g.Mloc) < 3 * g.Mloc) {
+        j = g.Nloc - 3 + t / g.Mloc;
+        i = t % g.Mloc;
+    } else if ((t -= 3 * g.Mloc) < 6 * g.Nglob) {
+        j = NG + t / 6;
+        const int c = t % 6;
+        i = c < 3 ? c : g.Mloc - 6 + c;
+    } else {
+        return;
+    }
+    f.Eta0[IDX(i, j)] = f.Eta[IDX(i, j)];
+}
+
+// begin of a step: U,V,HU,HV *= MASK after the ghost fill, the Eta0
+// (interior; the ring is copied by k_eta0_ring before the fill), Ubar0,
+// Vbar0, U0, V0 copies (main.F:295-297,331) and the CFL minimum
 template <typename T>
 __global__ void __launch_bounds__(256) k_begin(Grid g, Fields<T> f) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2221,7 +2247,7 @@ __global__ void __launch_bounds__(256) k_begin(Grid g, Fields<T> f) {
         f.V[id] = vv;
         f.HU[id] = f.HU[id] * m;
         f.HV[id] = f.HV[id] * m;
-        f.Eta0[id] = f.Eta[id];
+        if (i >= g.ib && i <= g.ie && j >= g.jb && j <= g.je) f.Eta0[id] = f.Eta[id];
         f.Ubar0[id] = f.Ubar[id];
         f.Vbar0[id] = f.Vbar[id];
         f.U0[id] = u;
@@ -2286,26 +2312,156 @@ static __global__ void k_dt_final(Grid g, double *dsc, float *fsc, unsigned long
 // end of a step: MAX_MIN_PROPERTY (Hmax, misc.F:307-383) and the
 // CHECK_BLOWUP maximum (misc.F:394-433)
 // ---------------------------------------------------------------------------
+// MIXING_STUFF's T_sum (mixing.F:60, 143-144, 224): one thread, before
+// k_end; S_MFLAG tells k_end what to do with the cells this step
+static __global__ void k_tsum(Grid g, double *dsc, float *fsc) {
+    int flag = 0;
+    double ts = dsc[S_TSUM], tsu = ts;
+    if (dsc[S_TIME] >= g.steady_time) {
+        ts = ts + dsc[S_DT];
+        tsu = ts;
+        if (ts >= g.t_intv_mean) {
+            flag = 2;
+            ts = ts - g.t_intv_mean;
+        } else {
+            flag = 1;
+        }
+    }
+    dsc[S_TSUM] = ts;
+    dsc[S_TSUMU] = tsu;
+    dsc[S_MFLAG] = (double)flag;
+    fsc[FS_TSUM] = (float)tsu;
+}
+
+// s += x with Kahan compensation k (mixed path), s = x + s otherwise
+template <typename T> __device__ __forceinline__ void stat_add(T *s, T *k, size_t id, T x) {
+    if constexpr (sizeof(T) == sizeof(double)) {
+        s[id] = x + s[id];
+    } else {
+        const float y = __fsub_rn(x, k[id]);
+        const float t = __fadd_rn(s[id], y);
+        k[id] = __fsub_rn(__fsub_rn(t, s[id]), y);
+        s[id] = t;
+    }
+}
+// the compensated value of a sum
+template <typename T> __device__ __forceinline__ T stat_val(const T *s, const T *k, size_t id) {
+    if constexpr (sizeof(T) == sizeof(double)) return s[id];
+    else return __fsub_rn(s[id], k[id]);
+}
+
+// CALCULATE_MEAN (mixing.F:141-301) at one cell: the Eta, U, V and
+// (Eta-ETAmean)^2 time sums, their means at the end of an interval, and the
+// zero-up-crossing wave heights; the float path keeps the sums compensated
+template <typename T> __device__ __forceinline__ void mean_cell(const Grid &g, const Fields<T> &f, size_t id,
+                                                                int flag) {
+    const T DT = DTV;
+    const T eta = f.Eta[id], u = f.U[id], v = f.V[id];
+    const T d = eta - f.ETAmean[id];
+    if (flag == 2) {
+        T Ts;
+        if constexpr (sizeof(T) == sizeof(double)) Ts = f.dsc[S_TSUMU];
+        else Ts = f.fsc[FS_TSUM];
+        stat_add(f.ETA2sum, f.kETA2sum, id, d * d * DT);
+        const T e2 = stat_val(f.ETA2sum, f.kETA2sum, id) / Ts;
+        f.ETA2mean[id] = e2;
+        stat_add(f.Usum, f.kUsum, id, u * DT);
+        stat_add(f.Vsum, f.kVsum, id, v * DT);
+        stat_add(f.ETAsum, f.kETAsum, id, eta * DT);
+        f.Umean[id] = stat_val(f.Usum, f.kUsum, id) / Ts;
+        f.Vmean[id] = stat_val(f.Vsum, f.kVsum, id) / Ts;
+        f.ETAmean[id] = stat_val(f.ETAsum, f.kETAsum, id) / Ts;
+        f.Usum[id] = (T)0;
+        f.Vsum[id] = (T)0;
+        f.ETAsum[id] = (T)0;
+        f.ETA2sum[id] = (T)0;
+        if constexpr (sizeof(T) == sizeof(float)) {
+            f.kUsum[id] = 0.0f;
+            f.kVsum[id] = 0.0f;
+            f.kETAsum[id] = 0.0f;
+            f.kETA2sum[id] = 0.0f;
+        }
+        f.SigWH[id] = (T)C4004_SP * fsqrt(e2);
+        const T nz = f.NZU[id];
+        if (nz >= (T)2) {
+            f.WHave[id] = f.HavgSum[id] / nz;
+            f.WHrms[id] = fsqrt(f.HrmsSum[id] / nz);
+        }
+    } else {
+        stat_add(f.Usum, f.kUsum, id, u * DT);
+        stat_add(f.Vsum, f.kVsum, id, v * DT);
+        stat_add(f.ETAsum, f.kETAsum, id, eta * DT);
+        stat_add(f.ETA2sum, f.kETA2sum, id, d * d * DT);
+        T emax = f.Emax[id], emin = f.Emin[id];
+        if (eta > emax) emax = eta;
+        if (eta < emin) emin = eta;
+        const T tmp0 = f.Eta0[id] - f.ETAmean[id];
+        if (d > tmp0 && d * tmp0 <= (T)0) {
+            const T nz = f.NZU[id] + (T)1;
+            f.NZU[id] = nz;
+            if (nz >= (T)2) {
+                const T h = emax - emin;
+                f.HavgSum[id] = (f.HavgSum[id] + emax) - emin;  // left to right (mixing.F:293)
+                f.HrmsSum[id] = f.HrmsSum[id] + h * h;
+            }
+            emax = (T)-1000;
+            emin = (T)1000;
+        }
+        f.Emax[id] = emax;
+        f.Emin[id] = emin;
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_end(Grid g, Fields<T> f, int track_hmax) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     T v = (T)0;
+    const int mflag = g.stats ? (int)f.dsc[S_MFLAG] : 0;
     if (i < g.Mloc && j < g.Nloc) {
         const size_t id = IDX(i, j);
+        if (mflag) mean_cell(g, f, id, mflag);
         const T eta = f.Eta[id];
-        if (track_hmax && f.MASK[id] > 0 && eta > f.Hmax[id]) f.Hmax[id] = eta;
+        // MAX_MIN_PROPERTY (misc.F:323-350), wet cells
+        if (f.MASK[id] > 0) {
+            if (track_hmax && eta > f.Hmax[id]) f.Hmax[id] = eta;
+            if (g.track_hmin && eta < f.Hmin[id]) f.Hmin[id] = eta;
+            if (g.track_umax || g.track_mfmax) {
+                const T u = f.U[id], w = f.V[id];
+                if (g.track_umax) {
+                    const T mv = fsqrt(u * u + w * w);
+                    if (mv > f.Umax[id]) f.Umax[id] = mv;
+                }
+                if (g.track_mfmax) {
+                    const T mv = (u * u + w * w) * (f.H[id]);
+                    if (mv > f.MFmax[id]) f.MFmax[id] = mv;
+                }
+            }
+        }
         if (i >= g.ib && i <= g.ie && j >= g.jb && j <= g.je) {
             const T a = fabs_(eta);
             v = (a == a) ? a : (T)INFINITY;  // NaN -> +inf
         }
     }
+    // block maximum, then one atomicMax per block on the (order-preserving)
+    // bits of the non-negative double
+    __shared__ T sm[32];
     for (int o = 16; o > 0; o >>= 1) {
         const T w = __shfl_xor_sync(0xffffffffu, v, o);
         v = w > v ? w : v;
     }
-    if (((threadIdx.x + threadIdx.y * blockDim.x) & 31) == 0)
-        atomicMax(f.etamax_bits, (unsigned long long)__double_as_longlong((double)v));
+    const int t = threadIdx.x + threadIdx.y * blockDim.x;
+    const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+    if ((t & 31) == 0) sm[t >> 5] = v;
+    __syncthreads();
+    if (t < 32) {
+        v = t < nw ? sm[t] : (T)0;
+        for (int o = 16; o > 0; o >>= 1) {
+            const T w = __shfl_xor_sync(0xffffffffu, v, o);
+            v = w > v ? w : v;
+        }
+        if (t == 0) atomicMax(f.etamax_bits, (unsigned long long)__double_as_longlong((double)v));
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -2370,6 +2526,9 @@ template <typename T> void launch_estimate_dt(fw_ctx *c) {
 
 template <typename T> void launch_begin_step(fw_ctx *c) {
     const Grid &g = c->g;
+    const int nring = 6 * g.Mloc + 6 * g.Nglob;
+    k_eta0_ring<T><<<(nring + 255) / 256, 256, 0, c->stream>>>(g, c->F<T>());
+    note(c);
     launch_ghost<T>(c, g.visc_breaking != 0);
     k_begin<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
     note(c);
@@ -2516,6 +2675,10 @@ template <typename T> void launch_breaking(fw_ctx *c) {
 
 template <typename T> void launch_end_step(fw_ctx *c) {
     const Grid &g = c->g;
+    if (g.stats) {
+        k_tsum<<<1, 1, 0, c->stream>>>(g, c->F<T>().dsc, c->F<T>().fsc);
+        note(c);
+    }
     k_end<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>(), c->p.track_hmax);
     note(c);
 }

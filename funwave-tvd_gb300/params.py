@@ -36,6 +36,9 @@ PARAM_DEFAULTS = {
     # build-side options of this library (not reference keys)
     "SPREADING": "WRAPPED_NORMAL", "SPREADING_S": 10.0,
     "PRECISION": "FP64", "OUT_Hmax": False,
+    # statistics (MAX_MIN_PROPERTY switches, MIXING_STUFF times)
+    "OUT_Hmin": False, "OUT_Umax": False, "OUT_MFmax": False,
+    "STEADY_TIME": 999999.0, "T_INTV_mean": 999999.0,
 }
 
 _BOOL = {k for k, v in PARAM_DEFAULTS.items() if isinstance(v, bool)}

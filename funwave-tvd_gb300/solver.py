@@ -118,6 +118,8 @@ class FwParams(ctypes.Structure):
         ("spreading", ctypes.c_int), ("spread_s", ctypes.c_double),
         ("precision", ctypes.c_int), ("device", ctypes.c_int),
         ("track_hmax", ctypes.c_int),
+        ("track_hmin", ctypes.c_int), ("track_umax", ctypes.c_int), ("track_mfmax", ctypes.c_int),
+        ("steady_time", ctypes.c_double), ("t_intv_mean", ctypes.c_double),
     ]
 
 
@@ -141,7 +143,8 @@ _KEYS = {
     "FreqMin": "freq_min", "FreqMax": "freq_max", "GammaTMA": "gamma_tma",
     "Hmo": "hmo", "ThetaPeak": "theta_peak", "Sigma_Theta": "sigma_theta",
     "Nfreq": "nfreq", "Ntheta": "ntheta", "SPREADING_S": "spread_s",
-    "OUT_Hmax": "track_hmax",
+    "OUT_Hmax": "track_hmax", "OUT_Hmin": "track_hmin", "OUT_Umax": "track_umax",
+    "OUT_MFmax": "track_mfmax", "STEADY_TIME": "steady_time", "T_INTV_mean": "t_intv_mean",
 }
 _WK = {"NONE": 0, "WK_REG": 1, "JON_2D": 2}
 

@@ -88,6 +88,10 @@ typedef struct fw_params {
     int    precision;             /* FW_PREC_FP64 or FW_PREC_MIXED */
     int    device;                /* CUDA device ordinal */
     int    track_hmax;            /* OUT_Hmax: keep the running max of eta */
+    /* statistics (misc.F:307-383, mixing.F:53-305) */
+    int    track_hmin, track_umax, track_mfmax;  /* OUT_Hmin, OUT_Umax, OUT_MFmax (F) */
+    double steady_time;           /* STEADY_TIME (LARGE): time means and wave heights from then on */
+    double t_intv_mean;           /* T_INTV_mean (LARGE): averaging interval */
 } fw_params;
 
 typedef struct fw_ctx fw_ctx;
@@ -116,12 +120,15 @@ int fw_init(fw_ctx *ctx, const double *depth, const double *eta, const double *u
  * "HV","H","MASK","MASK9","Depth","Depthx","Depthy","P","Q","Fx","Fy","Gx",
  * "Gy","U4","V4","U1p","V1p","Udisp","Vdisp","ETAx","ETAy","ETAT","AGE",
  * "nu_break","SPONGE","Cd","CD_4_SPONGE","MASK_STRUC","Eta0","Ubar0",
- * "Vbar0","U0","V0","SourceX","SourceY","WaveMaker_Mass","HeightMax").
+ * "Vbar0","U0","V0","SourceX","SourceY","WaveMaker_Mass","HeightMax"; with
+ * statistics on: "HeightMin","VelocityMax","MomentumFluxMax","ETAmean",
+ * "Umean","Vmean","ETA2mean","SigWaveHeight","WaveHeightAve",
+ * "WaveHeightRMS","Emax","Emin","Num_Zero_Up" (a count, as double)).
  * host points to a Fortran-ordered array of the field's full extent
  * (double, or int32 for MASK/MASK9/MASK_STRUC).  Synchronous. */
 int fw_get_field(fw_ctx *ctx, const char *name, void *host);
 int fw_set_field(fw_ctx *ctx, const char *name, const void *host);
-/* scalars "TIME","DT","EtaBlowVal","T_brk","Width_WK","ilo","ihi","jlo","jhi" */
+/* scalars "TIME","DT","EtaBlowVal","T_brk","Width_WK","ilo","ihi","jlo","jhi","T_sum" */
 int fw_get_scalar(fw_ctx *ctx, const char *name, double *value);
 int fw_set_scalar(fw_ctx *ctx, const char *name, double value);
 
@@ -131,8 +138,9 @@ int fw_set_scalar(fw_ctx *ctx, const char *name, double value);
 int fw_begin_step(fw_ctx *ctx);
 /* One SSP-RK stage, istage = 1..3: main.F:382-485. */
 int fw_stage(fw_ctx *ctx, int istage);
-/* MAX_MIN_PROPERTY (Hmax) and CHECK_BLOWUP: main.F:509-512. *status gets
- * FW_OK, FW_ERR_BLOWUP or FW_ERR_NAN. */
+/* MIXING_STUFF (time means from STEADY_TIME on), MAX_MIN_PROPERTY and
+ * CHECK_BLOWUP: main.F:496-517. *status gets FW_OK, FW_ERR_BLOWUP or
+ * FW_ERR_NAN. */
 int fw_end_step(fw_ctx *ctx, int *status);
 /* nsteps whole steps (fw_begin_step + 3 fw_stage + fw_end_step), replayed
  * from a CUDA graph; *status as fw_end_step for the last step, checked

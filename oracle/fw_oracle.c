@@ -56,6 +56,11 @@ struct ofw_ctx {
         *DUtx, *DVty, *DUtxx, *DUtxy, *DVtxy, *DVtyy, *U4, *V4, *U1p, *V1p,
         *U1pp, *V1pp, *U2, *V2, *U3, *V3, *SourceX, *SourceY, *WaveMaker_Mass,
         *AGE, *nu_break, *HeightMax;
+    /* statistics: MAX_MIN_PROPERTY and CALCULATE_MEAN */
+    double T_sum;
+    double *HeightMin, *VelocityMax, *MomentumFluxMax, *ETAmean, *Umean, *Vmean, *ETAsum, *Usum, *Vsum,
+        *ETA2sum, *ETA2mean, *SigWaveHeight, *Emax, *Emin, *HavgSum, *HrmsSum, *WaveHeightAve, *WaveHeightRMS;
+    int *Num_Zero_Up;
     int *MASK, *MASK9, *MASK_STRUC;
     /* x-face arrays */
     double *Depthx, *P, *Fx, *Gx, *UxL, *UxR, *VxL, *VxR, *HUxL, *HUxR, *HVxL,
@@ -114,6 +119,10 @@ static const field_desc FIELDS[] = {
     FD(V4, 0), FD(U1p, 0), FD(V1p, 0), FD(U1pp, 0), FD(V1pp, 0), FD(U2, 0),
     FD(V2, 0), FD(U3, 0), FD(V3, 0), FD(SourceX, 0), FD(SourceY, 0),
     FD(WaveMaker_Mass, 0), FD(AGE, 0), FD(nu_break, 0), FD(HeightMax, 0),
+    FD(HeightMin, 0), FD(VelocityMax, 0), FD(MomentumFluxMax, 0), FD(ETAmean, 0), FD(Umean, 0),
+    FD(Vmean, 0), FD(ETAsum, 0), FD(Usum, 0), FD(Vsum, 0), FD(ETA2sum, 0), FD(ETA2mean, 0),
+    FD(SigWaveHeight, 0), FD(Emax, 0), FD(Emin, 0), FD(HavgSum, 0), FD(HrmsSum, 0),
+    FD(WaveHeightAve, 0), FD(WaveHeightRMS, 0), FI(Num_Zero_Up, 0),
     FI(MASK, 0), FI(MASK9, 0), FI(MASK_STRUC, 0),
     FD(Depthx, 1), FD(P, 1), FD(Fx, 1), FD(Gx, 1), FD(UxL, 1), FD(UxR, 1),
     FD(VxL, 1), FD(VxR, 1), FD(HUxL, 1), FD(HUxR, 1), FD(HVxL, 1), FD(HVxR, 1),
@@ -203,6 +212,7 @@ double ofw_get_scalar(ofw_ctx *o, const char *n) {
     if (!strcmp(n, "ihi")) return o->ihi;
     if (!strcmp(n, "jlo")) return o->jlo;
     if (!strcmp(n, "jhi")) return o->jhi;
+    if (!strcmp(n, "T_sum")) return o->T_sum;
     return NAN;
 }
 
@@ -1479,11 +1489,97 @@ int ofw_check_blowup(ofw_ctx *o) {
     return (mx > o->EtaBlowVal || nan) ? 1 : 0;
 }
 
-/* MAX_MIN_PROPERTY (misc.F:307-383), OUT_Hmax only */
+/* MAX_MIN_PROPERTY (misc.F:307-383): running maxima/minima over wet cells
+ * of every Mloc x Nloc cell, each behind its OUT_* switch.  OUT_Hmax is
+ * always on here (the GPU library keeps it behind track_hmax). */
 void ofw_max_min_property(ofw_ctx *o) {
     const size_t nc = (size_t)o->Mloc * o->Nloc;
-    for (size_t k = 0; k < nc; k++)
-        if (o->MASK[k] > 0 && o->Eta[k] > o->HeightMax[k]) o->HeightMax[k] = o->Eta[k];
+    for (size_t k = 0; k < nc; k++) {
+        if (o->MASK[k] <= 0) continue;
+        const double eta = o->Eta[k], u = o->U[k], v = o->V[k];
+        if (eta > o->HeightMax[k]) o->HeightMax[k] = eta;
+        if (o->p.track_hmin && eta < o->HeightMin[k]) o->HeightMin[k] = eta;
+        if (o->p.track_umax) {
+            const double maxv = sqrt(u * u + v * v);
+            if (maxv > o->VelocityMax[k]) o->VelocityMax[k] = maxv;
+        }
+        if (o->p.track_mfmax) {
+            const double maxv = (u * u + v * v) * (o->H[k]);
+            if (maxv > o->MomentumFluxMax[k]) o->MomentumFluxMax[k] = maxv;
+        }
+    }
+}
+
+/* MIXING_STUFF / CALCULATE_MEAN (mixing.F:53-78, 108-305) from STEADY_TIME
+ * on: time sums of Eta, U, V and (Eta-ETAmean)^2 over intervals of
+ * T_INTV_mean, their means at the end of each interval, and zero-up-
+ * crossing wave heights.  The radiation-stress, momentum-flux and breaking-
+ * dissipation sums of the same routine are not restated.  ETAsum, Usum,
+ * Vsum, ETA2sum, ETA2mean and SigWaveHeight start at zero (the reference
+ * allocates them without setting them).  The literal 4.004 is default REAL. */
+void ofw_mixing_stuff(ofw_ctx *o) {
+    if (!(o->TIME >= o->p.steady_time)) return;
+    const size_t nc = (size_t)o->Mloc * o->Nloc;
+    const double DT = o->DT;
+    o->T_sum = o->T_sum + DT;
+    if (o->T_sum >= o->p.t_intv_mean) {
+        const double Ts = o->T_sum;
+        for (size_t k = 0; k < nc; k++) {
+            const double d = o->Eta[k] - o->ETAmean[k];
+            o->ETA2sum[k] = d * d * DT + o->ETA2sum[k];
+            o->ETA2mean[k] = o->ETA2sum[k] / Ts;
+            o->Usum[k] = o->U[k] * DT + o->Usum[k];
+            o->Vsum[k] = o->V[k] * DT + o->Vsum[k];
+            o->ETAsum[k] = o->Eta[k] * DT + o->ETAsum[k];
+            o->Umean[k] = o->Usum[k] / Ts;
+            o->Vmean[k] = o->Vsum[k] / Ts;
+            o->ETAmean[k] = o->ETAsum[k] / Ts;
+        }
+        o->T_sum = o->T_sum - o->p.t_intv_mean;
+        const double c4 = (double)(float)4.004;
+        for (size_t k = 0; k < nc; k++) {
+            o->Usum[k] = 0.0;
+            o->Vsum[k] = 0.0;
+            o->ETAsum[k] = 0.0;
+            o->ETA2sum[k] = 0.0;
+            o->SigWaveHeight[k] = c4 * sqrt(o->ETA2mean[k]);
+            if (o->Num_Zero_Up[k] >= 2) {
+                o->WaveHeightAve[k] = o->HavgSum[k] / o->Num_Zero_Up[k];
+                o->WaveHeightRMS[k] = sqrt(o->HrmsSum[k] / o->Num_Zero_Up[k]);
+            }
+        }
+    } else {
+        for (size_t k = 0; k < nc; k++) {
+            o->Usum[k] = o->U[k] * DT + o->Usum[k];
+            o->Vsum[k] = o->V[k] * DT + o->Vsum[k];
+            o->ETAsum[k] = o->Eta[k] * DT + o->ETAsum[k];
+            const double d = o->Eta[k] - o->ETAmean[k];
+            o->ETA2sum[k] = d * d * DT + o->ETA2sum[k];
+            const double eta = o->Eta[k];
+            if (eta > o->Emax[k]) o->Emax[k] = eta;
+            if (eta < o->Emin[k]) o->Emin[k] = eta;
+            const double tmpe = eta - o->ETAmean[k];
+            const double tmp0 = o->Eta0[k] - o->ETAmean[k];
+            if (tmpe > tmp0 && tmpe * tmp0 <= 0.0) {
+                o->Num_Zero_Up[k] = o->Num_Zero_Up[k] + 1;
+                if (o->Num_Zero_Up[k] >= 2) {
+                    const double h = o->Emax[k] - o->Emin[k];
+                    o->HavgSum[k] = (o->HavgSum[k] + o->Emax[k]) - o->Emin[k];  /* left to right */
+                    o->HrmsSum[k] = o->HrmsSum[k] + h * h;
+                }
+                o->Emax[k] = -1000.0;
+                o->Emin[k] = 1000.0;
+            }
+        }
+    }
+}
+
+/* after the stages (main.F:496-517): MIXING_STUFF, MAX_MIN_PROPERTY,
+ * CHECK_BLOWUP */
+int ofw_end_step(ofw_ctx *o) {
+    ofw_mixing_stuff(o);
+    ofw_max_min_property(o);
+    return ofw_check_blowup(o);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1514,7 +1610,7 @@ void ofw_stage(ofw_ctx *o, int istage) {
 int ofw_step(ofw_ctx *o) {
     ofw_begin_step(o);
     for (int s = 1; s <= 3; s++) ofw_stage(o, s);
-    return ofw_check_blowup(o);
+    return ofw_end_step(o);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -63,6 +63,10 @@ typedef struct {
     int    nfreq, ntheta;       /* Nfreq, Ntheta */
     int    spreading;           /* 0: reference wrapped normal; 1: cos^2s (extension) */
     double spread_s;            /* s of cos^2s */
+    /* statistics (misc.F:307-383, mixing.F:53-305) */
+    int    track_hmax, track_hmin, track_umax, track_mfmax;  /* OUT_Hmax, OUT_Hmin, OUT_Umax, OUT_MFmax (F) */
+    double steady_time;         /* STEADY_TIME (LARGE): time means from this time on */
+    double t_intv_mean;         /* T_INTV_mean (LARGE): averaging interval */
 } ofw_params;
 
 typedef struct ofw_ctx ofw_ctx;
@@ -114,7 +118,9 @@ void ofw_sponge_damping(ofw_ctx *o);           /* sponge.F:52 */
 void ofw_begin_step(ofw_ctx *o);               /* main.F:295-331 */
 void ofw_stage(ofw_ctx *o, int istage);        /* main.F:382-485 */
 int  ofw_check_blowup(ofw_ctx *o);             /* misc.F:394 */
-void ofw_max_min_property(ofw_ctx *o);         /* misc.F:307 (Hmax only) */
+void ofw_max_min_property(ofw_ctx *o);         /* misc.F:307 (Hmax, Hmin, Umax, MFmax) */
+void ofw_mixing_stuff(ofw_ctx *o);             /* mixing.F:53 (CALCULATE_MEAN, time means and wave heights) */
+int  ofw_end_step(ofw_ctx *o);                 /* main.F:496-517: MIXING_STUFF, MAX_MIN_PROPERTY, CHECK_BLOWUP */
 
 /* OpenMP threads used by the parallel-safe loops (0 = library default). */
 void ofw_set_threads(int n);

@@ -50,6 +50,8 @@ class OfwParams(ctypes.Structure):
         ("sigma_theta", ctypes.c_double),
         ("nfreq", ctypes.c_int), ("ntheta", ctypes.c_int),
         ("spreading", ctypes.c_int), ("spread_s", ctypes.c_double),
+        ("track_hmax", ctypes.c_int), ("track_hmin", ctypes.c_int), ("track_umax", ctypes.c_int),
+        ("track_mfmax", ctypes.c_int), ("steady_time", ctypes.c_double), ("t_intv_mean", ctypes.c_double),
     ]
 
 
@@ -76,6 +78,8 @@ _KEYMAP = {
     "FreqMax": "freq_max", "GammaTMA": "gamma_tma", "Hmo": "hmo",
     "ThetaPeak": "theta_peak", "Sigma_Theta": "sigma_theta", "Nfreq": "nfreq",
     "Ntheta": "ntheta", "SPREADING_S": "spread_s",
+    "OUT_Hmax": "track_hmax", "OUT_Hmin": "track_hmin", "OUT_Umax": "track_umax",
+    "OUT_MFmax": "track_mfmax", "STEADY_TIME": "steady_time", "T_INTV_mean": "t_intv_mean",
 }
 _WAVEMAKERS = {"NONE": 0, "WK_REG": 1, "JON_2D": 2}
 
@@ -116,12 +120,14 @@ def lib():
         L.ofw_step.restype = ctypes.c_int
         for n in ("exchange", "estimate_dt", "cal_dispersion", "fluxes", "source_terms",
                   "update_mask", "wave_breaking", "sponge_damping", "begin_step",
-                  "max_min_property"):
+                  "max_min_property", "mixing_stuff"):
             getattr(L, "ofw_" + n).argtypes = [vp]
         L.ofw_estimate_huv.argtypes = [vp, ctypes.c_int]
         L.ofw_stage.argtypes = [vp, ctypes.c_int]
         L.ofw_check_blowup.argtypes = [vp]
         L.ofw_check_blowup.restype = ctypes.c_int
+        L.ofw_end_step.argtypes = [vp]
+        L.ofw_end_step.restype = ctypes.c_int
         L.ofw_set_threads.argtypes = [ctypes.c_int]
         L.ofw_get_threads.restype = ctypes.c_int
         _lib = L
@@ -132,6 +138,8 @@ def make_params(p):
     """Fill an OfwParams from an input.txt-style dictionary (defaults applied
     by the caller)."""
     s = OfwParams()
+    s.steady_time = 999999.0   # STEADY_TIME and T_INTV_mean default to LARGE
+    s.t_intv_mean = 999999.0
     for k, v in p.items():
         if k in _KEYMAP:
             name = _KEYMAP[k]
@@ -227,6 +235,9 @@ class Oracle:
 
     def begin_step(self):
         self.L.ofw_begin_step(self.ctx)
+
+    def end_step(self):
+        return self.L.ofw_end_step(self.ctx)
 
     def stage(self, istage):
         self.L.ofw_stage(self.ctx, int(istage))

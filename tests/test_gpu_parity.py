@@ -76,7 +76,7 @@ def _unit_pipeline(fw, oracle_mod, params, depth, state, nstages=6, phases=None)
         o.begin_step()
         assert abs(s.scalar("DT") - o.scalar("DT")) <= 1e-12 * o.scalar("DT")
         assert abs(s.scalar("TIME") - o.scalar("TIME")) <= 1e-12 * o.scalar("TIME")
-        for name in ("U", "V", "HU", "HV", "Eta", "U0", "V0"):
+        for name in ("U", "V", "HU", "HV", "Eta", "U0", "V0", "Eta0", "Ubar0", "Vbar0"):
             _cmp(s, o, name, "all")
         for ist in (1, 2, 3):
             if stage >= nstages:
