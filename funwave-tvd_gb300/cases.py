@@ -72,7 +72,7 @@ def shoal_jonswap(Mglob=2048, Nglob=2048, dx=2.0, seed=0, **overrides):
     X, Y = np.meshgrid(x, y, indexing="ij")
     r2 = ((X - xc) / 200.0) ** 2 + ((Y - yc) / 150.0) ** 2
     depth = depth - 8.0 * np.sqrt(np.maximum(0.0, 1.0 - r2))
-    nf, nt = 50, 30
+    nf, nt = int(overrides.get("Nfreq", 50)), int(overrides.get("Ntheta", 30))
     rng = np.random.default_rng(seed)
     phases = np.asfortranarray(rng.uniform(0.0, 2.0 * np.pi, size=(nf, nt)))
     p = {
