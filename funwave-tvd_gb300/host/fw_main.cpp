@@ -1,0 +1,361 @@
+// fw_main.cpp -- a host driver with the shape of the reference's main
+// program (src/main.F:45-575) over the C ABI of libfunwave_gpu.
+//
+//   fw_main [input.txt] [--dry-run]
+//
+// It reads input.txt with the reference's rules (READ_VALUE,
+// mod_input.F:271-308: "KEY = value", "!" starts a comment, the first
+// matching line wins), builds the depth as INITIALIZATION does for
+// DEPTH_TYPE DATA / FLAT / SLOPE (init.F:684-760), creates and initialises
+// the GPU context, then runs the time loop of main.F:284-535: OUTPUT at the
+// top of every pass (io.F:52-134, PLOT_COUNT starting at PLOT_INTV so that
+// the initial state is file 00001, init.F:631), one whole step per pass
+// (fw_step), CHECK_BLOWUP's dump to file 99999 (misc.F:394-433).  PREVIEW
+// (io.F:4304-4621) writes eta_NNNNN, u_NNNNN, v_NNNNN, mask_NNNNN (and
+// hmax_NNNNN with OUT_Hmax) in RESULT_FOLDER with PutFile's ASCII format
+// (Mglob values per line, E16.6E4, interior only, io.F:4895-4921), dep.out
+// with the first file, and appends "TIME DT" to time_dt.out.
+//
+// --dry-run parses, builds the depth and writes dep.out without touching a
+// GPU.  JON_2D phases, which the reference draws from the compiler's
+// rand(0), come from SplitMix64 seeded by the key PHASE_SEED (default 1).
+#include <cctype>
+#include <cinttypes>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "funwave_gpu.h"
+
+namespace {
+
+constexpr double LARGE = 999999.0;
+constexpr double TWO_PI = 6.283185307179586;
+
+std::string upper(std::string s) {
+    for (auto &ch : s) ch = (char)std::toupper((unsigned char)ch);
+    return s;
+}
+std::string trim(const std::string &s) {
+    size_t a = s.find_first_not_of(" \t\r\n'\""), b = s.find_last_not_of(" \t\r\n'\"");
+    return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+// input.txt: key -> value text, first occurrence wins
+struct Input {
+    std::map<std::string, std::string> kv;
+    bool load(const std::string &path) {
+        std::ifstream f(path);
+        if (!f) return false;
+        std::string line;
+        while (std::getline(f, line)) {
+            const size_t bang = line.find('!');
+            if (bang != std::string::npos) line = line.substr(0, bang);
+            const size_t eq = line.find('=');
+            if (eq == std::string::npos) continue;
+            const std::string k = trim(line.substr(0, eq)), v = trim(line.substr(eq + 1));
+            if (!k.empty() && !kv.count(k)) kv[k] = v;
+        }
+        return true;
+    }
+    bool has(const char *k) const { return kv.count(k) != 0; }
+    std::string str(const char *k, const char *def) const { return has(k) ? kv.at(k) : std::string(def); }
+    double num(const char *k, double def) const {
+        if (!has(k)) return def;
+        std::string v = kv.at(k);
+        for (auto &ch : v)
+            if (ch == 'd' || ch == 'D') ch = 'e';  // Fortran double exponent
+        return std::strtod(v.c_str(), nullptr);
+    }
+    int flag(const char *k, int def) const {
+        if (!has(k)) return def;
+        const std::string u = upper(kv.at(k));
+        const size_t p = u.find_first_not_of('.');
+        return (p != std::string::npos && u[p] == 'T') ? 1 : 0;
+    }
+};
+
+// the input.txt keys of fw_params (names and defaults of src/io.F)
+void fill_params(const Input &in, fw_params &p) {
+    fw_params_default(&p);
+    p.Mglob = (int)in.num("Mglob", 0);
+    p.Nglob = (int)in.num("Nglob", 0);
+    p.DX = in.num("DX", 0.0);
+    p.DY = in.num("DY", 0.0);
+    p.periodic = in.flag("PERIODIC", p.periodic);
+    p.dispersion = in.flag("DISPERSION", p.dispersion);
+    p.gamma1 = in.num("Gamma1", p.gamma1);
+    p.gamma2 = in.num("Gamma2", p.gamma2);
+    p.gamma3 = in.num("Gamma3", p.gamma3);
+    p.beta_ref = in.num("Beta_ref", p.beta_ref);
+    p.viscosity_breaking = in.flag("VISCOSITY_BREAKING", p.viscosity_breaking);
+    p.show_breaking = in.flag("SHOW_BREAKING", p.show_breaking);
+    p.cbrk1 = in.num("Cbrk1", p.cbrk1);
+    p.cbrk2 = in.num("Cbrk2", p.cbrk2);
+    p.wavemaker_cbrk = in.num("WAVEMAKER_Cbrk", p.wavemaker_cbrk);
+    p.nu_bkg = in.num("nu_bkg", p.nu_bkg);
+    p.swe_eta_dep = in.num("SWE_ETA_DEP", p.swe_eta_dep);
+    p.cfl = in.num("CFL", p.cfl);
+    if (in.has("DT_fixed")) {
+        p.fixed_dt = 1;
+        p.dt_fixed = in.num("DT_fixed", 0.0);
+    }
+    p.froude_cap = in.num("FroudeCap", p.froude_cap);
+    p.min_depth = in.num("MinDepth", p.min_depth);
+    p.min_depth_frc = in.num("MinDepthFrc", p.min_depth_frc);
+    p.eta_limiter = in.flag("ETA_LIMITER", p.eta_limiter);
+    p.trough_limit = in.num("TroughLimit", -LARGE);
+    p.crest_limit = in.num("CrestLimit", LARGE);
+    p.direct_sponge = in.flag("DIRECT_SPONGE", p.direct_sponge);
+    p.sponge_west = in.num("Sponge_west_width", 0.0);
+    p.sponge_east = in.num("Sponge_east_width", 0.0);
+    p.sponge_south = in.num("Sponge_south_width", 0.0);
+    p.sponge_north = in.num("Sponge_north_width", 0.0);
+    p.r_sponge = in.num("R_sponge", p.r_sponge);
+    p.a_sponge = in.num("A_sponge", p.a_sponge);
+    p.friction_sponge = in.flag("FRICTION_SPONGE", p.friction_sponge);
+    p.cd_fixed = in.num("Cd", 0.0);
+    const std::string wk = upper(in.str("WAVEMAKER", "NONE"));
+    p.wavemaker = wk.rfind("WK_REG", 0) == 0 ? FW_WK_REG : wk.rfind("JON_2D", 0) == 0 ? FW_WK_JON_2D : -1;
+    if (wk == "NONE" || wk.empty()) p.wavemaker = FW_WK_NONE;
+    p.amp_wk = in.num("AMP_WK", 0.0);
+    p.tperiod = in.num("Tperiod", 0.0);
+    p.dep_wk = in.num("DEP_WK", 0.0);
+    p.xc_wk = in.num("Xc_WK", 0.0);
+    p.yc_wk = in.num("Yc_WK", 0.0);
+    p.theta_wk = in.num("Theta_WK", 0.0);
+    p.delta_wk = in.num("Delta_WK", p.delta_wk);
+    p.time_ramp = in.num("Time_ramp", 0.0);
+    p.ywidth_wk = in.num("Ywidth_WK", LARGE);
+    p.freq_peak = in.num("FreqPeak", 0.0);
+    p.freq_min = in.num("FreqMin", 0.0);
+    p.freq_max = in.num("FreqMax", 0.0);
+    p.gamma_tma = in.num("GammaTMA", 3.3);
+    p.hmo = in.num("Hmo", 0.0);
+    p.theta_peak = in.num("ThetaPeak", 0.0);
+    p.sigma_theta = in.num("Sigma_Theta", 10.0);
+    p.nfreq = (int)in.num("Nfreq", 0);
+    p.ntheta = (int)in.num("Ntheta", 1);
+    p.spreading = upper(in.str("SPREADING", "WRAPPED_NORMAL")) == "COS2S" ? FW_SPREAD_COS2S : FW_SPREAD_WRAPPED_NORMAL;
+    p.spread_s = in.num("SPREADING_S", 10.0);
+    p.precision = upper(in.str("PRECISION", "FP64")) == "MIXED" ? FW_PREC_MIXED : FW_PREC_FP64;
+    p.track_hmax = in.flag("OUT_Hmax", 0);
+    p.track_hmin = in.flag("OUT_Hmin", 0);
+    p.track_umax = in.flag("OUT_Umax", 0);
+    p.track_mfmax = in.flag("OUT_MFmax", 0);
+    p.steady_time = in.num("STEADY_TIME", LARGE);
+    p.t_intv_mean = in.num("T_INTV_mean", LARGE);
+}
+
+// DEPTH_TYPE DATA / FLAT / SLOPE (init.F:684-760), interior Mglob x Nglob,
+// column-major
+bool build_depth(const Input &in, const fw_params &p, std::vector<double> &d, std::string &err) {
+    const int M = p.Mglob, N = p.Nglob;
+    d.assign((size_t)M * N, 0.0);
+    const std::string type = upper(in.str("DEPTH_TYPE", "DATA")).substr(0, 3);
+    const double flat = in.num("DEPTH_FLAT", 10.0);
+    if (type == "DAT") {
+        const std::string file = in.str("DEPTH_FILE", "depth.txt");
+        std::ifstream f(file);
+        if (!f) {
+            err = file + " CANNOT BE FOUND";
+            return false;
+        }
+        // list-directed READ(1,*) row by row: Mglob values per J, J outer
+        for (int j = 0; j < N; j++)
+            for (int i = 0; i < M; i++) {
+                std::string tok;
+                if (!(f >> tok)) {
+                    err = "depth file " + file + " ends early";
+                    return false;
+                }
+                for (auto &ch : tok)
+                    if (ch == 'd' || ch == 'D') ch = 'e';
+                d[(size_t)i + (size_t)j * M] = std::strtod(tok.c_str(), nullptr);
+            }
+    } else if (type == "FLA") {
+        for (auto &v : d) v = flat;
+    } else if (type == "SLO") {
+        const double slp = in.num("SLP", 0.0), xslp = in.num("Xslp", 0.0);
+        const int i0 = (int)(xslp / p.DX) + 1;  // Fortran INT truncates
+        for (int j = 0; j < N; j++)
+            for (int I = 1; I <= M; I++)
+                d[(size_t)(I - 1) + (size_t)j * M] = I >= i0 ? flat - slp * (I - i0) * p.DX : flat;
+    } else {
+        err = "DEPTH_TYPE " + type + " is not built";
+        return false;
+    }
+    return true;
+}
+
+// PutFile's ASCII line format: E16.6E4 of REAL(SP) values
+void e16_6e4(float v, char *out) {
+    if (v == 0.0f) {
+        std::snprintf(out, 17, "%16s", "0.000000E+0000");
+        return;
+    }
+    char buf[32];
+    std::snprintf(buf, sizeof buf, "%.5E", (double)v);  // d.dddddE+xx, six significant digits
+    const bool neg = buf[0] == '-';
+    const char *m = buf + (neg ? 1 : 0);
+    const int e = std::atoi(std::strchr(m, 'E') + 1) + 1;
+    char digits[7] = {m[0], m[2], m[3], m[4], m[5], m[6], 0};
+    char body[48], res[64];
+    std::snprintf(body, sizeof body, "%s0.%sE%c%04d", neg ? "-" : "", digits, e < 0 ? '-' : '+', std::abs(e));
+    std::snprintf(res, sizeof res, "%16s", body);  // at most 15 characters: right-aligned in 16
+    std::memcpy(out, res, 16);
+    out[16] = 0;
+}
+
+bool put_file(const std::string &path, const std::vector<double> &phi, const fw_params &p) {
+    FILE *f = std::fopen(path.c_str(), "w");
+    if (!f) return false;
+    const int Mloc = p.Mglob + 6;
+    char cell[17];
+    for (int J = 4; J <= p.Nglob + 3; J++) {
+        for (int I = 4; I <= p.Mglob + 3; I++) {
+            e16_6e4((float)phi[(size_t)(I - 1) + (size_t)(J - 1) * Mloc], cell);
+            std::fputs(cell, f);
+        }
+        std::fputc('\n', f);
+    }
+    return std::fclose(f) == 0;
+}
+
+std::string numbered(const std::string &dir, const char *stem, int icount) {
+    char b[16];
+    std::snprintf(b, sizeof b, "%05d", icount % 100000);
+    return dir + stem + "_" + b;
+}
+
+uint64_t splitmix64(uint64_t &s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+int fail(const char *what, int rc) {
+    std::fprintf(stderr, "fw_main: %s: %s (%d)\n", what, fw_strerror(rc), rc);
+    return 1;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    std::string path = "input.txt";
+    bool dry = false;
+    for (int a = 1; a < argc; a++) {
+        if (!std::strcmp(argv[a], "--dry-run")) dry = true;
+        else path = argv[a];
+    }
+    Input in;
+    if (!in.load(path)) {
+        std::fprintf(stderr, "fw_main: cannot read %s\n", path.c_str());
+        return 1;
+    }
+    fw_params p;
+    fill_params(in, p);
+    if (p.Mglob <= 0 || p.Nglob <= 0 || !(p.DX > 0) || !(p.DY > 0)) {
+        std::fprintf(stderr, "fw_main: Mglob, Nglob, DX and DY are required\n");
+        return 1;
+    }
+    if (p.wavemaker < 0) {
+        std::fprintf(stderr, "fw_main: WAVEMAKER %s is not built\n", in.str("WAVEMAKER", "").c_str());
+        return 1;
+    }
+    std::vector<double> depth;
+    std::string err;
+    if (!build_depth(in, p, depth, err)) {
+        std::fprintf(stderr, "fw_main: %s\n", err.c_str());
+        return 1;
+    }
+    const std::string dir = in.str("RESULT_FOLDER", "./output/");
+    const double total = in.num("TOTAL_TIME", 0.0), plot_intv = in.num("PLOT_INTV", 1.0);
+    const double plot_start = in.num("PLOT_START_TIME", 0.0);
+    std::printf("fw_main: %d x %d, DX %g DY %g, %s, TOTAL_TIME %g, PLOT_INTV %g\n", p.Mglob, p.Nglob, p.DX, p.DY,
+                p.precision == FW_PREC_MIXED ? "MIXED" : "FP64", total, plot_intv);
+
+    const int Mloc = p.Mglob + 6, Nloc = p.Nglob + 6;
+    std::vector<double> full((size_t)Mloc * Nloc, 0.0);
+    // dep.out as PREVIEW writes it with the first file (interior of Depth)
+    for (int j = 0; j < p.Nglob; j++)
+        for (int i = 0; i < p.Mglob; i++) full[(size_t)(i + 3) + (size_t)(j + 3) * Mloc] = depth[(size_t)i + (size_t)j * p.Mglob];
+    if (!put_file(dir + "dep.out", full, p)) {
+        std::fprintf(stderr, "fw_main: cannot write to %s\n", dir.c_str());
+        return 1;
+    }
+    if (dry) return 0;
+
+    std::vector<double> phases;
+    if (p.wavemaker == FW_WK_JON_2D) {
+        uint64_t s = (uint64_t)in.num("PHASE_SEED", 1.0);
+        phases.resize((size_t)p.nfreq * p.ntheta);
+        for (auto &v : phases) v = (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0) * TWO_PI;
+    }
+    fw_ctx *ctx = nullptr;
+    int rc = fw_create(&p, &ctx);
+    if (rc != FW_OK) return fail("fw_create", rc);
+    rc = fw_init(ctx, depth.data(), nullptr, nullptr, nullptr, phases.empty() ? nullptr : phases.data());
+    if (rc != FW_OK) return fail("fw_init", rc);
+
+    FILE *tdt = std::fopen("time_dt.out", "w");
+    std::vector<int> mask((size_t)Mloc * Nloc);
+    int icount = 0;
+    auto preview = [&](int number) -> int {
+        icount = number;
+        double t = 0.0, dt = 0.0;
+        fw_get_scalar(ctx, "TIME", &t);
+        fw_get_scalar(ctx, "DT", &dt);
+        std::printf("PRINTING FILE NO. %5d TIME/TOTAL: %12.3f / %12.3f\n", icount, t, total);
+        if (tdt) std::fprintf(tdt, "%.9E %.9E\n", t, dt);
+        const char *names[] = {"Eta", "U", "V"};
+        const char *stems[] = {"eta", "u", "v"};
+        for (int k = 0; k < 3; k++) {
+            int r = fw_get_field(ctx, names[k], full.data());
+            if (r != FW_OK) return r;
+            put_file(numbered(dir, stems[k], icount), full, p);
+        }
+        int r = fw_get_field(ctx, "MASK", mask.data());
+        if (r != FW_OK) return r;
+        for (size_t q = 0; q < mask.size(); q++) full[q] = mask[q];
+        put_file(numbered(dir, "mask", icount), full, p);
+        if (p.track_hmax && fw_get_field(ctx, "HeightMax", full.data()) == FW_OK)
+            put_file(numbered(dir, "hmax", icount), full, p);
+        return FW_OK;
+    };
+
+    double time = 0.0, dt = 0.0, plot_count = plot_intv;  // init.F:631
+    while (time < total) {  // DO WHILE (TIME < TOTAL_TIME)
+        // OUTPUT (io.F:52-134) at the top of the pass, with the last DT
+        if (time >= plot_start) {
+            plot_count += dt;
+            if (plot_count >= plot_intv) {
+                plot_count -= plot_intv;
+                if ((rc = preview(icount + 1)) != FW_OK) return fail("PREVIEW", rc);
+            }
+        }
+        int status = FW_OK;
+        rc = fw_step(ctx, 1, &status);
+        if (rc != FW_OK) return fail("fw_step", rc);
+        if (status != FW_OK) {
+            // CHECK_BLOWUP: dump the state as file 99999, then stop
+            std::fprintf(stderr, "fw_main: %s, dumping file 99999\n", fw_strerror(status));
+            preview(99999);
+            fw_destroy(ctx);
+            return 2;
+        }
+        fw_get_scalar(ctx, "TIME", &time);
+        fw_get_scalar(ctx, "DT", &dt);
+    }
+    if (tdt) std::fclose(tdt);
+    rc = fw_destroy(ctx);
+    std::printf("fw_main: done, TIME %.6f, %d files\n", time, icount);
+    return rc == FW_OK ? 0 : 1;
+}

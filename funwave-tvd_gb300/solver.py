@@ -62,6 +62,7 @@ def build(verbose=False):
     deps = srcs + [os.path.join(_CSRC, h) for h in os.listdir(_CSRC)
                    if h.endswith(".h") or h.endswith(".cuh")] + [_HEADER]
     if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+        build_driver()
         return out
     nvcc = os.environ.get("NVCC", "nvcc")
     common = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-I" + os.path.join(_ROOT, "include")]
@@ -81,7 +82,26 @@ def build(verbose=False):
     link = [nvcc] + arch + ["-shared", "-o", out + ".tmp"] + objs
     subprocess.run(link, check=True)
     os.replace(out + ".tmp", out)
+    build_driver()
     return out
+
+
+def driver_path():
+    return os.path.join(_BUILD, "fw_main")
+
+
+def build_driver():
+    """Compile the C++ host driver (host/fw_main.cpp) against the library."""
+    src = os.path.join(_HERE, "host", "fw_main.cpp")
+    exe = driver_path()
+    if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(src), os.path.getmtime(lib_path())):
+        return exe
+    cxx = os.environ.get("CXX", "g++")
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(_ROOT, "include"), src, "-L" + _BUILD,
+           "-lfunwave_gpu", "-Wl,-rpath,$ORIGIN", "-o", exe + ".tmp"]
+    subprocess.run(cmd, check=True)
+    os.replace(exe + ".tmp", exe)
+    return exe
 
 
 class FwParams(ctypes.Structure):

@@ -1,0 +1,128 @@
+"""The C++ host driver (funwave-tvd_gb300/host/fw_main.cpp), which has the
+shape of the reference's main program over the C ABI.
+
+CPU: input.txt parsing and the DEPTH_TYPE DATA / FLAT / SLOPE depths
+(init.F:684-760), written as dep.out in PutFile's ASCII format (io.F:4895-
+4921: Mglob values per line, E16.6E4), in --dry-run mode (no GPU).
+GPU: a short run writes eta_00001 (the initial state) and one file per
+PLOT_INTV, and its last file equals the Python Solver's state at the same
+time to the printed precision.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+
+def e16_6e4(v):
+    """Fortran E16.6E4 of float(v)."""
+    v = float(np.float32(v))
+    if v == 0.0:
+        return "%16s" % "0.000000E+0000"
+    m, e = ("%.5E" % v).split("E")
+    neg = m.startswith("-")
+    digits = m.lstrip("-").replace(".", "")
+    return "%16s" % ("%s0.%sE%s%04d" % ("-" if neg else "", digits, "-" if int(e) + 1 < 0 else "+",
+                                        abs(int(e) + 1)))
+
+
+def read_put_file(path):
+    rows = []
+    for line in open(path):
+        line = line.rstrip("\n")
+        rows.append([float(line[k:k + 16]) for k in range(0, len(line), 16)])
+    return np.array(rows).T  # (Mglob, Nglob)
+
+
+def _write_input(d, extra):
+    keys = {"Mglob": 24, "Nglob": 16, "DX": 2.0, "DY": 2.0, "RESULT_FOLDER": d + "/"}
+    keys.update(extra)
+    with open(os.path.join(d, "input.txt"), "w") as f:
+        f.write("! test deck\n")
+        for k, v in keys.items():
+            f.write("%s = %s   ! comment\n" % (k, v))
+        f.write("Mglob = 999\n")  # a later duplicate is ignored
+    return keys
+
+
+def _driver(fw):
+    fw.build()
+    return fw.solver.driver_path()
+
+
+def _dry(fw, d):
+    r = subprocess.run([_driver(fw), os.path.join(d, "input.txt"), "--dry-run"], capture_output=True, text=True,
+                       cwd=d)
+    assert r.returncode == 0, r.stderr
+    return read_put_file(os.path.join(d, "dep.out"))
+
+
+def test_format_matches_fortran_e16_6e4():
+    assert e16_6e4(0.0) == "  0.000000E+0000"
+    assert e16_6e4(1.0) == "  0.100000E+0001"
+    assert e16_6e4(-0.00123456789) == " -0.123457E-0002"
+    assert e16_6e4(999999.0) == "  0.999999E+0006"
+
+
+def test_depth_data_file(fw, tmp_path):
+    d = str(tmp_path)
+    rng = np.random.default_rng(5)
+    depth = rng.uniform(-1.0, 8.0, size=(24, 16))
+    with open(os.path.join(d, "depth.txt"), "w") as f:
+        for j in range(16):
+            f.write(" ".join("%.6f" % depth[i, j] for i in range(24)) + "\n")
+    _write_input(d, {"DEPTH_TYPE": "DATA", "DEPTH_FILE": os.path.join(d, "depth.txt")})
+    out = _dry(fw, d)
+    assert out.shape == (24, 16)
+    written = np.array([[float("%.6f" % depth[i, j]) for j in range(16)] for i in range(24)])
+    # E16.6 keeps six significant digits of the float value
+    assert np.allclose(out, written, rtol=6e-6, atol=0.0)
+    line = open(os.path.join(d, "dep.out")).readline().rstrip("\n")
+    assert len(line) == 16 * 24
+    assert line[:16] == e16_6e4(float("%.6f" % depth[0, 0]))
+
+
+def test_depth_flat_and_slope(fw, tmp_path):
+    d = str(tmp_path)
+    _write_input(d, {"DEPTH_TYPE": "FLAT", "DEPTH_FLAT": 7.5})
+    assert np.all(_dry(fw, d) == 7.5)
+    _write_input(d, {"DEPTH_TYPE": "SLOPE", "DEPTH_FLAT": 6.0, "SLP": 0.05, "Xslp": 11.0})
+    out = _dry(fw, d)
+    i0 = int(11.0 / 2.0) + 1  # Fortran INT(Xslp/DX)+1, 1-based
+    I = np.arange(1, 25)
+    expect = np.where(I >= i0, 6.0 - 0.05 * (I - i0) * 2.0, 6.0)
+    assert np.allclose(out, expect[:, None], rtol=6e-6)
+
+
+@pytest.mark.gpu
+def test_driver_run_matches_solver(fw, tmp_path):
+    d = str(tmp_path)
+    extra = {"DEPTH_TYPE": "SLOPE", "DEPTH_FLAT": 3.0, "SLP": 0.04, "Xslp": 20.0, "WAVEMAKER": "WK_REG",
+             "AMP_WK": 0.05, "Tperiod": 3.0, "DEP_WK": 3.0, "Xc_WK": 10.0, "Time_ramp": 1.0,
+             "TOTAL_TIME": 3.0, "PLOT_INTV": 1.0, "PERIODIC": "T", "MinDepth": 0.01}
+    keys = _write_input(d, extra)
+    r = subprocess.run([_driver(fw), os.path.join(d, "input.txt")], capture_output=True, text=True, cwd=d,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    files = sorted(f for f in os.listdir(d) if f.startswith("eta_"))
+    assert files[0] == "eta_00001" and len(files) >= 3
+    assert np.all(read_put_file(os.path.join(d, "eta_00001")) == 0.0)
+    times = np.loadtxt(os.path.join(d, "time_dt.out"), ndmin=2)
+    assert times.shape[0] == len(files)
+    # the same run through the Python Solver, to the last file's time
+    p = {k: v for k, v in keys.items() if k not in ("RESULT_FOLDER",)}
+    p["PERIODIC"] = True
+    i0 = int(20.0 / 2.0) + 1
+    I = np.arange(1, 25)
+    depth = np.repeat(np.where(I >= i0, 3.0 - 0.04 * (I - i0) * 2.0, 3.0)[:, None], 16, axis=1)
+    s = fw.Solver(fw.with_defaults(p), precision="FP64")
+    s.init(np.asfortranarray(depth))
+    while s.scalar("TIME") < times[-1, 0] * (1.0 - 1e-8):  # the printed TIME has 10 digits
+        s.step(1)
+    assert abs(s.scalar("TIME") - times[-1, 0]) <= 1e-6 * times[-1, 0]
+    last = read_put_file(os.path.join(d, files[-1]))
+    eta = s.get("Eta")[3:-3, 3:-3]
+    assert np.abs(eta).max() > 1e-4
+    assert np.allclose(last, eta.astype(np.float32), rtol=6e-6, atol=1e-12)
+    s.close()
