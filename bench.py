@@ -19,6 +19,10 @@ on all host cores.
 import argparse
 import json
 import os
+
+# more hardware queues for the ensemble's concurrent streams (read at the
+# first CUDA call of the process)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 import statistics
 import subprocess
 import sys
@@ -44,13 +48,26 @@ KERNEL_BYTES = {
     "flux_x": lambda T: 11 * T + 2,       # U V HU HV Eta U4 V4 Depthx + MASK MASK9 -> P Fx Gx
     "flux_y": lambda T: 11 * T + 2,
     "update": lambda T: 32 * T + 2 + 16,  # 28 fields + MASK MASK9 -> Eta Ubar Vbar H + rhs_x rhs_y
-    "tri_x": lambda T: 2 * T + 10,        # Depth MASK9 MASK rhs_x -> U
-    "tri_y": lambda T: 2 * T + 10,
+    # mixed: rhs_x + the ten float factor arrays of the constant factorised
+    # matrix (1/diag, sweep A, L*r, c', the two spike columns, a and c as
+    # float pairs for the compensated residual) -> U; FP64: Depth MASK9
+    # MASK rhs_x -> U
+    "tri_x": lambda T: 2 * T + (40 if T == 4 else 10),
+    "tri_y": lambda T: 2 * T + (40 if T == 4 else 10),
     "post": lambda T: 7 * T + 1 + 6 * T,  # U V H Ubar Vbar HU HV + MASK -> U V HU HV Ubar Vbar
     "mask": lambda T: 4 * T + 4 + 2 * T,  # Eta Depth Depthx Depthy + MASK MASK_STRUC -> MASKn MASK9 Depthx Depthy
     "break_a": lambda T: 8 * T + 2 * T,   # H ETAx ETAy ETAT Depth Eta AGE nu -> AGEn nu
     "maskmul": lambda T: 6 * T + 1 + 5 * T,
     "begin": lambda T: 8 * T + 1 + 9 * T,
+}
+# DRAM bytes per unit (dram__bytes_read.sum + dram__bytes_write.sum of one
+# ncu capture of the 2048 x 2048 mixed step, per launch / units; the tri_y
+# figure sums the partitioned y-solve kernels of one stage); see
+# profiles/launches_mixed_step_2048.md for the command and the per-launch
+# numbers
+TRAFFIC_PER_UNIT_MIXED = {
+    "tri_x": 48.6, "update": 137.0, "flux_x": 41.0, "flux_y": 41.6, "disp_b": 72.6, "disp_a": 42.7,
+    "maskmul": 30.8, "tri_y": 95.2,
 }
 # kernel launches per stage (tri_* count the partitioned solve as one)
 PER_STAGE = ["disp_a", "disp_b", "flux_x", "flux_y", "update", "tri_x", "tri_y", "post",
@@ -215,6 +232,38 @@ def e2e_run(fw, s, K):
     return dt, 5 * nb, 3 * nb
 
 
+def ensemble_bench(fw, pg, ws, n=512, K=10, W=2, run_seconds=300.0):
+    """The 512-run ensemble (planar beaches of uneven size, slope, depth and
+    JONSWAP forcing; 1.5e8 cells in all): every member steps concurrently
+    through fw_ensemble_step.  cell-steps/s over K steps after W warm-up
+    steps (host wall clock around the call, which waits for every stream);
+    runs/hr extrapolates to run_seconds of simulated time per run, with each
+    run's step count from its own DT and the measured cell-step rate."""
+    members = fw.cases.ensemble_members(n, seed=2024)
+    t0 = time.perf_counter()
+    ens = fw.Ensemble(members, precision="MIXED")
+    t_init = time.perf_counter() - t0
+    ens.step(W)
+    barrier(pg)
+    t0 = time.perf_counter()
+    st = ens.step(K, check=False)
+    wall = max_over_ranks(time.perf_counter() - t0, pg)
+    barrier(pg)
+    cells = [p["Mglob"] * p["Nglob"] for p, _, _ in members]
+    dts = [s.scalar("DT") for s in ens.solvers]
+    ens.close()
+    rate = sum(cells) * K * ws / wall
+    work = sum(c * run_seconds / dt for c, dt in zip(cells, dts)) / n
+    return {"metric": "ensemble runs/hr", "value": 3600.0 * rate / work, "unit": "runs/hr",
+            "cell_steps_per_s": rate, "runs": n * ws, "cells_total": sum(cells) * ws,
+            "grid_cells_range": [min(cells), max(cells)], "steps_timed": K, "warmup": W,
+            "wall_s": wall, "init_s": t_init, "statuses_nonzero": sum(1 for v in st if v),
+            "run_seconds": run_seconds,
+            "how": "each run is a context with its own stream and two-step CUDA graph; fw_ensemble_step "
+                   "enqueues them round robin from native code; runs/hr extrapolates the measured cell-step "
+                   "rate to %g s of simulated time per run" % run_seconds}
+
+
 def cpu_baseline(fw, params, depth, phases, max_seconds=20.0, max_steps=5):
     """The oracle (C restatement, all host threads) on the same workload:
     init, one untimed step, then whole steps until max_seconds."""
@@ -288,6 +337,7 @@ def main():
     ap.add_argument("--size", type=int, default=2048, help="grid edge (2048 for the benchmark)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the 512-run ensemble measurement")
     ap.add_argument("--no-kernel-profile", action="store_true",
                     help="skip the per-kernel timing (e.g. for an ncu launch list of the stepping only)")
     args = ap.parse_args()
@@ -338,6 +388,7 @@ def main():
         sm, 4, cells, (params["Mglob"] + 1) * params["Nglob"], params["Mglob"] * (params["Nglob"] + 1), hbm)
     dom = max(prof, key=lambda k: prof[k]["ms"]) if prof else None
     sm.close()
+    ens = None if args.no_ensemble else ensemble_bench(fw, pg, ws)
     if rank != 0:
         return 0
     value = cells * K * ws / (ms_mixed * 1e-3)
@@ -359,13 +410,19 @@ def main():
                 "d2h_bytes_per_step": d2h,
                 "what": "per step: Eta,U,V,Ubar,Vbar uploaded from pinned host memory, fw_step, Eta,U,V read back"},
         "fp64": res64,
+        "ensemble": ens,
         "kernels_ms": {k: round(v["ms"], 4) for k, v in prof.items()},
     }
     if dom:
         d = prof[dom]
+        unit = ((params["Mglob"] + 1) * params["Nglob"] if dom == "flux_x" else
+                params["Mglob"] * (params["Nglob"] + 1) if dom == "flux_y" else cells)
+        tpu = TRAFFIC_PER_UNIT_MIXED.get(dom)
         line["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": d["gbs"], "peak": hbm, "unit": "GB/s",
-                            "frac": d["frac"], "traffic": None, "peak_kind": peak_kind,
-                            "algorithmic_bytes_per_launch": d["bytes"], "ms_per_launch": d["ms"]}
+                            "frac": d["frac"], "traffic": tpu * unit if tpu else None, "peak_kind": peak_kind,
+                            "algorithmic_bytes_per_launch": d["bytes"], "ms_per_launch": d["ms"],
+                            "traffic_from": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 2048x2048 capture, "
+                                            "bytes per unit x units of this launch"}
     if not args.no_cpu_baseline and ws == 1:
         line["cpu_baseline"] = cpu_baseline(fw, params, depth, phases)
     print(json.dumps(line), flush=True)

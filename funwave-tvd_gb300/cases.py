@@ -9,6 +9,8 @@ positive down) and the JON_2D phases (or None).
                  sponge, periodic in y (the 250 x 500 configuration)
   shoal_jonswap  1:50 slope from 20 m with an elliptic shoal and a
                  directional JONSWAP wavemaker (the 2048 x 2048 configuration)
+  ensemble_members  planar beaches of uneven grid size, slope, depth and
+                 JONSWAP forcing (the 512-run ensemble configuration)
 """
 import numpy as np
 
@@ -98,3 +100,44 @@ def random_state(Mglob, Nglob, seed=0, eta_amp=0.05, u_amp=0.1, smooth=3.0):
         s = np.abs(f).max()
         out.append(np.asfortranarray(f * (amp / s if s > 0 else 0.0)))
     return tuple(out)
+
+
+def ensemble_members(n=512, seed=0, nfreq=24, ntheta=8, cells_range=(128 * 256, 1024 * 1024)):
+    """n planar-beach runs drawn from one seeded stream: interior cells log-
+    uniform in cells_range with the cross-shore/alongshore aspect log-uniform
+    in [1/2, 2], dx uniform in [1, 4] m, slope uniform in [1/50, 1/10],
+    offshore depth uniform in [5, 20] m, JON_2D Hs uniform in [0.5, 3] m and
+    Tp uniform in [6, 14] s (gamma 3.3, cos^2s spreading s = 10, nfreq x
+    ntheta components, phases from the stream).  Depth is
+    min(h0, slope * (x_shore - x)) with the shoreline at 85 % of the domain,
+    so every run has dry land; the wavemaker sits at 20 % and a west sponge
+    covers 10 %.  Returns a list of (params, depth, phases)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    lo, hi = np.log(cells_range[0]), np.log(cells_range[1])
+    for _ in range(n):
+        cells = float(np.exp(rng.uniform(lo, hi)))
+        aspect = float(np.exp(rng.uniform(np.log(0.5), np.log(2.0))))
+        M = max(32, int(round(np.sqrt(cells * aspect) / 8.0)) * 8)
+        N = max(32, int(round(cells / M / 8.0)) * 8)
+        dx = float(rng.uniform(1.0, 4.0))
+        slope = float(rng.uniform(1.0 / 50.0, 1.0 / 10.0))
+        h0 = float(rng.uniform(5.0, 20.0))
+        hs = float(rng.uniform(0.5, 3.0))
+        tp = float(rng.uniform(6.0, 14.0))
+        x = (np.arange(M) + 0.5) * dx
+        x_shore = 0.85 * M * dx
+        h = np.minimum(h0, slope * (x_shore - x))
+        depth = np.asfortranarray(np.repeat(h[:, None], N, axis=1))
+        phases = np.asfortranarray(rng.uniform(0.0, 2.0 * np.pi, size=(nfreq, ntheta)))
+        p = {
+            "Mglob": M, "Nglob": N, "DX": dx, "DY": dx, "PERIODIC": False, "WAVEMAKER": "JON_2D",
+            "Hmo": hs, "FreqPeak": 1.0 / tp, "FreqMin": 0.5 / tp, "FreqMax": 3.0 / tp, "GammaTMA": 3.3,
+            "Nfreq": nfreq, "Ntheta": ntheta, "ThetaPeak": 0.0, "SPREADING": "COS2S", "SPREADING_S": 10.0,
+            "DEP_WK": float(min(h0, slope * (x_shore - 0.2 * M * dx))), "Xc_WK": 0.2 * M * dx,
+            "Delta_WK": 0.5, "Time_ramp": 1.0, "DIRECT_SPONGE": True, "Sponge_west_width": 0.1 * M * dx,
+            "DISPERSION": True, "VISCOSITY_BREAKING": True, "SHOW_BREAKING": True, "CFL": 0.5,
+            "MinDepth": 0.01, "MinDepthFrc": 0.1,
+        }
+        out.append((p, depth, phases))
+    return out

@@ -698,14 +698,14 @@ int fw_end_step(fw_ctx *c, int *status) {
     return read_status(c, status);
 }
 
-int fw_step(fw_ctx *c, int nsteps, int *status) {
-    int rc = check_ready(c);
-    if (rc != FW_OK) return rc;
-    if (nsteps < 0) return FW_ERR_BAD_PARAM;
-    if (status) *status = FW_OK;
-    if (nsteps == 0) return FW_OK;
-    cudaError_t e = cudaMemsetAsync(etamax_ptr(c), 0, sizeof(unsigned long long), c->stream);
-    if (e != cudaSuccess) return cuda_status(c, e);
+// the work of nsteps whole steps on the context's stream, without waiting;
+// reset_max restarts the CHECK_BLOWUP maximum that read_status reads
+static int enqueue_steps(fw_ctx *c, int nsteps, bool reset_max) {
+    cudaError_t e;
+    if (reset_max) {
+        e = cudaMemsetAsync(etamax_ptr(c), 0, sizeof(unsigned long long), c->stream);
+        if (e != cudaSuccess) return cuda_status(c, e);
+    }
     const bool fp64 = c->p.precision == FW_PREC_FP64;
     int left = nsteps;
     // a graph holds two steps, after which every ping-pong buffer is back in
@@ -742,8 +742,54 @@ int fw_step(fw_ctx *c, int nsteps, int *status) {
         else enqueue_step<float>(c);
         c->graph_ready = 0;
     }
-    if ((rc = finish(c)) != FW_OK) return rc;
+    return finish(c);
+}
+
+int fw_step(fw_ctx *c, int nsteps, int *status) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    if (nsteps < 0) return FW_ERR_BAD_PARAM;
+    if (status) *status = FW_OK;
+    if (nsteps == 0) return FW_OK;
+    if ((rc = enqueue_steps(c, nsteps, true)) != FW_OK) return rc;
     return read_status(c, status);
+}
+
+int fw_step_async(fw_ctx *c, int nsteps) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    if (nsteps < 0) return FW_ERR_BAD_PARAM;
+    return enqueue_steps(c, nsteps, true);
+}
+
+int fw_step_wait(fw_ctx *c, int *status) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    return read_status(c, status);
+}
+
+int fw_ensemble_step(fw_ctx *const *ctxs, int n, int nsteps, int *status) {
+    if (!ctxs || n < 0 || nsteps < 0) return FW_ERR_BAD_PARAM;
+    for (int k = 0; k < n; k++) {
+        const int rc = check_ready(ctxs[k]);
+        if (rc != FW_OK) return rc;
+        if (status) status[k] = FW_OK;
+    }
+    // round robin, one two-step graph per context per pass, so that every
+    // stream has work queued while the others run
+    for (int done = 0; done < nsteps; done += 2) {
+        const int now = std::min(2, nsteps - done);
+        for (int k = 0; k < n; k++) {
+            const int rc = enqueue_steps(ctxs[k], now, done == 0);
+            if (rc != FW_OK) return rc;
+        }
+    }
+    int first = FW_OK;
+    for (int k = 0; k < n; k++) {
+        const int rc = read_status(ctxs[k], status ? &status[k] : nullptr);
+        if (rc != FW_OK && first == FW_OK) first = rc;
+    }
+    return first;
 }
 
 int fw_sync(fw_ctx *c) {

@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
 // U1p, V1p and U1pp+U2+U3, V1pp+V2+V3 on the interior.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256) k_disp_b(Grid g, Fields<T> f) {
+__global__ void __launch_bounds__(256, sizeof(T) == sizeof(float) ? 4 : 1) k_disp_b(Grid g, Fields<T> f) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mloc || j >= g.Nloc) return;

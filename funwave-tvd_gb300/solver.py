@@ -224,6 +224,9 @@ def load_library(path=None):
     L.fw_estimate_huv.argtypes = [vp, ip]
     L.fw_end_step.argtypes = [vp, ctypes.POINTER(ip)]
     L.fw_step.argtypes = [vp, ip, ctypes.POINTER(ip)]
+    L.fw_step_async.argtypes = [vp, ip]
+    L.fw_step_wait.argtypes = [vp, ctypes.POINTER(ip)]
+    L.fw_ensemble_step.argtypes = [ctypes.POINTER(vp), ip, ip, ctypes.POINTER(ip)]
     L.fw_launch_count.argtypes = [vp]
     L.fw_launch_count.restype = ctypes.c_longlong
     L.fw_stream.argtypes = [vp]
@@ -331,6 +334,18 @@ class Solver:
         self._check(self.L.fw_step(self.ctx, int(nsteps), ctypes.byref(st)), "fw_step")
         if check and st.value != 0:
             raise FwError(st.value, "after %d steps" % nsteps)
+        return st.value
+
+    def step_async(self, nsteps=1):
+        """Enqueue nsteps whole steps and return at once (fw_step_async)."""
+        self._check(self.L.fw_step_async(self.ctx, int(nsteps)), "fw_step_async")
+
+    def step_wait(self, check=True):
+        """Wait for the steps of step_async; their CHECK_BLOWUP status."""
+        st = ctypes.c_int()
+        self._check(self.L.fw_step_wait(self.ctx, ctypes.byref(st)), "fw_step_wait")
+        if check and st.value != 0:
+            raise FwError(st.value, "after step_async")
         return st.value
 
     def begin_step(self):

@@ -146,6 +146,17 @@ int fw_end_step(fw_ctx *ctx, int *status);
  * from a CUDA graph; *status as fw_end_step for the last step, checked
  * once at the end. */
 int fw_step(fw_ctx *ctx, int nsteps, int *status);
+/* fw_step split in two: enqueue nsteps whole steps on the context's stream
+ * and return at once; then wait for them and get the CHECK_BLOWUP status of
+ * those steps.  No reference counterpart (the reference steps one run). */
+int fw_step_async(fw_ctx *ctx, int nsteps);
+int fw_step_wait(fw_ctx *ctx, int *status);
+/* An ensemble of independent runs (contexts of any sizes and precisions on
+ * the same device): nsteps whole steps of each, enqueued round robin two
+ * steps at a time so that the runs' streams execute concurrently, then
+ * waited for; status[k] as fw_end_step for run k.  Each run's results are
+ * those of fw_step on it alone, bit for bit.  No reference counterpart. */
+int fw_ensemble_step(fw_ctx *const *ctxs, int n, int nsteps, int *status);
 /* Synchronise the context's stream. */
 int fw_sync(fw_ctx *ctx);
 
