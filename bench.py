@@ -264,6 +264,56 @@ def ensemble_bench(fw, pg, ws, n=512, K=10, W=2, run_seconds=300.0):
                    "rate to %g s of simulated time per run" % run_seconds}
 
 
+def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
+    """The 4096 x 4096 barred beach with rip channels (1:40, bar 1.5 m high
+    80 m offshore, JONSWAP Hs = 1.5 m, Tp = 10 s), run to t_end s in mixed
+    precision and in FP64: eta RMS over cells wet in both, maximum run-up,
+    the time-mean current (Umean, Vmean over [t_steady, t_steady + t_mean])
+    and MASK mismatches of mixed against FP64, with both step rates."""
+    import numpy as np
+    params, depth, phases, rips = fw.cases.barred_beach(size, size, 1.0, seed=2024)
+    params = fw.with_defaults(params)
+    params.update({"OUT_Hmax": True, "STEADY_TIME": t_steady, "T_INTV_mean": t_mean})
+    out = {}
+    for prec in ("MIXED", "FP64"):
+        s = fw.Solver(params, precision=prec)
+        s.init(depth, phases=phases)
+        n = 0
+        ext, e0, e1 = cuda_timer(s)
+        s.sync()
+        e0.record(ext)
+        while s.scalar("TIME") < t_end:
+            s.step(20)
+            n += 20
+        e1.record(ext)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[prec] = {k: s.get(k)[3:-3, 3:-3] for k in ("Eta", "U", "V", "MASK", "HeightMax", "Umean", "Vmean")}
+        out[prec]["TIME"] = s.scalar("TIME")
+        out[prec]["steps"] = n
+        out[prec]["rate"] = size * size * n / (ms * 1e-3)
+        s.close()
+    m, d = out["MIXED"], out["FP64"]
+    wet = (m["MASK"] > 0) & (d["MASK"] > 0)
+    cur_d = np.sqrt(d["Umean"] ** 2 + d["Vmean"] ** 2)
+    du = np.sqrt((m["Umean"] - d["Umean"]) ** 2 + (m["Vmean"] - d["Vmean"]) ** 2)
+    ru_m, ru_d = fw.max_runup(np.pad(m["HeightMax"], 3), depth), fw.max_runup(np.pad(d["HeightMax"], 3), depth)
+    return {
+        "metric": "mixed vs FP64 on the 4096x4096 barred beach", "grid": [size, size], "dx_m": 1.0,
+        "rip_channels_y_m": rips, "t_end_s": t_end, "time_mixed_s": m["TIME"], "time_fp64_s": d["TIME"],
+        "steps_mixed": m["steps"], "steps_fp64": d["steps"],
+        "eta_rms_m": float(np.sqrt(np.mean((m["Eta"] - d["Eta"])[wet] ** 2))),
+        "eta_max_abs_m": float(np.abs(m["Eta"] - d["Eta"])[wet].max()),
+        "eta_rms_signal_m": float(np.sqrt(np.mean(d["Eta"][wet] ** 2))),
+        "max_runup_mixed_m": ru_m, "max_runup_fp64_m": ru_d,
+        "mean_current_rms_error_m_s": float(np.sqrt(np.mean(du[wet] ** 2))),
+        "mean_current_rms_fp64_m_s": float(np.sqrt(np.mean(cur_d[wet] ** 2))),
+        "mask_mismatch_cells": int(np.sum(m["MASK"] != d["MASK"])),
+        "cell_steps_per_s_mixed": m["rate"], "cell_steps_per_s_fp64": d["rate"],
+        "speedup_mixed_over_fp64": m["rate"] / d["rate"],
+    }
+
+
 def cpu_baseline(fw, params, depth, phases, max_seconds=20.0, max_steps=5):
     """The oracle (C restatement, all host threads) on the same workload:
     init, one untimed step, then whole steps until max_seconds."""
@@ -338,6 +388,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 512-run ensemble measurement")
+    ap.add_argument("--precision-report", action="store_true",
+                    help="only the 4096x4096 barred-beach mixed-vs-FP64 report (about 10 GPU minutes)")
     ap.add_argument("--no-kernel-profile", action="store_true",
                     help="skip the per-kernel timing (e.g. for an ncu launch list of the stepping only)")
     args = ap.parse_args()
@@ -346,6 +398,11 @@ def main():
     params = fw.with_defaults(params)
     if args.impl == "reference":
         return reference_arm(args, fw, params, depth, phases)
+    if args.precision_report:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(precision_report(fw)), flush=True)
+        return 0
 
     ws, rank, local = dist_env()
     pg = None

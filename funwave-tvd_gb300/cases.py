@@ -9,6 +9,9 @@ positive down) and the JON_2D phases (or None).
                  sponge, periodic in y (the 250 x 500 configuration)
   shoal_jonswap  1:50 slope from 20 m with an elliptic shoal and a
                  directional JONSWAP wavemaker (the 2048 x 2048 configuration)
+  barred_beach   1:40 slope with a Gaussian bar cut by rip channels and a
+                 normal-incidence JONSWAP wavemaker (the 4096 x 4096
+                 precision configuration)
   ensemble_members  planar beaches of uneven grid size, slope, depth and
                  JONSWAP forcing (the 512-run ensemble configuration)
 """
@@ -141,3 +144,47 @@ def ensemble_members(n=512, seed=0, nfreq=24, ntheta=8, cells_range=(128 * 256, 
         }
         out.append((p, depth, phases))
     return out
+
+
+def barred_beach(Mglob=4096, Nglob=4096, dx=1.0, seed=0, h_off=12.0, wk_from_shore=180.0, nfreq=32,
+                 ntheta=8, **overrides):
+    """A 1:40 beach whose shoreline lies 300 m from the east wall, seaward of
+    it a flat h_off offshore floor; an alongshore-uniform Gaussian bar 1.5 m
+    high and 30 m wide (standard deviation 30/2.355 m) centred 80 m offshore
+    of the shoreline, cut by 4 rip channels 20 m wide (the bar is removed
+    with cosine-tapered edges) at seeded alongshore positions at least 10 %
+    of the domain apart.  JON_2D Hs = 1.5 m, Tp = 10 s, gamma 3.3, normal
+    incidence (cos^2s, s = 10), nfreq x ntheta components, wavemaker
+    wk_from_shore metres offshore of the shoreline, west sponge 100 m.
+    Wetting-drying and breaking are on (the defaults)."""
+    x = (np.arange(Mglob) + 0.5) * dx
+    y = (np.arange(Nglob) + 0.5) * dx
+    x_shore = Mglob * dx - 300.0
+    h = np.minimum(h_off, (x_shore - x) / 40.0)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    bar = 1.5 * np.exp(-0.5 * ((X - (x_shore - 80.0)) / (30.0 / 2.355)) ** 2)
+    rng = np.random.default_rng(seed)
+    Ly = Nglob * dx
+    pos = []
+    while len(pos) < 4:
+        c = float(rng.uniform(0.05 * Ly, 0.95 * Ly))
+        if all(abs(c - q) >= 0.1 * Ly for q in pos):
+            pos.append(c)
+    cut = np.ones_like(Y)
+    for c in pos:
+        d = np.abs(Y - c)
+        cut = np.minimum(cut, np.where(d <= 10.0, 0.0, np.where(d <= 20.0, 0.5 - 0.5 * np.cos(np.pi * (d - 10.0) / 10.0), 1.0)))
+    depth = np.asfortranarray(h[:, None] - bar * cut)
+    phases = np.asfortranarray(rng.uniform(0.0, 2.0 * np.pi, size=(nfreq, ntheta)))
+    x_wk = x_shore - wk_from_shore
+    p = {
+        "Mglob": Mglob, "Nglob": Nglob, "DX": dx, "DY": dx, "PERIODIC": False, "WAVEMAKER": "JON_2D",
+        "Hmo": 1.5, "FreqPeak": 0.1, "FreqMin": 0.05, "FreqMax": 0.30, "GammaTMA": 3.3,
+        "Nfreq": nfreq, "Ntheta": ntheta, "ThetaPeak": 0.0, "SPREADING": "COS2S", "SPREADING_S": 10.0,
+        "DEP_WK": float(min(h_off, wk_from_shore / 40.0)), "Xc_WK": x_wk, "Delta_WK": 0.5, "Time_ramp": 1.0,
+        "DIRECT_SPONGE": True, "Sponge_west_width": 100.0,
+        "DISPERSION": True, "VISCOSITY_BREAKING": True, "SHOW_BREAKING": True,
+        "CFL": 0.5, "MinDepth": 0.01, "MinDepthFrc": 0.1,
+    }
+    p.update(overrides)
+    return p, depth, phases, pos

@@ -411,8 +411,12 @@ template <typename T> __device__ __forceinline__ T press(T Xi, T Deps, T g3) {
 
 // Limited face values of one field from Din(p-1), Din(p), Din(p+1) and the
 // cells p-1, p.  FP64 evaluates the reference's van Leer expressions
-// (fluxes.F:1602-1630); the mixed path uses the equal closed form
-// VAN1*TMP1 = VAN2*TMP2 = 2*TMP1*TMP2/(TMP1+TMP2) for TMP1*TMP2 > 0, else 0.
+// (fluxes.F:1602-1630), including its guard that replaces a slope
+// |t| <= SMALL by SMALL*sign(t).  The mixed path uses the equal closed form
+// VAN1*TMP1 = VAN2*TMP2 = 2*TMP1*TMP2/(TMP1+TMP2) for TMP1*TMP2 > 0, else 0,
+// without the guard (which only adds SMALL-sized corrections, e.g. on still
+// water; the closed form needs no guard since TMP1*TMP2 > 0 keeps
+// TMP1+TMP2 away from 0).
 template <typename T>
 __device__ __forceinline__ void ho_lr(T vm1, T v0, T d0, T d1, T d2, T &L, T &R) {
     if constexpr (sizeof(T) == sizeof(double)) {
@@ -425,7 +429,7 @@ __device__ __forceinline__ void ho_lr(T vm1, T v0, T d0, T d1, T d2, T &L, T &R)
         van2 = vl_phi(t1 / t2);
         R = v0 - ((T)1 / (T)6) * ((T)2 * van1 * t1 + van2 * t2);
     } else {
-        T t1 = vl_guard(d0), t2 = vl_guard(d1), t3 = vl_guard(d2);
+        const T t1 = d0, t2 = d1, t3 = d2;
         const T hl = (t1 * t2 > (T)0) ? (T)2 * t1 * t2 / (t1 + t2) : (T)0;
         const T hr = (t2 * t3 > (T)0) ? (T)2 * t2 * t3 / (t2 + t3) : (T)0;
         L = vm1 + (T)0.5 * hl;
@@ -1485,6 +1489,12 @@ __device__ __forceinline__ void pcr_solve(float *lo, float *di, float *up, float
 
 // y lines (and the periodic direction): per-chunk kernels, coalesced across
 // neighbouring lines.  PASS 0 solves d = rhs/tmp2, PASS 1 the residual.
+// per-stage reduced right-hand sides: pass 0 at the start of the scratch,
+// pass 1 right after it
+template <int PASS> __device__ __forceinline__ float *red_rhs(double *red, const LinePart &lp) {
+    return (float *)red + (PASS == 0 ? 0 : (size_t)lp.nlines * 2 * lp.P);
+}
+
 template <typename T, int DIR, bool PER, int PASS>
 __global__ void __launch_bounds__(128) k_sol_a(Grid g, Fields<T> f, LinePart lp) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1536,17 +1546,17 @@ __global__ void __launch_bounds__(128) k_sol_a(Grid g, Fields<T> f, LinePart lp)
         rs = ds - fl.cs[ch] * y1;
         re = de - fl.ae[ch] * yl;
     }
-    float *red = (float *)f.red + ((size_t)l * 2 * lp.P + 2 * ch);
+    float *red = red_rhs<PASS>(f.red, lp) + ((size_t)l * 2 * lp.P + 2 * ch);
     red[0] = rs;
     red[1] = re;
 }
 
-template <typename T, int DIR, bool PER>
+template <typename T, int DIR, bool PER, int PASS>
 __global__ void __launch_bounds__(512) k_sol_b(Grid g, Fields<T> f, LinePart lp) {
     extern __shared__ float shr[];
     const int l = blockIdx.x;
     const int n = 2 * lp.P;
-    float *red = (float *)f.red + (size_t)l * n;
+    float *red = red_rhs<PASS>(f.red, lp) + (size_t)l * n;
     FacLine fl = fac_line(f.fac_red[DIR], lp, l);
     float *lo = shr, *di = shr + n, *up = shr + 2 * n, *r = shr + 3 * n;
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
@@ -1571,7 +1581,7 @@ __global__ void __launch_bounds__(128) k_sol_c(Grid g, Fields<T> f, LinePart lp)
     chunk_of<DIR>(lp, t, l, ch);
     const int s = ch * lp.m;
     const int e = (ch == lp.P - 1) ? lp.L - 1 : s + lp.m - 1;
-    const float *red = (const float *)f.red + ((size_t)l * 2 * lp.P + 2 * ch);
+    const float *red = red_rhs<PASS>(f.red, lp) + ((size_t)l * 2 * lp.P + 2 * ch);
     const float xs = red[0], xe = red[1];
     const float *p_ = f.fac_p[DIR], *q_ = f.fac_q[DIR];
     const float *ys = (const float *)f.ty;
@@ -2584,11 +2594,11 @@ static bool launch_tri(fw_ctx *c, const LinePart &lp, bool fac = true, bool clea
         k_sol_a<T, DIR, PER, 0><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         const int nb = std::min(512, ((2 * lp.P + 31) / 32) * 32);
         const size_t sb = (size_t)16 * lp.P * sizeof(float);
-        k_sol_b<T, DIR, PER><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
+        k_sol_b<T, DIR, PER, 0><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
         k_sol_c<T, DIR, 0><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         k_resid<T, DIR, PER><<<gi, B2D, 0, c->stream>>>(g, c->F<T>(), lp);
         k_sol_a<T, DIR, PER, 1><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        k_sol_b<T, DIR, PER><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
+        k_sol_b<T, DIR, PER, 1><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
         k_sol_c<T, DIR, 1><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         note(c, 7);
         return false;
