@@ -544,32 +544,47 @@ int fw_init(fw_ctx *c, const double *depth, const double *eta, const double *u, 
         if (rc != FW_OK) return rc;
     }
     // JON_2D band tables
-    if (c->p.wavemaker == FW_WK_JON_2D && !hc.Cm.empty()) {
-        // stored in the field precision: the mixed path sums them in float
+    const int bw = hc.ihi - hc.ilo + 1, bh = hc.jhi - hc.jlo + 1;
+    if (c->p.wavemaker == FW_WK_JON_2D && bw > 0 && bh > 0) {
+        // the band Cm/Sm in the field precision (the mixed path sums them in
+        // float), computed on the device from the spectrum tables
         const bool d = c->p.precision == FW_PREC_FP64;
         const size_t es = d ? sizeof(double) : sizeof(float);
-        const size_t nb = hc.Cm.size() * es;
+        const size_t mf = c->p.nfreq, mt = c->p.ntheta;
+        const size_t nb = (size_t)bw * bh * mf * es;
         void *Cm = nullptr, *Sm = nullptr;
-        if (cudaMalloc(&Cm, nb) != cudaSuccess || cudaMalloc(&Sm, nb) != cudaSuccess) {
+        double *tab = nullptr;
+        const size_t ntab = 3 * mf * mt + mf;
+        if (cudaMalloc(&Cm, nb) != cudaSuccess || cudaMalloc(&Sm, nb) != cudaSuccess ||
+            cudaMalloc(&tab, ntab * sizeof(double)) != cudaSuccess) {
             cudaGetLastError();
             if (Cm) cudaFree(Cm);
+            if (Sm) cudaFree(Sm);
             return FW_ERR_OOM;
         }
         void *oldc = d ? (void *)c->fd.Cm : (void *)c->ff.Cm, *olds = d ? (void *)c->fd.Sm : (void *)c->ff.Sm;
         if (oldc) cudaFree(oldc);
         if (olds) cudaFree(olds);
+        std::vector<double> h(ntab);
+        std::copy(hc.jon_dgen.begin(), hc.jon_dgen.end(), h.begin());
+        std::copy(hc.jon_rlamda.begin(), hc.jon_rlamda.end(), h.begin() + mf * mt);
+        std::copy(hc.jon_phases.begin(), hc.jon_phases.end(), h.begin() + 2 * mf * mt);
+        std::copy(hc.jon_betagen.begin(), hc.jon_betagen.end(), h.begin() + 3 * mf * mt);
+        rc = upload_array(c, tab, h.data(), ntab * sizeof(double));
+        const int i0 = hc.ilo - (NG + 1), j0 = hc.jlo - (NG + 1);  // I-Ibeg, J-Jbeg of the band's first cell
         if (d) {
             c->fd.Cm = (double *)Cm;
             c->fd.Sm = (double *)Sm;
-            if ((rc = upload_array(c, Cm, hc.Cm.data(), nb)) != FW_OK) return rc;
-            if ((rc = upload_array(c, Sm, hc.Sm.data(), nb)) != FW_OK) return rc;
+            if (rc == FW_OK) launch_cm_sm<double>(c, bw, bh, i0, j0, tab, c->fd.Cm, c->fd.Sm);
         } else {
             c->ff.Cm = (float *)Cm;
             c->ff.Sm = (float *)Sm;
-            std::vector<float> tc(hc.Cm.begin(), hc.Cm.end()), ts(hc.Sm.begin(), hc.Sm.end());
-            if ((rc = upload_array(c, Cm, tc.data(), nb)) != FW_OK) return rc;
-            if ((rc = upload_array(c, Sm, ts.data(), nb)) != FW_OK) return rc;
+            if (rc == FW_OK) launch_cm_sm<float>(c, bw, bh, i0, j0, tab, c->ff.Cm, c->ff.Sm);
         }
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        cudaFree(tab);
+        if (rc != FW_OK) return rc;
+        if (e != cudaSuccess) return cuda_status(c, e);
         double *om = c->p.precision == FW_PREC_FP64 ? c->fd.omega : c->ff.omega;
         if ((rc = upload_array(c, om, hc.omega.data(), hc.omega.size() * sizeof(double))) != FW_OK) return rc;
     }
@@ -601,6 +616,35 @@ int fw_get_field(fw_ctx *c, const char *name, void *host) {
 int fw_set_field(fw_ctx *c, const char *name, const void *host) {
     if (!c || !name || !host) return FW_ERR_BAD_PARAM;
     return put_named(c, name, host);
+}
+
+int fw_get_points(fw_ctx *c, const char *name, int n, const int *I, const int *J, double *out) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    if (!name || n < 0 || (n > 0 && (!I || !J || !out))) return FW_ERR_BAD_PARAM;
+    if (n == 0) return FW_OK;
+    FieldRef r;
+    const bool d = c->p.precision == FW_PREC_FP64;
+    if (!(d ? find_field<double>(c, name, r) : find_field<float>(c, name, r))) return FW_ERR_BAD_PARAM;
+    int w, h;
+    extent(c, r.kind, w, h);
+    // offsets, then the gathered values, in the staging plane
+    const size_t cap = (size_t)c->g.pitch * (size_t)(c->g.Nloc + 1) * sizeof(double);
+    if ((size_t)n * (sizeof(int) + sizeof(double)) + 16 > cap) return FW_ERR_BAD_PARAM;
+    std::vector<int> off((size_t)n);
+    for (int k = 0; k < n; k++) {
+        if (I[k] < 1 || I[k] > w || J[k] < 1 || J[k] > h) return FW_ERR_BAD_PARAM;
+        off[k] = (I[k] - 1) + (J[k] - 1) * c->g.pitch;
+    }
+    int *d_off = (int *)c->staging;
+    double *d_out = (double *)((char *)c->staging + (((size_t)n * sizeof(int) + 15) / 16) * 16);
+    cudaError_t e = cudaMemcpyAsync(d_off, off.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        gather_points(c, r.ptr, r.is_mask ? 2 : (d ? 0 : 1), d_off, n, d_out);
+        e = cudaMemcpyAsync(out, d_out, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return cuda_status(c, e);
 }
 
 int fw_get_scalar(fw_ctx *c, const char *name, double *v) {

@@ -198,35 +198,6 @@ void jon_spectrum(const fw_params &p, HostCase &hc) {
     hc.Width_WK = delta * wave_length / 2.0;
 }
 
-// CALCULATE_Cm_Sm (wavemaker.F:831-891) on the band
-void jon_cm_sm(const fw_params &p, const double *phases, HostCase &hc) {
-    const int mf = p.nfreq, mt = p.ntheta;
-    const int bw = hc.ihi - hc.ilo + 1, bh = hc.jhi - hc.jlo + 1;
-    hc.Cm.clear();
-    hc.Sm.clear();
-    if (bw <= 0 || bh <= 0) return;
-    hc.Cm.assign((size_t)bw * bh * mf, 0.0);
-    hc.Sm.assign((size_t)bw * bh * mf, 0.0);
-    const int Ibeg = NG + 1, Jbeg = NG + 1;
-    for (int J = hc.jlo; J <= hc.jhi; J++)
-        for (int I = hc.ilo; I <= hc.ihi; I++) {
-            const size_t b = (size_t)(I - hc.ilo) + (size_t)(J - hc.jlo) * bw;
-            for (int kf = 1; kf <= mf; kf++) {
-                double cm = 0.0, sm = 0.0;
-                for (int kt = 1; kt <= mt; kt++) {
-                    const size_t k2 = (size_t)(kf - 1) + (size_t)(kt - 1) * mf;
-                    const double dx = (I - Ibeg) * p.DX - p.xc_wk;
-                    const double amp = hc.jon_dgen[k2] * std::exp(-hc.jon_betagen[kf - 1] * (dx * dx));
-                    const double arg = hc.jon_rlamda[k2] * ((J - Jbeg) * p.DY - 0.0) + phases[k2];
-                    cm = cm + amp * std::cos(arg);
-                    sm = sm + amp * std::sin(arg);
-                }
-                hc.Cm[b + (size_t)(kf - 1) * bw * bh] = cm;
-                hc.Sm[b + (size_t)(kf - 1) * bw * bh] = sm;
-            }
-        }
-}
-
 // CALCULATE_SPONGE (sponge.F:591-767), serial
 void direct_sponge(const fw_params &p, HostCase &hc) {
     const int M = hc.Mloc, N = hc.Nloc;
@@ -420,7 +391,11 @@ int build_case(const fw_params &p, const double *depth, const double *eta, const
             if (I > hc.ihi) hc.ihi = I;
         }
     }
-    if (p.wavemaker == FW_WK_JON_2D) jon_cm_sm(p, phases, hc);
+    if (p.wavemaker == FW_WK_JON_2D) {
+        const size_t n = (size_t)p.nfreq * p.ntheta;
+        hc.jon_phases.assign(n, 0.0);
+        if (phases) hc.jon_phases.assign(phases, phases + n);
+    }
     return FW_OK;
 }
 

@@ -20,9 +20,10 @@ struct HostCase {
     double D_gen = 0, beta_gen = 0, rlamda = 0, Width_WK = 0;
     // wavemaker band, 1-based inclusive (init.F:1236-1268); empty if ilo > ihi
     int ilo = 0, ihi = -1, jlo = 0, jhi = -1;
-    // JON_2D: omega_k and the band Cm/Sm (i fastest, then j, then k)
-    std::vector<double> omega, Cm, Sm;
-    std::vector<double> jon_dgen, jon_rlamda, jon_betagen;  // (kf fastest)
+    // JON_2D: omega_k and the spectrum tables the device turns into the band
+    // Cm/Sm (CALCULATE_Cm_Sm runs as a kernel); phases phi1 (kf fastest)
+    std::vector<double> omega;
+    std::vector<double> jon_dgen, jon_rlamda, jon_betagen, jon_phases;  // (kf fastest)
 };
 
 // Returns FW_OK or FW_ERR_BAD_PARAM (err says why).

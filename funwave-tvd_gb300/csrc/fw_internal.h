@@ -122,6 +122,9 @@ template <typename T> void launch_breaking(fw_ctx *c);
 template <typename T> void launch_sponge(fw_ctx *c);
 template <typename T> void launch_end_step(fw_ctx *c);
 template <typename T> void launch_stage(fw_ctx *c, int istage);
+void gather_points(fw_ctx *c, const void *field, int type, const int *d_off, int n, double *d_out);
+template <typename T>
+void launch_cm_sm(fw_ctx *c, int bw, int bh, int i0, int j0, const double *tab, T *Cm, T *Sm);
 template <typename T> int launch_by_name(fw_ctx *c, const char *name);
 // staging buffer <-> field (double <-> float fields, int32 <-> uint8 masks)
 void convert_in(fw_ctx *c, const void *staging, int is_mask, void *field, int w, int h);

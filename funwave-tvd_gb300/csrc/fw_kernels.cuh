@@ -2683,6 +2683,48 @@ template <typename T> void launch_breaking(fw_ctx *c) {
     F.AGEn = t;
 }
 
+// CALCULATE_Cm_Sm (wavemaker.F:831-891) on the wavemaker band: one thread
+// per (band cell, frequency) sums the Ntheta directional components
+//   Cm/Sm = sum_kt D_gen(kf,kt) exp(-beta_gen(kf) ((I-Ibeg) DX - Xc)^2)
+//           cos/sin(rlamda(kf,kt) (J-Jbeg) DY + phi1(kf,kt))
+// in double, in the reference's order, and stores it in the field precision.
+// i0, j0: I-Ibeg and J-Jbeg of the band's first cell.
+template <typename T>
+__global__ void __launch_bounds__(256) k_cm_sm(int bw, int bh, int mf, int mt, int i0, int j0, double DX,
+                                               double DY, double xc, const double *__restrict__ tab, T *Cm,
+                                               T *Sm) {
+    const long long nb = (long long)bw * bh;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nb * mf) return;
+    const int kf = (int)(t / nb);
+    const long long b = t - (long long)kf * nb;
+    const int bj = (int)(b / bw), bi = (int)(b - (long long)bj * bw);
+    const double *dgen = tab, *rlamda = tab + (size_t)mf * mt, *phi = tab + 2 * (size_t)mf * mt;
+    const double *betagen = tab + 3 * (size_t)mf * mt;
+    const double dx = (double)(i0 + bi) * DX - xc;
+    const double y = (double)(j0 + bj) * DY - 0.0;
+    const double ex = exp(-betagen[kf] * (dx * dx));
+    double cm = 0.0, sm = 0.0;
+    for (int kt = 0; kt < mt; kt++) {
+        const size_t k2 = (size_t)kf + (size_t)kt * mf;
+        const double amp = dgen[k2] * ex;
+        const double arg = rlamda[k2] * y + phi[k2];
+        cm = cm + amp * cos(arg);
+        sm = sm + amp * sin(arg);
+    }
+    Cm[b + (size_t)kf * nb] = (T)cm;
+    Sm[b + (size_t)kf * nb] = (T)sm;
+}
+
+template <typename T>
+void launch_cm_sm(fw_ctx *c, int bw, int bh, int i0, int j0, const double *tab, T *Cm, T *Sm) {
+    const Grid &g = c->g;
+    const long long n = (long long)bw * bh * g.nfreq;
+    k_cm_sm<T><<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(bw, bh, g.nfreq, c->p.ntheta, i0, j0, g.DX,
+                                                                   g.DY, g.xc_wk, tab, Cm, Sm);
+    note(c);
+}
+
 template <typename T> void launch_end_step(fw_ctx *c) {
     const Grid &g = c->g;
     if (g.stats) {
@@ -2760,6 +2802,20 @@ void convert_out(fw_ctx *c, const void *field, int is_mask, void *staging, int w
     note(c);
 }
 
+// values of one field at n cells (pitched offsets) as double; type 0 double,
+// 1 float, 2 uint8 mask
+__global__ void k_gather(const void *field, int type, const int *off, int n, double *out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int o = off[k];
+    out[k] = type == 0 ? ((const double *)field)[o]
+                       : type == 1 ? (double)((const float *)field)[o] : (double)((const uint8_t *)field)[o];
+}
+void gather_points(fw_ctx *c, const void *field, int type, const int *d_off, int n, double *d_out) {
+    k_gather<<<(n + 127) / 128, 128, 0, c->stream>>>(field, type, d_off, n, d_out);
+    note(c);
+}
+
 #endif  // FW_SHARED_DEFS
 
 // one kernel of the step by name, for timing (fw_time_kernel)
@@ -2803,6 +2859,7 @@ template <typename T> int launch_by_name(fw_ctx *c, const char *name) {
     template void launch_sponge<T>(fw_ctx *);                    \
     template void launch_end_step<T>(fw_ctx *);                  \
     template void launch_stage<T>(fw_ctx *, int);     \
+    template void launch_cm_sm<T>(fw_ctx *, int, int, int, int, const double *, T *, T *); \
     template int launch_by_name<T>(fw_ctx *, const char *);
 
 }  // namespace fw

@@ -13,12 +13,18 @@
 // (fw_step), CHECK_BLOWUP's dump to file 99999 (misc.F:394-433).  PREVIEW
 // (io.F:4304-4621) writes eta_NNNNN, u_NNNNN, v_NNNNN, mask_NNNNN (and
 // hmax_NNNNN with OUT_Hmax) in RESULT_FOLDER with PutFile's ASCII format
-// (Mglob values per line, E16.6E4, interior only, io.F:4895-4921), dep.out
-// with the first file, and appends "TIME DT" to time_dt.out.
+// (Mglob values per line, E16.6E4, interior only, io.F:4895-4921; or
+// headerless binary with FIELD_IO_TYPE = BINARY), dep.out with the first
+// file, and appends "TIME DT" to time_dt.out.  STATIONS writes sta_NNNN
+// (time, eta, u, v per row, E21.10E4 and 3E16.5E4): unlike the reference,
+// which drops the sample that finds its buffer full and pads the last
+// buffer with TOTAL_TIME rows, every sample is kept and the last buffer
+// holds only the rows taken.
 //
 // --dry-run parses, builds the depth and writes dep.out without touching a
 // GPU.  JON_2D phases, which the reference draws from the compiler's
 // rand(0), come from SplitMix64 seeded by the key PHASE_SEED (default 1).
+#include <algorithm>
 #include <cctype>
 #include <cinttypes>
 #include <cmath>
@@ -194,24 +200,32 @@ bool build_depth(const Input &in, const fw_params &p, std::vector<double> &d, st
     return true;
 }
 
-// PutFile's ASCII line format: E16.6E4 of REAL(SP) values
-void e16_6e4(float v, char *out) {
-    if (v == 0.0f) {
-        std::snprintf(out, 17, "%16s", "0.000000E+0000");
-        return;
+// Fortran Ew.dE4 of a value: 0.<d digits>E+eeee right-aligned in w
+// characters (w <= 40, d <= 16)
+void fortran_e4(double v, int w, int d, char *out) {
+    char body[64], res[80];
+    if (v == 0.0) {
+        std::snprintf(body, sizeof body, "0.%0*dE+0000", d, 0);
+    } else {
+        char buf[64];
+        std::snprintf(buf, sizeof buf, "%.*E", d - 1, v);  // m.mmmE+xx with d significant digits
+        const bool neg = buf[0] == '-';
+        const char *m = buf + (neg ? 1 : 0);
+        const int e = std::atoi(std::strchr(m, 'E') + 1) + 1;
+        char digits[24];
+        int k = 0;
+        for (const char *q = m; *q != 'E' && k < d; q++)
+            if (*q != '.') digits[k++] = *q;
+        digits[k] = 0;
+        std::snprintf(body, sizeof body, "%s0.%sE%c%04d", neg ? "-" : "", digits, e < 0 ? '-' : '+', std::abs(e));
     }
-    char buf[32];
-    std::snprintf(buf, sizeof buf, "%.5E", (double)v);  // d.dddddE+xx, six significant digits
-    const bool neg = buf[0] == '-';
-    const char *m = buf + (neg ? 1 : 0);
-    const int e = std::atoi(std::strchr(m, 'E') + 1) + 1;
-    char digits[7] = {m[0], m[2], m[3], m[4], m[5], m[6], 0};
-    char body[48], res[64];
-    std::snprintf(body, sizeof body, "%s0.%sE%c%04d", neg ? "-" : "", digits, e < 0 ? '-' : '+', std::abs(e));
-    std::snprintf(res, sizeof res, "%16s", body);  // at most 15 characters: right-aligned in 16
-    std::memcpy(out, res, 16);
-    out[16] = 0;
+    std::snprintf(res, sizeof res, "%*s", w, body);
+    std::memcpy(out, res, (size_t)w);
+    out[w] = 0;
 }
+
+// PutFile's ASCII line format: E16.6E4 of REAL(SP) values
+void e16_6e4(float v, char *out) { fortran_e4((double)v, 16, 6, out); }
 
 bool put_file(const std::string &path, const std::vector<double> &phi, const fw_params &p) {
     FILE *f = std::fopen(path.c_str(), "w");
@@ -225,6 +239,26 @@ bool put_file(const std::string &path, const std::vector<double> &phi, const fw_
         }
         std::fputc('\n', f);
     }
+    return std::fclose(f) == 0;
+}
+
+// FIELD_IO_TYPE = BINARY (mod_parallel_field_io.F:161-221): the interior
+// Mglob x Nglob in Fortran order, headerless, REAL(SP) of the build (double
+// for FP64, float for MIXED), native byte order
+bool put_file_binary(const std::string &path, const std::vector<double> &phi, const fw_params &p) {
+    FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) return false;
+    const int Mloc = p.Mglob + 6;
+    for (int J = 4; J <= p.Nglob + 3; J++)
+        for (int I = 4; I <= p.Mglob + 3; I++) {
+            const double v = phi[(size_t)(I - 1) + (size_t)(J - 1) * Mloc];
+            if (p.precision == FW_PREC_FP64) {
+                std::fwrite(&v, sizeof v, 1, f);
+            } else {
+                const float fv = (float)v;
+                std::fwrite(&fv, sizeof fv, 1, f);
+            }
+        }
     return std::fclose(f) == 0;
 }
 
@@ -308,6 +342,72 @@ int main(int argc, char **argv) {
     FILE *tdt = std::fopen("time_dt.out", "w");
     std::vector<int> mask((size_t)Mloc * Nloc);
     int icount = 0;
+    const bool binary = upper(in.str("FIELD_IO_TYPE", "ASCII")) == "BINARY";
+    auto write_field = [&](const std::string &path) {
+        return binary ? put_file_binary(path, full, p) : put_file(path, full, p);
+    };
+
+    // STATIONS (io.F:3786-3954): grid indices from STATIONS_FILE, sampled
+    // every PLOT_INTV_STATION into a buffer of StationOutputBuffer rows that
+    // is written to sta_NNNN when full and at the end of the run
+    const int nsta_req = (int)in.num("NumberStations", 0);
+    const double plot_intv_sta = in.num("PLOT_INTV_STATION", 1.0);
+    const int sta_buffer = std::max(1, (int)in.num("StationOutputBuffer", 1000));
+    std::vector<int> sta_id, sta_i, sta_j;
+    std::vector<FILE *> sta_f;
+    std::vector<std::vector<double>> sta_rows;
+    if (nsta_req > 0) {
+        std::ifstream sf(in.str("STATIONS_FILE", "stations.txt"));
+        if (!sf) {
+            std::fprintf(stderr, "fw_main: %s THE STATION FILE CANNOT BE FOUND\n", in.str("STATIONS_FILE", "").c_str());
+            return 1;
+        }
+        for (int k = 1; k <= nsta_req; k++) {
+            double d1 = 0, d2 = 0;
+            if (!(sf >> d1 >> d2)) break;
+            const int is = (int)(3 + d1), js = (int)(3 + d2);  // Nghost + index, INTEGER assignment truncates
+            if (is >= 4 && is <= p.Mglob + 3 && js >= 4 && js <= p.Nglob + 3) {
+                char b[16];
+                std::snprintf(b, sizeof b, "%04d", k);
+                FILE *f = std::fopen((dir + "sta_" + b).c_str(), "w");
+                if (!f) return 1;
+                sta_id.push_back(k);
+                sta_i.push_back(is);
+                sta_j.push_back(js);
+                sta_f.push_back(f);
+                sta_rows.emplace_back();
+            }
+        }
+    }
+    auto flush_station = [&](size_t s) {
+        char a[48], b[48];
+        for (size_t r = 0; r + 4 <= sta_rows[s].size(); r += 4) {
+            fortran_e4(sta_rows[s][r], 21, 10, a);
+            std::fputs(a, sta_f[s]);
+            for (int q = 1; q < 4; q++) {
+                fortran_e4(sta_rows[s][r + q], 16, 5, b);
+                std::fputs(b, sta_f[s]);
+            }
+            std::fputc('\n', sta_f[s]);
+        }
+        sta_rows[s].clear();
+    };
+    auto stations = [&](double t) -> int {
+        const int n = (int)sta_i.size();
+        if (n == 0) return FW_OK;
+        std::vector<double> e(n), u(n), v(n), m(n);
+        int r = fw_get_points(ctx, "Eta", n, sta_i.data(), sta_j.data(), e.data());
+        if (r == FW_OK) r = fw_get_points(ctx, "U", n, sta_i.data(), sta_j.data(), u.data());
+        if (r == FW_OK) r = fw_get_points(ctx, "V", n, sta_i.data(), sta_j.data(), v.data());
+        if (r == FW_OK) r = fw_get_points(ctx, "MASK", n, sta_i.data(), sta_j.data(), m.data());
+        if (r != FW_OK) return r;
+        for (int s2 = 0; s2 < n; s2++) {
+            const bool dry = m[s2] < 1.0;  // zeros on dry cells
+            sta_rows[s2].insert(sta_rows[s2].end(), {t, dry ? 0.0 : e[s2], dry ? 0.0 : u[s2], dry ? 0.0 : v[s2]});
+            if ((int)sta_rows[s2].size() / 4 >= sta_buffer) flush_station((size_t)s2);
+        }
+        return FW_OK;
+    };
     auto preview = [&](int number) -> int {
         icount = number;
         double t = 0.0, dt = 0.0;
@@ -320,20 +420,28 @@ int main(int argc, char **argv) {
         for (int k = 0; k < 3; k++) {
             int r = fw_get_field(ctx, names[k], full.data());
             if (r != FW_OK) return r;
-            put_file(numbered(dir, stems[k], icount), full, p);
+            write_field(numbered(dir, stems[k], icount));
         }
         int r = fw_get_field(ctx, "MASK", mask.data());
         if (r != FW_OK) return r;
         for (size_t q = 0; q < mask.size(); q++) full[q] = mask[q];
-        put_file(numbered(dir, "mask", icount), full, p);
+        write_field(numbered(dir, "mask", icount));
         if (p.track_hmax && fw_get_field(ctx, "HeightMax", full.data()) == FW_OK)
-            put_file(numbered(dir, "hmax", icount), full, p);
+            write_field(numbered(dir, "hmax", icount));
         return FW_OK;
     };
 
     double time = 0.0, dt = 0.0, plot_count = plot_intv;  // init.F:631
+    double plot_count_sta = plot_intv_sta;                  // init.F:632
     while (time < total) {  // DO WHILE (TIME < TOTAL_TIME)
         // OUTPUT (io.F:52-134) at the top of the pass, with the last DT
+        if (!sta_i.empty()) {
+            plot_count_sta += dt;
+            if (plot_count_sta >= plot_intv_sta) {
+                plot_count_sta -= plot_intv_sta;
+                if ((rc = stations(time)) != FW_OK) return fail("STATIONS", rc);
+            }
+        }
         if (time >= plot_start) {
             plot_count += dt;
             if (plot_count >= plot_intv) {
@@ -355,6 +463,10 @@ int main(int argc, char **argv) {
         fw_get_scalar(ctx, "DT", &dt);
     }
     if (tdt) std::fclose(tdt);
+    for (size_t k = 0; k < sta_f.size(); k++) {
+        flush_station(k);
+        std::fclose(sta_f[k]);
+    }
     rc = fw_destroy(ctx);
     std::printf("fw_main: done, TIME %.6f, %d files\n", time, icount);
     return rc == FW_OK ? 0 : 1;

@@ -225,6 +225,8 @@ def load_library(path=None):
     L.fw_end_step.argtypes = [vp, ctypes.POINTER(ip)]
     L.fw_step.argtypes = [vp, ip, ctypes.POINTER(ip)]
     L.fw_step_async.argtypes = [vp, ip]
+    L.fw_get_points.argtypes = [vp, ctypes.c_char_p, ip, ctypes.POINTER(ip), ctypes.POINTER(ip),
+                                ctypes.POINTER(dp)]
     L.fw_step_wait.argtypes = [vp, ctypes.POINTER(ip)]
     L.fw_ensemble_step.argtypes = [ctypes.POINTER(vp), ip, ip, ctypes.POINTER(ip)]
     L.fw_launch_count.argtypes = [vp]

@@ -128,6 +128,11 @@ int fw_init(fw_ctx *ctx, const double *depth, const double *eta, const double *u
  * (double, or int32 for MASK/MASK9/MASK_STRUC).  Synchronous. */
 int fw_get_field(fw_ctx *ctx, const char *name, void *host);
 int fw_set_field(fw_ctx *ctx, const char *name, const void *host);
+/* The values of one field (names as fw_get_field) at n cells given by
+ * 1-based Fortran indices I[k], J[k] (ghost cells included in the range),
+ * as double (masks as 0/1).  For station output (STATIONS, io.F:3786-3954)
+ * without moving whole fields.  Synchronous. */
+int fw_get_points(fw_ctx *ctx, const char *name, int n, const int *I, const int *J, double *out);
 /* scalars "TIME","DT","EtaBlowVal","T_brk","Width_WK","ilo","ihi","jlo","jhi","T_sum" */
 int fw_get_scalar(fw_ctx *ctx, const char *name, double *value);
 int fw_set_scalar(fw_ctx *ctx, const char *name, double value);

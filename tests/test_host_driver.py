@@ -126,3 +126,68 @@ def test_driver_run_matches_solver(fw, tmp_path):
     assert np.abs(eta).max() > 1e-4
     assert np.allclose(last, eta.astype(np.float32), rtol=6e-6, atol=1e-12)
     s.close()
+
+
+@pytest.mark.gpu
+def test_driver_binary_fields_and_stations(fw, tmp_path):
+    """FIELD_IO_TYPE = BINARY writes the interior in Fortran order as double
+    (FP64), equal to the solver's state; STATIONS samples eta, u, v at the
+    station cells each PLOT_INTV_STATION (zeros on dry cells)."""
+    d = str(tmp_path)
+    with open(os.path.join(d, "stations.txt"), "w") as f:
+        f.write("6 5\n24 8\n30 9\n")  # the last one lies outside the 24 x 16 grid
+    extra = {"DEPTH_TYPE": "SLOPE", "DEPTH_FLAT": 3.0, "SLP": 0.2, "Xslp": 20.0, "WAVEMAKER": "WK_REG",
+             "AMP_WK": 0.05, "Tperiod": 3.0, "DEP_WK": 3.0, "Xc_WK": 10.0, "Time_ramp": 1.0,
+             "TOTAL_TIME": 3.0, "PLOT_INTV": 1.0, "PERIODIC": "T", "MinDepth": 0.01,
+             "FIELD_IO_TYPE": "BINARY", "NumberStations": 3, "STATIONS_FILE": os.path.join(d, "stations.txt"),
+             "PLOT_INTV_STATION": 1.0, "StationOutputBuffer": 2}
+    _write_input(d, extra)
+    r = subprocess.run([_driver(fw), os.path.join(d, "input.txt")], capture_output=True, text=True, cwd=d,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    files = sorted(f for f in os.listdir(d) if f.startswith("eta_"))
+    assert len(files) >= 3
+    etas = [np.fromfile(os.path.join(d, f), dtype=np.float64).reshape(16, 24).T for f in files]
+    i0 = int(20.0 / 2.0) + 1
+    I = np.arange(1, 25)
+    wet = np.where(I >= i0, 3.0 - 0.2 * (I - i0) * 2.0, 3.0) > 0.0
+    assert np.all(etas[0][wet, :] == 0.0)  # still water; dry land holds MinDepth - h
+    assert np.abs(etas[-1][wet, :]).max() > 1e-4
+    assert sorted(f for f in os.listdir(d) if f.startswith("sta_")) == ["sta_0001", "sta_0002"]
+    rows = np.array([[float(line[:21])] + [float(line[21 + 16 * k:37 + 16 * k]) for k in range(3)]
+                     for line in open(os.path.join(d, "sta_0001"))])
+    times = np.loadtxt(os.path.join(d, "time_dt.out"), ndmin=2)[:, 0]
+    assert rows.shape[0] == len(files)  # one sample per output (same interval), none dropped
+    assert np.allclose(rows[:, 0], times, rtol=1e-9)
+    for k, e in enumerate(etas):
+        assert abs(rows[k, 1] - e[5, 4]) <= 1e-5 * max(abs(e[5, 4]), 1e-3)
+    # station 2 sits at x = 24 m on dry land: zeros
+    rows2 = np.loadtxt(os.path.join(d, "sta_0002"), ndmin=2)
+    assert np.all(rows2[:, 1:] == 0.0)
+
+
+@pytest.mark.gpu
+def test_get_points_equals_fields(fw):
+    import ctypes
+    p, depth, _ = fw.cases.planar_beach(Mglob=40, Nglob=24, seed=21)
+    for prec in ("FP64", "MIXED"):
+        s = fw.Solver(fw.with_defaults(p), precision=prec)
+        s.init(depth)
+        s.step(5)
+        I = np.array([1, 4, 20, 46, 33], dtype=np.int32)
+        J = np.array([1, 4, 12, 30, 7], dtype=np.int32)
+        for name in ("Eta", "U", "MASK", "P"):
+            out = np.zeros(5)
+            rc = s.L.fw_get_points(s.ctx, name.encode(), 5, I.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                   J.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                   out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+            assert rc == 0
+            full = s.get(name)
+            assert np.array_equal(out, full[I - 1, J - 1].astype(float)), name
+        bad = np.array([47], dtype=np.int32)  # beyond Mloc = 46
+        out = np.zeros(1)
+        rc = s.L.fw_get_points(s.ctx, b"Eta", 1, bad.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                               J[:1].ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                               out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        assert rc == -3
+        s.close()
