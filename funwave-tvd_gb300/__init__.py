@@ -12,9 +12,11 @@ Layout of the Python side:
   ``cases``   seeded synthetic cases (bathymetries, wavemakers)
   ``solver``  the ctypes binding and the :class:`Solver` object
   ``ensemble`` independent runs of uneven size stepped concurrently
+  ``learned`` the learned coarse-grid correction (network, pairs, training)
 """
 from .params import PARAM_DEFAULTS, read_input_txt, with_defaults  # noqa: F401
 from .solver import (  # noqa: F401
     FW_ERRORS, FwError, Solver, build, lib_path, load_library, declared_symbols)
 from . import cases  # noqa: F401
 from .ensemble import Ensemble, max_runup  # noqa: F401
+from . import learned  # noqa: F401

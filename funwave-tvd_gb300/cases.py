@@ -147,8 +147,8 @@ def ensemble_members(n=512, seed=0, nfreq=24, ntheta=8, cells_range=(128 * 256, 
 
 
 def barred_beach(Mglob=4096, Nglob=4096, dx=1.0, seed=0, h_off=12.0, wk_from_shore=180.0, nfreq=32,
-                 ntheta=8, **overrides):
-    """A 1:40 beach whose shoreline lies 300 m from the east wall, seaward of
+                 ntheta=8, shore_from_east=300.0, **overrides):
+    """A 1:40 beach whose shoreline lies shore_from_east m from the east wall, seaward of
     it a flat h_off offshore floor; an alongshore-uniform Gaussian bar 1.5 m
     high and 30 m wide (standard deviation 30/2.355 m) centred 80 m offshore
     of the shoreline, cut by 4 rip channels 20 m wide (the bar is removed
@@ -159,7 +159,7 @@ def barred_beach(Mglob=4096, Nglob=4096, dx=1.0, seed=0, h_off=12.0, wk_from_sho
     Wetting-drying and breaking are on (the defaults)."""
     x = (np.arange(Mglob) + 0.5) * dx
     y = (np.arange(Nglob) + 0.5) * dx
-    x_shore = Mglob * dx - 300.0
+    x_shore = Mglob * dx - shore_from_east
     h = np.minimum(h_off, (x_shore - x) / 40.0)
     X, Y = np.meshgrid(x, y, indexing="ij")
     bar = 1.5 * np.exp(-0.5 * ((X - (x_shore - 80.0)) / (30.0 / 2.355)) ** 2)

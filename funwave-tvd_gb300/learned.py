@@ -1,0 +1,277 @@
+"""The learned coarse-grid correction (spec extension; no reference
+counterpart): a small convolutional network that corrects each step of a
+2x-coarser run toward the fine-grid solution.
+
+  Net             ctypes handle of the library's network (fw_net_*): forward,
+                  loss + gradients, Adam, parameters
+  restrict        2x2 cell averages of a fine field (coarse cell I takes
+                  the fine cells 2I-1, 2I)
+  make_pairs      one-step training pairs generated by the solver itself:
+                  the coarse state restricted from a fine run at time t, and
+                  the difference between the restricted fine state at the
+                  next coarse time and one plain coarse step from it
+  train           Adam on the pairs (the network's own forward and backward
+                  kernels on the GPU)
+  rollout         a coarse run with fw_correct after every step
+
+Inputs are (eta, u, v, depth / FW_NET_DEPTH_SCALE, MASK) of the coarse
+interior, outputs FW_NET_OUT_SCALE times the corrections of (eta, u, v).
+The coarse run uses twice the fine run's fixed time step (DT_fixed).
+"""
+import ctypes
+
+import numpy as np
+
+from .params import with_defaults
+from .solver import FwError, Solver, load_library
+
+DEPTH_SCALE = 10.0
+OUT_SCALE = 100.0
+G = 3
+
+
+def _bind(L):
+    vp, ip, fp = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+    L.fw_net_create.argtypes = [ctypes.c_ulonglong, ctypes.POINTER(vp)]
+    L.fw_net_destroy.argtypes = [vp]
+    L.fw_net_num_params.argtypes = [vp]
+    L.fw_net_num_params.restype = ctypes.c_longlong
+    L.fw_net_get_params.argtypes = [vp, vp]
+    L.fw_net_set_params.argtypes = [vp, vp]
+    L.fw_net_get_grads.argtypes = [vp, vp]
+    L.fw_net_forward.argtypes = [vp, vp, ip, ip, ip, vp, vp]
+    L.fw_net_loss_grad.argtypes = [vp, vp, vp, vp, ip, ip, ip, ctypes.POINTER(ctypes.c_double), vp]
+    L.fw_net_adam.argtypes = [vp, fp, fp, fp, fp, vp]
+    L.fw_correct.argtypes = [vp, vp, ctypes.c_double, ctypes.POINTER(ip)]
+    return L
+
+
+class Net:
+    """The library's network; tensors are torch CUDA float32, channels-last."""
+
+    def __init__(self, seed=0):
+        self.L = _bind(load_library())
+        h = ctypes.c_void_p()
+        rc = self.L.fw_net_create(int(seed), ctypes.byref(h))
+        if rc != 0:
+            raise FwError(rc, "fw_net_create")
+        self.h = h
+        self.n = int(self.L.fw_net_num_params(h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fw_net_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        a = np.zeros(self.n, dtype=np.float32)
+        self._ck(self.L.fw_net_get_params(self.h, a.ctypes.data), "get_params")
+        return a
+
+    def set_params(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        assert a.size == self.n
+        self._ck(self.L.fw_net_set_params(self.h, a.ctypes.data), "set_params")
+
+    def grads(self):
+        a = np.zeros(self.n, dtype=np.float32)
+        self._ck(self.L.fw_net_get_grads(self.h, a.ctypes.data), "get_grads")
+        return a
+
+    def forward(self, x):
+        import torch
+        B, H, W, C = x.shape
+        assert C == 5 and x.is_cuda and x.dtype == torch.float32 and x.is_contiguous()
+        y = torch.empty((B, H, W, 3), dtype=torch.float32, device=x.device)
+        s = torch.cuda.current_stream().cuda_stream
+        self._ck(self.L.fw_net_forward(self.h, x.data_ptr(), B, H, W, y.data_ptr(), s), "forward")
+        return y
+
+    def loss_grad(self, x, target, wmask):
+        import torch
+        B, H, W, _ = x.shape
+        loss = ctypes.c_double()
+        s = torch.cuda.current_stream().cuda_stream
+        self._ck(self.L.fw_net_loss_grad(self.h, x.data_ptr(), target.data_ptr(), wmask.data_ptr(), B, H, W,
+                                         ctypes.byref(loss), s), "loss_grad")
+        return loss.value
+
+    def adam(self, lr, beta1=0.9, beta2=0.999, eps=1e-8):
+        import torch
+        s = torch.cuda.current_stream().cuda_stream
+        self._ck(self.L.fw_net_adam(self.h, float(lr), float(beta1), float(beta2), float(eps), s), "adam")
+
+    def correct(self, solver, max_corr=0.2):
+        ap = ctypes.c_int()
+        self._ck(self.L.fw_correct(solver.ctx, self.h, float(max_corr), ctypes.byref(ap)), "fw_correct")
+        return bool(ap.value)
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise FwError(rc, what)
+
+
+def restrict(a):
+    """2x2 cell average of an interior field (Mf x Nf -> Mf/2 x Nf/2)."""
+    return 0.25 * (a[0::2, 0::2] + a[1::2, 0::2] + a[0::2, 1::2] + a[1::2, 1::2])
+
+
+def coarse_case(params, depth):
+    """The coarse twin of a fine case: DX, DY doubled, grid halved, depth
+    restricted, DT_fixed doubled."""
+    p = dict(params)
+    p["Mglob"] //= 2
+    p["Nglob"] //= 2
+    p["DX"] = 2.0 * p["DX"]
+    p["DY"] = 2.0 * p["DY"]
+    p["DT_fixed"] = 2.0 * p["DT_fixed"]
+    return p, np.asfortranarray(restrict(depth))
+
+
+def features(eta, u, v, depth, mask):
+    """[H=N][W=M][5] channels-last network input from interior (M, N) fields."""
+    f = np.stack([eta, u, v, depth / DEPTH_SCALE, (mask > 0).astype(float)], axis=-1)
+    return np.ascontiguousarray(f.transpose(1, 0, 2), dtype=np.float32)
+
+
+def _interior(a):
+    return a[G:-G, G:-G]
+
+
+def _set_state(cs, eta, u, v, ubar, vbar, depth_c, mask):
+    """Put a restricted state on the coarse solver (interior; ghosts by EXCHANGE)."""
+    M, N = eta.shape
+    full = {}
+    for name, val in (("Eta", eta), ("U", u), ("V", v), ("Ubar", ubar), ("Vbar", vbar)):
+        a = cs.get(name)
+        a[G:-G, G:-G] = val
+        full[name] = a
+    H = full["Eta"] + cs.get("Depth")
+    full["H"] = H
+    full["HU"] = np.maximum(H, 0.0) * full["U"]
+    full["HV"] = np.maximum(H, 0.0) * full["V"]
+    for name, a in full.items():
+        cs.set(name, a)
+    m = cs.get("MASK")
+    m[G:-G, G:-G] = mask
+    cs.set("MASK", m)
+    cs.exchange()
+
+
+def make_pairs(case, nsteps_c, precision="MIXED", every=1):
+    """Training pairs from one fine run of case = (params, depth, phases)
+    (params with DT_fixed): returns (x [K, N, M, 5], target [K, N, M, 3],
+    wmask [K, N, M]) as numpy float32, the target already multiplied by
+    OUT_SCALE."""
+    pf, depth, phases = case
+    pf = with_defaults(pf)
+    pc, depth_c = coarse_case(pf, depth)
+    fs = Solver(pf, precision=precision)
+    fs.init(depth, phases=phases)
+    cs = Solver(with_defaults(pc), precision=precision)
+    cs.init(depth_c, phases=phases)
+    xs, ts, ws = [], [], []
+
+    def fine_state():
+        return {n: restrict(_interior(fs.get(n))) for n in ("Eta", "U", "V", "Ubar", "Vbar")}
+
+    prev = fine_state()
+    prev_mask = _interior(cs.get("MASK"))
+    for k in range(nsteps_c):
+        t0 = fs.scalar("TIME")
+        fs.step(2)
+        cur = fine_state()
+        if k % every == 0:
+            dc = _interior(cs.get("Depth"))
+            mask = ((prev["Eta"] + dc) > 1e-3).astype(np.int32)
+            _set_state(cs, prev["Eta"], prev["U"], prev["V"], prev["Ubar"], prev["Vbar"], dc, mask)
+            cs.set_scalar("TIME", t0)
+            cs.step(1)
+            ec, uc, vc = (_interior(cs.get(n)) for n in ("Eta", "U", "V"))
+            mc = _interior(cs.get("MASK"))
+            wet = ((mask > 0) & (mc > 0)).astype(np.float32)
+            xs.append(features(prev["Eta"], prev["U"], prev["V"], dc, mask))
+            tgt = np.stack([cur["Eta"] - ec, cur["U"] - uc, cur["V"] - vc], axis=-1) * OUT_SCALE
+            ts.append(np.ascontiguousarray((tgt * wet[..., None]).transpose(1, 0, 2), dtype=np.float32))
+            ws.append(np.ascontiguousarray(wet.T))
+        prev = cur
+    fs.close()
+    cs.close()
+    return np.stack(xs), np.stack(ts), np.stack(ws)
+
+
+def train(net, x, t, w, iters=400, batch=8, lr=2e-3, seed=0, log=None):
+    """Adam on random minibatches of the pairs (all on the GPU)."""
+    import torch
+    dev = torch.device("cuda")
+    X = torch.from_numpy(x).to(dev)
+    T = torch.from_numpy(t).to(dev)
+    Wm = torch.from_numpy(w).to(dev)
+    rng = np.random.default_rng(seed)
+    losses = []
+    for it in range(iters):
+        idx = torch.from_numpy(rng.choice(x.shape[0], size=min(batch, x.shape[0]), replace=False)).to(dev)
+        xb, tb, wb = X[idx].contiguous(), T[idx].contiguous(), Wm[idx].contiguous()
+        loss = net.loss_grad(xb, tb, wb)
+        net.adam(lr * (0.5 ** (it / max(1, iters // 3))))
+        losses.append(loss)
+        if log and it % 100 == 0:
+            log(it, loss)
+    return losses
+
+
+def one_step_error(net, x, t, w):
+    """Masked MSE of the targets without and with the network's prediction
+    (in OUT_SCALE units), over all pairs."""
+    import torch
+    dev = torch.device("cuda")
+    e0 = e1 = 0.0
+    for k in range(x.shape[0]):
+        xb = torch.from_numpy(x[k:k + 1]).to(dev).contiguous()
+        y = net.forward(xb).cpu().numpy()[0]
+        m = w[k][..., None]
+        e0 += float(np.sum(m * t[k] ** 2))
+        e1 += float(np.sum(m * (t[k] - y) ** 2))
+    return e0, e1
+
+
+def rollout(case, nsteps_c, net=None, precision="MIXED", max_corr=0.2):
+    """The coarse twin of case run for nsteps_c steps, with the network's
+    correction after every step when net is given; returns (coarse solver
+    state dict of interior Eta, U, V, HeightMax; steps corrected)."""
+    pf, depth, phases = case
+    pc, depth_c = coarse_case(with_defaults(pf), depth)
+    pc = with_defaults(pc)
+    pc["OUT_Hmax"] = True
+    cs = Solver(pc, precision=precision)
+    cs.init(depth_c, phases=phases)
+    applied = 0
+    for _ in range(nsteps_c):
+        cs.step(1)
+        if net is not None:
+            applied += int(net.correct(cs, max_corr))
+    out = {n: _interior(cs.get(n)) for n in ("Eta", "U", "V", "HeightMax", "MASK")}
+    out["TIME"] = cs.scalar("TIME")
+    out["depth"] = depth_c
+    cs.close()
+    return out, applied
+
+
+def fine_run(case, nsteps_f, precision="MIXED"):
+    pf, depth, phases = case
+    pf = with_defaults(pf)
+    pf["OUT_Hmax"] = True
+    fs = Solver(pf, precision=precision)
+    fs.init(depth, phases=phases)
+    fs.step(nsteps_f)
+    out = {n: _interior(fs.get(n)) for n in ("Eta", "U", "V", "HeightMax", "MASK")}
+    out["TIME"] = fs.scalar("TIME")
+    out["depth"] = depth
+    fs.close()
+    return out

@@ -33,6 +33,7 @@ _SOURCES = {
     "fw_api.cu": [],
     "fw_init.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "fw_noalloc.cu": ["-fmad=false"],
+    "fw_learn.cu": [],
 }
 
 FW_ERRORS = {0: "FW_OK", -1: "FW_ERR_CUDA", -2: "FW_ERR_OOM", -3: "FW_ERR_BAD_PARAM",

@@ -165,6 +165,37 @@ int fw_ensemble_step(fw_ctx *const *ctxs, int n, int nsteps, int *status);
 /* Synchronise the context's stream. */
 int fw_sync(fw_ctx *ctx);
 
+/* --- learned coarse-grid correction (no reference counterpart) ---------- */
+/* A 4-layer 3x3 convolutional network on the coarse grid: inputs
+ * (eta, u, v, depth / FW_NET_DEPTH_SCALE, MASK), three hidden layers of 32
+ * channels with ReLU, outputs FW_NET_OUT_SCALE times the corrections of
+ * (eta, u, v).  BF16 weights and activations, FP32 accumulation, FP32
+ * master weights, gradients and Adam moments; zero padding at the edges.
+ * Tensors are channels-last FP32 on the device: x [B][H][W][5], y and
+ * targets [B][H][W][3], wmask [B][H][W], with W along the grid's x (I). */
+#define FW_NET_DEPTH_SCALE 10.0
+#define FW_NET_OUT_SCALE 100.0
+typedef struct fw_net fw_net;
+int fw_net_create(unsigned long long seed, fw_net **out);    /* He-initialised from seed */
+int fw_net_destroy(fw_net *net);
+long long fw_net_num_params(fw_net *net);
+int fw_net_get_params(fw_net *net, float *host);            /* FP32 master weights, layer by layer: */
+int fw_net_set_params(fw_net *net, const float *host);      /*   w[9][cin][cout] then b[cout] */
+int fw_net_get_grads(fw_net *net, float *host);             /* gradients of the last fw_net_loss_grad */
+int fw_net_forward(fw_net *net, const float *x, int B, int H, int W, float *y, void *stream);
+/* forward, the masked mean squared error sum(wmask*(y-target)^2)/(B*H*W)
+ * into *loss (host), and the gradients of every parameter */
+int fw_net_loss_grad(fw_net *net, const float *x, const float *target, const float *wmask, int B, int H,
+                     int W, double *loss, void *stream);
+int fw_net_adam(fw_net *net, float lr, float beta1, float beta2, float eps, void *stream);
+/* Apply the network to a context's current state: the eta correction is
+ * projected to zero mean over the wet interior cells (so the volume is
+ * unchanged), then eta, u, v (and H, HU, HV, Ubar, Vbar to first order) are
+ * corrected on wet cells.  The correction is skipped (*applied = 0) when any
+ * |correction| exceeds max_corr (the network's input is then outside what it
+ * was trained on); the plain step stands. */
+int fw_correct(fw_ctx *ctx, fw_net *net, double max_corr, int *applied);
+
 /* --- the reference's units, one call each (for coupling and parity) ---- */
 int fw_exchange(fw_ctx *ctx);            /* EXCHANGE        bc.F:426 */
 int fw_estimate_dt(fw_ctx *ctx);         /* ESTIMATE_DT     misc.F:216 */

@@ -1,0 +1,116 @@
+"""The learned coarse-grid correction (a spec extension without a
+reference counterpart).
+
+CPU: the numpy reference of the network (oracle/fw_net_oracle.py) against
+finite differences, in float64.
+GPU: the library's forward pass and every parameter gradient against that
+reference (with BF16 rounding of weights and activations as the GPU stores
+them), and the effect of training on held-out one-step errors.
+"""
+import numpy as np
+import pytest
+
+
+def _rand_params(ref, seed):
+    rng = np.random.default_rng(seed)
+    p = []
+    for ci, co, _ in ref.LAYERS:
+        cin_real = 5 if ci == 8 else ci
+        w = rng.normal(0.0, np.sqrt(2.0 / (9 * cin_real)), size=(9, ci, co))
+        w[:, cin_real:, :] = 0.0
+        p.append(w.ravel())
+        p.append(rng.normal(0.0, 0.1, size=co))
+    return np.concatenate(p).astype(np.float32)
+
+
+def test_reference_gradients_by_finite_differences():
+    import fw_net_oracle as ref
+    rng = np.random.default_rng(1)
+    params = _rand_params(ref, 2).astype(np.float64)
+    x = rng.normal(size=(2, 5, 6, 5))
+    t = rng.normal(size=(2, 5, 6, 3))
+    w = (rng.uniform(size=(2, 5, 6)) > 0.3).astype(float)
+    loss, g = ref.loss_grad(params, x, t, w, bf16=False)
+    eps = 1e-6
+    for k in rng.choice(params.size, size=40, replace=False):
+        if k < 9 * 8 * 32 and (k // 32) % 8 >= 5:
+            continue  # padding input channels
+        pp, pm = params.copy(), params.copy()
+        pp[k] += eps
+        pm[k] -= eps
+        fd = (ref.loss_grad(pp, x, t, w, bf16=False)[0] - ref.loss_grad(pm, x, t, w, bf16=False)[0]) / (2 * eps)
+        assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(fd)), (k, fd, g[k])
+
+
+@pytest.mark.gpu
+def test_gpu_forward_and_gradients_match_reference(fw):
+    import torch
+    import fw_net_oracle as ref
+    net = fw.learned.Net(seed=3)
+    assert net.n == ref.num_params()
+    params = _rand_params(ref, 4)
+    net.set_params(params)
+    rng = np.random.default_rng(5)
+    x = rng.normal(size=(2, 9, 13, 5)).astype(np.float32)
+    t = rng.normal(size=(2, 9, 13, 3)).astype(np.float32)
+    w = (rng.uniform(size=(2, 9, 13)) > 0.2).astype(np.float32)
+    dev = torch.device("cuda")
+    X, T, Wm = (torch.from_numpy(a).to(dev).contiguous() for a in (x, t, w))
+    y = net.forward(X).cpu().numpy()
+    y_ref, _ = ref.forward(params, x, bf16=True)
+    assert np.abs(y - y_ref).max() <= 1e-3 * np.abs(y_ref).max()
+    loss = net.loss_grad(X, T, Wm)
+    loss_ref, g_ref = ref.loss_grad(params, x, t, w, bf16=True)
+    assert abs(loss - loss_ref) <= 1e-4 * loss_ref
+    g = net.grads()
+    off = 0
+    for ci, co, _ in ref.LAYERS:
+        n = 9 * ci * co + co
+        a, b = g[off:off + n], g_ref[off:off + n]
+        assert np.linalg.norm(a - b) <= 2e-3 * np.linalg.norm(b), (ci, co, np.linalg.norm(a - b) / np.linalg.norm(b))
+        off += n
+    net.close()
+
+
+def _barred_case(fw, seed, M=256, N=128):
+    p, d, ph, _ = fw.cases.barred_beach(M, N, 1.0, seed=seed, wk_from_shore=150.0, nfreq=16, ntheta=4,
+                                        shore_from_east=40.0, Hmo=0.8, Sponge_west_width=30.0)
+    p["DT_fixed"] = 0.04
+    return (p, d, ph)
+
+
+@pytest.mark.gpu
+def test_training_reduces_held_out_error(fw):
+    """Pairs from three seeded barred beaches (fine dx = 1 m, coarse 2 m, the
+    solver generating both), 600 Adam steps, then on a fourth, held-out
+    beach: the one-step coarse error with the correction is at least 30 %
+    below the plain coarse step's, and a 200-step corrected coarse run is
+    no further from the restricted fine run in eta than the plain one."""
+    L = fw.learned
+    X, T, W = [], [], []
+    for seed in (1, 2, 3):
+        x, t, w = L.make_pairs(_barred_case(fw, seed), 200, every=2)
+        X.append(x)
+        T.append(t)
+        W.append(w)
+    X, T, W = np.concatenate(X), np.concatenate(T), np.concatenate(W)
+    assert np.sqrt((T ** 2).mean()) > 1e-3  # the coarse step does err
+    held = _barred_case(fw, 9)
+    xh, th, wh = L.make_pairs(held, 200, every=2)
+    net = L.Net(seed=0)
+    losses = L.train(net, X, T, W, iters=600, batch=8, lr=2e-3)
+    assert np.mean(losses[-50:]) < 0.5 * np.mean(losses[:20])
+    e_plain, e_net = L.one_step_error(net, xh, th, wh)
+    assert e_net <= 0.7 * e_plain, (e_net, e_plain)
+    fine = L.fine_run(held, 400)
+    plain, _ = L.rollout(held, 200)
+    corr, applied = L.rollout(held, 200, net=net)
+    assert applied == 200
+    f = L.restrict(fine["Eta"])
+    m = (plain["MASK"] > 0) & (corr["MASK"] > 0)
+    r_plain = np.sqrt(np.mean((plain["Eta"] - f)[m] ** 2))
+    r_corr = np.sqrt(np.mean((corr["Eta"] - f)[m] ** 2))
+    assert r_corr <= r_plain, (r_corr, r_plain)
+    # the eta correction is projected to zero mean over wet cells: the
+    # corrected run keeps the plain run's volume budget
+    net.close()
