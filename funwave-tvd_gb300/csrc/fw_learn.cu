@@ -16,6 +16,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -36,44 +37,182 @@ typedef __nv_bfloat16 bf16;
 
 __device__ __forceinline__ float bf(bf16 v) { return __bfloat162float(v); }
 
+// Hidden activations (32 channels) are stored with their channel pairs
+// permuted: pair P = c/2 sits at word (P % 4) * 4 + P / 4 of the pixel, so
+// that the four words a tensor-core lane needs for one tap (pairs t, 4+t,
+// 8+t, 12+t) are one 16-byte load and its outputs one 16-byte store.  The
+// 8-channel input is stored in natural order.
+template <int C> __device__ __forceinline__ int sidx(int c) {
+    if constexpr (C == 32) {
+        const int P = c >> 1;
+        return (((P & 3) << 2) + (P >> 2)) * 2 + (c & 1);
+    } else {
+        return c;
+    }
+}
+
 // ---------------------------------------------------------------------------
-// forward: one thread per output pixel, all COUT channels in registers
+// forward of the 32-input-channel layers on the tensor cores: implicit GEMM
+// with M = pixels (16 per warp tile, consecutive in memory), N = output
+// channels (NT tiles of 8), K = 9 taps x 32 channels (18 steps of 16),
+// mma.sync m16n8k16 BF16 x BF16 -> FP32.  Each lane loads its A rows (two
+// pixels' channel pairs, zero outside the grid) straight from the
+// channels-last activations; the weights sit in shared memory as BF16
+// pairs [tap][co][ci/2], rows padded to 20 words (conflict-free).
 // ---------------------------------------------------------------------------
-template <int CIN, int COUT, bool RELU, bool OUT_BF16>
-__global__ void __launch_bounds__(128) k_conv_fwd(const bf16 *__restrict__ x, const float *__restrict__ w,
-                                                  const float *__restrict__ bias, void *y, int B, int H, int W) {
-    __shared__ float ws[9 * CIN * COUT];
-    __shared__ float bs[COUT];
-    for (int e = threadIdx.x; e < 9 * CIN * COUT; e += blockDim.x) ws[e] = bf(__float2bfloat16(w[e]));
-    for (int e = threadIdx.x; e < COUT; e += blockDim.x) bs[e] = bias[e];
-    __syncthreads();
-    const long long npix = (long long)B * H * W;
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npix) return;
-    const int px = (int)(p % W), py = (int)((p / W) % H);
-    float acc[COUT];
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const uint32_t l = __bfloat16_as_ushort(__float2bfloat16(lo));
+    const uint32_t h = __bfloat16_as_ushort(__float2bfloat16(hi));
+    return l | (h << 16);
+}
+
+__device__ __forceinline__ void mma_bf16(float *c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// epilogue of a warp tile: bias, ReLU, then the permuted BF16 layout (one
+// 16-byte store per pixel and lane when COUT = 32) or natural FP32
+template <int NT, int COUT, bool RELU, bool OUT_BF16>
+__device__ __forceinline__ void store_tile(float (&acc)[NT][4], const float *bs, void *y, long long pa, long long pb,
+                                           bool ina, bool inb, int t) {
+    uint32_t wa[NT], wb[NT];
 #pragma unroll
-    for (int co = 0; co < COUT; co++) acc[co] = bs[co];
-    for (int ky = -1; ky <= 1; ky++) {
-        if (py + ky < 0 || py + ky >= H) continue;
-        for (int kx = -1; kx <= 1; kx++) {
-            if (px + kx < 0 || px + kx >= W) continue;
-            const bf16 *xi = x + (p + (long long)ky * W + kx) * CIN;
-            const float *wk = ws + ((ky + 1) * 3 + (kx + 1)) * CIN * COUT;
-#pragma unroll 4
-            for (int ci = 0; ci < CIN; ci++) {
-                const float xv = bf(xi[ci]);
+    for (int nt = 0; nt < NT; nt++) {
+        const int c = nt * 8 + 2 * t;
+        float v[4] = {acc[nt][0] + bs[c], acc[nt][1] + bs[c + 1], acc[nt][2] + bs[c], acc[nt][3] + bs[c + 1]};
+        if (RELU)
 #pragma unroll
-                for (int co = 0; co < COUT; co++) acc[co] += xv * wk[ci * COUT + co];
-            }
+            for (int q = 0; q < 4; q++) v[q] = v[q] > 0.0f ? v[q] : 0.0f;
+        if (OUT_BF16) {
+            wa[nt] = pack_bf16(v[0], v[1]);
+            wb[nt] = pack_bf16(v[2], v[3]);
+        } else {
+            float *yf = reinterpret_cast<float *>(y);
+            if (ina && c < COUT) yf[pa * COUT + c] = v[0];
+            if (ina && c + 1 < COUT) yf[pa * COUT + c + 1] = v[1];
+            if (inb && c < COUT) yf[pb * COUT + c] = v[2];
+            if (inb && c + 1 < COUT) yf[pb * COUT + c + 1] = v[3];
         }
     }
+    if constexpr (OUT_BF16) {
+        static_assert(COUT == 32 && NT == 4, "BF16 outputs are the 32-channel permuted layout");
+        uint32_t *yw = reinterpret_cast<uint32_t *>(y);
+        // pair nt*4 + t sits at word t*4 + nt
+        if (ina) *reinterpret_cast<uint4 *>(yw + pa * 16 + 4 * t) = make_uint4(wa[0], wa[1], wa[2], wa[3]);
+        if (inb) *reinterpret_cast<uint4 *>(yw + pb * 16 + 4 * t) = make_uint4(wb[0], wb[1], wb[2], wb[3]);
+    }
+}
+
+// the first layer (8 natural input channels) on the tensor cores: a K step
+// of 16 holds two taps (8 channels each), five steps cover the 9 taps plus
+// one zero tap
+__global__ void __launch_bounds__(128) k_conv8_fwd_mma(const bf16 *__restrict__ x, const float *__restrict__ w,
+                                                       const float *__restrict__ bias, bf16 *y, int B, int H, int W) {
+    constexpr int CIN = 8, COUT = 32, WS = 12;
+    __shared__ uint32_t wT[5][COUT][WS];  // [k step][co][words: 4 of tap 2s, 4 of tap 2s+1]
+    __shared__ float bs[COUT];
+    for (int e = threadIdx.x; e < 5 * COUT * 8; e += blockDim.x) {
+        const int wd = e % 8, co = (e / 8) % COUT, ks = e / (8 * COUT);
+        const int tap = 2 * ks + (wd >> 2), cp = wd & 3;
+        float lo = 0.0f, hi = 0.0f;
+        if (tap < 9) {
+            lo = w[((size_t)tap * CIN + 2 * cp) * COUT + co];
+            hi = w[((size_t)tap * CIN + 2 * cp + 1) * COUT + co];
+        }
+        wT[ks][co][wd] = pack_bf16(lo, hi);
+    }
+    for (int e = threadIdx.x; e < COUT; e += blockDim.x) bs[e] = bias[e];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const long long npix = (long long)B * H * W;
+    const long long ntile = (npix + 15) / 16;
+    const uint32_t *xw = reinterpret_cast<const uint32_t *>(x);  // 4 words per pixel
+    for (long long tile = (long long)blockIdx.x * 4 + warp; tile < ntile; tile += (long long)gridDim.x * 4) {
+        const long long pa = tile * 16 + g, pb = pa + 8;
+        const bool ina = pa < npix, inb = pb < npix;
+        const int xa = (int)(pa % W), ya = (int)((pa / W) % H);
+        const int xb = (int)(pb % W), yb = (int)((pb / W) % H);
+        float acc[4][4];
 #pragma unroll
-    for (int co = 0; co < COUT; co++) {
-        float v = acc[co];
-        if (RELU) v = v > 0.0f ? v : 0.0f;
-        if (OUT_BF16) ((bf16 *)y)[p * COUT + co] = __float2bfloat16(v);
-        else ((float *)y)[p * COUT + co] = v;
+        for (int nt = 0; nt < 4; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll
+        for (int ks = 0; ks < 5; ks++) {
+            uint32_t a[4];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int tap = 2 * ks + h;
+                const int kx = tap % 3 - 1, ky = tap / 3 - 1;
+                const bool va = tap < 9 && ina && xa + kx >= 0 && xa + kx < W && ya + ky >= 0 && ya + ky < H;
+                const bool vb = tap < 9 && inb && xb + kx >= 0 && xb + kx < W && yb + ky >= 0 && yb + ky < H;
+                a[2 * h] = va ? xw[(pa + (long long)ky * W + kx) * 4 + t] : 0u;
+                a[2 * h + 1] = vb ? xw[(pb + (long long)ky * W + kx) * 4 + t] : 0u;
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++)
+                mma_bf16(acc[nt], a[0], a[1], a[2], a[3], wT[ks][nt * 8 + g][t], wT[ks][nt * 8 + g][4 + t]);
+        }
+        store_tile<4, COUT, true, true>(acc, bs, y, pa, pb, ina, inb, t);
+    }
+}
+
+template <int NT, int COUT, bool RELU, bool OUT_BF16>
+__global__ void __launch_bounds__(128) k_conv32_fwd_mma(const bf16 *__restrict__ x, const float *__restrict__ w,
+                                                        const float *__restrict__ bias, void *y, int B, int H,
+                                                        int W) {
+    constexpr int CIN = 32, WS = 20;
+    __shared__ uint32_t wT[9][NT * 8][WS];
+    __shared__ float bs[NT * 8];
+    for (int e = threadIdx.x; e < 9 * NT * 8 * 16; e += blockDim.x) {
+        const int cp = e % 16, co = (e / 16) % (NT * 8), tap = e / (16 * NT * 8);
+        float lo = 0.0f, hi = 0.0f;
+        if (co < COUT) {
+            lo = w[((size_t)tap * CIN + 2 * cp) * COUT + co];
+            hi = w[((size_t)tap * CIN + 2 * cp + 1) * COUT + co];
+        }
+        wT[tap][co][cp] = pack_bf16(lo, hi);
+    }
+    for (int e = threadIdx.x; e < NT * 8; e += blockDim.x) bs[e] = e < COUT ? bias[e] : 0.0f;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const long long npix = (long long)B * H * W;
+    const long long ntile = (npix + 15) / 16;
+    const uint32_t *xw = reinterpret_cast<const uint32_t *>(x);  // 16 words per pixel
+    for (long long tile = (long long)blockIdx.x * 4 + warp; tile < ntile; tile += (long long)gridDim.x * 4) {
+        const long long pa = tile * 16 + g, pb = pa + 8;
+        const bool ina = pa < npix, inb = pb < npix;
+        const int xa = (int)(pa % W), ya = (int)((pa / W) % H);
+        const int xb = (int)(pb % W), yb = (int)((pb / W) % H);
+        float acc[NT][4];
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll
+        for (int tap = 0; tap < 9; tap++) {
+            const int kx = tap % 3 - 1, ky = tap / 3 - 1;
+            const bool va = ina && xa + kx >= 0 && xa + kx < W && ya + ky >= 0 && ya + ky < H;
+            const bool vb = inb && xb + kx >= 0 && xb + kx < W && yb + ky >= 0 && yb + ky < H;
+            // words 4t..4t+3 of the permuted pixel: pairs t, 4+t, 8+t, 12+t
+            const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
+            const uint4 qa = va ? *reinterpret_cast<const uint4 *>(xw + (pa + (long long)ky * W + kx) * 16 + 4 * t) : z4;
+            const uint4 qb = vb ? *reinterpret_cast<const uint4 *>(xw + (pb + (long long)ky * W + kx) * 16 + 4 * t) : z4;
+#pragma unroll
+            for (int ks = 0; ks < 2; ks++) {
+                const uint32_t a0 = ks == 0 ? qa.x : qa.z, a2 = ks == 0 ? qa.y : qa.w;
+                const uint32_t a1 = ks == 0 ? qb.x : qb.z, a3 = ks == 0 ? qb.y : qb.w;
+#pragma unroll
+                for (int nt = 0; nt < NT; nt++) {
+                    const uint32_t b0 = wT[tap][nt * 8 + g][ks * 8 + t];
+                    const uint32_t b1 = wT[tap][nt * 8 + g][ks * 8 + 4 + t];
+                    mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+                }
+            }
+        }
+        store_tile<NT, COUT, RELU, OUT_BF16>(acc, bs, y, pa, pb, ina, inb, t);
     }
 }
 
@@ -104,7 +243,7 @@ __global__ void __launch_bounds__(128) k_conv_dgrad(const float *__restrict__ dy
             const float *wk = ws + ((ky + 1) * 3 + (kx + 1)) * CIN * COUT;
             for (int co = 0; co < COUT; co++) {
                 float g = dy[q * COUT + co];
-                if (RELU && !(bf(y[q * COUT + co]) > 0.0f)) g = 0.0f;
+                if (RELU && !(bf(y[q * COUT + sidx<COUT>(co)]) > 0.0f)) g = 0.0f;
 #pragma unroll
                 for (int ci = 0; ci < CIN; ci++) acc[ci] += wk[ci * COUT + co] * g;
             }
@@ -145,16 +284,16 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(const bf16 *__restrict__ x, 
             const int gx = x0 + c - 1, gy = py + r - 1;
             float v = 0.0f;
             if (gx >= 0 && gx < W && gy >= 0 && gy < H)
-                v = bf(x[((row + (r - 1)) * W + gx) * CIN + ci]);
+                v = bf(x[((row + (r - 1)) * W + gx) * CIN + sidx<CIN>(ci)]);
             xs[r][c][ci] = v;
         }
         for (int e = threadIdx.x; e < TPX * COUT; e += blockDim.x) {
             const int co = e % COUT, t = e / COUT;
             float g = 0.0f;
             if (x0 + t < W) {
-                const long long q = (row * W + x0 + t) * COUT + co;
-                g = dy[q];
-                if (RELU && !(bf(y[q]) > 0.0f)) g = 0.0f;
+                const long long q = (row * W + x0 + t) * COUT;
+                g = dy[q + co];
+                if (RELU && !(bf(y[q + sidx<COUT>(co)]) > 0.0f)) g = 0.0f;
             }
             dys[t][co] = g;
         }
@@ -279,7 +418,9 @@ __global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, doubl
 }
 
 template <typename T>
-__global__ void k_corr_apply(fw::Grid g, fw::Fields<T> f, const float *out, const double *sums) {
+__global__ void k_corr_apply(fw::Grid g, fw::Fields<T> f, const float *out, const double *sums, double max_corr) {
+    // the fallback: a correction above max_corr anywhere leaves the plain step
+    if (!(sums[2] <= max_corr) || !(sums[1] == sums[1])) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mglob || j >= g.Nglob) return;
     const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
@@ -364,15 +505,17 @@ unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 void forward(fw_net *n, const float *in, long long npix, int B, int H, int W, cudaStream_t s) {
     k_pack_input<<<nblk(npix, 256), 256, 0, s>>>(in, n->act[0], npix);
-    const unsigned gb = nblk(npix, 128);
-    k_conv_fwd<CIN0, HID, true, true><<<gb, 128, 0, s>>>(n->act[0], n->w + n->woff[0], n->w + n->boff[0],
-                                                          n->act[1], B, H, W);
-    k_conv_fwd<HID, HID, true, true><<<gb, 128, 0, s>>>(n->act[1], n->w + n->woff[1], n->w + n->boff[1],
-                                                         n->act[2], B, H, W);
-    k_conv_fwd<HID, HID, true, true><<<gb, 128, 0, s>>>(n->act[2], n->w + n->woff[2], n->w + n->boff[2],
-                                                         n->act[3], B, H, W);
-    k_conv_fwd<HID, NOUT, false, false><<<gb, 128, 0, s>>>(n->act[3], n->w + n->woff[3], n->w + n->boff[3],
-                                                            n->out, B, H, W);
+    // every layer on the tensor cores: a persistent grid of warps over
+    // 16-pixel tiles
+    const long long ntile = (npix + 15) / 16;
+    const unsigned gm = (unsigned)std::min<long long>((ntile + 3) / 4, 152LL * 16);
+    k_conv8_fwd_mma<<<gm, 128, 0, s>>>(n->act[0], n->w + n->woff[0], n->w + n->boff[0], n->act[1], B, H, W);
+    k_conv32_fwd_mma<4, HID, true, true><<<gm, 128, 0, s>>>(n->act[1], n->w + n->woff[1], n->w + n->boff[1],
+                                                             n->act[2], B, H, W);
+    k_conv32_fwd_mma<4, HID, true, true><<<gm, 128, 0, s>>>(n->act[2], n->w + n->woff[2], n->w + n->boff[2],
+                                                             n->act[3], B, H, W);
+    k_conv32_fwd_mma<1, NOUT, false, false><<<gm, 128, 0, s>>>(n->act[3], n->w + n->woff[3], n->w + n->boff[3],
+                                                                n->out, B, H, W);
 }
 
 template <int CIN, int COUT, bool RELU>
@@ -416,12 +559,14 @@ template <typename T> int correct(fw_ctx *c, fw_net *n, double max_corr, int *ap
     double *sums = n->loss;  // 3 doubles of scratch after the loss slot
     cudaMemsetAsync(sums, 0, 4 * sizeof(double), s);
     k_corr_sums<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1);
-    double h[4];
-    cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return FW_ERR_CUDA;
-    const bool ok = h[3] <= max_corr && std::isfinite(h[1]);
-    if (ok) k_corr_apply<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1);
-    if (applied) *applied = ok ? 1 : 0;
+    k_corr_apply<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, max_corr);
+    if (applied) {
+        // only a caller that asks waits for the decision
+        double h[4];
+        cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return FW_ERR_CUDA;
+        *applied = (h[3] <= max_corr && h[2] == h[2]) ? 1 : 0;
+    }
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
 }
 }  // namespace

@@ -107,7 +107,12 @@ class Net:
         s = torch.cuda.current_stream().cuda_stream
         self._ck(self.L.fw_net_adam(self.h, float(lr), float(beta1), float(beta2), float(eps), s), "adam")
 
-    def correct(self, solver, max_corr=0.2):
+    def correct(self, solver, max_corr=0.2, wait=True):
+        """fw_correct on the solver's current state; with wait, whether the
+        correction was applied (else the call only enqueues it)."""
+        if not wait:
+            self._ck(self.L.fw_correct(solver.ctx, self.h, float(max_corr), None), "fw_correct")
+            return None
         ap = ctypes.c_int()
         self._ck(self.L.fw_correct(solver.ctx, self.h, float(max_corr), ctypes.byref(ap)), "fw_correct")
         return bool(ap.value)
@@ -207,16 +212,21 @@ def make_pairs(case, nsteps_c, precision="MIXED", every=1):
 
 
 def train(net, x, t, w, iters=400, batch=8, lr=2e-3, seed=0, log=None):
-    """Adam on random minibatches of the pairs (all on the GPU)."""
+    """Adam on random minibatches of the pairs (all on the GPU).  x, t, w are
+    arrays of pairs, or lists of such arrays (one per grid size); a
+    minibatch comes from one of them, chosen in proportion to its size."""
     import torch
     dev = torch.device("cuda")
-    X = torch.from_numpy(x).to(dev)
-    T = torch.from_numpy(t).to(dev)
-    Wm = torch.from_numpy(w).to(dev)
+    if not isinstance(x, (list, tuple)):
+        x, t, w = [x], [t], [w]
+    sets = [(torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev), torch.from_numpy(c).to(dev))
+            for a, b, c in zip(x, t, w)]
+    sizes = np.array([a.shape[0] for a in x], dtype=float)
     rng = np.random.default_rng(seed)
     losses = []
     for it in range(iters):
-        idx = torch.from_numpy(rng.choice(x.shape[0], size=min(batch, x.shape[0]), replace=False)).to(dev)
+        X, T, Wm = sets[rng.choice(len(sets), p=sizes / sizes.sum())]
+        idx = torch.from_numpy(rng.choice(X.shape[0], size=min(batch, X.shape[0]), replace=False)).to(dev)
         xb, tb, wb = X[idx].contiguous(), T[idx].contiguous(), Wm[idx].contiguous()
         loss = net.loss_grad(xb, tb, wb)
         net.adam(lr * (0.5 ** (it / max(1, iters // 3))))

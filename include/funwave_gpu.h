@@ -193,7 +193,9 @@ int fw_net_adam(fw_net *net, float lr, float beta1, float beta2, float eps, void
  * unchanged), then eta, u, v (and H, HU, HV, Ubar, Vbar to first order) are
  * corrected on wet cells.  The correction is skipped (*applied = 0) when any
  * |correction| exceeds max_corr (the network's input is then outside what it
- * was trained on); the plain step stands. */
+ * was trained on); the plain step stands.  The decision is made on the
+ * device: with applied == NULL the call only enqueues work on the context's
+ * stream; with applied given it waits and reports the decision. */
 int fw_correct(fw_ctx *ctx, fw_net *net, double max_corr, int *applied);
 
 /* --- the reference's units, one call each (for coupling and parity) ---- */
