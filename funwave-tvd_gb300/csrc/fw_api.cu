@@ -184,6 +184,9 @@ LinePart make_part(int L, int nlines) {
     } else {
         lp.P = L / lp.m;
     }
+    lp.lgm = -1;
+    for (int b = 0; b < 31; b++)
+        if ((1 << b) == lp.m) lp.lgm = b;
     return lp;
 }
 

@@ -107,6 +107,7 @@ struct LinePart {
     int m;       // rows per chunk (the last chunk takes the remainder)
     int P;       // chunks per line
     long long red0;  // offset (doubles) of this direction's rows in the factorisation scratch
+    int lgm;         // log2(m) when m is a power of two, else -1
 };
 
 // launchers (fw_kernels.cu), all asynchronous on the context stream

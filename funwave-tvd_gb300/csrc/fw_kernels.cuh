@@ -1626,7 +1626,7 @@ __global__ void __launch_bounds__(256) k_resid(Grid g, Fields<T> f, LinePart lp)
 // at once fall into different shared-memory banks.
 __host__ __device__ __forceinline__ int lsx_pad(int k) { return k + (k >> 4); }
 __host__ __device__ __forceinline__ size_t lsx_smem_floats(int L, int P) {
-    return (size_t)5 * (lsx_pad(L) + 1) + (size_t)L + 16 * (size_t)P;
+    return (size_t)6 * (lsx_pad(L) + 1) + (size_t)L + 16 * (size_t)P;
 }
 
 template <typename T>
@@ -1643,7 +1643,8 @@ __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePa
     float *A = shf + 2 * LP;   // sweep constants, staged with unit-stride loads (padded)
     float *LR = shf + 3 * LP;
     float *CP = shf + 4 * LP;
-    float *x0 = shf + 5 * LP;  // L  first solution (unpadded)
+    float *dn = shf + 5 * LP;  // the normalised right-hand side, kept for the residual (padded)
+    float *x0 = shf + 6 * LP;  // L  first solution (unpadded)
     float *rr = x0 + L;        // 2P reduced right-hand sides / solution
     float *pb = rr + 2 * P;    // 7 x 2P PCR buffers
     const int j = g.jb + l;
@@ -1656,7 +1657,9 @@ __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePa
     const int e = (ch == P - 1) ? L - 1 : s + m - 1;
     for (int k = threadIdx.x; k < L; k += blockDim.x) {
         const int q = lsx_pad(k);
-        d[q] = (float)rhs[k] * IT[k];
+        const float dv = (float)rhs[k] * IT[k];
+        d[q] = dv;
+        dn[q] = dv;
         A[q] = f.fac_A[0][row + k];
         LR[q] = f.fac_lr[0][row + k];
         CP[q] = f.fac_cp[0][row + k];
@@ -1694,7 +1697,7 @@ __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePa
         __syncthreads();
         pcr_solve(pb, pb + n, pb + 2 * n, rr, pb + 3 * n, pb + 4 * n, pb + 5 * n, pb + 6 * n, n);
         for (int k = threadIdx.x; k < L; k += blockDim.x) {
-            const int c = min(k / m, P - 1);
+            const int c = min(lp.lgm >= 0 ? k >> lp.lgm : k / m, P - 1);
             const int cs = c * m, ce = (c == P - 1) ? L - 1 : cs + m - 1;
             const float x = (k == cs) ? rr[2 * c]
                           : (k == ce) ? rr[2 * c + 1]
@@ -1708,7 +1711,8 @@ __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePa
             const float *CH = f.fac_ch[0] + row, *CL = f.fac_cl[0] + row;
             for (int k = threadIdx.x; k < L; k += blockDim.x) {
                 const float xm = k > 0 ? x0[k - 1] : 0.0f, xp = k < L - 1 ? x0[k + 1] : 0.0f;
-                d[lsx_pad(k)] = residual((float)rhs[k] * IT[k], x0[k], xm, xp, AH[k], AL[k], CH[k], CL[k]);
+                const int q = lsx_pad(k);
+                d[q] = residual(dn[q], x0[k], xm, xp, AH[k], AL[k], CH[k], CL[k]);
             }
             __syncthreads();
         }
