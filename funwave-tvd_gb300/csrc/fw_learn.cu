@@ -4,13 +4,21 @@
 // backward, Adam) and its application to a running coarse context.
 //
 // Layout: activations channels-last (pixel-major, the channels of a pixel
-// contiguous), pixel p = x + y*W + b*W*H with x the grid's I (cross-shore)
-// direction.  Weights and activations are BF16 (weights rounded from an
-// FP32 master copy before each use), every sum accumulates in FP32, the
-// gradients and the Adam moments are FP32.  Zero padding at the grid edge.
+// contiguous, natural order), pixel p = x + y*W + b*W*H with x the grid's I
+// (cross-shore) direction.  Weights and activations are BF16 (weights
+// rounded from an FP32 master copy into packed images before use), every
+// sum accumulates in FP32, the weight gradients and the Adam moments are
+// FP32.  Zero padding at the grid edge.
 //
-// Layers: 5 (stored as 8) -> 32 ReLU -> 32 ReLU -> 32 ReLU -> 3.  Weight
-// index [k][ci][co] with k = (ky+1)*3 + (kx+1) for the tap at (x+kx, y+ky).
+// Layers: 5 (stored as 16 channels, weights for 8) -> 32 ReLU -> 32 ReLU
+// -> 32 ReLU -> 3.  Weight index [k][ci][co] with k = (ky+1)*3 + (kx+1) for
+// the tap at (x+kx, y+ky).
+//
+// The forward convolutions and the data gradients of the backward pass run
+// on the tcgen05 tensor cores (fw_tc.cuh).  The backward pass carries the
+// gradient of each hidden activation in BF16 with the ReLU mask already
+// applied (dy * [act > 0]), as the tensor-core data-gradient kernel writes
+// it; the weight gradients reduce those BF16 values in FP32.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -21,11 +29,14 @@
 #include <vector>
 
 #include "fw_internal.h"
+#include "fw_tc.cuh"
 
 namespace {
 
 constexpr int NL = 4;
-constexpr int CIN0 = 8;      // 5 input channels padded to 8
+constexpr int CIN0 = 8;      // 5 input channels padded to 8 (weights)
+constexpr int XC0 = 16;      // channels of the stored input (one K step of the tensor cores)
+constexpr int GC3 = 16;      // channels of the stored output gradient (3 used)
 constexpr int NIN = 5;
 constexpr int HID = 32;
 constexpr int NOUT = 3;
@@ -37,233 +48,24 @@ typedef __nv_bfloat16 bf16;
 
 __device__ __forceinline__ float bf(bf16 v) { return __bfloat162float(v); }
 
-// Hidden activations (32 channels) are stored with their channel pairs
-// permuted: pair P = c/2 sits at word (P % 4) * 4 + P / 4 of the pixel, so
-// that the four words a tensor-core lane needs for one tap (pairs t, 4+t,
-// 8+t, 12+t) are one 16-byte load and its outputs one 16-byte store.  The
-// 8-channel input is stored in natural order.
-template <int C> __device__ __forceinline__ int sidx(int c) {
-    if constexpr (C == 32) {
-        const int P = c >> 1;
-        return (((P & 3) << 2) + (P >> 2)) * 2 + (c & 1);
-    } else {
-        return c;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// forward of the 32-input-channel layers on the tensor cores: implicit GEMM
-// with M = pixels (16 per warp tile, consecutive in memory), N = output
-// channels (NT tiles of 8), K = 9 taps x 32 channels (18 steps of 16),
-// mma.sync m16n8k16 BF16 x BF16 -> FP32.  Each lane loads its A rows (two
-// pixels' channel pairs, zero outside the grid) straight from the
-// channels-last activations; the weights sit in shared memory as BF16
-// pairs [tap][co][ci/2], rows padded to 20 words (conflict-free).
-// ---------------------------------------------------------------------------
+// BF16 of a float, round to nearest even
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     const uint32_t l = __bfloat16_as_ushort(__float2bfloat16(lo));
     const uint32_t h = __bfloat16_as_ushort(__float2bfloat16(hi));
     return l | (h << 16);
 }
 
-__device__ __forceinline__ void mma_bf16(float *c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
-                                         uint32_t b1) {
-    asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// epilogue of a warp tile: bias, ReLU, then the permuted BF16 layout (one
-// 16-byte store per pixel and lane when COUT = 32) or natural FP32
-template <int NT, int COUT, bool RELU, bool OUT_BF16>
-__device__ __forceinline__ void store_tile(float (&acc)[NT][4], const float *bs, void *y, long long pa, long long pb,
-                                           bool ina, bool inb, int t) {
-    uint32_t wa[NT], wb[NT];
-#pragma unroll
-    for (int nt = 0; nt < NT; nt++) {
-        const int c = nt * 8 + 2 * t;
-        float v[4] = {acc[nt][0] + bs[c], acc[nt][1] + bs[c + 1], acc[nt][2] + bs[c], acc[nt][3] + bs[c + 1]};
-        if (RELU)
-#pragma unroll
-            for (int q = 0; q < 4; q++) v[q] = v[q] > 0.0f ? v[q] : 0.0f;
-        if (OUT_BF16) {
-            wa[nt] = pack_bf16(v[0], v[1]);
-            wb[nt] = pack_bf16(v[2], v[3]);
-        } else {
-            float *yf = reinterpret_cast<float *>(y);
-            if (ina && c < COUT) yf[pa * COUT + c] = v[0];
-            if (ina && c + 1 < COUT) yf[pa * COUT + c + 1] = v[1];
-            if (inb && c < COUT) yf[pb * COUT + c] = v[2];
-            if (inb && c + 1 < COUT) yf[pb * COUT + c + 1] = v[3];
-        }
-    }
-    if constexpr (OUT_BF16) {
-        static_assert(COUT == 32 && NT == 4, "BF16 outputs are the 32-channel permuted layout");
-        uint32_t *yw = reinterpret_cast<uint32_t *>(y);
-        // pair nt*4 + t sits at word t*4 + nt
-        if (ina) *reinterpret_cast<uint4 *>(yw + pa * 16 + 4 * t) = make_uint4(wa[0], wa[1], wa[2], wa[3]);
-        if (inb) *reinterpret_cast<uint4 *>(yw + pb * 16 + 4 * t) = make_uint4(wb[0], wb[1], wb[2], wb[3]);
-    }
-}
-
-// the first layer (8 natural input channels) on the tensor cores: a K step
-// of 16 holds two taps (8 channels each), five steps cover the 9 taps plus
-// one zero tap
-__global__ void __launch_bounds__(128) k_conv8_fwd_mma(const bf16 *__restrict__ x, const float *__restrict__ w,
-                                                       const float *__restrict__ bias, bf16 *y, int B, int H, int W) {
-    constexpr int CIN = 8, COUT = 32, WS = 12;
-    __shared__ uint32_t wT[5][COUT][WS];  // [k step][co][words: 4 of tap 2s, 4 of tap 2s+1]
-    __shared__ float bs[COUT];
-    for (int e = threadIdx.x; e < 5 * COUT * 8; e += blockDim.x) {
-        const int wd = e % 8, co = (e / 8) % COUT, ks = e / (8 * COUT);
-        const int tap = 2 * ks + (wd >> 2), cp = wd & 3;
-        float lo = 0.0f, hi = 0.0f;
-        if (tap < 9) {
-            lo = w[((size_t)tap * CIN + 2 * cp) * COUT + co];
-            hi = w[((size_t)tap * CIN + 2 * cp + 1) * COUT + co];
-        }
-        wT[ks][co][wd] = pack_bf16(lo, hi);
-    }
-    for (int e = threadIdx.x; e < COUT; e += blockDim.x) bs[e] = bias[e];
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = lane >> 2, t = lane & 3;
-    const long long npix = (long long)B * H * W;
-    const long long ntile = (npix + 15) / 16;
-    const uint32_t *xw = reinterpret_cast<const uint32_t *>(x);  // 4 words per pixel
-    for (long long tile = (long long)blockIdx.x * 4 + warp; tile < ntile; tile += (long long)gridDim.x * 4) {
-        const long long pa = tile * 16 + g, pb = pa + 8;
-        const bool ina = pa < npix, inb = pb < npix;
-        const int xa = (int)(pa % W), ya = (int)((pa / W) % H);
-        const int xb = (int)(pb % W), yb = (int)((pb / W) % H);
-        float acc[4][4];
-#pragma unroll
-        for (int nt = 0; nt < 4; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-#pragma unroll
-        for (int ks = 0; ks < 5; ks++) {
-            uint32_t a[4];
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int tap = 2 * ks + h;
-                const int kx = tap % 3 - 1, ky = tap / 3 - 1;
-                const bool va = tap < 9 && ina && xa + kx >= 0 && xa + kx < W && ya + ky >= 0 && ya + ky < H;
-                const bool vb = tap < 9 && inb && xb + kx >= 0 && xb + kx < W && yb + ky >= 0 && yb + ky < H;
-                a[2 * h] = va ? xw[(pa + (long long)ky * W + kx) * 4 + t] : 0u;
-                a[2 * h + 1] = vb ? xw[(pb + (long long)ky * W + kx) * 4 + t] : 0u;
-            }
-#pragma unroll
-            for (int nt = 0; nt < 4; nt++)
-                mma_bf16(acc[nt], a[0], a[1], a[2], a[3], wT[ks][nt * 8 + g][t], wT[ks][nt * 8 + g][4 + t]);
-        }
-        store_tile<4, COUT, true, true>(acc, bs, y, pa, pb, ina, inb, t);
-    }
-}
-
-template <int NT, int COUT, bool RELU, bool OUT_BF16>
-__global__ void __launch_bounds__(128) k_conv32_fwd_mma(const bf16 *__restrict__ x, const float *__restrict__ w,
-                                                        const float *__restrict__ bias, void *y, int B, int H,
-                                                        int W) {
-    constexpr int CIN = 32, WS = 20;
-    __shared__ uint32_t wT[9][NT * 8][WS];
-    __shared__ float bs[NT * 8];
-    for (int e = threadIdx.x; e < 9 * NT * 8 * 16; e += blockDim.x) {
-        const int cp = e % 16, co = (e / 16) % (NT * 8), tap = e / (16 * NT * 8);
-        float lo = 0.0f, hi = 0.0f;
-        if (co < COUT) {
-            lo = w[((size_t)tap * CIN + 2 * cp) * COUT + co];
-            hi = w[((size_t)tap * CIN + 2 * cp + 1) * COUT + co];
-        }
-        wT[tap][co][cp] = pack_bf16(lo, hi);
-    }
-    for (int e = threadIdx.x; e < NT * 8; e += blockDim.x) bs[e] = e < COUT ? bias[e] : 0.0f;
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = lane >> 2, t = lane & 3;
-    const long long npix = (long long)B * H * W;
-    const long long ntile = (npix + 15) / 16;
-    const uint32_t *xw = reinterpret_cast<const uint32_t *>(x);  // 16 words per pixel
-    for (long long tile = (long long)blockIdx.x * 4 + warp; tile < ntile; tile += (long long)gridDim.x * 4) {
-        const long long pa = tile * 16 + g, pb = pa + 8;
-        const bool ina = pa < npix, inb = pb < npix;
-        const int xa = (int)(pa % W), ya = (int)((pa / W) % H);
-        const int xb = (int)(pb % W), yb = (int)((pb / W) % H);
-        float acc[NT][4];
-#pragma unroll
-        for (int nt = 0; nt < NT; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-#pragma unroll
-        for (int tap = 0; tap < 9; tap++) {
-            const int kx = tap % 3 - 1, ky = tap / 3 - 1;
-            const bool va = ina && xa + kx >= 0 && xa + kx < W && ya + ky >= 0 && ya + ky < H;
-            const bool vb = inb && xb + kx >= 0 && xb + kx < W && yb + ky >= 0 && yb + ky < H;
-            // words 4t..4t+3 of the permuted pixel: pairs t, 4+t, 8+t, 12+t
-            const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
-            const uint4 qa = va ? *reinterpret_cast<const uint4 *>(xw + (pa + (long long)ky * W + kx) * 16 + 4 * t) : z4;
-            const uint4 qb = vb ? *reinterpret_cast<const uint4 *>(xw + (pb + (long long)ky * W + kx) * 16 + 4 * t) : z4;
-#pragma unroll
-            for (int ks = 0; ks < 2; ks++) {
-                const uint32_t a0 = ks == 0 ? qa.x : qa.z, a2 = ks == 0 ? qa.y : qa.w;
-                const uint32_t a1 = ks == 0 ? qb.x : qb.z, a3 = ks == 0 ? qb.y : qb.w;
-#pragma unroll
-                for (int nt = 0; nt < NT; nt++) {
-                    const uint32_t b0 = wT[tap][nt * 8 + g][ks * 8 + t];
-                    const uint32_t b1 = wT[tap][nt * 8 + g][ks * 8 + 4 + t];
-                    mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
-                }
-            }
-        }
-        store_tile<NT, COUT, RELU, OUT_BF16>(acc, bs, y, pa, pb, ina, inb, t);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// backward: dy of a layer's output (FP32) -> dx of its input (FP32), with the
-// layer's ReLU applied to dy first (y = the layer's stored output)
-// ---------------------------------------------------------------------------
-template <int CIN, int COUT, bool RELU>
-__global__ void __launch_bounds__(128) k_conv_dgrad(const float *__restrict__ dy, const bf16 *__restrict__ y,
-                                                    const float *__restrict__ w, float *__restrict__ dx, int B,
-                                                    int H, int W) {
-    __shared__ float ws[9 * CIN * COUT];
-    for (int e = threadIdx.x; e < 9 * CIN * COUT; e += blockDim.x) ws[e] = bf(__float2bfloat16(w[e]));
-    __syncthreads();
-    const long long npix = (long long)B * H * W;
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npix) return;
-    const int px = (int)(p % W), py = (int)((p / W) % H);
-    float acc[CIN];
-#pragma unroll
-    for (int ci = 0; ci < CIN; ci++) acc[ci] = 0.0f;
-    // output q = p - (kx, ky) read this input through tap k
-    for (int ky = -1; ky <= 1; ky++) {
-        if (py - ky < 0 || py - ky >= H) continue;
-        for (int kx = -1; kx <= 1; kx++) {
-            if (px - kx < 0 || px - kx >= W) continue;
-            const long long q = p - (long long)ky * W - kx;
-            const float *wk = ws + ((ky + 1) * 3 + (kx + 1)) * CIN * COUT;
-            for (int co = 0; co < COUT; co++) {
-                float g = dy[q * COUT + co];
-                if (RELU && !(bf(y[q * COUT + sidx<COUT>(co)]) > 0.0f)) g = 0.0f;
-#pragma unroll
-                for (int ci = 0; ci < CIN; ci++) acc[ci] += wk[ci * COUT + co] * g;
-            }
-        }
-    }
-#pragma unroll
-    for (int ci = 0; ci < CIN; ci++) dx[p * CIN + ci] = acc[ci];
-}
-
 // weight and bias gradients.  A tile is a row segment of TPX pixels; its
 // three input rows (with one pixel of halo on each side, zero outside the
-// grid) and its dy (with this layer's ReLU applied) are staged in shared
-// memory, then every thread adds its share of the 9*CIN*COUT + COUT
-// entries over the tile.  Each of the WG_BLOCKS blocks walks many tiles and
-// writes one partial; k_wgrad_reduce adds the partials.
+// grid) and its masked BF16 dy are staged in shared memory, then every
+// thread adds its share of the 9*CIN*COUT + COUT entries over the tile.
+// Each of the WG_BLOCKS blocks walks many tiles and writes one partial;
+// k_wgrad_reduce adds the partials.  x has XC channels a pixel (the first
+// CIN used), dy DYC (the first COUT used).
 constexpr int TPX = 64;
-template <int CIN, int COUT, bool RELU>
-__global__ void __launch_bounds__(256) k_conv_wgrad(const bf16 *__restrict__ x, const float *__restrict__ dy,
-                                                    const bf16 *__restrict__ y, float *__restrict__ part, int B,
-                                                    int H, int W) {
+template <int CIN, int COUT, int XC, int DYC>
+__global__ void __launch_bounds__(256) k_conv_wgrad(const bf16 *__restrict__ x, const bf16 *__restrict__ dy,
+                                                    float *__restrict__ part, int B, int H, int W) {
     constexpr int E = 9 * CIN * COUT + COUT;
     constexpr int NE = (E + 255) / 256;
     __shared__ float xs[3][TPX + 2][CIN];
@@ -283,19 +85,12 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(const bf16 *__restrict__ x, 
             const int ci = e % CIN, c = (e / CIN) % (TPX + 2), r = e / (CIN * (TPX + 2));
             const int gx = x0 + c - 1, gy = py + r - 1;
             float v = 0.0f;
-            if (gx >= 0 && gx < W && gy >= 0 && gy < H)
-                v = bf(x[((row + (r - 1)) * W + gx) * CIN + sidx<CIN>(ci)]);
+            if (gx >= 0 && gx < W && gy >= 0 && gy < H) v = bf(x[((row + (r - 1)) * W + gx) * XC + ci]);
             xs[r][c][ci] = v;
         }
         for (int e = threadIdx.x; e < TPX * COUT; e += blockDim.x) {
             const int co = e % COUT, t = e / COUT;
-            float g = 0.0f;
-            if (x0 + t < W) {
-                const long long q = (row * W + x0 + t) * COUT;
-                g = dy[q + co];
-                if (RELU && !(bf(y[q + sidx<COUT>(co)]) > 0.0f)) g = 0.0f;
-            }
-            dys[t][co] = g;
+            dys[t][co] = x0 + t < W ? bf(dy[(row * W + x0 + t) * DYC + co]) : 0.0f;
         }
         __syncthreads();
 #pragma unroll
@@ -330,26 +125,35 @@ __global__ void k_wgrad_reduce(const float *part, int nblocks, int E, float *gw,
     else gb[e - nw] = s;
 }
 
-// inputs: FP32 [npix][5] -> BF16 [npix][8] (three zero channels)
+// inputs: FP32 [npix][5] -> BF16 [npix][16] (eleven zero channels)
 __global__ void k_pack_input(const float *in, bf16 *x, long long npix) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npix) return;
+    float v[NIN];
 #pragma unroll
-    for (int c = 0; c < CIN0; c++) x[p * CIN0 + c] = __float2bfloat16(c < NIN ? in[p * NIN + c] : 0.0f);
+    for (int c = 0; c < NIN; c++) v[c] = in[p * NIN + c];
+    uint4 *xq = reinterpret_cast<uint4 *>(x + p * XC0);
+    xq[0] = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], 0.0f), 0u);
+    xq[1] = make_uint4(0u, 0u, 0u, 0u);
 }
 
-// masked mean squared error and its gradient w.r.t. the output
+// masked mean squared error and its gradient w.r.t. the output, stored as
+// BF16 [npix][16] (channels 3..15 zero)
 __global__ void k_loss(const float *out, const float *target, const float *wmask, long long npix, float inv_n,
-                       float *dy, double *loss) {
+                       bf16 *dy, double *loss) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     float l = 0.0f;
     if (p < npix) {
         const float m = wmask[p];
+        float g[NOUT];
         for (int c = 0; c < NOUT; c++) {
             const float d = out[p * NOUT + c] - target[p * NOUT + c];
             l += m * d * d;
-            dy[p * NOUT + c] = 2.0f * m * d * inv_n;
+            g[c] = 2.0f * m * d * inv_n;
         }
+        uint4 *dq = reinterpret_cast<uint4 *>(dy + p * GC3);
+        dq[0] = make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], 0.0f), 0u, 0u);
+        dq[1] = make_uint4(0u, 0u, 0u, 0u);
     }
     for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, (double)(l * inv_n));
@@ -456,11 +260,19 @@ struct fw_net {
     size_t woff[NL], boff[NL], nparam = 0;
     float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;  // FP32 master, grads, Adam moments
     long long adam_t = 0;
+    // packed BF16 weight images of the tensor-core convolutions: the four
+    // forward layers, then the data gradients of layers 1..3; rebuilt when
+    // the master weights change (wver != img_ver)
+    bf16 *img = nullptr;
+    size_t img_off[NL + 3] = {0};
+    unsigned long long wver = 1, img_ver = 0;
+    int *status = nullptr;      // set by a tensor-core kernel whose bounded wait expired
     // workspace for npix_cap pixels
     long long npix_cap = 0;
-    bf16 *act[NL] = {nullptr};  // act[0] = packed input, act[l] = output of layer l-1 (l = 1..3)
+    bf16 *act[NL] = {nullptr};  // act[0] = packed input [16 ch], act[l] = output of layer l-1 (l = 1..3)
     float *out = nullptr;       // output of the last layer, FP32 [npix][3]
-    float *dbuf[2] = {nullptr, nullptr};
+    bf16 *gout = nullptr;       // gradient of the output, BF16 [npix][16]
+    bf16 *gbuf[2] = {nullptr, nullptr};  // masked gradients of hidden activations, BF16 [npix][32]
     float *part = nullptr;
     double *loss = nullptr;
     float *corr_in = nullptr;   // fw_correct's input tensor
@@ -468,29 +280,37 @@ struct fw_net {
 
 namespace {
 
+// the images: {cin chunks, N} of each
+constexpr int IMG_CINC[NL + 3] = {2, 4, 4, 4, 4, 4, 2};
+constexpr int IMG_N[NL + 3] = {32, 32, 32, 16, 32, 32, 32};
+
+size_t img_elems(int i) { return (size_t)9 * IMG_CINC[i] * IMG_N[i] * 8; }
+
 void free_ws(fw_net *n) {
     for (auto &a : n->act) {
         if (a) cudaFree(a);
         a = nullptr;
     }
-    for (auto &b : n->dbuf) {
+    for (auto &b : n->gbuf) {
         if (b) cudaFree(b);
         b = nullptr;
     }
-    if (n->out) cudaFree(n->out);
-    if (n->corr_in) cudaFree(n->corr_in);
+    for (void *p : {(void *)n->out, (void *)n->corr_in, (void *)n->gout})
+        if (p) cudaFree(p);
     n->out = nullptr;
     n->corr_in = nullptr;
+    n->gout = nullptr;
     n->npix_cap = 0;
 }
 
 int ensure_ws(fw_net *n, long long npix) {
     if (npix <= n->npix_cap) return FW_OK;
     free_ws(n);
-    bool ok = cudaMalloc(&n->act[0], (size_t)npix * CIN0 * sizeof(bf16)) == cudaSuccess;
+    bool ok = cudaMalloc(&n->act[0], (size_t)npix * XC0 * sizeof(bf16)) == cudaSuccess;
     for (int l = 1; l < NL && ok; l++) ok = cudaMalloc(&n->act[l], (size_t)npix * HID * sizeof(bf16)) == cudaSuccess;
     ok = ok && cudaMalloc(&n->out, (size_t)npix * NOUT * sizeof(float)) == cudaSuccess;
-    for (int k = 0; k < 2 && ok; k++) ok = cudaMalloc(&n->dbuf[k], (size_t)npix * HID * sizeof(float)) == cudaSuccess;
+    ok = ok && cudaMalloc(&n->gout, (size_t)npix * GC3 * sizeof(bf16)) == cudaSuccess;
+    for (int k = 0; k < 2 && ok; k++) ok = cudaMalloc(&n->gbuf[k], (size_t)npix * HID * sizeof(bf16)) == cudaSuccess;
     ok = ok && cudaMalloc(&n->corr_in, (size_t)npix * NIN * sizeof(float)) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -503,44 +323,123 @@ int ensure_ws(fw_net *n, long long npix) {
 
 unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-void forward(fw_net *n, const float *in, long long npix, int B, int H, int W, cudaStream_t s) {
-    k_pack_input<<<nblk(npix, 256), 256, 0, s>>>(in, n->act[0], npix);
-    // every layer on the tensor cores: a persistent grid of warps over
-    // 16-pixel tiles
-    const long long ntile = (npix + 15) / 16;
-    const unsigned gm = (unsigned)std::min<long long>((ntile + 3) / 4, 152LL * 16);
-    k_conv8_fwd_mma<<<gm, 128, 0, s>>>(n->act[0], n->w + n->woff[0], n->w + n->boff[0], n->act[1], B, H, W);
-    k_conv32_fwd_mma<4, HID, true, true><<<gm, 128, 0, s>>>(n->act[1], n->w + n->woff[1], n->w + n->boff[1],
-                                                             n->act[2], B, H, W);
-    k_conv32_fwd_mma<4, HID, true, true><<<gm, 128, 0, s>>>(n->act[2], n->w + n->woff[2], n->w + n->boff[2],
-                                                             n->act[3], B, H, W);
-    k_conv32_fwd_mma<1, NOUT, false, false><<<gm, 128, 0, s>>>(n->act[3], n->w + n->woff[3], n->w + n->boff[3],
-                                                                n->out, B, H, W);
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// link against the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
 }
 
-template <int CIN, int COUT, bool RELU>
-void wgrad(fw_net *n, int l, const bf16 *x, const float *dy, const bf16 *y, long long npix, int B, int H, int W,
-           cudaStream_t s) {
+// tensor map of a BF16 activation [B][H][W][C]: boxes of 8 channels x 130
+// pixels x (TROWS + 2) rows of one image, zero outside the image
+bool act_map(CUtensorMap *m, const bf16 *base, int C, int B, int H, int W) {
+    EncodeTiledFn f = encode_fn();
+    if (!f) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)fwtc::HPX, (cuuint32_t)(fwtc::TROWS + 2), 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    return f(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(base), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int CINC, int N, int EPI, int NOUTF>
+int conv_tc(const bf16 *x, int C, const bf16 *img, const float *bias, const bf16 *act, void *y, int B, int H, int W,
+            int *status, cudaStream_t s) {
+    using Lt = fwtc::Layout<CINC, N>;
+    auto k = fwtc::k_conv_tc<CINC, N, EPI, NOUTF>;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, Lt::BYTES) != cudaSuccess) {
+            cudaGetLastError();
+            return FW_ERR_CUDA;
+        }
+        attr = true;
+    }
+    CUtensorMap m;
+    if (!act_map(&m, x, C, B, H, W)) return FW_ERR_CUDA;
+    const dim3 grid((unsigned)((W + fwtc::TPX - 1) / fwtc::TPX), (unsigned)((H + fwtc::TROWS - 1) / fwtc::TROWS),
+                    (unsigned)B);
+    k<<<grid, 128, Lt::BYTES, s>>>(m, img, bias, act, y, H, W, status);
+    return FW_OK;
+}
+
+// the grid of the tensor-core kernels: H / TROWS blocks in y, B in z
+bool shape_ok(int B, int H, int W) {
+    return B > 0 && H > 0 && W > 0 && B <= 65535 && (H + fwtc::TROWS - 1) / fwtc::TROWS <= 65535;
+}
+
+void pack_images(fw_net *n, cudaStream_t s) {
+    if (n->img_ver == n->wver) return;
+    for (int i = 0; i < NL + 3; i++) {
+        const int l = i < NL ? i : i - NL + 1;  // images 4..6 are the data gradients of layers 1..3
+        const int tot = (int)img_elems(i);
+        fwtc::k_pack_wimg<<<nblk(tot, 256), 256, 0, s>>>(n->w + n->woff[l], LCIN[l], LCOUT[l], IMG_CINC[i], IMG_N[i],
+                                                         i >= NL ? 1 : 0, n->img + n->img_off[i]);
+    }
+    n->img_ver = n->wver;
+}
+
+int forward(fw_net *n, const float *in, long long npix, int B, int H, int W, cudaStream_t s) {
+    using namespace fwtc;
+    pack_images(n, s);
+    k_pack_input<<<nblk(npix, 256), 256, 0, s>>>(in, n->act[0], npix);
+    const bf16 *im = n->img;
+    int rc = conv_tc<2, 32, EPI_RELU_BF16, 0>(n->act[0], XC0, im + n->img_off[0], n->w + n->boff[0], nullptr,
+                                              n->act[1], B, H, W, n->status, s);
+    for (int l = 1; l < 3 && rc == FW_OK; l++)
+        rc = conv_tc<4, 32, EPI_RELU_BF16, 0>(n->act[l], HID, im + n->img_off[l], n->w + n->boff[l], nullptr,
+                                              n->act[l + 1], B, H, W, n->status, s);
+    if (rc == FW_OK)
+        rc = conv_tc<4, 16, EPI_LINEAR_F32, NOUT>(n->act[3], HID, im + n->img_off[3], n->w + n->boff[3], nullptr,
+                                                  n->out, B, H, W, n->status, s);
+    return rc;
+}
+
+template <int CIN, int COUT, int XC, int DYC>
+void wgrad(fw_net *n, int l, const bf16 *x, const bf16 *dy, int B, int H, int W, cudaStream_t s) {
     constexpr int E = 9 * CIN * COUT + COUT;
-    k_conv_wgrad<CIN, COUT, RELU><<<WG_BLOCKS, 256, 0, s>>>(x, dy, y, n->part, B, H, W);
+    k_conv_wgrad<CIN, COUT, XC, DYC><<<WG_BLOCKS, 256, 0, s>>>(x, dy, n->part, B, H, W);
     k_wgrad_reduce<<<nblk(E, 256), 256, 0, s>>>(n->part, WG_BLOCKS, E, n->g + n->woff[l], n->g + n->boff[l],
                                                  9 * CIN * COUT);
 }
 
-void backward(fw_net *n, long long npix, int B, int H, int W, cudaStream_t s) {
-    const unsigned gb = nblk(npix, 128);
-    float *dy = n->dbuf[0], *dx = n->dbuf[1];
-    // dy of the last layer is in dbuf[0] ([npix][3])
-    wgrad<HID, NOUT, false>(n, 3, n->act[3], dy, nullptr, npix, B, H, W, s);
-    k_conv_dgrad<HID, NOUT, false><<<gb, 128, 0, s>>>(dy, nullptr, n->w + n->woff[3], dx, B, H, W);
-    for (int l = 2; l >= 1; l--) {
-        std::swap(dy, dx);  // dy: gradient of act[l+1]
-        wgrad<HID, HID, true>(n, l, n->act[l], dy, n->act[l + 1], npix, B, H, W, s);
-        k_conv_dgrad<HID, HID, true><<<gb, 128, 0, s>>>(dy, n->act[l + 1], n->w + n->woff[l], dx, B, H, W);
+// the output gradient is in gout; the images are current (forward ran)
+int backward(fw_net *n, int B, int H, int W, cudaStream_t s) {
+    using namespace fwtc;
+    const bf16 *im = n->img;
+    bf16 *ga = n->gbuf[0], *gb = n->gbuf[1];
+    wgrad<HID, NOUT, HID, GC3>(n, 3, n->act[3], n->gout, B, H, W, s);
+    // gradient of act[3] (the output of layer 2), masked by its ReLU
+    int rc = conv_tc<2, 32, EPI_MASK_BF16, 0>(n->gout, GC3, im + n->img_off[NL + 2], nullptr, n->act[3], ga, B, H, W,
+                                              n->status, s);
+    for (int l = 2; l >= 1 && rc == FW_OK; l--) {
+        wgrad<HID, HID, HID, HID>(n, l, n->act[l], ga, B, H, W, s);
+        rc = conv_tc<4, 32, EPI_MASK_BF16, 0>(ga, HID, im + n->img_off[NL + l - 1], nullptr, n->act[l], gb, B, H, W,
+                                              n->status, s);
+        std::swap(ga, gb);
     }
-    std::swap(dy, dx);  // gradient of act[1]
-    wgrad<CIN0, HID, true>(n, 0, n->act[0], dy, n->act[1], npix, B, H, W, s);
+    if (rc != FW_OK) return rc;
+    wgrad<CIN0, HID, XC0, HID>(n, 0, n->act[0], ga, B, H, W, s);
     k_zero_pad_grad<<<nblk(9 * CIN0 * HID, 256), 256, 0, s>>>(n->g + n->woff[0]);
+    return FW_OK;
 }
 
 }  // namespace
@@ -554,8 +453,10 @@ template <typename T> int correct(fw_ctx *c, fw_net *n, double max_corr, int *ap
     if (rc != FW_OK) return rc;
     cudaStream_t s = c->stream;
     const dim3 b(32, 8), gr((g.Mglob + 31) / 32, (g.Nglob + 7) / 8);
+    if (!shape_ok(1, g.Nglob, g.Mglob)) return FW_ERR_BAD_PARAM;
     k_corr_input<T><<<gr, b, 0, s>>>(g, f, n->corr_in);
-    forward(n, n->corr_in, npix, 1, g.Nglob, g.Mglob, s);
+    rc = forward(n, n->corr_in, npix, 1, g.Nglob, g.Mglob, s);
+    if (rc != FW_OK) return rc;
     double *sums = n->loss;  // 3 doubles of scratch after the loss slot
     cudaMemsetAsync(sums, 0, 4 * sizeof(double), s);
     k_corr_sums<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1);
@@ -563,8 +464,10 @@ template <typename T> int correct(fw_ctx *c, fw_net *n, double max_corr, int *ap
     if (applied) {
         // only a caller that asks waits for the decision
         double h[4];
+        int st = 0;
         cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) return FW_ERR_CUDA;
+        cudaMemcpyAsync(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess || st != 0) return FW_ERR_CUDA;
         *applied = (h[3] <= max_corr && h[2] == h[2]) ? 1 : 0;
     }
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
@@ -611,7 +514,15 @@ int fw_net_create(unsigned long long seed, fw_net **out) {
     bool ok = cudaMalloc(&n->w, off * sizeof(float)) == cudaSuccess && cudaMalloc(&n->g, off * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&n->m, off * sizeof(float)) == cudaSuccess && cudaMalloc(&n->v, off * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&n->part, (size_t)WG_BLOCKS * (9 * HID * HID + HID) * sizeof(float)) == cudaSuccess &&
-              cudaMalloc(&n->loss, 4 * sizeof(double)) == cudaSuccess;
+              cudaMalloc(&n->loss, 4 * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&n->status, sizeof(int)) == cudaSuccess;
+    size_t ioff = 0;
+    for (int i = 0; i < NL + 3; i++) {
+        n->img_off[i] = ioff;
+        ioff += img_elems(i);
+    }
+    ok = ok && cudaMalloc(&n->img, ioff * sizeof(bf16)) == cudaSuccess;
+    ok = ok && cudaMemset(n->status, 0, sizeof(int)) == cudaSuccess;
     ok = ok && cudaMemcpy(n->w, h.data(), off * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
     ok = ok && cudaMemset(n->g, 0, off * sizeof(float)) == cudaSuccess && cudaMemset(n->m, 0, off * sizeof(float)) == cudaSuccess &&
          cudaMemset(n->v, 0, off * sizeof(float)) == cudaSuccess;
@@ -631,6 +542,8 @@ int fw_net_destroy(fw_net *n) {
     for (float *p : {n->w, n->g, n->m, n->v, n->part})
         if (p) cudaFree(p);
     if (n->loss) cudaFree(n->loss);
+    if (n->img) cudaFree(n->img);
+    if (n->status) cudaFree(n->status);
     delete n;
     return FW_OK;
 }
@@ -644,6 +557,7 @@ int fw_net_get_params(fw_net *n, float *host) {
 
 int fw_net_set_params(fw_net *n, const float *host) {
     if (!n || !host) return FW_ERR_BAD_PARAM;
+    n->wver++;
     return cudaMemcpy(n->w, host, n->nparam * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess ? FW_OK : FW_ERR_CUDA;
 }
 
@@ -653,30 +567,35 @@ int fw_net_get_grads(fw_net *n, float *host) {
 }
 
 int fw_net_forward(fw_net *n, const float *x, int B, int H, int W, float *y, void *stream) {
-    if (!n || !x || !y || B <= 0 || H <= 0 || W <= 0) return FW_ERR_BAD_PARAM;
+    if (!n || !x || !y || !shape_ok(B, H, W)) return FW_ERR_BAD_PARAM;
     const long long npix = (long long)B * H * W;
     int rc = ensure_ws(n, npix);
     if (rc != FW_OK) return rc;
     cudaStream_t s = (cudaStream_t)stream;
-    forward(n, x, npix, B, H, W, s);
+    rc = forward(n, x, npix, B, H, W, s);
+    if (rc != FW_OK) return rc;
     cudaMemcpyAsync(y, n->out, (size_t)npix * NOUT * sizeof(float), cudaMemcpyDeviceToDevice, s);
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
 }
 
 int fw_net_loss_grad(fw_net *n, const float *x, const float *target, const float *wmask, int B, int H, int W,
                      double *loss, void *stream) {
-    if (!n || !x || !target || !wmask || B <= 0 || H <= 0 || W <= 0) return FW_ERR_BAD_PARAM;
+    if (!n || !x || !target || !wmask || !shape_ok(B, H, W)) return FW_ERR_BAD_PARAM;
     const long long npix = (long long)B * H * W;
     int rc = ensure_ws(n, npix);
     if (rc != FW_OK) return rc;
     cudaStream_t s = (cudaStream_t)stream;
-    forward(n, x, npix, B, H, W, s);
+    rc = forward(n, x, npix, B, H, W, s);
+    if (rc != FW_OK) return rc;
     cudaMemsetAsync(n->loss, 0, sizeof(double), s);
-    k_loss<<<nblk(npix, 256), 256, 0, s>>>(n->out, target, wmask, npix, 1.0f / (float)npix, n->dbuf[0], n->loss);
-    backward(n, npix, B, H, W, s);
+    k_loss<<<nblk(npix, 256), 256, 0, s>>>(n->out, target, wmask, npix, 1.0f / (float)npix, n->gout, n->loss);
+    rc = backward(n, B, H, W, s);
+    if (rc != FW_OK) return rc;
     if (loss) {
+        int st = 0;
         cudaMemcpyAsync(loss, n->loss, sizeof(double), cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
+        cudaMemcpyAsync(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess || st != 0) return FW_ERR_CUDA;
     }
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
 }
@@ -684,6 +603,7 @@ int fw_net_loss_grad(fw_net *n, const float *x, const float *target, const float
 int fw_net_adam(fw_net *n, float lr, float beta1, float beta2, float eps, void *stream) {
     if (!n || !(lr > 0.0f)) return FW_ERR_BAD_PARAM;
     n->adam_t++;
+    n->wver++;
     const float c1 = 1.0f - std::pow(beta1, (float)n->adam_t), c2 = 1.0f - std::pow(beta2, (float)n->adam_t);
     k_adam<<<nblk((long long)n->nparam, 256), 256, 0, (cudaStream_t)stream>>>(n->w, n->g, n->m, n->v,
                                                                               (long long)n->nparam, lr, beta1,

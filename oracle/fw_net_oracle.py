@@ -9,10 +9,12 @@ parameter layout as funwave-tvd_gb300/csrc/fw_learn.cu:
 with weights w[9][cin][cout] (tap k = (ky+1)*3 + (kx+1) reads (x+kx, y+ky)),
 then b[cout], per layer.  With bf16=True the weights, the packed input and
 the hidden activations are rounded to BF16 (round to nearest even) as the
-GPU stores them, and the convolutions accumulate in float32 in the GPU's
-order (bias, then taps, then input channels); the backward pass runs in
-float64 on those stored values.  With bf16=False everything is float64, for
-finite-difference checks.
+GPU stores them, and the convolutions accumulate in float32 (bias, then
+taps, then input channels; the tensor cores add in another order, which the
+tests' tolerances cover).  The backward pass runs in float64 on the stored
+values and rounds, as the GPU stores them, the output gradient and each
+hidden activation's gradient (with its ReLU mask applied) to BF16.  With
+bf16=False everything is float64, for finite-difference checks.
 
 No reference counterpart: the network is an extension of the reference.
 """
@@ -95,6 +97,8 @@ def loss_grad(params, x, target, wmask, bf16=True):
     d = y.astype(np.float64) - target
     loss = float(np.sum(wmask[..., None] * d * d) / n)
     dy = 2.0 * wmask[..., None] * d / n
+    if bf16:
+        dy = bf16_round(dy.astype(np.float32)).astype(np.float64)
     grads = []
     layers = unpack(params)
     for li in range(len(layers) - 1, -1, -1):
@@ -114,6 +118,8 @@ def loss_grad(params, x, target, wmask, bf16=True):
         if li > 0:
             prev_relu = layers[li - 1][2]
             dy = dx * (acts[li] > 0) if prev_relu else dx
+            if bf16:
+                dy = bf16_round(dy.astype(np.float32)).astype(np.float64)
     g = np.concatenate(grads[::-1])
     # the padding input channels carry no gradient
     w0 = g[:9 * 8 * 32].reshape(9, 8, 32)

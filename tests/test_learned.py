@@ -42,6 +42,17 @@ def test_reference_gradients_by_finite_differences():
         assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(fd)), (k, fd, g[k])
 
 
+def _check_forward(y, y_ref):
+    """The tensor cores add in another order than the reference, so a hidden
+    activation now and then rounds to the neighbouring BF16 value; the
+    three layers after it spread that 0.4 % step over a 7 x 7 patch of
+    outputs.  Most outputs agree to float rounding, a few by such a step."""
+    e = np.abs(y - y_ref)
+    scale = float(np.abs(y_ref).max())
+    assert float(e.max()) <= 1e-2 * scale
+    assert float(np.quantile(e, 0.9)) <= 1e-5 * scale
+
+
 @pytest.mark.gpu
 def test_gpu_forward_and_gradients_match_reference(fw):
     import torch
@@ -58,7 +69,39 @@ def test_gpu_forward_and_gradients_match_reference(fw):
     X, T, Wm = (torch.from_numpy(a).to(dev).contiguous() for a in (x, t, w))
     y = net.forward(X).cpu().numpy()
     y_ref, _ = ref.forward(params, x, bf16=True)
-    assert np.abs(y - y_ref).max() <= 1e-3 * np.abs(y_ref).max()
+    _check_forward(y, y_ref)
+    loss = net.loss_grad(X, T, Wm)
+    loss_ref, g_ref = ref.loss_grad(params, x, t, w, bf16=True)
+    assert abs(loss - loss_ref) <= 1e-4 * loss_ref
+    g = net.grads()
+    off = 0
+    for ci, co, _ in ref.LAYERS:
+        n = 9 * ci * co + co
+        a, b = g[off:off + n], g_ref[off:off + n]
+        assert np.linalg.norm(a - b) <= 2e-3 * np.linalg.norm(b), (ci, co, np.linalg.norm(a - b) / np.linalg.norm(b))
+        off += n
+    net.close()
+
+
+@pytest.mark.gpu
+def test_gpu_forward_and_gradients_several_tiles(fw):
+    """Images wider than one 128-pixel tile, with a row count that is not a
+    multiple of the tensor-core kernel's four rows, two to a batch: the
+    tiles' halos, the zero fill at every edge and the partial last tiles."""
+    import torch
+    import fw_net_oracle as ref
+    net = fw.learned.Net(seed=3)
+    params = _rand_params(ref, 6)
+    net.set_params(params)
+    rng = np.random.default_rng(7)
+    x = rng.normal(size=(2, 11, 150, 5)).astype(np.float32)
+    t = rng.normal(size=(2, 11, 150, 3)).astype(np.float32)
+    w = (rng.uniform(size=(2, 11, 150)) > 0.2).astype(np.float32)
+    dev = torch.device("cuda")
+    X, T, Wm = (torch.from_numpy(a).to(dev).contiguous() for a in (x, t, w))
+    y = net.forward(X).cpu().numpy()
+    y_ref, _ = ref.forward(params, x, bf16=True)
+    _check_forward(y, y_ref)
     loss = net.loss_grad(X, T, Wm)
     loss_ref, g_ref = ref.loss_grad(params, x, t, w, bf16=True)
     assert abs(loss - loss_ref) <= 1e-4 * loss_ref
