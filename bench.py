@@ -164,10 +164,13 @@ def max_over_ranks(v, pg):
     return float(t.item())
 
 
-def run_precision(fw, params, depth, phases, precision, K, W, local, pg):
+def run_precision(fw, params, depth, phases, precision, K, W, local, pg, autotune=True):
     import torch
     s = fw.Solver(params, precision=precision, device=local)
     s.init(depth, phases=phases)
+    t0 = time.perf_counter()
+    tuning = s.autotune() if autotune else s.tuning()
+    tune_s = time.perf_counter() - t0 if autotune else 0.0
     n0 = s.launch_count()
     s.step(2)                       # captures the two-step graph
     per_step = (s.launch_count() - n0) // 2
@@ -184,7 +187,8 @@ def run_precision(fw, params, depth, phases, precision, K, W, local, pg):
     s.sync()
     barrier(pg)
     ms = e0.elapsed_time(e1)
-    return s, {"ms": ms, "status": st, "launches_per_step": per_step, "clocks": clk.summary()}
+    return s, {"ms": ms, "status": st, "launches_per_step": per_step, "clocks": clk.summary(),
+               "tuning": tuning, "tune_s": tune_s}
 
 
 def kernel_profile(s, T, cells, faces_x, faces_y, hbm):
@@ -232,7 +236,7 @@ def e2e_run(fw, s, K):
     return dt, 5 * nb, 3 * nb
 
 
-def ensemble_bench(fw, pg, ws, n=512, K=10, W=2, run_seconds=300.0):
+def ensemble_bench(fw, pg, ws, n=512, K=10, W=2, run_seconds=300.0, autotune=True):
     """The 512-run ensemble (planar beaches of uneven size, slope, depth and
     JONSWAP forcing; 1.5e8 cells in all): every member steps concurrently
     through fw_ensemble_step.  cell-steps/s over K steps after W warm-up
@@ -241,7 +245,7 @@ def ensemble_bench(fw, pg, ws, n=512, K=10, W=2, run_seconds=300.0):
     run's step count from its own DT and the measured cell-step rate."""
     members = fw.cases.ensemble_members(n, seed=2024)
     t0 = time.perf_counter()
-    ens = fw.Ensemble(members, precision="MIXED")
+    ens = fw.Ensemble(members, precision="MIXED", autotune=autotune)
     t_init = time.perf_counter() - t0
     ens.step(W)
     barrier(pg)
@@ -499,6 +503,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 512-run ensemble measurement")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (no fw_autotune)")
     ap.add_argument("--learned-report", action="store_true",
                     help="only the learned coarse-grid correction report (training, held-out error, throughput)")
     ap.add_argument("--precision-report", action="store_true",
@@ -533,11 +538,11 @@ def main():
     cells = params["Mglob"] * params["Nglob"]
     hbm, peak_kind = peaks()
 
-    sm, rm = run_precision(fw, params, depth, phases, "MIXED", K, W, local, pg)
+    sm, rm = run_precision(fw, params, depth, phases, "MIXED", K, W, local, pg, autotune=not args.no_autotune)
     ms_mixed = max_over_ranks(rm["ms"], pg)
     res64 = None
     if not args.no_fp64:
-        s64, r64 = run_precision(fw, params, depth, phases, "FP64", K, W, local, pg)
+        s64, r64 = run_precision(fw, params, depth, phases, "FP64", K, W, local, pg, autotune=not args.no_autotune)
         ms64 = max_over_ranks(r64["ms"], pg)
         import numpy as np
         e_m = sm.get("Eta")[3:-3, 3:-3]
@@ -561,7 +566,7 @@ def main():
         sm, 4, cells, (params["Mglob"] + 1) * params["Nglob"], params["Mglob"] * (params["Nglob"] + 1), hbm)
     dom = max(prof, key=lambda k: prof[k]["ms"]) if prof else None
     sm.close()
-    ens = None if args.no_ensemble else ensemble_bench(fw, pg, ws)
+    ens = None if args.no_ensemble else ensemble_bench(fw, pg, ws, autotune=not args.no_autotune)
     if rank != 0:
         return 0
     value = cells * K * ws / (ms_mixed * 1e-3)
@@ -572,7 +577,8 @@ def main():
         "dtype": "f32 (f64 tridiagonal and depth tests)", "data": "synthetic",
         "config": {"workload": WORKLOAD, "grid": [params["Mglob"], params["Nglob"]], "dx_m": params["DX"],
                    "precision": "MIXED", "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "l2": "state (~0.8 GB mixed, ~1.6 GB FP64) exceeds the 129 MB L2; no flush"},
+                   "l2": "state (~0.8 GB mixed, ~1.6 GB FP64) exceeds the 129 MB L2; no flush",
+                   "launch_shapes": rm["tuning"], "autotune_s": rm["tune_s"]},
         "gpu_launches": rm["launches_per_step"] * K,
         "clocks": rm["clocks"],
         "status": rm["status"],

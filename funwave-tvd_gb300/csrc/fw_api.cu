@@ -4,6 +4,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -309,6 +312,50 @@ long long swap_state(fw_ctx *c) {
     return (long long)((uintptr_t)c->ff.MASK ^ ((uintptr_t)c->ff.AGE << 1));
 }
 
+// launch-shape candidates of the per-cell kernels (bx a multiple of 32,
+// at most 256 threads, as the kernels' launch bounds allow)
+const int CELL_CANDIDATES[][2] = {{32, 8}, {32, 4}, {64, 4}, {128, 2}, {64, 2}, {256, 1}};
+const char *const TUNE_NAMES[fw::TK_N] = {"disp_a", "disp_b", "update", "post_mask_break", "maskmul"};
+std::mutex tune_mu;
+std::map<std::array<long long, 8>, std::array<int, FW_TUNE_LEN>> tune_cache;
+
+bool tune_valid(const fw_ctx *c, const int *t) {
+    for (int k = 0; k < fw::TK_N; k++) {
+        const int bx = t[2 * k], by = t[2 * k + 1];
+        if (bx < 32 || bx % 32 != 0 || by < 1 || bx * by > 256) return false;
+    }
+    const bool fp64 = c->p.precision == FW_PREC_FP64;
+    const int fx = t[fw::TUNE_FLUX], fyv = t[fw::TUNE_FLUX + 1];
+    if (fx != 8 && fx != 16) return false;
+    if (fp64 ? (fyv != 8 && fyv != 16) : (fyv != 16 && fyv != 32)) return false;
+    return true;
+}
+
+// average ms of a launch of one named kernel: two warm-up launches, then
+// eight timed with CUDA events on the context stream; e records a failure
+double time_named(fw_ctx *c, bool fp64, const char *name, cudaError_t &e) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    double ms_out = 1e30;
+    if ((e = cudaEventCreate(&a)) != cudaSuccess || (e = cudaEventCreate(&b)) != cudaSuccess) {
+        if (a) cudaEventDestroy(a);
+        return ms_out;
+    }
+    auto launch = [&]() { return fp64 ? fw::launch_by_name<double>(c, name) : fw::launch_by_name<float>(c, name); };
+    constexpr int NREP = 8;
+    for (int k = 0; k < 2; k++) launch();
+    e = cudaEventRecord(a, c->stream);
+    for (int k = 0; k < NREP && e == cudaSuccess; k++) launch();
+    if (e == cudaSuccess) e = cudaEventRecord(b, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (e == cudaSuccess && c->sticky_error) e = (cudaError_t)c->sticky_error;
+    if (e == cudaSuccess) ms_out = (double)ms / NREP;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms_out;
+}
+
 int read_status(fw_ctx *c, int *status) {
     unsigned long long bits = 0;
     cudaError_t e = cudaMemcpyAsync(&bits, etamax_ptr(c), sizeof(bits), cudaMemcpyDeviceToHost, c->stream);
@@ -388,6 +435,7 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     fw_ctx *c = new (std::nothrow) fw_ctx();
     if (!c) return FW_ERR_OOM;
     c->p = *p;
+    if (p->precision == FW_PREC_FP64) c->tune[fw::TUNE_FLUX + 1] = 16;
     Grid &g = c->g;
     std::memset(&g, 0, sizeof(g));
     g.Mglob = p->Mglob;
@@ -875,5 +923,97 @@ int fw_time_kernel(fw_ctx *c, const char *name, int nrep, double *ms_per_launch)
     return finish(c);
 }
 void *fw_stream(fw_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int fw_get_tuning(fw_ctx *c, int *t) {
+    if (!c || !t) return FW_ERR_BAD_PARAM;
+    std::memcpy(t, c->tune, sizeof(c->tune));
+    return FW_OK;
+}
+
+int fw_set_tuning(fw_ctx *c, const int *t) {
+    if (!c || !t) return FW_ERR_BAD_PARAM;
+    if (!tune_valid(c, t)) return FW_ERR_BAD_PARAM;
+    std::memcpy(c->tune, t, sizeof(c->tune));
+    c->graph_ready = 0;
+    return FW_OK;
+}
+
+int fw_autotune(fw_ctx *c, int flags) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    // size class: the number of bits of Mglob - 1 and Nglob - 1 (grids
+    // within one power of two share a tuning), plus the kernels' path
+    auto bits = [](int v) {
+        int b = 0;
+        for (unsigned u = (unsigned)(v - 1); u; u >>= 1) b++;
+        return b;
+    };
+    const std::array<long long, 8> key = {c->p.precision, bits(c->g.Mglob), bits(c->g.Nglob), c->g.dispersion,
+                                          c->g.show_breaking, c->g.periodic, c->factored, c->g.direct_sponge};
+    if (!(flags & FW_TUNE_FRESH)) {
+        std::lock_guard<std::mutex> lk(tune_mu);
+        auto it = tune_cache.find(key);
+        if (it != tune_cache.end()) {
+            std::memcpy(c->tune, it->second.data(), sizeof(c->tune));
+            c->graph_ready = 0;
+            return FW_OK;
+        }
+    }
+    // the candidates run on the real state; save it and put it back after
+    void *save = nullptr;
+    if (cudaMalloc(&save, c->arena_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return FW_ERR_OOM;
+    }
+    cudaError_t e = cudaMemcpyAsync(save, c->arena, c->arena_bytes, cudaMemcpyDeviceToDevice, c->stream);
+    const bool fp64 = c->p.precision == FW_PREC_FP64;
+    const bool disp = c->g.dispersion != 0, pmb = disp && c->g.show_breaking;
+    const bool on_path[fw::TK_N] = {disp, disp, true, pmb, true};
+    for (int sweep = 0; sweep < 2 && e == cudaSuccess; sweep++) {
+        for (int k = 0; k < fw::TK_N && e == cudaSuccess; k++) {
+            if (!on_path[k]) continue;
+            double best = 1e30;
+            int bx = c->tune[2 * k], by = c->tune[2 * k + 1];
+            for (const auto &cand : CELL_CANDIDATES) {
+                c->tune[2 * k] = cand[0];
+                c->tune[2 * k + 1] = cand[1];
+                const double ms = time_named(c, fp64, TUNE_NAMES[k], e);
+                if (ms < best) {
+                    best = ms;
+                    bx = cand[0];
+                    by = cand[1];
+                }
+            }
+            c->tune[2 * k] = bx;
+            c->tune[2 * k + 1] = by;
+        }
+        for (int dir = 0; dir < 2 && e == cudaSuccess; dir++) {
+            double best = 1e30;
+            int pick = c->tune[fw::TUNE_FLUX + dir];
+            for (int fy : {8, 16, 32}) {
+                c->tune[fw::TUNE_FLUX + dir] = fy;
+                if (!tune_valid(c, c->tune)) continue;
+                const double ms = time_named(c, fp64, dir == 0 ? "flux_x" : "flux_y", e);
+                if (ms < best) {
+                    best = ms;
+                    pick = fy;
+                }
+            }
+            c->tune[fw::TUNE_FLUX + dir] = pick;
+        }
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->arena, save, c->arena_bytes, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(save);
+    c->graph_ready = 0;
+    if (e != cudaSuccess) return cuda_status(c, e);
+    {
+        std::lock_guard<std::mutex> lk(tune_mu);
+        std::array<int, FW_TUNE_LEN> v;
+        std::memcpy(v.data(), c->tune, sizeof(c->tune));
+        tune_cache[key] = v;
+    }
+    return finish(c);
+}
 
 }  // extern "C"

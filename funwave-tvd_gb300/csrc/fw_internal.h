@@ -136,8 +136,18 @@ void convert_out(fw_ctx *c, const void *field, int is_mask, void *staging, int w
 #include <cuda_runtime.h>
 
 // Host context behind the opaque C handle.
+namespace fw {
+// kernels whose block shape fw_autotune chooses (per-cell kernels, so any
+// shape gives the same results); the tuning vector holds (bx, by) for each,
+// then the tile heights of the x and y flux kernels (FW_TUNE_LEN ints)
+enum TuneKernel { TK_DISP_A = 0, TK_DISP_B, TK_UPDATE, TK_PMB, TK_MASKMUL, TK_N };
+constexpr int TUNE_FLUX = 2 * TK_N;
+}  // namespace fw
+
 struct fw_ctx {
     fw_params p;
+    int tune[FW_TUNE_LEN] = {32, 8, 32, 8, 32, 8, 32, 8, 32, 8, 8, 32};  // see fw::TuneKernel
+    dim3 blk(int k) const { return dim3((unsigned)tune[2 * k], (unsigned)tune[2 * k + 1]); }
     fw::Grid g;
     cudaStream_t stream = nullptr;
     fw::Fields<double> fd{};

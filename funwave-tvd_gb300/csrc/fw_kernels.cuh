@@ -437,16 +437,21 @@ __device__ __forceinline__ void ho_lr(T vm1, T v0, T d0, T d1, T d2, T &L, T &R)
     }
 }
 
-// Faces of direction DIR (0: x-faces, 1: y-faces).  A tile is 32 x 8
-// x-faces or 32 x 32 y-faces (four per thread, so that the three-cell halo
-// along y is shared by 32 faces; 32 x 16 in FP64).  Din of the seven reconstructed fields is
+// Faces of direction DIR (0: x-faces, 1: y-faces).  A tile is 32 x FY
+// faces, FY/8 per thread (by default 32 x 8 x-faces and 32 x 32 y-faces,
+// so that the three-cell halo along y is shared by 32 faces; 32 x 16 in
+// FP64; fw_autotune may pick another compiled height).  Din of the seven reconstructed fields is
 // computed once per cell position into shared memory; each thread then
 // finishes its faces: face values, Zhou wave speeds, HLL and the
 // boundary/dry-face rules.  Normal velocity is U for x and V for y.
-template <typename T, int DIR> struct FluxTile {
+template <typename T, int DIR> constexpr int flux_fy_default() {
+    return DIR == 0 ? 8 : (sizeof(T) == sizeof(double) ? 16 : 32);
+}
+
+template <typename T, int DIR, int FY_ = flux_fy_default<T, DIR>()> struct FluxTile {
     static constexpr int BX = 32, BY = 8;              // threads
-    // faces of a tile (y tiles of doubles are 16 high: 48 KB static shared memory)
-    static constexpr int FX = 32, FY = DIR == 0 ? 8 : (sizeof(T) == sizeof(double) ? 16 : 32);
+    // faces of a tile (y tiles of doubles at most 16 high: 48 KB static shared memory)
+    static constexpr int FX = 32, FY = FY_;
     static constexpr int FPT = FY / BY;                // faces per thread
     static constexpr int NB = DIR == 0 ? FX : FY;      // faces per tile line
     static constexpr int NTL = DIR == 0 ? FY : FX;     // tile lines
@@ -454,9 +459,10 @@ template <typename T, int DIR> struct FluxTile {
     static constexpr int NP = DIR == 0 ? NPOS : NPOS + 1;  // odd row length for y
 };
 
-template <typename T, int DIR>
+template <typename T, int DIR, int FY_ = flux_fy_default<T, DIR>()>
 __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
-    using TL = FluxTile<T, DIR>;
+    using TL = FluxTile<T, DIR, FY_>;
+    static_assert(TL::FY % TL::BY == 0, "whole faces per thread");
     constexpr int BX = TL::BX, BY = TL::BY, NTL = TL::NTL, NPOS = TL::NPOS, NP = TL::NP;
     __shared__ T din[7][NTL][NP];
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -504,7 +510,7 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
         if (i > g.ie || j > g.je + 1) continue;
     }
     const int own = DIR == 0 ? tx : ty + r * BY;
-    const int line = DIR == 0 ? ty : tx;
+    const int line = DIR == 0 ? ty + r * BY : tx;
     const int fid = i + j * g.pitch;
     const int cm = fid - stride;  // cell pos-1 (cell pos is fid)
     const int kf = own + 1;
@@ -2485,8 +2491,8 @@ static inline dim3 grid2(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / 
 static const dim3 B2D(32, 8);
 // blocks of k_flux: tiles of FX x FY faces over (Mglob+1) x Nglob x-faces
 // or Mglob x (Nglob+1) y-faces
-template <typename T, int DIR> static dim3 flux_grid(const Grid &g) {
-    using TL = FluxTile<T, DIR>;
+template <typename T, int DIR, int FY_ = flux_fy_default<T, DIR>()> static dim3 flux_grid(const Grid &g) {
+    using TL = FluxTile<T, DIR, FY_>;
     const int w = DIR == 0 ? g.Mglob + 1 : g.Mglob, h = DIR == 0 ? g.Nglob : g.Nglob + 1;
     return dim3((w + TL::FX - 1) / TL::FX, (h + TL::FY - 1) / TL::FY);
 }
@@ -2508,7 +2514,7 @@ template <typename T> void launch_ghost(fw_ctx *c, bool full) {
 template <typename T> void launch_exchange(fw_ctx *c, bool with_sponge) {
     const Grid &g = c->g;
     launch_ghost<T>(c, g.visc_breaking != 0);
-    k_maskmul<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>(), with_sponge ? 1 : 0);
+    k_maskmul<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_MASKMUL)), c->blk(TK_MASKMUL), 0, c->stream>>>(g, c->F<T>(), with_sponge ? 1 : 0);
     note(c);
 }
 
@@ -2551,18 +2557,41 @@ template <typename T> void launch_begin_step(fw_ctx *c) {
 
 template <typename T> void launch_dispersion(fw_ctx *c) {
     const Grid &g = c->g;
-    k_disp_a<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    k_disp_a<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_DISP_A)), c->blk(TK_DISP_A), 0, c->stream>>>(g, c->F<T>());
     note(c);
-    k_disp_b<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+    k_disp_b<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_DISP_B)), c->blk(TK_DISP_B), 0, c->stream>>>(g, c->F<T>());
+    note(c);
+}
+
+// the compiled flux tile heights: x faces 8 or 16; y faces 16 or 32
+// (float), 8 or 16 (double, whose 32-high tile would not fit 48 KB)
+template <typename T, int DIR> static bool flux_fy_ok(int fy) {
+    if (DIR == 0) return fy == 8 || fy == 16;
+    return sizeof(T) == sizeof(float) ? (fy == 16 || fy == 32) : (fy == 8 || fy == 16);
+}
+
+template <typename T, int DIR, int FY_> static void flux_at(fw_ctx *c) {
+    k_flux<T, DIR, FY_><<<flux_grid<T, DIR, FY_>(c->g), B2D, 0, c->stream>>>(c->g, c->F<T>());
+}
+
+template <typename T, int DIR> static void launch_flux(fw_ctx *c) {
+    const int fy = c->tune[TUNE_FLUX + DIR];
+    if constexpr (DIR == 0) {
+        if (fy == 16) flux_at<T, 0, 16>(c);
+        else flux_at<T, 0, 8>(c);
+    } else if constexpr (sizeof(T) == sizeof(float)) {
+        if (fy == 16) flux_at<T, 1, 16>(c);
+        else flux_at<T, 1, 32>(c);
+    } else {
+        if (fy == 8) flux_at<T, 1, 8>(c);
+        else flux_at<T, 1, 16>(c);
+    }
     note(c);
 }
 
 template <typename T> void launch_fluxes(fw_ctx *c) {
-    const Grid &g = c->g;
-    k_flux<T, 0><<<flux_grid<T, 0>(g), B2D, 0, c->stream>>>(g, c->F<T>());
-    note(c);
-    k_flux<T, 1><<<flux_grid<T, 1>(g), B2D, 0, c->stream>>>(g, c->F<T>());
-    note(c);
+    launch_flux<T, 0>(c);
+    launch_flux<T, 1>(c);
 }
 
 template <typename T> void launch_sources_debug(fw_ctx *c) {
@@ -2623,7 +2652,7 @@ template <typename T> static void launch_estimate_huv_opt(fw_ctx *c, int istage,
     static const double AL[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0};
     static const double BE[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
     const T al = (T)AL[istage - 1], be = (T)BE[istage - 1];
-    k_update<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>(), al, be);
+    k_update<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_UPDATE)), c->blk(TK_UPDATE), 0, c->stream>>>(g, c->F<T>(), al, be);
     note(c);
     if (g.dispersion) {
         if (sizeof(T) == sizeof(float) && c->factored) {
@@ -2747,7 +2776,7 @@ template <typename T> void launch_stage(fw_ctx *c, int istage) {
         // GET_Eta_U_V_HU_HV tail + UPDATE_MASK + BREAKING (parallel part)
         // in one kernel, then the breaking sweep's candidates
         launch_estimate_huv_opt<T>(c, istage, false);
-        k_post_mask_break<T><<<grid2(g.Mloc + 1, g.Nloc + 1, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+        k_post_mask_break<T><<<grid2(g.Mloc + 1, g.Nloc + 1, c->blk(TK_PMB)), c->blk(TK_PMB), 0, c->stream>>>(g, c->F<T>());
         note(c);
         auto &F = c->F<T>();
         uint8_t *t = F.MASK;
@@ -2828,11 +2857,15 @@ template <typename T> int launch_by_name(fw_ctx *c, const char *name) {
     Fields<T> &f = c->F<T>();
     const dim3 gc = grid2(g.Mloc, g.Nloc, B2D);
     auto is = [&](const char *n) { return std::strcmp(name, n) == 0; };
-    if (is("disp_a")) k_disp_a<T><<<gc, B2D, 0, c->stream>>>(g, f);
-    else if (is("disp_b")) k_disp_b<T><<<gc, B2D, 0, c->stream>>>(g, f);
-    else if (is("flux_x")) k_flux<T, 0><<<flux_grid<T, 0>(g), B2D, 0, c->stream>>>(g, f);
-    else if (is("flux_y")) k_flux<T, 1><<<flux_grid<T, 1>(g), B2D, 0, c->stream>>>(g, f);
-    else if (is("update")) k_update<T><<<gc, B2D, 0, c->stream>>>(g, f, (T)0.75, (T)0.25);
+    if (is("disp_a")) k_disp_a<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_DISP_A)), c->blk(TK_DISP_A), 0, c->stream>>>(g, f);
+    else if (is("disp_b")) k_disp_b<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_DISP_B)), c->blk(TK_DISP_B), 0, c->stream>>>(g, f);
+    else if (is("flux_x")) { launch_flux<T, 0>(c); return 0; }
+    else if (is("flux_y")) { launch_flux<T, 1>(c); return 0; }
+    else if (is("update")) k_update<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_UPDATE)), c->blk(TK_UPDATE), 0, c->stream>>>(g, f, (T)0.75, (T)0.25);
+    else if (is("post_mask_break")) {
+        const dim3 b = c->blk(TK_PMB);
+        k_post_mask_break<T><<<grid2(g.Mloc + 1, g.Nloc + 1, b), b, 0, c->stream>>>(g, f);
+    }
     else if (is("tri_x")) { launch_tri<T, 0, false>(c, c->px); return 0; }
     else if (is("tri_y")) {
         if (g.periodic) launch_tri<T, 1, true>(c, c->py);
@@ -2843,7 +2876,7 @@ template <typename T> int launch_by_name(fw_ctx *c, const char *name) {
     else if (is("mask")) k_mask<T><<<grid2(g.Mloc + 1, g.Nloc + 1, B2D), B2D, 0, c->stream>>>(g, f);
     else if (is("break_a")) k_break_a<T><<<gc, B2D, 0, c->stream>>>(g, f);
     else if (is("ghost")) { launch_ghost<T>(c, g.visc_breaking != 0); return 0; }
-    else if (is("maskmul")) k_maskmul<T><<<gc, B2D, 0, c->stream>>>(g, f, g.direct_sponge);
+    else if (is("maskmul")) k_maskmul<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_MASKMUL)), c->blk(TK_MASKMUL), 0, c->stream>>>(g, f, g.direct_sponge);
     else if (is("begin")) k_begin<T><<<gc, B2D, 0, c->stream>>>(g, f);
     else return -1;
     note(c);

@@ -34,9 +34,12 @@ def max_runup(height_max, depth):
 class Ensemble:
     """members: list of (params, depth, phases) as the case generators return.
     All members are created on ``device`` with ``precision``; OUT_Hmax is
-    switched on so that each run's maximum run-up can be read."""
+    switched on so that each run's maximum run-up can be read.  autotune:
+    choose each member's launch shapes with fw_autotune after its init
+    (cached per size class, so the 512-member ensemble tunes a few dozen
+    times, not 512); the results do not depend on it."""
 
-    def __init__(self, members, precision="MIXED", device=0):
+    def __init__(self, members, precision="MIXED", device=0, autotune=False):
         self.solvers = []
         self.depths = []
         for params, depth, phases in members:
@@ -44,6 +47,8 @@ class Ensemble:
             p["OUT_Hmax"] = True
             s = Solver(p, precision=precision, device=device)
             s.init(depth, phases=phases)
+            if autotune:
+                s.autotune()
             self.solvers.append(s)
             self.depths.append(np.asarray(depth))
         self.L = self.solvers[0].L if self.solvers else None

@@ -235,6 +235,9 @@ def load_library(path=None):
     L.fw_stream.argtypes = [vp]
     L.fw_stream.restype = vp
     L.fw_time_kernel.argtypes = [vp, ctypes.c_char_p, ip, ctypes.POINTER(dp)]
+    L.fw_autotune.argtypes = [vp, ip]
+    L.fw_get_tuning.argtypes = [vp, ctypes.POINTER(ip)]
+    L.fw_set_tuning.argtypes = [vp, ctypes.POINTER(ip)]
     L.fw_strerror.argtypes = [ip]
     L.fw_strerror.restype = ctypes.c_char_p
     if path == lib_path():
@@ -398,6 +401,35 @@ class Solver:
         ms = ctypes.c_double()
         self._check(self.L.fw_time_kernel(self.ctx, name.encode(), int(nrep), ctypes.byref(ms)), name)
         return ms.value
+
+    # FW_TUNE_LEN of include/funwave_gpu.h: (bx, by) of disp_a, disp_b,
+    # update, post_mask_break, maskmul, then the x and y flux tile heights
+    TUNE_LEN = 12
+    TUNE_NAMES = ("disp_a", "disp_b", "update", "post_mask_break", "maskmul")
+
+    def autotune(self, fresh=False):
+        """Time the candidate launch shapes on this run's state (saved and
+        restored around the measurement) and keep the fastest; returns the
+        tuning (see tuning())."""
+        self._check(self.L.fw_autotune(self.ctx, 1 if fresh else 0), "fw_autotune")
+        return self.tuning()
+
+    def tuning(self):
+        """{kernel: (bx, by)} of the per-cell kernels plus "flux_x"/"flux_y"
+        tile heights."""
+        t = (ctypes.c_int * self.TUNE_LEN)()
+        self._check(self.L.fw_get_tuning(self.ctx, t), "fw_get_tuning")
+        out = {n: (t[2 * k], t[2 * k + 1]) for k, n in enumerate(self.TUNE_NAMES)}
+        out["flux_x"], out["flux_y"] = t[10], t[11]
+        return out
+
+    def set_tuning(self, tuning):
+        """Set launch shapes explicitly (a dict as returned by tuning())."""
+        t = (ctypes.c_int * self.TUNE_LEN)()
+        for k, n in enumerate(self.TUNE_NAMES):
+            t[2 * k], t[2 * k + 1] = tuning[n]
+        t[10], t[11] = tuning["flux_x"], tuning["flux_y"]
+        self._check(self.L.fw_set_tuning(self.ctx, t), "fw_set_tuning")
 
     def launch_count(self):
         return int(self.L.fw_launch_count(self.ctx))

@@ -222,6 +222,29 @@ int fw_time_kernel(fw_ctx *ctx, const char *name, int nrep, double *ms_per_launc
 /* CUDA stream of the context, as a void* (cudaStream_t). */
 void *fw_stream(fw_ctx *ctx);
 
+/* --- launch-shape autotuning (no reference counterpart) ----------------- */
+/* The tuning vector: FW_TUNE_LEN ints, (bx, by) thread-block shapes of the
+ * per-cell kernels disp_a, disp_b, update, post_mask_break and maskmul
+ * (bx a multiple of 32, bx*by <= 256), then the tile heights of the x-face
+ * flux kernel (8 or 16) and of the y-face one (16 or 32 in MIXED, 8 or 16 in
+ * FP64).  Every choice computes the same values bit for bit; only the speed
+ * differs.  Defaults: 32 x 8 blocks, flux tiles 8 and 32 (16 in FP64). */
+#define FW_TUNE_LEN 12
+#define FW_TUNE_FRESH 1   /* fw_autotune flag: measure even if this shape was tuned before */
+/* Choose the tuning vector by timing every candidate of each kernel on this
+ * context's state with CUDA events (two sweeps, the faster of each), keeping
+ * the fastest.  The state is saved to a temporary device copy first and put
+ * back afterwards, so the run continues unchanged (the call allocates and
+ * frees that copy: one arena's size).  Results are cached per process by
+ * precision, size class (grids whose sides lie within the same powers of
+ * two) and path, so an ensemble of many sizes tunes once per class.  Call
+ * after fw_init; the next step recaptures its graph. */
+int fw_autotune(fw_ctx *ctx, int flags);
+int fw_get_tuning(fw_ctx *ctx, int *tuning);        /* FW_TUNE_LEN ints */
+/* Set the tuning vector explicitly; FW_ERR_BAD_PARAM for a shape outside the
+ * candidates above. */
+int fw_set_tuning(fw_ctx *ctx, const int *tuning);
+
 /* --- no device allocation ---------------------------------------------- */
 /* ESTIMATE_DT on device arrays the caller owns, allocating nothing: for
  * callers that cannot call cudaMalloc (device arrays owned by an OpenACC or
