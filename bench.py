@@ -169,8 +169,12 @@ def run_precision(fw, params, depth, phases, precision, K, W, local, pg, autotun
     s = fw.Solver(params, precision=precision, device=local)
     s.init(depth, phases=phases)
     t0 = time.perf_counter()
-    tuning = s.autotune() if autotune else s.tuning()
-    tune_s = time.perf_counter() - t0 if autotune else 0.0
+    if isinstance(autotune, dict):
+        s.set_tuning({k: tuple(v) if isinstance(v, list) else v for k, v in autotune.items()})
+        tuning, tune_s = s.tuning(), 0.0
+    else:
+        tuning = s.autotune() if autotune else s.tuning()
+        tune_s = time.perf_counter() - t0 if autotune else 0.0
     n0 = s.launch_count()
     s.step(2)                       # captures the two-step graph
     per_step = (s.launch_count() - n0) // 2
@@ -316,6 +320,50 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
         "cell_steps_per_s_mixed": m["rate"], "cell_steps_per_s_fp64": d["rate"],
         "speedup_mixed_over_fp64": m["rate"] / d["rate"],
     }
+
+
+def net_report(fw, size=1024, reps=20):
+    """The correction network alone, on a size x size coarse grid: the
+    forward pass (packing, four tcgen05 convolutions) and one training
+    iteration (forward, loss, backward with tcgen05 data gradients and
+    CUDA-core weight gradients, Adam) on a batch of 8 tiles of 128 x 128,
+    CUDA events on the current stream after 3 warm-up calls.  Tensor work:
+    2 x 9 x (16*32 + 32*32 + 32*32 + 32*16) MACs a pixel in the forward pass
+    (channels as padded for the tensor cores)."""
+    import torch
+    torch.cuda.set_device(0)
+    net = fw.learned.Net(seed=1)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.randn((1, size, size, 5), device="cuda", generator=g)
+    for _ in range(3):
+        net.forward(x)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        net.forward(x)
+    e1.record()
+    e1.synchronize()
+    ms_fwd = e0.elapsed_time(e1) / reps
+    xb = torch.randn((8, 128, 128, 5), device="cuda", generator=g)
+    tb = torch.randn((8, 128, 128, 3), device="cuda", generator=g)
+    wb = torch.ones((8, 128, 128), device="cuda")
+    for _ in range(3):
+        net.loss_grad(xb, tb, wb)
+        net.adam(1e-4)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        net.loss_grad(xb, tb, wb)
+        net.adam(1e-4)
+    e1.record()
+    e1.synchronize()
+    ms_iter = e0.elapsed_time(e1) / reps
+    net.close()
+    macs = 9 * (16 * 32 + 32 * 32 + 32 * 32 + 32 * 16)
+    return {"metric": "correction network", "grid": [size, size], "ms_forward": ms_fwd,
+            "forward_tflops_padded": 2.0 * macs * size * size / (ms_fwd * 1e-3) / 1e12,
+            "ms_train_iteration_batch8_128x128": ms_iter}
 
 
 def learned_report(fw, iters=4000, eval_coarse_steps=500):
@@ -504,6 +552,10 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 512-run ensemble measurement")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (no fw_autotune)")
+    ap.add_argument("--tuning", default=None,
+                    help="launch shapes as JSON (the config's launch_shapes of an earlier run) instead of fw_autotune")
+    ap.add_argument("--net-report", action="store_true",
+                    help="time the correction network's forward pass and training iteration")
     ap.add_argument("--learned-report", action="store_true",
                     help="only the learned coarse-grid correction report (training, held-out error, throughput)")
     ap.add_argument("--precision-report", action="store_true",
@@ -516,6 +568,9 @@ def main():
     params = fw.with_defaults(params)
     if args.impl == "reference":
         return reference_arm(args, fw, params, depth, phases)
+    if args.net_report:
+        print(json.dumps(net_report(fw)), flush=True)
+        return 0
     if args.learned_report:
         print(json.dumps(learned_report(fw)), flush=True)
         return 0
@@ -538,7 +593,8 @@ def main():
     cells = params["Mglob"] * params["Nglob"]
     hbm, peak_kind = peaks()
 
-    sm, rm = run_precision(fw, params, depth, phases, "MIXED", K, W, local, pg, autotune=not args.no_autotune)
+    tune_arg = json.loads(args.tuning) if args.tuning else (not args.no_autotune)
+    sm, rm = run_precision(fw, params, depth, phases, "MIXED", K, W, local, pg, autotune=tune_arg)
     ms_mixed = max_over_ranks(rm["ms"], pg)
     res64 = None
     if not args.no_fp64:
