@@ -373,17 +373,26 @@ int conv_tc(const bf16 *x, int C, const bf16 *img, const float *bias, const bf16
         }
         attr = true;
     }
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return FW_ERR_CUDA;
+        }
+    }
     CUtensorMap m;
     if (!act_map(&m, x, C, B, H, W)) return FW_ERR_CUDA;
-    const dim3 grid((unsigned)((W + fwtc::TPX - 1) / fwtc::TPX), (unsigned)((H + fwtc::TROWS - 1) / fwtc::TROWS),
-                    (unsigned)B);
-    k<<<grid, 128, Lt::BYTES, s>>>(m, img, bias, act, y, H, W, status);
+    const long long ntiles = (long long)((W + fwtc::TPX - 1) / fwtc::TPX) * ((H + fwtc::TROWS - 1) / fwtc::TROWS) * B;
+    const unsigned grid = (unsigned)std::min<long long>(ntiles, (long long)nsm * Lt::PER_SM);
+    k<<<grid, 64 + 32 * fwtc::EPI_WARPS, Lt::BYTES, s>>>(m, img, bias, act, y, H, W, B, status);
     return FW_OK;
 }
 
-// the grid of the tensor-core kernels: H / TROWS blocks in y, B in z
+// the tensor-core kernels number their tiles in an int
 bool shape_ok(int B, int H, int W) {
-    return B > 0 && H > 0 && W > 0 && B <= 65535 && (H + fwtc::TROWS - 1) / fwtc::TROWS <= 65535;
+    return B > 0 && H > 0 && W > 0 &&
+           (long long)((W + fwtc::TPX - 1) / fwtc::TPX) * ((H + fwtc::TROWS - 1) / fwtc::TROWS) * B < (1LL << 31);
 }
 
 void pack_images(fw_net *n, cudaStream_t s) {

@@ -7,14 +7,17 @@
 //
 //   1. one thread issues CINC TMA tensor loads (one per 8-channel chunk) of
 //      the (TROWS + 2) x 130-pixel input halo tile -- zero-filled by the
-//      TMA unit outside the grid -- and one bulk copy of the packed BF16
-//      weight image, all completing on one mbarrier;
+//      TMA unit outside the grid -- completing on an mbarrier (with the
+//      first tile, one bulk copy of the packed BF16 weight image too);
 //   2. the same thread issues TROWS x 9 x CINC/2 tcgen05.mma (kind::f16,
 //      BF16 x BF16 -> FP32) into TMEM, one 128 x N accumulator per output
 //      row, and commits them to a second mbarrier;
 //   3. the four warps read their 32 TMEM lanes (= pixels) back with
 //      tcgen05.ld and apply the epilogue (bias + ReLU -> BF16, bias ->
 //      FP32, or the backward ReLU mask -> BF16).
+// CTAs are persistent and warp-specialised (a TMA warp, an MMA warp, four
+// epilogue warps) with NSTAGE input stages and two TMEM accumulators, so
+// loads, MMAs and epilogues of successive tiles overlap.
 //
 // Shared-memory operand layout (no swizzle, K-major canonical layout): the
 // input tile is stored as CINC chunk planes, each [row][pixel][8 channels]
@@ -50,16 +53,24 @@ constexpr unsigned WAIT_LIMIT = 1u << 22;                      // polls of an mb
 
 enum { EPI_RELU_BF16 = 0, EPI_LINEAR_F32 = 1, EPI_MASK_BF16 = 2 };
 
+constexpr int NSTAGE = 3;                // input stages in flight per CTA
+constexpr int EPI_WARPS = 8;             // epilogue warps (two per TMEM lane quadrant)
+static_assert(TROWS % 2 == 0, "the epilogue splits a tile's rows in two halves");
+
 template <int CINC, int N> struct Layout {
-    static constexpr int X_BYTES = CINC * PLANE;
+    static constexpr int X_BYTES = CINC * PLANE;    // one input stage
     static constexpr int W_BYTES = 9 * CINC * N * 16;
-    static constexpr int BAR = X_BYTES + W_BYTES;  // two mbarriers, the TMEM address, a status word
-    static constexpr int TMEM_COLS = TROWS * N <= 32 ? 32 : (TROWS * N <= 64 ? 64 : 128);
-    // + slack for the 1024-byte alignment; at least 46 KB, so that no more
-    // than four CTAs (4 x 128 TMEM columns = all 512) share an SM and no
-    // tcgen05.alloc has to wait for another CTA's columns
-    static constexpr int NEED = BAR + 32 + 1024;
-    static constexpr int BYTES = NEED > 47104 ? NEED : 47104;
+    static constexpr int TMEM_COLS = TROWS * N <= 32 ? 32 : (TROWS * N <= 64 ? 64 : 128);  // one accumulator
+    // NSTAGE input stages, the weights, 2 NSTAGE + 4 mbarriers, the TMEM
+    // address and a flag, + slack for the 1024-byte alignment
+    static constexpr int NEED = NSTAGE * X_BYTES + W_BYTES + 8 * (2 * NSTAGE + 4) + 8 + 1024;
+    // CTAs an SM can hold: by shared memory (228 KB, 1 KB reserved each)
+    // and by TMEM (512 columns, two accumulators each); the host launches
+    // no more than this per SM, so no tcgen05.alloc waits for another CTA
+    static constexpr int PER_SM_SMEM = 233472 / (NEED + 1024);
+    static constexpr int PER_SM_TMEM = 512 / (2 * TMEM_COLS);
+    static constexpr int PER_SM = PER_SM_SMEM < PER_SM_TMEM ? PER_SM_SMEM : PER_SM_TMEM;
+    static constexpr int BYTES = NEED;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -153,36 +164,98 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
 __device__ __forceinline__ float lo_bf(uint32_t w) { return __uint_as_float(w << 16); }
 __device__ __forceinline__ float hi_bf(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
 
-// One CTA: TROWS output rows x 128 pixels of image b.  x: the input through
-// its tensor map ([B][H][W][8*CINC] BF16).  wimg: the packed weight image
-// (9 x CINC x N x 8 BF16).  EPI_RELU_BF16: y = BF16 relu(acc + bias),
-// [pix][32]; EPI_LINEAR_F32: y = FP32 acc + bias, [pix][NOUTF]; EPI_MASK_BF16:
-// y = BF16 acc where act > 0 else 0, [pix][32] (act: [pix][32] BF16).
-// status: set to 1 (input wait expired) or 2 (MMA wait expired).
+// Persistent, warp-specialised CTAs of 320 threads, each walking the tiles
+// t = blockIdx.x, + gridDim.x, ... (a tile: TROWS output rows x 128 pixels
+// of one image):
+//   warp 0 (one lane)   TMA producer: tile i's halo into input stage
+//                       i % NSTAGE once the MMAs of tile i - NSTAGE have
+//                       released it (the weight image with tile 0);
+//   warp 1              allocates TMEM; one lane issues tile i's MMAs into
+//                       accumulator i & 1 once its input has landed and
+//                       the epilogue of tile i - 2 has drained that
+//                       accumulator, then commits to the stage's "empty"
+//                       and the accumulator's "full" barriers;
+//   warps 2-9           the epilogue: each reads its TMEM lane quadrant
+//                       (warp % 4) of half of the finished accumulator's
+//                       rows (warps 2-5 the first half, 6-9 the second),
+//                       releases it, and stores.
+// No CTA-wide barrier sits inside the loop, so loads, MMAs and epilogues of
+// successive tiles overlap.  x: the input through its tensor map
+// ([B][H][W][8*CINC] BF16); wimg: the packed weight image (9 x CINC x N x 8
+// BF16).  EPI_RELU_BF16: y = BF16 relu(acc + bias), [pix][32];
+// EPI_LINEAR_F32: y = FP32 acc + bias, [pix][NOUTF]; EPI_MASK_BF16: y = BF16
+// acc where act > 0 else 0, [pix][32] (act: [pix][32] BF16).  status: set to
+// 1 (an input or accumulator wait expired) or 2 (an MMA wait expired); every
+// role then stops.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile uint32_t *flag) {
+    for (unsigned i = 0; i < WAIT_LIMIT; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\n"
+            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((i & 63) == 63 && *flag != 0u) return false;
+        if (i >= 32) __nanosleep(32);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 template <int CINC, int N, int EPI, int NOUTF>
-__global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtensorMap xmap,
-                                                 const bf16 *__restrict__ wimg, const float *__restrict__ bias,
-                                                 const bf16 *__restrict__ act, void *__restrict__ y, int H, int W,
-                                                 int *status) {
+__global__ void __launch_bounds__(320, 1) k_conv_tc(const __grid_constant__ CUtensorMap xmap,
+                                                    const bf16 *__restrict__ wimg, const float *__restrict__ bias,
+                                                    const bf16 *__restrict__ act, void *__restrict__ y, int H, int W,
+                                                    int B, int *status) {
     static_assert(CINC % 2 == 0 && (N == 16 || N == 32), "K steps of 16 channels; N of 16 or 32");
     using L = Layout<CINC, N>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    const uint32_t xs = smem_u32(smem), ws = xs + L::X_BYTES;
-    const uint32_t bar_in = xs + L::BAR, bar_mma = bar_in + 8, tptr = bar_in + 16;
-    volatile uint32_t *flag = reinterpret_cast<volatile uint32_t *>(smem + L::BAR + 20);
+    const uint32_t xs0 = smem_u32(smem), ws = xs0 + NSTAGE * L::X_BYTES;
+    const uint32_t bar = ws + L::W_BYTES;
+    // barriers: full[NSTAGE], empty[NSTAGE], accf[2], acce[2]
+    auto full_bar = [&](int st) { return bar + 8u * st; };
+    auto empty_bar = [&](int st) { return bar + 8u * (NSTAGE + st); };
+    auto accf_bar = [&](int a) { return bar + 8u * (2 * NSTAGE + a); };
+    auto acce_bar = [&](int a) { return bar + 8u * (2 * NSTAGE + 2 + a); };
+    const uint32_t tptr = bar + 8u * (2 * NSTAGE + 4);
+    volatile uint32_t *flag = reinterpret_cast<volatile uint32_t *>(smem + (tptr + 4u - xs0));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int x0 = blockIdx.x * TPX, y0 = blockIdx.y * TROWS, b = blockIdx.z;
+    const int tiles_x = (W + TPX - 1) / TPX, tiles_y = (H + TROWS - 1) / TROWS;
+    const int ntiles = tiles_x * tiles_y * B;
+    const int ntl = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    auto tile_xyb = [&](int i, int &x0, int &y0, int &b) {
+        const int t = (int)blockIdx.x + i * (int)gridDim.x;
+        x0 = (t % tiles_x) * TPX;
+        y0 = ((t / tiles_x) % tiles_y) * TROWS;
+        b = t / (tiles_x * tiles_y);
+    };
+    auto fail = [&](int code) {
+        *flag = 1u;
+        atomicExch(status, code);
+    };
 
     if (threadIdx.x == 0) {
-        mbar_init(bar_in, 1);
-        mbar_init(bar_mma, 1);
+        for (int k = 0; k < NSTAGE; k++) {
+            mbar_init(full_bar(k), 1);
+            mbar_init(empty_bar(k), 1);
+        }
+        for (int k = 0; k < 2; k++) {
+            mbar_init(accf_bar(k), 1);
+            mbar_init(acce_bar(k), EPI_WARPS);  // one arrival per epilogue warp
+        }
         *flag = 0u;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tptr),
-                     "r"((uint32_t)L::TMEM_COLS)
+                     "r"((uint32_t)(2 * L::TMEM_COLS))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -192,79 +265,140 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
     uint32_t tmem;
     asm volatile("ld.shared.u32 %0, [%1];" : "=r"(tmem) : "r"(tptr) : "memory");
 
-    if (threadIdx.x == 0) {
-        mbar_expect_tx(bar_in, (uint32_t)(CINC * BOX_BYTES + L::W_BYTES));
+    if (warp == 0) {
+        if (lane == 0) {
+            int last[NSTAGE];
 #pragma unroll
-        for (int c = 0; c < CINC; c++) tma_load_4d(xs + c * PLANE, &xmap, c * 8, x0 - 1, y0 - 1, b, bar_in);
-        bulk_load(ws, wimg, (uint32_t)L::W_BYTES, bar_in);
-        if (mbar_wait(bar_in, 0)) {
-            tc_fence_after();
+            for (int k = 0; k < NSTAGE; k++) last[k] = -1;
+            for (int i = 0; i < ntl; i++) {
+                const int st = i % NSTAGE;
+                if (i >= NSTAGE && !mbar_wait_or_abort(empty_bar(st), (uint32_t)(((i / NSTAGE) - 1) & 1), flag)) {
+                    if (*flag == 0u) fail(1);
+                    break;
+                }
+                int x0, y0, b;
+                tile_xyb(i, x0, y0, b);
+                mbar_expect_tx(full_bar(st), (uint32_t)(CINC * BOX_BYTES + (i == 0 ? L::W_BYTES : 0)));
+                const uint32_t xs = xs0 + st * L::X_BYTES;
+#pragma unroll
+                for (int c = 0; c < CINC; c++) tma_load_4d(xs + c * PLANE, &xmap, c * 8, x0 - 1, y0 - 1, b, full_bar(st));
+                if (i == 0) bulk_load(ws, wimg, (uint32_t)L::W_BYTES, full_bar(0));
+#pragma unroll
+                for (int k = 0; k < NSTAGE; k++)
+                    if (k == st) last[k] = i;
+            }
+            // after an abort: the loads still in flight (bounded)
+            if (*flag != 0u) {
+#pragma unroll
+                for (int k = 0; k < NSTAGE; k++)
+                    if (last[k] >= 0) mbar_wait(full_bar(k), (uint32_t)((last[k] / NSTAGE) & 1));
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
             constexpr uint32_t idesc = idesc_bf16<TPX, N>();
+            int committed = -1;
+            for (int i = 0; i < ntl; i++) {
+                const int st = i % NSTAGE, a = i & 1;
+                if (!mbar_wait_or_abort(full_bar(st), (uint32_t)((i / NSTAGE) & 1), flag)) {
+                    if (*flag == 0u) fail(1);
+                    break;
+                }
+                if (i >= 2 && !mbar_wait_or_abort(acce_bar(a), (uint32_t)(((i >> 1) - 1) & 1), flag)) {
+                    if (*flag == 0u) fail(1);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t xs = xs0 + st * L::X_BYTES, acc = tmem + (uint32_t)(a * L::TMEM_COLS);
 #pragma unroll 1
-            for (int r = 0; r < TROWS; r++) {
+                for (int r = 0; r < TROWS; r++) {
 #pragma unroll
-                for (int t = 0; t < 9; t++) {
-                    const int ky = t / 3, kx = t % 3;  // staged row and pixel offsets of the tap
+                    for (int t = 0; t < 9; t++) {
+                        const int ky = t / 3, kx = t % 3;  // staged row and pixel offsets of the tap
 #pragma unroll
-                    for (int h = 0; h < CINC / 2; h++) {
-                        const uint32_t a = xs + 2 * h * PLANE + (r + ky) * ROWB + kx * 16;
-                        const uint32_t bw = ws + (t * CINC + 2 * h) * N * 16;
-                        tc_mma(tmem + r * N, sdesc(a, PLANE, 128), sdesc(bw, N * 16, 128), idesc,
-                               (t | h) != 0 ? 1u : 0u);
+                        for (int h = 0; h < CINC / 2; h++) {
+                            const uint32_t aa = xs + 2 * h * PLANE + (r + ky) * ROWB + kx * 16;
+                            const uint32_t bw = ws + (t * CINC + 2 * h) * N * 16;
+                            tc_mma(acc + r * N, sdesc(aa, PLANE, 128), sdesc(bw, N * 16, 128), idesc,
+                                   (t | h) != 0 ? 1u : 0u);
+                        }
                     }
                 }
+                tc_commit(empty_bar(st));
+                tc_commit(accf_bar(a));
+                committed = i;
             }
-            tc_commit(bar_mma);
-        } else {
-            *flag = 1u;
-            atomicExch(status, 1);
-            mbar_wait(bar_in, 0);  // the copies in flight, once more (bounded)
+            // after an abort: the MMAs in flight, before TMEM is freed (bounded)
+            if (*flag != 0u && committed >= 0) mbar_wait(accf_bar(committed & 1), (uint32_t)((committed >> 1) & 1));
         }
-    }
-    __syncthreads();
-    if (*flag == 0u) {
-        const bool done = mbar_wait(bar_mma, 0);
-        if (!done) atomicExch(status, 2);
-        tc_fence_after();
-        const int px = x0 + warp * 32 + lane;
+    } else {
+        const int q = warp & 3;  // TMEM lane quadrant of this warp
+        constexpr int RH = TROWS / 2;
+        const int r0 = warp < 6 ? 0 : RH;  // this warp's rows: r0 .. r0 + RH - 1
+        float bs[EPI == EPI_MASK_BF16 ? 1 : N];
+        if constexpr (EPI != EPI_MASK_BF16) {
+#pragma unroll
+            for (int c = 0; c < N; c++) bs[c] = (EPI == EPI_LINEAR_F32 && c >= NOUTF) ? 0.0f : __ldg(bias + c);
+        }
+        for (int i = 0; i < ntl; i++) {
+            const int a = i & 1;
+            if (!mbar_wait_or_abort(accf_bar(a), (uint32_t)((i >> 1) & 1), flag)) {
+                if (*flag == 0u) fail(2);
+                break;
+            }
+            __syncwarp();
+            tc_fence_after();
+            int x0, y0, b;
+            tile_xyb(i, x0, y0, b);
+            const int px = x0 + q * 32 + lane;
 #pragma unroll 1
-        for (int r = 0; r < TROWS; r++) {
-            uint32_t v[N];
-            const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(r * N);
-            tc_ld16(ta, *reinterpret_cast<uint32_t(*)[16]>(&v[0]));
-            if constexpr (N == 32) tc_ld16(ta + 16, *reinterpret_cast<uint32_t(*)[16]>(&v[16]));
-            tc_wait_ld();
-            const int py = y0 + r;
-            if (!done || px >= W || py >= H) continue;
-            const long long p = ((long long)b * H + py) * W + px;
-            if constexpr (EPI == EPI_LINEAR_F32) {
-                float *yf = reinterpret_cast<float *>(y) + p * NOUTF;
+            for (int r = r0; r < r0 + RH; r++) {
+                uint32_t v[N];
+                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * L::TMEM_COLS + r * N);
+                tc_ld16(ta, *reinterpret_cast<uint32_t(*)[16]>(&v[0]));
+                if constexpr (N == 32) tc_ld16(ta + 16, *reinterpret_cast<uint32_t(*)[16]>(&v[16]));
+                tc_wait_ld();
+                if (r == r0 + RH - 1) {
+                    // the accumulator is read: release it to tile i + 2
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(acce_bar(a));
+                }
+                const int py = y0 + r;
+                if (px >= W || py >= H) continue;
+                const long long p = ((long long)b * H + py) * W + px;
+                if constexpr (EPI == EPI_LINEAR_F32) {
+                    float *yf = reinterpret_cast<float *>(y) + p * NOUTF;
 #pragma unroll
-                for (int c = 0; c < NOUTF; c++) yf[c] = __uint_as_float(v[c]) + __ldg(bias + c);
-            } else {
-                static_assert(EPI == EPI_LINEAR_F32 || N == 32, "BF16 outputs have 32 channels");
-                uint4 *yq = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(y) + p * 32);
-                if constexpr (EPI == EPI_RELU_BF16) {
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        float f[8];
-#pragma unroll
-                        for (int e = 0; e < 8; e++) f[e] = fmaxf(__uint_as_float(v[q * 8 + e]) + __ldg(bias + q * 8 + e), 0.0f);
-                        yq[q] = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7]));
-                    }
+                    for (int c = 0; c < NOUTF; c++) yf[c] = __uint_as_float(v[c]) + bs[c];
                 } else {
-                    const uint4 *aq = reinterpret_cast<const uint4 *>(act + p * 32);
+                    static_assert(EPI == EPI_LINEAR_F32 || N == 32, "BF16 outputs have 32 channels");
+                    uint4 *yq = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(y) + p * 32);
+                    if constexpr (EPI == EPI_RELU_BF16) {
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const uint4 m = __ldg(aq + q);
-                        const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
-                        float f[8];
+                        for (int qq = 0; qq < 4; qq++) {
+                            float f[8];
 #pragma unroll
-                        for (int e = 0; e < 4; e++) {
-                            f[2 * e] = lo_bf(mw[e]) > 0.0f ? __uint_as_float(v[q * 8 + 2 * e]) : 0.0f;
-                            f[2 * e + 1] = hi_bf(mw[e]) > 0.0f ? __uint_as_float(v[q * 8 + 2 * e + 1]) : 0.0f;
+                            for (int e = 0; e < 8; e++)
+                                f[e] = fmaxf(__uint_as_float(v[qq * 8 + e]) + bs[qq * 8 + e], 0.0f);
+                            yq[qq] = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]),
+                                                pack2(f[6], f[7]));
                         }
-                        yq[q] = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7]));
+                    } else {
+                        const uint4 *aq = reinterpret_cast<const uint4 *>(act + p * 32);
+#pragma unroll
+                        for (int qq = 0; qq < 4; qq++) {
+                            const uint4 m = __ldg(aq + qq);
+                            const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
+                            float f[8];
+#pragma unroll
+                            for (int e = 0; e < 4; e++) {
+                                f[2 * e] = lo_bf(mw[e]) > 0.0f ? __uint_as_float(v[qq * 8 + 2 * e]) : 0.0f;
+                                f[2 * e + 1] = hi_bf(mw[e]) > 0.0f ? __uint_as_float(v[qq * 8 + 2 * e + 1]) : 0.0f;
+                            }
+                            yq[qq] = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]),
+                                                pack2(f[6], f[7]));
+                        }
                     }
                 }
             }
@@ -272,9 +406,10 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 1) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)L::TMEM_COLS)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"((uint32_t)(2 * L::TMEM_COLS))
                      : "memory");
     }
 }
