@@ -366,7 +366,7 @@ def net_report(fw, size=1024, reps=20):
             "ms_train_iteration_batch8_128x128": ms_iter}
 
 
-def learned_report(fw, iters=4000, eval_coarse_steps=500):
+def learned_report(fw, iters=4000, eval_coarse_steps=500, unroll=1, every=2, scale=1):
     """The learned coarse-grid correction, at reduced training scale: pairs
     (one coarse step of 2 x dx against two fine steps, restricted) from
     seeded planar beaches, barred beaches and a shoal with JONSWAP Hs
@@ -405,10 +405,14 @@ def learned_report(fw, iters=4000, eval_coarse_steps=500):
 
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
-    train_cases = [barred(s) for s in (1, 2, 3, 4)] + [planar(s) for s in (11, 12, 13)] + [shoal(21)]
+    # scale x (4 barred beaches, 3 planar beaches of the ensemble's
+    # distribution, 1 shoal), seeds disjoint from the held-out 9 and 19
+    train_cases = ([barred(s) for s in range(1, 2 + 4 * scale) if s != 9][:4 * scale] +
+                   [planar(s) for s in range(11, 11 + 3 * scale) if s != 19] +
+                   [shoal(s) for s in range(21, 21 + scale)])
     X, T, Wm = [], [], []
     for c in train_cases:
-        x, t, w = L.make_pairs(c, 240, every=2)
+        x, t, w = L.make_pairs(c, 240, every=every, unroll=unroll)
         X.append(x)
         T.append(t)
         Wm.append(w)
@@ -467,6 +471,7 @@ def learned_report(fw, iters=4000, eval_coarse_steps=500):
     cs.close()
     net.close()
     return {"metric": "learned coarse-grid correction", "training_pairs": int(sum(a.shape[0] for a in X)),
+            "pairs_unroll": unroll, "pairs_every": every, "training_cases": len(train_cases),
             "training_iters": iters, "pairs_s": t_pairs, "train_s": t_train,
             "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-50:])),
             "evaluation": evals,
@@ -554,6 +559,13 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (no fw_autotune)")
     ap.add_argument("--tuning", default=None,
                     help="launch shapes as JSON (the config's launch_shapes of an earlier run) instead of fw_autotune")
+    ap.add_argument("--learned-unroll", type=int, default=1,
+                    help="learned report: coarse steps unrolled from each restricted fine start")
+    ap.add_argument("--learned-every", type=int, default=2,
+                    help="learned report: coarse steps between restricted fine starts")
+    ap.add_argument("--learned-scale", type=int, default=1,
+                    help="learned report: multiple of the 8 training cases")
+    ap.add_argument("--learned-iters", type=int, default=4000, help="learned report: Adam iterations")
     ap.add_argument("--net-report", action="store_true",
                     help="time the correction network's forward pass and training iteration")
     ap.add_argument("--learned-report", action="store_true",
@@ -572,7 +584,8 @@ def main():
         print(json.dumps(net_report(fw)), flush=True)
         return 0
     if args.learned_report:
-        print(json.dumps(learned_report(fw)), flush=True)
+        print(json.dumps(learned_report(fw, iters=args.learned_iters, unroll=args.learned_unroll,
+                                        every=args.learned_every, scale=args.learned_scale)), flush=True)
         return 0
     if args.precision_report:
         import torch

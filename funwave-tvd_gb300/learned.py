@@ -169,11 +169,18 @@ def _set_state(cs, eta, u, v, ubar, vbar, depth_c, mask):
     cs.exchange()
 
 
-def make_pairs(case, nsteps_c, precision="MIXED", every=1):
+def make_pairs(case, nsteps_c, precision="MIXED", every=1, unroll=1):
     """Training pairs from one fine run of case = (params, depth, phases)
     (params with DT_fixed): returns (x [K, N, M, 5], target [K, N, M, 3],
     wmask [K, N, M]) as numpy float32, the target already multiplied by
-    OUT_SCALE."""
+    OUT_SCALE.
+
+    Every `every` coarse steps the coarse twin starts from the restricted
+    fine state and then runs on its own for `unroll` steps; each of those
+    steps gives a pair: its input state (the restricted fine state first,
+    then states the coarse solver evolved itself, as in a corrected run) and
+    the difference between the restricted fine state one coarse step later
+    and the coarse step's result."""
     pf, depth, phases = case
     pf = with_defaults(pf)
     pc, depth_c = coarse_case(pf, depth)
@@ -186,27 +193,31 @@ def make_pairs(case, nsteps_c, precision="MIXED", every=1):
     def fine_state():
         return {n: restrict(_interior(fs.get(n))) for n in ("Eta", "U", "V", "Ubar", "Vbar")}
 
-    prev = fine_state()
-    prev_mask = _interior(cs.get("MASK"))
-    for k in range(nsteps_c):
-        t0 = fs.scalar("TIME")
+    # the restricted fine run at every coarse step (two fine steps each)
+    ref, times = [fine_state()], [fs.scalar("TIME")]
+    for _ in range(nsteps_c):
         fs.step(2)
-        cur = fine_state()
-        if k % every == 0:
-            dc = _interior(cs.get("Depth"))
-            mask = ((prev["Eta"] + dc) > 1e-3).astype(np.int32)
-            _set_state(cs, prev["Eta"], prev["U"], prev["V"], prev["Ubar"], prev["Vbar"], dc, mask)
-            cs.set_scalar("TIME", t0)
+        ref.append(fine_state())
+        times.append(fs.scalar("TIME"))
+    fs.close()
+    dc = _interior(cs.get("Depth"))
+    for start in range(0, nsteps_c - unroll + 1, every):
+        st = ref[start]
+        mask = ((st["Eta"] + dc) > 1e-3).astype(np.int32)
+        _set_state(cs, st["Eta"], st["U"], st["V"], st["Ubar"], st["Vbar"], dc, mask)
+        cs.set_scalar("TIME", times[start])
+        e_in, u_in, v_in = st["Eta"], st["U"], st["V"]
+        for k in range(unroll):
             cs.step(1)
             ec, uc, vc = (_interior(cs.get(n)) for n in ("Eta", "U", "V"))
             mc = _interior(cs.get("MASK"))
+            cur = ref[start + k + 1]
             wet = ((mask > 0) & (mc > 0)).astype(np.float32)
-            xs.append(features(prev["Eta"], prev["U"], prev["V"], dc, mask))
+            xs.append(features(e_in, u_in, v_in, dc, mask))
             tgt = np.stack([cur["Eta"] - ec, cur["U"] - uc, cur["V"] - vc], axis=-1) * OUT_SCALE
             ts.append(np.ascontiguousarray((tgt * wet[..., None]).transpose(1, 0, 2), dtype=np.float32))
             ws.append(np.ascontiguousarray(wet.T))
-        prev = cur
-    fs.close()
+            e_in, u_in, v_in, mask = ec, uc, vc, mc
     cs.close()
     return np.stack(xs), np.stack(ts), np.stack(ws)
 
