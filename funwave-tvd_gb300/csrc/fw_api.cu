@@ -68,6 +68,7 @@ template <typename T> bool find_field(fw_ctx *c, const char *name, FieldRef &r) 
         {"Q", f.Q, YFACE, 0}, {"Fy", f.Fy, YFACE, 0}, {"Gy", f.Gy, YFACE, 0}, {"MASK", f.MASK, CELL, 1},
         {"MASK9", f.MASK9, CELL, 1}, {"MASK_STRUC", f.MASK_STRUC, CELL, 1},
         {"HeightMin", f.Hmin, CELL, 0}, {"VelocityMax", f.Umax, CELL, 0}, {"MomentumFluxMax", f.MFmax, CELL, 0},
+        {"ROLLER_FLUX", f.ROLLER, CELL, 0}, {"UNDERTOW_U", f.UNDERTOW_U, CELL, 0}, {"UNDERTOW_V", f.UNDERTOW_V, CELL, 0},
         {"ETAmean", f.ETAmean, CELL, 0}, {"Umean", f.Umean, CELL, 0}, {"Vmean", f.Vmean, CELL, 0},
         {"ETA2mean", f.ETA2mean, CELL, 0}, {"SigWaveHeight", f.SigWH, CELL, 0},
         {"WaveHeightAve", f.WHave, CELL, 0}, {"WaveHeightRMS", f.WHrms, CELL, 0}, {"Emax", f.Emax, CELL, 0},
@@ -213,6 +214,11 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
     for (T **p : tf) *p = (T *)take(plane * sizeof(T));
     // statistics planes only when switched on
     if (g.track_hmin) f.Hmin = (T *)take(plane * sizeof(T));
+    if (g.track_roller) {
+        f.ROLLER = (T *)take(plane * sizeof(T));
+        f.UNDERTOW_U = (T *)take(plane * sizeof(T));
+        f.UNDERTOW_V = (T *)take(plane * sizeof(T));
+    }
     if (g.track_umax) f.Umax = (T *)take(plane * sizeof(T));
     if (g.track_mfmax) f.MFmax = (T *)take(plane * sizeof(T));
     if (g.stats) {
@@ -314,7 +320,7 @@ long long swap_state(fw_ctx *c) {
 
 // launch-shape candidates of the per-cell kernels (bx a multiple of 32,
 // at most 256 threads, as the kernels' launch bounds allow)
-const int CELL_CANDIDATES[][2] = {{32, 8}, {32, 4}, {64, 4}, {128, 2}, {64, 2}, {256, 1}};
+const int CELL_CANDIDATES[][2] = {{32, 8}, {32, 4}, {32, 2}, {64, 4}, {64, 2}, {128, 2}, {128, 1}, {256, 1}};
 const char *const TUNE_NAMES[fw::TK_N] = {"disp_a", "disp_b", "update", "post_mask_break", "maskmul"};
 std::mutex tune_mu;
 std::map<std::array<long long, 8>, std::array<int, FW_TUNE_LEN>> tune_cache;
@@ -325,9 +331,10 @@ bool tune_valid(const fw_ctx *c, const int *t) {
         if (bx < 32 || bx % 32 != 0 || by < 1 || bx * by > 256) return false;
     }
     const bool fp64 = c->p.precision == FW_PREC_FP64;
-    const int fx = t[fw::TUNE_FLUX], fyv = t[fw::TUNE_FLUX + 1];
-    if (fx != 8 && fx != 16) return false;
-    if (fp64 ? (fyv != 8 && fyv != 16) : (fyv != 16 && fyv != 32)) return false;
+    for (int d = 0; d < 2; d++) {
+        const int fy = t[fw::TUNE_FLUX + d];
+        if (fy != 8 && fy != 16 && (fp64 || fy != 32)) return false;
+    }
     return true;
 }
 
@@ -463,6 +470,7 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     g.gamma2 = p->dispersion ? p->gamma2 : 0.0;
     g.has_g2 = g.gamma2 > 0.0 ? 1 : 0;
     g.track_hmin = p->track_hmin;
+    g.track_roller = p->track_roller;
     g.track_umax = p->track_umax;
     g.track_mfmax = p->track_mfmax;
     g.steady_time = p->steady_time;

@@ -27,6 +27,7 @@ struct Grid {
     int nfreq;
     int has_g2;              // Gamma2 > 0 (the dispersive ETAx/ETAy exchange)
     int track_hmin, track_umax, track_mfmax, stats;  // statistics switches
+    int track_roller;        // BREAKING's roller flux and undertow (ROLLER / UNDERTOW output)
     double steady_time, t_intv_mean;
     double DX, DY;
     double gamma1, gamma2, gamma3, b1, b2, Beta_1, Beta_2;
@@ -75,6 +76,7 @@ struct Fields {
     T *ETAmean, *Umean, *Vmean, *ETAsum, *Usum, *Vsum, *ETA2sum, *ETA2mean, *SigWH, *Emax, *Emin, *HavgSum,
         *HrmsSum, *WHave, *WHrms, *NZU;
     T *kETAsum, *kUsum, *kVsum, *kETA2sum;  // Kahan compensations of the mixed path
+    T *ROLLER, *UNDERTOW_U, *UNDERTOW_V;    // breaker.F:316-339 (null unless tracked)
     uint8_t *MASK, *MASKn, *MASK9, *MASK_STRUC;
     T *rhs_x, *rhs_y;                 // tmp4 of GET_Eta_U_V_HU_HV
     double *ty, *tp, *tq, *tc;        // line-solver scratch

@@ -1899,6 +1899,33 @@ __device__ __forceinline__ T nu_value(const Grid &g, const Fields<T> &f, size_t 
     return (T)0 + GC(nu_bkg);
 }
 
+// roller flux and undertow of a breaking cell (breaker.F:316-339):
+// C1 = max(|ETAt|/tmp4, sqrt(g|H|)), R = min(|0.45 ETAt/max(C1,SMALL)|,
+// 0.1638), ROLLER = |C1 - |u|| R (eta - ETAmean), UNDERTOW = -ROLLER times
+// the direction cosines of ANGLE; 0.45 is a default-REAL literal and 0.1638
+// a _SP one, so both enter FP64 as their float values.  ETAmean is zero
+// until a mean is computed.
+template <typename T>
+__device__ __forceinline__ void roller_cell(const Grid &g, const Fields<T> &f, size_t id, T et) {
+    const T ex = f.ETAx[id], ey = f.ETAy[id];
+    const T tmp4 = tmax(fsqrt(ex * ex + ey * ey), (T)SMALL);
+    const T ANGLE = fatan2(-ey, -ex) * (T)180 / (T)PI_SP;
+    const T C1 = tmax(fabs_(et) / tmp4, fsqrt((T)GRAV * fabs_(f.H[id])));
+    T R = fabs_((T)(double)0.45f * et / tmax(C1, (T)SMALL));
+    R = tmin(R, (T)(double)0.1638f);
+    const T u = f.U[id], v = f.V[id];
+    const T em = g.stats ? f.ETAmean[id] : (T)0;
+    const T rf = fabs_(C1 - fsqrt(u * u + v * v)) * R * (f.Eta[id] - em);
+    f.ROLLER[id] = rf;
+    f.UNDERTOW_U[id] = -rf * fcos(ANGLE * (T)PI_SP / (T)180);
+    f.UNDERTOW_V[id] = -rf * fsin(ANGLE * (T)PI_SP / (T)180);
+}
+
+// the breaking branch of the viscosity (outside the wavemaker zone)
+template <typename T> __device__ __forceinline__ bool breaking_now(const Grid &g, const BrkLocal<T> &b, T age) {
+    return age > (T)0 && age < GC(T_brk) && b.et > b.tmp2;
+}
+
 template <typename T>
 __device__ __forceinline__ void break_cell(const Grid &g, const Fields<T> &f, int i, int j) {
     const size_t id = IDX(i, j);
@@ -1921,6 +1948,7 @@ __device__ __forceinline__ void break_cell(const Grid &g, const Fields<T> &f, in
         f.cand[slot] = i + j * g.pitch;
     }
     if (zone || !cand) f.nu[id] = nu_value(g, f, id, b, an, zone);
+    if (g.track_roller && !zone && !cand && breaking_now(g, b, an)) roller_cell(g, f, id, b.et);
 }
 
 template <typename T>
@@ -2030,6 +2058,7 @@ __global__ void __launch_bounds__(1024) k_break_b(Grid g, Fields<T> f) {
         if (in_wk_zone<T>(g, i, j)) continue;
         const BrkLocal<T> b = brk_local(g, f, id);
         f.nu[id] = nu_value(g, f, id, b, (T)N[id], false);
+        if (g.track_roller && breaking_now(g, b, (T)N[id])) roller_cell(g, f, id, b.et);
     }
     __syncthreads();
     if (threadIdx.x == 0) *f.ncand = 0;
@@ -2563,12 +2592,8 @@ template <typename T> void launch_dispersion(fw_ctx *c) {
     note(c);
 }
 
-// the compiled flux tile heights: x faces 8 or 16; y faces 16 or 32
-// (float), 8 or 16 (double, whose 32-high tile would not fit 48 KB)
-template <typename T, int DIR> static bool flux_fy_ok(int fy) {
-    if (DIR == 0) return fy == 8 || fy == 16;
-    return sizeof(T) == sizeof(float) ? (fy == 16 || fy == 32) : (fy == 8 || fy == 16);
-}
+// the compiled flux tile heights: 8, 16 or 32 faces in float; 8 or 16 in
+// double (a 32-high tile of doubles would not fit 48 KB)
 
 template <typename T, int DIR, int FY_> static void flux_at(fw_ctx *c) {
     k_flux<T, DIR, FY_><<<flux_grid<T, DIR, FY_>(c->g), B2D, 0, c->stream>>>(c->g, c->F<T>());
@@ -2576,15 +2601,13 @@ template <typename T, int DIR, int FY_> static void flux_at(fw_ctx *c) {
 
 template <typename T, int DIR> static void launch_flux(fw_ctx *c) {
     const int fy = c->tune[TUNE_FLUX + DIR];
-    if constexpr (DIR == 0) {
-        if (fy == 16) flux_at<T, 0, 16>(c);
-        else flux_at<T, 0, 8>(c);
-    } else if constexpr (sizeof(T) == sizeof(float)) {
-        if (fy == 16) flux_at<T, 1, 16>(c);
-        else flux_at<T, 1, 32>(c);
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (fy == 8) flux_at<T, DIR, 8>(c);
+        else if (fy == 16) flux_at<T, DIR, 16>(c);
+        else flux_at<T, DIR, 32>(c);
     } else {
-        if (fy == 8) flux_at<T, 1, 8>(c);
-        else flux_at<T, 1, 16>(c);
+        if (fy == 8) flux_at<T, DIR, 8>(c);
+        else flux_at<T, DIR, 16>(c);
     }
     note(c);
 }

@@ -12,7 +12,8 @@
 // the initial state is file 00001, init.F:631), one whole step per pass
 // (fw_step), CHECK_BLOWUP's dump to file 99999 (misc.F:394-433).  PREVIEW
 // (io.F:4304-4621) writes eta_NNNNN, u_NNNNN, v_NNNNN, mask_NNNNN (and
-// hmax_NNNNN with OUT_Hmax) in RESULT_FOLDER with PutFile's ASCII format
+// hmax_NNNNN with OUT_Hmax, roller_NNNNN with ROLLER, U_undertow_NNNNN and
+// V_undertow_NNNNN with UNDERTOW) in RESULT_FOLDER with PutFile's ASCII format
 // (Mglob values per line, E16.6E4, interior only, io.F:4895-4921; or
 // headerless binary with FIELD_IO_TYPE = BINARY), dep.out with the first
 // file, and appends "TIME DT" to time_dt.out.  STATIONS writes sta_NNNN
@@ -157,6 +158,7 @@ void fill_params(const Input &in, fw_params &p) {
     p.track_mfmax = in.flag("OUT_MFmax", 0);
     p.steady_time = in.num("STEADY_TIME", LARGE);
     p.t_intv_mean = in.num("T_INTV_mean", LARGE);
+    p.track_roller = (in.flag("ROLLER", 0) || in.flag("UNDERTOW", 0)) ? 1 : 0;
 }
 
 // DEPTH_TYPE DATA / FLAT / SLOPE (init.F:684-760), interior Mglob x Nglob,
@@ -343,6 +345,7 @@ int main(int argc, char **argv) {
     std::vector<int> mask((size_t)Mloc * Nloc);
     int icount = 0;
     const bool binary = upper(in.str("FIELD_IO_TYPE", "ASCII")) == "BINARY";
+    const bool out_roller = in.flag("ROLLER", 0) != 0, out_undertow = in.flag("UNDERTOW", 0) != 0;
     auto write_field = [&](const std::string &path) {
         return binary ? put_file_binary(path, full, p) : put_file(path, full, p);
     };
@@ -428,6 +431,13 @@ int main(int argc, char **argv) {
         write_field(numbered(dir, "mask", icount));
         if (p.track_hmax && fw_get_field(ctx, "HeightMax", full.data()) == FW_OK)
             write_field(numbered(dir, "hmax", icount));
+        // io.F:4461-4471: roller_NNNNN, U_undertow_NNNNN, V_undertow_NNNNN
+        if (out_roller && fw_get_field(ctx, "ROLLER_FLUX", full.data()) == FW_OK)
+            write_field(numbered(dir, "roller", icount));
+        if (out_undertow && fw_get_field(ctx, "UNDERTOW_U", full.data()) == FW_OK)
+            write_field(numbered(dir, "U_undertow", icount));
+        if (out_undertow && fw_get_field(ctx, "UNDERTOW_V", full.data()) == FW_OK)
+            write_field(numbered(dir, "V_undertow", icount));
         return FW_OK;
     };
 

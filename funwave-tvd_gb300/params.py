@@ -37,7 +37,7 @@ PARAM_DEFAULTS = {
     "SPREADING": "WRAPPED_NORMAL", "SPREADING_S": 10.0,
     "PRECISION": "FP64", "OUT_Hmax": False,
     # statistics (MAX_MIN_PROPERTY switches, MIXING_STUFF times)
-    "OUT_Hmin": False, "OUT_Umax": False, "OUT_MFmax": False,
+    "OUT_Hmin": False, "OUT_Umax": False, "OUT_MFmax": False, "ROLLER": False, "UNDERTOW": False,
     "STEADY_TIME": 999999.0, "T_INTV_mean": 999999.0,
 }
 

@@ -141,6 +141,7 @@ class FwParams(ctypes.Structure):
         ("track_hmax", ctypes.c_int),
         ("track_hmin", ctypes.c_int), ("track_umax", ctypes.c_int), ("track_mfmax", ctypes.c_int),
         ("steady_time", ctypes.c_double), ("t_intv_mean", ctypes.c_double),
+        ("track_roller", ctypes.c_int),
     ]
 
 
@@ -186,6 +187,8 @@ def params_struct(p, precision=None, device=0):
     prec = precision or p.get("PRECISION", "FP64")
     s.precision = {"FP64": 0, "MIXED": 1}[prec.upper()]
     s.device = int(device)
+    # ROLLER and UNDERTOW (output switches) both need the BREAKING diagnostics
+    s.track_roller = 1 if (p.get("ROLLER", False) or p.get("UNDERTOW", False)) else 0
     return s
 
 

@@ -92,6 +92,7 @@ typedef struct fw_params {
     int    track_hmin, track_umax, track_mfmax;  /* OUT_Hmin, OUT_Umax, OUT_MFmax (F) */
     double steady_time;           /* STEADY_TIME (LARGE): time means and wave heights from then on */
     double t_intv_mean;           /* T_INTV_mean (LARGE): averaging interval */
+    int    track_roller;          /* ROLLER or UNDERTOW output (F): BREAKING's ROLLER_FLUX, UNDERTOW_U/V */
 } fw_params;
 
 typedef struct fw_ctx fw_ctx;
@@ -226,8 +227,7 @@ void *fw_stream(fw_ctx *ctx);
 /* The tuning vector: FW_TUNE_LEN ints, (bx, by) thread-block shapes of the
  * per-cell kernels disp_a, disp_b, update, post_mask_break and maskmul
  * (bx a multiple of 32, bx*by <= 256), then the tile heights of the x-face
- * flux kernel (8 or 16) and of the y-face one (16 or 32 in MIXED, 8 or 16 in
- * FP64).  Every choice computes the same values bit for bit; only the speed
+ * and the y-face flux kernels (8, 16 or 32 in MIXED; 8 or 16 in FP64).  Every choice computes the same values bit for bit; only the speed
  * differs.  Defaults: 32 x 8 blocks, flux tiles 8 and 32 (16 in FP64). */
 #define FW_TUNE_LEN 12
 #define FW_TUNE_FRESH 1   /* fw_autotune flag: measure even if this shape was tuned before */

@@ -55,7 +55,7 @@ struct ofw_ctx {
         *DUxy, *DVxy, *DVyy, *Ut, *Vt, *Utx, *Vty, *Utxx, *Utxy, *Vtxy, *Vtyy,
         *DUtx, *DVty, *DUtxx, *DUtxy, *DVtxy, *DVtyy, *U4, *V4, *U1p, *V1p,
         *U1pp, *V1pp, *U2, *V2, *U3, *V3, *SourceX, *SourceY, *WaveMaker_Mass,
-        *AGE, *nu_break, *HeightMax;
+        *AGE, *nu_break, *HeightMax, *ROLLER_FLUX, *UNDERTOW_U, *UNDERTOW_V;
     /* statistics: MAX_MIN_PROPERTY and CALCULATE_MEAN */
     double T_sum;
     double *HeightMin, *VelocityMax, *MomentumFluxMax, *ETAmean, *Umean, *Vmean, *ETAsum, *Usum, *Vsum,
@@ -119,6 +119,7 @@ static const field_desc FIELDS[] = {
     FD(V4, 0), FD(U1p, 0), FD(V1p, 0), FD(U1pp, 0), FD(V1pp, 0), FD(U2, 0),
     FD(V2, 0), FD(U3, 0), FD(V3, 0), FD(SourceX, 0), FD(SourceY, 0),
     FD(WaveMaker_Mass, 0), FD(AGE, 0), FD(nu_break, 0), FD(HeightMax, 0),
+    FD(ROLLER_FLUX, 0), FD(UNDERTOW_U, 0), FD(UNDERTOW_V, 0),
     FD(HeightMin, 0), FD(VelocityMax, 0), FD(MomentumFluxMax, 0), FD(ETAmean, 0), FD(Umean, 0),
     FD(Vmean, 0), FD(ETAsum, 0), FD(Usum, 0), FD(Vsum, 0), FD(ETA2sum, 0), FD(ETA2mean, 0),
     FD(SigWaveHeight, 0), FD(Emax, 0), FD(Emin, 0), FD(HavgSum, 0), FD(HrmsSum, 0),
@@ -1458,6 +1459,16 @@ void ofw_wave_breaking(ofw_ctx *o) {
                 if (a > ZERO && a < T_brk && et > tmp2) {
                     double cap1 = 1.0 * (dmax(C2(o->Depth, I, J), mdf) + C2(o->Eta, I, J));
                     C2(o->nu_break, I, J) = cap1 * tmp2 + o->p.nu_bkg;
+                    /* roller and undertow (breaker.F:316-339); 0.45 is a
+                     * default-REAL literal, 0.1638 a _SP one */
+                    double C1 = dmax(fabs(et) / tmp4, sqrt(GRAV * fabs(Hc)));
+                    double R = fabs((double)0.45f * et / dmax(C1, SMALL));
+                    R = dmin(R, (double)0.1638f);
+                    double u = C2(o->U, I, J), v = C2(o->V, I, J);
+                    double rf = fabs(C1 - sqrt(u * u + v * v)) * R * (C2(o->Eta, I, J) - C2(o->ETAmean, I, J));
+                    C2(o->ROLLER_FLUX, I, J) = rf;
+                    C2(o->UNDERTOW_U, I, J) = -rf * cos(ANGLE * PI_SP / 180.0);
+                    C2(o->UNDERTOW_V, I, J) = -rf * sin(ANGLE * PI_SP / 180.0);
                 } else {
                     C2(o->nu_break, I, J) = ZERO + o->p.nu_bkg;
                 }
