@@ -895,6 +895,149 @@ int fw_ensemble_step(fw_ctx *const *ctxs, int n, int nsteps, int *status) {
     return first;
 }
 
+}  // extern "C"
+
+struct fw_ensemble {
+    std::vector<fw_ctx *> ctx;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    std::vector<cudaEvent_t> ready;  // one per run: its stream's earlier work
+    cudaGraphExec_t exec = nullptr;
+    std::vector<long long> states;   // swap_state of each run at capture
+    std::vector<std::array<int, FW_TUNE_LEN>> tunes;
+};
+
+namespace {
+
+bool ens_stale(const fw_ensemble *e) {
+    if (!e->exec) return true;
+    for (size_t k = 0; k < e->ctx.size(); k++) {
+        if (e->states[k] != swap_state(e->ctx[k])) return true;
+        if (std::memcmp(e->tunes[k].data(), e->ctx[k]->tune, sizeof(e->ctx[k]->tune)) != 0) return true;
+    }
+    return false;
+}
+
+// one parent graph whose child nodes are the runs' two-step captures
+int ens_build(fw_ensemble *e) {
+    if (e->exec) {
+        cudaGraphExecDestroy(e->exec);
+        e->exec = nullptr;
+    }
+    cudaGraph_t parent = nullptr;
+    cudaError_t err = cudaGraphCreate(&parent, 0);
+    for (size_t k = 0; k < e->ctx.size() && err == cudaSuccess; k++) {
+        fw_ctx *c = e->ctx[k];
+        cudaGraph_t g = nullptr;
+        err = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) break;
+        for (int s = 0; s < 2; s++) {
+            if (c->p.precision == FW_PREC_FP64) enqueue_step<double>(c);
+            else enqueue_step<float>(c);
+        }
+        err = cudaStreamEndCapture(c->stream, &g);
+        if (err != cudaSuccess) break;
+        cudaGraphNode_t node;
+        err = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, g);
+        cudaGraphDestroy(g);
+        e->states[k] = swap_state(c);
+        std::memcpy(e->tunes[k].data(), c->tune, sizeof(c->tune));
+    }
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&e->exec, parent, 0);
+    if (parent) cudaGraphDestroy(parent);
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        e->exec = nullptr;
+        return FW_ERR_CUDA;
+    }
+    return FW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fw_ensemble_create(fw_ctx *const *ctxs, int n, fw_ensemble **out) {
+    if (!ctxs || n <= 0 || !out) return FW_ERR_BAD_PARAM;
+    *out = nullptr;
+    for (int k = 0; k < n; k++) {
+        const int rc = check_ready(ctxs[k]);
+        if (rc != FW_OK) return rc;
+    }
+    fw_ensemble *e = new (std::nothrow) fw_ensemble();
+    if (!e) return FW_ERR_OOM;
+    e->ctx.assign(ctxs, ctxs + n);
+    e->states.assign(n, 0);
+    e->tunes.resize(n);
+    e->ready.assign(n, nullptr);
+    bool ok = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; k < n && ok; k++) ok = cudaEventCreateWithFlags(&e->ready[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        fw_ensemble_destroy(e);
+        return FW_ERR_CUDA;
+    }
+    *out = e;
+    return FW_OK;
+}
+
+int fw_ensemble_run(fw_ensemble *e, int nsteps, int *status) {
+    if (!e || nsteps < 0) return FW_ERR_BAD_PARAM;
+    const int n = (int)e->ctx.size();
+    for (int k = 0; k < n; k++) {
+        const int rc = check_ready(e->ctx[k]);
+        if (rc != FW_OK) return rc;
+        if (status) status[k] = FW_OK;
+    }
+    if (nsteps == 0) return FW_OK;
+    cudaError_t err = cudaSuccess;
+    if (nsteps >= 2) {
+        if (ens_stale(e)) {
+            const int rc = ens_build(e);
+            if (rc != FW_OK) return rc;
+        }
+        // the runs' earlier work, then the reset of their step maxima
+        for (int k = 0; k < n && err == cudaSuccess; k++) {
+            err = cudaEventRecord(e->ready[k], e->ctx[k]->stream);
+            if (err == cudaSuccess) err = cudaStreamWaitEvent(e->stream, e->ready[k], 0);
+            if (err == cudaSuccess)
+                err = cudaMemsetAsync(etamax_ptr(e->ctx[k]), 0, sizeof(unsigned long long), e->stream);
+        }
+        for (int s = 0; s + 2 <= nsteps && err == cudaSuccess; s += 2) err = cudaGraphLaunch(e->exec, e->stream);
+        if (err == cudaSuccess) err = cudaEventRecord(e->done, e->stream);
+        for (int k = 0; k < n && err == cudaSuccess; k++) err = cudaStreamWaitEvent(e->ctx[k]->stream, e->done, 0);
+        if (err != cudaSuccess) {
+            cudaGetLastError();
+            return FW_ERR_CUDA;
+        }
+    }
+    if (nsteps % 2) {
+        for (int k = 0; k < n; k++) {
+            const int rc = enqueue_steps(e->ctx[k], 1, nsteps == 1);
+            if (rc != FW_OK) return rc;
+        }
+    }
+    int first = FW_OK;
+    for (int k = 0; k < n; k++) {
+        const int rc = read_status(e->ctx[k], status ? &status[k] : nullptr);
+        if (rc != FW_OK && first == FW_OK) first = rc;
+    }
+    return first;
+}
+
+int fw_ensemble_destroy(fw_ensemble *e) {
+    if (!e) return FW_ERR_BAD_PARAM;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    for (cudaEvent_t ev : e->ready)
+        if (ev) cudaEventDestroy(ev);
+    if (e->done) cudaEventDestroy(e->done);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return FW_OK;
+}
+
 int fw_sync(fw_ctx *c) {
     if (!c) return FW_ERR_BAD_PARAM;
     return cuda_status(c, cudaStreamSynchronize(c->stream));

@@ -233,6 +233,9 @@ def load_library(path=None):
                                 ctypes.POINTER(dp)]
     L.fw_step_wait.argtypes = [vp, ctypes.POINTER(ip)]
     L.fw_ensemble_step.argtypes = [ctypes.POINTER(vp), ip, ip, ctypes.POINTER(ip)]
+    L.fw_ensemble_create.argtypes = [ctypes.POINTER(vp), ip, ctypes.POINTER(vp)]
+    L.fw_ensemble_run.argtypes = [vp, ip, ctypes.POINTER(ip)]
+    L.fw_ensemble_destroy.argtypes = [vp]
     L.fw_launch_count.argtypes = [vp]
     L.fw_launch_count.restype = ctypes.c_longlong
     L.fw_stream.argtypes = [vp]

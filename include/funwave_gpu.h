@@ -163,6 +163,20 @@ int fw_step_wait(fw_ctx *ctx, int *status);
  * waited for; status[k] as fw_end_step for run k.  Each run's results are
  * those of fw_step on it alone, bit for bit.  No reference counterpart. */
 int fw_ensemble_step(fw_ctx *const *ctxs, int n, int nsteps, int *status);
+/* The same ensemble as one launch per two steps: fw_ensemble_create captures
+ * every run's two-step graph as a child node of one parent CUDA graph (no
+ * edges between runs, so they execute concurrently), and fw_ensemble_run
+ * advances all runs by nsteps with one cudaGraphLaunch per two steps on the
+ * ensemble's own stream (an odd last step is enqueued per run).  The parent
+ * graph is rebuilt when a run's buffer state or launch shapes changed since
+ * it was captured.  Work queued earlier on a run's stream completes first,
+ * and work queued on it afterwards waits for the ensemble.  status[k] as in
+ * fw_ensemble_step; results equal fw_step on each run alone, bit for bit.
+ * The contexts must outlive the ensemble.  No reference counterpart. */
+typedef struct fw_ensemble fw_ensemble;
+int fw_ensemble_create(fw_ctx *const *ctxs, int n, fw_ensemble **out);
+int fw_ensemble_run(fw_ensemble *ens, int nsteps, int *status);
+int fw_ensemble_destroy(fw_ensemble *ens);
 /* Synchronise the context's stream. */
 int fw_sync(fw_ctx *ctx);
 

@@ -28,10 +28,12 @@ def test_max_runup_measure(fw):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["MIXED", "FP64"])
-def test_ensemble_equals_single_runs(fw, precision):
+@pytest.mark.parametrize("precision,single", [("MIXED", False), ("FP64", False), ("MIXED", True), ("FP64", True)])
+def test_ensemble_equals_single_runs(fw, precision, single):
+    """Members stepped together (round robin on their streams, or as one
+    parent graph per two steps) equal the same runs stepped alone."""
     members = fw.cases.ensemble_members(5, seed=7, nfreq=8, ntheta=4, cells_range=(48 * 48, 128 * 96))
-    ens = fw.Ensemble(members, precision=precision)
+    ens = fw.Ensemble(members, precision=precision, single_launch=single, autotune=single)
     st = ens.step(30)
     assert st == [0] * 5
     st = ens.step(11)  # an odd count as well
