@@ -1635,7 +1635,13 @@ __host__ __device__ __forceinline__ size_t lsx_smem_floats(int L, int P) {
     return (size_t)6 * (lsx_pad(L) + 1) + (size_t)L + 16 * (size_t)P;
 }
 
-template <typename T>
+// KPT > 0: lines of at most 256 x KPT cells; every global value a thread
+// needs later (the reconstruction's p, q and the residual's a, c pairs of
+// its cells k = tid + 256 j, the reduced rows and the chunk's spike ends)
+// is loaded into registers at the start, together with the staging loads,
+// so that the block waits for global memory once instead of once per phase.
+// KPT = 0: any length, loads where they are used.
+template <typename T, int KPT>
 __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePart lp, int clear_dirty) {
     extern __shared__ float shf[];
     const int l = blockIdx.x;
@@ -1657,10 +1663,39 @@ __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePa
     const size_t row = (size_t)j * g.pitch + g.ib;
     const T *rhs = f.rhs_x + row;
     const float *IT = f.fac_it[0] + row, *Pp = f.fac_p[0] + row, *Qq = f.fac_q[0] + row;
+    const float *AH = f.fac_ah[0] + row, *AL = f.fac_al[0] + row;
+    const float *CH = f.fac_ch[0] + row, *CL = f.fac_cl[0] + row;
     FacLine fl = fac_line(f.fac_red[0], lp, l);
     const int ch = threadIdx.x;
     const int s = ch * m;
     const int e = (ch == P - 1) ? L - 1 : s + m - 1;
+    const int n = 2 * P;
+    constexpr int KR = KPT > 0 ? KPT : 1;
+    float rP[KR], rQ[KR], rAH[KR], rAL[KR], rCH[KR], rCL[KR];
+    float lo_r = 0.0f, di_r = 0.0f, up_r = 0.0f, cs_r = 0.0f, ae_r = 0.0f;
+    if constexpr (KPT > 0) {
+#pragma unroll
+        for (int q = 0; q < KPT; q++) {
+            const int k = threadIdx.x + q * 256;
+            if (k < L) {
+                rP[q] = Pp[k];
+                rQ[q] = Qq[k];
+                rAH[q] = AH[k];
+                rAL[q] = AL[k];
+                rCH[q] = CH[k];
+                rCL[q] = CL[k];
+            }
+        }
+        if ((int)threadIdx.x < n) {
+            lo_r = fl.lo[threadIdx.x];
+            di_r = fl.di[threadIdx.x];
+            up_r = fl.up[threadIdx.x];
+        }
+        if (ch < P) {
+            cs_r = fl.cs[ch];
+            ae_r = fl.ae[ch];
+        }
+    }
     for (int k = threadIdx.x; k < L; k += blockDim.x) {
         const int q = lsx_pad(k);
         const float dv = (float)rhs[k] * IT[k];
@@ -1688,37 +1723,58 @@ __global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePa
                     yn = y[q] - CP[q] * yn;
                     y[q] = yn;
                 }
-                rs = rs - fl.cs[ch] * y[lsx_pad(s + 1)];
-                re = re - fl.ae[ch] * y[lsx_pad(e - 1)];
+                rs = rs - (KPT > 0 ? cs_r : fl.cs[ch]) * y[lsx_pad(s + 1)];
+                re = re - (KPT > 0 ? ae_r : fl.ae[ch]) * y[lsx_pad(e - 1)];
             }
             rr[2 * ch] = rs;
             rr[2 * ch + 1] = re;
         }
-        const int n = 2 * P;
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            pb[k] = fl.lo[k];
-            pb[n + k] = fl.di[k];
-            pb[2 * n + k] = fl.up[k];
+        if constexpr (KPT > 0) {
+            if ((int)threadIdx.x < n) {
+                pb[threadIdx.x] = lo_r;
+                pb[n + threadIdx.x] = di_r;
+                pb[2 * n + threadIdx.x] = up_r;
+            }
+        } else {
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
+                pb[k] = fl.lo[k];
+                pb[n + k] = fl.di[k];
+                pb[2 * n + k] = fl.up[k];
+            }
         }
         __syncthreads();
         pcr_solve(pb, pb + n, pb + 2 * n, rr, pb + 3 * n, pb + 4 * n, pb + 5 * n, pb + 6 * n, n);
-        for (int k = threadIdx.x; k < L; k += blockDim.x) {
+        auto recon = [&](int k, float p_, float q_) {
             const int c = min(lp.lgm >= 0 ? k >> lp.lgm : k / m, P - 1);
             const int cs = c * m, ce = (c == P - 1) ? L - 1 : cs + m - 1;
-            const float x = (k == cs) ? rr[2 * c]
-                          : (k == ce) ? rr[2 * c + 1]
-                                      : y[lsx_pad(k)] - Pp[k] * rr[2 * c] - Qq[k] * rr[2 * c + 1];
+            const float x = (k == cs) ? rr[2 * c] : (k == ce) ? rr[2 * c + 1] : y[lsx_pad(k)] - p_ * rr[2 * c] - q_ * rr[2 * c + 1];
             if (pass == 0) x0[k] = x;
             else f.U[row + k] = (T)(x0[k] + x);
+        };
+        if constexpr (KPT > 0) {
+#pragma unroll
+            for (int q = 0; q < KPT; q++) {
+                const int k = threadIdx.x + q * 256;
+                if (k < L) recon(k, rP[q], rQ[q]);
+            }
+        } else {
+            for (int k = threadIdx.x; k < L; k += blockDim.x) recon(k, Pp[k], Qq[k]);
         }
         __syncthreads();
         if (pass == 0) {
-            const float *AH = f.fac_ah[0] + row, *AL = f.fac_al[0] + row;
-            const float *CH = f.fac_ch[0] + row, *CL = f.fac_cl[0] + row;
-            for (int k = threadIdx.x; k < L; k += blockDim.x) {
+            auto resid = [&](int k, float ah, float al, float chv, float cl) {
                 const float xm = k > 0 ? x0[k - 1] : 0.0f, xp = k < L - 1 ? x0[k + 1] : 0.0f;
                 const int q = lsx_pad(k);
-                d[q] = residual(dn[q], x0[k], xm, xp, AH[k], AL[k], CH[k], CL[k]);
+                d[q] = residual(dn[q], x0[k], xm, xp, ah, al, chv, cl);
+            };
+            if constexpr (KPT > 0) {
+#pragma unroll
+                for (int q = 0; q < KPT; q++) {
+                    const int k = threadIdx.x + q * 256;
+                    if (k < L) resid(k, rAH[q], rAL[q], rCH[q], rCL[q]);
+                }
+            } else {
+                for (int k = threadIdx.x; k < L; k += blockDim.x) resid(k, AH[k], AL[k], CH[k], CL[k]);
             }
             __syncthreads();
         }
@@ -2640,9 +2696,10 @@ static bool launch_tri(fw_ctx *c, const LinePart &lp, bool fac = true, bool clea
         }
         const size_t smem = lsx_smem_floats(lp.L, lp.P) * sizeof(float);
         if (DIR == 0 && !PER && lp.P <= 256 && smem <= 200 * 1024) {
-            if (smem > 48 * 1024)
-                cudaFuncSetAttribute(k_linesolve_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_linesolve_x<T><<<lp.nlines, 256, smem, c->stream>>>(g, c->F<T>(), lp, clear_dirty ? 1 : 0);
+            // lines of up to 2048 cells keep their per-cell coefficients in registers
+            auto kern = lp.L <= 2048 ? k_linesolve_x<T, 8> : k_linesolve_x<T, 0>;
+            if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kern<<<lp.nlines, 256, smem, c->stream>>>(g, c->F<T>(), lp, clear_dirty ? 1 : 0);
             note(c);
             return clear_dirty;
         }
