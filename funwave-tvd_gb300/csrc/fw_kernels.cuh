@@ -1501,7 +1501,10 @@ template <int PASS> __device__ __forceinline__ float *red_rhs(double *red, const
     return (float *)red + (PASS == 0 ? 0 : (size_t)lp.nlines * 2 * lp.P);
 }
 
-template <typename T, int DIR, bool PER, int PASS>
+// M > 0: chunks of exactly M rows are walked in registers (all loads first,
+// the sweep values stored once); other chunks, and M = 0, walk the loop.
+// Both do the same operations in the same order.
+template <typename T, int DIR, bool PER, int PASS, int M>
 __global__ void __launch_bounds__(128) k_sol_a(Grid g, Fields<T> f, LinePart lp) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= lp.nlines * lp.P) return;
@@ -1531,6 +1534,42 @@ __global__ void __launch_bounds__(128) k_sol_a(Grid g, Fields<T> f, LinePart lp)
     line_cell<DIR>(g, l, e, i, j);
     const float de = dval(e, IDX(i, j));
     float rs = ds, re = de;
+    if constexpr (M > 2) {
+        if (e - s + 1 == M) {
+            const size_t stride = DIR == 0 ? 1 : (size_t)g.pitch;
+            line_cell<DIR>(g, l, s, i, j);
+            const size_t q0 = IDX(i, j);
+            float dv[M], av[M], lv[M], cv[M], yv[M];
+#pragma unroll
+            for (int k = 1; k < M - 1; k++) {
+                const size_t q = q0 + (size_t)k * stride;
+                dv[k] = dval(s + k, q);
+                av[k] = A_[q];
+                lv[k] = lr_[q];
+                cv[k] = cp_[q];
+            }
+            float yp = 0.0f;
+#pragma unroll
+            for (int k = 1; k < M - 1; k++) {
+                yp = dv[k] * av[k] - lv[k] * yp;
+                yv[k] = yp;
+            }
+            float yn = 0.0f;
+#pragma unroll
+            for (int k = M - 2; k >= 1; k--) {
+                yn = yv[k] - cv[k] * yn;
+                yv[k] = yn;
+            }
+#pragma unroll
+            for (int k = 1; k < M - 1; k++) ys[q0 + (size_t)k * stride] = yv[k];
+            rs = ds - fl.cs[ch] * yv[1];
+            re = de - fl.ae[ch] * yv[M - 2];
+            float *red = red_rhs<PASS>(f.red, lp) + ((size_t)l * 2 * lp.P + 2 * ch);
+            red[0] = rs;
+            red[1] = re;
+            return;
+        }
+    }
     if (e - s >= 2) {
         float yp = 0.0f;
         for (int k = s + 1; k <= e - 1; k++) {
@@ -1578,8 +1617,9 @@ __global__ void __launch_bounds__(512) k_sol_b(Grid g, Fields<T> f, LinePart lp)
     for (int k = threadIdx.x; k < n; k += blockDim.x) red[k] = PER ? r[k] + beta * fl.x2[k] : r[k];
 }
 
-// PASS 0: x0 -> tp scratch; PASS 1: out = x0 + correction
-template <typename T, int DIR, int PASS>
+// PASS 0: x0 -> tp scratch; PASS 1: out = x0 + correction.  M > 0: chunks
+// of exactly M rows with all loads first (as k_sol_a).
+template <typename T, int DIR, int PASS, int M>
 __global__ void __launch_bounds__(128) k_sol_c(Grid g, Fields<T> f, LinePart lp) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= lp.nlines * lp.P) return;
@@ -1593,6 +1633,28 @@ __global__ void __launch_bounds__(128) k_sol_c(Grid g, Fields<T> f, LinePart lp)
     const float *ys = (const float *)f.ty;
     float *x0 = (float *)f.tp;
     T *out = DIR == 0 ? f.U : f.V;
+    if constexpr (M > 2) {
+        if (e - s + 1 == M) {
+            const size_t stride = DIR == 0 ? 1 : (size_t)g.pitch;
+            int i, j;
+            line_cell<DIR>(g, l, s, i, j);
+            const size_t q0 = IDX(i, j);
+            float xv[M], x0v[M];
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const size_t q = q0 + (size_t)k * stride;
+                xv[k] = (k == 0) ? xs : (k == M - 1) ? xe : ys[q] - p_[q] * xs - q_[q] * xe;
+                if (PASS == 1) x0v[k] = x0[q];
+            }
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const size_t q = q0 + (size_t)k * stride;
+                if (PASS == 0) x0[q] = xv[k];
+                else out[q] = (T)(x0v[k] + xv[k]);
+            }
+            return;
+        }
+    }
     for (int k = s; k <= e; k++) {
         int i, j;
         line_cell<DIR>(g, l, k, i, j);
@@ -2704,15 +2766,27 @@ static bool launch_tri(fw_ctx *c, const LinePart &lp, bool fac = true, bool clea
             return clear_dirty;
         }
         const dim3 gi = grid2(g.Mglob, g.Nglob, B2D);
-        k_sol_a<T, DIR, PER, 0><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         const int nb = std::min(512, ((2 * lp.P + 31) / 32) * 32);
         const size_t sb = (size_t)16 * lp.P * sizeof(float);
-        k_sol_b<T, DIR, PER, 0><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
-        k_sol_c<T, DIR, 0><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        k_resid<T, DIR, PER><<<gi, B2D, 0, c->stream>>>(g, c->F<T>(), lp);
-        k_sol_a<T, DIR, PER, 1><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        k_sol_b<T, DIR, PER, 1><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
-        k_sol_c<T, DIR, 1><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        const unsigned ga = (unsigned)((nt + 127) / 128);
+        // chunks of 16 rows (lines of 512 cells and more) walk in registers
+        if (lp.m == 16) {
+            k_sol_a<T, DIR, PER, 0, 16><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_b<T, DIR, PER, 0><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_c<T, DIR, 0, 16><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_resid<T, DIR, PER><<<gi, B2D, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_a<T, DIR, PER, 1, 16><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_b<T, DIR, PER, 1><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_c<T, DIR, 1, 16><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        } else {
+            k_sol_a<T, DIR, PER, 0, 0><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_b<T, DIR, PER, 0><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_c<T, DIR, 0, 0><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_resid<T, DIR, PER><<<gi, B2D, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_a<T, DIR, PER, 1, 0><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_b<T, DIR, PER, 1><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_c<T, DIR, 1, 0><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+        }
         note(c, 7);
         return false;
     }
