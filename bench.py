@@ -55,6 +55,9 @@ KERNEL_BYTES = {
     "tri_x": lambda T: 2 * T + (40 if T == 4 else 10),
     "tri_y": lambda T: 2 * T + (40 if T == 4 else 10),
     "post": lambda T: 7 * T + 1 + 6 * T,  # U V H Ubar Vbar HU HV + MASK -> U V HU HV Ubar Vbar
+    # the fused GET_Eta_U_V_HU_HV tail + UPDATE_MASK + BREAKING (parallel part):
+    # U V H ETAT AGE Depth Eta + MASK MASK_STRUC MASK9 -> U V HU HV AGEn nu + MASKn MASK9
+    "post_mask_break": lambda T: 13 * T + 5,
     "mask": lambda T: 4 * T + 4 + 2 * T,  # Eta Depth Depthx Depthy + MASK MASK_STRUC -> MASKn MASK9 Depthx Depthy
     "break_a": lambda T: 8 * T + 2 * T,   # H ETAx ETAy ETAT Depth Eta AGE nu -> AGEn nu
     "maskmul": lambda T: 6 * T + 1 + 5 * T,
@@ -67,10 +70,10 @@ KERNEL_BYTES = {
 # numbers
 TRAFFIC_PER_UNIT_MIXED = {
     "tri_x": 48.6, "update": 137.0, "flux_x": 41.0, "flux_y": 41.6, "disp_b": 72.6, "disp_a": 42.7,
-    "maskmul": 30.8, "tri_y": 95.2,
+    "maskmul": 30.8, "tri_y": 95.2, "post_mask_break": 42.5,
 }
 # kernel launches per stage (tri_* count the partitioned solve as one)
-PER_STAGE = ["disp_a", "disp_b", "flux_x", "flux_y", "update", "tri_x", "tri_y", "post",
+PER_STAGE = ["disp_a", "disp_b", "flux_x", "flux_y", "update", "tri_x", "tri_y", "post_mask_break", "post",
              "mask", "break_a", "maskmul"]
 # whole-step algorithmic bytes per cell-step: the cross-stage state each of
 # the three stages must read and write once (61 reals + 6 mask bytes)

@@ -40,6 +40,12 @@ constexpr double GRAV = 9.81;
 constexpr double SMALL = 0.000001;
 constexpr double LARGE = 999999.0;
 
+// bring the cache line of p into L1 (no value, no register): later loads of
+// inputs that the compiler may not move above earlier stores then hit L1
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ double fsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float fsqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double fabs_(double x) { return fabs(x); }
@@ -739,6 +745,20 @@ __global__ void __launch_bounds__(256, 3) k_update(Grid g, Fields<T> f, T al, T 
     if (i < g.ib || i > g.ie || j < g.jb || j > g.je) {
         f.H[id] = f.Eta[id] * g3 + f.Depth[id];  // H = Eta*Gamma3+Depth on all cells
         return;
+    }
+    if constexpr (sizeof(T) == sizeof(float)) {
+        // the right-hand sides' inputs (rows j-1..j+1 of U, V, Depth, the
+        // masks), read after this kernel's stores
+        if (g.dispersion) {
+#pragma unroll
+            for (int b = -1; b <= 1; b++) {
+                prefetch_l1(f.U + IDX(i, j + b));
+                prefetch_l1(f.V + IDX(i, j + b));
+                prefetch_l1(f.Depth + IDX(i, j + b));
+            }
+            prefetch_l1(f.MASK9 + id);
+            prefetch_l1(f.MASK + id);
+        }
     }
     const T DX = GC(DX), DY = GC(DY);
     const T DT = DTV;
@@ -2088,6 +2108,13 @@ __global__ void __launch_bounds__(256) k_post_mask_break(Grid g, Fields<T> f) {
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i > g.Mloc || j > g.Nloc) return;
     if (i < g.Mloc && j < g.Nloc) {
+        // the breaking and mask parts' inputs, read after the post part's stores
+        const size_t id = IDX(i, j);
+        prefetch_l1(f.ETAT + id);
+        prefetch_l1(f.AGE + id);
+        prefetch_l1(f.Eta + id);
+        prefetch_l1(f.Depth + id);
+        prefetch_l1(f.MASK_STRUC + id);
         post_cell(g, f, i, j);
         break_cell(g, f, i, j);
     }
