@@ -477,15 +477,10 @@ def learned_report(fw, iters=4000, eval_coarse_steps=500, unroll=1, every=2, sca
     pc, dc = L.coarse_case(params, depth)
     cs = fw.Solver(fw.with_defaults(pc), precision="MIXED")
     cs.init(dc, phases=phases)
-    for _ in range(4):
-        cs.step_async(1)
-        net.correct(cs, wait=False)
+    net.correct_run(cs, 4)
     cs.sync()
     t1 = time.perf_counter()
-    for _ in range(20):
-        cs.step_async(1)
-        net.correct(cs, wait=False)
-    cs.sync()
+    net.correct_run(cs, 20)  # one graph replay per two (step + correction) pairs
     ms_coarse = (time.perf_counter() - t1) * 1e3 / 20
     cs.close()
     net.close()

@@ -897,6 +897,20 @@ int fw_ensemble_step(fw_ctx *const *ctxs, int n, int nsteps, int *status) {
 
 }  // extern "C"
 
+namespace fw {
+int enqueue_one_step(fw_ctx *c) {
+    if (c->p.precision == FW_PREC_FP64) enqueue_step<double>(c);
+    else enqueue_step<float>(c);
+    c->graph_ready = 0;
+    return finish(c);
+}
+int reset_step_max(fw_ctx *c) {
+    return cuda_status(c, cudaMemsetAsync(etamax_ptr(c), 0, sizeof(unsigned long long), c->stream));
+}
+int step_status(fw_ctx *c, int *status) { return read_status(c, status); }
+long long buffer_state(fw_ctx *c) { return swap_state(c); }
+}  // namespace fw
+
 struct fw_ensemble {
     std::vector<fw_ctx *> ctx;
     cudaStream_t stream = nullptr;

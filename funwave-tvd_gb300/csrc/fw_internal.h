@@ -169,5 +169,13 @@ struct fw_ctx {
     long long graph_state = 0;   // host buffer state the graph was captured with
     template <typename T> fw::Fields<T> &F();
 };
+namespace fw {
+// stepping pieces for other translation units (fw_api.cu)
+int enqueue_one_step(fw_ctx *c);          // one whole step on c->stream, no graph
+int reset_step_max(fw_ctx *c);            // CHECK_BLOWUP's maximum, before a run of steps
+int step_status(fw_ctx *c, int *status);  // waits for c->stream; FW_OK or the run's status
+long long buffer_state(fw_ctx *c);        // the host pointer state a captured step bakes in
+}  // namespace fw
+
 template <> inline fw::Fields<double> &fw_ctx::F<double>() { return fd; }
 template <> inline fw::Fields<float> &fw_ctx::F<float>() { return ff; }

@@ -276,6 +276,13 @@ struct fw_net {
     float *part = nullptr;
     double *loss = nullptr;
     float *corr_in = nullptr;   // fw_correct's input tensor
+    // fw_correct_run's graph of two (step + correction) pairs and what it was
+    // captured with
+    cudaGraphExec_t cexec = nullptr;
+    fw_ctx *cctx = nullptr;
+    long long cstate = 0;
+    int ctune[FW_TUNE_LEN] = {0};
+    double cmax = 0.0;
 };
 
 namespace {
@@ -360,19 +367,35 @@ bool act_map(CUtensorMap *m, const bf16 *base, int C, int B, int H, int W) {
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// the shared-memory size of one tensor-core convolution, set once (outside
+// any stream capture: fw_net_create sets every one the network uses)
+template <int CINC, int N, int EPI, int NOUTF> bool conv_attr() {
+    static bool attr = false;
+    if (!attr) {
+        using Lt = fwtc::Layout<CINC, N>;
+        if (cudaFuncSetAttribute(fwtc::k_conv_tc<CINC, N, EPI, NOUTF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 Lt::BYTES) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        attr = true;
+    }
+    return true;
+}
+
+bool conv_attrs_all() {
+    using namespace fwtc;
+    return conv_attr<2, 32, EPI_RELU_BF16, 0>() && conv_attr<4, 32, EPI_RELU_BF16, 0>() &&
+           conv_attr<4, 16, EPI_LINEAR_F32, NOUT>() && conv_attr<2, 32, EPI_MASK_BF16, 0>() &&
+           conv_attr<4, 32, EPI_MASK_BF16, 0>();
+}
+
 template <int CINC, int N, int EPI, int NOUTF>
 int conv_tc(const bf16 *x, int C, const bf16 *img, const float *bias, const bf16 *act, void *y, int B, int H, int W,
             int *status, cudaStream_t s) {
     using Lt = fwtc::Layout<CINC, N>;
     auto k = fwtc::k_conv_tc<CINC, N, EPI, NOUTF>;
-    static bool attr = false;
-    if (!attr) {
-        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, Lt::BYTES) != cudaSuccess) {
-            cudaGetLastError();
-            return FW_ERR_CUDA;
-        }
-        attr = true;
-    }
+    if (!conv_attr<CINC, N, EPI, NOUTF>()) return FW_ERR_CUDA;
     static int nsm = 0;
     if (!nsm) {
         int dev = 0;
@@ -454,22 +477,34 @@ int backward(fw_net *n, int B, int H, int W, cudaStream_t s) {
 }  // namespace
 
 namespace {
-template <typename T> int correct(fw_ctx *c, fw_net *n, double max_corr, int *applied) {
+// the correction's launches on the context's stream (no host wait, so a
+// stream capture may hold them); the workspace and images are ready
+template <typename T> int correct_enqueue(fw_ctx *c, fw_net *n, double max_corr) {
     const fw::Grid &g = c->g;
     fw::Fields<T> &f = c->F<T>();
+    const long long npix = (long long)g.Mglob * g.Nglob;
+    cudaStream_t s = c->stream;
+    const dim3 b(32, 8), gr((g.Mglob + 31) / 32, (g.Nglob + 7) / 8);
+    k_corr_input<T><<<gr, b, 0, s>>>(g, f, n->corr_in);
+    int rc = forward(n, n->corr_in, npix, 1, g.Nglob, g.Mglob, s);
+    if (rc != FW_OK) return rc;
+    double *sums = n->loss;  // 3 doubles of scratch after the loss slot
+    if (cudaMemsetAsync(sums, 0, 4 * sizeof(double), s) != cudaSuccess) return FW_ERR_CUDA;
+    k_corr_sums<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1);
+    k_corr_apply<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, max_corr);
+    return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
+}
+
+template <typename T> int correct(fw_ctx *c, fw_net *n, double max_corr, int *applied) {
+    const fw::Grid &g = c->g;
     const long long npix = (long long)g.Mglob * g.Nglob;
     int rc = ensure_ws(n, npix);
     if (rc != FW_OK) return rc;
     cudaStream_t s = c->stream;
-    const dim3 b(32, 8), gr((g.Mglob + 31) / 32, (g.Nglob + 7) / 8);
     if (!shape_ok(1, g.Nglob, g.Mglob)) return FW_ERR_BAD_PARAM;
-    k_corr_input<T><<<gr, b, 0, s>>>(g, f, n->corr_in);
-    rc = forward(n, n->corr_in, npix, 1, g.Nglob, g.Mglob, s);
+    rc = correct_enqueue<T>(c, n, max_corr);
     if (rc != FW_OK) return rc;
-    double *sums = n->loss;  // 3 doubles of scratch after the loss slot
-    cudaMemsetAsync(sums, 0, 4 * sizeof(double), s);
-    k_corr_sums<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1);
-    k_corr_apply<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, max_corr);
+    double *sums = n->loss;
     if (applied) {
         // only a caller that asks waits for the decision
         double h[4];
@@ -531,6 +566,7 @@ int fw_net_create(unsigned long long seed, fw_net **out) {
         ioff += img_elems(i);
     }
     ok = ok && cudaMalloc(&n->img, ioff * sizeof(bf16)) == cudaSuccess;
+    ok = ok && conv_attrs_all();
     ok = ok && cudaMemset(n->status, 0, sizeof(int)) == cudaSuccess;
     ok = ok && cudaMemcpy(n->w, h.data(), off * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
     ok = ok && cudaMemset(n->g, 0, off * sizeof(float)) == cudaSuccess && cudaMemset(n->m, 0, off * sizeof(float)) == cudaSuccess &&
@@ -552,6 +588,7 @@ int fw_net_destroy(fw_net *n) {
         if (p) cudaFree(p);
     if (n->loss) cudaFree(n->loss);
     if (n->img) cudaFree(n->img);
+    if (n->cexec) cudaGraphExecDestroy(n->cexec);
     if (n->status) cudaFree(n->status);
     delete n;
     return FW_OK;
@@ -618,6 +655,69 @@ int fw_net_adam(fw_net *n, float lr, float beta1, float beta2, float eps, void *
                                                                               (long long)n->nparam, lr, beta1,
                                                                               beta2, eps, c1, c2);
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
+}
+
+// nsteps of (fw_step + fw_correct without waiting), two pairs per replay
+// of a captured graph; status as fw_step's
+int fw_correct_run(fw_ctx *c, fw_net *n, int nsteps, double max_corr, int *status) {
+    if (!c || !n || !c->initialized || nsteps < 0) return FW_ERR_BAD_PARAM;
+    if (status) *status = FW_OK;
+    if (nsteps == 0) return FW_OK;
+    const fw::Grid &g = c->g;
+    const long long npix = (long long)g.Mglob * g.Nglob;
+    if (!shape_ok(1, g.Nglob, g.Mglob)) return FW_ERR_BAD_PARAM;
+    int rc = ensure_ws(n, npix);
+    if (rc != FW_OK) return rc;
+    const bool fp64 = c->p.precision == FW_PREC_FP64;
+    pack_images(n, c->stream);  // before any capture: the graph reads the images
+    if ((rc = fw::reset_step_max(c)) != FW_OK) return rc;
+    auto pair = [&]() -> int {
+        int r = fw::enqueue_one_step(c);
+        if (r == FW_OK) r = fp64 ? correct_enqueue<double>(c, n, max_corr) : correct_enqueue<float>(c, n, max_corr);
+        return r;
+    };
+    for (int s2 = 0; s2 + 2 <= nsteps; s2 += 2) {
+        const bool stale = !n->cexec || n->cctx != c || n->cstate != fw::buffer_state(c) ||
+                           std::memcmp(n->ctune, c->tune, sizeof(n->ctune)) != 0 || n->cmax != max_corr;
+        if (stale) {
+            if (n->cexec) cudaGraphExecDestroy(n->cexec);
+            n->cexec = nullptr;
+            const long long st = fw::buffer_state(c);
+            cudaGraph_t gr;
+            if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                cudaGetLastError();
+                return FW_ERR_CUDA;
+            }
+            int r1 = pair();
+            if (r1 == FW_OK) r1 = pair();
+            const cudaError_t e1 = cudaStreamEndCapture(c->stream, &gr);
+            if (r1 != FW_OK || e1 != cudaSuccess) {
+                cudaGetLastError();
+                if (e1 == cudaSuccess) cudaGraphDestroy(gr);
+                return r1 != FW_OK ? r1 : FW_ERR_CUDA;
+            }
+            const cudaError_t e2 = cudaGraphInstantiate(&n->cexec, gr, 0);
+            cudaGraphDestroy(gr);
+            if (e2 != cudaSuccess) {
+                cudaGetLastError();
+                n->cexec = nullptr;
+                return FW_ERR_CUDA;
+            }
+            n->cctx = c;
+            n->cstate = st;
+            std::memcpy(n->ctune, c->tune, sizeof(n->ctune));
+            n->cmax = max_corr;
+        }
+        if (cudaGraphLaunch(n->cexec, c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            return FW_ERR_CUDA;
+        }
+    }
+    if (nsteps % 2 && (rc = pair()) != FW_OK) return rc;
+    rc = fw::step_status(c, status);
+    int st = 0;
+    if (cudaMemcpy(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess || st != 0) return FW_ERR_CUDA;
+    return rc;
 }
 
 int fw_correct(fw_ctx *c, fw_net *n, double max_corr, int *applied) {

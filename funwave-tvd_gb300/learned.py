@@ -43,6 +43,7 @@ def _bind(L):
     L.fw_net_loss_grad.argtypes = [vp, vp, vp, vp, ip, ip, ip, ctypes.POINTER(ctypes.c_double), vp]
     L.fw_net_adam.argtypes = [vp, fp, fp, fp, fp, vp]
     L.fw_correct.argtypes = [vp, vp, ctypes.c_double, ctypes.POINTER(ip)]
+    L.fw_correct_run.argtypes = [vp, vp, ip, ctypes.c_double, ctypes.POINTER(ip)]
     return L
 
 
@@ -116,6 +117,14 @@ class Net:
         ap = ctypes.c_int()
         self._ck(self.L.fw_correct(solver.ctx, self.h, float(max_corr), ctypes.byref(ap)), "fw_correct")
         return bool(ap.value)
+
+    def correct_run(self, solver, nsteps, max_corr=0.2):
+        """nsteps of (step + correction) on the solver through fw_correct_run:
+        one graph replay per two pairs; returns the CHECK_BLOWUP status."""
+        st = ctypes.c_int()
+        self._ck(self.L.fw_correct_run(solver.ctx, self.h, int(nsteps), float(max_corr), ctypes.byref(st)),
+                 "fw_correct_run")
+        return st.value
 
     def _ck(self, rc, what):
         if rc != 0:

@@ -212,6 +212,12 @@ int fw_net_adam(fw_net *net, float lr, float beta1, float beta2, float eps, void
  * device: with applied == NULL the call only enqueues work on the context's
  * stream; with applied given it waits and reports the decision. */
 int fw_correct(fw_ctx *ctx, fw_net *net, double max_corr, int *applied);
+/* nsteps of (fw_step + fw_correct without waiting) on a coarse run, two
+ * pairs per replay of one captured CUDA graph; status as fw_step's.  The
+ * graph is captured again when the run, its buffer state, its launch
+ * shapes or max_corr change; new weights are packed before each call.  No
+ * reference counterpart. */
+int fw_correct_run(fw_ctx *ctx, fw_net *net, int nsteps, double max_corr, int *status);
 
 /* --- the reference's units, one call each (for coupling and parity) ---- */
 int fw_exchange(fw_ctx *ctx);            /* EXCHANGE        bc.F:426 */

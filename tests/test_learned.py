@@ -115,6 +115,32 @@ def test_gpu_forward_and_gradients_several_tiles(fw):
     net.close()
 
 
+@pytest.mark.gpu
+def test_correct_run_equals_step_and_correct(fw):
+    """fw_correct_run (graph replays of two step + correction pairs, and an
+    odd last pair) computes what stepping and correcting one by one does."""
+    case = _barred_case(fw, 5)
+    pc, dc = fw.learned.coarse_case(fw.with_defaults(case[0]), case[1])
+    net = fw.learned.Net(seed=7)
+    runs = []
+    for mode in ("loop", "graph"):
+        s = fw.Solver(fw.with_defaults(pc), precision="MIXED")
+        s.init(dc, phases=case[2])
+        if mode == "loop":
+            for _ in range(7):
+                s.step(1)
+                net.correct(s, wait=False)
+            s.sync()
+        else:
+            assert net.correct_run(s, 7) == 0
+        runs.append({n: s.get(n) for n in ("Eta", "U", "V", "Ubar", "Vbar", "MASK")})
+        s.close()
+    for name in runs[0]:
+        assert np.array_equal(runs[0][name], runs[1][name]), name
+    assert np.abs(runs[0]["Eta"]).max() > 0
+    net.close()
+
+
 def _barred_case(fw, seed, M=256, N=128):
     p, d, ph, _ = fw.cases.barred_beach(M, N, 1.0, seed=seed, wk_from_shore=150.0, nfreq=16, ntheta=4,
                                         shore_from_east=40.0, Hmo=0.8, Sponge_west_width=30.0)
