@@ -315,7 +315,7 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
         e1.record(ext)
         e1.synchronize()
         ms = e0.elapsed_time(e1)
-        out[prec] = {k: s.get(k)[3:-3, 3:-3] for k in ("Eta", "U", "V", "MASK", "HeightMax", "Umean", "Vmean")}
+        out[prec] = {k: s.get(k)[3:-3, 3:-3] for k in ("Eta", "U", "V", "MASK", "HeightMax", "Umean", "Vmean", "AGE")}
         out[prec]["TIME"] = s.scalar("TIME")
         out[prec]["steps"] = n
         out[prec]["rate"] = size * size * n / (ms * 1e-3)
@@ -325,6 +325,20 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
     cur_d = np.sqrt(d["Umean"] ** 2 + d["Vmean"] ** 2)
     du = np.sqrt((m["Umean"] - d["Umean"]) ** 2 + (m["Vmean"] - d["Vmean"]) ** 2)
     ru_m, ru_d = fw.max_runup(np.pad(m["HeightMax"], 3), depth), fw.max_runup(np.pad(d["HeightMax"], 3), depth)
+    # where the difference sits: cells breaking in either run (AGE > 0),
+    # widened by 4 cells on every side, against the rest of the wet cells
+    brk = (m["AGE"] > 0) | (d["AGE"] > 0)
+    zone = brk.copy()
+    for _ in range(4):
+        z = zone.copy()
+        z[1:, :] |= zone[:-1, :]
+        z[:-1, :] |= zone[1:, :]
+        z[:, 1:] |= zone[:, :-1]
+        z[:, :-1] |= zone[:, 1:]
+        zone = z
+    de2 = ((m["Eta"] - d["Eta"]) ** 2) * wet
+    quiet = wet & ~zone
+    ad = np.abs(m["Eta"] - d["Eta"])[wet]
     return {
         "metric": "mixed vs FP64 on the 4096x4096 barred beach", "grid": [size, size], "dx_m": 1.0,
         "rip_channels_y_m": rips, "t_end_s": t_end, "time_mixed_s": m["TIME"], "time_fp64_s": d["TIME"],
@@ -332,6 +346,10 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
         "eta_rms_m": float(np.sqrt(np.mean((m["Eta"] - d["Eta"])[wet] ** 2))),
         "eta_max_abs_m": float(np.abs(m["Eta"] - d["Eta"])[wet].max()),
         "eta_rms_signal_m": float(np.sqrt(np.mean(d["Eta"][wet] ** 2))),
+        "eta_rms_outside_breaking_m": float(np.sqrt(np.sum(de2[quiet]) / max(1, quiet.sum()))),
+        "breaking_zone_cells": int((wet & zone).sum()), "wet_cells": int(wet.sum()),
+        "share_of_squared_error_in_breaking_zone": float(np.sum(de2[zone]) / max(np.sum(de2), 1e-300)),
+        "eta_abs_diff_percentiles_m": {q: float(np.percentile(ad, float(q))) for q in ("50", "99", "99.9", "99.99")},
         "max_runup_mixed_m": ru_m, "max_runup_fp64_m": ru_d,
         "mean_current_rms_error_m_s": float(np.sqrt(np.mean(du[wet] ** 2))),
         "mean_current_rms_fp64_m_s": float(np.sqrt(np.mean(cur_d[wet] ** 2))),
