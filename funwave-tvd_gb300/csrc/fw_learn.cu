@@ -3,8 +3,8 @@
 // 32 channels; outputs corrections of eta, u, v), its training (forward,
 // backward, Adam) and its application to a running coarse context.
 //
-// Layout: activations channels-last (pixel-major, the channels of a pixel
-// contiguous, natural order), pixel p = x + y*W + b*W*H with x the grid's I
+// Layout: the network's FP32 inputs and outputs are channels-last
+// ([pixel][channel]), pixel p = x + y*W + b*W*H with x the grid's I
 // (cross-shore) direction.  Weights and activations are BF16 (weights
 // rounded from an FP32 master copy into packed images before use), every
 // sum accumulates in FP32, the weight gradients and the Adam moments are
@@ -15,7 +15,9 @@
 // the tap at (x+kx, y+ky).
 //
 // The forward convolutions and the data gradients of the backward pass run
-// on the tcgen05 tensor cores (fw_tc.cuh).  The backward pass carries the
+// on the tcgen05 tensor cores (fw_tc.cuh).  Their BF16 activations and
+// gradients are stored chunk-planar with a zero border (fwtc::act_idx); the
+// network's FP32 inputs and outputs are plain [pixel][channel].  The backward pass carries the
 // gradient of each hidden activation in BF16 with the ReLU mask already
 // applied (dy * [act > 0]), as the tensor-core data-gradient kernel writes
 // it; the weight gradients reduce those BF16 values in FP32.
@@ -60,10 +62,11 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // grid) and its masked BF16 dy are staged in shared memory, then every
 // thread adds its share of the 9*CIN*COUT + COUT entries over the tile.
 // Each of the WG_BLOCKS blocks walks many tiles and writes one partial;
-// k_wgrad_reduce adds the partials.  x has XC channels a pixel (the first
-// CIN used), dy DYC (the first COUT used).
+// k_wgrad_reduce adds the partials.  x and dy are padded chunk-planar
+// activations (fwtc::act_idx) with XCC and DYCC chunks (the first CIN and
+// COUT channels used).
 constexpr int TPX = 64;
-template <int CIN, int COUT, int XC, int DYC>
+template <int CIN, int COUT, int XCC, int DYCC>
 __global__ void __launch_bounds__(256) k_conv_wgrad(const bf16 *__restrict__ x, const bf16 *__restrict__ dy,
                                                     float *__restrict__ part, int B, int H, int W) {
     constexpr int E = 9 * CIN * COUT + COUT;
@@ -73,24 +76,25 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(const bf16 *__restrict__ x, 
     float acc[NE];
 #pragma unroll
     for (int r = 0; r < NE; r++) acc[r] = 0.0f;
+    const fwtc::ActGeom gx_{B, H, W, XCC}, gd_{B, H, W, DYCC};
     const int tiles_x = (W + TPX - 1) / TPX;
     const long long ntiles = (long long)B * H * tiles_x;
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int tx = (int)(tile % tiles_x);
         const long long row = tile / tiles_x;  // b*H + y
-        const int py = (int)(row % H);
+        const int py = (int)(row % H), pb = (int)(row / H);
         const int x0 = tx * TPX;
         __syncthreads();
         for (int e = threadIdx.x; e < 3 * (TPX + 2) * CIN; e += blockDim.x) {
             const int ci = e % CIN, c = (e / CIN) % (TPX + 2), r = e / (CIN * (TPX + 2));
             const int gx = x0 + c - 1, gy = py + r - 1;
             float v = 0.0f;
-            if (gx >= 0 && gx < W && gy >= 0 && gy < H) v = bf(x[((row + (r - 1)) * W + gx) * XC + ci]);
+            if (gx >= 0 && gx < W && gy >= 0 && gy < H) v = bf(x[8 * fwtc::act_idx(gx_, pb, gy, ci >> 3, gx) + (ci & 7)]);
             xs[r][c][ci] = v;
         }
         for (int e = threadIdx.x; e < TPX * COUT; e += blockDim.x) {
             const int co = e % COUT, t = e / COUT;
-            dys[t][co] = x0 + t < W ? bf(dy[(row * W + x0 + t) * DYC + co]) : 0.0f;
+            dys[t][co] = x0 + t < W ? bf(dy[8 * fwtc::act_idx(gd_, pb, py, co >> 3, x0 + t) + (co & 7)]) : 0.0f;
         }
         __syncthreads();
 #pragma unroll
@@ -125,23 +129,28 @@ __global__ void k_wgrad_reduce(const float *part, int nblocks, int E, float *gw,
     else gb[e - nw] = s;
 }
 
-// inputs: FP32 [npix][5] -> BF16 [npix][16] (eleven zero channels)
-__global__ void k_pack_input(const float *in, bf16 *x, long long npix) {
+// inputs: FP32 [npix][5] -> the padded BF16 input of 2 chunks (channels
+// 5..15 zero)
+__global__ void k_pack_input(const float *in, bf16 *x, int B, int H, int W) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npix) return;
+    if (p >= (long long)B * H * W) return;
+    const int px = (int)(p % W), py = (int)((p / W) % H), pb = (int)(p / ((long long)W * H));
     float v[NIN];
 #pragma unroll
     for (int c = 0; c < NIN; c++) v[c] = in[p * NIN + c];
-    uint4 *xq = reinterpret_cast<uint4 *>(x + p * XC0);
-    xq[0] = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], 0.0f), 0u);
-    xq[1] = make_uint4(0u, 0u, 0u, 0u);
+    const fwtc::ActGeom g{B, H, W, XC0 / 8};
+    uint4 *xq = reinterpret_cast<uint4 *>(x);
+    const long long o = fwtc::act_idx(g, pb, py, 0, px);
+    xq[o] = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], 0.0f), 0u);
+    xq[o + W + 2] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 // masked mean squared error and its gradient w.r.t. the output, stored as
-// BF16 [npix][16] (channels 3..15 zero)
-__global__ void k_loss(const float *out, const float *target, const float *wmask, long long npix, float inv_n,
+// a padded BF16 activation of 2 chunks (channels 3..15 zero)
+__global__ void k_loss(const float *out, const float *target, const float *wmask, int B, int H, int W, float inv_n,
                        bf16 *dy, double *loss) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long npix = (long long)B * H * W;
     float l = 0.0f;
     if (p < npix) {
         const float m = wmask[p];
@@ -151,9 +160,12 @@ __global__ void k_loss(const float *out, const float *target, const float *wmask
             l += m * d * d;
             g[c] = 2.0f * m * d * inv_n;
         }
-        uint4 *dq = reinterpret_cast<uint4 *>(dy + p * GC3);
-        dq[0] = make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], 0.0f), 0u, 0u);
-        dq[1] = make_uint4(0u, 0u, 0u, 0u);
+        const int px = (int)(p % W), py = (int)((p / W) % H), pb = (int)(p / ((long long)W * H));
+        const fwtc::ActGeom ga{B, H, W, GC3 / 8};
+        uint4 *dq = reinterpret_cast<uint4 *>(dy);
+        const long long o = fwtc::act_idx(ga, pb, py, 0, px);
+        dq[o] = make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], 0.0f), 0u, 0u);
+        dq[o + W + 2] = make_uint4(0u, 0u, 0u, 0u);
     }
     for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, (double)(l * inv_n));
@@ -267,12 +279,16 @@ struct fw_net {
     size_t img_off[NL + 3] = {0};
     unsigned long long wver = 1, img_ver = 0;
     int *status = nullptr;      // set by a tensor-core kernel whose bounded wait expired
-    // workspace for npix_cap pixels
+    // workspace: FP32 buffers for npix_cap pixels; padded BF16 activations
+    // (fwtc::act_idx) of cap16 / cap32 bytes, laid out for the batch shape
+    // sB x sH x sW (their zero borders are set when the shape changes)
     long long npix_cap = 0;
-    bf16 *act[NL] = {nullptr};  // act[0] = packed input [16 ch], act[l] = output of layer l-1 (l = 1..3)
+    size_t cap16 = 0, cap32 = 0;
+    int sB = 0, sH = 0, sW = 0;
+    bf16 *act[NL] = {nullptr};  // act[0] = packed input (2 chunks), act[l] = output of layer l-1 (4 chunks)
     float *out = nullptr;       // output of the last layer, FP32 [npix][3]
-    bf16 *gout = nullptr;       // gradient of the output, BF16 [npix][16]
-    bf16 *gbuf[2] = {nullptr, nullptr};  // masked gradients of hidden activations, BF16 [npix][32]
+    bf16 *gout = nullptr;       // gradient of the output (2 chunks)
+    bf16 *gbuf[2] = {nullptr, nullptr};  // masked gradients of hidden activations (4 chunks)
     float *part = nullptr;
     double *loss = nullptr;
     float *corr_in = nullptr;   // fw_correct's input tensor
@@ -308,64 +324,52 @@ void free_ws(fw_net *n) {
     n->corr_in = nullptr;
     n->gout = nullptr;
     n->npix_cap = 0;
+    n->cap16 = n->cap32 = 0;
+    n->sB = n->sH = n->sW = 0;
 }
 
-int ensure_ws(fw_net *n, long long npix) {
-    if (npix <= n->npix_cap) return FW_OK;
-    free_ws(n);
-    bool ok = cudaMalloc(&n->act[0], (size_t)npix * XC0 * sizeof(bf16)) == cudaSuccess;
-    for (int l = 1; l < NL && ok; l++) ok = cudaMalloc(&n->act[l], (size_t)npix * HID * sizeof(bf16)) == cudaSuccess;
-    ok = ok && cudaMalloc(&n->out, (size_t)npix * NOUT * sizeof(float)) == cudaSuccess;
-    ok = ok && cudaMalloc(&n->gout, (size_t)npix * GC3 * sizeof(bf16)) == cudaSuccess;
-    for (int k = 0; k < 2 && ok; k++) ok = cudaMalloc(&n->gbuf[k], (size_t)npix * HID * sizeof(bf16)) == cudaSuccess;
-    ok = ok && cudaMalloc(&n->corr_in, (size_t)npix * NIN * sizeof(float)) == cudaSuccess;
-    if (!ok) {
-        cudaGetLastError();
+// buffers for a batch of B images of H x W; a new shape zeroes the padded
+// activations (their borders are the convolutions' zero padding)
+int ensure_ws(fw_net *n, int B, int H, int W, cudaStream_t s) {
+    const long long npix = (long long)B * H * W;
+    const size_t need16 = fwtc::act_bytes(fwtc::ActGeom{B, H, W, 2});
+    const size_t need32 = fwtc::act_bytes(fwtc::ActGeom{B, H, W, 4});
+    if (npix > n->npix_cap || need16 > n->cap16 || need32 > n->cap32) {
+        const long long np = std::max(npix, n->npix_cap);
+        const size_t c16 = std::max(need16, n->cap16), c32 = std::max(need32, n->cap32);
         free_ws(n);
-        return FW_ERR_OOM;
+        bool ok = cudaMalloc(&n->act[0], c16) == cudaSuccess;
+        for (int l = 1; l < NL && ok; l++) ok = cudaMalloc(&n->act[l], c32) == cudaSuccess;
+        ok = ok && cudaMalloc(&n->out, (size_t)np * NOUT * sizeof(float)) == cudaSuccess;
+        ok = ok && cudaMalloc(&n->gout, c16) == cudaSuccess;
+        for (int k = 0; k < 2 && ok; k++) ok = cudaMalloc(&n->gbuf[k], c32) == cudaSuccess;
+        ok = ok && cudaMalloc(&n->corr_in, (size_t)np * NIN * sizeof(float)) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            free_ws(n);
+            return FW_ERR_OOM;
+        }
+        n->npix_cap = np;
+        n->cap16 = c16;
+        n->cap32 = c32;
     }
-    n->npix_cap = npix;
+    if (n->sB != B || n->sH != H || n->sW != W) {
+        bool ok = cudaMemsetAsync(n->act[0], 0, n->cap16, s) == cudaSuccess &&
+                  cudaMemsetAsync(n->gout, 0, n->cap16, s) == cudaSuccess;
+        for (int l = 1; l < NL && ok; l++) ok = cudaMemsetAsync(n->act[l], 0, n->cap32, s) == cudaSuccess;
+        for (int k = 0; k < 2 && ok; k++) ok = cudaMemsetAsync(n->gbuf[k], 0, n->cap32, s) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            return FW_ERR_CUDA;
+        }
+        n->sB = B;
+        n->sH = H;
+        n->sW = W;
+    }
     return FW_OK;
 }
 
 unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
-
-// cuTensorMapEncodeTiled through the runtime's driver entry point (no
-// link against the driver library)
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-    static EncodeTiledFn fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (EncodeTiledFn)p;
-        else
-            cudaGetLastError();
-    }
-    return fn;
-}
-
-// tensor map of a BF16 activation [B][H][W][C]: boxes of 8 channels x 130
-// pixels x (TROWS + 2) rows of one image, zero outside the image
-bool act_map(CUtensorMap *m, const bf16 *base, int C, int B, int H, int W) {
-    EncodeTiledFn f = encode_fn();
-    if (!f) return false;
-    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
-    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
-    const cuuint32_t box[4] = {8, (cuuint32_t)fwtc::HPX, (cuuint32_t)(fwtc::TROWS + 2), 1};
-    const cuuint32_t es[4] = {1, 1, 1, 1};
-    return f(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(base), dims, strides, box, es,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
 
 // the shared-memory size of one tensor-core convolution, set once (outside
 // any stream capture: fw_net_create sets every one the network uses)
@@ -391,7 +395,7 @@ bool conv_attrs_all() {
 }
 
 template <int CINC, int N, int EPI, int NOUTF>
-int conv_tc(const bf16 *x, int C, const bf16 *img, const float *bias, const bf16 *act, void *y, int B, int H, int W,
+int conv_tc(const bf16 *x, const bf16 *img, const float *bias, const bf16 *act, void *y, int B, int H, int W,
             int *status, cudaStream_t s) {
     using Lt = fwtc::Layout<CINC, N>;
     auto k = fwtc::k_conv_tc<CINC, N, EPI, NOUTF>;
@@ -404,11 +408,9 @@ int conv_tc(const bf16 *x, int C, const bf16 *img, const float *bias, const bf16
             return FW_ERR_CUDA;
         }
     }
-    CUtensorMap m;
-    if (!act_map(&m, x, C, B, H, W)) return FW_ERR_CUDA;
     const long long ntiles = (long long)((W + fwtc::TPX - 1) / fwtc::TPX) * ((H + fwtc::TROWS - 1) / fwtc::TROWS) * B;
     const unsigned grid = (unsigned)std::min<long long>(ntiles, (long long)nsm * Lt::PER_SM);
-    k<<<grid, 64 + 32 * fwtc::EPI_WARPS, Lt::BYTES, s>>>(m, img, bias, act, y, H, W, B, status);
+    k<<<grid, 64 + 32 * fwtc::EPI_WARPS, Lt::BYTES, s>>>(x, img, bias, act, y, H, W, B, status);
     return FW_OK;
 }
 
@@ -432,23 +434,23 @@ void pack_images(fw_net *n, cudaStream_t s) {
 int forward(fw_net *n, const float *in, long long npix, int B, int H, int W, cudaStream_t s) {
     using namespace fwtc;
     pack_images(n, s);
-    k_pack_input<<<nblk(npix, 256), 256, 0, s>>>(in, n->act[0], npix);
+    k_pack_input<<<nblk(npix, 256), 256, 0, s>>>(in, n->act[0], B, H, W);
     const bf16 *im = n->img;
-    int rc = conv_tc<2, 32, EPI_RELU_BF16, 0>(n->act[0], XC0, im + n->img_off[0], n->w + n->boff[0], nullptr,
+    int rc = conv_tc<2, 32, EPI_RELU_BF16, 0>(n->act[0], im + n->img_off[0], n->w + n->boff[0], nullptr,
                                               n->act[1], B, H, W, n->status, s);
     for (int l = 1; l < 3 && rc == FW_OK; l++)
-        rc = conv_tc<4, 32, EPI_RELU_BF16, 0>(n->act[l], HID, im + n->img_off[l], n->w + n->boff[l], nullptr,
+        rc = conv_tc<4, 32, EPI_RELU_BF16, 0>(n->act[l], im + n->img_off[l], n->w + n->boff[l], nullptr,
                                               n->act[l + 1], B, H, W, n->status, s);
     if (rc == FW_OK)
-        rc = conv_tc<4, 16, EPI_LINEAR_F32, NOUT>(n->act[3], HID, im + n->img_off[3], n->w + n->boff[3], nullptr,
+        rc = conv_tc<4, 16, EPI_LINEAR_F32, NOUT>(n->act[3], im + n->img_off[3], n->w + n->boff[3], nullptr,
                                                   n->out, B, H, W, n->status, s);
     return rc;
 }
 
-template <int CIN, int COUT, int XC, int DYC>
+template <int CIN, int COUT, int XCC, int DYCC>
 void wgrad(fw_net *n, int l, const bf16 *x, const bf16 *dy, int B, int H, int W, cudaStream_t s) {
     constexpr int E = 9 * CIN * COUT + COUT;
-    k_conv_wgrad<CIN, COUT, XC, DYC><<<WG_BLOCKS, 256, 0, s>>>(x, dy, n->part, B, H, W);
+    k_conv_wgrad<CIN, COUT, XCC, DYCC><<<WG_BLOCKS, 256, 0, s>>>(x, dy, n->part, B, H, W);
     k_wgrad_reduce<<<nblk(E, 256), 256, 0, s>>>(n->part, WG_BLOCKS, E, n->g + n->woff[l], n->g + n->boff[l],
                                                  9 * CIN * COUT);
 }
@@ -458,18 +460,18 @@ int backward(fw_net *n, int B, int H, int W, cudaStream_t s) {
     using namespace fwtc;
     const bf16 *im = n->img;
     bf16 *ga = n->gbuf[0], *gb = n->gbuf[1];
-    wgrad<HID, NOUT, HID, GC3>(n, 3, n->act[3], n->gout, B, H, W, s);
+    wgrad<HID, NOUT, HID / 8, GC3 / 8>(n, 3, n->act[3], n->gout, B, H, W, s);
     // gradient of act[3] (the output of layer 2), masked by its ReLU
-    int rc = conv_tc<2, 32, EPI_MASK_BF16, 0>(n->gout, GC3, im + n->img_off[NL + 2], nullptr, n->act[3], ga, B, H, W,
+    int rc = conv_tc<2, 32, EPI_MASK_BF16, 0>(n->gout, im + n->img_off[NL + 2], nullptr, n->act[3], ga, B, H, W,
                                               n->status, s);
     for (int l = 2; l >= 1 && rc == FW_OK; l--) {
-        wgrad<HID, HID, HID, HID>(n, l, n->act[l], ga, B, H, W, s);
-        rc = conv_tc<4, 32, EPI_MASK_BF16, 0>(ga, HID, im + n->img_off[NL + l - 1], nullptr, n->act[l], gb, B, H, W,
+        wgrad<HID, HID, HID / 8, HID / 8>(n, l, n->act[l], ga, B, H, W, s);
+        rc = conv_tc<4, 32, EPI_MASK_BF16, 0>(ga, im + n->img_off[NL + l - 1], nullptr, n->act[l], gb, B, H, W,
                                               n->status, s);
         std::swap(ga, gb);
     }
     if (rc != FW_OK) return rc;
-    wgrad<CIN0, HID, XC0, HID>(n, 0, n->act[0], ga, B, H, W, s);
+    wgrad<CIN0, HID, XC0 / 8, HID / 8>(n, 0, n->act[0], ga, B, H, W, s);
     k_zero_pad_grad<<<nblk(9 * CIN0 * HID, 256), 256, 0, s>>>(n->g + n->woff[0]);
     return FW_OK;
 }
@@ -497,11 +499,10 @@ template <typename T> int correct_enqueue(fw_ctx *c, fw_net *n, double max_corr)
 
 template <typename T> int correct(fw_ctx *c, fw_net *n, double max_corr, int *applied) {
     const fw::Grid &g = c->g;
-    const long long npix = (long long)g.Mglob * g.Nglob;
-    int rc = ensure_ws(n, npix);
-    if (rc != FW_OK) return rc;
-    cudaStream_t s = c->stream;
     if (!shape_ok(1, g.Nglob, g.Mglob)) return FW_ERR_BAD_PARAM;
+    cudaStream_t s = c->stream;
+    int rc = ensure_ws(n, 1, g.Nglob, g.Mglob, s);
+    if (rc != FW_OK) return rc;
     rc = correct_enqueue<T>(c, n, max_corr);
     if (rc != FW_OK) return rc;
     double *sums = n->loss;
@@ -615,9 +616,9 @@ int fw_net_get_grads(fw_net *n, float *host) {
 int fw_net_forward(fw_net *n, const float *x, int B, int H, int W, float *y, void *stream) {
     if (!n || !x || !y || !shape_ok(B, H, W)) return FW_ERR_BAD_PARAM;
     const long long npix = (long long)B * H * W;
-    int rc = ensure_ws(n, npix);
-    if (rc != FW_OK) return rc;
     cudaStream_t s = (cudaStream_t)stream;
+    int rc = ensure_ws(n, B, H, W, s);
+    if (rc != FW_OK) return rc;
     rc = forward(n, x, npix, B, H, W, s);
     if (rc != FW_OK) return rc;
     cudaMemcpyAsync(y, n->out, (size_t)npix * NOUT * sizeof(float), cudaMemcpyDeviceToDevice, s);
@@ -628,13 +629,13 @@ int fw_net_loss_grad(fw_net *n, const float *x, const float *target, const float
                      double *loss, void *stream) {
     if (!n || !x || !target || !wmask || !shape_ok(B, H, W)) return FW_ERR_BAD_PARAM;
     const long long npix = (long long)B * H * W;
-    int rc = ensure_ws(n, npix);
-    if (rc != FW_OK) return rc;
     cudaStream_t s = (cudaStream_t)stream;
+    int rc = ensure_ws(n, B, H, W, s);
+    if (rc != FW_OK) return rc;
     rc = forward(n, x, npix, B, H, W, s);
     if (rc != FW_OK) return rc;
     cudaMemsetAsync(n->loss, 0, sizeof(double), s);
-    k_loss<<<nblk(npix, 256), 256, 0, s>>>(n->out, target, wmask, npix, 1.0f / (float)npix, n->gout, n->loss);
+    k_loss<<<nblk(npix, 256), 256, 0, s>>>(n->out, target, wmask, B, H, W, 1.0f / (float)npix, n->gout, n->loss);
     rc = backward(n, B, H, W, s);
     if (rc != FW_OK) return rc;
     if (loss) {
@@ -664,9 +665,8 @@ int fw_correct_run(fw_ctx *c, fw_net *n, int nsteps, double max_corr, int *statu
     if (status) *status = FW_OK;
     if (nsteps == 0) return FW_OK;
     const fw::Grid &g = c->g;
-    const long long npix = (long long)g.Mglob * g.Nglob;
     if (!shape_ok(1, g.Nglob, g.Mglob)) return FW_ERR_BAD_PARAM;
-    int rc = ensure_ws(n, npix);
+    int rc = ensure_ws(n, 1, g.Nglob, g.Mglob, c->stream);
     if (rc != FW_OK) return rc;
     const bool fp64 = c->p.precision == FW_PREC_FP64;
     pack_images(n, c->stream);  // before any capture: the graph reads the images

@@ -5,9 +5,9 @@
 // tcgen05.mma tile), N = the output channels (16 or 32), K = 9 taps x the
 // input channels.  A CTA computes TROWS rows of 128 pixels:
 //
-//   1. one thread issues CINC TMA tensor loads (one per 8-channel chunk) of
-//      the (TROWS + 2) x 130-pixel input halo tile -- zero-filled by the
-//      TMA unit outside the grid -- completing on an mbarrier (with the
+//   1. one thread issues (TROWS + 2) x CINC bulk copies (cp.async.bulk),
+//      one contiguous 130-pixel run per staged row and 8-channel chunk of
+//      the padded activation (below), completing on an mbarrier (with the
 //      first tile, one bulk copy of the packed BF16 weight image too);
 //   2. the same thread issues TROWS x 9 x CINC/2 tcgen05.mma (kind::f16,
 //      BF16 x BF16 -> FP32) into TMEM, one 128 x N accumulator per output
@@ -19,11 +19,16 @@
 // epilogue warps) with NSTAGE input stages and two TMEM accumulators, so
 // loads, MMAs and epilogues of successive tiles overlap.
 //
+// Activations in global memory are BF16, chunk-planar and padded:
+// [B][H + 2][chunks][W + 2][8 channels], a zero pixel on every side of each
+// image (act_idx).  A staged row of one chunk is then 130 contiguous
+// 16-byte pixels, and the zero border is the convolution's padding.
+//
 // Shared-memory operand layout (no swizzle, K-major canonical layout): the
-// input tile is stored as CINC chunk planes, each [row][pixel][8 channels]
-// (16 bytes a pixel).  A core matrix -- 8 pixels x 16 bytes -- is then 128
-// contiguous bytes, consecutive pixel groups are 128 bytes apart (SBO) and
-// consecutive K chunks one plane apart (LBO).  A tap's shift by one pixel
+// staged tile is [row][chunk][pixel][8 channels] (16 bytes a pixel).  A
+// core matrix -- 8 pixels x 16 bytes -- is then 128 contiguous bytes,
+// consecutive pixel groups are 128 bytes apart (SBO) and consecutive K
+// chunks one staged row of a chunk apart (LBO).  A tap's shift by one pixel
 // is a shift of the descriptor's start address by 16 bytes, so all nine
 // taps read the same staged tile.  The weight image of one tap is
 // [chunk][n][8 channels] (SBO 128 bytes, LBO N x 16 bytes).
@@ -33,7 +38,6 @@
 // returns.
 #pragma once
 
-#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -47,9 +51,22 @@ constexpr int TPX = 128;                 // pixels of an output row tile (the MM
 constexpr int TROWS = 4;                 // output rows per CTA
 constexpr int HPX = TPX + 2;             // staged pixels of a row (one halo pixel each side)
 constexpr int ROWB = HPX * 16;           // bytes of one staged row of one chunk
-constexpr int PLANE = ((TROWS + 2) * ROWB + 127) / 128 * 128;  // bytes of one chunk plane
-constexpr int BOX_BYTES = 8 * HPX * (TROWS + 2) * 2;           // bytes one tensor load delivers
-constexpr unsigned WAIT_LIMIT = 1u << 22;                      // polls of an mbarrier (~0.3-1 s)
+constexpr unsigned WAIT_LIMIT = 1u << 22;  // polls of an mbarrier (~0.3-1 s)
+
+// the padded chunk-planar activation of a B x H x W image batch with CC
+// 8-channel chunks, in 16-byte units: [B][H + 2][CC][W + 2]
+struct ActGeom {
+    int B, H, W, CC;
+};
+__host__ __device__ __forceinline__ long long act_idx(const ActGeom &a, int b, int y, int c, int x) {
+    return (((long long)b * (a.H + 2) + (y + 1)) * a.CC + c) * (a.W + 2) + (x + 1);
+}
+// bytes of such a buffer, with slack for the staged runs of the last tiles,
+// which may read up to 128 pixels past a row's end and TROWS + 2 rows past
+// the last image (values that only masked outputs use)
+__host__ __device__ __forceinline__ size_t act_bytes(const ActGeom &a) {
+    return (size_t)a.B * (a.H + 2) * a.CC * (a.W + 2) * 16 + (size_t)(TROWS + 2) * a.CC * (a.W + 2) * 16 + 4096;
+}
 
 enum { EPI_RELU_BF16 = 0, EPI_LINEAR_F32 = 1, EPI_MASK_BF16 = 2 };
 
@@ -58,7 +75,7 @@ constexpr int EPI_WARPS = 8;             // epilogue warps (two per TMEM lane qu
 static_assert(TROWS % 2 == 0, "the epilogue splits a tile's rows in two halves");
 
 template <int CINC, int N> struct Layout {
-    static constexpr int X_BYTES = CINC * PLANE;    // one input stage
+    static constexpr int X_BYTES = (TROWS + 2) * CINC * ROWB;  // one input stage
     static constexpr int W_BYTES = 9 * CINC * N * 16;
     static constexpr int TMEM_COLS = TROWS * N <= 32 ? 32 : (TROWS * N <= 64 ? 64 : 128);  // one accumulator
     // NSTAGE input stages, the weights, 2 NSTAGE + 4 mbarriers, the TMEM
@@ -100,15 +117,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         if (i >= 32) __nanosleep(64);
     }
     return false;
-}
-
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
-                                            uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
-        : "memory");
 }
 
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
@@ -180,11 +188,11 @@ __device__ __forceinline__ float hi_bf(uint32_t w) { return __uint_as_float(w & 
 //                       rows (warps 2-5 the first half, 6-9 the second),
 //                       releases it, and stores.
 // No CTA-wide barrier sits inside the loop, so loads, MMAs and epilogues of
-// successive tiles overlap.  x: the input through its tensor map
-// ([B][H][W][8*CINC] BF16); wimg: the packed weight image (9 x CINC x N x 8
-// BF16).  EPI_RELU_BF16: y = BF16 relu(acc + bias), [pix][32];
-// EPI_LINEAR_F32: y = FP32 acc + bias, [pix][NOUTF]; EPI_MASK_BF16: y = BF16
-// acc where act > 0 else 0, [pix][32] (act: [pix][32] BF16).  status: set to
+// successive tiles overlap.  x: the padded input (CINC chunks); wimg: the
+// packed weight image (9 x CINC x N x 8 BF16).  EPI_RELU_BF16: y = BF16
+// relu(acc + bias), padded with 4 chunks; EPI_LINEAR_F32: y = FP32 acc +
+// bias, [pix][NOUTF] unpadded; EPI_MASK_BF16: y = BF16 acc where act > 0
+// else 0, padded with 4 chunks (act: padded, 4 chunks).  status: set to
 // 1 (an input or accumulator wait expired) or 2 (an MMA wait expired); every
 // role then stops.
 __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile uint32_t *flag) {
@@ -209,10 +217,9 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 }
 
 template <int CINC, int N, int EPI, int NOUTF>
-__global__ void __launch_bounds__(320, 1) k_conv_tc(const __grid_constant__ CUtensorMap xmap,
-                                                    const bf16 *__restrict__ wimg, const float *__restrict__ bias,
-                                                    const bf16 *__restrict__ act, void *__restrict__ y, int H, int W,
-                                                    int B, int *status) {
+__global__ void __launch_bounds__(320, 1) k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wimg,
+                                                    const float *__restrict__ bias, const bf16 *__restrict__ act,
+                                                    void *__restrict__ y, int H, int W, int B, int *status) {
     static_assert(CINC % 2 == 0 && (N == 16 || N == 32), "K steps of 16 channels; N of 16 or 32");
     using L = Layout<CINC, N>;
     extern __shared__ uint8_t smem_raw[];
@@ -227,6 +234,7 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const __grid_constant__ CUte
     const uint32_t tptr = bar + 8u * (2 * NSTAGE + 4);
     volatile uint32_t *flag = reinterpret_cast<volatile uint32_t *>(smem + (tptr + 4u - xs0));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const ActGeom gin{B, H, W, CINC}, gout{B, H, W, 4};
     const int tiles_x = (W + TPX - 1) / TPX, tiles_y = (H + TROWS - 1) / TROWS;
     const int ntiles = tiles_x * tiles_y * B;
     const int ntl = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
@@ -278,10 +286,15 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const __grid_constant__ CUte
                 }
                 int x0, y0, b;
                 tile_xyb(i, x0, y0, b);
-                mbar_expect_tx(full_bar(st), (uint32_t)(CINC * BOX_BYTES + (i == 0 ? L::W_BYTES : 0)));
+                mbar_expect_tx(full_bar(st), (uint32_t)(L::X_BYTES + (i == 0 ? L::W_BYTES : 0)));
                 const uint32_t xs = xs0 + st * L::X_BYTES;
+                // staged row rr, chunk c: pixels x0-1 .. x0+128 of image row y0-1+rr
+#pragma unroll 1
+                for (int rr = 0; rr < TROWS + 2; rr++)
 #pragma unroll
-                for (int c = 0; c < CINC; c++) tma_load_4d(xs + c * PLANE, &xmap, c * 8, x0 - 1, y0 - 1, b, full_bar(st));
+                    for (int c = 0; c < CINC; c++)
+                        bulk_load(xs + (rr * CINC + c) * ROWB, x + 8 * act_idx(gin, b, y0 - 1 + rr, c, x0 - 1),
+                                  (uint32_t)ROWB, full_bar(st));
                 if (i == 0) bulk_load(ws, wimg, (uint32_t)L::W_BYTES, full_bar(0));
 #pragma unroll
                 for (int k = 0; k < NSTAGE; k++)
@@ -310,17 +323,22 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const __grid_constant__ CUte
                 }
                 tc_fence_after();
                 const uint32_t xs = xs0 + st * L::X_BYTES, acc = tmem + (uint32_t)(a * L::TMEM_COLS);
+                // the start address is the descriptors' low field (16-byte
+                // units), so each MMA's descriptors are these two plus a
+                // compile-time offset (all shared addresses stay below 256 KB,
+                // so the field does not overflow)
+                const uint64_t a_base = sdesc(xs, ROWB, 128), b_base = sdesc(ws, N * 16, 128);
 #pragma unroll 1
                 for (int r = 0; r < TROWS; r++) {
+                    const uint64_t a_row = a_base + (uint64_t)((r * CINC * ROWB) >> 4);
 #pragma unroll
                     for (int t = 0; t < 9; t++) {
                         const int ky = t / 3, kx = t % 3;  // staged row and pixel offsets of the tap
 #pragma unroll
                         for (int h = 0; h < CINC / 2; h++) {
-                            const uint32_t aa = xs + 2 * h * PLANE + (r + ky) * ROWB + kx * 16;
-                            const uint32_t bw = ws + (t * CINC + 2 * h) * N * 16;
-                            tc_mma(acc + r * N, sdesc(aa, PLANE, 128), sdesc(bw, N * 16, 128), idesc,
-                                   (t | h) != 0 ? 1u : 0u);
+                            const uint32_t a_off = (uint32_t)(((ky * CINC + 2 * h) * ROWB + kx * 16) >> 4);
+                            const uint32_t b_off = (uint32_t)(((t * CINC + 2 * h) * N * 16) >> 4);
+                            tc_mma(acc + r * N, a_row + a_off, b_base + b_off, idesc, (t | h) != 0 ? 1u : 0u);
                         }
                     }
                 }
@@ -373,7 +391,9 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const __grid_constant__ CUte
                     for (int c = 0; c < NOUTF; c++) yf[c] = __uint_as_float(v[c]) + bs[c];
                 } else {
                     static_assert(EPI == EPI_LINEAR_F32 || N == 32, "BF16 outputs have 32 channels");
-                    uint4 *yq = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(y) + p * 32);
+                    // chunk qq of this pixel: consecutive lanes write consecutive 16 bytes
+                    uint4 *yq = reinterpret_cast<uint4 *>(y);
+                    const long long o0 = act_idx(gout, b, py, 0, px), ostep = (long long)(W + 2);
                     if constexpr (EPI == EPI_RELU_BF16) {
 #pragma unroll
                         for (int qq = 0; qq < 4; qq++) {
@@ -381,14 +401,14 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const __grid_constant__ CUte
 #pragma unroll
                             for (int e = 0; e < 8; e++)
                                 f[e] = fmaxf(__uint_as_float(v[qq * 8 + e]) + bs[qq * 8 + e], 0.0f);
-                            yq[qq] = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]),
-                                                pack2(f[6], f[7]));
+                            yq[o0 + qq * ostep] = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]),
+                                                             pack2(f[6], f[7]));
                         }
                     } else {
-                        const uint4 *aq = reinterpret_cast<const uint4 *>(act + p * 32);
+                        const uint4 *aq = reinterpret_cast<const uint4 *>(act);
 #pragma unroll
                         for (int qq = 0; qq < 4; qq++) {
-                            const uint4 m = __ldg(aq + qq);
+                            const uint4 m = __ldg(aq + o0 + qq * ostep);
                             const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
                             float f[8];
 #pragma unroll
@@ -396,8 +416,8 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const __grid_constant__ CUte
                                 f[2 * e] = lo_bf(mw[e]) > 0.0f ? __uint_as_float(v[qq * 8 + 2 * e]) : 0.0f;
                                 f[2 * e + 1] = hi_bf(mw[e]) > 0.0f ? __uint_as_float(v[qq * 8 + 2 * e + 1]) : 0.0f;
                             }
-                            yq[qq] = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]),
-                                                pack2(f[6], f[7]));
+                            yq[o0 + qq * ostep] = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]),
+                                                             pack2(f[6], f[7]));
                         }
                     }
                 }
