@@ -403,7 +403,7 @@ def net_report(fw, size=1024, reps=20):
             "ms_train_iteration_batch8_128x128": ms_iter}
 
 
-def learned_report(fw, iters=4000, eval_coarse_steps=500, unroll=1, every=2, scale=1):
+def learned_report(fw, iters=4000, eval_coarse_steps=500, unroll=1, every=2, scale=1, relax=(0.5, 0.25), nudge=None):
     """The learned coarse-grid correction, at reduced training scale: pairs
     (one coarse step of 2 x dx against two fine steps, restricted) from
     seeded planar beaches, barred beaches and a shoal with JONSWAP Hs
@@ -449,7 +449,7 @@ def learned_report(fw, iters=4000, eval_coarse_steps=500, unroll=1, every=2, sca
                    [shoal(s) for s in range(21, 21 + scale)])
     X, T, Wm = [], [], []
     for c in train_cases:
-        x, t, w = L.make_pairs(c, 240, every=every, unroll=unroll)
+        x, t, w = L.make_pairs(c, 240, every=every, unroll=unroll, nudge=nudge)
         X.append(x)
         T.append(t)
         Wm.append(w)
@@ -471,12 +471,29 @@ def learned_report(fw, iters=4000, eval_coarse_steps=500, unroll=1, every=2, sca
         def ru(o):
             return fw.max_runup(np.pad(o["HeightMax"], 3), o["depth"])
 
-        evals.append({"case": name, "grid_fine": [c[0]["Mglob"], c[0]["Nglob"]], "coarse_steps": eval_coarse_steps,
-                      "one_step_error_ratio": e1 / e0 if e0 > 0 else None,
-                      "eta_rms_plain_m": float(np.sqrt(np.mean((plain["Eta"] - f)[m] ** 2))),
-                      "eta_rms_corrected_m": float(np.sqrt(np.mean((corr["Eta"] - f)[m] ** 2))),
-                      "max_runup_fine_m": ru(fine), "max_runup_plain_m": ru(plain),
-                      "max_runup_corrected_m": ru(corr), "corrections_applied": applied})
+        ev = {"case": name, "grid_fine": [c[0]["Mglob"], c[0]["Nglob"]], "coarse_steps": eval_coarse_steps,
+              "one_step_error_ratio": e1 / e0 if e0 > 0 else None,
+              "eta_rms_plain_m": float(np.sqrt(np.mean((plain["Eta"] - f)[m] ** 2))),
+              "eta_rms_corrected_m": float(np.sqrt(np.mean((corr["Eta"] - f)[m] ** 2))),
+              "max_runup_fine_m": ru(fine), "max_runup_plain_m": ru(plain),
+              "max_runup_corrected_m": ru(corr), "corrections_applied": applied}
+        # relaxed corrections: the last layer is linear, so scaling its
+        # weights and bias by alpha scales the correction by alpha
+        p0 = net.params()
+        nw = len(p0) - (9 * 32 * 3 + 3)
+        relaxed = {}
+        for alpha in relax:
+            pa = p0.copy()
+            pa[nw:] *= alpha
+            net.set_params(pa)
+            ca, _ = L.rollout(c, eval_coarse_steps, net=net)
+            ma = (plain["MASK"] > 0) & (ca["MASK"] > 0)
+            relaxed[str(alpha)] = {"eta_rms_m": float(np.sqrt(np.mean((ca["Eta"] - f)[ma] ** 2))),
+                                   "max_runup_m": ru(ca)}
+        net.set_params(p0)
+        if relaxed:
+            ev["relaxed"] = relaxed
+        evals.append(ev)
     # throughput at the configuration's sizes
     params, depth, phases = fw.cases.shoal_jonswap(2048, 2048, dx=1.0, seed=5, Nfreq=16, Ntheta=4)
     params = fw.with_defaults(params)
@@ -503,7 +520,7 @@ def learned_report(fw, iters=4000, eval_coarse_steps=500, unroll=1, every=2, sca
     cs.close()
     net.close()
     return {"metric": "learned coarse-grid correction", "training_pairs": int(sum(a.shape[0] for a in X)),
-            "pairs_unroll": unroll, "pairs_every": every, "training_cases": len(train_cases),
+            "pairs_unroll": unroll, "pairs_every": every, "pairs_nudge": nudge, "training_cases": len(train_cases),
             "training_iters": iters, "pairs_s": t_pairs, "train_s": t_train,
             "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-50:])),
             "evaluation": evals,
@@ -595,6 +612,8 @@ def main():
                     help="learned report: coarse steps unrolled from each restricted fine start")
     ap.add_argument("--learned-every", type=int, default=2,
                     help="learned report: coarse steps between restricted fine starts")
+    ap.add_argument("--learned-nudge", type=float, default=None,
+                    help="learned report: pairs along one coarse run nudged by this fraction toward the fine run")
     ap.add_argument("--learned-scale", type=int, default=1,
                     help="learned report: multiple of the 8 training cases")
     ap.add_argument("--learned-iters", type=int, default=4000, help="learned report: Adam iterations")
@@ -617,7 +636,8 @@ def main():
         return 0
     if args.learned_report:
         print(json.dumps(learned_report(fw, iters=args.learned_iters, unroll=args.learned_unroll,
-                                        every=args.learned_every, scale=args.learned_scale)), flush=True)
+                                        every=args.learned_every, scale=args.learned_scale,
+                                        nudge=args.learned_nudge)), flush=True)
         return 0
     if args.precision_report:
         import torch

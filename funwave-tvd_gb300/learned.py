@@ -178,7 +178,7 @@ def _set_state(cs, eta, u, v, ubar, vbar, depth_c, mask):
     cs.exchange()
 
 
-def make_pairs(case, nsteps_c, precision="MIXED", every=1, unroll=1):
+def make_pairs(case, nsteps_c, precision="MIXED", every=1, unroll=1, nudge=None):
     """Training pairs from one fine run of case = (params, depth, phases)
     (params with DT_fixed): returns (x [K, N, M, 5], target [K, N, M, 3],
     wmask [K, N, M]) as numpy float32, the target already multiplied by
@@ -189,7 +189,13 @@ def make_pairs(case, nsteps_c, precision="MIXED", every=1, unroll=1):
     steps gives a pair: its input state (the restricted fine state first,
     then states the coarse solver evolved itself, as in a corrected run) and
     the difference between the restricted fine state one coarse step later
-    and the coarse step's result."""
+    and the coarse step's result.
+
+    nudge = beta (0 < beta <= 1) instead: one coarse run over the whole
+    trajectory that, after each step, moves beta of the way to the restricted
+    fine state (eta, u, v, ubar, vbar): the state a run corrected by a
+    network that removes a fraction beta of each step's error would be in.
+    Every step gives a pair (every `every`-th is kept)."""
     pf, depth, phases = case
     pf = with_defaults(pf)
     pc, depth_c = coarse_case(pf, depth)
@@ -210,6 +216,29 @@ def make_pairs(case, nsteps_c, precision="MIXED", every=1, unroll=1):
         times.append(fs.scalar("TIME"))
     fs.close()
     dc = _interior(cs.get("Depth"))
+    if nudge is not None:
+        st = ref[0]
+        mask = ((st["Eta"] + dc) > 1e-3).astype(np.int32)
+        _set_state(cs, st["Eta"], st["U"], st["V"], st["Ubar"], st["Vbar"], dc, mask)
+        cs.set_scalar("TIME", times[0])
+        cur_in = {k: st[k] for k in ("Eta", "U", "V", "Ubar", "Vbar")}
+        for k in range(nsteps_c):
+            cs.step(1)
+            c1 = {n: _interior(cs.get(n)) for n in ("Eta", "U", "V", "Ubar", "Vbar")}
+            mc = _interior(cs.get("MASK"))
+            cur = ref[k + 1]
+            if k % every == 0:
+                wet = ((mask > 0) & (mc > 0)).astype(np.float32)
+                xs.append(features(cur_in["Eta"], cur_in["U"], cur_in["V"], dc, mask))
+                tgt = np.stack([cur["Eta"] - c1["Eta"], cur["U"] - c1["U"], cur["V"] - c1["V"]], axis=-1) * OUT_SCALE
+                ts.append(np.ascontiguousarray((tgt * wet[..., None]).transpose(1, 0, 2), dtype=np.float32))
+                ws.append(np.ascontiguousarray(wet.T))
+            nxt = {n: c1[n] + nudge * (cur[n] - c1[n]) for n in c1}
+            mask = ((nxt["Eta"] + dc) > 1e-3).astype(np.int32)
+            _set_state(cs, nxt["Eta"], nxt["U"], nxt["V"], nxt["Ubar"], nxt["Vbar"], dc, mask)
+            cur_in = nxt
+        cs.close()
+        return np.stack(xs), np.stack(ts), np.stack(ws)
     for start in range(0, nsteps_c - unroll + 1, every):
         st = ref[start]
         mask = ((st["Eta"] + dc) > 1e-3).astype(np.int32)
