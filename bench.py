@@ -157,6 +157,12 @@ def barrier(pg):
         dist.barrier()
 
 
+def aggregate_rate(cells, steps, ws, ms_max):
+    """Whole-job cell-steps/s of ws replicas that each advanced `cells`
+    cells by `steps` steps, over the slowest rank's time (ms)."""
+    return cells * steps * ws / (ms_max * 1e-3)
+
+
 def max_over_ranks(v, pg):
     if not pg:
         return v
@@ -671,7 +677,7 @@ def main():
         wet = (s64.get("MASK")[3:-3, 3:-3] > 0)
         rms = float(np.sqrt(np.mean((e_m - e_d)[wet] ** 2)))
         mask_mis = int(np.sum(sm.get("MASK") != s64.get("MASK")))
-        res64 = {"value": cells * K * ws / (ms64 * 1e-3), "ms_per_step": ms64 / K, "dtype": "f64",
+        res64 = {"value": aggregate_rate(cells, K, ws, ms64), "ms_per_step": ms64 / K, "dtype": "f64",
                  "step_roofline_frac_hbm": STEP_BYTES["fp64"] * cells / (ms64 / K * 1e-3) / 1e9 / hbm,
                  "eta_rms_mixed_vs_fp64_m": rms, "mask_mismatch_cells": mask_mis,
                  "time_mixed_s": sm.scalar("TIME"), "time_fp64_s": s64.scalar("TIME"),
@@ -690,7 +696,7 @@ def main():
     ens = None if args.no_ensemble else ensemble_bench(fw, pg, ws, autotune=not args.no_autotune)
     if rank != 0:
         return 0
-    value = cells * K * ws / (ms_mixed * 1e-3)
+    value = aggregate_rate(cells, K, ws, ms_mixed)
     step_s = ms_mixed / K * 1e-3
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
