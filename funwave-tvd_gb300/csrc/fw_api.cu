@@ -318,6 +318,67 @@ long long swap_state(fw_ctx *c) {
     return (long long)((uintptr_t)c->ff.MASK ^ ((uintptr_t)c->ff.AGE << 1));
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// the flux kernels' tensor maps (fw::FluxMaps): a plane of pitch x (Nloc+1)
+// elements, boxes 40 (fields) or 48 (MASK) cells wide and as high as the
+// tile's staged rows; zero outside the plane
+template <typename T> bool build_flux_maps(fw_ctx *c) {
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return false;
+    fw::Fields<T> &f = c->F<T>();
+    const Grid &g = c->g;
+    T *fld[7] = {f.U, f.V, f.HU, f.HV, f.Eta, f.U4, f.V4};
+    uint8_t *mb[2] = {f.MASK, f.MASKn};
+    const cuuint64_t dims[2] = {(cuuint64_t)g.pitch, (cuuint64_t)(g.Nloc + 1)};
+    const cuuint64_t st_f[1] = {(cuuint64_t)g.pitch * sizeof(T)}, st_m[1] = {(cuuint64_t)g.pitch};
+    const cuuint32_t es[2] = {1, 1};
+    const CUtensorMapDataType dt = sizeof(T) == sizeof(double) ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                                               : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    for (int dir = 0; dir < 2; dir++)
+        for (int fi = 0; fi < fw::FLUX_FY_N; fi++) {
+            const int fy = 8 << fi;
+            if (sizeof(T) == sizeof(double) && fy == 32) continue;
+            const cuuint32_t bh = (cuuint32_t)(dir == 0 ? fy : fy + 6);
+            const cuuint32_t box_f[2] = {40, bh}, box_m[2] = {48, bh};
+            for (int mi = 0; mi < 2; mi++) {
+                fw::FluxMaps &m = c->fmaps[dir][fi][mi];
+                for (int v = 0; v < 7; v++)
+                    if (enc(&m.m[v], dt, 2, fld[v], dims, st_f, box_f, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                        return false;
+                if (enc(&m.m[7], CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, mb[mi], dims, st_m, box_m, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                    return false;
+            }
+        }
+    c->fmask_base[0] = f.MASK;
+    c->fmask_base[1] = f.MASKn;
+    return fw::flux_tma_attrs<T>();
+}
+
 // launch-shape candidates of the per-cell kernels (bx a multiple of 32,
 // at most 256 threads, as the kernels' launch bounds allow)
 const int CELL_CANDIDATES[][2] = {{32, 8}, {32, 4}, {32, 2}, {64, 4}, {64, 2}, {128, 2}, {128, 1}, {256, 1}};
@@ -334,6 +395,9 @@ bool tune_valid(const fw_ctx *c, const int *t) {
     for (int d = 0; d < 2; d++) {
         const int fy = t[fw::TUNE_FLUX + d];
         if (fy != 8 && fy != 16 && (fp64 || fy != 32)) return false;
+        const int tma = t[fw::TUNE_FLUX_TMA + d];
+        if (tma != 0 && tma != 1) return false;
+        if (tma == 1 && !c->fmaps_ok) return false;
     }
     return true;
 }
@@ -536,6 +600,10 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     c->arena_bytes = bytes;
     if (fp64) carve<double>(c, (char *)c->arena, true);
     else carve<float>(c, (char *)c->arena, true);
+    // the TMA-staged flux kernels are a tuning choice; without their maps
+    // the load-based kernels run
+    c->fmaps_ok = (fp64 ? build_flux_maps<double>(c) : build_flux_maps<float>(c)) ? 1 : 0;
+    cudaGetLastError();
     cudaError_t e = cudaMemsetAsync(c->arena, 0, bytes, c->stream);
     const unsigned long long inf_bits = 0x7ff0000000000000ull;
     unsigned long long *dtb = fp64 ? c->fd.dtmin_bits : c->ff.dtmin_bits;
@@ -1154,17 +1222,21 @@ int fw_autotune(fw_ctx *c, int flags) {
         }
         for (int dir = 0; dir < 2 && e == cudaSuccess; dir++) {
             double best = 1e30;
-            int pick = c->tune[fw::TUNE_FLUX + dir];
-            for (int fy : {8, 16, 32}) {
-                c->tune[fw::TUNE_FLUX + dir] = fy;
-                if (!tune_valid(c, c->tune)) continue;
-                const double ms = time_named(c, fp64, dir == 0 ? "flux_x" : "flux_y", e);
-                if (ms < best) {
-                    best = ms;
-                    pick = fy;
+            int pick = c->tune[fw::TUNE_FLUX + dir], pick_tma = c->tune[fw::TUNE_FLUX_TMA + dir];
+            for (int tma = 0; tma < 2; tma++)
+                for (int fy : {8, 16, 32}) {
+                    c->tune[fw::TUNE_FLUX + dir] = fy;
+                    c->tune[fw::TUNE_FLUX_TMA + dir] = tma;
+                    if (!tune_valid(c, c->tune)) continue;
+                    const double ms = time_named(c, fp64, dir == 0 ? "flux_x" : "flux_y", e);
+                    if (ms < best) {
+                        best = ms;
+                        pick = fy;
+                        pick_tma = tma;
+                    }
                 }
-            }
             c->tune[fw::TUNE_FLUX + dir] = pick;
+            c->tune[fw::TUNE_FLUX_TMA + dir] = pick_tma;
         }
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->arena, save, c->arena_bytes, cudaMemcpyDeviceToDevice, c->stream);

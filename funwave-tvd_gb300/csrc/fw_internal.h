@@ -10,6 +10,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include <cuda.h>
+
 #include "funwave_gpu.h"
 
 namespace fw {
@@ -129,6 +131,7 @@ void gather_points(fw_ctx *c, const void *field, int type, const int *d_off, int
 template <typename T>
 void launch_cm_sm(fw_ctx *c, int bw, int bh, int i0, int j0, const double *tab, T *Cm, T *Sm);
 template <typename T> int launch_by_name(fw_ctx *c, const char *name);
+template <typename T> bool flux_tma_attrs();  // shared-memory sizes of the TMA-staged flux kernels
 // staging buffer <-> field (double <-> float fields, int32 <-> uint8 masks)
 void convert_in(fw_ctx *c, const void *staging, int is_mask, void *field, int w, int h);
 void convert_out(fw_ctx *c, const void *field, int is_mask, void *staging, int w, int h);
@@ -139,16 +142,28 @@ void convert_out(fw_ctx *c, const void *field, int is_mask, void *staging, int w
 
 // Host context behind the opaque C handle.
 namespace fw {
+// tensor maps of the flux kernels' TMA-staged tiles: U V HU HV Eta U4 V4 and
+// MASK, for one direction and tile height (the box shape is part of a map)
+// and one of the two MASK buffers
+struct FluxMaps {
+    CUtensorMap m[8];
+};
+constexpr int FLUX_FY_N = 3;  // tile heights 8, 16, 32
 // kernels whose block shape fw_autotune chooses (per-cell kernels, so any
 // shape gives the same results); the tuning vector holds (bx, by) for each,
 // then the tile heights of the x and y flux kernels (FW_TUNE_LEN ints)
 enum TuneKernel { TK_DISP_A = 0, TK_DISP_B, TK_UPDATE, TK_PMB, TK_MASKMUL, TK_N };
-constexpr int TUNE_FLUX = 2 * TK_N;
+constexpr int TUNE_FLUX = 2 * TK_N;      // flux tile heights (x, y)
+constexpr int TUNE_FLUX_TMA = 2 * TK_N + 2;  // flux staging by TMA (x, y): 0 loads, 1 TMA
 }  // namespace fw
 
 struct fw_ctx {
     fw_params p;
-    int tune[FW_TUNE_LEN] = {32, 8, 32, 8, 32, 8, 32, 8, 32, 8, 8, 32};  // see fw::TuneKernel
+    int tune[FW_TUNE_LEN] = {32, 8, 32, 8, 32, 8, 32, 8, 32, 8, 8, 32, 0, 0};  // see fw::TuneKernel
+    // the flux kernels' tensor maps: [direction][tile height 8/16/32][MASK buffer]
+    fw::FluxMaps fmaps[2][fw::FLUX_FY_N][2];
+    const void *fmask_base[2] = {nullptr, nullptr};  // the two MASK buffers the maps were made for
+    int fmaps_ok = 0;
     dim3 blk(int k) const { return dim3((unsigned)tune[2 * k], (unsigned)tune[2 * k + 1]); }
     fw::Grid g;
     cudaStream_t stream = nullptr;

@@ -27,6 +27,7 @@
 #include <cstring>
 
 #include "fw_internal.h"
+#include "fw_tc.cuh"
 
 namespace fw {
 
@@ -603,6 +604,193 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
     }
     }
 }
+
+// The tile's inputs staged by TMA: one 2-D tensor load of each of U V HU HV
+// Eta U4 V4 (40 cells wide from i0 - 3, FY rows from j0 for x faces or FY+6
+// rows from j0 - 3 for y faces) and of MASK (48 wide), completing on one
+// mbarrier; Din and the faces then read shared memory.  i0 - 3 is a
+// multiple of 32 (ib = 3), so every box starts on a 16-byte boundary.  The
+// same arithmetic as k_flux, so the same results.
+template <typename T, int DIR, int FY_> struct FluxStage {
+    using TL = FluxTile<T, DIR, FY_>;
+    static constexpr int BW = 40, BWM = 48;             // staged columns from i0 - 3
+    static constexpr int BH = DIR == 0 ? FY_ : FY_ + 6;  // staged rows from j0 (x) or j0 - 3 (y)
+    static constexpr int FB = (BW * BH * (int)sizeof(T) + 127) / 128 * 128;
+    static constexpr int MB = (BWM * BH + 127) / 128 * 128;
+    static constexpr int DB = (7 * TL::NTL * TL::NP * (int)sizeof(T) + 127) / 128 * 128;
+    static constexpr int BYTES = 7 * FB + MB + DB + 16 + 128;
+};
+
+template <typename T> __device__ __forceinline__ T fnan();
+template <> __device__ __forceinline__ float fnan<float>() { return __int_as_float(0x7fffffff); }
+template <> __device__ __forceinline__ double fnan<double>() { return __longlong_as_double(0x7fffffffffffffffll); }
+
+template <typename T, int DIR, int FY_>
+__global__ void __launch_bounds__(256) k_flux_tma(Grid g, Fields<T> f, const __grid_constant__ FluxMaps maps) {
+    using TL = FluxTile<T, DIR, FY_>;
+    using S = FluxStage<T, DIR, FY_>;
+    static_assert(TL::FY % TL::BY == 0, "whole faces per thread");
+    constexpr int BX = TL::BX, BY = TL::BY, NTL = TL::NTL, NPOS = TL::NPOS, NP = TL::NP;
+    extern __shared__ uint8_t fsm_raw[];
+    uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(fsm_raw) + 127) & ~(uintptr_t)127);
+    T(*din)[NTL][NP] = reinterpret_cast<T(*)[NTL][NP]>(sm + 7 * S::FB + S::MB);
+    const uint32_t bar = fwtc::smem_u32(sm + 7 * S::FB + S::MB + S::DB);
+#define FLD(v_, r_, c_) (reinterpret_cast<const T *>(sm + (v_) * S::FB)[(r_) * S::BW + (c_)])
+#define MSK(r_, c_) ((int)(sm + 7 * S::FB)[(r_) * S::BWM + (c_)])
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = tx + ty * BX;
+    const int i0 = g.ib + blockIdx.x * TL::FX, j0 = g.jb + blockIdx.y * TL::FY;
+    const int lo = DIR == 0 ? g.ib : g.jb, hi = DIR == 0 ? g.ie : g.je;
+    const int base = (DIR == 0 ? i0 : j0) - 1;
+    const int nvar = g.dispersion ? 7 : 5;
+    const int stride = DIR == 0 ? 1 : g.pitch;
+    if (tid == 0) {
+        fwtc::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const int xs = i0 - 3, ysr = DIR == 0 ? j0 : j0 - 3;
+        fwtc::mbar_expect_tx(bar, (uint32_t)(nvar * S::BW * S::BH * (int)sizeof(T) + S::BWM * S::BH));
+        for (int v = 0; v < nvar; v++) fwtc::tma_load_2d(fwtc::smem_u32(sm + v * S::FB), &maps.m[v], xs, ysr, bar);
+        fwtc::tma_load_2d(fwtc::smem_u32(sm + 7 * S::FB), &maps.m[7], xs, ysr, bar);
+    }
+    const bool staged = fwtc::mbar_wait(bar, 0);
+    // the NTL x NPOS Din positions of the tile, spread over all threads
+    for (int it = tid; it < NTL * NPOS; it += BX * BY) {
+        const int k = DIR == 0 ? it % NPOS : it / NTL;
+        const int ln = DIR == 0 ? it / NPOS : it % NTL;
+        const int p = base + k;
+        const int ci = DIR == 0 ? p : i0 + ln;
+        const int cj = DIR == 0 ? j0 + ln : p;
+        const bool lok = DIR == 0 ? (cj <= g.je) : (ci <= g.ie);
+        if (lok && p >= lo - 1 && p <= hi + 2) {
+            // cells p-2 .. p+1: staged columns k .. k+3 of row ln (x), or
+            // rows k .. k+3 of column ln + 3 (y)
+            int m[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) m[q] = DIR == 0 ? MSK(ln, k + q) : MSK(k + q, ln + 3);
+#pragma unroll
+            for (int vv = 0; vv < 7; vv++) {
+                if (vv < nvar) {
+                    T v[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) v[q] = DIR == 0 ? FLD(vv, ln, k + q) : FLD(vv, k + q, ln + 3);
+                    din[vv][ln][k] = ho_din(v, m);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const T g1 = GC(gamma1), g3 = GC(gamma3);
+    for (int r = 0; r < TL::FPT; r++) {
+    const int i = i0 + tx;
+    const int j = j0 + ty + r * BY;
+    if (DIR == 0) {
+        if (i > g.ie + 1 || j > g.je) continue;
+    } else {
+        if (i > g.ie || j > g.je + 1) continue;
+    }
+    const int own = DIR == 0 ? tx : ty + r * BY;
+    const int line = DIR == 0 ? ty + r * BY : tx;
+    const int fid = i + j * g.pitch;
+    const int cm = fid - stride;  // cell pos-1 (cell pos is fid)
+    const int kf = own + 1;
+    T Lv[7], Rv[7];
+#pragma unroll
+    for (int vv = 0; vv < 7; vv++) {
+        if (vv >= nvar) {
+            Lv[vv] = (T)0;
+            Rv[vv] = (T)0;
+            continue;
+        }
+        // cells pos-1 and pos from the staged tile
+        ho_lr(FLD(vv, DIR == 0 ? line : own + 2, DIR == 0 ? own + 2 : line + 3),
+              FLD(vv, DIR == 0 ? line : own + 3, DIR == 0 ? own + 3 : line + 3), din[vv][line][kf - 1],
+              din[vv][line][kf], din[vv][line][kf + 1], Lv[vv], Rv[vv]);
+    }
+    const T UL = Lv[0], UR = Rv[0], VL = Lv[1], VR = Rv[1], HUL = Lv[2], HUR = Rv[2];
+    const T HVL = Lv[3], HVR = Rv[3], EL = Lv[4], ER = Rv[4];
+    const T U4L = Lv[5], U4R = Rv[5], V4L = Lv[6], V4R = Rv[6];
+    const T Dd = DIR == 0 ? f.Depthx[fid] : f.Depthy[fid];
+    const T HL = EL + Dd, HR = ER + Dd;
+    // MASK9u(Mloc1,:) = MASK9(Mloc,:) (fluxes.F:1333); the faces computed
+    // here never reach that column
+    const T m9 = m2r<T>(f.MASK9[fid]);
+    const T nL = DIR == 0 ? UL : VL, nR = DIR == 0 ? UR : VR;
+    const T tL = DIR == 0 ? VL : UL, tR = DIR == 0 ? VR : UR;
+    const T n4L = DIR == 0 ? U4L : V4L, n4R = DIR == 0 ? U4R : V4R;
+    const T t4L = DIR == 0 ? V4L : U4L, t4R = DIR == 0 ? V4R : U4R;
+    const T qnL = DIR == 0 ? HUL : HVL, qnR = DIR == 0 ? HUR : HVR;  // HU for x, HV for y
+    const T qtL = DIR == 0 ? HVL : HUL, qtR = DIR == 0 ? HVR : HUR;
+    // mass flux PL/QL, normal momentum flux FxL/GyL, tangential GxL/FyL
+    const T ML = qnL + g1 * m9 * HL * n4L;
+    const T MR = qnR + g1 * m9 * HR * n4R;
+    const T NL = g3 * ML * (nL + g1 * m9 * n4L) + (T)0.5 * (T)GRAV * ((EL) * (EL)*g3 + (T)2 * (EL) * (Dd));
+    const T NR = g3 * MR * (nR + g1 * m9 * n4R) + (T)0.5 * (T)GRAV * ((ER) * (ER)*g3 + (T)2 * (ER) * (Dd));
+    T TL, TR;
+    if (DIR == 0) {
+        TL = HL * (nL + g1 * m9 * n4L) * (tL + g1 * m9 * t4L) * g3;
+        TR = HR * (nR + g1 * m9 * n4R) * (tR + g1 * m9 * t4R) * g3;
+    } else {
+        TL = HL * (tL + g1 * m9 * t4L) * (nL + g1 * m9 * n4L) * g3;
+        TR = HR * (tR + g1 * m9 * t4R) * (nR + g1 * m9 * n4R) * g3;
+    }
+    // WAVE_SPEED (Zhou et al. 2001)
+    const T SQR_PHI_L = fsqrt((T)GRAV * fabs_(HL));
+    const T SQR_PHI_R = fsqrt((T)GRAV * fabs_(HR));
+    const T SQR_PHI_S = (T)0.5 * (SQR_PHI_L + SQR_PHI_R) + (T)0.25 * (nL - nR);
+    const T U_S = (T)0.5 * (nL + nR) + SQR_PHI_L - SQR_PHI_R;
+    const T SL = tmin(nL - SQR_PHI_L, U_S - SQR_PHI_S);
+    const T SR = tmax(nR + SQR_PHI_R, U_S + SQR_PHI_S);
+    T Pm = hll(SL, SR, ML, MR, EL, ER);
+    T Nm = hll(SL, SR, NL, NR, qnL, qnR);
+    T Tm = hll(SL, SR, TL, TR, qtL, qtR);
+    // BOUNDARY_CONDITION: walls, then the dry-cell loop (last write wins)
+    const int pos = DIR == 0 ? i : j;
+    const bool wall_on = DIR == 0 || !g.periodic;
+    if (wall_on && pos == lo) {
+        Pm = (T)0;
+        Nm = press(ER, Dd, g3);
+        Tm = (T)0;
+    }
+    if (wall_on && pos == hi + 1) {
+        Pm = (T)0;
+        Nm = press(EL, Dd, g3);
+        Tm = (T)0;
+    }
+    const int mL = MSK(DIR == 0 ? line : own + 2, DIR == 0 ? own + 2 : line + 3);  // cell pos-1
+    const int mR = MSK(DIR == 0 ? line : own + 3, DIR == 0 ? own + 3 : line + 3);  // cell pos
+    if (mL < 1) {
+        Pm = (T)0;
+        Nm = (pos - 1 != hi) ? press(ER, Dd, g3) * m2r<T>(mR) : (T)0;
+        Tm = (T)0;
+    }
+    if (mR < 1) {
+        Pm = (T)0;
+        Nm = (pos != lo) ? press(EL, Dd, g3) * m2r<T>(mL) : (T)0;
+        Tm = (T)0;
+    }
+    if (!staged) {  // the tile never arrived: poison the fluxes (the step reports NaN)
+        Pm = Nm = Tm = fnan<T>();
+    }
+    if (DIR == 0) {
+        f.P[fid] = Pm;
+        f.Fx[fid] = Nm;
+        f.Gx[fid] = Tm;
+    } else {
+        f.Q[fid] = Pm;
+        f.Gy[fid] = Nm;
+        f.Fy[fid] = Tm;
+    }
+    }
+    // the tile never arrived: its copies may still be in flight; one more
+    // bounded wait keeps this block's shared memory until they land
+    if (!staged && tid == 0) fwtc::mbar_wait(bar, 0);
+}
+
+#undef FLD
+#undef MSK
 
 // ---------------------------------------------------------------------------
 // SourceTerms (sources.F:56-548) at one interior cell, with the wavemaker
@@ -2744,8 +2932,35 @@ template <typename T, int DIR, int FY_> static void flux_at(fw_ctx *c) {
     k_flux<T, DIR, FY_><<<flux_grid<T, DIR, FY_>(c->g), B2D, 0, c->stream>>>(c->g, c->F<T>());
 }
 
+// the TMA-staged flux kernel with the maps of the current MASK buffer (its
+// shared-memory size is set when the maps are made, outside any capture)
+template <typename T, int DIR, int FY_> static void flux_tma_at(fw_ctx *c) {
+    using S = FluxStage<T, DIR, FY_>;
+    const int fi = FY_ == 8 ? 0 : (FY_ == 16 ? 1 : 2);
+    const int mi = ((const void *)c->F<T>().MASK == c->fmask_base[0]) ? 0 : 1;
+    k_flux_tma<T, DIR, FY_><<<flux_grid<T, DIR, FY_>(c->g), B2D, S::BYTES, c->stream>>>(c->g, c->F<T>(),
+                                                                                        c->fmaps[DIR][fi][mi]);
+}
+template <typename T, int DIR, int FY_> bool flux_tma_attr() {
+    return cudaFuncSetAttribute(k_flux_tma<T, DIR, FY_>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                FluxStage<T, DIR, FY_>::BYTES) == cudaSuccess;
+}
+template <typename T> bool flux_tma_attrs() {
+    bool ok = flux_tma_attr<T, 0, 8>() && flux_tma_attr<T, 0, 16>() && flux_tma_attr<T, 1, 8>() &&
+              flux_tma_attr<T, 1, 16>();
+    if constexpr (sizeof(T) == sizeof(float)) ok = ok && flux_tma_attr<T, 0, 32>() && flux_tma_attr<T, 1, 32>();
+    return ok;
+}
+
 template <typename T, int DIR> static void launch_flux(fw_ctx *c) {
     const int fy = c->tune[TUNE_FLUX + DIR];
+    if (c->tune[TUNE_FLUX_TMA + DIR] && c->fmaps_ok) {
+        if (fy == 8) flux_tma_at<T, DIR, 8>(c);
+        else if (fy == 16 || sizeof(T) == sizeof(double)) flux_tma_at<T, DIR, 16>(c);
+        else if constexpr (sizeof(T) == sizeof(float)) flux_tma_at<T, DIR, 32>(c);
+        note(c);
+        return;
+    }
     if constexpr (sizeof(T) == sizeof(float)) {
         if (fy == 8) flux_at<T, DIR, 8>(c);
         else if (fy == 16) flux_at<T, DIR, 16>(c);
@@ -3078,6 +3293,7 @@ template <typename T> int launch_by_name(fw_ctx *c, const char *name) {
     template void launch_end_step<T>(fw_ctx *);                  \
     template void launch_stage<T>(fw_ctx *, int);     \
     template void launch_cm_sm<T>(fw_ctx *, int, int, int, int, const double *, T *, T *); \
-    template int launch_by_name<T>(fw_ctx *, const char *);
+    template int launch_by_name<T>(fw_ctx *, const char *);      \
+    template bool flux_tma_attrs<T>();
 
 }  // namespace fw

@@ -119,6 +119,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
+// TMA tiled load of a 2-D box at (c0, c1) (elements) through a tensor map
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void *map, int c0, int c1, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+        : "memory");
+}
+
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
                  "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
@@ -439,7 +448,7 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const bf16 *__restrict__ x, 
 // co, tap t reads w[t][ci][co].  Backward data gradient (dgrad != 0): the
 // convolution runs over dy, so K = co, n = ci, and tap t reads the layer's
 // tap 8 - t (the mirrored offset).  Channels beyond cin / cout are zero.
-__global__ void k_pack_wimg(const float *__restrict__ w, int cin, int cout, int cinc, int n_img, int dgrad,
+static __global__ void k_pack_wimg(const float *__restrict__ w, int cin, int cout, int cinc, int n_img, int dgrad,
                             bf16 *__restrict__ img) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int total = 9 * cinc * n_img * 8;

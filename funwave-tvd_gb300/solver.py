@@ -410,7 +410,7 @@ class Solver:
 
     # FW_TUNE_LEN of include/funwave_gpu.h: (bx, by) of disp_a, disp_b,
     # update, post_mask_break, maskmul, then the x and y flux tile heights
-    TUNE_LEN = 12
+    TUNE_LEN = 14
     TUNE_NAMES = ("disp_a", "disp_b", "update", "post_mask_break", "maskmul")
 
     def autotune(self, fresh=False):
@@ -427,6 +427,7 @@ class Solver:
         self._check(self.L.fw_get_tuning(self.ctx, t), "fw_get_tuning")
         out = {n: (t[2 * k], t[2 * k + 1]) for k, n in enumerate(self.TUNE_NAMES)}
         out["flux_x"], out["flux_y"] = t[10], t[11]
+        out["flux_x_tma"], out["flux_y_tma"] = t[12], t[13]
         return out
 
     def set_tuning(self, tuning):
@@ -435,6 +436,8 @@ class Solver:
         for k, n in enumerate(self.TUNE_NAMES):
             t[2 * k], t[2 * k + 1] = tuning[n]
         t[10], t[11] = tuning["flux_x"], tuning["flux_y"]
+        # TMA staging of the flux tiles; 0 (each thread loads) when not given
+        t[12], t[13] = tuning.get("flux_x_tma", 0), tuning.get("flux_y_tma", 0)
         self._check(self.L.fw_set_tuning(self.ctx, t), "fw_set_tuning")
 
     def launch_count(self):

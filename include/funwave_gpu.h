@@ -247,9 +247,11 @@ void *fw_stream(fw_ctx *ctx);
 /* The tuning vector: FW_TUNE_LEN ints, (bx, by) thread-block shapes of the
  * per-cell kernels disp_a, disp_b, update, post_mask_break and maskmul
  * (bx a multiple of 32, bx*by <= 256), then the tile heights of the x-face
- * and the y-face flux kernels (8, 16 or 32 in MIXED; 8 or 16 in FP64).  Every choice computes the same values bit for bit; only the speed
+ * and the y-face flux kernels (8, 16 or 32 in MIXED; 8 or 16 in FP64), then
+ * how those two stage their tiles (0: each thread loads its inputs; 1: TMA
+ * tensor loads of the tile's fields into shared memory).  Every choice computes the same values bit for bit; only the speed
  * differs.  Defaults: 32 x 8 blocks, flux tiles 8 and 32 (16 in FP64). */
-#define FW_TUNE_LEN 12
+#define FW_TUNE_LEN 14
 #define FW_TUNE_FRESH 1   /* fw_autotune flag: measure even if this shape was tuned before */
 /* Choose the tuning vector by timing every candidate of each kernel on this
  * context's state with CUDA events (two sweeps, the faster of each), keeping

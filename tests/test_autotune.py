@@ -49,10 +49,15 @@ def test_every_launch_shape_computes_the_same(fw, precision):
          "maskmul": (64, 2), "flux_x": 16, "flux_y": 16 if precision == "MIXED" else 8},
         {"disp_a": (256, 1), "disp_b": (32, 2), "update": (128, 1), "post_mask_break": (128, 2),
          "maskmul": (32, 8), "flux_x": 32 if precision == "MIXED" else 8, "flux_y": 8 if precision == "MIXED" else 16},
+        # the flux tiles staged by TMA
+        {"disp_a": (32, 8), "disp_b": (32, 8), "update": (32, 8), "post_mask_break": (32, 8), "maskmul": (32, 8),
+         "flux_x": 16, "flux_y": 16, "flux_x_tma": 1, "flux_y_tma": 1},
+        {"disp_a": (32, 8), "disp_b": (32, 8), "update": (32, 8), "post_mask_break": (32, 8), "maskmul": (32, 8),
+         "flux_x": 8, "flux_y": 32 if precision == "MIXED" else 8, "flux_x_tma": 1, "flux_y_tma": 1},
     ]
     for t in alts:
         out = _run(fw, precision, 24, tuning=t)
-        assert out["tuning"] == t
+        assert out["tuning"] == dict({"flux_x_tma": 0, "flux_y_tma": 0}, **t)
         _same(out, ref)
 
 
@@ -68,6 +73,7 @@ def test_autotune_leaves_the_run_unchanged(fw, precision):
         assert bx % 32 == 0 and bx * by <= 256
     for k in ("flux_x", "flux_y"):
         assert t[k] in ((8, 16, 32) if precision == "MIXED" else (8, 16))
+        assert t[k + "_tma"] in (0, 1)
 
 
 @pytest.mark.gpu
@@ -76,7 +82,7 @@ def test_set_tuning_refuses_shapes_that_are_not_built(fw):
     s = fw.Solver(fw.with_defaults(p), precision="MIXED")
     s.init(d)
     good = s.tuning()
-    for bad in ({"update": (48, 4)}, {"maskmul": (64, 8)}, {"flux_x": 64}, {"flux_y": 12}):
+    for bad in ({"update": (48, 4)}, {"maskmul": (64, 8)}, {"flux_x": 64}, {"flux_y": 12}, {"flux_x_tma": 2}):
         t = dict(good)
         t.update(bad)
         with pytest.raises(fw.FwError):
