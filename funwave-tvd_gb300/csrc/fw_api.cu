@@ -8,6 +8,7 @@
 #include <map>
 #include <mutex>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -29,7 +30,8 @@ const char *kErrText[] = {"ok",
                           "non-finite eta",
                           "option not supported by this build",
                           "call out of order (context not initialised)",
-                          "no usable CUDA device"};
+                          "no usable CUDA device",
+                          "checkpoint file unreadable, unwritable or malformed"};
 
 int cuda_status(fw_ctx *c, cudaError_t e) {
     if (e == cudaSuccess && c && c->sticky_error == 0) return FW_OK;
@@ -486,7 +488,7 @@ void fw_params_default(fw_params *p) {
 }
 
 const char *fw_strerror(int s) {
-    if (s > 0 || s < -8) return "unknown status";
+    if (s > 0 || s < -9) return "unknown status";
     return kErrText[-s];
 }
 
@@ -1123,6 +1125,250 @@ int fw_ensemble_destroy(fw_ensemble *e) {
 int fw_sync(fw_ctx *c) {
     if (!c) return FW_ERR_BAD_PARAM;
     return cuda_status(c, cudaStreamSynchronize(c->stream));
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoint / restore of the whole run state.  The reference restarts from
+// written output fields (HOT_START, mod_global.F:387, io.F:805, main.F:189);
+// a checkpoint here holds every device byte the step reads instead (the
+// arena: fields, factorisation, device scalars, statistics, Kahan terms),
+// the orientation of the MASK and AGE ping-pong buffers, the JON_2D band
+// tables, EtaBlowVal and the host-side Grid, so that a restored run goes on
+// bit for bit as the saved one would have.
+// ---------------------------------------------------------------------------
+}  // extern "C"
+namespace {
+
+const char kCkMagic[8] = {'F', 'W', 'C', 'K', 'P', 'T', '0', '1'};
+
+struct CkHeader {
+    char magic[8];
+    uint32_t sizeof_params, sizeof_grid;
+    int32_t precision, pad;
+    uint64_t arena_bytes, band_bytes;  // band_bytes: each of Cm and Sm
+    int64_t off_mask, off_maskn, off_age, off_agen;
+    double EtaBlowVal;
+};
+
+// the fields of fw_params a restore requires to agree (all but device)
+bool same_params(const fw_params &a, const fw_params &b) {
+#define FW_SAME(x) (a.x == b.x)
+    return FW_SAME(Mglob) && FW_SAME(Nglob) && FW_SAME(DX) && FW_SAME(DY) && FW_SAME(periodic) &&
+           FW_SAME(dispersion) && FW_SAME(gamma1) && FW_SAME(gamma2) && FW_SAME(gamma3) && FW_SAME(beta_ref) &&
+           FW_SAME(viscosity_breaking) && FW_SAME(show_breaking) && FW_SAME(cbrk1) && FW_SAME(cbrk2) &&
+           FW_SAME(wavemaker_cbrk) && FW_SAME(nu_bkg) && FW_SAME(swe_eta_dep) && FW_SAME(cfl) && FW_SAME(fixed_dt) &&
+           FW_SAME(dt_fixed) && FW_SAME(froude_cap) && FW_SAME(min_depth) && FW_SAME(min_depth_frc) &&
+           FW_SAME(eta_limiter) && FW_SAME(trough_limit) && FW_SAME(crest_limit) && FW_SAME(direct_sponge) &&
+           FW_SAME(sponge_west) && FW_SAME(sponge_east) && FW_SAME(sponge_south) && FW_SAME(sponge_north) &&
+           FW_SAME(r_sponge) && FW_SAME(a_sponge) && FW_SAME(friction_sponge) && FW_SAME(cd_fixed) &&
+           FW_SAME(wavemaker) && FW_SAME(amp_wk) && FW_SAME(tperiod) && FW_SAME(dep_wk) && FW_SAME(xc_wk) &&
+           FW_SAME(yc_wk) && FW_SAME(theta_wk) && FW_SAME(delta_wk) && FW_SAME(time_ramp) && FW_SAME(ywidth_wk) &&
+           FW_SAME(freq_peak) && FW_SAME(freq_min) && FW_SAME(freq_max) && FW_SAME(gamma_tma) && FW_SAME(hmo) &&
+           FW_SAME(theta_peak) && FW_SAME(sigma_theta) && FW_SAME(nfreq) && FW_SAME(ntheta) && FW_SAME(spreading) &&
+           FW_SAME(spread_s) && FW_SAME(precision) && FW_SAME(track_hmax) && FW_SAME(track_hmin) &&
+           FW_SAME(track_umax) && FW_SAME(track_mfmax) && FW_SAME(steady_time) && FW_SAME(t_intv_mean) &&
+           FW_SAME(track_roller);
+#undef FW_SAME
+}
+
+// the Grid values fw_init (and fw_set_scalar "T_brk") set, taken from src
+void copy_init_grid(Grid &dst, const Grid &src) {
+    dst.T_brk = src.T_brk;
+    dst.width_wk = src.width_wk;
+    dst.D_gen = src.D_gen;
+    dst.beta_gen = src.beta_gen;
+    dst.rlamda = src.rlamda;
+    dst.ilo = src.ilo;
+    dst.ihi = src.ihi;
+    dst.jlo = src.jlo;
+    dst.jhi = src.jhi;
+    fill_float_constants(dst);
+}
+
+template <typename T> void ck_offsets(fw_ctx *c, CkHeader &h, void **band) {
+    fw::Fields<T> &f = c->F<T>();
+    const char *a = (const char *)c->arena;
+    h.off_mask = (const char *)f.MASK - a;
+    h.off_maskn = (const char *)f.MASKn - a;
+    h.off_age = (const char *)f.AGE - a;
+    h.off_agen = (const char *)f.AGEn - a;
+    band[0] = f.Cm;
+    band[1] = f.Sm;
+}
+
+template <typename T> void ck_set_offsets(fw_ctx *c, const CkHeader &h) {
+    fw::Fields<T> &f = c->F<T>();
+    char *a = (char *)c->arena;
+    f.MASK = (uint8_t *)(a + h.off_mask);
+    f.MASKn = (uint8_t *)(a + h.off_maskn);
+    f.AGE = (T *)(a + h.off_age);
+    f.AGEn = (T *)(a + h.off_agen);
+}
+
+size_t band_bytes(const fw_ctx *c, const Grid &g) {
+    if (c->p.wavemaker != FW_WK_JON_2D || g.ihi < g.ilo || g.jhi < g.jlo) return 0;
+    const size_t es = c->p.precision == FW_PREC_FP64 ? sizeof(double) : sizeof(float);
+    return (size_t)(g.ihi - g.ilo + 1) * (size_t)(g.jhi - g.jlo + 1) * (size_t)c->p.nfreq * es;
+}
+
+// device <-> file through one pinned host buffer, in pieces
+const size_t kCkChunk = 64u << 20;
+
+int ck_write(fw_ctx *c, FILE *fp, const void *dev, size_t n, void *pin) {
+    for (size_t o = 0; o < n; o += kCkChunk) {
+        const size_t k = std::min(kCkChunk, n - o);
+        cudaError_t e = cudaMemcpyAsync(pin, (const char *)dev + o, k, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_status(c, e);
+        if (std::fwrite(pin, 1, k, fp) != k) return FW_ERR_IO;
+    }
+    return FW_OK;
+}
+
+int ck_read(fw_ctx *c, FILE *fp, void *dev, size_t n, void *pin) {
+    for (size_t o = 0; o < n; o += kCkChunk) {
+        const size_t k = std::min(kCkChunk, n - o);
+        if (std::fread(pin, 1, k, fp) != k) return FW_ERR_IO;
+        cudaError_t e = cudaMemcpyAsync((char *)dev + o, pin, k, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_status(c, e);
+    }
+    return FW_OK;
+}
+
+struct PinnedBuf {
+    void *p = nullptr;
+    explicit PinnedBuf(size_t n) {
+        if (cudaMallocHost(&p, n) != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+    }
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+struct FileCloser {
+    FILE *f;
+    ~FileCloser() {
+        if (f) std::fclose(f);
+    }
+};
+
+}  // namespace
+extern "C" {
+
+int fw_checkpoint(fw_ctx *c, const char *path) {
+    if (!path) return FW_ERR_BAD_PARAM;
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    CkHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, kCkMagic, sizeof(h.magic));
+    h.sizeof_params = (uint32_t)sizeof(fw_params);
+    h.sizeof_grid = (uint32_t)sizeof(Grid);
+    h.precision = c->p.precision;
+    h.arena_bytes = c->arena_bytes;
+    h.band_bytes = band_bytes(c, c->g);
+    h.EtaBlowVal = c->EtaBlowVal;
+    void *band[2];
+    if (c->p.precision == FW_PREC_FP64) ck_offsets<double>(c, h, band);
+    else ck_offsets<float>(c, h, band);
+    if (h.band_bytes && (!band[0] || !band[1])) return FW_ERR_NOT_READY;
+    PinnedBuf pin(std::min(kCkChunk, std::max(h.arena_bytes, (uint64_t)1)));
+    if (!pin.p) return FW_ERR_OOM;
+    FileCloser fc{std::fopen(path, "wb")};
+    if (!fc.f) return FW_ERR_IO;
+    if (std::fwrite(&h, sizeof(h), 1, fc.f) != 1 || std::fwrite(&c->p, sizeof(fw_params), 1, fc.f) != 1 ||
+        std::fwrite(&c->g, sizeof(Grid), 1, fc.f) != 1)
+        return FW_ERR_IO;
+    if ((rc = ck_write(c, fc.f, c->arena, c->arena_bytes, pin.p)) != FW_OK) return rc;
+    for (int k = 0; k < 2 && h.band_bytes; k++)
+        if ((rc = ck_write(c, fc.f, band[k], h.band_bytes, pin.p)) != FW_OK) return rc;
+    if (std::fflush(fc.f) != 0) return FW_ERR_IO;
+    std::FILE *f = fc.f;
+    fc.f = nullptr;
+    return std::fclose(f) == 0 ? FW_OK : FW_ERR_IO;
+}
+
+int fw_restore(fw_ctx *c, const char *path) {
+    if (!c || !path) return FW_ERR_BAD_PARAM;
+    if (c->sticky_error) return FW_ERR_CUDA;
+    FileCloser fc{std::fopen(path, "rb")};
+    if (!fc.f) return FW_ERR_IO;
+    CkHeader h;
+    fw_params p;
+    Grid g;
+    if (std::fread(&h, sizeof(h), 1, fc.f) != 1 || std::memcmp(h.magic, kCkMagic, sizeof(h.magic)) != 0 ||
+        h.sizeof_params != sizeof(fw_params) || h.sizeof_grid != sizeof(Grid) ||
+        std::fread(&p, sizeof(p), 1, fc.f) != 1 || std::fread(&g, sizeof(g), 1, fc.f) != 1)
+        return FW_ERR_IO;
+    // the saved run must be one this context could have run: the same
+    // parameters, the same arena, and a Grid that differs from this one's
+    // only in what fw_init sets
+    if (!same_params(p, c->p) || h.arena_bytes != c->arena_bytes) return FW_ERR_BAD_PARAM;
+    Grid want = c->g;
+    copy_init_grid(want, g);
+    if (std::memcmp(&want, &g, sizeof(Grid)) != 0) return FW_ERR_BAD_PARAM;
+    if (h.band_bytes != band_bytes(c, g)) return FW_ERR_IO;
+    // the ping-pong buffers must be the two this context carved
+    const bool fp64 = c->p.precision == FW_PREC_FP64;
+    CkHeader mine;
+    void *band[2];
+    if (fp64) ck_offsets<double>(c, mine, band);
+    else ck_offsets<float>(c, mine, band);
+    const bool mask_ok = (h.off_mask == mine.off_mask && h.off_maskn == mine.off_maskn) ||
+                         (h.off_mask == mine.off_maskn && h.off_maskn == mine.off_mask);
+    const bool age_ok = (h.off_age == mine.off_age && h.off_agen == mine.off_agen) ||
+                        (h.off_age == mine.off_agen && h.off_agen == mine.off_age);
+    if (!mask_ok || !age_ok) return FW_ERR_IO;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    // band tables: (re)allocate to the saved size
+    void *nb[2] = {nullptr, nullptr};
+    if (h.band_bytes) {
+        if (cudaMalloc(&nb[0], h.band_bytes) != cudaSuccess || cudaMalloc(&nb[1], h.band_bytes) != cudaSuccess) {
+            cudaGetLastError();
+            if (nb[0]) cudaFree(nb[0]);
+            return FW_ERR_OOM;
+        }
+    }
+    PinnedBuf pin(std::min(kCkChunk, std::max(h.arena_bytes, (uint64_t)1)));
+    int rc = pin.p ? FW_OK : FW_ERR_OOM;
+    // from here a failure leaves the context un-initialised: its arena may
+    // hold part of the file
+    c->initialized = 0;
+    if (rc == FW_OK) rc = ck_read(c, fc.f, c->arena, c->arena_bytes, pin.p);
+    for (int k = 0; k < 2 && h.band_bytes && rc == FW_OK; k++) rc = ck_read(c, fc.f, nb[k], h.band_bytes, pin.p);
+    if (rc == FW_OK && std::fgetc(fc.f) != EOF) rc = FW_ERR_IO;  // trailing bytes: not this format
+    if (rc != FW_OK) {
+        for (void *b : nb)
+            if (b) cudaFree(b);
+        return rc;
+    }
+    for (void *b : band)
+        if (b) cudaFree(b);
+    if (fp64) {
+        ck_set_offsets<double>(c, h);
+        c->fd.Cm = (double *)nb[0];
+        c->fd.Sm = (double *)nb[1];
+    } else {
+        ck_set_offsets<float>(c, h);
+        c->ff.Cm = (float *)nb[0];
+        c->ff.Sm = (float *)nb[1];
+    }
+    c->g = g;
+    c->EtaBlowVal = h.EtaBlowVal;
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    c->graph_ready = 0;
+    c->initialized = 1;
+    return FW_OK;
 }
 
 long long fw_launch_count(fw_ctx *c) { return c ? c->launches : -1; }

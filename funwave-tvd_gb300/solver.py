@@ -38,7 +38,7 @@ _SOURCES = {
 
 FW_ERRORS = {0: "FW_OK", -1: "FW_ERR_CUDA", -2: "FW_ERR_OOM", -3: "FW_ERR_BAD_PARAM",
              -4: "FW_ERR_BLOWUP", -5: "FW_ERR_NAN", -6: "FW_ERR_UNSUPPORTED",
-             -7: "FW_ERR_NOT_READY", -8: "FW_ERR_NO_DEVICE"}
+             -7: "FW_ERR_NOT_READY", -8: "FW_ERR_NO_DEVICE", -9: "FW_ERR_IO"}
 
 
 class FwError(RuntimeError):
@@ -244,6 +244,8 @@ def load_library(path=None):
     L.fw_autotune.argtypes = [vp, ip]
     L.fw_get_tuning.argtypes = [vp, ctypes.POINTER(ip)]
     L.fw_set_tuning.argtypes = [vp, ctypes.POINTER(ip)]
+    L.fw_checkpoint.argtypes = [vp, ctypes.c_char_p]
+    L.fw_restore.argtypes = [vp, ctypes.c_char_p]
     L.fw_strerror.argtypes = [ip]
     L.fw_strerror.restype = ctypes.c_char_p
     if path == lib_path():
@@ -373,6 +375,17 @@ class Solver:
 
     def sync(self):
         self._check(self.L.fw_sync(self.ctx), "fw_sync")
+
+    # --- restart ----------------------------------------------------------
+    def checkpoint(self, path):
+        """Write the complete run state to path (fw_checkpoint)."""
+        self._check(self.L.fw_checkpoint(self.ctx, os.fsencode(path)), "fw_checkpoint")
+
+    def restore(self, path):
+        """Load a checkpoint written by a Solver with the same parameters;
+        no init() is needed first (fw_restore).  The run then continues bit
+        for bit as the checkpointed one."""
+        self._check(self.L.fw_restore(self.ctx, os.fsencode(path)), "fw_restore")
 
     # --- the reference's units ------------------------------------------
     def exchange(self):

@@ -33,6 +33,7 @@ extern "C" {
 #define FW_ERR_UNSUPPORTED -6   /* option not built into this library */
 #define FW_ERR_NOT_READY   -7   /* call order violated (e.g. step before init) */
 #define FW_ERR_NO_DEVICE   -8   /* no usable CUDA device */
+#define FW_ERR_IO          -9   /* checkpoint file unreadable, unwritable or malformed */
 
 /* precision of the bulk arithmetic */
 #define FW_PREC_FP64  0   /* every field and operation in double */
@@ -232,6 +233,23 @@ int fw_sponge_damping(fw_ctx *ctx);      /* SPONGE_DAMPING  sponge.F:52 */
 
 /* Kernel launches issued by this context since creation (diagnostics;
  * launches recorded into a CUDA graph are counted once, at capture). */
+/* Checkpoint / restore of the complete run state: every device field and
+ * scalar the step reads (TIME, DT, masks, AGE, the statistics and their
+ * compensation terms, the factorisation), the JON_2D band tables and the
+ * values fw_init computed on the host.  A restored run continues bit for
+ * bit as the checkpointed one.  Replaces the reference's HOT_START restart
+ * from output fields (mod_global.F:387, io.F:805, main.F:189), which
+ * restarts from rounded fields and zero statistics instead.
+ *   fw_checkpoint  waits for the stream, then writes path; FW_ERR_IO when
+ *                  the file cannot be written.
+ *   fw_restore     into a context created with the same fw_params (device
+ *                  may differ), initialised or not; FW_ERR_BAD_PARAM when
+ *                  the parameters differ, FW_ERR_IO for an unreadable or
+ *                  malformed file.  A failure after the file's header
+ *                  checked out leaves the context un-initialised. */
+int fw_checkpoint(fw_ctx *ctx, const char *path);
+int fw_restore(fw_ctx *ctx, const char *path);
+
 long long fw_launch_count(fw_ctx *ctx);
 /* Time nrep back-to-back launches of one kernel of the step with CUDA events
  * on the context stream; *ms_per_launch = average duration.  Names:
