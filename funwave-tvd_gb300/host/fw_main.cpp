@@ -22,6 +22,10 @@
 // buffer with TOTAL_TIME rows, every sample is kept and the last buffer
 // holds only the rows taken.
 //
+// INI_UVZ starts from ETA_FILE / U_FILE / V_FILE at HotStartTime as the
+// reference does; HOT_START / HOTSTART_FILE / HOTSTART_INTV restart from and
+// write exact checkpoints (fw_checkpoint, fw_restore).
+//
 // --dry-run parses, builds the depth and writes dep.out without touching a
 // GPU.  JON_2D phases, which the reference draws from the compiler's
 // rand(0), come from SplitMix64 seeded by the key PHASE_SEED (default 1).
@@ -163,30 +167,37 @@ void fill_params(const Input &in, fw_params &p) {
 
 // DEPTH_TYPE DATA / FLAT / SLOPE (init.F:684-760), interior Mglob x Nglob,
 // column-major
+// an interior Mglob x Nglob array as GetFile reads it: list-directed
+// READ(1,*) row by row, Mglob values per J, J outer (init.F:1359-1379)
+bool read_interior(const std::string &file, const fw_params &p, std::vector<double> &d, std::string &err) {
+    const int M = p.Mglob, N = p.Nglob;
+    d.assign((size_t)M * N, 0.0);
+    std::ifstream f(file);
+    if (!f) {
+        err = file + " CANNOT BE FOUND";
+        return false;
+    }
+    for (int j = 0; j < N; j++)
+        for (int i = 0; i < M; i++) {
+            std::string tok;
+            if (!(f >> tok)) {
+                err = "file " + file + " ends early";
+                return false;
+            }
+            for (auto &ch : tok)
+                if (ch == 'd' || ch == 'D') ch = 'e';
+            d[(size_t)i + (size_t)j * M] = std::strtod(tok.c_str(), nullptr);
+        }
+    return true;
+}
+
 bool build_depth(const Input &in, const fw_params &p, std::vector<double> &d, std::string &err) {
     const int M = p.Mglob, N = p.Nglob;
     d.assign((size_t)M * N, 0.0);
     const std::string type = upper(in.str("DEPTH_TYPE", "DATA")).substr(0, 3);
     const double flat = in.num("DEPTH_FLAT", 10.0);
     if (type == "DAT") {
-        const std::string file = in.str("DEPTH_FILE", "depth.txt");
-        std::ifstream f(file);
-        if (!f) {
-            err = file + " CANNOT BE FOUND";
-            return false;
-        }
-        // list-directed READ(1,*) row by row: Mglob values per J, J outer
-        for (int j = 0; j < N; j++)
-            for (int i = 0; i < M; i++) {
-                std::string tok;
-                if (!(f >> tok)) {
-                    err = "depth file " + file + " ends early";
-                    return false;
-                }
-                for (auto &ch : tok)
-                    if (ch == 'd' || ch == 'D') ch = 'e';
-                d[(size_t)i + (size_t)j * M] = std::strtod(tok.c_str(), nullptr);
-            }
+        if (!read_interior(in.str("DEPTH_FILE", "depth.txt"), p, d, err)) return false;
     } else if (type == "FLA") {
         for (auto &v : d) v = flat;
     } else if (type == "SLO") {
@@ -335,13 +346,61 @@ int main(int argc, char **argv) {
         phases.resize((size_t)p.nfreq * p.ntheta);
         for (auto &v : phases) v = (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0) * TWO_PI;
     }
+    // INI_UVZ (io.F:712-801, init.F:1283-1386): the initial eta from
+    // ETA_FILE and u, v from U_FILE and V_FILE (zero when V_FILE is not
+    // given: the reference decides NO_UV_FILE by V_FILE alone), and TIME =
+    // HotStartTime (main.F:188-190).  MASK_FILE is not read: the mask follows
+    // from eta and depth (init.F:1000-1014, the NO_MASK_FILE rule).
+    std::vector<double> eta0, u0, v0;
+    const bool ini_uvz = in.flag("INI_UVZ", 0) != 0;
+    if (ini_uvz) {
+        if (in.flag("BED_DEFORMATION", 0)) {
+            std::fprintf(stderr, "fw_main: BED_DEFORMATION is not built\n");
+            return 1;
+        }
+        if (!in.has("ETA_FILE")) {
+            std::fprintf(stderr, "fw_main: You use INI_UVZ, ETA_FILE NOT FOUND, STOP\n");
+            return 1;
+        }
+        bool ok = read_interior(in.str("ETA_FILE", ""), p, eta0, err);
+        if (ok && in.has("V_FILE"))
+            ok = read_interior(in.str("U_FILE", ""), p, u0, err) && read_interior(in.str("V_FILE", ""), p, v0, err);
+        if (!ok) {
+            std::fprintf(stderr, "fw_main: %s\n", err.c_str());
+            return 1;
+        }
+    }
+    // exact checkpoints through fw_checkpoint / fw_restore, under the names
+    // of the reference's declared hot-start variables (mod_global.F:141-145,
+    // 387; main.F:73-133), which its input reader never sets:
+    //   HOT_START = T     restore HOTSTART_FILE instead of initialising
+    //   HOTSTART_INTV     every HOTSTART_INTV s of model time, write
+    //                     RESULT_FOLDER/hotstart_NNNNN (NNNNN from 1)
+    // Each checkpoint has a text companion <file>.host holding this driver's
+    // output counters, so a restored run numbers and times its files as the
+    // uninterrupted run would; station files are appended to.
+    const bool hot_start = in.flag("HOT_START", 0) != 0;
+    const std::string hot_file = in.str("HOTSTART_FILE", "");
+    const double hot_intv = in.num("HOTSTART_INTV", 0.0);
+    if (hot_start && hot_file.empty()) {
+        std::fprintf(stderr, "fw_main: HOT_START needs HOTSTART_FILE\n");
+        return 1;
+    }
     fw_ctx *ctx = nullptr;
     int rc = fw_create(&p, &ctx);
     if (rc != FW_OK) return fail("fw_create", rc);
-    rc = fw_init(ctx, depth.data(), nullptr, nullptr, nullptr, phases.empty() ? nullptr : phases.data());
-    if (rc != FW_OK) return fail("fw_init", rc);
+    if (hot_start) {
+        rc = fw_restore(ctx, hot_file.c_str());
+        if (rc != FW_OK) return fail("fw_restore", rc);
+    } else {
+        rc = fw_init(ctx, depth.data(), eta0.empty() ? nullptr : eta0.data(), u0.empty() ? nullptr : u0.data(),
+                     v0.empty() ? nullptr : v0.data(), phases.empty() ? nullptr : phases.data());
+        if (rc != FW_OK) return fail("fw_init", rc);
+        if (ini_uvz && (rc = fw_set_scalar(ctx, "TIME", in.num("HotStartTime", 0.0))) != FW_OK)
+            return fail("HotStartTime", rc);
+    }
 
-    FILE *tdt = std::fopen("time_dt.out", "w");
+    FILE *tdt = std::fopen("time_dt.out", hot_start ? "a" : "w");
     std::vector<int> mask((size_t)Mloc * Nloc);
     int icount = 0;
     const bool binary = upper(in.str("FIELD_IO_TYPE", "ASCII")) == "BINARY";
@@ -372,7 +431,7 @@ int main(int argc, char **argv) {
             if (is >= 4 && is <= p.Mglob + 3 && js >= 4 && js <= p.Nglob + 3) {
                 char b[16];
                 std::snprintf(b, sizeof b, "%04d", k);
-                FILE *f = std::fopen((dir + "sta_" + b).c_str(), "w");
+                FILE *f = std::fopen((dir + "sta_" + b).c_str(), hot_start ? "a" : "w");
                 if (!f) return 1;
                 sta_id.push_back(k);
                 sta_i.push_back(is);
@@ -443,22 +502,66 @@ int main(int argc, char **argv) {
 
     double time = 0.0, dt = 0.0, plot_count = plot_intv;  // init.F:631
     double plot_count_sta = plot_intv_sta;                  // init.F:632
+    double hot_count = 0.0;
+    int hot_number = 0;
+    fw_get_scalar(ctx, "TIME", &time);
+    if (hot_start) {
+        // the counters the checkpointing run had (TIME and DT are restored)
+        FILE *hf = std::fopen((hot_file + ".host").c_str(), "r");
+        if (!hf || std::fscanf(hf, "%d %la %la %la %d", &icount, &plot_count, &plot_count_sta, &hot_count,
+                               &hot_number) != 5) {
+            std::fprintf(stderr, "fw_main: cannot read %s.host\n", hot_file.c_str());
+            if (hf) std::fclose(hf);
+            return 1;
+        }
+        std::fclose(hf);
+        fw_get_scalar(ctx, "DT", &dt);
+    }
+    // a checkpoint at the top of a pass, after that pass's output; the
+    // station rows taken so far are written first
+    auto hotstart = [&]() -> int {
+        for (size_t k = 0; k < sta_f.size(); k++) {
+            flush_station(k);
+            std::fflush(sta_f[k]);
+        }
+        if (tdt) std::fflush(tdt);
+        char b[16];
+        std::snprintf(b, sizeof b, "%05d", ++hot_number);
+        const std::string f = dir + "hotstart_" + b;
+        int r = fw_checkpoint(ctx, f.c_str());
+        if (r != FW_OK) return r;
+        FILE *hf = std::fopen((f + ".host").c_str(), "w");
+        if (!hf) return FW_ERR_IO;
+        std::fprintf(hf, "%d %a %a %a %d\n", icount, plot_count, plot_count_sta, hot_count, hot_number);
+        return std::fclose(hf) == 0 ? FW_OK : FW_ERR_IO;
+    };
+    // a restored run begins at the step of the pass its checkpoint was
+    // written in: that pass's output and counters are already done
+    bool resume = hot_start;
     while (time < total) {  // DO WHILE (TIME < TOTAL_TIME)
         // OUTPUT (io.F:52-134) at the top of the pass, with the last DT
-        if (!sta_i.empty()) {
+        if (!resume && !sta_i.empty()) {
             plot_count_sta += dt;
             if (plot_count_sta >= plot_intv_sta) {
                 plot_count_sta -= plot_intv_sta;
                 if ((rc = stations(time)) != FW_OK) return fail("STATIONS", rc);
             }
         }
-        if (time >= plot_start) {
+        if (!resume && time >= plot_start) {
             plot_count += dt;
             if (plot_count >= plot_intv) {
                 plot_count -= plot_intv;
                 if ((rc = preview(icount + 1)) != FW_OK) return fail("PREVIEW", rc);
             }
         }
+        if (!resume && hot_intv > 0.0) {
+            hot_count += dt;
+            if (hot_count >= hot_intv) {
+                hot_count -= hot_intv;
+                if ((rc = hotstart()) != FW_OK) return fail("fw_checkpoint", rc);
+            }
+        }
+        resume = false;
         int status = FW_OK;
         rc = fw_step(ctx, 1, &status);
         if (rc != FW_OK) return fail("fw_step", rc);

@@ -191,3 +191,114 @@ def test_get_points_equals_fields(fw):
                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
         assert rc == -3
         s.close()
+
+
+def _run_driver(fw, d, extra):
+    _write_input(d, extra)
+    r = subprocess.run([_driver(fw), os.path.join(d, "input.txt")], capture_output=True, text=True, cwd=d,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r
+
+
+_SLOPE = {"DEPTH_TYPE": "SLOPE", "DEPTH_FLAT": 3.0, "SLP": 0.2, "Xslp": 20.0, "WAVEMAKER": "WK_REG",
+          "AMP_WK": 0.05, "Tperiod": 3.0, "DEP_WK": 3.0, "Xc_WK": 10.0, "Time_ramp": 1.0, "PERIODIC": "T",
+          "MinDepth": 0.01, "FIELD_IO_TYPE": "BINARY"}
+
+
+@pytest.mark.gpu
+def test_driver_hot_start_continues_the_run_exactly(fw, tmp_path):
+    """HOTSTART_INTV writes exact checkpoints (fw_checkpoint); a run with
+    HOT_START from one of them writes the same files, byte for byte, as the
+    uninterrupted run from that point on: fields, time_dt.out and station
+    rows."""
+    a, b = str(tmp_path / "a"), str(tmp_path / "b")
+    os.makedirs(a)
+    os.makedirs(b)
+    for d in (a, b):
+        with open(os.path.join(d, "stations.txt"), "w") as f:
+            f.write("6 5\n12 9\n")
+    common = dict(_SLOPE, TOTAL_TIME=4.0, PLOT_INTV=0.5, NumberStations=2, PLOT_INTV_STATION=0.25,
+                  StationOutputBuffer=3, PRECISION="MIXED")
+    _run_driver(fw, a, dict(common, STATIONS_FILE=os.path.join(a, "stations.txt"), HOTSTART_INTV=1.5))
+    assert sorted(f for f in os.listdir(a) if f.startswith("hotstart_")) == [
+        "hotstart_00001", "hotstart_00001.host", "hotstart_00002", "hotstart_00002.host"]
+    ck = os.path.join(a, "hotstart_00001")
+    n_before = int(open(ck + ".host").read().split()[0])  # files written before the checkpoint
+    _run_driver(fw, b, dict(common, STATIONS_FILE=os.path.join(b, "stations.txt"), HOT_START="T",
+                            HOTSTART_FILE=ck))
+    fa = sorted(f for f in os.listdir(a) if f.startswith(("eta_", "u_", "v_", "mask_")))
+    fb = sorted(f for f in os.listdir(b) if f.startswith(("eta_", "u_", "v_", "mask_")))
+    assert fb == [f for f in fa if int(f.split("_")[1]) > n_before] and len(fb) >= 8
+    for f in fb:
+        assert open(os.path.join(a, f), "rb").read() == open(os.path.join(b, f), "rb").read(), f
+    ta = open(os.path.join(a, "time_dt.out")).read().splitlines()
+    tb = open(os.path.join(b, "time_dt.out")).read().splitlines()
+    assert tb == ta[n_before:]
+    for k in ("sta_0001", "sta_0002"):
+        ra = open(os.path.join(a, k)).read().splitlines()
+        rb = open(os.path.join(b, k)).read().splitlines()
+        assert len(rb) >= 4 and ra[len(ra) - len(rb):] == rb
+    # the restored run's next checkpoint falls on the same pass with the
+    # same counters
+    _run_driver(fw, b, dict(common, STATIONS_FILE=os.path.join(b, "stations.txt"), HOT_START="T",
+                            HOTSTART_FILE=ck, HOTSTART_INTV=1.5))
+    for f in ("hotstart_00002.host",):
+        assert open(os.path.join(a, f)).read() == open(os.path.join(b, f)).read()
+    assert os.path.getsize(os.path.join(a, "hotstart_00002")) == os.path.getsize(os.path.join(b, "hotstart_00002"))
+
+
+@pytest.mark.gpu
+def test_driver_ini_uvz_hot_start_time(fw, tmp_path):
+    """INI_UVZ (init.F:1283-1386): eta, u, v from ETA_FILE, U_FILE, V_FILE
+    (list-directed rows of Mglob values) and TIME = HotStartTime
+    (main.F:188-190): the run equals the Solver initialised with the same
+    state and TIME; without V_FILE u and v start at zero."""
+    d = str(tmp_path)
+    rng = np.random.default_rng(3)
+    I = np.arange(1, 25)
+    i0 = int(20.0 / 2.0) + 1
+    h = np.where(I >= i0, 3.0 - 0.2 * (I - i0) * 2.0, 3.0)
+    depth = np.asfortranarray(np.repeat(h[:, None], 16, axis=1))
+    wet = depth > 0.5
+    eta = np.where(wet, 0.02 * rng.standard_normal((24, 16)), 0.0)
+    u = np.where(wet, 0.05 * rng.standard_normal((24, 16)), 0.0)
+    v = np.where(wet, 0.05 * rng.standard_normal((24, 16)), 0.0)
+    for name, arr in (("eta0.txt", eta), ("u0.txt", u), ("v0.txt", v)):
+        with open(os.path.join(d, name), "w") as f:
+            for j in range(16):
+                f.write(" ".join("%.17e" % x for x in arr[:, j]) + "\n")
+    t0 = 7.25
+    keys = _write_input(d, dict(_SLOPE, TOTAL_TIME=t0 + 1.0, PLOT_INTV=0.5, INI_UVZ="T", HotStartTime=t0,
+                                ETA_FILE=os.path.join(d, "eta0.txt"), U_FILE=os.path.join(d, "u0.txt"),
+                                V_FILE=os.path.join(d, "v0.txt")))
+    r = subprocess.run([_driver(fw), os.path.join(d, "input.txt")], capture_output=True, text=True, cwd=d,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    times = np.loadtxt(os.path.join(d, "time_dt.out"), ndmin=2)
+    assert times[0, 0] == t0
+    files = sorted(f for f in os.listdir(d) if f.startswith("eta_"))
+    first = np.fromfile(os.path.join(d, files[0]), dtype=np.float64).reshape(16, 24).T
+    kept = eta >= -depth  # elsewhere dry: eta = -MinDepth - depth (init.F:1000-1014)
+    assert np.array_equal(first[kept], eta[kept]) and np.all(first[~kept] == -0.01 - depth[~kept])
+    p = {k: v for k, v in keys.items() if k not in ("RESULT_FOLDER", "FIELD_IO_TYPE", "INI_UVZ", "HotStartTime",
+                                                     "ETA_FILE", "U_FILE", "V_FILE", "DEPTH_TYPE", "DEPTH_FLAT",
+                                                     "SLP", "Xslp")}
+    p["PERIODIC"] = True
+    s = fw.Solver(fw.with_defaults(p), precision="FP64")
+    s.init(depth, np.asfortranarray(eta), np.asfortranarray(u), np.asfortranarray(v))
+    s.set_scalar("TIME", t0)
+    while s.scalar("TIME") < times[-1, 0] * (1.0 - 1e-12):
+        s.step(1)
+    last = np.fromfile(os.path.join(d, files[-1]), dtype=np.float64).reshape(16, 24).T
+    assert np.array_equal(last, s.get("Eta")[3:-3, 3:-3])
+    s.close()
+    # no V_FILE: u and v start at zero
+    os.remove(os.path.join(d, "time_dt.out"))
+    _write_input(d, dict(_SLOPE, TOTAL_TIME=t0 + 0.1, PLOT_INTV=0.5, INI_UVZ="T", HotStartTime=t0,
+                         ETA_FILE=os.path.join(d, "eta0.txt"), U_FILE=os.path.join(d, "u0.txt")))
+    r = subprocess.run([_driver(fw), os.path.join(d, "input.txt")], capture_output=True, text=True, cwd=d,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    u1 = np.fromfile(os.path.join(d, "u_00001"), dtype=np.float64).reshape(16, 24).T
+    assert np.all(u1 == 0.0)
