@@ -314,6 +314,22 @@ unsigned long long *etamax_ptr(fw_ctx *c) {
     return c->p.precision == FW_PREC_FP64 ? c->fd.etamax_bits : c->ff.etamax_bits;
 }
 
+template <typename T> void save_pingpong(fw_ctx *c, void **p) {
+    fw::Fields<T> &f = c->F<T>();
+    p[0] = f.MASK;
+    p[1] = f.MASKn;
+    p[2] = f.AGE;
+    p[3] = f.AGEn;
+}
+
+template <typename T> void load_pingpong(fw_ctx *c, void *const *p) {
+    fw::Fields<T> &f = c->F<T>();
+    f.MASK = (uint8_t *)p[0];
+    f.MASKn = (uint8_t *)p[1];
+    f.AGE = (T *)p[2];
+    f.AGEn = (T *)p[3];
+}
+
 // host pointer state that a captured graph bakes in
 long long swap_state(fw_ctx *c) {
     if (c->p.precision == FW_PREC_FP64) return (long long)((uintptr_t)c->fd.MASK ^ ((uintptr_t)c->fd.AGE << 1));
@@ -623,7 +639,14 @@ int fw_create(const fw_params *p, fw_ctx **out) {
 int fw_destroy(fw_ctx *c) {
     if (!c) return FW_ERR_BAD_PARAM;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->out_stream) cudaStreamSynchronize(c->out_stream);
     if (c->graph) cudaGraphExecDestroy(c->graph);
+    for (cudaGraphExec_t g1 : c->graph1)
+        if (g1) cudaGraphExecDestroy(g1);
+    if (c->out_buf) cudaFree(c->out_buf);
+    if (c->out_ready) cudaEventDestroy(c->out_ready);
+    if (c->out_done) cudaEventDestroy(c->out_done);
+    if (c->out_stream) cudaStreamDestroy(c->out_stream);
     void *band[4] = {(void *)c->fd.Cm, (void *)c->fd.Sm, (void *)c->ff.Cm, (void *)c->ff.Sm};
     for (void *b : band)
         if (b) cudaFree(b);
@@ -726,7 +749,7 @@ int fw_init(fw_ctx *c, const double *depth, const double *eta, const double *u, 
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;
     }
-    c->graph_ready = 0;
+    c->invalidate_graphs();
     c->initialized = 1;
     return FW_OK;
 }
@@ -814,7 +837,7 @@ int fw_set_scalar(fw_ctx *c, const char *name, double v) {
         c->g.T_brk = v;
         fill_float_constants(c->g);
     } else return FW_ERR_BAD_PARAM;
-    c->graph_ready = 0;
+    c->invalidate_graphs();
     return FW_OK;
 }
 
@@ -911,9 +934,39 @@ static int enqueue_steps(fw_ctx *c, int nsteps, bool reset_max) {
         left -= 2;
     }
     if (left == 1) {
-        if (fp64) enqueue_step<double>(c);
-        else enqueue_step<float>(c);
-        c->graph_ready = 0;
+        // a one-step graph for the current orientation (a step flips it);
+        // two are kept, so a loop of single steps replays them in turn
+        const long long st = swap_state(c);
+        int slot = -1;
+        for (int k = 0; k < 2; k++)
+            if (c->graph1[k] && c->graph1_ok[k] && c->graph1_state[k] == st) slot = k;
+        if (slot < 0) {
+            slot = !c->graph1_ok[0] ? 0 : !c->graph1_ok[1] ? 1 : c->graph1_next;
+            c->graph1_next = slot ^ 1;
+            if (c->graph1[slot]) {
+                cudaGraphExecDestroy(c->graph1[slot]);
+                c->graph1[slot] = nullptr;
+            }
+            c->graph1_ok[slot] = 0;
+            cudaGraph_t graph;
+            e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return cuda_status(c, e);
+            if (fp64) enqueue_step<double>(c);
+            else enqueue_step<float>(c);
+            e = cudaStreamEndCapture(c->stream, &graph);
+            if (e != cudaSuccess) return cuda_status(c, e);
+            e = cudaGraphInstantiate(&c->graph1[slot], graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_status(c, e);
+            c->graph1_ok[slot] = 1;
+            c->graph1_state[slot] = st;
+            if (fp64) save_pingpong<double>(c, c->graph1_post[slot]);
+            else save_pingpong<float>(c, c->graph1_post[slot]);
+        }
+        e = cudaGraphLaunch(c->graph1[slot], c->stream);
+        if (e != cudaSuccess) return cuda_status(c, e);
+        if (fp64) load_pingpong<double>(c, c->graph1_post[slot]);
+        else load_pingpong<float>(c, c->graph1_post[slot]);
     }
     return finish(c);
 }
@@ -1366,8 +1419,113 @@ int fw_restore(fw_ctx *c, const char *path) {
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;
     }
-    c->graph_ready = 0;
+    c->invalidate_graphs();
     c->initialized = 1;
+    return FW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Asynchronous output: PREVIEW's field transfers (io.F:4304-4621) without
+// holding the step.  The snapshot is taken on the step stream, so it sees
+// the state after every step enqueued before it; the device-to-host copies
+// run on a second stream while later steps run.
+// ---------------------------------------------------------------------------
+int fw_output_wait(fw_ctx *c) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    if (!c->out_pending) return FW_OK;
+    cudaError_t e = cudaEventSynchronize(c->out_done);
+    c->out_pending = 0;
+    return cuda_status(c, e);
+}
+
+int fw_output_done(fw_ctx *c) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    if (!c->out_pending) return 1;
+    cudaError_t e = cudaEventQuery(c->out_done);
+    if (e == cudaErrorNotReady) return 0;
+    if (e != cudaSuccess) return cuda_status(c, e);
+    c->out_pending = 0;
+    return 1;
+}
+
+int fw_output_begin(fw_ctx *c, int n, const char *const *names, void *const *host) {
+    int rc = check_ready(c);
+    if (rc != FW_OK) return rc;
+    if (n < 1 || !names || !host) return FW_ERR_BAD_PARAM;
+    const bool fp64 = c->p.precision == FW_PREC_FP64;
+    std::vector<FieldRef> refs((size_t)n);
+    std::vector<size_t> off((size_t)n + 1, 0);
+    for (int k = 0; k < n; k++) {
+        if (!names[k] || !host[k]) return FW_ERR_BAD_PARAM;
+        const bool ok = fp64 ? find_field<double>(c, names[k], refs[k]) : find_field<float>(c, names[k], refs[k]);
+        if (!ok) return FW_ERR_BAD_PARAM;
+        int w, h;
+        extent(c, refs[k].kind, w, h);
+        const size_t bytes = (size_t)w * h * (refs[k].is_mask ? sizeof(int) : sizeof(double));
+        off[k + 1] = off[k] + (bytes + 255) / 256 * 256;
+    }
+    // the previous snapshot's copies read out_buf: let them finish
+    if ((rc = fw_output_wait(c)) != FW_OK) return rc;
+    cudaError_t e = cudaSuccess;
+    if (!c->out_stream) {
+        e = cudaStreamCreateWithFlags(&c->out_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->out_ready, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->out_done, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_status(c, e);
+    }
+    if (off[n] > c->out_cap) {
+        // nothing reads the old buffer: the copies waited for above ran
+        // after the previous snapshot's kernels
+        if (c->out_buf) cudaFree(c->out_buf);
+        c->out_buf = nullptr;
+        c->out_cap = 0;
+        if (cudaMalloc(&c->out_buf, off[n]) != cudaSuccess) {
+            cudaGetLastError();
+            return FW_ERR_OOM;
+        }
+        c->out_cap = off[n];
+    }
+    char *buf = (char *)c->out_buf;
+    for (int k = 0; k < n && e == cudaSuccess; k++) {
+        const FieldRef &r = refs[k];
+        int w, h;
+        extent(c, r.kind, w, h);
+        if (!r.is_mask && fp64)
+            e = cudaMemcpy2DAsync(buf + off[k], (size_t)w * sizeof(double), r.ptr, (size_t)c->g.pitch * sizeof(double),
+                                  (size_t)w * sizeof(double), (size_t)h, cudaMemcpyDeviceToDevice, c->stream);
+        else
+            convert_out(c, r.ptr, r.is_mask, buf + off[k], w, h);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(c->out_ready, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->out_stream, c->out_ready, 0);
+    for (int k = 0; k < n && e == cudaSuccess; k++) {
+        int w, h;
+        extent(c, refs[k].kind, w, h);
+        const size_t bytes = (size_t)w * h * (refs[k].is_mask ? sizeof(int) : sizeof(double));
+        e = cudaMemcpyAsync(host[k], buf + off[k], bytes, cudaMemcpyDeviceToHost, c->out_stream);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(c->out_done, c->out_stream);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    c->out_pending = 1;
+    return finish(c);
+}
+
+int fw_host_alloc(size_t bytes, void **ptr) {
+    if (!ptr) return FW_ERR_BAD_PARAM;
+    *ptr = nullptr;
+    if (cudaMallocHost(ptr, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return FW_ERR_OOM;
+    }
+    return FW_OK;
+}
+
+int fw_host_free(void *ptr) {
+    if (ptr && cudaFreeHost(ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return FW_ERR_CUDA;
+    }
     return FW_OK;
 }
 
@@ -1413,7 +1571,7 @@ int fw_set_tuning(fw_ctx *c, const int *t) {
     if (!c || !t) return FW_ERR_BAD_PARAM;
     if (!tune_valid(c, t)) return FW_ERR_BAD_PARAM;
     std::memcpy(c->tune, t, sizeof(c->tune));
-    c->graph_ready = 0;
+    c->invalidate_graphs();
     return FW_OK;
 }
 
@@ -1434,7 +1592,7 @@ int fw_autotune(fw_ctx *c, int flags) {
         auto it = tune_cache.find(key);
         if (it != tune_cache.end()) {
             std::memcpy(c->tune, it->second.data(), sizeof(c->tune));
-            c->graph_ready = 0;
+            c->invalidate_graphs();
             return FW_OK;
         }
     }
@@ -1488,7 +1646,7 @@ int fw_autotune(fw_ctx *c, int flags) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->arena, save, c->arena_bytes, cudaMemcpyDeviceToDevice, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     cudaFree(save);
-    c->graph_ready = 0;
+    c->invalidate_graphs();
     if (e != cudaSuccess) return cuda_status(c, e);
     {
         std::lock_guard<std::mutex> lk(tune_mu);

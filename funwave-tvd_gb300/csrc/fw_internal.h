@@ -182,6 +182,23 @@ struct fw_ctx {
     int graph_ready = 0;
     int factored = 0;            // mixed path solves with the constant factorisation
     long long graph_state = 0;   // host buffer state the graph was captured with
+    // one-step graphs, one per ping-pong orientation (fw_step(ctx, 1, ...)
+    // as a time loop with the reference's shape calls it)
+    cudaGraphExec_t graph1[2] = {nullptr, nullptr};
+    long long graph1_state[2] = {0, 0};
+    // the MASK, MASKn, AGE, AGEn pointers after each graph's step: a replay
+    // does not run the host-side swaps that capturing the step did
+    void *graph1_post[2][4] = {};
+    int graph1_ok[2] = {0, 0};
+    int graph1_next = 0;
+    void invalidate_graphs() { graph_ready = graph1_ok[0] = graph1_ok[1] = 0; }
+    // asynchronous output (fw_output_begin / fw_output_wait): host-layout
+    // snapshots in out_buf, copied to the caller's buffers on out_stream
+    void *out_buf = nullptr;
+    size_t out_cap = 0;
+    cudaStream_t out_stream = nullptr;
+    cudaEvent_t out_ready = nullptr, out_done = nullptr;
+    int out_pending = 0;
     template <typename T> fw::Fields<T> &F();
 };
 namespace fw {

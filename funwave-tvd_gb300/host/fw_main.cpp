@@ -35,11 +35,16 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
 #include <fstream>
+#include <functional>
 #include <map>
+#include <mutex>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "funwave_gpu.h"
@@ -401,13 +406,9 @@ int main(int argc, char **argv) {
     }
 
     FILE *tdt = std::fopen("time_dt.out", hot_start ? "a" : "w");
-    std::vector<int> mask((size_t)Mloc * Nloc);
     int icount = 0;
     const bool binary = upper(in.str("FIELD_IO_TYPE", "ASCII")) == "BINARY";
     const bool out_roller = in.flag("ROLLER", 0) != 0, out_undertow = in.flag("UNDERTOW", 0) != 0;
-    auto write_field = [&](const std::string &path) {
-        return binary ? put_file_binary(path, full, p) : put_file(path, full, p);
-    };
 
     // STATIONS (io.F:3786-3954): grid indices from STATIONS_FILE, sampled
     // every PLOT_INTV_STATION into a buffer of StationOutputBuffer rows that
@@ -470,6 +471,118 @@ int main(int argc, char **argv) {
         }
         return FW_OK;
     };
+    // PREVIEW's fields, staged asynchronously (fw_output_begin): a snapshot
+    // goes to one of two sets of pinned host buffers while the time loop
+    // goes on; a writer thread formats and writes each set once its copies
+    // are done, so neither the copies nor the formatting hold the steps
+    std::vector<const char *> out_names = {"Eta", "U", "V", "MASK"};
+    std::vector<std::string> out_stems = {"eta", "u", "v", "mask"};
+    if (p.track_hmax) {
+        out_names.push_back("HeightMax");
+        out_stems.push_back("hmax");
+    }
+    if (out_roller) {  // io.F:4461-4471: roller_NNNNN, U_undertow_NNNNN, V_undertow_NNNNN
+        out_names.push_back("ROLLER_FLUX");
+        out_stems.push_back("roller");
+    }
+    if (out_undertow) {
+        out_names.push_back("UNDERTOW_U");
+        out_stems.push_back("U_undertow");
+        out_names.push_back("UNDERTOW_V");
+        out_stems.push_back("V_undertow");
+    }
+    const size_t nout = out_names.size(), plane = (size_t)Mloc * Nloc;
+    struct OutSet {
+        std::vector<void *> buf;
+        int number = 0;
+        bool busy = false;  // between fw_output_begin and the end of its writing
+    } sets[2];
+    for (auto &st : sets)
+        for (size_t k = 0; k < nout; k++) {
+            void *b = nullptr;
+            const bool is_mask = out_stems[k] == "mask";
+            if ((rc = fw_host_alloc(plane * (is_mask ? sizeof(int) : sizeof(double)), &b)) != FW_OK)
+                return fail("fw_host_alloc", rc);
+            st.buf.push_back(b);
+        }
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<int> ready;  // sets whose copies are done, in order
+    bool stop = false, write_failed = false;
+    std::thread writer([&]() {
+        std::vector<double> w(plane);
+        for (;;) {
+            int k;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return stop || !ready.empty(); });
+                if (ready.empty()) return;
+                k = ready.front();
+                ready.pop_front();
+            }
+            OutSet &st = sets[k];
+            bool ok = true;
+            for (size_t f = 0; f < nout; f++) {
+                if (out_stems[f] == "mask") {
+                    const int *m = (const int *)st.buf[f];
+                    for (size_t q = 0; q < plane; q++) w[q] = m[q];
+                } else {
+                    std::memcpy(w.data(), st.buf[f], plane * sizeof(double));
+                }
+                const std::string path = numbered(dir, out_stems[f].c_str(), st.number);
+                ok = (binary ? put_file_binary(path, w, p) : put_file(path, w, p)) && ok;
+            }
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                st.busy = false;
+                if (!ok) write_failed = true;
+            }
+            cv.notify_all();
+        }
+    });
+    // on an early return the writer is stopped and joined (the files of
+    // the snapshots already handed to it are written first)
+    struct WriterGuard {
+        std::function<void()> f;
+        ~WriterGuard() { f(); }
+    } writer_guard{[&] {
+        if (!writer.joinable()) return;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        writer.join();
+    }};
+    int in_flight = -1;  // the set whose copies may still run
+    int next_set = 0;
+    // hand the in-flight set to the writer once its copies are done
+    auto collect = [&](bool wait) -> int {
+        if (in_flight < 0) return FW_OK;
+        if (wait) {
+            const int r = fw_output_wait(ctx);
+            if (r != FW_OK) return r;
+        } else {
+            const int d = fw_output_done(ctx);
+            if (d < 0) return d;
+            if (d == 0) return FW_OK;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            ready.push_back(in_flight);
+        }
+        cv.notify_all();
+        in_flight = -1;
+        return FW_OK;
+    };
+    // every snapshot taken so far written to its files
+    auto drain = [&]() -> int {
+        const int r = collect(true);
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [&] { return ready.empty() && !sets[0].busy && !sets[1].busy; });
+        if (r != FW_OK) return r;
+        return write_failed ? FW_ERR_IO : FW_OK;
+    };
     auto preview = [&](int number) -> int {
         icount = number;
         double t = 0.0, dt = 0.0;
@@ -477,27 +590,37 @@ int main(int argc, char **argv) {
         fw_get_scalar(ctx, "DT", &dt);
         std::printf("PRINTING FILE NO. %5d TIME/TOTAL: %12.3f / %12.3f\n", icount, t, total);
         if (tdt) std::fprintf(tdt, "%.9E %.9E\n", t, dt);
-        const char *names[] = {"Eta", "U", "V"};
-        const char *stems[] = {"eta", "u", "v"};
-        for (int k = 0; k < 3; k++) {
-            int r = fw_get_field(ctx, names[k], full.data());
-            if (r != FW_OK) return r;
-            write_field(numbered(dir, stems[k], icount));
-        }
-        int r = fw_get_field(ctx, "MASK", mask.data());
+        int r = collect(true);
         if (r != FW_OK) return r;
-        for (size_t q = 0; q < mask.size(); q++) full[q] = mask[q];
-        write_field(numbered(dir, "mask", icount));
-        if (p.track_hmax && fw_get_field(ctx, "HeightMax", full.data()) == FW_OK)
-            write_field(numbered(dir, "hmax", icount));
-        // io.F:4461-4471: roller_NNNNN, U_undertow_NNNNN, V_undertow_NNNNN
-        if (out_roller && fw_get_field(ctx, "ROLLER_FLUX", full.data()) == FW_OK)
-            write_field(numbered(dir, "roller", icount));
-        if (out_undertow && fw_get_field(ctx, "UNDERTOW_U", full.data()) == FW_OK)
-            write_field(numbered(dir, "U_undertow", icount));
-        if (out_undertow && fw_get_field(ctx, "UNDERTOW_V", full.data()) == FW_OK)
-            write_field(numbered(dir, "V_undertow", icount));
+        OutSet &st = sets[next_set];
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv.wait(lk, [&] { return !st.busy; });
+            if (write_failed) return FW_ERR_IO;
+        }
+        st.number = number;
+        st.busy = true;
+        r = fw_output_begin(ctx, (int)nout, out_names.data(), st.buf.data());
+        if (r != FW_OK) {
+            std::lock_guard<std::mutex> lk(mu);
+            st.busy = false;
+            return r;
+        }
+        in_flight = next_set;
+        next_set ^= 1;
         return FW_OK;
+    };
+    auto finish_output = [&]() -> int {
+        const int r = drain();
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        writer.join();
+        for (auto &st : sets)
+            for (void *b : st.buf) fw_host_free(b);
+        return r;
     };
 
     double time = 0.0, dt = 0.0, plot_count = plot_intv;  // init.F:631
@@ -520,6 +643,8 @@ int main(int argc, char **argv) {
     // a checkpoint at the top of a pass, after that pass's output; the
     // station rows taken so far are written first
     auto hotstart = [&]() -> int {
+        int r = drain();
+        if (r != FW_OK) return r;
         for (size_t k = 0; k < sta_f.size(); k++) {
             flush_station(k);
             std::fflush(sta_f[k]);
@@ -528,7 +653,7 @@ int main(int argc, char **argv) {
         char b[16];
         std::snprintf(b, sizeof b, "%05d", ++hot_number);
         const std::string f = dir + "hotstart_" + b;
-        int r = fw_checkpoint(ctx, f.c_str());
+        r = fw_checkpoint(ctx, f.c_str());
         if (r != FW_OK) return r;
         FILE *hf = std::fopen((f + ".host").c_str(), "w");
         if (!hf) return FW_ERR_IO;
@@ -569,12 +694,15 @@ int main(int argc, char **argv) {
             // CHECK_BLOWUP: dump the state as file 99999, then stop
             std::fprintf(stderr, "fw_main: %s, dumping file 99999\n", fw_strerror(status));
             preview(99999);
+            finish_output();
             fw_destroy(ctx);
             return 2;
         }
+        if ((rc = collect(false)) != FW_OK) return fail("fw_output_done", rc);
         fw_get_scalar(ctx, "TIME", &time);
         fw_get_scalar(ctx, "DT", &dt);
     }
+    if ((rc = finish_output()) != FW_OK) return fail("output", rc);
     if (tdt) std::fclose(tdt);
     for (size_t k = 0; k < sta_f.size(); k++) {
         flush_station(k);

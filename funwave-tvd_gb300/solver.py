@@ -98,7 +98,7 @@ def build_driver():
     if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(src), os.path.getmtime(lib_path())):
         return exe
     cxx = os.environ.get("CXX", "g++")
-    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(_ROOT, "include"), src, "-L" + _BUILD,
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-pthread", "-I" + os.path.join(_ROOT, "include"), src, "-L" + _BUILD,
            "-lfunwave_gpu", "-Wl,-rpath,$ORIGIN", "-o", exe + ".tmp"]
     subprocess.run(cmd, check=True)
     os.replace(exe + ".tmp", exe)
@@ -244,6 +244,11 @@ def load_library(path=None):
     L.fw_autotune.argtypes = [vp, ip]
     L.fw_get_tuning.argtypes = [vp, ctypes.POINTER(ip)]
     L.fw_set_tuning.argtypes = [vp, ctypes.POINTER(ip)]
+    L.fw_output_begin.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(vp)]
+    L.fw_output_wait.argtypes = [vp]
+    L.fw_output_done.argtypes = [vp]
+    L.fw_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(vp)]
+    L.fw_host_free.argtypes = [vp]
     L.fw_checkpoint.argtypes = [vp, ctypes.c_char_p]
     L.fw_restore.argtypes = [vp, ctypes.c_char_p]
     L.fw_strerror.argtypes = [ip]
@@ -376,6 +381,14 @@ class Solver:
     def sync(self):
         self._check(self.L.fw_sync(self.ctx), "fw_sync")
 
+    # --- asynchronous output ---------------------------------------------
+    def output_begin(self, names):
+        """Snapshot the named fields after the steps enqueued so far and copy
+        them to pinned host buffers while later steps run (fw_output_begin).
+        Returns an :class:`Output`; its wait() gives {name: array} as get()
+        would.  A later output_begin first waits for this one's copies."""
+        return Output(self, list(names))
+
     # --- restart ----------------------------------------------------------
     def checkpoint(self, path):
         """Write the complete run state to path (fw_checkpoint)."""
@@ -458,3 +471,67 @@ class Solver:
 
     def stream(self):
         return self.L.fw_stream(self.ctx)
+
+
+class Output:
+    """The pinned host buffers of one fw_output_begin (Solver.output_begin)."""
+
+    def __init__(self, solver, names):
+        self.s, self.names = solver, names
+        self.arrays, self._ptrs = {}, []
+        self._seq = None
+        L = solver.L
+        try:
+            for n in names:
+                shape = solver.shape(n)
+                dt = np.int32 if n in _MASKS else np.float64
+                nbytes = int(np.prod(shape)) * np.dtype(dt).itemsize
+                p = ctypes.c_void_p()
+                solver._check(L.fw_host_alloc(nbytes, ctypes.byref(p)), "fw_host_alloc")
+                self._ptrs.append(p.value)
+                buf = (ctypes.c_char * nbytes).from_address(p.value)
+                self.arrays[n] = np.frombuffer(buf, dtype=dt).reshape(shape, order="F")
+            cn = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+            hp = (ctypes.c_void_p * len(names))(*self._ptrs)
+            solver._check(L.fw_output_begin(solver.ctx, len(names), cn, hp), "fw_output_begin")
+            # a later fw_output_begin waits for this one's copies first
+            solver._out_seq = getattr(solver, "_out_seq", 0) + 1
+            self._seq = solver._out_seq
+        except Exception:
+            self._free()
+            raise
+
+    def _superseded(self):
+        return self._seq != self.s._out_seq
+
+    def done(self):
+        if self._superseded():
+            return True
+        rc = self.s.L.fw_output_done(self.s.ctx)
+        if rc < 0:
+            raise FwError(rc, "fw_output_done")
+        return rc == 1
+
+    def wait(self):
+        """Wait for the copies; returns {name: array} (copies of the pinned
+        buffers, which are then released)."""
+        if not self._superseded():
+            self.s._check(self.s.L.fw_output_wait(self.s.ctx), "fw_output_wait")
+        out = {n: a.copy() for n, a in self.arrays.items()}
+        self._free()
+        return out
+
+    def _free(self):
+        self.arrays = {}
+        for p in self._ptrs:
+            self.s.L.fw_host_free(p)
+        self._ptrs = []
+
+    def __del__(self):
+        try:
+            if self._ptrs:
+                if not self._superseded():
+                    self.s.L.fw_output_wait(self.s.ctx)
+                self._free()
+        except Exception:
+            pass

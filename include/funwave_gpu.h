@@ -19,6 +19,8 @@
 #ifndef FUNWAVE_GPU_H
 #define FUNWAVE_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -249,6 +251,30 @@ int fw_sponge_damping(fw_ctx *ctx);      /* SPONGE_DAMPING  sponge.F:52 */
  *                  checked out leaves the context un-initialised. */
 int fw_checkpoint(fw_ctx *ctx, const char *path);
 int fw_restore(fw_ctx *ctx, const char *path);
+
+/* Asynchronous output: PREVIEW's field transfers (io.F:4304-4621) without
+ * holding the time loop.
+ *   fw_output_begin  enqueues on the context's stream a snapshot of n fields
+ *                    (names as fw_get_field) into a device output buffer,
+ *                    then their device-to-host copies into host[k] (the
+ *                    layout and types of fw_get_field) on a second stream,
+ *                    and returns without waiting.  The snapshot holds the
+ *                    state after every step enqueued before the call; steps
+ *                    enqueued after it run while the copies proceed.  A
+ *                    call first waits for the previous call's copies.
+ *                    host[k] must stay untouched until the copies are done
+ *                    and should be pinned (fw_host_alloc) for them to
+ *                    overlap with the steps.  FW_ERR_BAD_PARAM for an
+ *                    unknown or switched-off field, before anything runs.
+ *   fw_output_wait   waits for the copies of the last fw_output_begin.
+ *   fw_output_done   1 when they are done (or none are pending), 0 while
+ *                    they run, a negative status on an error; no wait.
+ *   fw_host_alloc / fw_host_free  pinned host memory for the buffers. */
+int fw_output_begin(fw_ctx *ctx, int n, const char *const *names, void *const *host);
+int fw_output_wait(fw_ctx *ctx);
+int fw_output_done(fw_ctx *ctx);
+int fw_host_alloc(size_t bytes, void **ptr);
+int fw_host_free(void *ptr);
 
 long long fw_launch_count(fw_ctx *ctx);
 /* Time nrep back-to-back launches of one kernel of the step with CUDA events
