@@ -84,6 +84,23 @@ template <typename T> bool find_field(fw_ctx *c, const char *name, FieldRef &r) 
             r.is_mask = e.m;
             return true;
         }
+    // CALCULATE_MEAN's radiation-stress planes (fw::RadPlane order), with
+    // the reference's names
+    static const char *const rad_names[fw::RP_KAHAN] = {
+        "P_center", "Q_center", "U_davg", "V_davg", "Wsurf", "BreakSourceX", "BreakSourceY",
+        "U_davg_sum", "V_davg_sum", "P_sum", "Q_sum", "UUsum", "UVsum", "VVsum", "WWsum", "FRCXsum", "FRCYsum",
+        "BreakDissX_sum", "BreakDissY_sum",
+        "U_davg_mean", "V_davg_mean", "P_mean", "Q_mean", "UUmean", "UVmean", "VVmean", "WWmean", "FRCXmean",
+        "FRCYmean", "BreakDissX", "BreakDissY",
+        "DxSxx", "DySxy", "DySyy", "DxSxy", "PgrdX", "PgrdY", "DxUUH", "DyUVH", "DyVVH", "DxUVH"};
+    for (int k = 0; k < fw::RP_KAHAN; k++)
+        if (std::strcmp(rad_names[k], name) == 0) {
+            if (!f.rad) return false;
+            r.ptr = f.rad + (size_t)k * (size_t)c->g.pitch * (size_t)(c->g.Nloc + 1);
+            r.kind = CELL;
+            r.is_mask = 0;
+            return true;
+        }
     return false;
 }
 
@@ -231,6 +248,8 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
             T **kf[] = {&f.kETAsum, &f.kUsum, &f.kVsum, &f.kETA2sum};
             for (T **p : kf) *p = (T *)take(plane * sizeof(T));
         }
+        if (g.track_rad)
+            f.rad = (T *)take((size_t)(sizeof(T) == sizeof(double) ? fw::RP_N64 : fw::RP_N32) * plane * sizeof(T));
     }
     uint8_t **mf[] = {&f.MASK, &f.MASKn, &f.MASK9, &f.MASK_STRUC};
     for (uint8_t **p : mf) *p = (uint8_t *)take(plane);
@@ -553,6 +572,7 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     g.has_g2 = g.gamma2 > 0.0 ? 1 : 0;
     g.track_hmin = p->track_hmin;
     g.track_roller = p->track_roller;
+    g.track_rad = p->track_radiation && p->steady_time < 999999.0 ? 1 : 0;
     g.track_umax = p->track_umax;
     g.track_mfmax = p->track_mfmax;
     g.steady_time = p->steady_time;
@@ -801,12 +821,16 @@ int fw_get_points(fw_ctx *c, const char *name, int n, const int *I, const int *J
 
 int fw_get_scalar(fw_ctx *c, const char *name, double *v) {
     if (!c || !name || !v) return FW_ERR_BAD_PARAM;
-    if (!std::strcmp(name, "TIME") || !std::strcmp(name, "DT") || !std::strcmp(name, "T_sum")) {
+    if (!std::strcmp(name, "TIME") || !std::strcmp(name, "DT") || !std::strcmp(name, "T_sum") ||
+        !std::strcmp(name, "ICOUNT_MEAN")) {
         double sc[S_NSLOT];
         cudaError_t e = cudaMemcpyAsync(sc, dsc_ptr(c), sizeof(sc), cudaMemcpyDeviceToHost, c->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) return cuda_status(c, e);
-        *v = !std::strcmp(name, "TIME") ? sc[S_TIME] : !std::strcmp(name, "DT") ? sc[S_DT] : sc[S_TSUM];
+        *v = !std::strcmp(name, "TIME") ? sc[S_TIME]
+             : !std::strcmp(name, "DT") ? sc[S_DT]
+             : !std::strcmp(name, "T_sum") ? sc[S_TSUM]
+                                            : sc[S_NMEAN];
         return FW_OK;
     }
     if (!std::strcmp(name, "EtaBlowVal")) *v = c->EtaBlowVal;
@@ -1220,7 +1244,7 @@ bool same_params(const fw_params &a, const fw_params &b) {
            FW_SAME(theta_peak) && FW_SAME(sigma_theta) && FW_SAME(nfreq) && FW_SAME(ntheta) && FW_SAME(spreading) &&
            FW_SAME(spread_s) && FW_SAME(precision) && FW_SAME(track_hmax) && FW_SAME(track_hmin) &&
            FW_SAME(track_umax) && FW_SAME(track_mfmax) && FW_SAME(steady_time) && FW_SAME(t_intv_mean) &&
-           FW_SAME(track_roller);
+           FW_SAME(track_roller) && FW_SAME(track_radiation);
 #undef FW_SAME
 }
 

@@ -30,6 +30,7 @@ struct Grid {
     int has_g2;              // Gamma2 > 0 (the dispersive ETAx/ETAy exchange)
     int track_hmin, track_umax, track_mfmax, stats;  // statistics switches
     int track_roller;        // BREAKING's roller flux and undertow (ROLLER / UNDERTOW output)
+    int track_rad;           // CALCULATE_MEAN's radiation-stress, momentum-flux, dissipation sums
     double steady_time, t_intv_mean;
     double DX, DY;
     double gamma1, gamma2, gamma3, b1, b2, Beta_1, Beta_2;
@@ -57,8 +58,11 @@ enum : int { FS_DT = 0, FS_RDT = 1, FS_WKAA = 2, FS_WKPH = 3, FS_TSUM = 4, FS_NS
 
 // device scalar slots (double array)
 // S_TSUM: T_sum of MIXING_STUFF; S_TSUMU: the T_sum this step's means use;
-// S_MFLAG: 0 no statistics this step, 1 accumulate, 2 end of an interval
-enum : int { S_TIME = 0, S_DT = 1, S_DTMIN = 2, S_ETAMAX = 3, S_TSUM = 4, S_TSUMU = 5, S_MFLAG = 6, S_NSLOT = 8 };
+// S_MFLAG: 0 no statistics this step, 1 accumulate, 2 end of an interval;
+// S_NMEAN: intervals ended so far (the reference's ICOUNT_MEAN, io.F:4641)
+enum : int {
+    S_TIME = 0, S_DT = 1, S_DTMIN = 2, S_ETAMAX = 3, S_TSUM = 4, S_TSUMU = 5, S_MFLAG = 6, S_NMEAN = 7, S_NSLOT = 8
+};
 
 template <typename T>
 struct Fields {
@@ -79,6 +83,7 @@ struct Fields {
         *HrmsSum, *WHave, *WHrms, *NZU;
     T *kETAsum, *kUsum, *kVsum, *kETA2sum;  // Kahan compensations of the mixed path
     T *ROLLER, *UNDERTOW_U, *UNDERTOW_V;    // breaker.F:316-339 (null unless tracked)
+    T *rad;  // radiation-stress planes (fw::RadPlane), consecutive planes of the field plane size; null if off
     uint8_t *MASK, *MASKn, *MASK9, *MASK_STRUC;
     T *rhs_x, *rhs_y;                 // tmp4 of GET_Eta_U_V_HU_HV
     double *ty, *tp, *tq, *tc;        // line-solver scratch
@@ -102,6 +107,23 @@ struct Fields {
     int *cand, *ncand;                // breaking candidates
     unsigned long long *dtmin_bits;
     unsigned long long *etamax_bits;
+};
+
+// the planes behind Fields::rad: the per-step inputs that ESTIMATE_HUV and
+// SourceTerms leave at the last stage (etauv_solver.F:94-101, 247;
+// sources.F:428-456), twelve time sums, their twelve means and the ten
+// gradient fields of CALCULATE_MEAN (mixing.F:156-219); the mixed path adds
+// the sums' Kahan compensations.  Sums and means share one order:
+// U_davg, V_davg, P_center, Q_center, UU, UV, VV, WW, FRCX, FRCY,
+// BreakDissX, BreakDissY
+enum RadPlane {
+    RP_PC, RP_QC, RP_UD, RP_VD, RP_WS, RP_BX, RP_BY,
+    RP_SUM = 7,
+    RP_MEAN = RP_SUM + 12,
+    RP_DER = RP_MEAN + 12,  // DxSxx, DySxy, DySyy, DxSxy, PgrdX, PgrdY, DxUUH, DyUVH, DyVVH, DxUVH
+    RP_KAHAN = RP_DER + 10,
+    RP_N64 = RP_KAHAN,
+    RP_N32 = RP_KAHAN + 12
 };
 
 // line-solver partition of one direction

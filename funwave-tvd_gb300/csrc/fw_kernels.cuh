@@ -838,9 +838,13 @@ __device__ __forceinline__ T wavemaker_mass(const Grid &g, const Fields<T> &f, i
     return (T)0;
 }
 
+// SourceTerms at one cell; BX, BY get BreakSourceX/Y (sources.F:428-456),
+// zero without viscosity breaking
 template <typename T>
-__device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, int i, int j, T wm, T &SX,
-                                             T &SY) {
+__device__ __forceinline__ void source_terms_b(const Grid &g, const Fields<T> &f, int i, int j, T wm, T &SX,
+                                               T &SY, T &BX, T &BY) {
+    BX = (T)0;
+    BY = (T)0;
     constexpr bool EXACT = sizeof(T) == sizeof(double);
     const T DX = GC(DX), DY = GC(DY), mdf = GC(min_depth_frc);
     const T rdx = GC(rdx), rdy = GC(rdy);
@@ -897,11 +901,19 @@ __device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, 
         }
         sx = sx + bx;
         sy = sy + by;
+        BX = bx;
+        BY = by;
     }
 #undef OX
 #undef OY
     SX = sx;
     SY = sy;
+}
+template <typename T>
+__device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, int i, int j, T wm, T &SX,
+                                             T &SY) {
+    T bx, by;
+    source_terms_b(g, f, i, j, wm, SX, SY, bx, by);
 }
 
 // SourceTerms alone (materialises SourceX, SourceY, WaveMaker_Mass)
@@ -921,9 +933,12 @@ __global__ void __launch_bounds__(256) k_sources(Grid g, Fields<T> f) {
 // ---------------------------------------------------------------------------
 // ESTIMATE_HUV (etauv_solver.F:53-351) fused with SourceTerms, plus the H
 // update and the right-hand sides of the tridiagonal systems of
-// GET_Eta_U_V_HU_HV (etauv_solver.F:365-539).
+// GET_Eta_U_V_HU_HV (etauv_solver.F:365-539).  RAD (the last two stages,
+// with the radiation sums on) also stores P_center, Q_center, U_davg, V_davg
+// with the stage's starting H (etauv_solver.F:94-101), Wsurf = R1
+// (etauv_solver.F:247) and BreakSourceX/Y.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, bool RAD = false>
 __global__ void __launch_bounds__(256, 3) k_update(Grid g, Fields<T> f, T al, T be) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -952,8 +967,8 @@ __global__ void __launch_bounds__(256, 3) k_update(Grid g, Fields<T> f, T al, T 
     const T DT = DTV;
     const double TIME = f.dsc[S_TIME];
     const T wm = wavemaker_mass(g, f, i, j, TIME);
-    T SX, SY;
-    source_terms(g, f, i, j, wm, SX, SY);
+    T SX, SY, BX, BY;
+    source_terms_b(g, f, i, j, wm, SX, SY, BX, BY);
 
     const size_t ie_ = IDX(i + 1, j), in_ = IDX(i, j + 1);
     constexpr bool EXACT = sizeof(T) == sizeof(double);
@@ -963,6 +978,18 @@ __global__ void __launch_bounds__(256, 3) k_update(Grid g, Fields<T> f, T al, T 
         const T xmk = i2r<T>(i - g.ib) * DX, ymk = i2r<T>(j - g.jb) * DY;
         if (fabs_(xmk - GC(xc_wk)) < GC(width_wk) && fabs_(ymk - GC(yc_wk)) < GC(ywidth_wk) / (T)2)
             R1 = R1 + wm;
+    }
+    if constexpr (RAD) {
+        const size_t PL = (size_t)g.pitch * (size_t)(g.Nloc + 1);
+        const T pc = (T)0.5 * (f.P[ie_] + f.P[id]), qc = (T)0.5 * (f.Q[in_] + f.Q[id]);
+        const T hm = tmax(f.H[id], GC(min_depth_frc));  // H before this stage's update
+        f.rad[RP_PC * PL + id] = pc;
+        f.rad[RP_QC * PL + id] = qc;
+        f.rad[RP_UD * PL + id] = pc / hm;
+        f.rad[RP_VD * PL + id] = qc / hm;
+        f.rad[RP_WS * PL + id] = R1;
+        f.rad[RP_BX * PL + id] = BX;
+        f.rad[RP_BY * PL + id] = BY;
     }
     T eta = al * f.Eta0[id] + be * (f.Eta[id] + DT * R1);
     if (g.eta_limiter) {
@@ -2434,6 +2461,32 @@ __device__ __forceinline__ void ghost_y_cell(const Grid &g, T *phi, int i, int j
     phi[IDX(i, j)] = r;
 }
 
+// EXCHANGE's PHI_COLL of Wsurf, P_center, Q_center, U_davg and V_davg
+// (bc.F:438-443), scalar rules, after the last two stages
+template <typename T>
+__global__ void __launch_bounds__(256) k_ghost_rad(Grid g, Fields<T> f) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nX = 6 * g.Nglob, nY = 6 * g.Mloc;
+    if (t >= nX + nY) return;
+    const size_t PL = (size_t)g.pitch * (size_t)(g.Nloc + 1);
+    T *const planes[5] = {f.rad + RP_WS * PL, f.rad + RP_PC * PL, f.rad + RP_QC * PL, f.rad + RP_UD * PL,
+                          f.rad + RP_VD * PL};
+    if (t < nX) {
+        const int col = t % 6;
+        const int i = col < 3 ? col : g.ie + 1 + (col - 3);
+        const int j = g.jb + t / 6;
+#pragma unroll
+        for (int k = 0; k < 5; k++) ghost_x_cell(g, planes[k], i, j, 1);
+    } else {
+        const int u = t - nX;
+        const int row = u / g.Mloc;
+        const int i = u % g.Mloc;
+        const int j = row < 3 ? row : g.je + 1 + (row - 3);
+#pragma unroll
+        for (int k = 0; k < 5; k++) ghost_y_cell(g, planes[k], i, j, 1);
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_ghost(Grid g, Fields<T> f, int with_age) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2705,6 +2758,7 @@ static __global__ void k_tsum(Grid g, double *dsc, float *fsc) {
         if (ts >= g.t_intv_mean) {
             flag = 2;
             ts = ts - g.t_intv_mean;
+            dsc[S_NMEAN] = dsc[S_NMEAN] + 1.0;
         } else {
             flag = 1;
         }
@@ -2732,6 +2786,50 @@ template <typename T> __device__ __forceinline__ T stat_val(const T *s, const T 
     else return __fsub_rn(s[id], k[id]);
 }
 
+// CALCULATE_MEAN's radiation-stress, momentum-flux and breaking-dissipation
+// sums at one cell (mixing.F:156-167, 270-281), with the ETAmean the
+// caller's branch has at that point and the last interval's U_davg_mean
+template <typename T> __device__ __forceinline__ void rad_sums(const Grid &g, const Fields<T> &f, size_t id, T DT,
+                                                               T etamean) {
+    const size_t PL = (size_t)g.pitch * (size_t)(g.Nloc + 1);
+    T *const r = f.rad;
+    T *const ks = sizeof(T) == sizeof(float) ? r + RP_KAHAN * PL : nullptr;
+#define RV(k) r[(size_t)(k) * PL + id]
+#define SUM(k, x) stat_add(r + (RP_SUM + (k)) * PL, ks ? ks + (size_t)(k) * PL : nullptr, id, (T)(x))
+    const T udv = RV(RP_UD), vdv = RV(RP_VD);
+    const T ud = udv - RV(RP_MEAN + 0), vd = vdv - RV(RP_MEAN + 1);
+    const T hd = f.Eta[id] - etamean + f.Depth[id];
+    const T u = f.U[id], v = f.V[id], w = RV(RP_WS);
+    const T sp = fsqrt(u * u + v * v);
+    SUM(0, udv * DT);
+    SUM(1, vdv * DT);
+    SUM(2, RV(RP_PC) * DT);
+    SUM(3, RV(RP_QC) * DT);
+    SUM(4, ud * ud * hd * DT);
+    SUM(5, ud * vd * hd * DT);
+    SUM(6, vd * vd * hd * DT);
+    SUM(7, (T)0.25 * w * w * hd * DT);
+    SUM(8, u * sp * DT);
+    SUM(9, v * sp * DT);
+    SUM(10, RV(RP_BX) * DT);
+    SUM(11, RV(RP_BY) * DT);
+#undef SUM
+#undef RV
+}
+// the means at the end of an interval, then the sums restart
+template <typename T> __device__ __forceinline__ void rad_means(const Grid &g, const Fields<T> &f, size_t id, T Ts) {
+    const size_t PL = (size_t)g.pitch * (size_t)(g.Nloc + 1);
+    T *const r = f.rad;
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+        T *s = r + (RP_SUM + k) * PL;
+        T *kk = sizeof(T) == sizeof(float) ? r + (RP_KAHAN + k) * PL : nullptr;
+        r[(RP_MEAN + k) * PL + id] = stat_val(s, kk, id) / Ts;
+        s[id] = (T)0;
+        if (kk) kk[id] = (T)0;
+    }
+}
+
 // CALCULATE_MEAN (mixing.F:141-301) at one cell: the Eta, U, V and
 // (Eta-ETAmean)^2 time sums, their means at the end of an interval, and the
 // zero-up-crossing wave heights; the float path keeps the sums compensated
@@ -2752,7 +2850,12 @@ template <typename T> __device__ __forceinline__ void mean_cell(const Grid &g, c
         stat_add(f.ETAsum, f.kETAsum, id, eta * DT);
         f.Umean[id] = stat_val(f.Usum, f.kUsum, id) / Ts;
         f.Vmean[id] = stat_val(f.Vsum, f.kVsum, id) / Ts;
-        f.ETAmean[id] = stat_val(f.ETAsum, f.kETAsum, id) / Ts;
+        const T em = stat_val(f.ETAsum, f.kETAsum, id) / Ts;
+        f.ETAmean[id] = em;
+        if (f.rad) {
+            rad_sums(g, f, id, DT, em);
+            rad_means(g, f, id, Ts);
+        }
         f.Usum[id] = (T)0;
         f.Vsum[id] = (T)0;
         f.ETAsum[id] = (T)0;
@@ -2774,6 +2877,7 @@ template <typename T> __device__ __forceinline__ void mean_cell(const Grid &g, c
         stat_add(f.Vsum, f.kVsum, id, v * DT);
         stat_add(f.ETAsum, f.kETAsum, id, eta * DT);
         stat_add(f.ETA2sum, f.kETA2sum, id, d * d * DT);
+        if (f.rad) rad_sums(g, f, id, DT, f.ETAmean[id]);
         T emax = f.Emax[id], emin = f.Emin[id];
         if (eta > emax) emax = eta;
         if (eta < emin) emin = eta;
@@ -2792,6 +2896,46 @@ template <typename T> __device__ __forceinline__ void mean_cell(const Grid &g, c
         f.Emax[id] = emax;
         f.Emin[id] = emin;
     }
+}
+
+// the end of a CALCULATE_MEAN interval (mixing.F:183-219): the gradient
+// fields DxSxx .. DxUVH of the new means on the interior, and FRCXmean,
+// FRCYmean times Cd there.  Runs after k_end; a no-op on other steps.  The
+// literals 9.80 and 0.5*9.80 are default REAL.
+template <typename T>
+__global__ void __launch_bounds__(256) k_rad_derived(Grid g, Fields<T> f) {
+    if ((int)f.dsc[S_MFLAG] != 2) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + g.ib;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + g.jb;
+    if (i > g.ie || j > g.je) return;
+    const size_t PL = (size_t)g.pitch * (size_t)(g.Nloc + 1);
+    const size_t id = IDX(i, j), e = IDX(i + 1, j), w = IDX(i - 1, j), n = IDX(i, j + 1), s = IDX(i, j - 1);
+    T *const r = f.rad;
+    const T *M = r + RP_MEAN * PL;
+#define MN(k, c) M[(size_t)(k) * PL + (c)]
+    const T DX = GC(DX), DY = GC(DY), mdf = GC(min_depth_frc);
+    const T g98 = (T)9.80f, g49 = (T)(0.5f * 9.80f);
+    const T *E2 = f.ETA2mean, *EM = f.ETAmean, *D = f.Depth;
+    T *O = r + RP_DER * PL;
+    // UU 4, UV 5, VV 6, WW 7; P 2, Q 3
+    O[0 * PL + id] = (MN(4, e) - MN(4, w)) / (T)2 / DX - (MN(7, e) - MN(7, w)) / (T)2 / DX +
+                     g49 * (E2[e] - E2[w]) / (T)2 / DX;
+    O[1 * PL + id] = (MN(5, n) - MN(5, s)) / (T)2 / DY;
+    O[2 * PL + id] = (MN(6, n) - MN(6, s)) / (T)2 / DY - (MN(7, n) - MN(7, s)) / (T)2 / DY +
+                     g49 * (E2[n] - E2[s]) / (T)2 / DY;
+    O[3 * PL + id] = (MN(5, e) - MN(5, w)) / (T)2 / DX;
+    O[4 * PL + id] = g98 * (D[id] + EM[id]) * (EM[e] - EM[w]) / (T)2 / DX;
+    O[5 * PL + id] = g98 * (D[id] + EM[id]) * (EM[n] - EM[s]) / (T)2 / DY;
+    const T he = tmax(D[e] + EM[e], mdf), hw = tmax(D[w] + EM[w], mdf);
+    const T hn = tmax(D[n] + EM[n], mdf), hs = tmax(D[s] + EM[s], mdf);
+    O[6 * PL + id] = (MN(2, e) * MN(2, e) / he - MN(2, w) * MN(2, w) / hw) / (T)2 / DX;
+    O[7 * PL + id] = (MN(2, n) * MN(3, n) / hn - MN(2, s) * MN(3, s) / hs) / (T)2 / DY;
+    O[8 * PL + id] = (MN(3, n) * MN(3, n) / hn - MN(3, s) * MN(3, s) / hs) / (T)2 / DY;
+    O[9 * PL + id] = (MN(2, e) * MN(3, e) / he - MN(2, w) * MN(3, w) / hw) / (T)2 / DX;
+    T *FX = r + (RP_MEAN + 8) * PL, *FY = r + (RP_MEAN + 9) * PL;
+    FX[id] = FX[id] * f.Cd[id];
+    FY[id] = FY[id] * f.Cd[id];
+#undef MN
 }
 
 template <typename T>
@@ -3048,7 +3192,15 @@ template <typename T> static void launch_estimate_huv_opt(fw_ctx *c, int istage,
     static const double AL[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0};
     static const double BE[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
     const T al = (T)AL[istage - 1], be = (T)BE[istage - 1];
-    k_update<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_UPDATE)), c->blk(TK_UPDATE), 0, c->stream>>>(g, c->F<T>(), al, be);
+    // stage 2 too: with PERIODIC, EXCHANGE leaves the x-ghost values of the
+    // previous exchange in the ghost corners (bc.F:735-740), so the last
+    // stage's corners hold the second stage's values
+    if (istage >= 2 && g.track_rad)
+        k_update<T, true><<<grid2(g.Mloc, g.Nloc, c->blk(TK_UPDATE)), c->blk(TK_UPDATE), 0, c->stream>>>(
+            g, c->F<T>(), al, be);
+    else
+        k_update<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_UPDATE)), c->blk(TK_UPDATE), 0, c->stream>>>(g, c->F<T>(), al,
+                                                                                                     be);
     note(c);
     if (g.dispersion) {
         if (sizeof(T) == sizeof(float) && c->factored) {
@@ -3162,6 +3314,10 @@ template <typename T> void launch_end_step(fw_ctx *c) {
     }
     k_end<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>(), c->p.track_hmax);
     note(c);
+    if (g.track_rad) {
+        k_rad_derived<T><<<grid2(g.ie - g.ib + 1, g.je - g.jb + 1, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
+        note(c);
+    }
 }
 
 template <typename T> void launch_stage(fw_ctx *c, int istage) {
@@ -3189,6 +3345,11 @@ template <typename T> void launch_stage(fw_ctx *c, int istage) {
         launch_breaking<T>(c);
     }
     launch_exchange<T>(c, g.direct_sponge != 0);
+    if (istage >= 2 && g.track_rad) {
+        const int n = 6 * g.Nglob + 6 * g.Mloc;
+        k_ghost_rad<T><<<(n + 255) / 256, 256, 0, c->stream>>>(g, c->F<T>());
+        note(c);
+    }
 }
 
 #ifdef FW_SHARED_DEFS

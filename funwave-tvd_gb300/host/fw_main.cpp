@@ -97,6 +97,12 @@ struct Input {
     }
 };
 
+// an output switch: its input.txt key (e.g. "Hmax") or OUT_<key>
+int out_flag(const Input &in, const char *key) {
+    if (in.has(key)) return in.flag(key, 0);
+    return in.flag((std::string("OUT_") + key).c_str(), 0);
+}
+
 // the input.txt keys of fw_params (names and defaults of src/io.F)
 void fill_params(const Input &in, fw_params &p) {
     fw_params_default(&p);
@@ -161,13 +167,18 @@ void fill_params(const Input &in, fw_params &p) {
     p.spreading = upper(in.str("SPREADING", "WRAPPED_NORMAL")) == "COS2S" ? FW_SPREAD_COS2S : FW_SPREAD_WRAPPED_NORMAL;
     p.spread_s = in.num("SPREADING_S", 10.0);
     p.precision = upper(in.str("PRECISION", "FP64")) == "MIXED" ? FW_PREC_MIXED : FW_PREC_FP64;
-    p.track_hmax = in.flag("OUT_Hmax", 0);
-    p.track_hmin = in.flag("OUT_Hmin", 0);
-    p.track_umax = in.flag("OUT_Umax", 0);
-    p.track_mfmax = in.flag("OUT_MFmax", 0);
+    // the output switches under their input.txt keys (io.F:3392-3424), or
+    // the OUT_* variable names
+    p.track_hmax = out_flag(in, "Hmax");
+    p.track_hmin = out_flag(in, "Hmin");
+    p.track_umax = out_flag(in, "Umax");
+    p.track_mfmax = out_flag(in, "MFmax");
     p.steady_time = in.num("STEADY_TIME", LARGE);
     p.t_intv_mean = in.num("T_INTV_mean", LARGE);
     p.track_roller = (in.flag("ROLLER", 0) || in.flag("UNDERTOW", 0)) ? 1 : 0;
+    // PREVIEW_MEAN's Radiation files, and ulagm/vlagm of Umean/Vmean, need
+    // CALCULATE_MEAN's radiation-stress sums
+    p.track_radiation = (out_flag(in, "Radiation") || out_flag(in, "Umean") || out_flag(in, "Vmean")) ? 1 : 0;
 }
 
 // DEPTH_TYPE DATA / FLAT / SLOPE (init.F:684-760), interior Mglob x Nglob,
@@ -623,11 +634,79 @@ int main(int argc, char **argv) {
         return r;
     };
 
+    // PREVIEW_MEAN (io.F:4630-4736): at the end of each CALCULATE_MEAN
+    // interval, the means under RESULT_FOLDER/<stem>_NNNNN (NNNNN counts
+    // the intervals); Sxx and Syy add 0.5*9.8*ETA2mean (default REAL)
+    const bool o_umean = out_flag(in, "Umean"), o_vmean = out_flag(in, "Vmean");
+    const bool o_etamean = out_flag(in, "ETAmean"), o_wh = out_flag(in, "WaveHeight");
+    const bool o_rad = out_flag(in, "Radiation");
+    const bool any_mean = p.steady_time < LARGE && (o_umean || o_vmean || o_etamean || o_wh || o_rad);
+    double icount_mean = 0.0;
+    std::vector<double> dep_full, etam, a, b;
+    auto preview_mean = [&](int number) -> int {
+        std::printf("  PRINTING MEAN FILE%6d\n", number);
+        int r = FW_OK;
+        auto get = [&](const char *name, std::vector<double> &v) {
+            v.resize(plane);
+            if (r == FW_OK) r = fw_get_field(ctx, name, v.data());
+        };
+        auto put = [&](const char *stem, const std::vector<double> &v) {
+            if (r != FW_OK) return;
+            const std::string path = numbered(dir, stem, number);
+            if (!(binary ? put_file_binary(path, v, p) : put_file(path, v, p))) r = FW_ERR_IO;
+        };
+        if (dep_full.empty()) get("Depth", dep_full);
+        get("ETAmean", etam);
+        auto lagm = [&](const char *mean, const char *flux, const char *s1, const char *s2) {
+            get(mean, a);
+            put(s1, a);
+            get(flux, b);
+            for (size_t q = 0; q < plane; q++) b[q] = b[q] / std::max(dep_full[q] + etam[q], p.min_depth_frc);
+            put(s2, b);
+        };
+        if (o_umean) lagm("Umean", "P_mean", "umean", "ulagm");
+        if (o_vmean) lagm("Vmean", "Q_mean", "vmean", "vlagm");
+        if (o_etamean) put("etamean", etam);
+        if (o_wh) {
+            get("WaveHeightRMS", a);
+            put("Hrms", a);
+            get("WaveHeightAve", a);
+            put("Havg", a);
+            get("SigWaveHeight", a);
+            put("Hsig", a);
+        }
+        if (o_rad) {
+            const double c49 = (double)(0.5f * 9.8f);
+            std::vector<double> e2, ww;
+            get("ETA2mean", e2);
+            get("WWmean", ww);
+            get("UUmean", a);
+            for (size_t q = 0; q < plane && r == FW_OK; q++) a[q] = a[q] - ww[q] + c49 * e2[q];
+            put("Sxx", a);
+            get("UVmean", a);
+            put("Sxy", a);
+            get("VVmean", a);
+            for (size_t q = 0; q < plane && r == FW_OK; q++) a[q] = a[q] - ww[q] + c49 * e2[q];
+            put("Syy", a);
+            const char *const names[][2] = {{"DxSxx", "DxSxx"}, {"DySxy", "DySxy"}, {"DySyy", "DySyy"},
+                                            {"DxSxy", "DxSxy"}, {"PgrdX", "PgrdX"}, {"PgrdY", "PgrdY"},
+                                            {"DxUUH", "DxUUH"}, {"DyUVH", "DyUVH"}, {"DyVVH", "DyVVH"},
+                                            {"DxUVH", "DxUVH"}, {"FRCXmean", "FRCX"}, {"FRCYmean", "FRCY"},
+                                            {"BreakDissX", "BrkDissX"}, {"BreakDissY", "BrkDissY"}};
+            for (auto &nm : names) {
+                get(nm[0], a);
+                put(nm[1], a);
+            }
+        }
+        return r;
+    };
+
     double time = 0.0, dt = 0.0, plot_count = plot_intv;  // init.F:631
     double plot_count_sta = plot_intv_sta;                  // init.F:632
     double hot_count = 0.0;
     int hot_number = 0;
     fw_get_scalar(ctx, "TIME", &time);
+    if (any_mean) fw_get_scalar(ctx, "ICOUNT_MEAN", &icount_mean);  // nonzero after a hot start
     if (hot_start) {
         // the counters the checkpointing run had (TIME and DT are restored)
         FILE *hf = std::fopen((hot_file + ".host").c_str(), "r");
@@ -701,6 +780,14 @@ int main(int argc, char **argv) {
         if ((rc = collect(false)) != FW_OK) return fail("fw_output_done", rc);
         fw_get_scalar(ctx, "TIME", &time);
         fw_get_scalar(ctx, "DT", &dt);
+        if (any_mean) {
+            double n = 0.0;
+            fw_get_scalar(ctx, "ICOUNT_MEAN", &n);
+            if (n > icount_mean) {
+                icount_mean = n;
+                if ((rc = preview_mean((int)n)) != FW_OK) return fail("PREVIEW_MEAN", rc);
+            }
+        }
     }
     if ((rc = finish_output()) != FW_OK) return fail("output", rc);
     if (tdt) std::fclose(tdt);

@@ -39,6 +39,16 @@ PARAM_DEFAULTS = {
     # statistics (MAX_MIN_PROPERTY switches, MIXING_STUFF times)
     "OUT_Hmin": False, "OUT_Umax": False, "OUT_MFmax": False, "ROLLER": False, "UNDERTOW": False,
     "STEADY_TIME": 999999.0, "T_INTV_mean": 999999.0,
+    # PREVIEW_MEAN's files (io.F:4666-4733)
+    "OUT_Umean": False, "OUT_Vmean": False, "OUT_ETAmean": False, "OUT_WaveHeight": False,
+    "OUT_Radiation": False,
+}
+
+# input.txt keys of the output switches (io.F:3392-3424) -> the OUT_*
+# variable names this package uses; either spelling is accepted
+REFERENCE_KEYS = {
+    "Hmax": "OUT_Hmax", "Hmin": "OUT_Hmin", "Umax": "OUT_Umax", "MFmax": "OUT_MFmax", "Umean": "OUT_Umean",
+    "Vmean": "OUT_Vmean", "ETAmean": "OUT_ETAmean", "WaveHeight": "OUT_WaveHeight", "Radiation": "OUT_Radiation",
 }
 
 _BOOL = {k for k, v in PARAM_DEFAULTS.items() if isinstance(v, bool)}
@@ -92,6 +102,7 @@ def read_input_txt(path_or_text):
             continue
         key, val = body.split("=", 1)
         key = key.strip()
+        key = REFERENCE_KEYS.get(key, key)
         if not key or key in out:
             continue
         out[key] = _convert(key, val)

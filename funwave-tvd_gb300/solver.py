@@ -98,7 +98,9 @@ def build_driver():
     if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(src), os.path.getmtime(lib_path())):
         return exe
     cxx = os.environ.get("CXX", "g++")
-    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-pthread", "-I" + os.path.join(_ROOT, "include"), src, "-L" + _BUILD,
+    # no fused multiply-adds in host arithmetic: the same files on x86 and Arm
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-pthread", "-ffp-contract=off", "-I" + os.path.join(_ROOT, "include"),
+           src, "-L" + _BUILD,
            "-lfunwave_gpu", "-Wl,-rpath,$ORIGIN", "-o", exe + ".tmp"]
     subprocess.run(cmd, check=True)
     os.replace(exe + ".tmp", exe)
@@ -141,7 +143,7 @@ class FwParams(ctypes.Structure):
         ("track_hmax", ctypes.c_int),
         ("track_hmin", ctypes.c_int), ("track_umax", ctypes.c_int), ("track_mfmax", ctypes.c_int),
         ("steady_time", ctypes.c_double), ("t_intv_mean", ctypes.c_double),
-        ("track_roller", ctypes.c_int),
+        ("track_roller", ctypes.c_int), ("track_radiation", ctypes.c_int),
     ]
 
 
@@ -189,6 +191,9 @@ def params_struct(p, precision=None, device=0):
     s.device = int(device)
     # ROLLER and UNDERTOW (output switches) both need the BREAKING diagnostics
     s.track_roller = 1 if (p.get("ROLLER", False) or p.get("UNDERTOW", False)) else 0
+    # PREVIEW_MEAN's Radiation files and the ulagm/vlagm of Umean/Vmean need
+    # CALCULATE_MEAN's radiation-stress sums (P_mean, Q_mean among them)
+    s.track_radiation = 1 if any(p.get(k, False) for k in ("OUT_Radiation", "OUT_Umean", "OUT_Vmean")) else 0
     return s
 
 

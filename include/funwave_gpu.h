@@ -96,6 +96,8 @@ typedef struct fw_params {
     double steady_time;           /* STEADY_TIME (LARGE): time means and wave heights from then on */
     double t_intv_mean;           /* T_INTV_mean (LARGE): averaging interval */
     int    track_roller;          /* ROLLER or UNDERTOW output (F): BREAKING's ROLLER_FLUX, UNDERTOW_U/V */
+    int    track_radiation;       /* Radiation, Umean or Vmean output (F): the radiation-stress, momentum-flux
+                                     and breaking-dissipation sums of CALCULATE_MEAN (mixing.F:156-219) */
 } fw_params;
 
 typedef struct fw_ctx fw_ctx;
@@ -137,7 +139,16 @@ int fw_set_field(fw_ctx *ctx, const char *name, const void *host);
  * as double (masks as 0/1).  For station output (STATIONS, io.F:3786-3954)
  * without moving whole fields.  Synchronous. */
 int fw_get_points(fw_ctx *ctx, const char *name, int n, const int *I, const int *J, double *out);
-/* scalars "TIME","DT","EtaBlowVal","T_brk","Width_WK","ilo","ihi","jlo","jhi","T_sum" */
+/* scalars "TIME","DT","EtaBlowVal","T_brk","Width_WK","ilo","ihi","jlo","jhi","T_sum",
+ * "ICOUNT_MEAN" (CALCULATE_MEAN intervals ended so far, the number of
+ * PREVIEW_MEAN's files).  With track_radiation, fw_get_field also knows
+ * CALCULATE_MEAN's "P_center","Q_center","U_davg","V_davg","Wsurf",
+ * "BreakSourceX","BreakSourceY" (last stage's values), their sums
+ * ("U_davg_sum" .. "BreakDissY_sum"), the means "U_davg_mean","V_davg_mean",
+ * "P_mean","Q_mean","UUmean","UVmean","VVmean","WWmean","FRCXmean",
+ * "FRCYmean","BreakDissX","BreakDissY" and the gradient fields "DxSxx",
+ * "DySxy","DySyy","DxSxy","PgrdX","PgrdY","DxUUH","DyUVH","DyVVH","DxUVH"
+ * (mixing.F:156-219). */
 int fw_get_scalar(fw_ctx *ctx, const char *name, double *value);
 int fw_set_scalar(fw_ctx *ctx, const char *name, double value);
 

@@ -61,6 +61,16 @@ struct ofw_ctx {
     double *HeightMin, *VelocityMax, *MomentumFluxMax, *ETAmean, *Umean, *Vmean, *ETAsum, *Usum, *Vsum,
         *ETA2sum, *ETA2mean, *SigWaveHeight, *Emax, *Emin, *HavgSum, *HrmsSum, *WaveHeightAve, *WaveHeightRMS;
     int *Num_Zero_Up;
+    /* radiation stress, momentum flux and breaking dissipation of
+     * CALCULATE_MEAN (mixing.F:156-200), with their per-stage inputs from
+     * ESTIMATE_HUV (etauv_solver.F:94-101, 247) and SourceTerms
+     * (sources.F:428-456) */
+    double *P_center, *Q_center, *U_davg, *V_davg, *Wsurf, *BreakSourceX, *BreakSourceY;
+    double *U_davg_sum, *V_davg_sum, *P_sum, *Q_sum, *UUsum, *UVsum, *VVsum, *WWsum, *FRCXsum, *FRCYsum,
+        *BreakDissX_sum, *BreakDissY_sum;
+    double *U_davg_mean, *V_davg_mean, *P_mean, *Q_mean, *UUmean, *UVmean, *VVmean, *WWmean, *FRCXmean,
+        *FRCYmean, *BreakDissX, *BreakDissY;
+    double *DxSxx, *DySxy, *DySyy, *DxSxy, *PgrdX, *PgrdY, *DxUUH, *DyUVH, *DyVVH, *DxUVH;
     int *MASK, *MASK9, *MASK_STRUC;
     /* x-face arrays */
     double *Depthx, *P, *Fx, *Gx, *UxL, *UxR, *VxL, *VxR, *HUxL, *HUxR, *HVxL,
@@ -124,6 +134,13 @@ static const field_desc FIELDS[] = {
     FD(Vmean, 0), FD(ETAsum, 0), FD(Usum, 0), FD(Vsum, 0), FD(ETA2sum, 0), FD(ETA2mean, 0),
     FD(SigWaveHeight, 0), FD(Emax, 0), FD(Emin, 0), FD(HavgSum, 0), FD(HrmsSum, 0),
     FD(WaveHeightAve, 0), FD(WaveHeightRMS, 0), FI(Num_Zero_Up, 0),
+    FD(P_center, 0), FD(Q_center, 0), FD(U_davg, 0), FD(V_davg, 0), FD(Wsurf, 0), FD(BreakSourceX, 0),
+    FD(BreakSourceY, 0), FD(U_davg_sum, 0), FD(V_davg_sum, 0), FD(P_sum, 0), FD(Q_sum, 0), FD(UUsum, 0),
+    FD(UVsum, 0), FD(VVsum, 0), FD(WWsum, 0), FD(FRCXsum, 0), FD(FRCYsum, 0), FD(BreakDissX_sum, 0),
+    FD(BreakDissY_sum, 0), FD(U_davg_mean, 0), FD(V_davg_mean, 0), FD(P_mean, 0), FD(Q_mean, 0), FD(UUmean, 0),
+    FD(UVmean, 0), FD(VVmean, 0), FD(WWmean, 0), FD(FRCXmean, 0), FD(FRCYmean, 0), FD(BreakDissX, 0),
+    FD(BreakDissY, 0), FD(DxSxx, 0), FD(DySxy, 0), FD(DySyy, 0), FD(DxSxy, 0), FD(PgrdX, 0), FD(PgrdY, 0),
+    FD(DxUUH, 0), FD(DyUVH, 0), FD(DyVVH, 0), FD(DxUVH, 0),
     FI(MASK, 0), FI(MASK9, 0), FI(MASK_STRUC, 0),
     FD(Depthx, 1), FD(P, 1), FD(Fx, 1), FD(Gx, 1), FD(UxL, 1), FD(UxR, 1),
     FD(VxL, 1), FD(VxR, 1), FD(HUxL, 1), FD(HUxR, 1), FD(HVxL, 1), FD(HVxR, 1),
@@ -313,6 +330,12 @@ static void phi_coll_var(ofw_ctx *o, double *PHI, int ld, int m, int ie, int je)
  * and V_davg are output-only diagnostics and are not kept here. */
 void ofw_exchange(ofw_ctx *o) {
     phi_coll(o, o->Eta, 1);
+    /* for radiation stress (bc.F:438-443) */
+    phi_coll(o, o->Wsurf, 1);
+    phi_coll(o, o->P_center, 1);
+    phi_coll(o, o->Q_center, 1);
+    phi_coll(o, o->U_davg, 1);
+    phi_coll(o, o->V_davg, 1);
     if (o->p.viscosity_breaking) phi_coll(o, o->AGE, 1);
     if (o->p.viscosity_breaking) phi_coll(o, o->nu_break, 1);
     if (o->p.viscosity_breaking) {
@@ -1093,6 +1116,7 @@ void ofw_source_terms(ofw_ctx *o) {
                             0.5 / DY *
                                 (nyp * 1.0 / DY * (C2(o->HU, I, J + 1) - HUc) -
                                  nym * 1.0 / DY * (HUc - C2(o->HU, I, J - 1)));
+                C2(o->BreakSourceX, I, J) = BX;
                 SX = SX + BX;
                 double BY = 0.5 / DX *
                                 (nxp * 1.0 / DX * (C2(o->HV, I + 1, J) - HVc) -
@@ -1100,6 +1124,7 @@ void ofw_source_terms(ofw_ctx *o) {
                             0.5 / DY *
                                 (nyp * 1.0 / DY * (C2(o->HV, I, J + 1) - HVc) -
                                  nym * 1.0 / DY * (HVc - C2(o->HV, I, J - 1)));
+                C2(o->BreakSourceY, I, J) = BY;
                 SY = SY + BY;
             }
             C2(o->SourceX, I, J) = SX;
@@ -1301,6 +1326,19 @@ void ofw_estimate_huv(ofw_ctx *o, int istage) {
     const double DX = o->p.DX, DY = o->p.DY, DT = o->DT;
     const double al = RK_ALPHA[istage - 1], be = RK_BETA[istage - 1];
     const int wk = o->p.wavemaker;
+    /* for radiation stress (etauv_solver.F:94-101), with the H of the
+     * stage's start */
+    OMP_FOR
+    for (int J = o->Jbeg; J <= o->Jend; J++)
+        for (int I = o->Ibeg; I <= o->Iend; I++) {
+            const double pc = 0.5 * (X2(o->P, I + 1, J) + X2(o->P, I, J));
+            const double qc = 0.5 * (Y2(o->Q, I, J + 1) + Y2(o->Q, I, J));
+            const double hm = dmax(C2(o->H, I, J), o->p.min_depth_frc);
+            C2(o->P_center, I, J) = pc;
+            C2(o->Q_center, I, J) = qc;
+            C2(o->U_davg, I, J) = pc / hm;
+            C2(o->V_davg, I, J) = qc / hm;
+        }
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++) {
@@ -1312,6 +1350,7 @@ void ofw_estimate_huv(ofw_ctx *o, int istage) {
                 if (fabs(xmk - o->p.xc_wk) < o->Width_WK && fabs(ymk - o->p.yc_wk) < o->p.ywidth_wk / 2.0)
                     R1 = R1 + C2(o->WaveMaker_Mass, I, J);
             }
+            C2(o->Wsurf, I, J) = R1; /* etauv_solver.F:247 */
             double eta = al * C2(o->Eta0, I, J) + be * (C2(o->Eta, I, J) + DT * R1);
             if (o->p.eta_limiter) {
                 if (eta < o->p.trough_limit) eta = o->p.trough_limit;
@@ -1521,13 +1560,35 @@ void ofw_max_min_property(ofw_ctx *o) {
     }
 }
 
+/* the radiation-stress, momentum-flux and breaking-dissipation sums of one
+ * cell (mixing.F:156-167 and 270-281), with the ETAmean and U_davg_mean the
+ * caller's branch has at that point */
+static void radiation_sums(ofw_ctx *o, size_t k, double DT) {
+    const double ud = o->U_davg[k] - o->U_davg_mean[k], vd = o->V_davg[k] - o->V_davg_mean[k];
+    const double hd = o->Eta[k] - o->ETAmean[k] + o->Depth[k];
+    const double u = o->U[k], v = o->V[k];
+    o->U_davg_sum[k] = o->U_davg[k] * DT + o->U_davg_sum[k];
+    o->V_davg_sum[k] = o->V_davg[k] * DT + o->V_davg_sum[k];
+    o->P_sum[k] = o->P_center[k] * DT + o->P_sum[k];
+    o->Q_sum[k] = o->Q_center[k] * DT + o->Q_sum[k];
+    o->UUsum[k] = ud * ud * hd * DT + o->UUsum[k];
+    o->UVsum[k] = ud * vd * hd * DT + o->UVsum[k];
+    o->VVsum[k] = vd * vd * hd * DT + o->VVsum[k];
+    o->WWsum[k] = 0.25 * o->Wsurf[k] * o->Wsurf[k] * hd * DT + o->WWsum[k];
+    o->FRCXsum[k] = u * sqrt(u * u + v * v) * DT + o->FRCXsum[k];
+    o->FRCYsum[k] = v * sqrt(u * u + v * v) * DT + o->FRCYsum[k];
+    o->BreakDissX_sum[k] = o->BreakDissX_sum[k] + o->BreakSourceX[k] * DT;
+    o->BreakDissY_sum[k] = o->BreakDissY_sum[k] + o->BreakSourceY[k] * DT;
+}
+
 /* MIXING_STUFF / CALCULATE_MEAN (mixing.F:53-78, 108-305) from STEADY_TIME
  * on: time sums of Eta, U, V and (Eta-ETAmean)^2 over intervals of
  * T_INTV_mean, their means at the end of each interval, and zero-up-
- * crossing wave heights.  The radiation-stress, momentum-flux and breaking-
- * dissipation sums of the same routine are not restated.  ETAsum, Usum,
- * Vsum, ETA2sum, ETA2mean and SigWaveHeight start at zero (the reference
- * allocates them without setting them).  The literal 4.004 is default REAL. */
+ * crossing wave heights; the radiation-stress, momentum-flux and breaking-
+ * dissipation sums and means, and at the end of an interval the gradient
+ * fields DxSxx .. DxUVH on the interior (mixing.F:183-219).  Every sum and
+ * mean starts at zero (the reference allocates some of them without setting
+ * them).  The literals 4.004, 9.80 and 0.5*9.80 are default REAL. */
 void ofw_mixing_stuff(ofw_ctx *o) {
     if (!(o->TIME >= o->p.steady_time)) return;
     const size_t nc = (size_t)o->Mloc * o->Nloc;
@@ -1545,7 +1606,51 @@ void ofw_mixing_stuff(ofw_ctx *o) {
             o->Umean[k] = o->Usum[k] / Ts;
             o->Vmean[k] = o->Vsum[k] / Ts;
             o->ETAmean[k] = o->ETAsum[k] / Ts;
+            radiation_sums(o, k, DT);
+            o->U_davg_mean[k] = o->U_davg_sum[k] / Ts;
+            o->V_davg_mean[k] = o->V_davg_sum[k] / Ts;
+            o->P_mean[k] = o->P_sum[k] / Ts;
+            o->Q_mean[k] = o->Q_sum[k] / Ts;
+            o->UUmean[k] = o->UUsum[k] / Ts;
+            o->UVmean[k] = o->UVsum[k] / Ts;
+            o->VVmean[k] = o->VVsum[k] / Ts;
+            o->WWmean[k] = o->WWsum[k] / Ts;
+            o->FRCXmean[k] = o->FRCXsum[k] / Ts;
+            o->FRCYmean[k] = o->FRCYsum[k] / Ts;
+            o->BreakDissX[k] = o->BreakDissX_sum[k] / Ts;
+            o->BreakDissY[k] = o->BreakDissY_sum[k] / Ts;
         }
+        const double DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
+        const double g98 = (double)9.80f, g49 = (double)(0.5f * 9.80f);
+        for (int J = o->Jbeg; J <= o->Jend; J++)
+            for (int I = o->Ibeg; I <= o->Iend; I++) {
+#define RX(a) ((C2(o->a, I + 1, J) - C2(o->a, I - 1, J)) / 2.0 / DX)
+#define RY(a) ((C2(o->a, I, J + 1) - C2(o->a, I, J - 1)) / 2.0 / DY)
+#define HM(I_, J_) dmax(C2(o->Depth, I_, J_) + C2(o->ETAmean, I_, J_), mdf)
+                C2(o->DxSxx, I, J) = RX(UUmean) - RX(WWmean) +
+                                     g49 * (C2(o->ETA2mean, I + 1, J) - C2(o->ETA2mean, I - 1, J)) / 2.0 / DX;
+                C2(o->DySxy, I, J) = RY(UVmean);
+                C2(o->DySyy, I, J) = RY(VVmean) - RY(WWmean) +
+                                     g49 * (C2(o->ETA2mean, I, J + 1) - C2(o->ETA2mean, I, J - 1)) / 2.0 / DY;
+                C2(o->DxSxy, I, J) = RX(UVmean);
+                C2(o->PgrdX, I, J) = g98 * (C2(o->Depth, I, J) + C2(o->ETAmean, I, J)) *
+                                     (C2(o->ETAmean, I + 1, J) - C2(o->ETAmean, I - 1, J)) / 2.0 / DX;
+                C2(o->PgrdY, I, J) = g98 * (C2(o->Depth, I, J) + C2(o->ETAmean, I, J)) *
+                                     (C2(o->ETAmean, I, J + 1) - C2(o->ETAmean, I, J - 1)) / 2.0 / DY;
+                C2(o->DxUUH, I, J) = (C2(o->P_mean, I + 1, J) * C2(o->P_mean, I + 1, J) / HM(I + 1, J) -
+                                      C2(o->P_mean, I - 1, J) * C2(o->P_mean, I - 1, J) / HM(I - 1, J)) / 2.0 / DX;
+                C2(o->DyUVH, I, J) = (C2(o->P_mean, I, J + 1) * C2(o->Q_mean, I, J + 1) / HM(I, J + 1) -
+                                      C2(o->P_mean, I, J - 1) * C2(o->Q_mean, I, J - 1) / HM(I, J - 1)) / 2.0 / DY;
+                C2(o->DyVVH, I, J) = (C2(o->Q_mean, I, J + 1) * C2(o->Q_mean, I, J + 1) / HM(I, J + 1) -
+                                      C2(o->Q_mean, I, J - 1) * C2(o->Q_mean, I, J - 1) / HM(I, J - 1)) / 2.0 / DY;
+                C2(o->DxUVH, I, J) = (C2(o->P_mean, I + 1, J) * C2(o->Q_mean, I + 1, J) / HM(I + 1, J) -
+                                      C2(o->P_mean, I - 1, J) * C2(o->Q_mean, I - 1, J) / HM(I - 1, J)) / 2.0 / DX;
+                C2(o->FRCXmean, I, J) = C2(o->FRCXmean, I, J) * C2(o->Cd, I, J);
+                C2(o->FRCYmean, I, J) = C2(o->FRCYmean, I, J) * C2(o->Cd, I, J);
+#undef RX
+#undef RY
+#undef HM
+            }
         o->T_sum = o->T_sum - o->p.t_intv_mean;
         const double c4 = (double)(float)4.004;
         for (size_t k = 0; k < nc; k++) {
@@ -1553,6 +1658,9 @@ void ofw_mixing_stuff(ofw_ctx *o) {
             o->Vsum[k] = 0.0;
             o->ETAsum[k] = 0.0;
             o->ETA2sum[k] = 0.0;
+            o->U_davg_sum[k] = o->V_davg_sum[k] = o->P_sum[k] = o->Q_sum[k] = 0.0;
+            o->UUsum[k] = o->UVsum[k] = o->VVsum[k] = o->WWsum[k] = 0.0;
+            o->FRCXsum[k] = o->FRCYsum[k] = o->BreakDissX_sum[k] = o->BreakDissY_sum[k] = 0.0;
             o->SigWaveHeight[k] = c4 * sqrt(o->ETA2mean[k]);
             if (o->Num_Zero_Up[k] >= 2) {
                 o->WaveHeightAve[k] = o->HavgSum[k] / o->Num_Zero_Up[k];
@@ -1566,6 +1674,7 @@ void ofw_mixing_stuff(ofw_ctx *o) {
             o->ETAsum[k] = o->Eta[k] * DT + o->ETAsum[k];
             const double d = o->Eta[k] - o->ETAmean[k];
             o->ETA2sum[k] = d * d * DT + o->ETA2sum[k];
+            radiation_sums(o, k, DT);
             const double eta = o->Eta[k];
             if (eta > o->Emax[k]) o->Emax[k] = eta;
             if (eta < o->Emin[k]) o->Emin[k] = eta;

@@ -65,3 +65,18 @@ def test_strerror(fw):
     L = fw.load_library()
     assert L.fw_strerror(-4).decode().startswith("blow-up")
     assert L.fw_strerror(0).decode() == "ok"
+    assert L.fw_strerror(-9).decode().startswith("checkpoint file")
+
+
+def test_output_switches_under_their_input_keys(fw):
+    """input.txt names the output switches Hmax, Umean, Radiation, ...
+    (io.F:3392-3424); read_input_txt maps them to the OUT_* names, and the
+    radiation sums are switched on for Radiation, Umean or Vmean."""
+    from funwave_tvd_gb300.solver import params_struct
+    deck = "Mglob = 8\nNglob = 8\nDX = 1.0\nDY = 1.0\nHmax = T\nMFmax = T\nUmean = T\nRadiation = F\n"
+    p = fw.read_input_txt(deck)
+    assert p["OUT_Hmax"] is True and p["OUT_MFmax"] is True and p["OUT_Umean"] is True
+    assert p["OUT_Radiation"] is False and "Hmax" not in p
+    s = params_struct(p)
+    assert s.track_hmax == 1 and s.track_mfmax == 1 and s.track_hmin == 0 and s.track_radiation == 1
+    assert params_struct(fw.read_input_txt("Mglob = 8\nNglob = 8\nDX = 1.0\nDY = 1.0\n")).track_radiation == 0

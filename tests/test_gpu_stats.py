@@ -70,3 +70,72 @@ def test_statistics_mixed_against_fp64(fw):
     assert np.abs(ed).max() > 0.0
     assert float(np.sqrt(np.mean((em - ed) ** 2))) <= 1e-4
     assert float(np.abs(hm - hd).max()) <= 5e-3
+
+
+# CALCULATE_MEAN's radiation-stress, momentum-flux and breaking-dissipation
+# part (mixing.F:156-219) with the last stage's inputs (etauv_solver.F:94-101,
+# 247; sources.F:428-456) and their exchange (bc.F:438-443)
+RAD_STEP = ("P_center", "Q_center", "U_davg", "V_davg", "Wsurf", "BreakSourceX", "BreakSourceY")
+RAD_MEANS = ("U_davg_mean", "V_davg_mean", "P_mean", "Q_mean", "UUmean", "UVmean", "VVmean", "WWmean",
+             "FRCXmean", "FRCYmean", "BreakDissX", "BreakDissY")
+RAD_GRAD = ("DxSxx", "DySxy", "DySyy", "DxSxy", "PgrdX", "PgrdY", "DxUUH", "DyUVH", "DyVVH", "DxUVH")
+
+
+def _rad_params(fw, Mglob, Nglob, seed, t_intv, periodic=True):
+    p, depth = _stat_params(fw, Mglob, Nglob, seed, t_intv)
+    p.update({"OUT_Radiation": True, "PERIODIC": periodic, "Cd": 0.002})
+    return p, depth
+
+
+@pytest.mark.parametrize("periodic", [True, False])
+def test_radiation_fp64_parity(fw, oracle_mod, periodic):
+    p, depth = _rad_params(fw, 64, 48, 7, 0.5, periodic)
+    s, o = make_pair(fw, oracle_mod, p, depth)
+    for _ in range(45):
+        s.step(1)
+        o.step()
+    assert s.scalar("ICOUNT_MEAN") >= 2  # at least two intervals ended
+    for name in RAD_STEP:
+        a, b = s.get(name), o[name]
+        scale = max(float(np.abs(b).max()), 1e-6)
+        e = float(np.abs(a - b).max()) / scale
+        assert e <= 1e-9, "%s: %.3e" % (name, e)
+    for name in RAD_MEANS + RAD_GRAD:
+        a, b = s.get(name), o[name]
+        scale = float(np.abs(b).max())
+        assert scale > 0.0 or name.startswith("BreakDiss"), name
+        e = float(np.abs(a - b).max()) / max(scale, 1e-12)
+        assert e <= 1e-8, "%s: %.3e" % (name, e)
+    s.close()
+
+
+def test_radiation_mixed_against_fp64(fw):
+    """Mixed against FP64 after 300 steps with 6 s intervals: the means of
+    the second interval to a few 1e-3 of their scale (the float sums are
+    Kahan-compensated; the flows differ at the stated eta error)."""
+    p, depth = _rad_params(fw, 96, 64, 9, 6.0)
+    res = {}
+    for prec in ("FP64", "MIXED"):
+        s = fw.Solver(fw.with_defaults(p), precision=prec)
+        s.init(depth)
+        s.step(300)
+        res[prec] = {n: interior(s.get(n)) for n in RAD_MEANS[:10] + ("DxSxx", "PgrdX")}
+        assert s.scalar("ICOUNT_MEAN") >= 2
+        s.close()
+    for n, d in res["FP64"].items():
+        m = res["MIXED"][n]
+        scale = float(np.abs(d).max())
+        assert scale > 0.0, n
+        rms = float(np.sqrt(np.mean((m - d) ** 2))) / scale
+        assert rms <= 5e-3, "%s: %.3e" % (n, rms)
+
+
+def test_radiation_fields_absent_when_off(fw):
+    p, depth = _stat_params(fw, 32, 24, 1, 0.5)
+    s = fw.Solver(fw.with_defaults(p), precision="MIXED")
+    s.init(depth)
+    s.step(4)
+    for n in ("UUmean", "DxSxx", "Wsurf"):
+        with pytest.raises(fw.FwError):
+            s.get(n)
+    s.close()

@@ -302,3 +302,49 @@ def test_driver_ini_uvz_hot_start_time(fw, tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     u1 = np.fromfile(os.path.join(d, "u_00001"), dtype=np.float64).reshape(16, 24).T
     assert np.all(u1 == 0.0)
+
+
+@pytest.mark.gpu
+def test_driver_preview_mean_files(fw, tmp_path):
+    """PREVIEW_MEAN (io.F:4630-4736): at the end of every CALCULATE_MEAN
+    interval the driver writes umean/ulagm, vmean/vlagm, etamean, Hrms/Havg/
+    Hsig and the Radiation files numbered by interval; the last set equals
+    the Solver's means after the same steps (binary, bit for bit)."""
+    d = str(tmp_path)
+    extra = dict(_SLOPE, TOTAL_TIME=3.2, PLOT_INTV=10.0, STEADY_TIME=0.0, T_INTV_mean=1.0, Umean="T",
+                 Vmean="T", ETAmean="T", WaveHeight="T", Radiation="T", Cd=0.003)
+    keys = _run_driver(fw, d, extra)
+    n = len([f for f in os.listdir(d) if f.startswith("etamean_")])
+    assert n == 3
+    for stem in ("umean", "ulagm", "vmean", "vlagm", "Hrms", "Havg", "Hsig", "Sxx", "Sxy", "Syy", "DxSxx",
+                 "DySxy", "DySyy", "DxSxy", "PgrdX", "PgrdY", "DxUUH", "DyUVH", "DyVVH", "DxUVH", "FRCX", "FRCY",
+                 "BrkDissX", "BrkDissY"):
+        assert os.path.exists(os.path.join(d, "%s_%05d" % (stem, n))), stem
+    p = {k: v for k, v in _SLOPE.items() if k not in ("FIELD_IO_TYPE", "DEPTH_TYPE", "DEPTH_FLAT", "SLP", "Xslp")}
+    p.update({"Mglob": 24, "Nglob": 16, "DX": 2.0, "DY": 2.0, "PERIODIC": True, "STEADY_TIME": 0.0,
+              "T_INTV_mean": 1.0, "OUT_Radiation": True, "OUT_Umean": True, "Cd": 0.003})
+    i0 = int(20.0 / 2.0) + 1
+    I = np.arange(1, 25)
+    depth = np.asfortranarray(np.repeat(np.where(I >= i0, 3.0 - 0.2 * (I - i0) * 2.0, 3.0)[:, None], 16, axis=1))
+    s = fw.Solver(fw.with_defaults(p), precision="FP64")
+    s.init(depth)
+    while s.scalar("TIME") < 3.2:
+        s.step(1)
+    assert s.scalar("ICOUNT_MEAN") == n
+
+    def rd(stem):
+        return np.fromfile(os.path.join(d, "%s_%05d" % (stem, n)), dtype=np.float64).reshape(16, 24).T
+
+    def cur(name):
+        return s.get(name)[3:-3, 3:-3]
+
+    for stem, name in (("etamean", "ETAmean"), ("umean", "Umean"), ("Hsig", "SigWaveHeight"), ("Sxy", "UVmean"),
+                       ("DxSxx", "DxSxx"), ("PgrdX", "PgrdX"), ("DyVVH", "DyVVH"), ("FRCX", "FRCXmean"),
+                       ("BrkDissX", "BreakDissX")):
+        assert np.array_equal(rd(stem), cur(name)), stem
+    c49 = float(np.float32(0.5) * np.float32(9.8))
+    assert np.array_equal(rd("Sxx"), cur("UUmean") - cur("WWmean") + c49 * cur("ETA2mean"))
+    hm = np.maximum(cur("Depth") + cur("ETAmean"), 0.1)
+    assert np.array_equal(rd("ulagm"), cur("P_mean") / hm)
+    assert np.abs(rd("DxSxx")).max() > 0 and np.abs(rd("FRCX")).max() > 0
+    s.close()

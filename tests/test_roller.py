@@ -16,12 +16,14 @@ from helpers import G, make_pair
 
 pytestmark = pytest.mark.gpu
 
-FIELDS = ("ROLLER_FLUX", "UNDERTOW_U", "UNDERTOW_V")
+# with the breaking-dissipation means of CALCULATE_MEAN (mixing.F:166-180),
+# which sum BreakSourceX/Y of the last stage
+FIELDS = ("ROLLER_FLUX", "UNDERTOW_U", "UNDERTOW_V", "BreakDissX", "BreakDissY", "BreakSourceX")
 
 
 def _case(fw):
     p, d, ph, _ = fw.cases.barred_beach(480, 64, 1.0, seed=4, wk_from_shore=120.0)
-    p.update({"ROLLER": True, "UNDERTOW": True, "STEADY_TIME": 0.0, "T_INTV_mean": 4.0})
+    p.update({"ROLLER": True, "UNDERTOW": True, "STEADY_TIME": 0.0, "T_INTV_mean": 4.0, "OUT_Radiation": True})
     return p, d, ph
 
 
