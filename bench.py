@@ -221,7 +221,8 @@ def kernel_profile(s, T, cells, faces_x, faces_y, hbm):
 
 def e2e_run(fw, s, K):
     """Per step through the C ABI with pinned host buffers: upload Eta, U,
-    V, Ubar, Vbar, one fw_step, read back Eta, U, V."""
+    V, Ubar, Vbar (one fw_set_fields), one fw_step, read back Eta, U, V (one
+    fw_get_fields)."""
     import numpy as np
     import torch
     shp = (s.Mloc, s.Nloc)
@@ -233,16 +234,19 @@ def e2e_run(fw, s, K):
         bufs[n] = (t, a)
     import ctypes
     L = s.L
+    up, down = ("Eta", "U", "V", "Ubar", "Vbar"), ("Eta", "U", "V")
+    up_n = (ctypes.c_char_p * 5)(*[n.encode() for n in up])
+    up_p = (ctypes.c_void_p * 5)(*[bufs[n][1].ctypes.data for n in up])
+    down_n = (ctypes.c_char_p * 3)(*[n.encode() for n in down])
+    down_p = (ctypes.c_void_p * 3)(*[bufs[n][1].ctypes.data for n in down])
     s.sync()
     t0 = time.perf_counter()
     for _ in range(K):
-        for n in ("Eta", "U", "V", "Ubar", "Vbar"):
-            rc = L.fw_set_field(s.ctx, n.encode(), bufs[n][1].ctypes.data)
-            assert rc == 0
+        rc = L.fw_set_fields(s.ctx, 5, up_n, up_p)
+        assert rc == 0
         s.step(1, check=False)
-        for n in ("Eta", "U", "V"):
-            rc = L.fw_get_field(s.ctx, n.encode(), bufs[n][1].ctypes.data)
-            assert rc == 0
+        rc = L.fw_get_fields(s.ctx, 3, down_n, down_p)
+        assert rc == 0
     s.sync()
     dt = time.perf_counter() - t0
     nb = s.Mloc * s.Nloc * 8
@@ -714,7 +718,7 @@ def main():
                           "frac": STEP_BYTES["mixed"] * cells / step_s / 1e9 / hbm, "peak_kind": peak_kind},
         "e2e": {"value": cells * e2e_steps / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "what": "per step: Eta,U,V,Ubar,Vbar uploaded from pinned host memory, fw_step, Eta,U,V read back"},
+                "what": "per step: Eta,U,V,Ubar,Vbar uploaded from pinned host memory (one fw_set_fields), fw_step, Eta,U,V read back (one fw_get_fields)"},
         "fp64": res64,
         "ensemble": ens,
         "kernels_ms": {k: round(v["ms"], 4) for k, v in prof.items()},

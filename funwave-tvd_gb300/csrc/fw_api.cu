@@ -664,6 +664,9 @@ int fw_destroy(fw_ctx *c) {
     for (cudaGraphExec_t g1 : c->graph1)
         if (g1) cudaGraphExecDestroy(g1);
     if (c->out_buf) cudaFree(c->out_buf);
+    if (c->in_buf) cudaFree(c->in_buf);
+    for (cudaEvent_t ev : c->in_ev)
+        if (ev) cudaEventDestroy(ev);
     if (c->out_ready) cudaEventDestroy(c->out_ready);
     if (c->out_done) cudaEventDestroy(c->out_done);
     if (c->out_stream) cudaStreamDestroy(c->out_stream);
@@ -1454,6 +1457,15 @@ int fw_restore(fw_ctx *c, const char *path) {
 // the state after every step enqueued before it; the device-to-host copies
 // run on a second stream while later steps run.
 // ---------------------------------------------------------------------------
+// both output streams and events, created on first use
+static int ensure_out_stream(fw_ctx *c) {
+    if (c->out_stream) return FW_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->out_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->out_ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->out_done, cudaEventDisableTiming);
+    return cuda_status(c, e);
+}
+
 int fw_output_wait(fw_ctx *c) {
     if (!c) return FW_ERR_BAD_PARAM;
     if (!c->out_pending) return FW_OK;
@@ -1491,12 +1503,7 @@ int fw_output_begin(fw_ctx *c, int n, const char *const *names, void *const *hos
     // the previous snapshot's copies read out_buf: let them finish
     if ((rc = fw_output_wait(c)) != FW_OK) return rc;
     cudaError_t e = cudaSuccess;
-    if (!c->out_stream) {
-        e = cudaStreamCreateWithFlags(&c->out_stream, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->out_ready, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->out_done, cudaEventDisableTiming);
-        if (e != cudaSuccess) return cuda_status(c, e);
-    }
+    if ((rc = ensure_out_stream(c)) != FW_OK) return rc;
     if (off[n] > c->out_cap) {
         // nothing reads the old buffer: the copies waited for above ran
         // after the previous snapshot's kernels
@@ -1532,6 +1539,77 @@ int fw_output_begin(fw_ctx *c, int n, const char *const *names, void *const *hos
     if (e != cudaSuccess) return cuda_status(c, e);
     c->out_pending = 1;
     return finish(c);
+}
+
+// Several fields from the host at once: every plane is copied into a device
+// input buffer on the second stream, and each conversion into its field
+// starts on the step stream as soon as that plane has arrived, so copies and
+// conversions overlap; one wait at the end.
+int fw_set_fields(fw_ctx *c, int n, const char *const *names, const void *const *host) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    if (c->sticky_error) return FW_ERR_CUDA;
+    if (n < 1 || n > 16 || !names || !host) return FW_ERR_BAD_PARAM;
+    const bool fp64 = c->p.precision == FW_PREC_FP64;
+    std::vector<FieldRef> refs((size_t)n);
+    std::vector<size_t> off((size_t)n + 1, 0);
+    for (int k = 0; k < n; k++) {
+        if (!names[k] || !host[k]) return FW_ERR_BAD_PARAM;
+        const bool ok = fp64 ? find_field<double>(c, names[k], refs[k]) : find_field<float>(c, names[k], refs[k]);
+        if (!ok) return FW_ERR_BAD_PARAM;
+        int w, h;
+        extent(c, refs[k].kind, w, h);
+        const size_t bytes = (size_t)w * h * (refs[k].is_mask ? sizeof(int) : sizeof(double));
+        off[k + 1] = off[k] + (bytes + 255) / 256 * 256;
+    }
+    int rc = ensure_out_stream(c);
+    if (rc != FW_OK) return rc;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < n && e == cudaSuccess; k++)
+        if (!c->in_ev[k]) e = cudaEventCreateWithFlags(&c->in_ev[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    // the step stream may still read the buffer (an earlier call's
+    // conversions): it is idle after this wait
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cuda_status(c, e);
+    if (off[n] > c->in_cap) {
+        if (c->in_buf) cudaFree(c->in_buf);
+        c->in_buf = nullptr;
+        c->in_cap = 0;
+        if (cudaMalloc(&c->in_buf, off[n]) != cudaSuccess) {
+            cudaGetLastError();
+            return FW_ERR_OOM;
+        }
+        c->in_cap = off[n];
+    }
+    char *buf = (char *)c->in_buf;
+    // the second stream must not start before the step stream's earlier work
+    e = cudaEventRecord(c->out_ready, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->out_stream, c->out_ready, 0);
+    for (int k = 0; k < n && e == cudaSuccess; k++) {
+        const FieldRef &r = refs[k];
+        int w, h;
+        extent(c, r.kind, w, h);
+        const size_t bytes = (size_t)w * h * (r.is_mask ? sizeof(int) : sizeof(double));
+        e = cudaMemcpyAsync(buf + off[k], host[k], bytes, cudaMemcpyHostToDevice, c->out_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(c->in_ev[k], c->out_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->in_ev[k], 0);
+        if (e != cudaSuccess) break;
+        if (!r.is_mask && fp64)
+            e = cudaMemcpy2DAsync(r.ptr, (size_t)c->g.pitch * sizeof(double), buf + off[k], (size_t)w * sizeof(double),
+                                  (size_t)w * sizeof(double), (size_t)h, cudaMemcpyDeviceToDevice, c->stream);
+        else
+            convert_in(c, buf + off[k], r.is_mask, r.ptr, w, h);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    return finish(c);
+}
+
+// Several fields to the host at once: the asynchronous output's snapshot and
+// copies, then the wait
+int fw_get_fields(fw_ctx *c, int n, const char *const *names, void *const *host) {
+    int rc = fw_output_begin(c, n, names, host);
+    if (rc != FW_OK) return rc;
+    return fw_output_wait(c);
 }
 
 int fw_host_alloc(size_t bytes, void **ptr) {

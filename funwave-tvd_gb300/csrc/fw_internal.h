@@ -221,6 +221,11 @@ struct fw_ctx {
     cudaStream_t out_stream = nullptr;
     cudaEvent_t out_ready = nullptr, out_done = nullptr;
     int out_pending = 0;
+    // batched uploads (fw_set_fields): host-layout planes in in_buf, one
+    // event per plane
+    void *in_buf = nullptr;
+    size_t in_cap = 0;
+    cudaEvent_t in_ev[16] = {};
     template <typename T> fw::Fields<T> &F();
 };
 namespace fw {

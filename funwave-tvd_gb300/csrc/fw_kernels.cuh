@@ -939,7 +939,7 @@ __global__ void __launch_bounds__(256) k_sources(Grid g, Fields<T> f) {
 // (etauv_solver.F:247) and BreakSourceX/Y.
 // ---------------------------------------------------------------------------
 template <typename T, bool RAD = false>
-__global__ void __launch_bounds__(256, 3) k_update(Grid g, Fields<T> f, T al, T be) {
+__global__ void __launch_bounds__(256, sizeof(T) == sizeof(float) ? 4 : 3) k_update(Grid g, Fields<T> f, T al, T be) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mloc || j >= g.Nloc) return;

@@ -250,6 +250,8 @@ def load_library(path=None):
     L.fw_get_tuning.argtypes = [vp, ctypes.POINTER(ip)]
     L.fw_set_tuning.argtypes = [vp, ctypes.POINTER(ip)]
     L.fw_output_begin.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(vp)]
+    L.fw_set_fields.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(vp)]
+    L.fw_get_fields.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(vp)]
     L.fw_output_wait.argtypes = [vp]
     L.fw_output_done.argtypes = [vp]
     L.fw_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(vp)]
@@ -340,6 +342,30 @@ class Solver:
         if a.shape != self.shape(name):
             raise FwError(-3, "%s must have shape %s" % (name, self.shape(name)))
         self._check(self.L.fw_set_field(self.ctx, name.encode(), a.ctypes.data), "set " + name)
+
+    def set_fields(self, arrays):
+        """{name: array} to the device in one call (fw_set_fields); arrays in
+        the layout of set() (Fortran-ordered float64, int32 for masks)."""
+        names = list(arrays)
+        keep = []
+        for n in names:
+            dt = np.int32 if n in _MASKS else np.float64
+            a = np.asfortranarray(arrays[n], dtype=dt)
+            if a.shape != self.shape(n):
+                raise ValueError("%s: shape %s, expected %s" % (n, a.shape, self.shape(n)))
+            keep.append(a)
+        cn = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+        hp = (ctypes.c_void_p * len(names))(*[a.ctypes.data for a in keep])
+        self._check(self.L.fw_set_fields(self.ctx, len(names), cn, hp), "fw_set_fields")
+
+    def get_fields(self, names):
+        """{name: array} from the device in one call (fw_get_fields)."""
+        names = list(names)
+        out = {n: np.zeros(self.shape(n), dtype=np.int32 if n in _MASKS else np.float64, order="F") for n in names}
+        cn = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+        hp = (ctypes.c_void_p * len(names))(*[out[n].ctypes.data for n in names])
+        self._check(self.L.fw_get_fields(self.ctx, len(names), cn, hp), "fw_get_fields")
+        return out
 
     def __getitem__(self, name):
         return self.get(name)

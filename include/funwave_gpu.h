@@ -134,6 +134,13 @@ int fw_init(fw_ctx *ctx, const double *depth, const double *eta, const double *u
  * (double, or int32 for MASK/MASK9/MASK_STRUC).  Synchronous. */
 int fw_get_field(fw_ctx *ctx, const char *name, void *host);
 int fw_set_field(fw_ctx *ctx, const char *name, const void *host);
+/* n fields at once (n <= 16; names and host layouts as above), synchronous.
+ * fw_set_fields copies every plane to the device on a second stream and
+ * converts each one as soon as it has arrived; fw_get_fields is
+ * fw_output_begin followed by fw_output_wait.  With pinned host buffers
+ * (fw_host_alloc) the copies run at the host link's rate. */
+int fw_set_fields(fw_ctx *ctx, int n, const char *const *names, const void *const *host);
+int fw_get_fields(fw_ctx *ctx, int n, const char *const *names, void *const *host);
 /* The values of one field (names as fw_get_field) at n cells given by
  * 1-based Fortran indices I[k], J[k] (ghost cells included in the range),
  * as double (masks as 0/1).  For station output (STATIONS, io.F:3786-3954)

@@ -46,3 +46,36 @@ def test_unknown_or_switched_off_fields_are_refused(fw):
         assert e.value.status == -3
     assert s.output_begin(("Eta",)).wait()["Eta"].shape == (70, 38)
     s.close()
+
+
+@pytest.mark.parametrize("precision", ["MIXED", "FP64"])
+def test_batched_transfers_equal_single_ones(fw, precision):
+    """fw_set_fields / fw_get_fields move the same values as fw_set_field /
+    fw_get_field, masks included."""
+    p, d, _ = fw.cases.planar_beach(Mglob=90, Nglob=40, seed=3)
+    s = fw.Solver(fw.with_defaults(p), precision=precision)
+    s.init(d)
+    s.step(12)
+    names = ("Eta", "U", "V", "Ubar", "Vbar", "MASK", "P")
+    before = s.get_fields(names)
+    for n in names:
+        assert np.array_equal(before[n], s.get(n)), n
+    rng = np.random.default_rng(1)
+    new = {n: before[n] + (0 if n == "MASK" else 1e-3 * rng.standard_normal(before[n].shape)) for n in names}
+    new["MASK"] = before["MASK"].copy()
+    new["MASK"][5, 7] = 1 - new["MASK"][5, 7]
+    s.set_fields(new)
+    ref = fw.Solver(fw.with_defaults(p), precision=precision)
+    ref.init(d)
+    ref.step(12)
+    for n in names:
+        ref.set(n, new[n])
+    for n in names:
+        assert np.array_equal(s.get(n), ref.get(n)), n
+    assert s.step(3) == 0 and ref.step(3) == 0
+    for n in ("Eta", "U", "MASK"):
+        assert np.array_equal(s.get(n), ref.get(n)), n
+    with pytest.raises(fw.FwError):
+        s.set_fields({"Eta": new["Eta"], "nope": new["U"]})
+    s.close()
+    ref.close()
