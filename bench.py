@@ -253,6 +253,26 @@ def e2e_run(fw, s, K):
     return dt, 5 * nb, 3 * nb
 
 
+def link_rates(nbytes, reps=10):
+    """Pinned host <-> device copy rates (GB/s) for planes of nbytes, the
+    bound of the end-to-end leg's transfers."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, f in (("h2d", lambda: d.copy_(h, non_blocking=True)), ("d2h", lambda: h.copy_(d, non_blocking=True))):
+        for _ in range(3):
+            f()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            f()
+        torch.cuda.synchronize()
+        out[name] = nbytes * reps / (time.perf_counter() - t) / 1e9
+    del h, d
+    return out
+
+
 def ensemble_bench(fw, pg, ws, n=512, K=10, W=2, run_seconds=300.0, autotune=True):
     """The 512-run ensemble (planar beaches of uneven size, slope, depth and
     JONSWAP forcing; 1.5e8 cells in all): every member steps concurrently,
@@ -692,6 +712,7 @@ def main():
         s64.close()
     e2e_steps = min(K, 10)
     e2e_dt, h2d, d2h = e2e_run(fw, sm, e2e_steps)
+    link = link_rates(h2d // 5)
     # per-kernel timing last: some kernels update the state in place
     prof = {} if args.no_kernel_profile else kernel_profile(
         sm, 4, cells, (params["Mglob"] + 1) * params["Nglob"], params["Mglob"] * (params["Nglob"] + 1), hbm)
@@ -718,7 +739,12 @@ def main():
                           "frac": STEP_BYTES["mixed"] * cells / step_s / 1e9 / hbm, "peak_kind": peak_kind},
         "e2e": {"value": cells * e2e_steps / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "what": "per step: Eta,U,V,Ubar,Vbar uploaded from pinned host memory (one fw_set_fields), fw_step, Eta,U,V read back (one fw_get_fields)"},
+                "what": "per step: Eta,U,V,Ubar,Vbar uploaded from pinned host memory (one fw_set_fields), fw_step, Eta,U,V read back (one fw_get_fields)",
+                # the transfers' share of a step against the pinned copy rates
+                # of this machine's host link
+                "transfer_ms_per_step": e2e_dt / e2e_steps * 1e3 - ms_mixed / K,
+                "link_gbs": {k: round(v, 1) for k, v in link.items()},
+                "link_bound_ms_per_step": (h2d / link["h2d"] + d2h / link["d2h"]) / 1e6},
         "fp64": res64,
         "ensemble": ens,
         "kernels_ms": {k: round(v["ms"], 4) for k, v in prof.items()},
