@@ -382,8 +382,17 @@ __global__ void __launch_bounds__(256, sizeof(T) == sizeof(float) ? 4 : 1) k_dis
 // BOUNDARY_CONDITION (bc.F:53-295), fused per face.
 // ---------------------------------------------------------------------------
 template <typename T> __device__ __forceinline__ T lim3(T a, T b, T c) {
-    if (a >= (T)0) return tmax((T)0, tmin(tmin(a, (T)2 * b), (T)2 * c));
-    return tmin((T)0, tmax(tmax(a, (T)2 * b), (T)2 * c));
+    if constexpr (sizeof(T) == sizeof(float)) {
+        // s * max(0, min(|a|, 2 s b, 2 s c)), s = sign(a): the same value
+        // without a branch, except that a zero result may carry the other
+        // sign, which the float face values (harmonic means of products
+        // tested > 0) never see
+        const float s = a >= 0.0f ? 1.0f : -1.0f;
+        return s * fmaxf(0.0f, fminf(fminf(fabsf(a), 2.0f * s * b), 2.0f * s * c));
+    } else {
+        if (a >= (T)0) return tmax((T)0, tmin(tmin(a, (T)2 * b), (T)2 * c));
+        return tmin((T)0, tmax(tmax(a, (T)2 * b), (T)2 * c));
+    }
 }
 // Din(p) from v[0..3] = Vin(p-2..p+1), m[0..3] = MASK(p-2..p+1)
 // (fluxes.F:1548-1598).  When any of the four cells is dry the reference
