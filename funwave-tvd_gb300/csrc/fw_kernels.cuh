@@ -1948,7 +1948,7 @@ __host__ __device__ __forceinline__ size_t lsx_smem_floats(int L, int P) {
 // so that the block waits for global memory once instead of once per phase.
 // KPT = 0: any length, loads where they are used.
 template <typename T, int KPT>
-__global__ void __launch_bounds__(256) k_linesolve_x(Grid g, Fields<T> f, LinePart lp, int clear_dirty) {
+__global__ void __launch_bounds__(256, KPT > 0 ? 3 : 1) k_linesolve_x(Grid g, Fields<T> f, LinePart lp, int clear_dirty) {
     extern __shared__ float shf[];
     const int l = blockIdx.x;
     // the factorisation of this stage is complete: the MASK9 change flag
