@@ -46,6 +46,10 @@ constexpr double LARGE = 999999.0;
 __device__ __forceinline__ void prefetch_l1(const void *p) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
+// a load of an array that the kernel does not write: the read-only data
+// path, which also frees the compiler to issue it before the kernel's
+// stores (the Fields pointers could otherwise alias them)
+template <typename X> __device__ __forceinline__ X ro(const X *p) { return __ldg(p); }
 
 __device__ __forceinline__ double fsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float fsqrt(float x) { return sqrtf(x); }
@@ -863,50 +867,50 @@ __device__ __forceinline__ void source_terms_b(const Grid &g, const Fields<T> &f
     const T g1 = GC(gamma1), g2 = GC(gamma2);
     const size_t id = IDX(i, j);
     const size_t ie_ = IDX(i + 1, j), iw = IDX(i - 1, j), in_ = IDX(i, j + 1), is = IDX(i, j - 1);
-    const T U = f.U[id], V = f.V[id];
+    const T U = ro(f.U + (id)), V = ro(f.V + (id));
     const T spd = fsqrt(U * U + V * V);
-    const T m9 = m2r<T>(f.MASK9[id]);
-    const T mk = m2r<T>(f.MASK[id]);
+    const T m9 = m2r<T>(ro(f.MASK9 + (id)));
+    const T mk = m2r<T>(ro(f.MASK + (id)));
     const T Hm = tmax(f.H[id], mdf);
     const T Eta = f.Eta[id];
-    const T U4 = f.U4[id], V4 = f.V4[id];
-    const T dPQ = OX(f.P[ie_] - f.P[id]) + OY(f.Q[in_] - f.Q[id]);
-    const T FrcInsX = -f.Cd[id] * U * spd;
-    T sx = OX((T)GRAV * (Eta)) * (f.Depthx[ie_] - f.Depthx[id]) * mk + FrcInsX +
+    const T U4 = ro(f.U4 + (id)), V4 = ro(f.V4 + (id));
+    const T dPQ = OX(ro(f.P + (ie_)) - ro(f.P + (id))) + OY(ro(f.Q + (in_)) - ro(f.Q + (id)));
+    const T FrcInsX = -ro(f.Cd + (id)) * U * spd;
+    T sx = OX((T)GRAV * (Eta)) * (ro(f.Depthx + (ie_)) - ro(f.Depthx + (id))) * mk + FrcInsX +
            g1 * m9 * Hm *
-               (OX(U * (T)0.5 * (f.U4[ie_] - f.U4[iw])) + OY(V * (T)0.5 * (f.U4[in_] - f.U4[is])) +
-                OX(U4 * (T)0.5 * (f.U[ie_] - f.U[iw])) + OY(V4 * (T)0.5 * (f.U[in_] - f.U[is])) -
-                g2 * m9 * f.Udisp[id]) +
-           g1 * m9 * dPQ * (U4 - f.U1p[id]) + wm * U;
-    const T FrcInsY = -f.Cd[id] * V * spd;
-    T sy = OY((T)GRAV * (Eta)) * (f.Depthy[in_] - f.Depthy[id]) * mk + FrcInsY +
+               (OX(U * (T)0.5 * (ro(f.U4 + (ie_)) - ro(f.U4 + (iw)))) + OY(V * (T)0.5 * (ro(f.U4 + (in_)) - ro(f.U4 + (is)))) +
+                OX(U4 * (T)0.5 * (ro(f.U + (ie_)) - ro(f.U + (iw)))) + OY(V4 * (T)0.5 * (ro(f.U + (in_)) - ro(f.U + (is)))) -
+                g2 * m9 * ro(f.Udisp + (id))) +
+           g1 * m9 * dPQ * (U4 - ro(f.U1p + (id))) + wm * U;
+    const T FrcInsY = -ro(f.Cd + (id)) * V * spd;
+    T sy = OY((T)GRAV * (Eta)) * (ro(f.Depthy + (in_)) - ro(f.Depthy + (id))) * mk + FrcInsY +
            g1 * m9 * Hm *
-               (OX(U * (T)0.5 * (f.V4[ie_] - f.V4[iw])) + OY(V * (T)0.5 * (f.V4[in_] - f.V4[is])) +
-                OX(U4 * (T)0.5 * (f.V[ie_] - f.V[iw])) + OY(V4 * (T)0.5 * (f.V[in_] - f.V[is])) -
-                g2 * m9 * f.Vdisp[id]) +
-           g1 * m9 * dPQ * (V4 - f.V1p[id]) + wm * V;
+               (OX(U * (T)0.5 * (ro(f.V4 + (ie_)) - ro(f.V4 + (iw)))) + OY(V * (T)0.5 * (ro(f.V4 + (in_)) - ro(f.V4 + (is)))) +
+                OX(U4 * (T)0.5 * (ro(f.V + (ie_)) - ro(f.V + (iw)))) + OY(V4 * (T)0.5 * (ro(f.V + (in_)) - ro(f.V + (is)))) -
+                g2 * m9 * ro(f.Vdisp + (id))) +
+           g1 * m9 * dPQ * (V4 - ro(f.V1p + (id))) + wm * V;
     if (g.friction_sponge) {
-        sx = sx - f.CD4[id] * U * spd * f.Depth[id];
-        sy = sy - f.CD4[id] * V * spd * f.Depth[id];
+        sx = sx - ro(f.CD4 + (id)) * U * spd * ro(f.Depth + (id));
+        sy = sy - ro(f.CD4 + (id)) * V * spd * ro(f.Depth + (id));
     }
     if (g.visc_breaking) {
         // nu_vis is a float array (sources.F:69): the face sums are float sums
-        const float nc = (float)f.nu[id];
-        const T nxp = (T)((float)f.nu[ie_] + nc), nxm = (T)((float)f.nu[iw] + nc);
-        const T nyp = (T)((float)f.nu[in_] + nc), nym = (T)((float)f.nu[is] + nc);
-        const T HUc = f.HU[id], HVc = f.HV[id];
+        const float nc = (float)ro(f.nu + (id));
+        const T nxp = (T)((float)ro(f.nu + (ie_)) + nc), nxm = (T)((float)ro(f.nu + (iw)) + nc);
+        const T nyp = (T)((float)ro(f.nu + (in_)) + nc), nym = (T)((float)ro(f.nu + (is)) + nc);
+        const T HUc = ro(f.HU + (id)), HVc = ro(f.HV + (id));
         T bx, by;
         if constexpr (EXACT) {
-            bx = (T)0.5 / DX * (nxp * (T)1 / DX * (f.HU[ie_] - HUc) - nxm * (T)1 / DX * (HUc - f.HU[iw])) +
-                 (T)0.5 / DY * (nyp * (T)1 / DY * (f.HU[in_] - HUc) - nym * (T)1 / DY * (HUc - f.HU[is]));
-            by = (T)0.5 / DX * (nxp * (T)1 / DX * (f.HV[ie_] - HVc) - nxm * (T)1 / DX * (HVc - f.HV[iw])) +
-                 (T)0.5 / DY * (nyp * (T)1 / DY * (f.HV[in_] - HVc) - nym * (T)1 / DY * (HVc - f.HV[is]));
+            bx = (T)0.5 / DX * (nxp * (T)1 / DX * (ro(f.HU + (ie_)) - HUc) - nxm * (T)1 / DX * (HUc - ro(f.HU + (iw)))) +
+                 (T)0.5 / DY * (nyp * (T)1 / DY * (ro(f.HU + (in_)) - HUc) - nym * (T)1 / DY * (HUc - ro(f.HU + (is))));
+            by = (T)0.5 / DX * (nxp * (T)1 / DX * (ro(f.HV + (ie_)) - HVc) - nxm * (T)1 / DX * (HVc - ro(f.HV + (iw)))) +
+                 (T)0.5 / DY * (nyp * (T)1 / DY * (ro(f.HV + (in_)) - HVc) - nym * (T)1 / DY * (HVc - ro(f.HV + (is))));
         } else {
             const T cx = (T)g.f_cx, cy = (T)g.f_cy;
-            bx = cx * (nxp * (f.HU[ie_] - HUc) - nxm * (HUc - f.HU[iw])) +
-                 cy * (nyp * (f.HU[in_] - HUc) - nym * (HUc - f.HU[is]));
-            by = cx * (nxp * (f.HV[ie_] - HVc) - nxm * (HVc - f.HV[iw])) +
-                 cy * (nyp * (f.HV[in_] - HVc) - nym * (HVc - f.HV[is]));
+            bx = cx * (nxp * (ro(f.HU + (ie_)) - HUc) - nxm * (HUc - ro(f.HU + (iw)))) +
+                 cy * (nyp * (ro(f.HU + (in_)) - HUc) - nym * (HUc - ro(f.HU + (is))));
+            by = cx * (nxp * (ro(f.HV + (ie_)) - HVc) - nxm * (HVc - ro(f.HV + (iw)))) +
+                 cy * (nyp * (ro(f.HV + (in_)) - HVc) - nym * (HVc - ro(f.HV + (is))));
         }
         sx = sx + bx;
         sy = sy + by;
@@ -955,7 +959,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == sizeof(float) ? 4 : 3) k_upd
     const size_t id = IDX(i, j);
     const T g3 = GC(gamma3);
     if (i < g.ib || i > g.ie || j < g.jb || j > g.je) {
-        f.H[id] = f.Eta[id] * g3 + f.Depth[id];  // H = Eta*Gamma3+Depth on all cells
+        f.H[id] = f.Eta[id] * g3 + ro(f.Depth + (id));  // H = Eta*Gamma3+Depth on all cells
         return;
     }
     if constexpr (sizeof(T) == sizeof(float)) {
@@ -982,7 +986,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == sizeof(float) ? 4 : 3) k_upd
     const size_t ie_ = IDX(i + 1, j), in_ = IDX(i, j + 1);
     constexpr bool EXACT = sizeof(T) == sizeof(double);
     const T cdx = EXACT ? (T)1 / DX : GC(rdx), cdy = EXACT ? (T)1 / DY : GC(rdy);
-    T R1 = -cdx * (f.P[ie_] * (T)1 + f.P[id] * (T)-1) - cdy * (f.Q[in_] * (T)1 + f.Q[id] * (T)-1);
+    T R1 = -cdx * (ro(f.P + (ie_)) * (T)1 + ro(f.P + (id)) * (T)-1) - cdy * (ro(f.Q + (in_)) * (T)1 + ro(f.Q + (id)) * (T)-1);
     if (g.wavemaker != FW_WK_NONE) {
         const T xmk = i2r<T>(i - g.ib) * DX, ymk = i2r<T>(j - g.jb) * DY;
         if (fabs_(xmk - GC(xc_wk)) < GC(width_wk) && fabs_(ymk - GC(yc_wk)) < GC(ywidth_wk) / (T)2)
@@ -990,7 +994,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == sizeof(float) ? 4 : 3) k_upd
     }
     if constexpr (RAD) {
         const size_t PL = (size_t)g.pitch * (size_t)(g.Nloc + 1);
-        const T pc = (T)0.5 * (f.P[ie_] + f.P[id]), qc = (T)0.5 * (f.Q[in_] + f.Q[id]);
+        const T pc = (T)0.5 * (ro(f.P + (ie_)) + ro(f.P + (id))), qc = (T)0.5 * (ro(f.Q + (in_)) + ro(f.Q + (id)));
         const T hm = tmax(f.H[id], GC(min_depth_frc));  // H before this stage's update
         f.rad[RP_PC * PL + id] = pc;
         f.rad[RP_QC * PL + id] = qc;
@@ -1000,19 +1004,19 @@ __global__ void __launch_bounds__(256, sizeof(T) == sizeof(float) ? 4 : 3) k_upd
         f.rad[RP_BX * PL + id] = BX;
         f.rad[RP_BY * PL + id] = BY;
     }
-    T eta = al * f.Eta0[id] + be * (f.Eta[id] + DT * R1);
+    T eta = al * ro(f.Eta0 + (id)) + be * (f.Eta[id] + DT * R1);
     if (g.eta_limiter) {
         if (eta < GC(trough)) eta = GC(trough);
         if (eta > GC(crest)) eta = GC(crest);
     }
-    const T R2 = -cdx * (f.Fx[ie_] * (T)1 + f.Fx[id] * (T)-1) - cdy * (f.Fy[in_] * (T)1 + f.Fy[id] * (T)-1) + SX;
-    const T ubar = al * f.Ubar0[id] + be * (f.Ubar[id] + DT * R2);
-    const T R3 = -cdx * (f.Gx[ie_] * (T)1 + f.Gx[id] * (T)-1) - cdy * (f.Gy[in_] * (T)1 + f.Gy[id] * (T)-1) + SY;
-    const T vbar = al * f.Vbar0[id] + be * (f.Vbar[id] + DT * R3);
+    const T R2 = -cdx * (ro(f.Fx + (ie_)) * (T)1 + ro(f.Fx + (id)) * (T)-1) - cdy * (ro(f.Fy + (in_)) * (T)1 + ro(f.Fy + (id)) * (T)-1) + SX;
+    const T ubar = al * ro(f.Ubar0 + (id)) + be * (f.Ubar[id] + DT * R2);
+    const T R3 = -cdx * (ro(f.Gx + (ie_)) * (T)1 + ro(f.Gx + (id)) * (T)-1) - cdy * (ro(f.Gy + (in_)) * (T)1 + ro(f.Gy + (id)) * (T)-1) + SY;
+    const T vbar = al * ro(f.Vbar0 + (id)) + be * (f.Vbar[id] + DT * R3);
     f.Eta[id] = eta;
     f.Ubar[id] = ubar;
     f.Vbar[id] = vbar;
-    const T H = eta * g3 + f.Depth[id];
+    const T H = eta * g3 + ro(f.Depth + (id));
     f.H[id] = H;
     if (!g.dispersion) return;
 
@@ -1020,29 +1024,29 @@ __global__ void __launch_bounds__(256, sizeof(T) == sizeof(float) ? 4 : 3) k_upd
     if constexpr (sizeof(T) == sizeof(double)) {
         const double mdf = g.min_depth_frc;
         const double g1 = g.gamma1, b1 = g.b1, b2 = g.b2;
-        const double m9 = (double)f.MASK9[id];
-        const double mk = (double)f.MASK[id];
-        const double dep = tmax((double)f.Depth[id], mdf);
+        const double m9 = (double)ro(f.MASK9 + (id));
+        const double mk = (double)ro(f.MASK + (id));
+        const double dep = tmax((double)ro(f.Depth + (id)), mdf);
         const double Hm = tmax((double)H, mdf);
         // the cross derivatives CAL_DISPERSION left at the start of the stage
-        const double Vxy = f.Vxy[id], DVxy = f.DVxy[id], Uxy = f.Uxy[id], DUxy = f.DUxy[id];
+        const double Vxy = ro(f.Vxy + (id)), DVxy = ro(f.DVxy + (id)), Uxy = ro(f.Uxy + (id)), DUxy = ro(f.DUxy + (id));
         f.rhs_x[id] = (double)ubar * mk / Hm + g1 * m9 * (-b1 / 2.0 * dep * dep * Vxy - b2 * dep * DVxy);
         f.rhs_y[id] = (double)vbar * mk / Hm + g1 * m9 * (-b1 / 2.0 * dep * dep * Uxy - b2 * dep * DUxy);
     } else {
         // mixed: float arithmetic; the cross derivatives of the stage-start
         // U, V are recomputed here
         const T mf = g.f_min_depth_frc;
-        const T m9 = m2r<T>(f.MASK9[id]), mk = m2r<T>(f.MASK[id]);
-        const T dep = tmax(f.Depth[id], mf);
+        const T m9 = m2r<T>(ro(f.MASK9 + (id))), mk = m2r<T>(ro(f.MASK + (id)));
+        const T dep = tmax(ro(f.Depth + (id)), mf);
         const bool wall = (i == g.ib) || (i == g.ie) || (j == g.jb) || (j == g.je);
         T Vxy = (T)0, DVxy = (T)0, Uxy = (T)0, DUxy = (T)0;
         if (!wall) {
             const T q = g.f_rdxy4 * m9;
 #define XY(F) (((F(1, 1) - F(1, -1)) - (F(-1, 1) - F(-1, -1))) * q)
-#define LV(a, b) (f.V[IDX(i + (a), j + (b))])
-#define LU(a, b) (f.U[IDX(i + (a), j + (b))])
-#define LDV(a, b) (tmax(f.Depth[IDX(i + (a), j + (b))], mf) * LV(a, b))
-#define LDU(a, b) (tmax(f.Depth[IDX(i + (a), j + (b))], mf) * LU(a, b))
+#define LV(a, b) (ro(f.V + (IDX(i + (a), j + (b)))))
+#define LU(a, b) (ro(f.U + (IDX(i + (a), j + (b)))))
+#define LDV(a, b) (tmax(ro(f.Depth + (IDX(i + (a), j + (b)))), mf) * LV(a, b))
+#define LDU(a, b) (tmax(ro(f.Depth + (IDX(i + (a), j + (b)))), mf) * LU(a, b))
             Vxy = XY(LV);
             DVxy = XY(LDV);
             Uxy = XY(LU);
