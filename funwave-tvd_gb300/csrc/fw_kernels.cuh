@@ -115,9 +115,9 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
     // ETAT from the previous stage's face fluxes (dispersion.F:103-119)
     if (i <= g.Mloc - 2 && j <= g.Nloc - 2) {
         if constexpr (sizeof(T) == sizeof(double))
-            f.ETAT[id] = -(f.P[IDX(i + 1, j)] - f.P[id]) / DX - (f.Q[IDX(i, j + 1)] - f.Q[id]) / DY;
+            f.ETAT[id] = -(ro(f.P + (IDX(i + 1, j))) - ro(f.P + (id))) / DX - (ro(f.Q + (IDX(i, j + 1))) - ro(f.Q + (id))) / DY;
         else
-            f.ETAT[id] = -(f.P[IDX(i + 1, j)] - f.P[id]) * GC(rdx) - (f.Q[IDX(i, j + 1)] - f.Q[id]) * GC(rdy);
+            f.ETAT[id] = -(ro(f.P + (IDX(i + 1, j))) - ro(f.P + (id))) * GC(rdx) - (ro(f.Q + (IDX(i, j + 1))) - ro(f.Q + (id))) * GC(rdy);
     }
 
     const bool gx = (i < g.ib) || (i > g.ie);
@@ -137,12 +137,12 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
     }
     const T sx2 = gx ? (T)-1 : (T)1;  // sign of VTYPE 2 fields in an x ghost
 
-    const T m9 = m2r<T>(f.MASK9[IDX(si, sj)]);
+    const T m9 = m2r<T>(ro(f.MASK9 + (IDX(si, sj))));
     const bool wall = (si == g.ib) || (si == g.ie) || (sj == g.jb) || (sj == g.je);
-#define LU(a, b) f.U[IDX(si + (a), sj + (b))]
-#define LV(a, b) f.V[IDX(si + (a), sj + (b))]
-#define LDU(a, b) (tmax(f.Depth[IDX(si + (a), sj + (b))], mdf) * LU(a, b))
-#define LDV(a, b) (tmax(f.Depth[IDX(si + (a), sj + (b))], mdf) * LV(a, b))
+#define LU(a, b) ro(f.U + (IDX(si + (a), sj + (b))))
+#define LV(a, b) ro(f.V + (IDX(si + (a), sj + (b))))
+#define LDU(a, b) (tmax(ro(f.Depth + (IDX(si + (a), sj + (b)))), mdf) * LU(a, b))
+#define LDV(a, b) (tmax(ro(f.Depth + (IDX(si + (a), sj + (b)))), mdf) * LV(a, b))
     // FP64: the reference's divisions; mixed: reciprocal constants
     constexpr bool EXACT = sizeof(T) == sizeof(double);
     const T rdx2 = (T)g.f_rdx2, rdy2 = (T)g.f_rdy2, rdxy4 = (T)g.f_rdxy4;
@@ -185,8 +185,8 @@ __global__ void __launch_bounds__(256) k_disp_a(Grid g, Fields<T> f) {
     // (bc.F:395-398); without Gamma2 the ghosts keep their old values
     const bool exch = g.has_g2 != 0;
     if (exch || (g.show_breaking && !gx && !gy)) {
-        const T dex = f.Eta[IDX(si + 1, sj)] - f.Eta[IDX(si - 1, sj)];
-        const T dey = f.Eta[IDX(si, sj + 1)] - f.Eta[IDX(si, sj - 1)];
+        const T dex = ro(f.Eta + (IDX(si + 1, sj))) - ro(f.Eta + (IDX(si - 1, sj)));
+        const T dey = ro(f.Eta + (IDX(si, sj + 1))) - ro(f.Eta + (IDX(si, sj - 1)));
         const T ex = EXACT ? dex / DX / (T)2 * m9 : dex * (T)g.f_hdx * m9;
         const T ey = EXACT ? dey / DY / (T)2 * m9 : dey * (T)g.f_hdy * m9;
         if (!stale) {
@@ -507,13 +507,13 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
             const int o0 = ci + cj * g.pitch - 2 * stride;
             int m[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) m[q] = f.MASK[o0 + q * stride];
+            for (int q = 0; q < 4; q++) m[q] = ro(f.MASK + (o0 + q * stride));
 #pragma unroll
             for (int vv = 0; vv < 7; vv++) {
                 if (vv < nvar) {
                     T v[4];
 #pragma unroll
-                    for (int q = 0; q < 4; q++) v[q] = src[vv][o0 + q * stride];
+                    for (int q = 0; q < 4; q++) v[q] = ro(src[vv] + (o0 + q * stride));
                     din[vv][ln][k] = ho_din(v, m);
                 }
             }
@@ -542,17 +542,17 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
             Rv[vv] = (T)0;
             continue;
         }
-        ho_lr(src[vv][cm], src[vv][fid], din[vv][line][kf - 1], din[vv][line][kf], din[vv][line][kf + 1], Lv[vv],
+        ho_lr(ro(src[vv] + (cm)), ro(src[vv] + (fid)), din[vv][line][kf - 1], din[vv][line][kf], din[vv][line][kf + 1], Lv[vv],
               Rv[vv]);
     }
     const T UL = Lv[0], UR = Rv[0], VL = Lv[1], VR = Rv[1], HUL = Lv[2], HUR = Rv[2];
     const T HVL = Lv[3], HVR = Rv[3], EL = Lv[4], ER = Rv[4];
     const T U4L = Lv[5], U4R = Rv[5], V4L = Lv[6], V4R = Rv[6];
-    const T Dd = DIR == 0 ? f.Depthx[fid] : f.Depthy[fid];
+    const T Dd = DIR == 0 ? ro(f.Depthx + (fid)) : ro(f.Depthy + (fid));
     const T HL = EL + Dd, HR = ER + Dd;
     // MASK9u(Mloc1,:) = MASK9(Mloc,:) (fluxes.F:1333); the faces computed
     // here never reach that column
-    const T m9 = m2r<T>(f.MASK9[fid]);
+    const T m9 = m2r<T>(ro(f.MASK9 + (fid)));
     const T nL = DIR == 0 ? UL : VL, nR = DIR == 0 ? UR : VR;
     const T tL = DIR == 0 ? VL : UL, tR = DIR == 0 ? VR : UR;
     const T n4L = DIR == 0 ? U4L : V4L, n4R = DIR == 0 ? U4R : V4R;
@@ -595,7 +595,7 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
         Nm = press(EL, Dd, g3);
         Tm = (T)0;
     }
-    const int mL = f.MASK[cm], mR = f.MASK[fid];  // cells pos-1 and pos
+    const int mL = ro(f.MASK + (cm)), mR = ro(f.MASK + (fid));  // cells pos-1 and pos
     if (mL < 1) {
         Pm = (T)0;
         Nm = (pos - 1 != hi) ? press(ER, Dd, g3) * m2r<T>(mR) : (T)0;
@@ -725,11 +725,11 @@ __global__ void __launch_bounds__(256) k_flux_tma(Grid g, Fields<T> f, const __g
     const T UL = Lv[0], UR = Rv[0], VL = Lv[1], VR = Rv[1], HUL = Lv[2], HUR = Rv[2];
     const T HVL = Lv[3], HVR = Rv[3], EL = Lv[4], ER = Rv[4];
     const T U4L = Lv[5], U4R = Rv[5], V4L = Lv[6], V4R = Rv[6];
-    const T Dd = DIR == 0 ? f.Depthx[fid] : f.Depthy[fid];
+    const T Dd = DIR == 0 ? ro(f.Depthx + (fid)) : ro(f.Depthy + (fid));
     const T HL = EL + Dd, HR = ER + Dd;
     // MASK9u(Mloc1,:) = MASK9(Mloc,:) (fluxes.F:1333); the faces computed
     // here never reach that column
-    const T m9 = m2r<T>(f.MASK9[fid]);
+    const T m9 = m2r<T>(ro(f.MASK9 + (fid)));
     const T nL = DIR == 0 ? UL : VL, nR = DIR == 0 ? UR : VR;
     const T tL = DIR == 0 ? VL : UL, tR = DIR == 0 ? VR : UR;
     const T n4L = DIR == 0 ? U4L : V4L, n4R = DIR == 0 ? U4R : V4R;
@@ -2102,11 +2102,11 @@ __device__ __forceinline__ void post_cell(const Grid &g, const Fields<T> &f, int
     const bool interior = !(i < g.ib || i > g.ie || j < g.jb || j > g.je);
     if (interior) {
         if (!g.dispersion) {
-            const T Hm = tmax(f.H[id], mdf);
+            const T Hm = tmax(ro(f.H + (id)), mdf);
             f.U[id] = f.Ubar[id] / Hm;
             f.V[id] = f.Vbar[id] / Hm;
         }
-        if (f.MASK[id] < 1) {
+        if (ro(f.MASK + (id)) < 1) {
             f.Ubar[id] = (T)0;
             f.Vbar[id] = (T)0;
             f.U[id] = (T)0;
@@ -2114,7 +2114,7 @@ __device__ __forceinline__ void post_cell(const Grid &g, const Fields<T> &f, int
             f.HU[id] = (T)0;
             f.HV[id] = (T)0;
         } else {
-            const T Hm = tmax(f.H[id], mdf);
+            const T Hm = tmax(ro(f.H + (id)), mdf);
             const T u = f.U[id], v = f.V[id];
             f.HU[id] = Hm * u;
             f.HV[id] = Hm * v;
@@ -2164,21 +2164,21 @@ __device__ __forceinline__ bool in_mask_range(const Grid &g, int a, int b) {
 template <typename T>
 __device__ __forceinline__ int new_mask(const Grid &g, const Fields<T> &f, int a, int b) {
     const size_t q = IDX(a, b);
-    const int m = f.MASK[q];
-    if (!in_mask_range<T>(g, a, b) || f.MASK_STRUC[q] != 1) return m;
+    const int m = ro(f.MASK + (q));
+    if (!in_mask_range<T>(g, a, b) || ro(f.MASK_STRUC + (q)) != 1) return m;
     // total-depth tests: comparing the stored values in T is exact (a
     // float widened to double compares the same), so no FP64 work is needed
-    const T eta = f.Eta[q];
+    const T eta = ro(f.Eta + (q));
     if (m < 1) {
         int r = m;
-        if (eta > -f.Depth[q]) r = 1;
-        if (f.MASK[IDX(a - 1, b)] == 1 && f.Eta[IDX(a - 1, b)] > eta) r = 1;
-        if (f.MASK[IDX(a + 1, b)] == 1 && f.Eta[IDX(a + 1, b)] > eta) r = 1;
-        if (f.MASK[IDX(a, b - 1)] == 1 && f.Eta[IDX(a, b - 1)] > eta) r = 1;
-        if (f.MASK[IDX(a, b + 1)] == 1 && f.Eta[IDX(a, b + 1)] > eta) r = 1;
+        if (eta > -ro(f.Depth + (q))) r = 1;
+        if (ro(f.MASK + (IDX(a - 1, b))) == 1 && ro(f.Eta + (IDX(a - 1, b))) > eta) r = 1;
+        if (ro(f.MASK + (IDX(a + 1, b))) == 1 && ro(f.Eta + (IDX(a + 1, b))) > eta) r = 1;
+        if (ro(f.MASK + (IDX(a, b - 1))) == 1 && ro(f.Eta + (IDX(a, b - 1))) > eta) r = 1;
+        if (ro(f.MASK + (IDX(a, b + 1))) == 1 && ro(f.Eta + (IDX(a, b + 1))) > eta) r = 1;
         return r;
     }
-    return (eta < -f.Depth[q]) ? 0 : m;
+    return (eta < -ro(f.Depth + (q))) ? 0 : m;
 }
 
 // one thread of UPDATE_MASK at (i, j) in 0..Mloc x 0..Nloc
@@ -2188,15 +2188,15 @@ __device__ __forceinline__ void mask_cell(const Grid &g, const Fields<T> &f, int
     if (j < g.Nloc && j >= g.jb - 2 && j <= g.je + 2) {
         const bool rin = (i >= g.ib - 2 && i <= g.ie + 2);
         const bool lin = (i - 1 >= g.ib - 2 && i - 1 <= g.ie + 2);
-        if (rin && f.MASK[IDX(i, j)] < 1) f.Depthx[IDX(i, j)] = f.Depth[IDX(i - 1, j)];
-        else if (lin && f.MASK[IDX(i - 1, j)] < 1) f.Depthx[IDX(i, j)] = f.Depth[IDX(i, j)];
+        if (rin && ro(f.MASK + (IDX(i, j))) < 1) f.Depthx[IDX(i, j)] = ro(f.Depth + (IDX(i - 1, j)));
+        else if (lin && ro(f.MASK + (IDX(i - 1, j))) < 1) f.Depthx[IDX(i, j)] = ro(f.Depth + (IDX(i, j)));
     }
     // Depthy at y-face j of column i
     if (i < g.Mloc && i >= g.ib - 2 && i <= g.ie + 2) {
         const bool tin = (j >= g.jb - 2 && j <= g.je + 2);
         const bool bin = (j - 1 >= g.jb - 2 && j - 1 <= g.je + 2);
-        if (tin && f.MASK[IDX(i, j)] < 1) f.Depthy[IDX(i, j)] = f.Depth[IDX(i, j - 1)];
-        else if (bin && f.MASK[IDX(i, j - 1)] < 1) f.Depthy[IDX(i, j)] = f.Depth[IDX(i, j)];
+        if (tin && ro(f.MASK + (IDX(i, j))) < 1) f.Depthy[IDX(i, j)] = ro(f.Depth + (IDX(i, j - 1)));
+        else if (bin && ro(f.MASK + (IDX(i, j - 1))) < 1) f.Depthy[IDX(i, j)] = ro(f.Depth + (IDX(i, j)));
     }
     if (i >= g.Mloc || j >= g.Nloc) return;
     const size_t id = IDX(i, j);
@@ -2211,7 +2211,7 @@ __device__ __forceinline__ void mask_cell(const Grid &g, const Fields<T> &f, int
             int p = 1;
             for (int b = -1; b <= 1; b++)
                 for (int a = -1; a <= 1; a++) p *= new_mask(g, f, i + a, j + b);
-            if (fabs_(f.Eta[id]) / tmax(f.Depth[id], GC(min_depth_frc)) > GC(swe_eta_dep)) p = 0;
+            if (fabs_(ro(f.Eta + (id))) / tmax(ro(f.Depth + (id)), GC(min_depth_frc)) > GC(swe_eta_dep)) p = 0;
             m9 = (uint8_t)p;
         }
     }
@@ -2236,10 +2236,10 @@ template <typename T> struct BrkLocal {
 template <typename T>
 __device__ __forceinline__ BrkLocal<T> brk_local(const Grid &g, const Fields<T> &f, size_t id) {
     BrkLocal<T> b;
-    b.tmp3 = fsqrt((T)GRAV * tmax(GC(min_depth_frc), f.H[id]));
+    b.tmp3 = fsqrt((T)GRAV * tmax(GC(min_depth_frc), ro(f.H + (id))));
     b.tmp1 = GC(cbrk1) * b.tmp3;
     b.tmp2 = GC(cbrk2) * b.tmp3;
-    b.et = f.ETAT[id];
+    b.et = ro(f.ETAT + (id));
     return b;
 }
 template <typename T>
@@ -2253,13 +2253,13 @@ __device__ __forceinline__ T nu_value(const Grid &g, const Fields<T> &f, size_t 
     const T mdf = GC(min_depth_frc);
     if (zone) {
         if (b.et > tmin(b.tmp2, GC(wavemaker_cbrk) * b.tmp3)) {
-            const T cap1 = (T)1 * (tmax(f.Depth[id], mdf) + f.Eta[id]);
+            const T cap1 = (T)1 * (tmax(ro(f.Depth + (id)), mdf) + ro(f.Eta + (id)));
             return cap1 * GC(wavemaker_cbrk) * b.tmp3 + GC(nu_bkg);
         }
         return (T)0 + GC(nu_bkg);
     }
     if (age > (T)0 && age < GC(T_brk) && b.et > b.tmp2) {
-        const T cap1 = (T)1 * (tmax(f.Depth[id], mdf) + f.Eta[id]);
+        const T cap1 = (T)1 * (tmax(ro(f.Depth + (id)), mdf) + ro(f.Eta + (id)));
         return cap1 * b.tmp2 + GC(nu_bkg);
     }
     return (T)0 + GC(nu_bkg);
@@ -2273,15 +2273,15 @@ __device__ __forceinline__ T nu_value(const Grid &g, const Fields<T> &f, size_t 
 // until a mean is computed.
 template <typename T>
 __device__ __forceinline__ void roller_cell(const Grid &g, const Fields<T> &f, size_t id, T et) {
-    const T ex = f.ETAx[id], ey = f.ETAy[id];
+    const T ex = ro(f.ETAx + (id)), ey = ro(f.ETAy + (id));
     const T tmp4 = tmax(fsqrt(ex * ex + ey * ey), (T)SMALL);
     const T ANGLE = fatan2(-ey, -ex) * (T)180 / (T)PI_SP;
-    const T C1 = tmax(fabs_(et) / tmp4, fsqrt((T)GRAV * fabs_(f.H[id])));
+    const T C1 = tmax(fabs_(et) / tmp4, fsqrt((T)GRAV * fabs_(ro(f.H + (id)))));
     T R = fabs_((T)(double)0.45f * et / tmax(C1, (T)SMALL));
     R = tmin(R, (T)(double)0.1638f);
     const T u = f.U[id], v = f.V[id];
     const T em = g.stats ? f.ETAmean[id] : (T)0;
-    const T rf = fabs_(C1 - fsqrt(u * u + v * v)) * R * (f.Eta[id] - em);
+    const T rf = fabs_(C1 - fsqrt(u * u + v * v)) * R * (ro(f.Eta + (id)) - em);
     f.ROLLER[id] = rf;
     f.UNDERTOW_U[id] = -rf * fcos(ANGLE * (T)PI_SP / (T)180);
     f.UNDERTOW_V[id] = -rf * fsin(ANGLE * (T)PI_SP / (T)180);
@@ -2295,7 +2295,7 @@ template <typename T> __device__ __forceinline__ bool breaking_now(const Grid &g
 template <typename T>
 __device__ __forceinline__ void break_cell(const Grid &g, const Fields<T> &f, int i, int j) {
     const size_t id = IDX(i, j);
-    const T age = f.AGE[id];
+    const T age = ro(f.AGE + (id));
     if (i < g.ib - 1 || i > g.ie + 1 || j < g.jb - 1 || j > g.je + 1) {
         f.AGEn[id] = age;
         return;
@@ -2354,11 +2354,11 @@ template <typename T>
 __device__ __forceinline__ bool brk_neigh(const Grid &g, const Fields<T> &f, const volatile T *N, int i, int j,
                                           T DT) {
     const size_t id = IDX(i, j);
-    const T ex = f.ETAx[id], ey = f.ETAy[id];
+    const T ex = ro(f.ETAx + (id)), ey = ro(f.ETAy + (id));
     const T ANGLE = fatan2(-ey, -ex) * (T)180 / (T)PI_SP;
     const T tmp4 = tmax(fsqrt(ex * ex + ey * ey), (T)SMALL);
-    const T Hc = f.H[id];
-    const T C = tmin(fabs_(f.ETAT[id]) / tmp4, fsqrt((T)GRAV * fabs_(Hc)));
+    const T Hc = ro(f.H + (id));
+    const T C = tmin(fabs_(ro(f.ETAT + (id))) / tmp4, fsqrt((T)GRAV * fabs_(Hc)));
     const T DX = GC(DX), DY = GC(DY);
     const T propxy = fsqrt(DX * DX + DY * DY) / tmax(C, (T)SMALL);
     const T propx = fsqrt(DX * DX) / tmax(C, (T)SMALL);
