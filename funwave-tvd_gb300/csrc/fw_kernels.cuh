@@ -2591,14 +2591,17 @@ __global__ void __launch_bounds__(256) k_maskmul(Grid g, Fields<T> f, int sponge
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mloc || j >= g.Nloc) return;
     const size_t id = IDX(i, j);
+    // every load before the first store (see k_begin)
     const uint8_t mi = f.MASK[id];
     const T m = m2r<T>(mi);
-    T u = f.U[id] * m, v = f.V[id] * m;
-    f.HU[id] = f.HU[id] * m;
-    f.HV[id] = f.HV[id] * m;
+    const T u0 = f.U[id], v0 = f.V[id], hu = f.HU[id], hv = f.HV[id];
+    const T s = sponge ? f.SPONGE[id] : (T)1;
+    const T eta = (sponge && mi > 0) ? f.Eta[id] : (T)0;
+    T u = u0 * m, v = v0 * m;
+    f.HU[id] = hu * m;
+    f.HV[id] = hv * m;
     if (sponge) {
-        const T s = f.SPONGE[id];
-        if (mi > 0) f.Eta[id] = f.Eta[id] / s;
+        if (mi > 0) f.Eta[id] = eta / s;
         u = u / s;
         v = v / s;
     }
@@ -2624,15 +2627,19 @@ __global__ void k_sponge(Grid g, Fields<T> f) {
 // TIME on the device.  Positive doubles order like their bit patterns.
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ __forceinline__ T dt_cell(const Grid &g, const Fields<T> &f, size_t id) {
-    const T c = fsqrt((T)GRAV * tmax(f.H[id], GC(min_depth_frc)));
-    T t1 = fabs_(f.U[id]) + c;
+__device__ __forceinline__ T dt_val(const Grid &g, T H, T U, T V) {
+    const T c = fsqrt((T)GRAV * tmax(H, GC(min_depth_frc)));
+    T t1 = fabs_(U) + c;
     T t2 = (t1 < (T)SMALL) ? GC(DX) / (T)SMALL : GC(DX) / t1;
     T m = t2;
-    t1 = fabs_(f.V[id]) + c;
+    t1 = fabs_(V) + c;
     t2 = (t1 < (T)SMALL) ? GC(DY) / (T)SMALL : GC(DY) / t1;
     if (t2 < m) m = t2;
     return m;
+}
+template <typename T>
+__device__ __forceinline__ T dt_cell(const Grid &g, const Fields<T> &f, size_t id) {
+    return dt_val(g, f.H[id], f.U[id], f.V[id]);
 }
 
 __device__ __forceinline__ double tminr(double a, double b) { return fmin(a, b); }
@@ -2689,18 +2696,24 @@ __global__ void __launch_bounds__(256) k_begin(Grid g, Fields<T> f) {
     T v = (T)1.0e30;
     if (i < g.Mloc && j < g.Nloc) {
         const size_t id = IDX(i, j);
+        // every load before the first store: the copies' sources and
+        // destinations are different arrays, which the compiler cannot know
+        const bool in = i >= g.ib && i <= g.ie && j >= g.jb && j <= g.je;
         const T m = m2r<T>(f.MASK[id]);
-        const T u = f.U[id] * m, vv = f.V[id] * m;
+        const T u0 = f.U[id], v0 = f.V[id], hu = f.HU[id], hv = f.HV[id];
+        const T ub = f.Ubar[id], vb = f.Vbar[id], h = f.H[id];
+        const T eta = in ? f.Eta[id] : (T)0;
+        const T u = u0 * m, vv = v0 * m;
         f.U[id] = u;
         f.V[id] = vv;
-        f.HU[id] = f.HU[id] * m;
-        f.HV[id] = f.HV[id] * m;
-        if (i >= g.ib && i <= g.ie && j >= g.jb && j <= g.je) f.Eta0[id] = f.Eta[id];
-        f.Ubar0[id] = f.Ubar[id];
-        f.Vbar0[id] = f.Vbar[id];
+        f.HU[id] = hu * m;
+        f.HV[id] = hv * m;
+        if (in) f.Eta0[id] = eta;
+        f.Ubar0[id] = ub;
+        f.Vbar0[id] = vb;
         f.U0[id] = u;
         f.V0[id] = vv;
-        v = dt_cell(g, f, id);
+        v = dt_val(g, h, u, vv);
     }
     block_min_to_global(v, f.dtmin_bits);
 }
