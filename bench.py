@@ -69,7 +69,7 @@ KERNEL_BYTES = {
 # profiles/launches_mixed_step_2048.md for the command and the per-launch
 # numbers
 TRAFFIC_PER_UNIT_MIXED = {
-    "tri_x": 48.6, "update": 137.0, "flux_x": 41.0, "flux_y": 41.6, "disp_b": 72.6, "disp_a": 42.7,
+    "tri_x": 49.4, "update": 137.4, "flux_x": 41.0, "flux_y": 41.6, "disp_b": 72.6, "disp_a": 42.7,
     "maskmul": 30.8, "tri_y": 95.2, "post_mask_break": 42.5,
 }
 # kernel launches per stage (tri_* count the partitioned solve as one)
