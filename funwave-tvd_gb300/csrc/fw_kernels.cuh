@@ -656,7 +656,6 @@ __global__ void __launch_bounds__(256) k_flux_tma(Grid g, Fields<T> f, const __g
     const int lo = DIR == 0 ? g.ib : g.jb, hi = DIR == 0 ? g.ie : g.je;
     const int base = (DIR == 0 ? i0 : j0) - 1;
     const int nvar = g.dispersion ? 7 : 5;
-    const int stride = DIR == 0 ? 1 : g.pitch;
     if (tid == 0) {
         fwtc::mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -707,7 +706,6 @@ __global__ void __launch_bounds__(256) k_flux_tma(Grid g, Fields<T> f, const __g
     const int own = DIR == 0 ? tx : ty + r * BY;
     const int line = DIR == 0 ? ty + r * BY : tx;
     const int fid = i + j * g.pitch;
-    const int cm = fid - stride;  // cell pos-1 (cell pos is fid)
     const int kf = own + 1;
     T Lv[7], Rv[7];
 #pragma unroll
