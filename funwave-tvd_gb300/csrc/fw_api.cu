@@ -534,6 +534,13 @@ int fw_create(const fw_params *p, fw_ctx **out) {
         (p->precision != FW_PREC_FP64 && p->precision != FW_PREC_MIXED) ||
         (p->wavemaker < FW_WK_NONE || p->wavemaker > FW_WK_JON_2D) || !(p->min_depth_frc > 0))
         return FW_ERR_BAD_PARAM;
+    {
+        // the kernels index a plane with 32-bit offsets: a plane (padded
+        // rows of Mloc+1 cells, Nloc+1 rows) must hold fewer than 2^31
+        // elements
+        const long long pitch = ((long long)p->Mglob + 2 * NG + 1 + 31) / 32 * 32;
+        if (pitch * ((long long)p->Nglob + 2 * NG + 1) >= (1ll << 31)) return FW_ERR_UNSUPPORTED;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p->device) {
         cudaGetLastError();

@@ -106,7 +106,10 @@ typedef struct fw_ctx fw_ctx;
 void fw_params_default(fw_params *p);
 
 /* Create a context and allocate its device state (no kernel runs yet).
- * Replaces ALLOCATE_VARIABLES (init.F:54-269) and INDEX (misc.F:54-178). */
+ * Replaces ALLOCATE_VARIABLES (init.F:54-269) and INDEX (misc.F:54-178).
+ * FW_ERR_UNSUPPORTED for a grid whose padded field plane, (Mglob+7 rounded
+ * up to 32) x (Nglob+7) cells, would reach 2^31 elements (the kernels use
+ * 32-bit offsets within a plane); FW_ERR_OOM when the state does not fit. */
 int fw_create(const fw_params *p, fw_ctx **out);
 int fw_destroy(fw_ctx *ctx);
 

@@ -80,3 +80,16 @@ def test_output_switches_under_their_input_keys(fw):
     s = params_struct(p)
     assert s.track_hmax == 1 and s.track_mfmax == 1 and s.track_hmin == 0 and s.track_radiation == 1
     assert params_struct(fw.read_input_txt("Mglob = 8\nNglob = 8\nDX = 1.0\nDY = 1.0\n")).track_radiation == 0
+
+
+def test_create_refuses_planes_beyond_32_bit_offsets(fw):
+    """A grid whose padded plane would hold 2^31 elements or more is refused
+    (FW_ERR_UNSUPPORTED) before any device is touched."""
+    L = fw.load_library()
+    from funwave_tvd_gb300.solver import FwParams
+    p = FwParams()
+    L.fw_params_default(ctypes.byref(p))
+    p.Mglob, p.Nglob, p.DX, p.DY = 2_000_000, 1100, 1.0, 1.0
+    h = ctypes.c_void_p()
+    assert L.fw_create(ctypes.byref(p), ctypes.byref(h)) == -6
+    assert not h.value
