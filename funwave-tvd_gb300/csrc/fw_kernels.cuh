@@ -394,8 +394,11 @@ template <typename T> __device__ __forceinline__ T lim3(T a, T b, T c) {
         const float s = a >= 0.0f ? 1.0f : -1.0f;
         return s * fmaxf(0.0f, fminf(fminf(fabsf(a), 2.0f * s * b), 2.0f * s * c));
     } else {
-        if (a >= (T)0) return tmax((T)0, tmin(tmin(a, (T)2 * b), (T)2 * c));
-        return tmin((T)0, tmax(tmax(a, (T)2 * b), (T)2 * c));
+        // both arms, then a select: each thread gets the value of its arm
+        // (signed zeros included) without the warp splitting on the sign
+        const T pos = tmax((T)0, tmin(tmin(a, (T)2 * b), (T)2 * c));
+        const T neg = tmin((T)0, tmax(tmax(a, (T)2 * b), (T)2 * c));
+        return a >= (T)0 ? pos : neg;
     }
 }
 // Din(p) from v[0..3] = Vin(p-2..p+1), m[0..3] = MASK(p-2..p+1)
