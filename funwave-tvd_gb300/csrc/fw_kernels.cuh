@@ -2344,6 +2344,11 @@ __global__ void __launch_bounds__(256) k_post_mask_break(Grid g, Fields<T> f) {
         prefetch_l1(f.Eta + id);
         prefetch_l1(f.Depth + id);
         prefetch_l1(f.MASK_STRUC + id);
+        // the post part's inputs, which it reads after a branch on MASK
+        prefetch_l1(f.MASK + id);
+        prefetch_l1(f.H + id);
+        prefetch_l1(f.U + id);
+        prefetch_l1(f.V + id);
         post_cell(g, f, i, j);
         break_cell(g, f, i, j);
     }
