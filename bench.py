@@ -65,9 +65,8 @@ KERNEL_BYTES = {
 }
 # DRAM bytes per unit (dram__bytes_read.sum + dram__bytes_write.sum of one
 # ncu capture of the 2048 x 2048 mixed step, per launch / units; the tri_y
-# figure sums the partitioned y-solve kernels of one stage); see
-# profiles/launches_mixed_step_2048.md for the command and the per-launch
-# numbers
+# figure sums the partitioned y-solve kernels of one stage), taken with
+# the launch shapes pinned to the autotuner's choice
 TRAFFIC_PER_UNIT_MIXED = {
     "tri_x": 49.4, "update": 137.4, "flux_x": 41.0, "flux_y": 41.6, "disp_b": 72.6, "disp_a": 42.7,
     "maskmul": 30.8, "tri_y": 95.2, "post_mask_break": 42.5,

@@ -5,7 +5,7 @@
  * of argument-less Fortran subroutines called from the time loop of
  * src/main.F:284-535 on shared MODULE GLOBAL state (src/mod_global.F).  This
  * library replaces that loop body.  A Fortran host binds these functions with
- * ISO_C_BINDING; every entry point takes plain pointers,
+ * ISO_C_BINDING (BIND(C) interfaces, VALUE for the scalars); every entry point takes plain pointers,
  * sizes and a POD parameter block, returns an int status (0 = OK, negative =
  * FW_ERR_*), never exits, aborts or traps, and keeps all solver state
  * resident on one GPU between calls.

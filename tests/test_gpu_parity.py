@@ -223,7 +223,7 @@ def test_mixed_vs_fp64_long_run(fw):
     """The 250 x 500 planar beach for 300 steps (about 21 s of waves):
     mixed precision (float fields, float line solve with one compensated
     refinement step) against the FP64 path, which matches the oracle: eta
-    RMS over wet cells <= 1e-4 m, the benchmark spec's tolerance."""
+    RMS over wet cells <= 1e-4 m, the error the mixed mode is specified to."""
     p, depth, _ = fw.cases.planar_beach(seed=7)
     d64 = fw.Solver(p, precision="FP64")
     d64.init(depth)
