@@ -14,6 +14,7 @@
 // held by every GPU that loads the library until the process exits).  The
 // arithmetic per cell is the one of the context path (k_dt_only and
 // k_dt_final), so both give the same DT bit for bit.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -36,9 +37,22 @@ constexpr int FW_DT_MAX_BLOCKS = 65536;
 // before it reads them, so nothing here has to start at zero.
 static __device__ __align__(256) double fw_dt_scratch[FW_DT_MAX_BLOCKS];
 
-constexpr int MAX_DEVICES = 64;
-double *g_scratch[MAX_DEVICES] = {nullptr};
+// The device address of fw_dt_scratch differs between CUDA contexts: a
+// context that is reset (cudaDeviceReset) or a caller's own non-primary
+// context loads this module again, at another address, and a reset primary
+// context may come back under the same handle.  So the address is cached
+// under the context's unique id (cuCtxGetId: never reused in a process).
+constexpr int MAX_CONTEXTS = 64;
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    double *ptr;
+};
+ScratchSlot g_slots[MAX_CONTEXTS] = {};
+int g_nslots = 0;
 std::mutex g_mutex;
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
 
 // dx / (|u| + sqrt(g max(H, MinDepthFrc))) and the same in y (misc.F:243-262)
 __device__ __forceinline__ double cell_dt(double u, double v, double h, double dx, double dy, double mdf) {
@@ -99,21 +113,88 @@ __global__ void __launch_bounds__(1024) k_dt_reduce(int nblocks, double cfl, dou
     }
 }
 
-// The device address of fw_dt_scratch for the current device, looked up
-// once per device.  Host code must not pass fw_dt_scratch itself to a
-// kernel: on the host that name is only a stand-in for the device array.
-int scratch_for_current_device(double **out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return FW_ERR_NO_DEVICE;
-    if (dev < 0 || dev >= MAX_DEVICES) return FW_ERR_UNSUPPORTED;
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, fw_dt_scratch) != cudaSuccess || !p) return FW_ERR_CUDA;
-        g_scratch[dev] = (double *)p;
+// cuCtxGetCurrent and cuCtxGetId through the runtime's driver entry point
+// (the library does not link libcuda).
+template <typename F>
+F driver_fn(const char *name) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+        cudaGetLastError();
+        return nullptr;
     }
-    *out = g_scratch[dev];
+    return (F)p;
+}
+
+// The id of the context current on this thread; 0 when there is none.
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        get = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent");
+        get_id = driver_fn<CtxGetIdFn>("cuCtxGetId");
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get || !get_id || get(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// The device address of fw_dt_scratch in the current context, looked up
+// with cudaGetSymbolAddress once per context (in the usual case one per
+// device: the device's primary context).  Host code must not pass
+// fw_dt_scratch itself to a kernel: on the host that name is only a
+// stand-in for the device array.
+int scratch_for_current_context(double **out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return FW_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> lock(g_mutex);
+    unsigned long long id = current_context_id();
+    if (id) {
+        for (int k = 0; k < g_nslots; k++)
+            if (g_slots[k].ctx_id == id) {
+                *out = g_slots[k].ptr;
+                return FW_OK;
+            }
+    }
+    // The lookup binds the device's primary context to this thread when no
+    // context was current, so the id is read again after it.
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, fw_dt_scratch) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return FW_ERR_CUDA;
+    }
+    if (!id) id = current_context_id();
+    if (!id) return FW_ERR_CUDA;
+    // a small table: when it is full the oldest entry goes
+    if (g_nslots == MAX_CONTEXTS) {
+        for (int i = 1; i < MAX_CONTEXTS; i++) g_slots[i - 1] = g_slots[i];
+        g_nslots--;
+    }
+    g_slots[g_nslots++] = {id, (double *)p};
+    *out = (double *)p;
     return FW_OK;
+}
+
+// True when ptr is device (or managed) memory that the current device can
+// use as a kernel argument.  Host memory, pinned or not, and memory of
+// another GPU are refused, so a wrong pointer becomes FW_ERR_BAD_PARAM
+// instead of a fault inside the kernel.
+bool on_current_device(const void *ptr, int dev) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeDevice) return a.device == dev;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return false;
 }
 
 }  // namespace
@@ -127,8 +208,13 @@ extern "C" int fw_estimate_dt_device(int Mloc, int Nloc, double DX, double DY, c
     const long long nblocks = (ncell + FW_DT_CELLS_PER_BLOCK - 1) / FW_DT_CELLS_PER_BLOCK;
     if (nblocks > FW_DT_MAX_BLOCKS) return FW_ERR_BAD_PARAM;  // beyond FW_DT_DEVICE_MAX_CELLS
     double *scratch = nullptr;
-    const int st = scratch_for_current_device(&scratch);
+    const int st = scratch_for_current_context(&scratch);
     if (st != FW_OK) return st;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FW_ERR_CUDA;
+    if (!on_current_device(U, dev) || !on_current_device(V, dev) || !on_current_device(H, dev) ||
+        !on_current_device(DT, dev) || (TIME && !on_current_device(TIME, dev)))
+        return FW_ERR_BAD_PARAM;
     cudaStream_t s = (cudaStream_t)stream;
     k_dt_blocks<<<(unsigned)nblocks, DT_THREADS, 0, s>>>(ncell, DX, DY, MinDepthFrc, U, V, H, scratch);
     if (cudaGetLastError() != cudaSuccess) return FW_ERR_CUDA;

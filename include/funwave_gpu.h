@@ -333,25 +333,33 @@ int fw_get_tuning(fw_ctx *ctx, int *tuning);        /* FW_TUNE_LEN ints */
 int fw_set_tuning(fw_ctx *ctx, const int *tuning);
 
 /* --- no device allocation ---------------------------------------------- */
-/* ESTIMATE_DT on device arrays the caller owns, allocating nothing: for
- * callers that cannot call cudaMalloc (device arrays owned by an OpenACC or
- * CUDA Fortran runtime, a fixed memory pool, a loop where allocation is
- * forbidden).  No counterpart in the reference as an entry point; its
- * arguments follow ESTIMATE_DT(M,N,DX,DY,U,V,H,MinDepthFrc,DT,CFL,TIME)
- * (misc.F:216).
+/* The CFL time step of a grid whose velocity and depth arrays the caller
+ * already holds on the GPU, computed without allocating any device memory:
+ * for callers that cannot call cudaMalloc (device arrays owned by an OpenACC
+ * or CUDA Fortran runtime, a fixed memory pool, a loop in which allocation
+ * is forbidden).  It has no counterpart in the reference as an entry point.
+ *   Mloc, Nloc the array extents (every cell, ghost cells included, takes
+ *              part in the minimum)
+ *   DX, DY     grid spacings (> 0)
  *   U, V, H    device pointers to contiguous Mloc x Nloc column-major double
- *              arrays (ghost cells included, as the reference's loop covers
- *              them), on the current CUDA device
- *   dt_fixed   > 0 applies the DT_fixed halving, else 0
- *   DT         device pointer, receives CFL * min(dx/(|u|+c), dy/(|v|+c))
+ *              arrays of the velocities and the total depth, on the current
+ *              CUDA device
+ *   MinDepthFrc  floor of the depth in the wave celerity sqrt(g max(H, .))
+ *   CFL        Courant number (> 0)
+ *   dt_fixed   > 0: the step is dt_fixed halved until it is at most the CFL
+ *              step; 0: the CFL step itself
+ *   DT         device pointer, receives CFL * min(DX/(|U|+c), DY/(|V|+c))
+ *              (or the halved dt_fixed)
  *   TIME       device pointer (or NULL), TIME += DT
  *   stream     cudaStream_t (NULL = legacy default stream)
  * Mloc*Nloc may be at most FW_DT_DEVICE_MAX_CELLS; larger grids get
- * FW_ERR_BAD_PARAM before anything runs.  The call's scratch is one static
- * 512 KB device array per GPU: the first call on a device looks up its
- * address (set-up; make that first call before any stream capture), and
- * calls whose work overlaps on the GPU race on that array.  Asynchronous on
- * stream; DT and TIME are valid once the stream reaches that point. */
+ * FW_ERR_BAD_PARAM before anything runs, and so do pointers that are not
+ * device (or managed) memory of the current device.  The call's scratch is
+ * one static 512 KB device array per GPU: the first call in a CUDA context
+ * looks up its address (set-up; make that first call before any stream
+ * capture), and calls whose work overlaps on the GPU race on that array.
+ * Asynchronous on stream; DT and TIME are valid once the stream reaches
+ * that point. */
 #define FW_DT_DEVICE_MAX_CELLS 134217728LL   /* 65536 blocks x 2048 cells */
 int fw_estimate_dt_device(int Mloc, int Nloc, double DX, double DY, const double *U, const double *V,
                           const double *H, double MinDepthFrc, double CFL, double dt_fixed, double *DT,
