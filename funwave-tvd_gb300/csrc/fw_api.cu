@@ -31,7 +31,8 @@ const char *kErrText[] = {"ok",
                           "option not supported by this build",
                           "call out of order (context not initialised)",
                           "no usable CUDA device",
-                          "checkpoint file unreadable, unwritable or malformed"};
+                          "checkpoint file unreadable, unwritable or malformed",
+                          "a bounded device wait ran out"};
 
 int cuda_status(fw_ctx *c, cudaError_t e) {
     if (e == cudaSuccess && c && c->sticky_error == 0) return FW_OK;
@@ -523,7 +524,7 @@ void fw_params_default(fw_params *p) {
 }
 
 const char *fw_strerror(int s) {
-    if (s > 0 || s < -9) return "unknown status";
+    if (s > 0 || s < -10) return "unknown status";
     return kErrText[-s];
 }
 
@@ -854,6 +855,7 @@ int fw_get_scalar(fw_ctx *c, const char *name, double *v) {
     else if (!std::strcmp(name, "jlo")) *v = c->g.jlo + 1;
     else if (!std::strcmp(name, "jhi")) *v = c->g.jhi + 1;
     else if (!std::strcmp(name, "pitch")) *v = c->g.pitch;
+    else if (!std::strcmp(name, "WAIT_LIMIT")) *v = c->fmaps[0][0][0].wait_limit;
     else return FW_ERR_BAD_PARAM;
     return FW_OK;
 }
@@ -867,7 +869,12 @@ int fw_set_scalar(fw_ctx *c, const char *name, double v) {
         return cuda_status(c, e);
     }
     if (!std::strcmp(name, "EtaBlowVal")) c->EtaBlowVal = v;
-    else if (!std::strcmp(name, "T_brk")) {
+    else if (!std::strcmp(name, "WAIT_LIMIT")) {
+        if (!(v >= 0.0 && v <= 4294967295.0)) return FW_ERR_BAD_PARAM;
+        for (auto &by_dir : c->fmaps)
+            for (auto &by_fy : by_dir)
+                for (auto &m : by_fy) m.wait_limit = (unsigned)v;
+    } else if (!std::strcmp(name, "T_brk")) {
         c->g.T_brk = v;
         fill_float_constants(c->g);
     } else return FW_ERR_BAD_PARAM;

@@ -169,6 +169,10 @@ namespace fw {
 // and one of the two MASK buffers
 struct FluxMaps {
     CUtensorMap m[8];
+    // polls of the wait for the staged tile before the block gives up and
+    // writes NaN fluxes (which the step reports); 0 = the default limit.
+    // Set through fw_set_scalar("WAIT_LIMIT").
+    unsigned wait_limit;
 };
 constexpr int FLUX_FY_N = 3;  // tile heights 8, 16, 32
 // kernels whose block shape fw_autotune chooses (per-cell kernels, so any

@@ -670,7 +670,7 @@ __global__ void __launch_bounds__(256) k_flux_tma(Grid g, Fields<T> f, const __g
         for (int v = 0; v < nvar; v++) fwtc::tma_load_2d(fwtc::smem_u32(sm + v * S::FB), &maps.m[v], xs, ysr, bar);
         fwtc::tma_load_2d(fwtc::smem_u32(sm + 7 * S::FB), &maps.m[7], xs, ysr, bar);
     }
-    const bool staged = fwtc::mbar_wait(bar, 0);
+    const bool staged = fwtc::mbar_wait(bar, 0, maps.wait_limit ? maps.wait_limit : fwtc::WAIT_LIMIT);
     // the NTL x NPOS Din positions of the tile, spread over all threads
     for (int it = tid; it < NTL * NPOS; it += BX * BY) {
         const int k = DIR == 0 ? it % NPOS : it / NTL;
@@ -799,8 +799,9 @@ __global__ void __launch_bounds__(256) k_flux_tma(Grid g, Fields<T> f, const __g
     }
     }
     // the tile never arrived: its copies may still be in flight; one more
-    // bounded wait keeps this block's shared memory until they land
-    if (!staged && tid == 0) fwtc::mbar_wait(bar, 0);
+    // bounded wait (the full limit) keeps this block's shared memory until
+    // they land
+    if (!staged && tid == 0) fwtc::mbar_wait(bar, 0, fwtc::WAIT_LIMIT);
 }
 
 #undef FLD

@@ -279,6 +279,7 @@ struct fw_net {
     size_t img_off[NL + 3] = {0};
     unsigned long long wver = 1, img_ver = 0;
     int *status = nullptr;      // set by a tensor-core kernel whose bounded wait expired
+    unsigned wait_limit = fwtc::WAIT_LIMIT;  // polls of those waits (fw_net_set_wait_limit)
     // workspace: FP32 buffers for npix_cap pixels; padded BF16 activations
     // (fwtc::act_idx) of cap16 / cap32 bytes, laid out for the batch shape
     // sB x sH x sW (their zero borders are set when the shape changes)
@@ -396,7 +397,7 @@ bool conv_attrs_all() {
 
 template <int CINC, int N, int EPI, int NOUTF>
 int conv_tc(const bf16 *x, const bf16 *img, const float *bias, const bf16 *act, void *y, int B, int H, int W,
-            int *status, cudaStream_t s) {
+            int *status, unsigned wait_limit, cudaStream_t s) {
     using Lt = fwtc::Layout<CINC, N>;
     auto k = fwtc::k_conv_tc<CINC, N, EPI, NOUTF>;
     if (!conv_attr<CINC, N, EPI, NOUTF>()) return FW_ERR_CUDA;
@@ -410,8 +411,19 @@ int conv_tc(const bf16 *x, const bf16 *img, const float *bias, const bf16 *act, 
     }
     const long long ntiles = (long long)((W + fwtc::TPX - 1) / fwtc::TPX) * ((H + fwtc::TROWS - 1) / fwtc::TROWS) * B;
     const unsigned grid = (unsigned)std::min<long long>(ntiles, (long long)nsm * Lt::PER_SM);
-    k<<<grid, 64 + 32 * fwtc::EPI_WARPS, Lt::BYTES, s>>>(x, img, bias, act, y, H, W, B, status);
+    k<<<grid, 64 + 32 * fwtc::EPI_WARPS, Lt::BYTES, s>>>(x, img, bias, act, y, H, W, B, status,
+                                                                      wait_limit);
     return FW_OK;
+}
+
+// The status word of the tensor-core kernels, read after the stream's work:
+// a bounded wait that ran out becomes FW_ERR_TIMEOUT, and the word is
+// cleared so that the network can be used again.
+int take_status(fw_net *n, int st, cudaStream_t s) {
+    if (st == 0) return FW_OK;
+    if (cudaMemsetAsync(n->status, 0, sizeof(int), s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+        return FW_ERR_CUDA;
+    return FW_ERR_TIMEOUT;
 }
 
 // the tensor-core kernels number their tiles in an int
@@ -437,13 +449,13 @@ int forward(fw_net *n, const float *in, long long npix, int B, int H, int W, cud
     k_pack_input<<<nblk(npix, 256), 256, 0, s>>>(in, n->act[0], B, H, W);
     const bf16 *im = n->img;
     int rc = conv_tc<2, 32, EPI_RELU_BF16, 0>(n->act[0], im + n->img_off[0], n->w + n->boff[0], nullptr,
-                                              n->act[1], B, H, W, n->status, s);
+                                              n->act[1], B, H, W, n->status, n->wait_limit, s);
     for (int l = 1; l < 3 && rc == FW_OK; l++)
         rc = conv_tc<4, 32, EPI_RELU_BF16, 0>(n->act[l], im + n->img_off[l], n->w + n->boff[l], nullptr,
-                                              n->act[l + 1], B, H, W, n->status, s);
+                                              n->act[l + 1], B, H, W, n->status, n->wait_limit, s);
     if (rc == FW_OK)
         rc = conv_tc<4, 16, EPI_LINEAR_F32, NOUT>(n->act[3], im + n->img_off[3], n->w + n->boff[3], nullptr,
-                                                  n->out, B, H, W, n->status, s);
+                                                  n->out, B, H, W, n->status, n->wait_limit, s);
     return rc;
 }
 
@@ -463,11 +475,11 @@ int backward(fw_net *n, int B, int H, int W, cudaStream_t s) {
     wgrad<HID, NOUT, HID / 8, GC3 / 8>(n, 3, n->act[3], n->gout, B, H, W, s);
     // gradient of act[3] (the output of layer 2), masked by its ReLU
     int rc = conv_tc<2, 32, EPI_MASK_BF16, 0>(n->gout, im + n->img_off[NL + 2], nullptr, n->act[3], ga, B, H, W,
-                                              n->status, s);
+                                              n->status, n->wait_limit, s);
     for (int l = 2; l >= 1 && rc == FW_OK; l--) {
         wgrad<HID, HID, HID / 8, HID / 8>(n, l, n->act[l], ga, B, H, W, s);
         rc = conv_tc<4, 32, EPI_MASK_BF16, 0>(ga, im + n->img_off[NL + l - 1], nullptr, n->act[l], gb, B, H, W,
-                                              n->status, s);
+                                              n->status, n->wait_limit, s);
         std::swap(ga, gb);
     }
     if (rc != FW_OK) return rc;
@@ -512,7 +524,8 @@ template <typename T> int correct(fw_ctx *c, fw_net *n, double max_corr, int *ap
         int st = 0;
         cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess || st != 0) return FW_ERR_CUDA;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return FW_ERR_CUDA;
+        if (st != 0) return take_status(n, st, s);
         *applied = (h[3] <= max_corr && h[2] == h[2]) ? 1 : 0;
     }
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
@@ -581,6 +594,17 @@ int fw_net_create(unsigned long long seed, fw_net **out) {
     return FW_OK;
 }
 
+int fw_net_set_wait_limit(fw_net *n, unsigned polls) {
+    if (!n) return FW_ERR_BAD_PARAM;
+    n->wait_limit = polls ? polls : fwtc::WAIT_LIMIT;
+    // fw_correct_run's graph holds the old limit
+    if (n->cexec) {
+        cudaGraphExecDestroy(n->cexec);
+        n->cexec = nullptr;
+    }
+    return FW_OK;
+}
+
 int fw_net_destroy(fw_net *n) {
     if (!n) return FW_ERR_BAD_PARAM;
     cudaDeviceSynchronize();
@@ -642,7 +666,8 @@ int fw_net_loss_grad(fw_net *n, const float *x, const float *target, const float
         int st = 0;
         cudaMemcpyAsync(loss, n->loss, sizeof(double), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess || st != 0) return FW_ERR_CUDA;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return FW_ERR_CUDA;
+        if (st != 0) return take_status(n, st, s);
     }
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
 }
@@ -716,7 +741,8 @@ int fw_correct_run(fw_ctx *c, fw_net *n, int nsteps, double max_corr, int *statu
     if (nsteps % 2 && (rc = pair()) != FW_OK) return rc;
     rc = fw::step_status(c, status);
     int st = 0;
-    if (cudaMemcpy(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess || st != 0) return FW_ERR_CUDA;
+    if (cudaMemcpy(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FW_ERR_CUDA;
+    if (st != 0) return take_status(n, st, c->stream);
     return rc;
 }
 

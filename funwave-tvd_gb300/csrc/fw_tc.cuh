@@ -103,8 +103,13 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
 }
 
 // bounded wait for the phase with the given parity to complete
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (unsigned i = 0; i < WAIT_LIMIT; i++) {
+// limit: polls before giving up.  Waits whose expiry the kernel turns into
+// an error status take the caller's limit (a run-time setting, so that a
+// test can make them run out); the waits that drain a block's own copies
+// and MMAs before it frees its shared memory and TMEM always take
+// WAIT_LIMIT.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned limit = WAIT_LIMIT) {
+    for (unsigned i = 0; i < limit; i++) {
         uint32_t done;
         asm volatile(
             "{\n.reg .pred p;\n"
@@ -204,8 +209,9 @@ __device__ __forceinline__ float hi_bf(uint32_t w) { return __uint_as_float(w & 
 // else 0, padded with 4 chunks (act: padded, 4 chunks).  status: set to
 // 1 (an input or accumulator wait expired) or 2 (an MMA wait expired); every
 // role then stops.
-__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile uint32_t *flag) {
-    for (unsigned i = 0; i < WAIT_LIMIT; i++) {
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile uint32_t *flag,
+                                                   unsigned limit) {
+    for (unsigned i = 0; i < limit; i++) {
         uint32_t done;
         asm volatile(
             "{\n.reg .pred p;\n"
@@ -228,7 +234,8 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 template <int CINC, int N, int EPI, int NOUTF>
 __global__ void __launch_bounds__(320, 1) k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wimg,
                                                     const float *__restrict__ bias, const bf16 *__restrict__ act,
-                                                    void *__restrict__ y, int H, int W, int B, int *status) {
+                                                    void *__restrict__ y, int H, int W, int B, int *status,
+                                                    unsigned wait_limit) {
     static_assert(CINC % 2 == 0 && (N == 16 || N == 32), "K steps of 16 channels; N of 16 or 32");
     using L = Layout<CINC, N>;
     extern __shared__ uint8_t smem_raw[];
@@ -282,14 +289,18 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const bf16 *__restrict__ x, 
     uint32_t tmem;
     asm volatile("ld.shared.u32 %0, [%1];" : "=r"(tmem) : "r"(tptr) : "memory");
 
+    // the last tile issued to each input stage (producer lane) and the last
+    // tile whose MMAs were committed (MMA lane): what a block that aborts
+    // must wait for before it frees its shared memory and TMEM
+    int last[NSTAGE];
+#pragma unroll
+    for (int k = 0; k < NSTAGE; k++) last[k] = -1;
+    int committed = -1;
     if (warp == 0) {
         if (lane == 0) {
-            int last[NSTAGE];
-#pragma unroll
-            for (int k = 0; k < NSTAGE; k++) last[k] = -1;
             for (int i = 0; i < ntl; i++) {
                 const int st = i % NSTAGE;
-                if (i >= NSTAGE && !mbar_wait_or_abort(empty_bar(st), (uint32_t)(((i / NSTAGE) - 1) & 1), flag)) {
+                if (i >= NSTAGE && !mbar_wait_or_abort(empty_bar(st), (uint32_t)(((i / NSTAGE) - 1) & 1), flag, wait_limit)) {
                     if (*flag == 0u) fail(1);
                     break;
                 }
@@ -309,24 +320,17 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const bf16 *__restrict__ x, 
                 for (int k = 0; k < NSTAGE; k++)
                     if (k == st) last[k] = i;
             }
-            // after an abort: the loads still in flight (bounded)
-            if (*flag != 0u) {
-#pragma unroll
-                for (int k = 0; k < NSTAGE; k++)
-                    if (last[k] >= 0) mbar_wait(full_bar(k), (uint32_t)((last[k] / NSTAGE) & 1));
-            }
         }
     } else if (warp == 1) {
         if (lane == 0) {
             constexpr uint32_t idesc = idesc_bf16<TPX, N>();
-            int committed = -1;
             for (int i = 0; i < ntl; i++) {
                 const int st = i % NSTAGE, a = i & 1;
-                if (!mbar_wait_or_abort(full_bar(st), (uint32_t)((i / NSTAGE) & 1), flag)) {
+                if (!mbar_wait_or_abort(full_bar(st), (uint32_t)((i / NSTAGE) & 1), flag, wait_limit)) {
                     if (*flag == 0u) fail(1);
                     break;
                 }
-                if (i >= 2 && !mbar_wait_or_abort(acce_bar(a), (uint32_t)(((i >> 1) - 1) & 1), flag)) {
+                if (i >= 2 && !mbar_wait_or_abort(acce_bar(a), (uint32_t)(((i >> 1) - 1) & 1), flag, wait_limit)) {
                     if (*flag == 0u) fail(1);
                     break;
                 }
@@ -355,8 +359,6 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const bf16 *__restrict__ x, 
                 tc_commit(accf_bar(a));
                 committed = i;
             }
-            // after an abort: the MMAs in flight, before TMEM is freed (bounded)
-            if (*flag != 0u && committed >= 0) mbar_wait(accf_bar(committed & 1), (uint32_t)((committed >> 1) & 1));
         }
     } else {
         const int q = warp & 3;  // TMEM lane quadrant of this warp
@@ -369,7 +371,7 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const bf16 *__restrict__ x, 
         }
         for (int i = 0; i < ntl; i++) {
             const int a = i & 1;
-            if (!mbar_wait_or_abort(accf_bar(a), (uint32_t)((i >> 1) & 1), flag)) {
+            if (!mbar_wait_or_abort(accf_bar(a), (uint32_t)((i >> 1) & 1), flag, wait_limit)) {
                 if (*flag == 0u) fail(2);
                 break;
             }
@@ -434,6 +436,23 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const bf16 *__restrict__ x, 
         }
     }
     tc_fence_before();
+    __syncthreads();
+    // Every role has finished or given up, so the abort flag is final here.
+    // After an abort, loads and MMAs may still be in flight (a role can give
+    // up while another has already issued work, and the producer may have
+    // issued its last loads before any role gave up): wait for them
+    // (bounded, with the full limit) before the block frees its TMEM and
+    // its shared memory.
+    if (*flag != 0u) {
+        if (warp == 0 && lane == 0) {
+#pragma unroll
+            for (int k = 0; k < NSTAGE; k++)
+                if (last[k] >= 0) mbar_wait(full_bar(k), (uint32_t)((last[k] / NSTAGE) & 1));
+        }
+        if (warp == 1 && lane == 0 && committed >= 0)
+            mbar_wait(accf_bar(committed & 1), (uint32_t)((committed >> 1) & 1));
+        __syncwarp();
+    }
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();

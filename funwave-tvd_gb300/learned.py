@@ -42,6 +42,7 @@ def _bind(L):
     L.fw_net_forward.argtypes = [vp, vp, ip, ip, ip, vp, vp]
     L.fw_net_loss_grad.argtypes = [vp, vp, vp, vp, ip, ip, ip, ctypes.POINTER(ctypes.c_double), vp]
     L.fw_net_adam.argtypes = [vp, fp, fp, fp, fp, vp]
+    L.fw_net_set_wait_limit.argtypes = [vp, ctypes.c_uint]
     L.fw_correct.argtypes = [vp, vp, ctypes.c_double, ctypes.POINTER(ip)]
     L.fw_correct_run.argtypes = [vp, vp, ip, ctypes.c_double, ctypes.POINTER(ip)]
     return L
@@ -107,6 +108,10 @@ class Net:
         import torch
         s = torch.cuda.current_stream().cuda_stream
         self._ck(self.L.fw_net_adam(self.h, float(lr), float(beta1), float(beta2), float(eps), s), "adam")
+
+    def set_wait_limit(self, polls=0):
+        """Polls of the tensor-core kernels' bounded waits (0 = default)."""
+        self._ck(self.L.fw_net_set_wait_limit(self.h, int(polls)), "set_wait_limit")
 
     def correct(self, solver, max_corr=0.2, wait=True):
         """fw_correct on the solver's current state; with wait, whether the

@@ -38,7 +38,8 @@ _SOURCES = {
 
 FW_ERRORS = {0: "FW_OK", -1: "FW_ERR_CUDA", -2: "FW_ERR_OOM", -3: "FW_ERR_BAD_PARAM",
              -4: "FW_ERR_BLOWUP", -5: "FW_ERR_NAN", -6: "FW_ERR_UNSUPPORTED",
-             -7: "FW_ERR_NOT_READY", -8: "FW_ERR_NO_DEVICE", -9: "FW_ERR_IO"}
+             -7: "FW_ERR_NOT_READY", -8: "FW_ERR_NO_DEVICE", -9: "FW_ERR_IO",
+             -10: "FW_ERR_TIMEOUT"}
 
 
 class FwError(RuntimeError):

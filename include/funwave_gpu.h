@@ -36,6 +36,7 @@ extern "C" {
 #define FW_ERR_NOT_READY   -7   /* call order violated (e.g. step before init) */
 #define FW_ERR_NO_DEVICE   -8   /* no usable CUDA device */
 #define FW_ERR_IO          -9   /* checkpoint file unreadable, unwritable or malformed */
+#define FW_ERR_TIMEOUT     -10  /* a bounded device wait ran out (the kernel gave up and returned) */
 
 /* precision of the bulk arithmetic */
 #define FW_PREC_FP64  0   /* every field and operation in double */
@@ -158,7 +159,13 @@ int fw_get_points(fw_ctx *ctx, const char *name, int n, const int *I, const int 
  * "P_mean","Q_mean","UUmean","UVmean","VVmean","WWmean","FRCXmean",
  * "FRCYmean","BreakDissX","BreakDissY" and the gradient fields "DxSxx",
  * "DySxy","DySyy","DxSxy","PgrdX","PgrdY","DxUUH","DyUVH","DyVVH","DxUVH"
- * (mixing.F:156-219). */
+ * (mixing.F:156-219).
+ * "WAIT_LIMIT" (get and set) is not a reference quantity: the polls of the
+ * bounded wait with which a TMA-staged flux tile waits for its copies
+ * (0 = the default, about 0.3-1 s).  A wait that runs out leaves the
+ * block's fluxes NaN, and the step reports FW_ERR_NAN; the context stays
+ * usable.  Lowering it makes that path run on purpose (a test of failure
+ * reporting).  Setting it drops the captured step graphs. */
 int fw_get_scalar(fw_ctx *ctx, const char *name, double *value);
 int fw_set_scalar(fw_ctx *ctx, const char *name, double value);
 
@@ -227,6 +234,13 @@ int fw_net_forward(fw_net *net, const float *x, int B, int H, int W, float *y, v
 int fw_net_loss_grad(fw_net *net, const float *x, const float *target, const float *wmask, int B, int H,
                      int W, double *loss, void *stream);
 int fw_net_adam(fw_net *net, float lr, float beta1, float beta2, float eps, void *stream);
+/* Polls of the tensor-core kernels' bounded waits (0 = the default, about
+ * 0.3-1 s).  A wait that runs out makes the kernel give up, wait for its
+ * own copies and MMAs, free its TMEM and return; the next call that reads
+ * the status (fw_net_loss_grad with a loss pointer, fw_correct with
+ * applied, fw_correct_run) returns FW_ERR_TIMEOUT and clears it.  Lowering
+ * the limit makes that path run on purpose (a test of failure reporting). */
+int fw_net_set_wait_limit(fw_net *net, unsigned polls);
 /* Apply the network to a context's current state: the eta correction is
  * projected to zero mean over the wet interior cells (so the volume is
  * unchanged), then eta, u, v (and H, HU, HV, Ubar, Vbar to first order) are
