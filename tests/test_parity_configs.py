@@ -49,7 +49,8 @@ def test_planar_beach_full_size_300_steps(fw, oracle_mod):
     s, o = make_pair(fw, oracle_mod, p, depth)
     t = _run_and_compare(s, o, 300, 50)
     assert t > 10.0                                 # ~14 s of model time: waves on the slope
-    assert float(np.abs(interior(s.get("Eta"))).max()) > 0.1
+    # waves from the wavemaker fill the flat part (x < 100 m)
+    assert float(np.abs(interior(s.get("Eta"))[:100]).max()) > 0.05
     s.close()
     o.close()
 
