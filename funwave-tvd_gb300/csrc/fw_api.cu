@@ -465,6 +465,19 @@ double time_named(fw_ctx *c, bool fp64, const char *name, cudaError_t &e) {
     return ms_out;
 }
 
+// Every field and device scalar to zero, the CFL minimum to +inf: the
+// state of a new context, which fw_init also starts from, so that a context
+// initialised again runs like a new one (nothing of an earlier run, such as
+// a NaN in a face flux, survives).
+cudaError_t clear_arena(fw_ctx *c) {
+    cudaError_t e = cudaMemsetAsync(c->arena, 0, c->arena_bytes, c->stream);
+    const unsigned long long inf_bits = 0x7ff0000000000000ull;
+    unsigned long long *dtb = c->p.precision == FW_PREC_FP64 ? c->fd.dtmin_bits : c->ff.dtmin_bits;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dtb, &inf_bits, sizeof(inf_bits), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return e;
+}
+
 int read_status(fw_ctx *c, int *status) {
     unsigned long long bits = 0;
     cudaError_t e = cudaMemcpyAsync(&bits, etamax_ptr(c), sizeof(bits), cudaMemcpyDeviceToHost, c->stream);
@@ -650,11 +663,7 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     // the load-based kernels run
     c->fmaps_ok = (fp64 ? build_flux_maps<double>(c) : build_flux_maps<float>(c)) ? 1 : 0;
     cudaGetLastError();
-    cudaError_t e = cudaMemsetAsync(c->arena, 0, bytes, c->stream);
-    const unsigned long long inf_bits = 0x7ff0000000000000ull;
-    unsigned long long *dtb = fp64 ? c->fd.dtmin_bits : c->ff.dtmin_bits;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dtb, &inf_bits, sizeof(inf_bits), cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaError_t e = clear_arena(c);
     if (e != cudaSuccess) {
         cudaGetLastError();
         fw_destroy(c);
@@ -694,6 +703,8 @@ int fw_init(fw_ctx *c, const double *depth, const double *eta, const double *u, 
     std::string err;
     int rc = build_case(c->p, depth, eta, u, v, phases, hc, err);
     if (rc != FW_OK) return rc;
+    cudaError_t ce = clear_arena(c);
+    if (ce != cudaSuccess) return cuda_status(c, ce);
     Grid &g = c->g;
     g.T_brk = hc.T_brk;
     g.width_wk = hc.Width_WK;
@@ -799,6 +810,49 @@ int fw_get_field(fw_ctx *c, const char *name, void *host) {
 int fw_set_field(fw_ctx *c, const char *name, const void *host) {
     if (!c || !name || !host) return FW_ERR_BAD_PARAM;
     return put_named(c, name, host);
+}
+
+// REAL(SP) host arrays: the mixed build's float fields move with one 2-D
+// copy each way; the FP64 build's go through the staging plane and a
+// conversion kernel.  Masks keep their int32 transfers (fw_get_field).
+int fw_get_field_f32(fw_ctx *c, const char *name, float *host) {
+    if (!c || !name || !host) return FW_ERR_BAD_PARAM;
+    const bool fp64 = c->p.precision == FW_PREC_FP64;
+    FieldRef r;
+    if (!(fp64 ? find_field<double>(c, name, r) : find_field<float>(c, name, r)) || r.is_mask)
+        return FW_ERR_BAD_PARAM;
+    int w, h;
+    extent(c, r.kind, w, h);
+    cudaError_t e;
+    if (fp64) {
+        convert_out_f32(c, (const double *)r.ptr, (float *)c->staging, w, h);
+        e = cudaMemcpyAsync(host, c->staging, (size_t)w * h * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    } else {
+        e = cudaMemcpy2DAsync(host, (size_t)w * sizeof(float), r.ptr, (size_t)c->g.pitch * sizeof(float),
+                              (size_t)w * sizeof(float), (size_t)h, cudaMemcpyDeviceToHost, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return cuda_status(c, e);
+}
+
+int fw_set_field_f32(fw_ctx *c, const char *name, const float *host) {
+    if (!c || !name || !host) return FW_ERR_BAD_PARAM;
+    const bool fp64 = c->p.precision == FW_PREC_FP64;
+    FieldRef r;
+    if (!(fp64 ? find_field<double>(c, name, r) : find_field<float>(c, name, r)) || r.is_mask)
+        return FW_ERR_BAD_PARAM;
+    int w, h;
+    extent(c, r.kind, w, h);
+    cudaError_t e;
+    if (fp64) {
+        e = cudaMemcpyAsync(c->staging, host, (size_t)w * h * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) convert_in_f32(c, (const float *)c->staging, (double *)r.ptr, w, h);
+    } else {
+        e = cudaMemcpy2DAsync(r.ptr, (size_t)c->g.pitch * sizeof(float), host, (size_t)w * sizeof(float),
+                              (size_t)w * sizeof(float), (size_t)h, cudaMemcpyHostToDevice, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return cuda_status(c, e);
 }
 
 int fw_get_points(fw_ctx *c, const char *name, int n, const int *I, const int *J, double *out) {

@@ -157,6 +157,8 @@ template <typename T> bool flux_tma_attrs();  // shared-memory sizes of the TMA-
 // staging buffer <-> field (double <-> float fields, int32 <-> uint8 masks)
 void convert_in(fw_ctx *c, const void *staging, int is_mask, void *field, int w, int h);
 void convert_out(fw_ctx *c, const void *field, int is_mask, void *staging, int w, int h);
+void convert_in_f32(fw_ctx *c, const float *staging, double *field, int w, int h);
+void convert_out_f32(fw_ctx *c, const double *field, float *staging, int w, int h);
 
 }  // namespace fw
 

@@ -3425,6 +3425,19 @@ void convert_out(fw_ctx *c, const void *field, int is_mask, void *staging, int w
     note(c);
 }
 
+// float host arrays (an FP32 host's REAL(SP) fields) of the FP64 build:
+// widened on the way in, rounded to nearest on the way out
+void convert_in_f32(fw_ctx *c, const float *staging, double *field, int w, int h) {
+    const dim3 b(32, 8), gr((w + 31) / 32, (h + 7) / 8);
+    k_unpack<float, double><<<gr, b, 0, c->stream>>>(staging, w, h, field, c->g.pitch);
+    note(c);
+}
+void convert_out_f32(fw_ctx *c, const double *field, float *staging, int w, int h) {
+    const dim3 b(32, 8), gr((w + 31) / 32, (h + 7) / 8);
+    k_pack<double, float><<<gr, b, 0, c->stream>>>(field, c->g.pitch, w, h, staging);
+    note(c);
+}
+
 // values of one field at n cells (pitched offsets) as double; type 0 double,
 // 1 float, 2 uint8 mask
 __global__ void k_gather(const void *field, int type, const int *off, int n, double *out) {

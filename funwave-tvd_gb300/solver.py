@@ -224,6 +224,8 @@ def load_library(path=None):
     L.fw_destroy.argtypes = [vp]
     L.fw_init.argtypes = [vp] + [ctypes.POINTER(dp)] * 5
     L.fw_get_field.argtypes = [vp, ctypes.c_char_p, vp]
+    L.fw_get_field_f32.argtypes = [vp, ctypes.c_char_p, vp]
+    L.fw_set_field_f32.argtypes = [vp, ctypes.c_char_p, vp]
     L.fw_set_field.argtypes = [vp, ctypes.c_char_p, vp]
     L.fw_get_scalar.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(dp)]
     L.fw_set_scalar.argtypes = [vp, ctypes.c_char_p, dp]
@@ -336,6 +338,19 @@ class Solver:
         a = np.zeros(self.shape(name), dtype=dt, order="F")
         self._check(self.L.fw_get_field(self.ctx, name.encode(), a.ctypes.data), "get " + name)
         return a
+
+    def get_f32(self, name):
+        """A field as float32 (fw_get_field_f32: the REAL(SP) host arrays of
+        a single-precision build)."""
+        a = np.zeros(self.shape(name), dtype=np.float32, order="F")
+        self._check(self.L.fw_get_field_f32(self.ctx, name.encode(), a.ctypes.data), "get_f32 " + name)
+        return a
+
+    def set_f32(self, name, arr):
+        a = np.asfortranarray(np.asarray(arr, dtype=np.float32))
+        if a.shape != self.shape(name):
+            raise FwError(-3, "%s must have shape %s" % (name, self.shape(name)))
+        self._check(self.L.fw_set_field_f32(self.ctx, name.encode(), a.ctypes.data), "set_f32 " + name)
 
     def set(self, name, arr):
         dt = np.int32 if name in _MASKS else np.float64

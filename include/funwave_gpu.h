@@ -138,6 +138,15 @@ int fw_init(fw_ctx *ctx, const double *depth, const double *eta, const double *u
  * (double, or int32 for MASK/MASK9/MASK_STRUC).  Synchronous. */
 int fw_get_field(fw_ctx *ctx, const char *name, void *host);
 int fw_set_field(fw_ctx *ctx, const char *name, const void *host);
+/* The same with float host arrays, for a host built in single precision
+ * (the reference's default build: REAL(SP) = 4-byte reals, mod_param.F:58-
+ * 68), whose GLOBAL arrays are float.  Any field but the masks (which stay
+ * int32 through fw_get_field/fw_set_field).  Values are rounded to nearest
+ * float on the way out of the FP64 build and exact in the mixed build.
+ * Initial inputs (fw_init) stay double: a single-precision host widens its
+ * depth and initial state once at start-up. */
+int fw_get_field_f32(fw_ctx *ctx, const char *name, float *host);
+int fw_set_field_f32(fw_ctx *ctx, const char *name, const float *host);
 /* n fields at once (n <= 16; names and host layouts as above), synchronous.
  * fw_set_fields copies every plane to the device on a second stream and
  * converts each one as soon as it has arrived; fw_get_fields is
