@@ -631,6 +631,13 @@ int fw_create(const fw_params *p, fw_ctx **out) {
         g.cA[d] = g.b1 / 2.0 / (h * h);
         g.cB[d] = g.b2 / (h * h);
         g.cC[d] = (-g.b1 - 2.0 * g.b2) / (h * h);
+        // the FP64 path's constant sub-expressions of etauv_solver.F:406-409
+        // and 504-507, evaluated left to right as there (IEEE division gives
+        // the device's value)
+        g.tK1[d] = g.b1 / 2.0 / h / h;
+        g.tK2[d] = g.b2 / h / h;
+        g.tK3[d] = -g.b1 / h / h;
+        g.tK4[d] = 2.0 * g.b2 / h / h;
     }
     g.rdx = 1.0 / p->DX;
     g.rdy = 1.0 / p->DY;

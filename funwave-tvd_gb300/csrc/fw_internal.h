@@ -43,6 +43,9 @@ struct Grid {
     // constants of the mixed path: tridiagonal coefficient factors per
     // direction (b1/2/h^2, b2/h^2, (-b1-2*b2)/h^2) and 1/DX, 1/DY
     double cA[2], cB[2], cC[2];
+    // FP64 path: b1/2/h/h, b2/h/h, -b1/h/h, 2*b2/h/h per direction, in the
+    // reference's evaluation order
+    double tK1[2], tK2[2], tK3[2], tK4[2];
     double rdx, rdy;
     // float copies of the constants for the mixed path (no FP64 work per
     // thread there): f_<name> = (float)<name>; f_hdx = 0.5/DX, f_rdx2 =

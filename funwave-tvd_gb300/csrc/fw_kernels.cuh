@@ -1087,11 +1087,13 @@ __device__ __forceinline__ void tri_coef(const Grid &g, const Fields<T> &f, int 
     const double tmp4 = DIR == 0 ? f.rhs_x[id] : f.rhs_y[id];
     double tmp1, tmp2, tmp3;
     if constexpr (sizeof(T) == sizeof(double)) {
-        // the reference's expressions (etauv_solver.F:406-409, 504-507)
-        const double h = DIR == 0 ? g.DX : g.DY, b1 = g.b1, b2 = g.b2;
-        tmp1 = g1 * m9 * (b1 / 2.0 / h / h * dep * dep + b2 / h / h * depl * dep);
-        tmp2 = 1.0 + g1 * m9 * (-b1 / h / h * dep * dep - 2.0 * b2 / h / h * dep * dep);
-        tmp3 = g1 * m9 * (b1 / 2.0 / h / h * dep * dep + b2 / h / h * dep * depr);
+        // the reference's expressions (etauv_solver.F:406-409, 504-507);
+        // their constant left parts (b1 / 2.0 / h / h and so on) come
+        // evaluated in the same order
+        const double k1 = g.tK1[DIR], k2 = g.tK2[DIR], k3 = g.tK3[DIR], k4 = g.tK4[DIR];
+        tmp1 = g1 * m9 * (k1 * dep * dep + k2 * depl * dep);
+        tmp2 = 1.0 + g1 * m9 * (k3 * dep * dep - k4 * dep * dep);
+        tmp3 = g1 * m9 * (k1 * dep * dep + k2 * dep * depr);
         if (tmp2 != 0.0 || f.MASK[id] > 0) {
             a = tmp1 / tmp2;
             c = tmp3 / tmp2;
@@ -1345,88 +1347,187 @@ __global__ void __launch_bounds__(128) k_tri_c(Grid g, Fields<T> f, LinePart lp)
     }
 }
 
-// FP64: one thread per line, the reference's Thomas recurrence in its own
-// operation order (TRIDx_ser / TRIDy_ser, tridiagnal.F:338-398) and, for
-// periodic y, TRIDy_periodic's two solves and combination
-// (tridiagnal.F:59-325).  c' and d' (and e' for the second periodic
-// solve) are kept in the solver scratch.
+// FP64: the reference's Thomas recurrence (TRIDx_ser / TRIDy_ser,
+// tridiagnal.F:338-398; periodic y: TRIDy_periodic, :59-325) in its own
+// operation order, in two kernels.
+//   k_thomas_rows (one thread per cell) computes every row's a, c, d
+//   (etauv_solver.F:406-409, 504-507), with TRIDy_periodic's end-row
+//   scaling, and stores what the recurrence needs: 1/a, c/a, d/a for a row
+//   that is eliminated (a != 0 and not the first row), else 0, c, d.
+//   k_thomas_lines (one thread per line) then walks the line: only the
+//   dependent part, den = 1/a - c'(k-1), c' = (c/a)/den and
+//   d' = (d/a - d'(k-1))/den, is on its critical path, and the loads of the
+//   next block of rows are issued before the current block is worked.
+// The results equal the one-pass recurrence bit for bit: the same IEEE
+// operations on the same operands, in a translation unit compiled without
+// contraction.  Scratch: tc = 1/a, tp = c/a then c', ty = d/a then d' then
+// the first solution, tq = e' then the second solution (periodic).
 template <typename T, int DIR, bool PER>
-__global__ void __launch_bounds__(128) k_thomas(Grid g, Fields<T> f, LinePart lp) {
+__global__ void __launch_bounds__(256) k_thomas_rows(Grid g, Fields<T> f, LinePart lp) {
+    const int i = g.ib + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = g.jb + blockIdx.y * blockDim.y + threadIdx.y;
+    if (i > g.ie || j > g.je) return;
+    const int k = DIR == 0 ? i - g.ib : j - g.jb;
+    double a, c, d;
+    tri_coef<T, DIR>(g, f, i, j, a, c, d);
+    if (PER) {
+        if (k == 0) {  // scaled by 1 + c_end, the c of the line's last row
+            double a2, c2, d2;
+            tri_coef<T, DIR>(g, f, DIR == 0 ? g.ie : i, DIR == 0 ? j : g.je, a2, c2, d2);
+            c = c / (1 + c2);
+            d = d / (1 + c2);
+        }
+        if (k == lp.L - 1) {  // scaled by 1 + a_beg, the a of the first row
+            double a2, c2, d2;
+            tri_coef<T, DIR>(g, f, DIR == 0 ? g.ib : i, DIR == 0 ? j : g.jb, a2, c2, d2);
+            a = a / (1 + a2);
+            d = d / (1 + a2);
+        }
+    }
+    const size_t q = IDX(i, j);
+    if (k > 0 && a != 0.0) {
+        f.tc[q] = 1.0 / a;
+        f.tp[q] = c / a;
+        f.ty[q] = d / a;
+    } else {
+        f.tc[q] = 0.0;
+        f.tp[q] = c;
+        f.ty[q] = d;
+    }
+}
+
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(32) k_thomas_lines(Grid g, Fields<T> f, LinePart lp) {
+    constexpr int U = 8;  // rows per block of loads
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= lp.nlines) return;
     const int L = lp.L;
-    double a_beg = 0.0, c_end = 0.0;
-    int i, j;
+    const size_t base = DIR == 0 ? IDX(g.ib, g.jb + l) : IDX(g.ib + l, g.jb);
+    const size_t step = DIR == 0 ? 1 : (size_t)g.pitch;
+    double a_beg = 0.0, c_end = 0.0, e_first = 0.0, e_last = 0.0, ea_last = 0.0;
     if (PER) {
         double a, c, d;
+        int i, j;
         line_cell<DIR>(g, l, 0, i, j);
         tri_coef<T, DIR>(g, f, i, j, a, c, d);
         a_beg = a;
         line_cell<DIR>(g, l, L - 1, i, j);
         tri_coef<T, DIR>(g, f, i, j, a, c, d);
         c_end = c;
+        // e = [1/(1+c_end), 0, ..., 0, -1/(1+a_beg)] (tridiagnal.F:207-215);
+        // the last row eliminates e/a with its scaled a
+        e_first = 1.0 / (1.0 + c_end);
+        e_last = -1.0 / (1.0 + a_beg);
+        ea_last = e_last / (a / (1 + a_beg));
+    }
+    double cra[U], cca[U], cda[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        const size_t q = base + (size_t)u * step;
+        cra[u] = u < L ? f.tc[q] : 0.0;
+        cca[u] = u < L ? f.tp[q] : 0.0;
+        cda[u] = u < L ? f.ty[q] : 0.0;
     }
     double cp = 0.0, dp = 0.0, ep = 0.0;
-    for (int k = 0; k < L; k++) {
-        double a, c, d;
-        line_cell<DIR>(g, l, k, i, j);
-        tri_coef<T, DIR>(g, f, i, j, a, c, d);
-        double e = 0.0;
-        if (PER) {
-            if (k == 0) {
-                c = c / (1 + c_end);
-                d = d / (1 + c_end);
-                e = 1.0 / (1.0 + c_end);
-            }
-            if (k == L - 1) {
-                a = a / (1 + a_beg);
-                d = d / (1 + a_beg);
-                e = -1.0 / (1.0 + a_beg);
+    for (int k0 = 0; k0 < L; k0 += U) {
+        double nra[U], nca[U], nda[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int kk = k0 + U + u;
+            const size_t q = base + (size_t)kk * step;
+            nra[u] = kk < L ? f.tc[q] : 0.0;
+            nca[u] = kk < L ? f.tp[q] : 0.0;
+            nda[u] = kk < L ? f.ty[q] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int k = k0 + u;
+            if (k < L) {
+                double c, d, e = 0.0;
+                if (cra[u] != 0.0) {
+                    const double den = cra[u] - cp;
+                    c = cca[u] / den;
+                    d = (cda[u] - dp) / den;
+                    // e/a: 0/a is a zero with the sign of a (that of 1/a)
+                    if (PER) e = ((k == L - 1 ? ea_last : fcopysign(0.0, cra[u])) - ep) / den;
+                } else {
+                    c = cca[u];
+                    d = cda[u];
+                    if (PER) e = k == L - 1 ? e_last : (k == 0 ? e_first : 0.0);
+                }
+                cp = c;
+                dp = d;
+                ep = e;
+                const size_t q = base + (size_t)k * step;
+                f.tp[q] = c;
+                f.ty[q] = d;
+                if (PER) f.tq[q] = e;
             }
         }
-        if (k > 0 && a != 0.0) {
-            const double den = 1.0 / a - cp;
-            c = c / a / den;
-            d = (d / a - dp) / den;
-            if (PER) e = (e / a - ep) / den;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            cra[u] = nra[u];
+            cca[u] = nca[u];
+            cda[u] = nda[u];
         }
-        cp = c;
-        dp = d;
-        ep = e;
-        const size_t q = IDX(i, j);
-        f.tp[q] = c;
-        f.ty[q] = d;
-        if (PER) f.tq[q] = e;
     }
-    // back substitution; y1 into ty, y2 into tq
+    // back substitution, blocks of U rows from the end; the first solution
+    // into ty, the second into tq (periodic), else straight into U / V
+    T *out = DIR == 0 ? f.U : f.V;
     double z1 = 0.0, z2 = 0.0;
-    for (int k = L - 1; k >= 0; k--) {
-        line_cell<DIR>(g, l, k, i, j);
-        const size_t q = IDX(i, j);
-        if (k == L - 1) {
-            z1 = f.ty[q];
-            if (PER) z2 = f.tq[q];
-        } else {
-            z1 = f.ty[q] - f.tp[q] * z1;
-            if (PER) z2 = f.tq[q] - f.tp[q] * z2;
+    const int nblk = (L + U - 1) / U;
+    double ccp[U], cdp[U], cep[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        const int k = L - 1 - u;
+        const size_t q = base + (size_t)(k >= 0 ? k : 0) * step;
+        ccp[u] = k >= 0 ? f.tp[q] : 0.0;
+        cdp[u] = k >= 0 ? f.ty[q] : 0.0;
+        cep[u] = (PER && k >= 0) ? f.tq[q] : 0.0;
+    }
+    for (int b = 0; b < nblk; b++) {
+        double ncp[U], ndp[U], nep[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int k = L - 1 - (b + 1) * U - u;
+            const size_t q = base + (size_t)(k >= 0 ? k : 0) * step;
+            ncp[u] = k >= 0 ? f.tp[q] : 0.0;
+            ndp[u] = k >= 0 ? f.ty[q] : 0.0;
+            nep[u] = (PER && k >= 0) ? f.tq[q] : 0.0;
         }
-        if (PER) {
-            f.ty[q] = z1;
-            f.tq[q] = z2;
-        } else {
-            (DIR == 0 ? f.U : f.V)[q] = (T)z1;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int k = L - 1 - b * U - u;
+            if (k >= 0) {
+                if (k == L - 1) {
+                    z1 = cdp[u];
+                    if (PER) z2 = cep[u];
+                } else {
+                    z1 = cdp[u] - ccp[u] * z1;
+                    if (PER) z2 = cep[u] - ccp[u] * z2;
+                }
+                const size_t q = base + (size_t)k * step;
+                if (PER) {
+                    f.ty[q] = z1;
+                    f.tq[q] = z2;
+                } else {
+                    out[q] = (T)z1;
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            ccp[u] = ncp[u];
+            cdp[u] = ndp[u];
+            cep[u] = nep[u];
         }
     }
     if (PER) {
-        line_cell<DIR>(g, l, 0, i, j);
-        const size_t q0 = IDX(i, j);
-        line_cell<DIR>(g, l, L - 1, i, j);
-        const size_t q1 = IDX(i, j);
+        const size_t q0 = base, q1 = base + (size_t)(L - 1) * step;
         const double beta = (c_end * f.ty[q0] - a_beg * f.ty[q1]) / (1.0 - (c_end * f.tq[q0] - a_beg * f.tq[q1]));
         for (int k = 0; k < L; k++) {
-            line_cell<DIR>(g, l, k, i, j);
-            const size_t q = IDX(i, j);
-            (DIR == 0 ? f.U : f.V)[q] = (T)(f.ty[q] + beta * f.tq[q]);
+            const size_t q = base + (size_t)k * step;
+            out[q] = (T)(f.ty[q] + beta * f.tq[q]);
         }
     }
 }
@@ -3163,13 +3264,8 @@ template <typename T> void launch_sources_debug(fw_ctx *c) {
 template <typename T, int DIR, bool PER>
 static bool launch_tri(fw_ctx *c, const LinePart &lp, bool fac = true, bool clear_dirty = false) {
     const Grid &g = c->g;
-    if constexpr (sizeof(T) == sizeof(double)) {
-        k_thomas<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
-        note(c);
-        return false;
-    }
     const int nt = lp.nlines * lp.P;
-    if (c->factored) {
+    if constexpr (sizeof(T) == sizeof(float)) if (c->factored) {
         if (fac) {
             k_fac_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
             k_fac_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
@@ -3209,6 +3305,14 @@ static bool launch_tri(fw_ctx *c, const LinePart &lp, bool fac = true, bool clea
         note(c, 7);
         return false;
     }
+    if constexpr (sizeof(T) == sizeof(double)) {
+        k_thomas_rows<T, DIR, PER><<<grid2(g.Mglob, g.Nglob, B2D), B2D, 0, c->stream>>>(g, c->F<T>(), lp);
+        k_thomas_lines<T, DIR, PER><<<(lp.nlines + 31) / 32, 32, 0, c->stream>>>(g, c->F<T>(), lp);
+        note(c, 2);
+        return false;
+    }
+    // mixed without a constant factorisation: the partitioned solve in
+    // double, one thread per chunk of m rows
     k_tri_a<T, DIR, PER><<<(nt + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
     note(c);
     k_tri_b<T, DIR, PER><<<(lp.nlines + 127) / 128, 128, 0, c->stream>>>(g, c->F<T>(), lp);
