@@ -560,64 +560,99 @@ def learned_report(fw, iters=4000, eval_coarse_steps=500, unroll=1, every=2, sca
                           "1024^2 sizes"}
 
 
-def cpu_baseline(fw, params, depth, phases, max_seconds=20.0, max_steps=5):
-    """The oracle (C restatement, all host threads) on the same workload:
-    init, one untimed step, then whole steps until max_seconds."""
+def host_info():
+    """The host the CPU legs run on: the cores the OS has, the cores this
+    process may run on (its affinity mask), and the CPU model."""
+    import platform
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as fh:
+                for ln in fh:
+                    if ln.lower().startswith("model name"):
+                        model = ln.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return {"nproc": os.cpu_count(), "affinity_cores": len(os.sched_getaffinity(0)),
+            "cpu_model": model or platform.machine(), "arch": platform.machine()}
+
+
+def oracle_rate(params, depth, phases, fp32, threads, steps, warmup=1, max_seconds=None):
+    """Cell-steps/s of the oracle on the workload: init, warm-up steps, then
+    `steps` whole steps (fewer if max_seconds runs out); (rate, steps, s)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import fw_oracle
     fw_oracle.build()
-    o = fw_oracle.Oracle(params)
+    o = fw_oracle.Oracle(params, threads=threads, fp32=fp32)
     o["Depth"][3:-3, 3:-3] = depth
     if phases is not None:
         o.set_phases(phases)
     o.init()
-    o.step()
+    for _ in range(warmup):
+        o.step()
     n, t0 = 0, time.perf_counter()
-    while n < max_steps:
+    while n < steps:
         o.step()
         n += 1
-        if time.perf_counter() - t0 > max_seconds:
+        if max_seconds is not None and time.perf_counter() - t0 > max_seconds:
             break
     dt = time.perf_counter() - t0
-    cores = fw_oracle.lib().ofw_get_threads()
-    cells = params["Mglob"] * params["Nglob"]
     o.close()
-    return {"value": cells * n / dt, "unit": UNIT, "cores": int(cores), "kind": "port",
-            "sample": "%d whole steps of the %dx%d workload after init and one warm-up step (%.1f s)"
-                      % (n, params["Mglob"], params["Nglob"], dt)}
+    return params["Mglob"] * params["Nglob"] * n / dt, n, dt
+
+
+def cpu_baseline(fw, params, depth, phases, max_seconds=12.0, max_steps=5):
+    """The oracle (the C restatement of the reference) on every core this
+    process may use, on the same workload: its single-precision build (the
+    reference's default REAL(SP) = 4-byte build) as the value, the FP64
+    build beside it."""
+    host = host_info()
+    threads = host["affinity_cores"]
+    r32, n32, t32 = oracle_rate(params, depth, phases, True, threads, max_steps, max_seconds=max_seconds)
+    r64, n64, t64 = oracle_rate(params, depth, phases, False, threads, max_steps, max_seconds=max_seconds)
+    return {"value": r32, "unit": UNIT, "cores": threads, "kind": "port", "dtype": "f32",
+            "sample": "%d whole single-precision steps of the %dx%d workload after init and one warm-up step "
+                      "(%.1f s), on %d OpenMP threads" % (n32, params["Mglob"], params["Nglob"], t32, threads),
+            "fp64": {"value": r64, "unit": UNIT, "dtype": "f64",
+                     "sample": "%d whole FP64 steps, the same way (%.1f s)" % (n64, t64)},
+            "host": host}
 
 
 def reference_arm(args, fw, params, depth, phases):
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import fw_oracle
-    fw_oracle.build()
-    o = fw_oracle.Oracle(params)
-    o["Depth"][3:-3, 3:-3] = depth
-    if phases is not None:
-        o.set_phases(phases)
-    o.init()
-    for _ in range(args.warmup):
-        o.step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        o.step()
-    dt = time.perf_counter() - t0
-    cells = params["Mglob"] * params["Nglob"]
-    v = cells * args.steps / dt
-    cores = int(fw_oracle.lib().ofw_get_threads())
+    host = host_info()
+    threads = host["affinity_cores"]
+    # the reference's default build is single precision (REAL(SP) = 4 bytes,
+    # mod_param.F:58-68); the FP64 build is timed beside it on a short sample
+    v, n, dt = oracle_rate(params, depth, phases, True, threads, args.steps, warmup=args.warmup)
+    v64, n64, dt64 = oracle_rate(params, depth, phases, False, threads, 3, warmup=1, max_seconds=10.0)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "precision": "FP64"},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "%d whole FP64 steps of the %dx%d workload after %d warm-up steps; the "
-                                   "Fortran reference cannot be compiled (no Fortran compiler on either "
-                                   "host), so its C restatement (oracle/) runs on %d OpenMP threads"
-                                   % (args.steps, params["Mglob"], params["Nglob"], args.warmup, cores)},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [params["Mglob"], params["Nglob"]], "dx_m": params["DX"],
+                   "precision": "FP32 (the reference's default single-precision build)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "dtype": "f32",
+                         "sample": "%d whole single-precision steps of the %dx%d workload after %d warm-up "
+                                   "steps; the Fortran reference cannot be compiled (no Fortran compiler on "
+                                   "either host), so its C restatement (oracle/) runs on %d OpenMP threads, "
+                                   "one per core of this process's affinity mask"
+                                   % (n, params["Mglob"], params["Nglob"], args.warmup, threads),
+                         "host": host},
+        "fp64": {"value": v64, "unit": UNIT, "dtype": "f64",
+                 "sample": "%d whole FP64 steps after one warm-up step (%.1f s)" % (n64, dt64)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -17,7 +17,7 @@
  *   - BREAKING's local DXg/DYg (breaker.F:98-100,123-124) are DX/DY.
  *   - DT before the first ESTIMATE_DT is 0 (module variable).
  * Default-REAL literals of the FP64 build are widened from float with
- * (double)(float)x (mod_param.F:71 pi, wavemaker.F:2378-2399), and nu_vis is
+ * (ofr)(float)x (mod_param.F:71 pi, wavemaker.F:2378-2399), and nu_vis is
  * a float array (sources.F:69).
  */
 #include "fw_oracle.h"
@@ -29,6 +29,30 @@
 #include <omp.h>
 #endif
 
+/* The arithmetic type.  The default build is the FP64 restatement.  With
+ * OFW_FP32 (and -fsingle-precision-constant) the same source is a single-
+ * precision build, as the reference's default REAL(SP) = 4-byte build is
+ * (mod_param.F:58-68): every real and literal is a float and the math
+ * functions are their float forms.  It serves only the CPU baseline's
+ * timing; the checker is the FP64 build. */
+#ifdef OFW_FP32
+typedef float ofr;
+#define sqrt sqrtf
+#define fabs fabsf
+#define exp expf
+#define sin sinf
+#define cos cosf
+#define tanh tanhf
+#define atan2 atan2f
+#define pow powf
+#define copysign copysignf
+#define asin asinf
+#else
+typedef double ofr;
+#endif
+
+int ofw_real_bytes(void) { return (int)sizeof(ofr); }
+
 #define GRAV 9.81
 #define SMALL 0.000001
 #define LARGE 999999.0
@@ -36,20 +60,20 @@
 #define NGHOST 3
 
 /* pi is a default-REAL literal assigned to REAL(SP) (mod_param.F:71). */
-static const double PI_SP = (double)(float)3.141592653;
+static const ofr PI_SP = (ofr)(float)3.141592653;
 
 struct ofw_ctx {
     ofw_params p;
     int Mloc, Nloc, Mloc1, Nloc1, Ibeg, Iend, Jbeg, Jend, Iend1, Jend1;
-    double TIME, DT, T_brk, EtaBlowVal;
-    double a1, a2, b1, b2, Beta_1, Beta_2;
-    double D_gen, beta_gen, rlamda, Width_WK;
+    ofr TIME, DT, T_brk, EtaBlowVal;
+    ofr a1, a2, b1, b2, Beta_1, Beta_2;
+    ofr D_gen, beta_gen, rlamda, Width_WK;
     int ilo, ihi, jlo, jhi;
-    double *xmk_wk, *ymk_wk;
+    ofr *xmk_wk, *ymk_wk;
     double *omgn_ir, *Cm, *Sm; /* JON_2D band storage */
     double *phi1, *jon_dgen, *jon_rlamda, *jon_betagen;
     /* cell arrays */
-    double *Depth, *H, *Eta, *Eta0, *U, *V, *U0, *V0, *Ubar, *Vbar, *Ubar0,
+    ofr *Depth, *H, *Eta, *Eta0, *U, *V, *U0, *V0, *Ubar, *Vbar, *Ubar0,
         *Vbar0, *HU, *HV, *Cd, *SPONGE, *CD_4_SPONGE, *ETAT, *ETAx, *ETAy, *Ux,
         *Vx, *Uy, *Vy, *DUx, *DVx, *DUy, *DVy, *Uxx, *Uxy, *Vxy, *Vyy, *DUxx,
         *DUxy, *DVxy, *DVyy, *Ut, *Vt, *Utx, *Vty, *Utxx, *Utxy, *Vtxy, *Vtyy,
@@ -57,27 +81,27 @@ struct ofw_ctx {
         *U1pp, *V1pp, *U2, *V2, *U3, *V3, *SourceX, *SourceY, *WaveMaker_Mass,
         *AGE, *nu_break, *HeightMax, *ROLLER_FLUX, *UNDERTOW_U, *UNDERTOW_V;
     /* statistics: MAX_MIN_PROPERTY and CALCULATE_MEAN */
-    double T_sum;
-    double *HeightMin, *VelocityMax, *MomentumFluxMax, *ETAmean, *Umean, *Vmean, *ETAsum, *Usum, *Vsum,
+    ofr T_sum;
+    ofr *HeightMin, *VelocityMax, *MomentumFluxMax, *ETAmean, *Umean, *Vmean, *ETAsum, *Usum, *Vsum,
         *ETA2sum, *ETA2mean, *SigWaveHeight, *Emax, *Emin, *HavgSum, *HrmsSum, *WaveHeightAve, *WaveHeightRMS;
     int *Num_Zero_Up;
     /* radiation stress, momentum flux and breaking dissipation of
      * CALCULATE_MEAN (mixing.F:156-200), with their per-stage inputs from
      * ESTIMATE_HUV (etauv_solver.F:94-101, 247) and SourceTerms
      * (sources.F:428-456) */
-    double *P_center, *Q_center, *U_davg, *V_davg, *Wsurf, *BreakSourceX, *BreakSourceY;
-    double *U_davg_sum, *V_davg_sum, *P_sum, *Q_sum, *UUsum, *UVsum, *VVsum, *WWsum, *FRCXsum, *FRCYsum,
+    ofr *P_center, *Q_center, *U_davg, *V_davg, *Wsurf, *BreakSourceX, *BreakSourceY;
+    ofr *U_davg_sum, *V_davg_sum, *P_sum, *Q_sum, *UUsum, *UVsum, *VVsum, *WWsum, *FRCXsum, *FRCYsum,
         *BreakDissX_sum, *BreakDissY_sum;
-    double *U_davg_mean, *V_davg_mean, *P_mean, *Q_mean, *UUmean, *UVmean, *VVmean, *WWmean, *FRCXmean,
+    ofr *U_davg_mean, *V_davg_mean, *P_mean, *Q_mean, *UUmean, *UVmean, *VVmean, *WWmean, *FRCXmean,
         *FRCYmean, *BreakDissX, *BreakDissY;
-    double *DxSxx, *DySxy, *DySyy, *DxSxy, *PgrdX, *PgrdY, *DxUUH, *DyUVH, *DyVVH, *DxUVH;
+    ofr *DxSxx, *DySxy, *DySyy, *DxSxy, *PgrdX, *PgrdY, *DxUUH, *DyUVH, *DyVVH, *DxUVH;
     int *MASK, *MASK9, *MASK_STRUC;
     /* x-face arrays */
-    double *Depthx, *P, *Fx, *Gx, *UxL, *UxR, *VxL, *VxR, *HUxL, *HUxR, *HVxL,
+    ofr *Depthx, *P, *Fx, *Gx, *UxL, *UxR, *VxL, *VxR, *HUxL, *HUxR, *HVxL,
         *HVxR, *EtaRxL, *EtaRxR, *HxL, *HxR, *U4xL, *U4xR, *V4xL, *V4xR, *PL,
         *PR, *FxL, *FxR, *GxL, *GxR, *SxL, *SxR;
     /* y-face arrays */
-    double *Depthy, *Q, *Fy, *Gy, *UyL, *UyR, *VyL, *VyR, *HUyL, *HUyR, *HVyL,
+    ofr *Depthy, *Q, *Fy, *Gy, *UyL, *UyR, *VyL, *VyR, *HUyL, *HUyR, *HVyL,
         *HVyR, *EtaRyL, *EtaRyR, *HyL, *HyR, *U4yL, *U4yR, *V4yL, *V4yR, *QL,
         *QR, *FyL, *FyR, *GyL, *GyR, *SyL, *SyR;
 };
@@ -102,11 +126,11 @@ int ofw_get_threads(void) {
 #define OMP_FOR
 #endif
 
-static inline double dmax(double a, double b) { return a > b ? a : b; }
-static inline double dmin(double a, double b) { return a < b ? a : b; }
+static inline ofr dmax(ofr a, ofr b) { return a > b ? a : b; }
+static inline ofr dmin(ofr a, ofr b) { return a < b ? a : b; }
 /* Fortran MAX(a,b,c) / MIN(a,b,c) */
-static inline double max3(double a, double b, double c) { return dmax(dmax(a, b), c); }
-static inline double min3(double a, double b, double c) { return dmin(dmin(a, b), c); }
+static inline ofr max3(ofr a, ofr b, ofr c) { return dmax(dmax(a, b), c); }
+static inline ofr min3(ofr a, ofr b, ofr c) { return dmin(dmin(a, b), c); }
 
 /* ------------------------------------------------------------------------ */
 /* construction / field table                                               */
@@ -175,12 +199,12 @@ ofw_ctx *ofw_create(const ofw_params *p) {
     size_t ny = (size_t)o->Mloc * o->Nloc1;
     for (size_t k = 0; k < NFIELDS; k++) {
         size_t n = FIELDS[k].kind == 0 ? nc : FIELDS[k].kind == 1 ? nx : ny;
-        void *buf = calloc(n, FIELDS[k].is_int ? sizeof(int) : sizeof(double));
+        void *buf = calloc(n, FIELDS[k].is_int ? sizeof(int) : sizeof(ofr));
         if (!buf) { ofw_destroy(o); return NULL; }
         *(void **)((char *)o + FIELDS[k].off) = buf;
     }
-    o->xmk_wk = (double *)calloc((size_t)o->Mloc, sizeof(double));
-    o->ymk_wk = (double *)calloc((size_t)o->Nloc, sizeof(double));
+    o->xmk_wk = (ofr *)calloc((size_t)o->Mloc, sizeof(ofr));
+    o->ymk_wk = (ofr *)calloc((size_t)o->Nloc, sizeof(ofr));
     /* ALLOCATE_VARIABLES / INITIALIZATION defaults (init.F:445-560,624,214) */
     for (size_t k = 0; k < nc; k++) {
         o->Depth[k] = 10.0;
@@ -249,7 +273,7 @@ void ofw_set_scalar(ofw_ctx *o, const char *n, double v) {
 /* PHI_COLL(Mloc,Nloc,Ibeg,Iend,Jbeg,Jend,Nghost,PHI,VTYPE,PERIODIC) for a
  * cell array (bc.F:631-1272; periodic serial copy :735-740, VTYPE 1
  * :753-844, VTYPE 2 :847-937, VTYPE 3 :939-1029). */
-static void phi_coll(ofw_ctx *o, double *PHI, int vtype) {
+static void phi_coll(ofw_ctx *o, ofr *PHI, int vtype) {
     const int M = o->Mloc, Ib = o->Ibeg, Ie = o->Iend, Jb = o->Jbeg, Je = o->Jend;
     const int per = o->p.periodic;
     if (per) {
@@ -259,28 +283,28 @@ static void phi_coll(ofw_ctx *o, double *PHI, int vtype) {
                 C2(PHI, I, Je + K) = C2(PHI, I, NGHOST + K);
             }
     }
-    const double sx = (vtype == 2) ? -1.0 : 1.0; /* u: x-antisymmetric */
-    const double sy = (vtype == 3) ? -1.0 : 1.0; /* v: y-antisymmetric */
+    const ofr sx = (vtype == 2) ? -1.0 : 1.0; /* u: x-antisymmetric */
+    const ofr sy = (vtype == 3) ? -1.0 : 1.0; /* v: y-antisymmetric */
     for (int J = Jb; J <= Je; J++)
         for (int K = 1; K <= NGHOST; K++) {
-            double w = C2(PHI, Ib + NGHOST - K, J);
+            ofr w = C2(PHI, Ib + NGHOST - K, J);
             C2(PHI, K, J) = (vtype == 2) ? -w : w;
         }
     for (int J = Jb; J <= Je; J++)
         for (int K = 1; K <= NGHOST; K++) {
-            double e = C2(PHI, Ie - K + 1, J);
+            ofr e = C2(PHI, Ie - K + 1, J);
             C2(PHI, Ie + K, J) = (vtype == 2) ? -e : e;
         }
     (void)sx;
     if (!per) {
         for (int I = 1; I <= M; I++)
             for (int K = 1; K <= NGHOST; K++) {
-                double s = C2(PHI, I, Jb + NGHOST - K);
+                ofr s = C2(PHI, I, Jb + NGHOST - K);
                 C2(PHI, I, K) = (vtype == 3) ? -s : s;
             }
         for (int I = 1; I <= M; I++)
             for (int K = 1; K <= NGHOST; K++) {
-                double n = C2(PHI, I, Je - K + 1);
+                ofr n = C2(PHI, I, Je - K + 1);
                 C2(PHI, I, Je + K) = (vtype == 3) ? -n : n;
             }
     }
@@ -312,7 +336,7 @@ static void phi_coll_int(ofw_ctx *o, int *PHI) {
 /* PHI_COLL_VARIABLE_LENGTH (bc.F:530-629), VTYPE 1: plain mirror on all four
  * sides, periodic ignored.  ld = leading dimension, (m,n) the extents,
  * ie/je the last interior index passed in (Iend1 for P, Jend1 for Q). */
-static void phi_coll_var(ofw_ctx *o, double *PHI, int ld, int m, int ie, int je) {
+static void phi_coll_var(ofw_ctx *o, ofr *PHI, int ld, int m, int ie, int je) {
     const int Ib = o->Ibeg, Jb = o->Jbeg;
 #define V2(I, J) PHI[(size_t)((I)-1) + (size_t)((J)-1) * (size_t)ld]
     for (int J = Jb; J <= je; J++)
@@ -350,7 +374,7 @@ void ofw_exchange(ofw_ctx *o) {
     const size_t nc = (size_t)o->Mloc * o->Nloc;
     OMP_FOR
     for (size_t k = 0; k < nc; k++) {
-        double m = (double)o->MASK[k];
+        ofr m = (ofr)o->MASK[k];
         o->U[k] = o->U[k] * m;
         o->V[k] = o->V[k] * m;
         o->HU[k] = o->HU[k] * m;
@@ -362,23 +386,23 @@ void ofw_exchange(ofw_ctx *o) {
 /* ESTIMATE_DT (misc.F:216-296), CARTESIAN                                  */
 /* ------------------------------------------------------------------------ */
 void ofw_estimate_dt(ofw_ctx *o) {
-    const double DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
-    double TMP3 = LARGE;
+    const ofr DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
+    ofr TMP3 = LARGE;
     const int M = o->Mloc, N = o->Nloc;
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(ofw_get_threads()) reduction(min : TMP3)
 #endif
     for (int J = 1; J <= N; J++)
         for (int I = 1; I <= M; I++) {
-            double c = sqrt(GRAV * dmax(C2(o->H, I, J), mdf));
-            double TMP1 = fabs(C2(o->U, I, J)) + c;
-            double TMP2 = (TMP1 < SMALL) ? DX / SMALL : DX / TMP1;
+            ofr c = sqrt(GRAV * dmax(C2(o->H, I, J), mdf));
+            ofr TMP1 = fabs(C2(o->U, I, J)) + c;
+            ofr TMP2 = (TMP1 < SMALL) ? DX / SMALL : DX / TMP1;
             if (TMP2 < TMP3) TMP3 = TMP2;
             TMP1 = fabs(C2(o->V, I, J)) + c;
             TMP2 = (TMP1 < SMALL) ? DY / SMALL : DY / TMP1;
             if (TMP2 < TMP3) TMP3 = TMP2;
         }
-    double DT_tmp = o->p.cfl * TMP3;
+    ofr DT_tmp = o->p.cfl * TMP3;
     if (o->p.fixed_dt) {
         o->DT = o->p.dt_fixed;
         while (o->DT > DT_tmp) o->DT = o->DT / 2.0;
@@ -391,44 +415,44 @@ void ofw_estimate_dt(ofw_ctx *o) {
 /* ------------------------------------------------------------------------ */
 /* 2nd-order masked central derivatives (derivatives.F:123-289), interior   */
 /* ------------------------------------------------------------------------ */
-static void d_x(ofw_ctx *o, const double *in, double *out) {
-    const double DX = o->p.DX;
+static void d_x(ofw_ctx *o, const ofr *in, ofr *out) {
+    const ofr DX = o->p.DX;
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++)
-            C2(out, I, J) = (C2(in, I + 1, J) - C2(in, I - 1, J)) / DX / 2.0 * (double)C2(o->MASK9, I, J);
+            C2(out, I, J) = (C2(in, I + 1, J) - C2(in, I - 1, J)) / DX / 2.0 * (ofr)C2(o->MASK9, I, J);
 }
-static void d_y(ofw_ctx *o, const double *in, double *out) {
-    const double DY = o->p.DY;
+static void d_y(ofw_ctx *o, const ofr *in, ofr *out) {
+    const ofr DY = o->p.DY;
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++)
-            C2(out, I, J) = (C2(in, I, J + 1) - C2(in, I, J - 1)) / DY / 2.0 * (double)C2(o->MASK9, I, J);
+            C2(out, I, J) = (C2(in, I, J + 1) - C2(in, I, J - 1)) / DY / 2.0 * (ofr)C2(o->MASK9, I, J);
 }
-static void d_xx(ofw_ctx *o, const double *in, double *out) {
-    const double DX = o->p.DX;
+static void d_xx(ofw_ctx *o, const ofr *in, ofr *out) {
+    const ofr DX = o->p.DX;
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++)
             C2(out, I, J) = (C2(in, I + 1, J) - 2.0 * C2(in, I, J) + C2(in, I - 1, J)) / DX / DX *
-                            (double)C2(o->MASK9, I, J);
+                            (ofr)C2(o->MASK9, I, J);
 }
-static void d_yy(ofw_ctx *o, const double *in, double *out) {
-    const double DY = o->p.DY;
+static void d_yy(ofw_ctx *o, const ofr *in, ofr *out) {
+    const ofr DY = o->p.DY;
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++)
             C2(out, I, J) = (C2(in, I, J + 1) - 2.0 * C2(in, I, J) + C2(in, I, J - 1)) / DY / DY *
-                            (double)C2(o->MASK9, I, J);
+                            (ofr)C2(o->MASK9, I, J);
 }
-static void d_xy(ofw_ctx *o, const double *in, double *out) {
-    const double DX = o->p.DX, DY = o->p.DY;
+static void d_xy(ofw_ctx *o, const ofr *in, ofr *out) {
+    const ofr DX = o->p.DX, DY = o->p.DY;
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++) {
-            double t1 = (C2(in, I + 1, J + 1) - C2(in, I + 1, J - 1)) / 2.0 / DY;
-            double t2 = (C2(in, I - 1, J + 1) - C2(in, I - 1, J - 1)) / 2.0 / DY;
-            C2(out, I, J) = (t1 - t2) / 2.0 / DX * (double)C2(o->MASK9, I, J);
+            ofr t1 = (C2(in, I + 1, J + 1) - C2(in, I + 1, J - 1)) / 2.0 / DY;
+            ofr t2 = (C2(in, I - 1, J + 1) - C2(in, I - 1, J - 1)) / 2.0 / DY;
+            C2(out, I, J) = (t1 - t2) / 2.0 / DX * (ofr)C2(o->MASK9, I, J);
         }
 }
 
@@ -474,13 +498,13 @@ static void exchange_dispersion(ofw_ctx *o) {
 void ofw_cal_dispersion(ofw_ctx *o) {
     const int M = o->Mloc, N = o->Nloc;
     const size_t nc = (size_t)M * N;
-    const double DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
-    const double gamma2 = o->p.gamma2;
-    const double Beta_1 = o->Beta_1, Beta_2 = o->Beta_2, b2 = o->b2;
-    double *DU = (double *)calloc(nc, sizeof(double));
-    double *DV = (double *)calloc(nc, sizeof(double));
-    double *DUt = (double *)calloc(nc, sizeof(double));
-    double *DVt = (double *)calloc(nc, sizeof(double));
+    const ofr DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
+    const ofr gamma2 = o->p.gamma2;
+    const ofr Beta_1 = o->Beta_1, Beta_2 = o->Beta_2, b2 = o->b2;
+    ofr *DU = (ofr *)calloc(nc, sizeof(ofr));
+    ofr *DV = (ofr *)calloc(nc, sizeof(ofr));
+    ofr *DUt = (ofr *)calloc(nc, sizeof(ofr));
+    ofr *DVt = (ofr *)calloc(nc, sizeof(ofr));
 
     d_xx(o, o->U, o->Uxx);
     d_xy(o, o->U, o->Uxy);
@@ -539,7 +563,7 @@ void ofw_cal_dispersion(ofw_ctx *o) {
         d_xy(o, DVt, o->DVtxy);
     }
     /* wall rows of the cross derivatives (dispersion.F:189-286) */
-    double *cross[8] = {o->Uxy, o->DUxy, o->Vxy, o->DVxy, o->Utxy, o->DUtxy, o->Vtxy, o->DVtxy};
+    ofr *cross[8] = {o->Uxy, o->DUxy, o->Vxy, o->DVxy, o->Utxy, o->DUtxy, o->Vtxy, o->DVtxy};
     for (int k = 0; k < 8; k++) {
         for (int J = 1; J <= N; J++) C2(cross[k], o->Ibeg, J) = ZERO;
         for (int J = 1; J <= N; J++) C2(cross[k], o->Iend, J) = ZERO;
@@ -549,11 +573,11 @@ void ofw_cal_dispersion(ofw_ctx *o) {
     exchange_dispersion(o);
 
     /* U4, V4, U1p, V1p over all cells (dispersion.F:293-384) */
-    const double c4a = 1.0 / 3.0 - Beta_1 + 0.5 * Beta_1 * Beta_1;
+    const ofr c4a = 1.0 / 3.0 - Beta_1 + 0.5 * Beta_1 * Beta_1;
     OMP_FOR
     for (int J = 1; J <= N; J++)
         for (int I = 1; I <= M; I++) {
-            double D = C2(o->Depth, I, J);
+            ofr D = C2(o->Depth, I, J);
             C2(o->U4, I, J) = (1.0 / 3.0 - Beta_1 + 0.5 * Beta_1 * Beta_1) * D * D *
                                   (C2(o->Uxx, I, J) + C2(o->Vxy, I, J)) +
                               (Beta_1 - 1.0 / 2.0) * D * (C2(o->DUxx, I, J) + C2(o->DVxy, I, J));
@@ -561,15 +585,15 @@ void ofw_cal_dispersion(ofw_ctx *o) {
                                   (C2(o->Uxy, I, J) + C2(o->Vyy, I, J)) +
                               (Beta_1 - 1.0 / 2.0) * D * (C2(o->DUxy, I, J) + C2(o->DVyy, I, J));
             if (gamma2 > ZERO) {
-                double UxxVxy = C2(o->Uxx, I, J) + C2(o->Vxy, I, J);
-                double UxyVyy = C2(o->Uxy, I, J) + C2(o->Vyy, I, J);
-                double HUxxHVxy = C2(o->DUxx, I, J) + C2(o->DVxy, I, J);
-                double HUxyHVyy = C2(o->DUxy, I, J) + C2(o->DVyy, I, J);
-                double rh = D, reta = C2(o->Eta, I, J);
-                double ken1 = (1.0 / 6.0 - Beta_1 + Beta_1 * Beta_1) * rh * reta * Beta_2 +
+                ofr UxxVxy = C2(o->Uxx, I, J) + C2(o->Vxy, I, J);
+                ofr UxyVyy = C2(o->Uxy, I, J) + C2(o->Vyy, I, J);
+                ofr HUxxHVxy = C2(o->DUxx, I, J) + C2(o->DVxy, I, J);
+                ofr HUxyHVyy = C2(o->DUxy, I, J) + C2(o->DVyy, I, J);
+                ofr rh = D, reta = C2(o->Eta, I, J);
+                ofr ken1 = (1.0 / 6.0 - Beta_1 + Beta_1 * Beta_1) * rh * reta * Beta_2 +
                               (1.0 / 2.0 * Beta_1 * Beta_1 - 1.0 / 6.0) * reta * reta * Beta_2 * Beta_2;
-                double ken2 = (Beta_1 - 1.0 / 2.0) * reta * Beta_2;
-                double m9 = (double)C2(o->MASK9, I, J);
+                ofr ken2 = (Beta_1 - 1.0 / 2.0) * reta * Beta_2;
+                ofr m9 = (ofr)C2(o->MASK9, I, J);
                 C2(o->U4, I, J) = C2(o->U4, I, J) + gamma2 * m9 * (ken1 * UxxVxy + ken2 * HUxxHVxy);
                 C2(o->V4, I, J) = C2(o->V4, I, J) + gamma2 * m9 * (ken1 * UxyVyy + ken2 * HUxyHVyy);
             }
@@ -587,46 +611,46 @@ void ofw_cal_dispersion(ofw_ctx *o) {
         OMP_FOR
         for (int J = o->Jbeg; J <= o->Jend; J++)
             for (int I = o->Ibeg; I <= o->Iend; I++) {
-                double UxxVxy = C2(o->Uxx, I, J) + C2(o->Vxy, I, J);
-                double UxyVyy = C2(o->Uxy, I, J) + C2(o->Vyy, I, J);
-                double UxxVxy_x = (C2(o->Uxx, I + 1, J) + C2(o->Vxy, I + 1, J) - C2(o->Uxx, I - 1, J) -
+                ofr UxxVxy = C2(o->Uxx, I, J) + C2(o->Vxy, I, J);
+                ofr UxyVyy = C2(o->Uxy, I, J) + C2(o->Vyy, I, J);
+                ofr UxxVxy_x = (C2(o->Uxx, I + 1, J) + C2(o->Vxy, I + 1, J) - C2(o->Uxx, I - 1, J) -
                                    C2(o->Vxy, I - 1, J)) / 2.0 / DX;
-                double UxxVxy_y = (C2(o->Uxx, I, J + 1) + C2(o->Vxy, I, J + 1) - C2(o->Uxx, I, J - 1) -
+                ofr UxxVxy_y = (C2(o->Uxx, I, J + 1) + C2(o->Vxy, I, J + 1) - C2(o->Uxx, I, J - 1) -
                                    C2(o->Vxy, I, J - 1)) / 2.0 / DY;
-                double UxyVyy_x = (C2(o->Uxy, I + 1, J) + C2(o->Vyy, I + 1, J) - C2(o->Uxy, I - 1, J) -
+                ofr UxyVyy_x = (C2(o->Uxy, I + 1, J) + C2(o->Vyy, I + 1, J) - C2(o->Uxy, I - 1, J) -
                                    C2(o->Vyy, I - 1, J)) / 2.0 / DX;
-                double UxyVyy_y = (C2(o->Uxy, I, J + 1) + C2(o->Vyy, I, J + 1) - C2(o->Uxy, I, J - 1) -
+                ofr UxyVyy_y = (C2(o->Uxy, I, J + 1) + C2(o->Vyy, I, J + 1) - C2(o->Uxy, I, J - 1) -
                                    C2(o->Vyy, I, J - 1)) / 2.0 / DY;
-                double HUxxHVxy = C2(o->DUxx, I, J) + C2(o->DVxy, I, J);
-                double HUxyHVyy = C2(o->DUxy, I, J) + C2(o->DVyy, I, J);
-                double HUxxHVxy_x = (C2(o->DUxx, I + 1, J) + C2(o->DVxy, I + 1, J) -
+                ofr HUxxHVxy = C2(o->DUxx, I, J) + C2(o->DVxy, I, J);
+                ofr HUxyHVyy = C2(o->DUxy, I, J) + C2(o->DVyy, I, J);
+                ofr HUxxHVxy_x = (C2(o->DUxx, I + 1, J) + C2(o->DVxy, I + 1, J) -
                                      C2(o->DUxx, I - 1, J) - C2(o->DVxy, I - 1, J)) / 2.0 / DX;
-                double HUxxHVxy_y = (C2(o->DUxx, I, J + 1) + C2(o->DVxy, I, J + 1) -
+                ofr HUxxHVxy_y = (C2(o->DUxx, I, J + 1) + C2(o->DVxy, I, J + 1) -
                                      C2(o->DUxx, I, J - 1) - C2(o->DVxy, I, J - 1)) / 2.0 / DY;
-                double HUxyHVyy_x = (C2(o->DUxy, I + 1, J) + C2(o->DVyy, I + 1, J) -
+                ofr HUxyHVyy_x = (C2(o->DUxy, I + 1, J) + C2(o->DVyy, I + 1, J) -
                                      C2(o->DUxy, I - 1, J) - C2(o->DVyy, I - 1, J)) / 2.0 / DX;
-                double HUxyHVyy_y = (C2(o->DUxy, I, J + 1) + C2(o->DVyy, I, J + 1) -
+                ofr HUxyHVyy_y = (C2(o->DUxy, I, J + 1) + C2(o->DVyy, I, J + 1) -
                                      C2(o->DUxy, I, J - 1) - C2(o->DVyy, I, J - 1)) / 2.0 / DY;
-                double rh = C2(o->Depth, I, J);
-                double rhx = (C2(o->Depth, I + 1, J) - C2(o->Depth, I - 1, J)) / 2.0 / DX;
-                double rhy = (C2(o->Depth, I, J + 1) - C2(o->Depth, I, J - 1)) / 2.0 / DY;
-                double reta = C2(o->Eta, I, J);
-                double ETAx = C2(o->ETAx, I, J), ETAy = C2(o->ETAy, I, J), ETAT = C2(o->ETAT, I, J);
-                double Utx = C2(o->Utx, I, J), Vty = C2(o->Vty, I, J);
-                double U1pp = -reta * Beta_2 * ETAx * Beta_2 * (Utx + Vty) -
+                ofr rh = C2(o->Depth, I, J);
+                ofr rhx = (C2(o->Depth, I + 1, J) - C2(o->Depth, I - 1, J)) / 2.0 / DX;
+                ofr rhy = (C2(o->Depth, I, J + 1) - C2(o->Depth, I, J - 1)) / 2.0 / DY;
+                ofr reta = C2(o->Eta, I, J);
+                ofr ETAx = C2(o->ETAx, I, J), ETAy = C2(o->ETAy, I, J), ETAT = C2(o->ETAT, I, J);
+                ofr Utx = C2(o->Utx, I, J), Vty = C2(o->Vty, I, J);
+                ofr U1pp = -reta * Beta_2 * ETAx * Beta_2 * (Utx + Vty) -
                               0.5 * reta * reta * Beta_2 * Beta_2 * (C2(o->Utxx, I, J) + C2(o->Vtxy, I, J)) -
                               ETAx * Beta_2 * (C2(o->DUtx, I, J) + C2(o->DVty, I, J)) -
                               reta * Beta_2 * (C2(o->DUtxx, I, J) + C2(o->DVtxy, I, J));
-                double V1pp = -reta * Beta_2 * ETAy * Beta_2 * (Utx + Vty) -
+                ofr V1pp = -reta * Beta_2 * ETAy * Beta_2 * (Utx + Vty) -
                               0.5 * reta * reta * Beta_2 * Beta_2 * (C2(o->Utxy, I, J) + C2(o->Vtyy, I, J)) -
                               ETAy * Beta_2 * (C2(o->DUtx, I, J) + C2(o->DVty, I, J)) -
                               reta * Beta_2 * (C2(o->DUtxy, I, J) + C2(o->DVtyy, I, J));
-                double ken1 = Beta_1 * (1.0 - Beta_1) * rh * ETAT * Beta_2 -
+                ofr ken1 = Beta_1 * (1.0 - Beta_1) * rh * ETAT * Beta_2 -
                               Beta_1 * Beta_1 * reta * Beta_2 * ETAT * Beta_2;
-                double ken2 = Beta_1 * (1.0 - Beta_1) * rh * reta * Beta_2 -
+                ofr ken2 = Beta_1 * (1.0 - Beta_1) * rh * reta * Beta_2 -
                               0.5 * Beta_1 * Beta_1 * reta * reta * Beta_2 * Beta_2;
-                double ken3 = Beta_1 * ETAT * Beta_2;
-                double ken4 = Beta_1 * reta * Beta_2;
+                ofr ken3 = Beta_1 * ETAT * Beta_2;
+                ofr ken4 = Beta_1 * reta * Beta_2;
                 U1pp = U1pp - ken1 * UxxVxy - ken2 * (C2(o->Utxx, I, J) + C2(o->Vtxy, I, J)) +
                        ken3 * HUxxHVxy + ken4 * (C2(o->DUtxx, I, J) + C2(o->DVtxy, I, J));
                 V1pp = V1pp - ken1 * UxyVyy - ken2 * (C2(o->Utxy, I, J) + C2(o->Vtyy, I, J)) +
@@ -634,10 +658,10 @@ void ofw_cal_dispersion(ofw_ctx *o) {
                 C2(o->U1pp, I, J) = U1pp;
                 C2(o->V1pp, I, J) = V1pp;
 
-                double Ux = C2(o->Ux, I, J), Vx = C2(o->Vx, I, J), Uy = C2(o->Uy, I, J),
+                ofr Ux = C2(o->Ux, I, J), Vx = C2(o->Vx, I, J), Uy = C2(o->Uy, I, J),
                        Vy = C2(o->Vy, I, J);
-                double DUx = C2(o->DUx, I, J), DVy = C2(o->DVy, I, J);
-                double Uc = C2(o->U, I, J), Vc = C2(o->V, I, J);
+                ofr DUx = C2(o->DUx, I, J), DVy = C2(o->DVy, I, J);
+                ofr Uc = C2(o->U, I, J), Vc = C2(o->V, I, J);
                 ken1 = (Beta_1 - 1.0) * (rhx + ETAx) * Beta_2;
                 ken2 = (Beta_1 - 1.0) * (rh + reta) * Beta_2;
                 ken3 = ((1.0 - Beta_1) * (1.0 - Beta_1) * rh * rhx * Beta_2 * Beta_2 -
@@ -646,7 +670,7 @@ void ofw_cal_dispersion(ofw_ctx *o) {
                 ken4 = (0.5 * (1.0 - Beta_1) * (1.0 - Beta_1) * rh * rh * Beta_2 * Beta_2 -
                         Beta_1 * (1.0 - Beta_1) * rh * reta * Beta_2 +
                         0.5 * (Beta_1 * Beta_1 - 1.0) * reta * reta * Beta_2 * Beta_2);
-                double ken5 = ((1.0 - Beta_1) * (1.0 - Beta_1) * rh * rhy * Beta_2 * Beta_2 -
+                ofr ken5 = ((1.0 - Beta_1) * (1.0 - Beta_1) * rh * rhy * Beta_2 * Beta_2 -
                                Beta_1 * (1.0 - Beta_1) * (rhy * reta * Beta_2 + rh * ETAy * Beta_2) +
                                (Beta_1 * Beta_1 - 1.0) * reta * ETAy * Beta_2 * Beta_2);
                 C2(o->U2, I, J) =
@@ -664,8 +688,8 @@ void ofw_cal_dispersion(ofw_ctx *o) {
                     ken4 * (Uy * UxxVxy + Uc * UxxVxy_y + Vy * UxyVyy + Vc * UxyVyy_y) +
                     Beta_2 * Beta_2 * (DUx + DVy + reta * Beta_2 * (Ux + Vy)) *
                         (HUxyHVyy + ETAy * Beta_2 * (Ux + Vy) + reta * Beta_2 * UxyVyy);
-                double omega_0 = Vx - Uy;
-                double omega_1 = (b2 * rhx + Beta_1 * ETAx) * Beta_2 *
+                ofr omega_0 = Vx - Uy;
+                ofr omega_1 = (b2 * rhx + Beta_1 * ETAx) * Beta_2 *
                                      (HUxyHVyy + (b2 * rh + Beta_1 * reta) * Beta_2 * UxyVyy) -
                                  (b2 * rhy + Beta_1 * ETAy) * Beta_2 *
                                      (HUxxHVxy + (b2 * rh + Beta_1 * reta) * Beta_2 * UxxVxy);
@@ -688,20 +712,20 @@ void ofw_cal_dispersion(ofw_ctx *o) {
 /* ------------------------------------------------------------------------ */
 
 /* 3-argument minmod-like limiter of CONSTRUCT_HO_X (fluxes.F:1552-1566) */
-static inline double lim3(double a, double b, double c) {
+static inline ofr lim3(ofr a, ofr b, ofr c) {
     if (a >= 0.0) return dmax(0.0, min3(a, 2.0 * b, 2.0 * c));
     return dmin(0.0, max3(a, 2.0 * b, 2.0 * c));
 }
 
 /* Din for one position: v[0..3] = Vin(i-2..i+1), m[0..3] = MASK(i-2..i+1).
  * fluxes.F:1548-1598 */
-static inline double ho_din(const double *v, const int *m) {
-    double TXP1 = v[1] - v[0];
-    double TXP2 = v[2] - v[1];
-    double TXP3 = v[3] - v[2];
-    double DVP1 = lim3(TXP1, TXP2, TXP3);
-    double DVP2 = lim3(TXP2, TXP3, TXP1);
-    double DVP3 = lim3(TXP3, TXP1, TXP2);
+static inline ofr ho_din(const ofr *v, const int *m) {
+    ofr TXP1 = v[1] - v[0];
+    ofr TXP2 = v[2] - v[1];
+    ofr TXP3 = v[3] - v[2];
+    ofr DVP1 = lim3(TXP1, TXP2, TXP3);
+    ofr DVP2 = lim3(TXP2, TXP3, TXP1);
+    ofr DVP3 = lim3(TXP3, TXP1, TXP2);
     if (m[0] == 0 || m[3] == 0) {
         TXP2 = v[2] - v[1];
         TXP1 = TXP2;
@@ -720,36 +744,36 @@ static inline double ho_din(const double *v, const int *m) {
 
 /* van Leer face values (fluxes.F:1602-1630): returns OutL at face i from
  * Din(i-1), Din(i) and Vin(i-1); OutR from Din(i), Din(i+1) and Vin(i). */
-static inline double vl_guard(double t) {
+static inline ofr vl_guard(ofr t) {
     if (fabs(t) <= SMALL) t = SMALL * copysign(1.0, t);
     return t;
 }
-static inline double vl_phi(double rat) {
-    double van = 0.0;
+static inline ofr vl_phi(ofr rat) {
+    ofr van = 0.0;
     if (fabs(1.0 + rat) > SMALL) van = (rat + fabs(rat)) / (1.0 + rat);
     return van;
 }
-static inline double ho_left(double vim1, double d0, double d1) {
-    double TMP1 = vl_guard(d0), TMP2 = vl_guard(d1);
-    double VAN1 = vl_phi(TMP2 / TMP1);
-    double VAN2 = vl_phi(TMP1 / TMP2);
+static inline ofr ho_left(ofr vim1, ofr d0, ofr d1) {
+    ofr TMP1 = vl_guard(d0), TMP2 = vl_guard(d1);
+    ofr VAN1 = vl_phi(TMP2 / TMP1);
+    ofr VAN2 = vl_phi(TMP1 / TMP2);
     return vim1 + (1.0 / 6.0) * (VAN1 * TMP1 + 2.0 * VAN2 * TMP2);
 }
-static inline double ho_right(double vi, double d0, double d1) {
-    double TMP1 = vl_guard(d0), TMP2 = vl_guard(d1);
-    double VAN1 = vl_phi(TMP2 / TMP1);
-    double VAN2 = vl_phi(TMP1 / TMP2);
+static inline ofr ho_right(ofr vi, ofr d0, ofr d1) {
+    ofr TMP1 = vl_guard(d0), TMP2 = vl_guard(d1);
+    ofr VAN1 = vl_phi(TMP2 / TMP1);
+    ofr VAN2 = vl_phi(TMP1 / TMP2);
     return vi - (1.0 / 6.0) * (2.0 * VAN1 * TMP1 + VAN2 * TMP2);
 }
 
 /* CONSTRUCT_HO_X (fluxes.F:1531-1639) */
-static void construct_ho_x(ofw_ctx *o, const double *Vin, double *OutL, double *OutR) {
+static void construct_ho_x(ofw_ctx *o, const ofr *Vin, ofr *OutL, ofr *OutR) {
     const int Ib = o->Ibeg, Ie = o->Iend, M = o->Mloc;
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++) {
-        double *Din = (double *)calloc((size_t)M + 1, sizeof(double));
+        ofr *Din = (ofr *)calloc((size_t)M + 1, sizeof(ofr));
         for (int I = Ib - 1; I <= Ie + 2; I++) {
-            double v[4];
+            ofr v[4];
             int m[4];
             for (int k = 0; k < 4; k++) {
                 v[k] = C2(Vin, I - 2 + k, J);
@@ -766,13 +790,13 @@ static void construct_ho_x(ofw_ctx *o, const double *Vin, double *OutL, double *
 }
 
 /* CONSTRUCT_HO_Y (fluxes.F:1646-1754) */
-static void construct_ho_y(ofw_ctx *o, const double *Vin, double *OutL, double *OutR) {
+static void construct_ho_y(ofw_ctx *o, const ofr *Vin, ofr *OutL, ofr *OutR) {
     const int Jb = o->Jbeg, Je = o->Jend, N = o->Nloc;
     OMP_FOR
     for (int I = o->Ibeg; I <= o->Iend; I++) {
-        double *Din = (double *)calloc((size_t)N + 1, sizeof(double));
+        ofr *Din = (ofr *)calloc((size_t)N + 1, sizeof(ofr));
         for (int J = Jb - 1; J <= Je + 2; J++) {
-            double v[4];
+            ofr v[4];
             int m[4];
             for (int k = 0; k < 4; k++) {
                 v[k] = C2(Vin, I, J - 2 + k);
@@ -791,7 +815,7 @@ static void construct_ho_y(ofw_ctx *o, const double *Vin, double *OutL, double *
 /* CONSTRUCTION_HO (fluxes.F:1324-1524), CARTESIAN, DISPERSION */
 static void construction_ho(ofw_ctx *o) {
     const int M = o->Mloc, N = o->Nloc, M1 = o->Mloc1, N1 = o->Nloc1;
-    const double g1 = o->p.gamma1, g3 = o->p.gamma3;
+    const ofr g1 = o->p.gamma1, g3 = o->p.gamma3;
     construct_ho_x(o, o->U, o->UxL, o->UxR);
     construct_ho_x(o, o->V, o->VxL, o->VxR);
     construct_ho_x(o, o->HU, o->HUxL, o->HUxR);
@@ -811,8 +835,8 @@ static void construction_ho(ofw_ctx *o) {
     for (int J = 1; J <= N; J++)
         for (int I = 1; I <= M1; I++) {
             /* MASK9u(Mloc1,:) = MASK9(Mloc,:) (fluxes.F:1333) */
-            double m9 = (double)C2(o->MASK9, I <= M ? I : M, J);
-            double EL = X2(o->EtaRxL, I, J), ER = X2(o->EtaRxR, I, J), Dx = X2(o->Depthx, I, J);
+            ofr m9 = (ofr)C2(o->MASK9, I <= M ? I : M, J);
+            ofr EL = X2(o->EtaRxL, I, J), ER = X2(o->EtaRxR, I, J), Dx = X2(o->Depthx, I, J);
             X2(o->PL, I, J) = X2(o->HUxL, I, J) + g1 * m9 * X2(o->HxL, I, J) * X2(o->U4xL, I, J);
             X2(o->PR, I, J) = X2(o->HUxR, I, J) + g1 * m9 * X2(o->HxR, I, J) * X2(o->U4xR, I, J);
             X2(o->FxL, I, J) = g3 * X2(o->PL, I, J) * (X2(o->UxL, I, J) + g1 * m9 * X2(o->U4xL, I, J)) +
@@ -842,8 +866,8 @@ static void construction_ho(ofw_ctx *o) {
     OMP_FOR
     for (int J = 1; J <= N1; J++)
         for (int I = 1; I <= M; I++) {
-            double m9 = (double)C2(o->MASK9, I, J <= N ? J : N);
-            double EL = Y2(o->EtaRyL, I, J), ER = Y2(o->EtaRyR, I, J), Dy = Y2(o->Depthy, I, J);
+            ofr m9 = (ofr)C2(o->MASK9, I, J <= N ? J : N);
+            ofr EL = Y2(o->EtaRyL, I, J), ER = Y2(o->EtaRyR, I, J), Dy = Y2(o->Depthy, I, J);
             Y2(o->QL, I, J) = Y2(o->HVyL, I, J) + g1 * m9 * Y2(o->HyL, I, J) * Y2(o->V4yL, I, J);
             Y2(o->QR, I, J) = Y2(o->HVyR, I, J) + g1 * m9 * Y2(o->HyR, I, J) * Y2(o->V4yR, I, J);
             Y2(o->GyL, I, J) = g3 * Y2(o->QL, I, J) * (Y2(o->VyL, I, J) + g1 * m9 * Y2(o->V4yL, I, J)) +
@@ -863,11 +887,11 @@ static void wave_speed(ofw_ctx *o) {
     OMP_FOR
     for (int J = 1 + NGHOST; J <= N - NGHOST; J++)
         for (int I = 1 + NGHOST; I <= M1 - NGHOST; I++) {
-            double UL = X2(o->UxL, I, J), UR = X2(o->UxR, I, J);
-            double SQR_PHI_L = sqrt(GRAV * fabs(X2(o->HxL, I, J)));
-            double SQR_PHI_R = sqrt(GRAV * fabs(X2(o->HxR, I, J)));
-            double SQR_PHI_S = 0.5 * (SQR_PHI_L + SQR_PHI_R) + 0.25 * (UL - UR);
-            double U_S = 0.5 * (UL + UR) + SQR_PHI_L - SQR_PHI_R;
+            ofr UL = X2(o->UxL, I, J), UR = X2(o->UxR, I, J);
+            ofr SQR_PHI_L = sqrt(GRAV * fabs(X2(o->HxL, I, J)));
+            ofr SQR_PHI_R = sqrt(GRAV * fabs(X2(o->HxR, I, J)));
+            ofr SQR_PHI_S = 0.5 * (SQR_PHI_L + SQR_PHI_R) + 0.25 * (UL - UR);
+            ofr U_S = 0.5 * (UL + UR) + SQR_PHI_L - SQR_PHI_R;
             X2(o->SxL, I, J) = dmin(UL - SQR_PHI_L, U_S - SQR_PHI_S);
             X2(o->SxR, I, J) = dmax(UR + SQR_PHI_R, U_S + SQR_PHI_S);
         }
@@ -894,11 +918,11 @@ static void wave_speed(ofw_ctx *o) {
     OMP_FOR
     for (int J = 1 + NGHOST; J <= N1 - NGHOST; J++)
         for (int I = 1 + NGHOST; I <= M - NGHOST; I++) {
-            double VL = Y2(o->VyL, I, J), VR = Y2(o->VyR, I, J);
-            double SQR_PHI_L = sqrt(GRAV * fabs(Y2(o->HyL, I, J)));
-            double SQR_PHI_R = sqrt(GRAV * fabs(Y2(o->HyR, I, J)));
-            double SQR_PHI_S = 0.5 * (SQR_PHI_L + SQR_PHI_R) + 0.25 * (VL - VR);
-            double U_S = 0.5 * (VL + VR) + SQR_PHI_L - SQR_PHI_R;
+            ofr VL = Y2(o->VyL, I, J), VR = Y2(o->VyR, I, J);
+            ofr SQR_PHI_L = sqrt(GRAV * fabs(Y2(o->HyL, I, J)));
+            ofr SQR_PHI_R = sqrt(GRAV * fabs(Y2(o->HyR, I, J)));
+            ofr SQR_PHI_S = 0.5 * (SQR_PHI_L + SQR_PHI_R) + 0.25 * (VL - VR);
+            ofr U_S = 0.5 * (VL + VR) + SQR_PHI_L - SQR_PHI_R;
             Y2(o->SyL, I, J) = dmin(VL - SQR_PHI_L, U_S - SQR_PHI_S);
             Y2(o->SyR, I, J) = dmax(VR + SQR_PHI_R, U_S + SQR_PHI_S);
         }
@@ -925,8 +949,8 @@ static void wave_speed(ofw_ctx *o) {
 }
 
 /* HLL (fluxes.F:171-194) on a whole array of n entries */
-static void hll(size_t n, const double *SL, const double *SR, const double *FL, const double *FR,
-                const double *UL, const double *UR, double *FOUT) {
+static void hll(size_t n, const ofr *SL, const ofr *SR, const ofr *FL, const ofr *FR,
+                const ofr *UL, const ofr *UR, ofr *FOUT) {
     OMP_FOR
     for (size_t k = 0; k < n; k++) {
         if (SL[k] >= ZERO) {
@@ -934,7 +958,7 @@ static void hll(size_t n, const double *SL, const double *SR, const double *FL, 
         } else if (SR[k] <= ZERO) {
             FOUT[k] = FR[k];
         } else {
-            double f = SR[k] * FL[k] - SL[k] * FR[k] + SL[k] * SR[k] * (UR[k] - UL[k]);
+            ofr f = SR[k] * FL[k] - SL[k] * FR[k] + SL[k] * SR[k] * (UR[k] - UL[k]);
             if (fabs(SR[k] - SL[k]) < SMALL) f = f / SMALL;
             else f = f / (SR[k] - SL[k]);
             FOUT[k] = f;
@@ -944,7 +968,7 @@ static void hll(size_t n, const double *SL, const double *SR, const double *FL, 
 
 /* BOUNDARY_CONDITION (bc.F:53-295), serial, no ABS/LEFT_BC_IRR/COUPLING */
 static void boundary_condition(ofw_ctx *o) {
-    const double g3 = o->p.gamma3;
+    const ofr g3 = o->p.gamma3;
     const int Ib = o->Ibeg, Ie = o->Iend, Jb = o->Jbeg, Je = o->Jend;
 #define PRESS(Xi, Deps) (0.5 * GRAV * ((Xi) * (Xi)*g3 + 2.0 * (Xi) * (Deps)))
     for (int J = Jb; J <= Je; J++) {
@@ -974,28 +998,28 @@ static void boundary_condition(ofw_ctx *o) {
             if (C2(o->MASK, I, J) < 1) {
                 X2(o->P, I, J) = ZERO;
                 if (I != Ib)
-                    X2(o->Fx, I, J) = PRESS(X2(o->EtaRxL, I, J), X2(o->Depthx, I, J)) * (double)C2(o->MASK, I - 1, J);
+                    X2(o->Fx, I, J) = PRESS(X2(o->EtaRxL, I, J), X2(o->Depthx, I, J)) * (ofr)C2(o->MASK, I - 1, J);
                 else
                     X2(o->Fx, I, J) = ZERO;
                 X2(o->Gx, I, J) = ZERO;
                 X2(o->P, I + 1, J) = ZERO;
                 if (I != Ie)
                     X2(o->Fx, I + 1, J) =
-                        PRESS(X2(o->EtaRxR, I + 1, J), X2(o->Depthx, I + 1, J)) * (double)C2(o->MASK, I + 1, J);
+                        PRESS(X2(o->EtaRxR, I + 1, J), X2(o->Depthx, I + 1, J)) * (ofr)C2(o->MASK, I + 1, J);
                 else
                     X2(o->Fx, I + 1, J) = ZERO;
                 X2(o->Gx, I + 1, J) = ZERO;
                 Y2(o->Q, I, J) = ZERO;
                 Y2(o->Fy, I, J) = ZERO;
                 if (J != Jb)
-                    Y2(o->Gy, I, J) = PRESS(Y2(o->EtaRyL, I, J), Y2(o->Depthy, I, J)) * (double)C2(o->MASK, I, J - 1);
+                    Y2(o->Gy, I, J) = PRESS(Y2(o->EtaRyL, I, J), Y2(o->Depthy, I, J)) * (ofr)C2(o->MASK, I, J - 1);
                 else
                     Y2(o->Gy, I, J) = ZERO;
                 Y2(o->Q, I, J + 1) = ZERO;
                 Y2(o->Fy, I, J + 1) = ZERO;
                 if (J != Je)
                     Y2(o->Gy, I, J + 1) =
-                        PRESS(Y2(o->EtaRyR, I, J + 1), Y2(o->Depthy, I, J + 1)) * (double)C2(o->MASK, I, J + 1);
+                        PRESS(Y2(o->EtaRyR, I, J + 1), Y2(o->Depthy, I, J + 1)) * (ofr)C2(o->MASK, I, J + 1);
                 else
                     Y2(o->Gy, I, J + 1) = ZERO;
             }
@@ -1021,13 +1045,13 @@ void ofw_fluxes(ofw_ctx *o) {
 /* SourceTerms (sources.F:56-548), CARTESIAN, no MANNING/METEO/VESSEL       */
 /* ------------------------------------------------------------------------ */
 static void wavemaker_mass(ofw_ctx *o) {
-    const double TIME = o->TIME;
+    const ofr TIME = o->TIME;
     if (o->p.wavemaker == 1) {
         /* WK_REG (sources.F:109-118) */
-        double AA = tanh(PI_SP / (o->p.time_ramp * o->p.tperiod) * TIME) * o->D_gen;
+        ofr AA = tanh(PI_SP / (o->p.time_ramp * o->p.tperiod) * TIME) * o->D_gen;
         for (int J = o->jlo; J <= o->jhi; J++)
             for (int I = o->ilo; I <= o->ihi; I++) {
-                double dxm = o->xmk_wk[I - 1] - o->p.xc_wk;
+                ofr dxm = o->xmk_wk[I - 1] - o->p.xc_wk;
                 C2(o->WaveMaker_Mass, I, J) =
                     AA * exp(-o->beta_gen * (dxm * dxm)) *
                     sin(o->rlamda * (o->ymk_wk[J - 1] - ZERO) - 2.0 * PI_SP / o->p.tperiod * TIME);
@@ -1035,8 +1059,8 @@ static void wavemaker_mass(ofw_ctx *o) {
     } else if (o->p.wavemaker == 2 && o->Cm) {
         /* JON_2D (sources.F:119-134) over the band */
         int nf = o->p.nfreq;
-        double AA = tanh(PI_SP / (o->p.time_ramp / o->p.freq_peak) * TIME);
-        double *BB = (double *)malloc(sizeof(double) * nf), *CC = (double *)malloc(sizeof(double) * nf);
+        ofr AA = tanh(PI_SP / (o->p.time_ramp / o->p.freq_peak) * TIME);
+        ofr *BB = (ofr *)malloc(sizeof(ofr) * nf), *CC = (ofr *)malloc(sizeof(ofr) * nf);
         for (int k = 0; k < nf; k++) {
             BB[k] = cos(o->omgn_ir[k] * TIME);
             CC[k] = sin(o->omgn_ir[k] * TIME);
@@ -1044,7 +1068,7 @@ static void wavemaker_mass(ofw_ctx *o) {
         int bw = o->ihi - o->ilo + 1, bh = o->jhi - o->jlo + 1;
         for (int J = o->jlo; J <= o->jhi; J++)
             for (int I = o->ilo; I <= o->ihi; I++) {
-                double s = ZERO;
+                ofr s = ZERO;
                 size_t b = (size_t)(I - o->ilo) + (size_t)(J - o->jlo) * bw;
                 for (int k = 0; k < nf; k++)
                     s = s + AA * (o->Cm[b + (size_t)k * bw * bh] * BB[k] + o->Sm[b + (size_t)k * bw * bh] * CC[k]);
@@ -1057,8 +1081,8 @@ static void wavemaker_mass(ofw_ctx *o) {
 
 void ofw_source_terms(ofw_ctx *o) {
     const int M = o->Mloc, N = o->Nloc;
-    const double DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
-    const double g1 = o->p.gamma1, g2 = o->p.gamma2;
+    const ofr DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
+    const ofr g1 = o->p.gamma1, g2 = o->p.gamma2;
     wavemaker_mass(o);
     /* nu_vis is default REAL (sources.F:69,190-224) */
     float *nu_vis = (float *)calloc((size_t)M * N, sizeof(float));
@@ -1069,12 +1093,12 @@ void ofw_source_terms(ofw_ctx *o) {
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++) {
-            double U = C2(o->U, I, J), V = C2(o->V, I, J);
-            double spd = sqrt(U * U + V * V);
-            double m9 = (double)C2(o->MASK9, I, J);
-            double FrcInsX = -C2(o->Cd, I, J) * U * spd;
-            double SX = GRAV * (C2(o->Eta, I, J)) / DX * (X2(o->Depthx, I + 1, J) - X2(o->Depthx, I, J)) *
-                            (double)C2(o->MASK, I, J) +
+            ofr U = C2(o->U, I, J), V = C2(o->V, I, J);
+            ofr spd = sqrt(U * U + V * V);
+            ofr m9 = (ofr)C2(o->MASK9, I, J);
+            ofr FrcInsX = -C2(o->Cd, I, J) * U * spd;
+            ofr SX = GRAV * (C2(o->Eta, I, J)) / DX * (X2(o->Depthx, I + 1, J) - X2(o->Depthx, I, J)) *
+                            (ofr)C2(o->MASK, I, J) +
                         FrcInsX +
                         g1 * m9 * dmax(C2(o->H, I, J), mdf) *
                             (U * 0.5 * (C2(o->U4, I + 1, J) - C2(o->U4, I - 1, J)) / DX +
@@ -1087,9 +1111,9 @@ void ofw_source_terms(ofw_ctx *o) {
                         C2(o->WaveMaker_Mass, I, J) * U;
             if (o->p.friction_sponge)
                 SX = SX - C2(o->CD_4_SPONGE, I, J) * U * spd * C2(o->Depth, I, J);
-            double FrcInsY = -C2(o->Cd, I, J) * V * spd;
-            double SY = GRAV * (C2(o->Eta, I, J)) / DY * (Y2(o->Depthy, I, J + 1) - Y2(o->Depthy, I, J)) *
-                            (double)C2(o->MASK, I, J) +
+            ofr FrcInsY = -C2(o->Cd, I, J) * V * spd;
+            ofr SY = GRAV * (C2(o->Eta, I, J)) / DY * (Y2(o->Depthy, I, J + 1) - Y2(o->Depthy, I, J)) *
+                            (ofr)C2(o->MASK, I, J) +
                         FrcInsY +
                         g1 * m9 * dmax(C2(o->H, I, J), mdf) *
                             (U * 0.5 * (C2(o->V4, I + 1, J) - C2(o->V4, I - 1, J)) / DX +
@@ -1105,12 +1129,12 @@ void ofw_source_terms(ofw_ctx *o) {
             if (o->p.viscosity_breaking) {
                 /* BreakSourceX/Y, non-PQ scheme (sources.F:428-456); the sums
                  * of two nu_vis values are float additions. */
-                double nxp = (double)(float)(NV(I + 1, J) + NV(I, J));
-                double nxm = (double)(float)(NV(I - 1, J) + NV(I, J));
-                double nyp = (double)(float)(NV(I, J + 1) + NV(I, J));
-                double nym = (double)(float)(NV(I, J - 1) + NV(I, J));
-                double HUc = C2(o->HU, I, J), HVc = C2(o->HV, I, J);
-                double BX = 0.5 / DX *
+                ofr nxp = (ofr)(float)(NV(I + 1, J) + NV(I, J));
+                ofr nxm = (ofr)(float)(NV(I - 1, J) + NV(I, J));
+                ofr nyp = (ofr)(float)(NV(I, J + 1) + NV(I, J));
+                ofr nym = (ofr)(float)(NV(I, J - 1) + NV(I, J));
+                ofr HUc = C2(o->HU, I, J), HVc = C2(o->HV, I, J);
+                ofr BX = 0.5 / DX *
                                 (nxp * 1.0 / DX * (C2(o->HU, I + 1, J) - HUc) -
                                  nxm * 1.0 / DX * (HUc - C2(o->HU, I - 1, J))) +
                             0.5 / DY *
@@ -1118,7 +1142,7 @@ void ofw_source_terms(ofw_ctx *o) {
                                  nym * 1.0 / DY * (HUc - C2(o->HU, I, J - 1)));
                 C2(o->BreakSourceX, I, J) = BX;
                 SX = SX + BX;
-                double BY = 0.5 / DX *
+                ofr BY = 0.5 / DX *
                                 (nxp * 1.0 / DX * (C2(o->HV, I + 1, J) - HVc) -
                                  nxm * 1.0 / DX * (HVc - C2(o->HV, I - 1, J))) +
                             0.5 / DY *
@@ -1138,11 +1162,11 @@ void ofw_source_terms(ofw_ctx *o) {
 /* tridiagonal solvers (tridiagnal.F:59-398), serial                        */
 /* ------------------------------------------------------------------------ */
 /* TRIDx_ser (tridiagnal.F:375-398) */
-static void tridx_ser(ofw_ctx *o, double *A, double *C, double *D, double *Z) {
+static void tridx_ser(ofw_ctx *o, ofr *A, ofr *C, ofr *D, ofr *Z) {
     OMP_FOR
     for (int JJ = o->Jbeg; JJ <= o->Jend; JJ++) {
         for (int II = o->Ibeg + 1; II <= o->Iend; II++) {
-            double a = C2(A, II, JJ);
+            ofr a = C2(A, II, JJ);
             if (a != ZERO) {
                 C2(C, II, JJ) = C2(C, II, JJ) / a / (1.0 / a - C2(C, II - 1, JJ));
                 C2(D, II, JJ) = (C2(D, II, JJ) / a - C2(D, II - 1, JJ)) / (1.0 / a - C2(C, II - 1, JJ));
@@ -1155,11 +1179,11 @@ static void tridx_ser(ofw_ctx *o, double *A, double *C, double *D, double *Z) {
 }
 
 /* TRIDy_ser (tridiagnal.F:338-361) */
-static void tridy_ser(ofw_ctx *o, double *A, double *C, double *D, double *Z) {
+static void tridy_ser(ofw_ctx *o, ofr *A, ofr *C, ofr *D, ofr *Z) {
     OMP_FOR
     for (int II = o->Ibeg; II <= o->Iend; II++) {
         for (int JJ = o->Jbeg + 1; JJ <= o->Jend; JJ++) {
-            double a = C2(A, II, JJ);
+            ofr a = C2(A, II, JJ);
             if (a != ZERO) {
                 C2(C, II, JJ) = C2(C, II, JJ) / a / (1.0 / a - C2(C, II, JJ - 1));
                 C2(D, II, JJ) = (C2(D, II, JJ) / a - C2(D, II, JJ - 1)) / (1.0 / a - C2(C, II, JJ - 1));
@@ -1172,14 +1196,14 @@ static void tridy_ser(ofw_ctx *o, double *A, double *C, double *D, double *Z) {
 }
 
 /* TRIDy_periodic (tridiagnal.F:59-325), serial branch */
-static void tridy_periodic(ofw_ctx *o, double *a, double *c, double *d, double *f) {
+static void tridy_periodic(ofw_ctx *o, ofr *a, ofr *c, ofr *d, ofr *f) {
     const int M = o->Mloc, N = o->Nloc, Jb = o->Jbeg, Je = o->Jend;
     const size_t nc = (size_t)M * N;
-    double *c1 = (double *)malloc(nc * sizeof(double));
-    double *y1 = (double *)calloc(nc, sizeof(double));
-    double *y2 = (double *)calloc(nc, sizeof(double));
-    double *a_beg = (double *)calloc((size_t)M + 1, sizeof(double));
-    double *c_end = (double *)calloc((size_t)M + 1, sizeof(double));
+    ofr *c1 = (ofr *)malloc(nc * sizeof(ofr));
+    ofr *y1 = (ofr *)calloc(nc, sizeof(ofr));
+    ofr *y2 = (ofr *)calloc(nc, sizeof(ofr));
+    ofr *a_beg = (ofr *)calloc((size_t)M + 1, sizeof(ofr));
+    ofr *c_end = (ofr *)calloc((size_t)M + 1, sizeof(ofr));
     for (int I = o->Ibeg; I <= o->Iend; I++) {
         a_beg[I] = C2(a, I, Jb);
         c_end[I] = C2(c, I, Je);
@@ -1190,7 +1214,7 @@ static void tridy_periodic(ofw_ctx *o, double *a, double *c, double *d, double *
         C2(a, i, Je) = C2(a, i, Je) / (1 + a_beg[i]);
         C2(d, i, Je) = C2(d, i, Je) / (1 + a_beg[i]);
     }
-    memcpy(c1, c, nc * sizeof(double));
+    memcpy(c1, c, nc * sizeof(ofr));
     tridy_ser(o, a, c1, d, y1);
     for (int i = o->Ibeg; i <= o->Iend; i++) {
         C2(d, i, Jb) = 1.0 / (1.0 + c_end[i]);
@@ -1199,7 +1223,7 @@ static void tridy_periodic(ofw_ctx *o, double *a, double *c, double *d, double *
     }
     tridy_ser(o, a, c, d, y2);
     for (int i = o->Ibeg; i <= o->Iend; i++) {
-        double beta = (c_end[i] * C2(y1, i, Jb) - a_beg[i] * C2(y1, i, Je)) /
+        ofr beta = (c_end[i] * C2(y1, i, Jb) - a_beg[i] * C2(y1, i, Je)) /
                       (1.0 - (c_end[i] * C2(y2, i, Jb) - a_beg[i] * C2(y2, i, Je)));
         for (int j = Jb; j <= Je; j++) C2(f, i, j) = C2(y1, i, j) + beta * C2(y2, i, j);
     }
@@ -1216,25 +1240,25 @@ static void tridy_periodic(ofw_ctx *o, double *a, double *c, double *d, double *
 static void get_eta_u_v_hu_hv(ofw_ctx *o) {
     const int M = o->Mloc, N = o->Nloc;
     const size_t nc = (size_t)M * N;
-    const double DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
-    const double g1 = o->p.gamma1, g3 = o->p.gamma3, b1 = o->b1, b2 = o->b2;
+    const ofr DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
+    const ofr g1 = o->p.gamma1, g3 = o->p.gamma3, b1 = o->b1, b2 = o->b2;
     for (size_t k = 0; k < nc; k++) o->H[k] = o->Eta[k] * g3 + o->Depth[k];
     if (o->p.dispersion) {
-        double *myA = (double *)calloc(nc, sizeof(double));
-        double *myC = (double *)calloc(nc, sizeof(double));
-        double *myD = (double *)calloc(nc, sizeof(double));
-        double *myF = (double *)calloc(nc, sizeof(double));
+        ofr *myA = (ofr *)calloc(nc, sizeof(ofr));
+        ofr *myC = (ofr *)calloc(nc, sizeof(ofr));
+        ofr *myD = (ofr *)calloc(nc, sizeof(ofr));
+        ofr *myF = (ofr *)calloc(nc, sizeof(ofr));
         OMP_FOR
         for (int J = o->Jbeg; J <= o->Jend; J++)
             for (int I = o->Ibeg; I <= o->Iend; I++) {
-                double dep = dmax(C2(o->Depth, I, J), mdf);
-                double depl = dmax(C2(o->Depth, I - 1, J), mdf);
-                double depr = dmax(C2(o->Depth, I + 1, J), mdf);
-                double m9 = (double)C2(o->MASK9, I, J);
-                double tmp1 = g1 * m9 * (b1 / 2.0 / DX / DX * dep * dep + b2 / DX / DX * depl * dep);
-                double tmp2 = 1.0 + g1 * m9 * (-b1 / DX / DX * dep * dep - 2.0 * b2 / DX / DX * dep * dep);
-                double tmp3 = g1 * m9 * (b1 / 2.0 / DX / DX * dep * dep + b2 / DX / DX * dep * depr);
-                double tmp4 = C2(o->Ubar, I, J) * (double)C2(o->MASK, I, J) / dmax(C2(o->H, I, J), mdf) +
+                ofr dep = dmax(C2(o->Depth, I, J), mdf);
+                ofr depl = dmax(C2(o->Depth, I - 1, J), mdf);
+                ofr depr = dmax(C2(o->Depth, I + 1, J), mdf);
+                ofr m9 = (ofr)C2(o->MASK9, I, J);
+                ofr tmp1 = g1 * m9 * (b1 / 2.0 / DX / DX * dep * dep + b2 / DX / DX * depl * dep);
+                ofr tmp2 = 1.0 + g1 * m9 * (-b1 / DX / DX * dep * dep - 2.0 * b2 / DX / DX * dep * dep);
+                ofr tmp3 = g1 * m9 * (b1 / 2.0 / DX / DX * dep * dep + b2 / DX / DX * dep * depr);
+                ofr tmp4 = C2(o->Ubar, I, J) * (ofr)C2(o->MASK, I, J) / dmax(C2(o->H, I, J), mdf) +
                               g1 * m9 * (-b1 / 2.0 * dep * dep * C2(o->Vxy, I, J) - b2 * dep * C2(o->DVxy, I, J));
                 if (tmp2 != 0.0 || C2(o->MASK, I, J) > 0) {
                     C2(myA, I, J) = tmp1 / tmp2;
@@ -1252,14 +1276,14 @@ static void get_eta_u_v_hu_hv(ofw_ctx *o) {
         OMP_FOR
         for (int I = o->Ibeg; I <= o->Iend; I++)
             for (int J = o->Jbeg; J <= o->Jend; J++) {
-                double dep = dmax(C2(o->Depth, I, J), mdf);
-                double depl = dmax(C2(o->Depth, I, J - 1), mdf);
-                double depr = dmax(C2(o->Depth, I, J + 1), mdf);
-                double m9 = (double)C2(o->MASK9, I, J);
-                double tmp1 = g1 * m9 * (b1 / 2.0 / DY / DY * dep * dep + b2 / DY / DY * depl * dep);
-                double tmp2 = 1.0 + g1 * m9 * (-b1 / DY / DY * dep * dep - 2.0 * b2 / DY / DY * dep * dep);
-                double tmp3 = g1 * m9 * (b1 / 2.0 / DY / DY * dep * dep + b2 / DY / DY * dep * depr);
-                double tmp4 = C2(o->Vbar, I, J) * (double)C2(o->MASK, I, J) / dmax(C2(o->H, I, J), mdf) +
+                ofr dep = dmax(C2(o->Depth, I, J), mdf);
+                ofr depl = dmax(C2(o->Depth, I, J - 1), mdf);
+                ofr depr = dmax(C2(o->Depth, I, J + 1), mdf);
+                ofr m9 = (ofr)C2(o->MASK9, I, J);
+                ofr tmp1 = g1 * m9 * (b1 / 2.0 / DY / DY * dep * dep + b2 / DY / DY * depl * dep);
+                ofr tmp2 = 1.0 + g1 * m9 * (-b1 / DY / DY * dep * dep - 2.0 * b2 / DY / DY * dep * dep);
+                ofr tmp3 = g1 * m9 * (b1 / 2.0 / DY / DY * dep * dep + b2 / DY / DY * dep * depr);
+                ofr tmp4 = C2(o->Vbar, I, J) * (ofr)C2(o->MASK, I, J) / dmax(C2(o->H, I, J), mdf) +
                               g1 * m9 * (-b1 / 2.0 * dep * dep * C2(o->Uxy, I, J) - b2 * dep * C2(o->DUxy, I, J));
                 if (tmp2 != 0.0 || C2(o->MASK, I, J) > 0) {
                     C2(myA, I, J) = tmp1 / tmp2;
@@ -1286,7 +1310,7 @@ static void get_eta_u_v_hu_hv(ofw_ctx *o) {
                 C2(o->V, I, J) = C2(o->Vbar, I, J) / dmax(C2(o->H, I, J), mdf);
             }
     }
-    const double fc = o->p.froude_cap;
+    const ofr fc = o->p.froude_cap;
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++) {
@@ -1298,14 +1322,14 @@ static void get_eta_u_v_hu_hv(ofw_ctx *o) {
                 C2(o->HU, I, J) = ZERO;
                 C2(o->HV, I, J) = ZERO;
             } else {
-                double Hm = dmax(C2(o->H, I, J), mdf);
-                double u = C2(o->U, I, J), v = C2(o->V, I, J);
+                ofr Hm = dmax(C2(o->H, I, J), mdf);
+                ofr u = C2(o->U, I, J), v = C2(o->V, I, J);
                 C2(o->HU, I, J) = Hm * u;
                 C2(o->HV, I, J) = Hm * v;
-                double Utotal = sqrt(u * u + v * v);
-                double Fr = sqrt(GRAV * Hm);
+                ofr Utotal = sqrt(u * u + v * v);
+                ofr Fr = sqrt(GRAV * Hm);
                 if (Utotal / Fr > fc) {
-                    double Utheta = atan2(v, u);
+                    ofr Utheta = atan2(v, u);
                     C2(o->U, I, J) = fc * Fr * cos(Utheta);
                     C2(o->V, I, J) = fc * Fr * sin(Utheta);
                     C2(o->HU, I, J) = C2(o->U, I, J) * Hm;
@@ -1314,26 +1338,26 @@ static void get_eta_u_v_hu_hv(ofw_ctx *o) {
             }
         }
     if (!o->p.dispersion) {
-        memcpy(o->Ubar, o->HU, nc * sizeof(double));
-        memcpy(o->Vbar, o->HV, nc * sizeof(double));
+        memcpy(o->Ubar, o->HU, nc * sizeof(ofr));
+        memcpy(o->Vbar, o->HV, nc * sizeof(ofr));
     }
 }
 
-static const double RK_ALPHA[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0};
-static const double RK_BETA[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
+static const ofr RK_ALPHA[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0};
+static const ofr RK_BETA[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
 
 void ofw_estimate_huv(ofw_ctx *o, int istage) {
-    const double DX = o->p.DX, DY = o->p.DY, DT = o->DT;
-    const double al = RK_ALPHA[istage - 1], be = RK_BETA[istage - 1];
+    const ofr DX = o->p.DX, DY = o->p.DY, DT = o->DT;
+    const ofr al = RK_ALPHA[istage - 1], be = RK_BETA[istage - 1];
     const int wk = o->p.wavemaker;
     /* for radiation stress (etauv_solver.F:94-101), with the H of the
      * stage's start */
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++) {
-            const double pc = 0.5 * (X2(o->P, I + 1, J) + X2(o->P, I, J));
-            const double qc = 0.5 * (Y2(o->Q, I, J + 1) + Y2(o->Q, I, J));
-            const double hm = dmax(C2(o->H, I, J), o->p.min_depth_frc);
+            const ofr pc = 0.5 * (X2(o->P, I + 1, J) + X2(o->P, I, J));
+            const ofr qc = 0.5 * (Y2(o->Q, I, J + 1) + Y2(o->Q, I, J));
+            const ofr hm = dmax(C2(o->H, I, J), o->p.min_depth_frc);
             C2(o->P_center, I, J) = pc;
             C2(o->Q_center, I, J) = qc;
             C2(o->U_davg, I, J) = pc / hm;
@@ -1342,16 +1366,16 @@ void ofw_estimate_huv(ofw_ctx *o, int istage) {
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++) {
-            double F_left = X2(o->P, I, J), F_right = X2(o->P, I + 1, J);
-            double F_bottom = Y2(o->Q, I, J), F_top = Y2(o->Q, I, J + 1);
-            double R1 = -1.0 / DX * (F_right * 1.0 + F_left * -1.0) - 1.0 / DY * (F_top * 1.0 + F_bottom * -1.0);
+            ofr F_left = X2(o->P, I, J), F_right = X2(o->P, I + 1, J);
+            ofr F_bottom = Y2(o->Q, I, J), F_top = Y2(o->Q, I, J + 1);
+            ofr R1 = -1.0 / DX * (F_right * 1.0 + F_left * -1.0) - 1.0 / DY * (F_top * 1.0 + F_bottom * -1.0);
             if (wk == 1 || wk == 2) {
-                double xmk = (I - o->Ibeg) * DX, ymk = (J - o->Jbeg) * DY;
+                ofr xmk = (I - o->Ibeg) * DX, ymk = (J - o->Jbeg) * DY;
                 if (fabs(xmk - o->p.xc_wk) < o->Width_WK && fabs(ymk - o->p.yc_wk) < o->p.ywidth_wk / 2.0)
                     R1 = R1 + C2(o->WaveMaker_Mass, I, J);
             }
             C2(o->Wsurf, I, J) = R1; /* etauv_solver.F:247 */
-            double eta = al * C2(o->Eta0, I, J) + be * (C2(o->Eta, I, J) + DT * R1);
+            ofr eta = al * C2(o->Eta0, I, J) + be * (C2(o->Eta, I, J) + DT * R1);
             if (o->p.eta_limiter) {
                 if (eta < o->p.trough_limit) eta = o->p.trough_limit;
                 if (eta > o->p.crest_limit) eta = o->p.crest_limit;
@@ -1361,10 +1385,10 @@ void ofw_estimate_huv(ofw_ctx *o, int istage) {
     OMP_FOR
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++) {
-            double R2 = -1.0 / DX * (X2(o->Fx, I + 1, J) * 1.0 + X2(o->Fx, I, J) * -1.0) -
+            ofr R2 = -1.0 / DX * (X2(o->Fx, I + 1, J) * 1.0 + X2(o->Fx, I, J) * -1.0) -
                         1.0 / DY * (Y2(o->Fy, I, J + 1) * 1.0 + Y2(o->Fy, I, J) * -1.0) + C2(o->SourceX, I, J);
             C2(o->Ubar, I, J) = al * C2(o->Ubar0, I, J) + be * (C2(o->Ubar, I, J) + DT * R2);
-            double R3 = -1.0 / DX * (X2(o->Gx, I + 1, J) * 1.0 + X2(o->Gx, I, J) * -1.0) -
+            ofr R3 = -1.0 / DX * (X2(o->Gx, I + 1, J) * 1.0 + X2(o->Gx, I, J) * -1.0) -
                         1.0 / DY * (Y2(o->Gy, I, J + 1) * 1.0 + Y2(o->Gy, I, J) * -1.0) + C2(o->SourceY, I, J);
             C2(o->Vbar, I, J) = al * C2(o->Vbar0, I, J) + be * (C2(o->Vbar, I, J) + DT * R3);
         }
@@ -1382,7 +1406,7 @@ void ofw_update_mask(ofw_ctx *o) {
     for (int J = o->Jbeg - 2; J <= o->Jend + 2; J++)
         for (int I = o->Ibeg - 2; I <= o->Iend + 2; I++) {
             if (C2(o->MASK_STRUC, I, J) == 1) {
-                double eta = C2(o->Eta, I, J);
+                ofr eta = C2(o->Eta, I, J);
                 if (C2(o->MASK, I, J) < 1) {
                     if (eta > -C2(o->Depth, I, J)) C2(MASKtmp, I, J) = 1;
                     if (C2(o->MASK, I - 1, J) == 1 && C2(o->Eta, I - 1, J) > eta) C2(MASKtmp, I, J) = 1;
@@ -1427,30 +1451,30 @@ void ofw_update_mask(ofw_ctx *o) {
 /* ------------------------------------------------------------------------ */
 void ofw_wave_breaking(ofw_ctx *o) {
     if (!o->p.show_breaking) return;
-    const double DX = o->p.DX, DY = o->p.DY, DT = o->DT, mdf = o->p.min_depth_frc;
-    const double Cbrk1 = o->p.cbrk1, Cbrk2 = o->p.cbrk2, T_brk = o->T_brk;
-    double *AGE = o->AGE;
+    const ofr DX = o->p.DX, DY = o->p.DY, DT = o->DT, mdf = o->p.min_depth_frc;
+    const ofr Cbrk1 = o->p.cbrk1, Cbrk2 = o->p.cbrk2, T_brk = o->T_brk;
+    ofr *AGE = o->AGE;
     for (int J = o->Jbeg - 1; J <= o->Jend + 1; J++)
         for (int I = o->Ibeg - 1; I <= o->Iend + 1; I++) {
-            double Hc = C2(o->H, I, J);
-            double tmp3 = sqrt(GRAV * dmax(mdf, Hc));
-            double tmp1 = Cbrk1 * tmp3;
-            double tmp2 = Cbrk2 * tmp3;
-            double ex = C2(o->ETAx, I, J), ey = C2(o->ETAy, I, J), et = C2(o->ETAT, I, J);
-            double ANGLE = atan2(-ey, -ex) * 180.0 / PI_SP;
-            double tmp4 = dmax(sqrt(ex * ex + ey * ey), SMALL);
-            double age = C2(AGE, I, J);
+            ofr Hc = C2(o->H, I, J);
+            ofr tmp3 = sqrt(GRAV * dmax(mdf, Hc));
+            ofr tmp1 = Cbrk1 * tmp3;
+            ofr tmp2 = Cbrk2 * tmp3;
+            ofr ex = C2(o->ETAx, I, J), ey = C2(o->ETAy, I, J), et = C2(o->ETAT, I, J);
+            ofr ANGLE = atan2(-ey, -ex) * 180.0 / PI_SP;
+            ofr tmp4 = dmax(sqrt(ex * ex + ey * ey), SMALL);
+            ofr age = C2(AGE, I, J);
             if (et >= tmp1 && (age == ZERO || age > T_brk)) {
                 C2(AGE, I, J) = DT;
             } else if (age > ZERO) {
                 C2(AGE, I, J) = age + DT;
             } else {
-                double Cc = dmin(fabs(et) / tmp4, sqrt(GRAV * fabs(Hc)));
-                double propxy = sqrt(DX * DX + DY * DY) / dmax(Cc, SMALL);
-                double propx = sqrt(DX * DX) / dmax(Cc, SMALL);
-                double propy = sqrt(DY * DY) / dmax(Cc, SMALL);
+                ofr Cc = dmin(fabs(et) / tmp4, sqrt(GRAV * fabs(Hc)));
+                ofr propxy = sqrt(DX * DX + DY * DY) / dmax(Cc, SMALL);
+                ofr propx = sqrt(DX * DX) / dmax(Cc, SMALL);
+                ofr propy = sqrt(DY * DY) / dmax(Cc, SMALL);
                 if (et >= tmp2) {
-                    double AGE1, AGE2, AGE3;
+                    ofr AGE1, AGE2, AGE3;
                     if (ANGLE >= ZERO && ANGLE < 90.0) {
                         AGE1 = C2(AGE, I - 1, J);
                         AGE2 = C2(AGE, I - 1, J - 1);
@@ -1485,26 +1509,26 @@ void ofw_wave_breaking(ofw_ctx *o) {
                     }
                 }
             }
-            double xmk = (I - o->Ibeg) * DX, ymk = (J - o->Jbeg) * DY;
-            double a = C2(AGE, I, J);
+            ofr xmk = (I - o->Ibeg) * DX, ymk = (J - o->Jbeg) * DY;
+            ofr a = C2(AGE, I, J);
             if (fabs(xmk - o->p.xc_wk) < o->Width_WK && fabs(ymk - o->p.yc_wk) < o->p.ywidth_wk / 2.0) {
                 if (et > dmin(tmp2, o->p.wavemaker_cbrk * tmp3)) {
-                    double cap1 = 1.0 * (dmax(C2(o->Depth, I, J), mdf) + C2(o->Eta, I, J));
+                    ofr cap1 = 1.0 * (dmax(C2(o->Depth, I, J), mdf) + C2(o->Eta, I, J));
                     C2(o->nu_break, I, J) = cap1 * o->p.wavemaker_cbrk * tmp3 + o->p.nu_bkg;
                 } else {
                     C2(o->nu_break, I, J) = ZERO + o->p.nu_bkg;
                 }
             } else {
                 if (a > ZERO && a < T_brk && et > tmp2) {
-                    double cap1 = 1.0 * (dmax(C2(o->Depth, I, J), mdf) + C2(o->Eta, I, J));
+                    ofr cap1 = 1.0 * (dmax(C2(o->Depth, I, J), mdf) + C2(o->Eta, I, J));
                     C2(o->nu_break, I, J) = cap1 * tmp2 + o->p.nu_bkg;
                     /* roller and undertow (breaker.F:316-339); 0.45 is a
                      * default-REAL literal, 0.1638 a _SP one */
-                    double C1 = dmax(fabs(et) / tmp4, sqrt(GRAV * fabs(Hc)));
-                    double R = fabs((double)0.45f * et / dmax(C1, SMALL));
-                    R = dmin(R, (double)0.1638f);
-                    double u = C2(o->U, I, J), v = C2(o->V, I, J);
-                    double rf = fabs(C1 - sqrt(u * u + v * v)) * R * (C2(o->Eta, I, J) - C2(o->ETAmean, I, J));
+                    ofr C1 = dmax(fabs(et) / tmp4, sqrt(GRAV * fabs(Hc)));
+                    ofr R = fabs((ofr)0.45f * et / dmax(C1, SMALL));
+                    R = dmin(R, (ofr)0.1638f);
+                    ofr u = C2(o->U, I, J), v = C2(o->V, I, J);
+                    ofr rf = fabs(C1 - sqrt(u * u + v * v)) * R * (C2(o->Eta, I, J) - C2(o->ETAmean, I, J));
                     C2(o->ROLLER_FLUX, I, J) = rf;
                     C2(o->UNDERTOW_U, I, J) = -rf * cos(ANGLE * PI_SP / 180.0);
                     C2(o->UNDERTOW_V, I, J) = -rf * sin(ANGLE * PI_SP / 180.0);
@@ -1520,7 +1544,7 @@ void ofw_sponge_damping(ofw_ctx *o) {
     const size_t nc = (size_t)o->Mloc * o->Nloc;
     OMP_FOR
     for (size_t k = 0; k < nc; k++) {
-        if ((double)o->MASK[k] > ZERO) o->Eta[k] = o->Eta[k] / o->SPONGE[k];
+        if ((ofr)o->MASK[k] > ZERO) o->Eta[k] = o->Eta[k] / o->SPONGE[k];
         o->U[k] = o->U[k] / o->SPONGE[k];
         o->V[k] = o->V[k] / o->SPONGE[k];
     }
@@ -1528,11 +1552,11 @@ void ofw_sponge_damping(ofw_ctx *o) {
 
 /* CHECK_BLOWUP (misc.F:394-433): 1 if max|Eta| (interior) > EtaBlowVal */
 int ofw_check_blowup(ofw_ctx *o) {
-    double mx = 0.0;
+    ofr mx = 0.0;
     int nan = 0;
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++) {
-            double a = fabs(C2(o->Eta, I, J));
+            ofr a = fabs(C2(o->Eta, I, J));
             if (a != a) nan = 1;
             if (a > mx) mx = a;
         }
@@ -1546,15 +1570,15 @@ void ofw_max_min_property(ofw_ctx *o) {
     const size_t nc = (size_t)o->Mloc * o->Nloc;
     for (size_t k = 0; k < nc; k++) {
         if (o->MASK[k] <= 0) continue;
-        const double eta = o->Eta[k], u = o->U[k], v = o->V[k];
+        const ofr eta = o->Eta[k], u = o->U[k], v = o->V[k];
         if (eta > o->HeightMax[k]) o->HeightMax[k] = eta;
         if (o->p.track_hmin && eta < o->HeightMin[k]) o->HeightMin[k] = eta;
         if (o->p.track_umax) {
-            const double maxv = sqrt(u * u + v * v);
+            const ofr maxv = sqrt(u * u + v * v);
             if (maxv > o->VelocityMax[k]) o->VelocityMax[k] = maxv;
         }
         if (o->p.track_mfmax) {
-            const double maxv = (u * u + v * v) * (o->H[k]);
+            const ofr maxv = (u * u + v * v) * (o->H[k]);
             if (maxv > o->MomentumFluxMax[k]) o->MomentumFluxMax[k] = maxv;
         }
     }
@@ -1563,10 +1587,10 @@ void ofw_max_min_property(ofw_ctx *o) {
 /* the radiation-stress, momentum-flux and breaking-dissipation sums of one
  * cell (mixing.F:156-167 and 270-281), with the ETAmean and U_davg_mean the
  * caller's branch has at that point */
-static void radiation_sums(ofw_ctx *o, size_t k, double DT) {
-    const double ud = o->U_davg[k] - o->U_davg_mean[k], vd = o->V_davg[k] - o->V_davg_mean[k];
-    const double hd = o->Eta[k] - o->ETAmean[k] + o->Depth[k];
-    const double u = o->U[k], v = o->V[k];
+static void radiation_sums(ofw_ctx *o, size_t k, ofr DT) {
+    const ofr ud = o->U_davg[k] - o->U_davg_mean[k], vd = o->V_davg[k] - o->V_davg_mean[k];
+    const ofr hd = o->Eta[k] - o->ETAmean[k] + o->Depth[k];
+    const ofr u = o->U[k], v = o->V[k];
     o->U_davg_sum[k] = o->U_davg[k] * DT + o->U_davg_sum[k];
     o->V_davg_sum[k] = o->V_davg[k] * DT + o->V_davg_sum[k];
     o->P_sum[k] = o->P_center[k] * DT + o->P_sum[k];
@@ -1592,12 +1616,12 @@ static void radiation_sums(ofw_ctx *o, size_t k, double DT) {
 void ofw_mixing_stuff(ofw_ctx *o) {
     if (!(o->TIME >= o->p.steady_time)) return;
     const size_t nc = (size_t)o->Mloc * o->Nloc;
-    const double DT = o->DT;
+    const ofr DT = o->DT;
     o->T_sum = o->T_sum + DT;
     if (o->T_sum >= o->p.t_intv_mean) {
-        const double Ts = o->T_sum;
+        const ofr Ts = o->T_sum;
         for (size_t k = 0; k < nc; k++) {
-            const double d = o->Eta[k] - o->ETAmean[k];
+            const ofr d = o->Eta[k] - o->ETAmean[k];
             o->ETA2sum[k] = d * d * DT + o->ETA2sum[k];
             o->ETA2mean[k] = o->ETA2sum[k] / Ts;
             o->Usum[k] = o->U[k] * DT + o->Usum[k];
@@ -1620,8 +1644,8 @@ void ofw_mixing_stuff(ofw_ctx *o) {
             o->BreakDissX[k] = o->BreakDissX_sum[k] / Ts;
             o->BreakDissY[k] = o->BreakDissY_sum[k] / Ts;
         }
-        const double DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
-        const double g98 = (double)9.80f, g49 = (double)(0.5f * 9.80f);
+        const ofr DX = o->p.DX, DY = o->p.DY, mdf = o->p.min_depth_frc;
+        const ofr g98 = (ofr)9.80f, g49 = (ofr)(0.5f * 9.80f);
         for (int J = o->Jbeg; J <= o->Jend; J++)
             for (int I = o->Ibeg; I <= o->Iend; I++) {
 #define RX(a) ((C2(o->a, I + 1, J) - C2(o->a, I - 1, J)) / 2.0 / DX)
@@ -1652,7 +1676,7 @@ void ofw_mixing_stuff(ofw_ctx *o) {
 #undef HM
             }
         o->T_sum = o->T_sum - o->p.t_intv_mean;
-        const double c4 = (double)(float)4.004;
+        const ofr c4 = (ofr)(float)4.004;
         for (size_t k = 0; k < nc; k++) {
             o->Usum[k] = 0.0;
             o->Vsum[k] = 0.0;
@@ -1672,18 +1696,18 @@ void ofw_mixing_stuff(ofw_ctx *o) {
             o->Usum[k] = o->U[k] * DT + o->Usum[k];
             o->Vsum[k] = o->V[k] * DT + o->Vsum[k];
             o->ETAsum[k] = o->Eta[k] * DT + o->ETAsum[k];
-            const double d = o->Eta[k] - o->ETAmean[k];
+            const ofr d = o->Eta[k] - o->ETAmean[k];
             o->ETA2sum[k] = d * d * DT + o->ETA2sum[k];
             radiation_sums(o, k, DT);
-            const double eta = o->Eta[k];
+            const ofr eta = o->Eta[k];
             if (eta > o->Emax[k]) o->Emax[k] = eta;
             if (eta < o->Emin[k]) o->Emin[k] = eta;
-            const double tmpe = eta - o->ETAmean[k];
-            const double tmp0 = o->Eta0[k] - o->ETAmean[k];
+            const ofr tmpe = eta - o->ETAmean[k];
+            const ofr tmp0 = o->Eta0[k] - o->ETAmean[k];
             if (tmpe > tmp0 && tmpe * tmp0 <= 0.0) {
                 o->Num_Zero_Up[k] = o->Num_Zero_Up[k] + 1;
                 if (o->Num_Zero_Up[k] >= 2) {
-                    const double h = o->Emax[k] - o->Emin[k];
+                    const ofr h = o->Emax[k] - o->Emin[k];
                     o->HavgSum[k] = (o->HavgSum[k] + o->Emax[k]) - o->Emin[k];  /* left to right */
                     o->HrmsSum[k] = o->HrmsSum[k] + h * h;
                 }
@@ -1707,13 +1731,13 @@ int ofw_end_step(ofw_ctx *o) {
 /* ------------------------------------------------------------------------ */
 void ofw_begin_step(ofw_ctx *o) {
     const size_t nc = (size_t)o->Mloc * o->Nloc;
-    memcpy(o->Eta0, o->Eta, nc * sizeof(double));
-    memcpy(o->Ubar0, o->Ubar, nc * sizeof(double));
-    memcpy(o->Vbar0, o->Vbar, nc * sizeof(double));
+    memcpy(o->Eta0, o->Eta, nc * sizeof(ofr));
+    memcpy(o->Ubar0, o->Ubar, nc * sizeof(ofr));
+    memcpy(o->Vbar0, o->Vbar, nc * sizeof(ofr));
     ofw_exchange(o);
     ofw_estimate_dt(o);
-    memcpy(o->U0, o->U, nc * sizeof(double));
-    memcpy(o->V0, o->V, nc * sizeof(double));
+    memcpy(o->U0, o->U, nc * sizeof(ofr));
+    memcpy(o->V0, o->V, nc * sizeof(ofr));
 }
 
 void ofw_stage(ofw_ctx *o, int istage) {
@@ -1741,8 +1765,8 @@ static void jon_spectrum(ofw_ctx *o);
 static void jon_cm_sm(ofw_ctx *o);
 
 /* integer power as gfortran's run-time helper: square-and-multiply */
-static double powi(double x, int n) {
-    double r = 1.0;
+static ofr powi(ofr x, int n) {
+    ofr r = 1.0;
     int neg = n < 0;
     unsigned u = neg ? (unsigned)(-n) : (unsigned)n;
     while (u) {
@@ -1756,18 +1780,18 @@ static double powi(double x, int n) {
 /* CALCULATE_SPONGE (sponge.F:591-767), serial */
 static void calculate_sponge(ofw_ctx *o) {
     const int M = o->Mloc, N = o->Nloc;
-    const double R = o->p.r_sponge, A = o->p.a_sponge;
+    const ofr R = o->p.r_sponge, A = o->p.a_sponge;
     const size_t nc = (size_t)M * N;
-    double *t1 = (double *)calloc(nc, sizeof(double));
-    double *t2 = (double *)calloc(nc, sizeof(double));
-    double *S = o->SPONGE;
-    const double floor_ = pow(A, powi(R, 50));
+    ofr *t1 = (ofr *)calloc(nc, sizeof(ofr));
+    ofr *t2 = (ofr *)calloc(nc, sizeof(ofr));
+    ofr *S = o->SPONGE;
+    const ofr floor_ = pow(A, powi(R, 50));
     if (o->p.sponge_west > ZERO) {
         int Iw = (int)(o->p.sponge_west / o->p.DX) + NGHOST;
         for (int J = 1; J <= N; J++)
             for (int I = 1; I <= M; I++) {
-                double lim = C2(S, I, J) > 1.0 ? C2(S, I, J) : 1.0;
-                double ri = powi(R, 50 * (I - 1) / (Iw - 1));
+                ofr lim = C2(S, I, J) > 1.0 ? C2(S, I, J) : 1.0;
+                ofr ri = powi(R, 50 * (I - 1) / (Iw - 1));
                 C2(t1, I, J) = dmax(pow(A, ri), lim);
             }
     }
@@ -1775,8 +1799,8 @@ static void calculate_sponge(ofw_ctx *o) {
         int Iw = (int)(o->p.sponge_east / o->p.DX) + NGHOST;
         for (int J = 1; J <= N; J++)
             for (int I = 1; I <= M; I++) {
-                double lim = C2(S, I, J) > 1.0 ? C2(S, I, J) : 1.0;
-                double ri = powi(R, 50 * (M - I) / (Iw - 1));
+                ofr lim = C2(S, I, J) > 1.0 ? C2(S, I, J) : 1.0;
+                ofr ri = powi(R, 50 * (M - I) / (Iw - 1));
                 C2(t2, I, J) = dmax(pow(A, ri), lim);
             }
     }
@@ -1788,8 +1812,8 @@ static void calculate_sponge(ofw_ctx *o) {
         int Iw = (int)(o->p.sponge_south / o->p.DY) + NGHOST;
         for (int I = 1; I <= M; I++)
             for (int J = 1; J <= N; J++) {
-                double lim = C2(S, I, J) > 1.0 ? C2(S, I, J) : 1.0;
-                double ri = powi(R, 50 * (J - 1) / (Iw - 1));
+                ofr lim = C2(S, I, J) > 1.0 ? C2(S, I, J) : 1.0;
+                ofr ri = powi(R, 50 * (J - 1) / (Iw - 1));
                 C2(t1, I, J) = dmax(pow(A, ri), lim);
             }
     }
@@ -1797,8 +1821,8 @@ static void calculate_sponge(ofw_ctx *o) {
         int Iw = (int)(o->p.sponge_north / o->p.DY) + NGHOST;
         for (int I = 1; I <= M; I++)
             for (int J = 1; J <= N; J++) {
-                double lim = C2(S, I, J) > 1.0 ? C2(S, I, J) : 1.0;
-                double ri = powi(R, 50 * (N - J) / (Iw - 1));
+                ofr lim = C2(S, I, J) > 1.0 ? C2(S, I, J) : 1.0;
+                ofr ri = powi(R, 50 * (N - J) / (Iw - 1));
                 C2(t2, I, J) = dmax(pow(A, ri), lim);
             }
     }
@@ -1813,23 +1837,23 @@ static void calculate_sponge(ofw_ctx *o) {
 /* WK_WAVEMAKER_REGULAR_WAVE (wavemaker.F:2369-2405); default-REAL literals
  * widened from float. */
 static void wk_regular(ofw_ctx *o) {
-    const double F1_3 = (double)(1.0f / 3.0f);
+    const ofr F1_3 = (ofr)(1.0f / 3.0f);
     double theta = o->p.theta_wk * PI_SP / 180.0;
-    double alpha = (double)(float)-0.39;
-    double alpha1 = alpha + F1_3;
+    ofr alpha = (ofr)(float)-0.39;
+    ofr alpha1 = alpha + F1_3;
     double omgn = 2.0 * PI_SP / o->p.tperiod;
-    double h_gen = o->p.dep_wk;
-    double tb = omgn * omgn * h_gen / GRAV;
-    double tc = 1.0 + tb * alpha;
-    double wkn = sqrt((tc - sqrt(tc * tc - 4.0 * alpha1 * tb)) / (2.0 * alpha1)) / h_gen;
+    ofr h_gen = o->p.dep_wk;
+    ofr tb = omgn * omgn * h_gen / GRAV;
+    ofr tc = 1.0 + tb * alpha;
+    ofr wkn = sqrt((tc - sqrt(tc * tc - 4.0 * alpha1 * tb)) / (2.0 * alpha1)) / h_gen;
     double C_phase = 1.0 / wkn / o->p.tperiod * 2.0 * PI_SP;
-    double wave_length = C_phase * o->p.tperiod;
+    ofr wave_length = C_phase * o->p.tperiod;
     o->rlamda = wkn * sin(theta);
     o->Width_WK = o->p.delta_wk * wave_length / 2.0;
     o->beta_gen = 80.0 / (o->p.delta_wk * o->p.delta_wk) / (wave_length * wave_length);
-    double rl_gen = wkn * cos(theta);
-    double rI = sqrt((double)(float)3.14159 / o->beta_gen) * exp(-(rl_gen * rl_gen) / 4.0 / o->beta_gen);
-    double wh = wkn * h_gen;
+    ofr rl_gen = wkn * cos(theta);
+    ofr rI = sqrt((ofr)(float)3.14159 / o->beta_gen) * exp(-(rl_gen * rl_gen) / 4.0 / o->beta_gen);
+    ofr wh = wkn * h_gen;
     o->D_gen = 2.0 * o->p.amp_wk * cos(theta) *
                (omgn * omgn - alpha1 * GRAV * powi(wkn, 4) * powi(h_gen, 3)) /
                (omgn * wkn * rI * (1.0 - alpha * (wh * wh)));
@@ -1838,9 +1862,9 @@ static void wk_regular(ofw_ctx *o) {
 int ofw_init(ofw_ctx *o) {
     const int M = o->Mloc, N = o->Nloc, M1 = o->Mloc1, N1 = o->Nloc1;
     const size_t nc = (size_t)M * N;
-    const double mdf = o->p.min_depth_frc, g1 = o->p.gamma1, g3 = o->p.gamma3;
+    const ofr mdf = o->p.min_depth_frc, g1 = o->p.gamma1, g3 = o->p.gamma3;
     /* dispersion coefficients (init.F:656-664) */
-    double br = o->p.beta_ref;
+    ofr br = o->p.beta_ref;
     o->a1 = br * br / 2.0 - 1.0 / 6.0;
     o->a2 = br + 1.0 / 2.0;
     o->b1 = br * br;
@@ -1867,7 +1891,7 @@ int ofw_init(ofw_ctx *o) {
         Y2(o->Depthy, I, N1) = 0.5 * (3.0 * C2(o->Depth, I, N) - C2(o->Depth, I, N - 1));
     }
     /* EtaBlowVal (init.F:847) */
-    double mx = 0.0;
+    ofr mx = 0.0;
     for (int J = o->Jbeg; J <= o->Jend; J++)
         for (int I = o->Ibeg; I <= o->Iend; I++) mx = dmax(mx, fabs(C2(o->Depth, I, J)));
     o->EtaBlowVal = 100.0 * mx;
@@ -1960,7 +1984,7 @@ void ofw_set_phases(ofw_ctx *o, const double *phi1) {
 }
 
 /* theta of direction ktheta (1-based), clamped to +-pi/2 (wavemaker.F:2211-2216) */
-static double jon_theta(const ofw_params *p, int ktheta) {
+static ofr jon_theta(const ofw_params *p, int ktheta) {
     double theta = -PI_SP / 3.0 + p->theta_peak * PI_SP / 180.0 +
                    2.0 / 3.0 * PI_SP / ((double)(float)p->ntheta - 1.0) * ((double)(float)ktheta - 1.0);
     if (theta > 0.5 * PI_SP) theta = 0.5 * PI_SP;
@@ -1971,10 +1995,10 @@ static double jon_theta(const ofw_params *p, int ktheta) {
 static void jon_spectrum(ofw_ctx *o) {
     const ofw_params *p = &o->p;
     const int mf = p->nfreq, mt = p->ntheta;
-    const double h_gen = p->dep_wk, fm = p->freq_peak, delta = p->delta_wk;
-    double *freq = (double *)calloc((size_t)mf, sizeof(double));
-    double *EB = (double *)calloc((size_t)mf, sizeof(double));
-    double *AG = (double *)calloc((size_t)mt, sizeof(double));
+    const ofr h_gen = p->dep_wk, fm = p->freq_peak, delta = p->delta_wk;
+    ofr *freq = (ofr *)calloc((size_t)mf, sizeof(ofr));
+    ofr *EB = (ofr *)calloc((size_t)mf, sizeof(ofr));
+    ofr *AG = (ofr *)calloc((size_t)mt, sizeof(ofr));
     free(o->omgn_ir);
     free(o->jon_dgen);
     free(o->jon_rlamda);
@@ -1983,16 +2007,16 @@ static void jon_spectrum(ofw_ctx *o) {
     o->jon_dgen = (double *)calloc((size_t)mf * mt, sizeof(double));
     o->jon_rlamda = (double *)calloc((size_t)mf * mt, sizeof(double));
     o->jon_betagen = (double *)calloc((size_t)mf, sizeof(double));
-    double df = (p->freq_max - p->freq_min) / (mf - 1.0);
-    double Ef = ZERO;
+    ofr df = (p->freq_max - p->freq_min) / (mf - 1.0);
+    ofr Ef = ZERO;
     for (int kff = 1; kff <= mf; kff++) {
-        double f = p->freq_min + (kff - 1) * df;
+        ofr f = p->freq_min + (kff - 1) * df;
         freq[kff - 1] = f;
         /* JON spectra use phi = 1 (wavemaker.F:2164-2166) */
-        double phi = 1.0;
-        double sigma_spec = 0.07;
+        ofr phi = 1.0;
+        ofr sigma_spec = 0.07;
         if (f > fm) sigma_spec = 0.09;
-        double r = f / fm - 1.0;
+        ofr r = f / fm - 1.0;
         double Etma = GRAV * GRAV * powi(f, -5) * powi(2.0 * PI_SP, -4) * phi *
                       exp(-5.0 / 4.0 * powi(f / fm, -4)) *
                       pow(p->gamma_tma, exp(-(r * r) / (2.0 * (sigma_spec * sigma_spec))));
@@ -2004,9 +2028,9 @@ static void jon_spectrum(ofw_ctx *o) {
     } else if (p->spreading == 1) {
         /* cos^2s((theta - theta_p)/2), normalised to unit sum like the
          * reference's AG (an extension: the reference has no cos^2s) */
-        double sumAG = 0.0;
+        ofr sumAG = 0.0;
         for (int kt = 1; kt <= mt; kt++) {
-            double th = jon_theta(p, kt);
+            ofr th = jon_theta(p, kt);
             double c = cos((th - p->theta_peak * PI_SP / 180.0) / 2.0);
             AG[kt - 1] = pow(fabs(c), 2.0 * p->spread_s);
             sumAG = sumAG + AG[kt - 1];
@@ -2015,12 +2039,12 @@ static void jon_spectrum(ofw_ctx *o) {
     } else {
         double sigma_theta = p->sigma_theta * PI_SP / 180.0;
         int N_spec = (int)(20.0 / sigma_theta);
-        double sumAG = 0.0;
+        ofr sumAG = 0.0;
         for (int kt = 1; kt <= mt; kt++) {
-            double th = jon_theta(p, kt);
+            ofr th = jon_theta(p, kt);
             double ag = 1.0 / (2.0 * PI_SP);
             for (int k_n = 1; k_n <= N_spec; k_n++) {
-                double a = (double)(float)k_n * sigma_theta;
+                ofr a = (ofr)(float)k_n * sigma_theta;
                 ag = ag + (1.0 / PI_SP) * exp(-0.5 * (a * a)) * cos(k_n * (th - p->theta_peak * PI_SP / 180.0));
             }
             AG[kt - 1] = ag;
@@ -2028,20 +2052,20 @@ static void jon_spectrum(ofw_ctx *o) {
         }
         for (int kt = 0; kt < mt; kt++) AG[kt] = fabs(AG[kt] / sumAG);
     }
-    double alpha_spec = p->hmo * p->hmo / 16.0 / Ef;
-    const double alpha = -0.39, alpha1 = alpha + 1.0 / 3.0;
-    double wave_length = 0.0;
+    ofr alpha_spec = p->hmo * p->hmo / 16.0 / Ef;
+    const ofr alpha = -0.39, alpha1 = alpha + 1.0 / 3.0;
+    ofr wave_length = 0.0;
     for (int kf = 1; kf <= mf; kf++)
         for (int kt = 1; kt <= mt; kt++) {
-            double Hmo_each = 4.0 * sqrt((alpha_spec * EB[kf - 1] * AG[kt - 1]));
-            double ap = Hmo_each / sqrt(2.0) / 2.0;
+            ofr Hmo_each = 4.0 * sqrt((alpha_spec * EB[kf - 1] * AG[kt - 1]));
+            ofr ap = Hmo_each / sqrt(2.0) / 2.0;
             double theta = (mt == 1) ? p->theta_peak * PI_SP / 180.0 : jon_theta(p, kt);
             double omgn = 2.0 * PI_SP * freq[kf - 1];
             o->omgn_ir[kf - 1] = omgn;
-            double tb = omgn * omgn * h_gen / GRAV;
-            double tc = 1.0 + tb * alpha;
-            double wkn = sqrt((tc - sqrt(tc * tc - 4.0 * alpha1 * tb)) / (2.0 * alpha1)) / h_gen;
-            double C_phase;
+            ofr tb = omgn * omgn * h_gen / GRAV;
+            ofr tc = 1.0 + tb * alpha;
+            ofr wkn = sqrt((tc - sqrt(tc * tc - 4.0 * alpha1 * tb)) / (2.0 * alpha1)) / h_gen;
+            ofr C_phase;
             if (wkn == 0.0) {
                 wkn = SMALL;
                 C_phase = sqrt(GRAV * h_gen);
@@ -2053,7 +2077,7 @@ static void jon_spectrum(ofw_ctx *o) {
             if (p->periodic) {
                 /* snap the direction to a y-periodic wavenumber
                  * (wavemaker.F:2262-2296) */
-                double tmp1 = wkn, tmp2 = 0.0, tmp3 = ZERO;
+                ofr tmp1 = wkn, tmp2 = 0.0, tmp3 = ZERO;
                 int I = 0;
                 if (theta > ZERO) {
                     while (tmp3 < theta) {
@@ -2079,11 +2103,11 @@ static void jon_spectrum(ofw_ctx *o) {
             }
             size_t k2 = (size_t)(kf - 1) + (size_t)(kt - 1) * mf;
             o->jon_rlamda[k2] = wkn * sin(theta);
-            double bg = 80.0 / (delta * delta) / (wave_length * wave_length);
+            ofr bg = 80.0 / (delta * delta) / (wave_length * wave_length);
             o->jon_betagen[kf - 1] = bg;
-            double rl_gen = wkn * cos(theta);
+            ofr rl_gen = wkn * cos(theta);
             double rI = sqrt(PI_SP / bg) * exp(-(rl_gen * rl_gen) / 4.0 / bg);
-            double wh = wkn * h_gen;
+            ofr wh = wkn * h_gen;
             o->jon_dgen[k2] = 2.0 * ap * cos(theta) *
                               (omgn * omgn - alpha1 * GRAV * powi(wkn, 4) * powi(h_gen, 3)) /
                               (omgn * wkn * rI * (1.0 - alpha * (wh * wh)));
@@ -2109,12 +2133,12 @@ static void jon_cm_sm(ofw_ctx *o) {
         for (int I = o->ilo; I <= o->ihi; I++) {
             size_t b = (size_t)(I - o->ilo) + (size_t)(J - o->jlo) * bw;
             for (int kf = 1; kf <= mf; kf++) {
-                double cm = ZERO, sm = ZERO;
+                ofr cm = ZERO, sm = ZERO;
                 for (int kt = 1; kt <= mt; kt++) {
                     size_t k2 = (size_t)(kf - 1) + (size_t)(kt - 1) * mf;
-                    double dxm = (I - o->Ibeg) * o->p.DX - o->p.xc_wk;
-                    double amp = o->jon_dgen[k2] * exp(-o->jon_betagen[kf - 1] * (dxm * dxm));
-                    double arg = o->jon_rlamda[k2] * ((J - o->Jbeg) * o->p.DY - ZERO) + o->phi1[k2];
+                    ofr dxm = (I - o->Ibeg) * o->p.DX - o->p.xc_wk;
+                    ofr amp = o->jon_dgen[k2] * exp(-o->jon_betagen[kf - 1] * (dxm * dxm));
+                    ofr arg = o->jon_rlamda[k2] * ((J - o->Jbeg) * o->p.DY - ZERO) + o->phi1[k2];
                     cm = cm + amp * cos(arg);
                     sm = sm + amp * sin(arg);
                 }

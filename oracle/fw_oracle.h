@@ -122,6 +122,11 @@ void ofw_max_min_property(ofw_ctx *o);         /* misc.F:307 (Hmax, Hmin, Umax, 
 void ofw_mixing_stuff(ofw_ctx *o);             /* mixing.F:53 (CALCULATE_MEAN, time means and wave heights) */
 int  ofw_end_step(ofw_ctx *o);                 /* main.F:496-517: MIXING_STUFF, MAX_MIN_PROPERTY, CHECK_BLOWUP */
 
+/* Bytes of the arithmetic type: 8 for the FP64 build (the checker), 4 for
+ * the single-precision build that only the CPU baseline times.  Field
+ * arrays (ofw_field) hold that type; masks stay int32. */
+int ofw_real_bytes(void);
+
 /* OpenMP threads used by the parallel-safe loops (0 = library default). */
 void ofw_set_threads(int n);
 int  ofw_get_threads(void);

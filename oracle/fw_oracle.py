@@ -16,6 +16,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libfw_oracle.so")
+_LIB32_PATH = os.path.join(_HERE, "_build", "libfw_oracle_f32.so")
 
 
 class OfwParams(ctypes.Structure):
@@ -90,15 +91,17 @@ def build():
     return _LIB_PATH
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(_LIB_PATH):
+def lib(fp32=False):
+    """The FP64 oracle (the checker), or with fp32 its single-precision build
+    (timed only, as the CPU baseline of a REAL(SP) = 4-byte reference build)."""
+    if fp32 not in _libs:
+        path = _LIB32_PATH if fp32 else _LIB_PATH
+        if not os.path.exists(path):
             build()
-        L = ctypes.CDLL(_LIB_PATH)
+        L = ctypes.CDLL(path)
         vp = ctypes.c_void_p
         L.ofw_create.restype = vp
         L.ofw_create.argtypes = [ctypes.POINTER(OfwParams)]
@@ -130,8 +133,9 @@ def lib():
         L.ofw_end_step.restype = ctypes.c_int
         L.ofw_set_threads.argtypes = [ctypes.c_int]
         L.ofw_get_threads.restype = ctypes.c_int
-        _lib = L
-    return _lib
+        L.ofw_real_bytes.restype = ctypes.c_int
+        _libs[fp32] = L
+    return _libs[fp32]
 
 
 def make_params(p):
@@ -152,10 +156,11 @@ def make_params(p):
 
 
 class Oracle:
-    def __init__(self, params, threads=0):
+    def __init__(self, params, threads=0, fp32=False):
         self.params = dict(params)
         self._p = make_params(self.params)
-        self.L = lib()
+        self.L = lib(fp32)
+        self.real = np.float32 if self.L.ofw_real_bytes() == 4 else np.float64
         if threads:
             self.L.ofw_set_threads(int(threads))
         self.ctx = self.L.ofw_create(ctypes.byref(self._p))
@@ -186,10 +191,9 @@ class Oracle:
         if not ptr:
             raise KeyError(name)
         m, n = self.shape(kind.value)
-        ct = ctypes.c_int32 if isint.value else ctypes.c_double
-        buf = (ct * (m * n)).from_address(ptr)
-        return np.frombuffer(buf, dtype=np.int32 if isint.value else np.float64).reshape(
-            (m, n), order="F")
+        dt = np.int32 if isint.value else self.real
+        buf = (ctypes.c_char * (m * n * np.dtype(dt).itemsize)).from_address(ptr)
+        return np.frombuffer(buf, dtype=dt).reshape((m, n), order="F")
 
     def __getitem__(self, name):
         return self.field(name)
