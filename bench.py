@@ -218,21 +218,25 @@ def kernel_profile(s, T, cells, faces_x, faces_y, hbm):
     return out
 
 
-def e2e_run(fw, s, K):
+def e2e_run(fw, s, K, f32=True):
     """Per step through the C ABI with pinned host buffers: upload Eta, U,
-    V, Ubar, Vbar (one fw_set_fields), one fw_step, read back Eta, U, V (one
-    fw_get_fields)."""
+    V, Ubar, Vbar (one fw_set_fields_f32, or fw_set_fields with f32=False),
+    one fw_step, read back Eta, U, V (one fw_get_fields_f32 / fw_get_fields).
+    Float host arrays are those of the reference's default single-precision
+    build (REAL(SP) = 4 bytes); double ones those of its -DDOUBLE_PRECISION
+    build."""
     import numpy as np
     import torch
-    shp = (s.Mloc, s.Nloc)
+    import ctypes
+    dt_t, dt_n = (torch.float32, 4) if f32 else (torch.float64, 8)
     bufs = {}
     for n in ("Eta", "U", "V", "Ubar", "Vbar"):
-        t = torch.empty((s.Nloc, s.Mloc), dtype=torch.float64, pin_memory=True)
+        t = torch.empty((s.Nloc, s.Mloc), dtype=dt_t, pin_memory=True)
         a = t.numpy().T  # Fortran-ordered (Mloc, Nloc) view of pinned memory
         a[...] = s.get(n)
         bufs[n] = (t, a)
-    import ctypes
     L = s.L
+    setf, getf = (L.fw_set_fields_f32, L.fw_get_fields_f32) if f32 else (L.fw_set_fields, L.fw_get_fields)
     up, down = ("Eta", "U", "V", "Ubar", "Vbar"), ("Eta", "U", "V")
     up_n = (ctypes.c_char_p * 5)(*[n.encode() for n in up])
     up_p = (ctypes.c_void_p * 5)(*[bufs[n][1].ctypes.data for n in up])
@@ -241,14 +245,14 @@ def e2e_run(fw, s, K):
     s.sync()
     t0 = time.perf_counter()
     for _ in range(K):
-        rc = L.fw_set_fields(s.ctx, 5, up_n, up_p)
+        rc = setf(s.ctx, 5, up_n, up_p)
         assert rc == 0
         s.step(1, check=False)
-        rc = L.fw_get_fields(s.ctx, 3, down_n, down_p)
+        rc = getf(s.ctx, 3, down_n, down_p)
         assert rc == 0
     s.sync()
     dt = time.perf_counter() - t0
-    nb = s.Mloc * s.Nloc * 8
+    nb = s.Mloc * s.Nloc * dt_n
     return dt, 5 * nb, 3 * nb
 
 
@@ -320,6 +324,38 @@ def ensemble_bench(fw, pg, ws, n=512, K=10, W=2, run_seconds=300.0, autotune=Tru
                    "per run" % run_seconds}
 
 
+def c1_full_run(fw):
+    """The 250 x 500 planar beach (WK_REG H = 0.3 m, T = 6 s, periodic in y,
+    west sponge, breaking on) through its whole 300 s of model time in mixed
+    precision and in FP64: the stated eta error of the mixed path over a full
+    run, with both wall times."""
+    import numpy as np
+    params, depth, _ = fw.cases.planar_beach()
+    params = fw.with_defaults(params)
+    t_end = float(params["TOTAL_TIME"])
+    out = {}
+    for prec in ("MIXED", "FP64"):
+        s = fw.Solver(params, precision=prec)
+        s.init(depth)
+        n, t0 = 0, time.perf_counter()
+        while s.scalar("TIME") < t_end:
+            s.step(50)
+            n += 50
+        out[prec] = {"Eta": s.get("Eta")[3:-3, 3:-3], "MASK": s.get("MASK")[3:-3, 3:-3],
+                     "TIME": s.scalar("TIME"), "steps": n, "wall_s": time.perf_counter() - t0}
+        s.close()
+    m, d = out["MIXED"], out["FP64"]
+    wet = (m["MASK"] > 0) & (d["MASK"] > 0)
+    diff = (m["Eta"] - d["Eta"])[wet]
+    return {"config": "250x500 planar beach, WK_REG H=0.3 m T=6 s, periodic y, 300 s", "t_end_s": t_end,
+            "time_mixed_s": m["TIME"], "time_fp64_s": d["TIME"], "steps": d["steps"],
+            "eta_rms_mixed_vs_fp64_m": float(np.sqrt(np.mean(diff ** 2))),
+            "eta_max_abs_mixed_vs_fp64_m": float(np.abs(diff).max()),
+            "eta_rms_signal_m": float(np.sqrt(np.mean(d["Eta"][wet] ** 2))),
+            "mask_mismatch_cells": int((m["MASK"] != d["MASK"]).sum()),
+            "wall_s": {"MIXED": m["wall_s"], "FP64": d["wall_s"]}}
+
+
 def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
     """The 4096 x 4096 barred beach with rip channels (1:40, bar 1.5 m high
     80 m offshore, JONSWAP Hs = 1.5 m, Tp = 10 s), run to t_end s in mixed
@@ -331,9 +367,13 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
     params = fw.with_defaults(params)
     params.update({"OUT_Hmax": True, "STEADY_TIME": t_steady, "T_INTV_mean": t_mean})
     out = {}
-    for prec in ("MIXED", "FP64"):
-        s = fw.Solver(params, precision=prec)
-        s.init(depth, phases=phases)
+    # FP64_F32DEPTH: FP64 from the depth rounded to float, a change of the
+    # inputs at float rounding; its distance from FP64 is what rounding
+    # alone grows to by t_end through the run's threshold events (breaking
+    # onsets, wet/dry), the floor for any path that stores floats
+    for prec in ("MIXED", "FP64", "FP64_F32DEPTH"):
+        s = fw.Solver(params, precision=prec[:4] if prec.startswith("FP64") else prec)
+        s.init(depth.astype(np.float32).astype(np.float64) if prec == "FP64_F32DEPTH" else depth, phases=phases)
         n = 0
         ext, e0, e1 = cuda_timer(s)
         s.sync()
@@ -349,8 +389,12 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
         out[prec]["steps"] = n
         out[prec]["rate"] = size * size * n / (ms * 1e-3)
         s.close()
-    m, d = out["MIXED"], out["FP64"]
+    m, d, r = out["MIXED"], out["FP64"], out["FP64_F32DEPTH"]
     wet = (m["MASK"] > 0) & (d["MASK"] > 0)
+    wet_r = (r["MASK"] > 0) & (d["MASK"] > 0)
+    floor = {"eta_rms_m": float(np.sqrt(np.mean((r["Eta"] - d["Eta"])[wet_r] ** 2))),
+             "eta_max_abs_m": float(np.abs(r["Eta"] - d["Eta"])[wet_r].max()),
+             "mask_mismatch_cells": int((r["MASK"] != d["MASK"]).sum()), "steps": r["steps"]}
     cur_d = np.sqrt(d["Umean"] ** 2 + d["Vmean"] ** 2)
     du = np.sqrt((m["Umean"] - d["Umean"]) ** 2 + (m["Vmean"] - d["Vmean"]) ** 2)
     ru_m, ru_d = fw.max_runup(np.pad(m["HeightMax"], 3), depth), fw.max_runup(np.pad(d["HeightMax"], 3), depth)
@@ -385,6 +429,7 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
         "mask_mismatch_cells": int(np.sum(m["MASK"] != d["MASK"])),
         "cell_steps_per_s_mixed": m["rate"], "cell_steps_per_s_fp64": d["rate"],
         "speedup_mixed_over_fp64": m["rate"] / d["rate"],
+        "rounding_floor_fp64_from_float_depth": floor,
     }
 
 
@@ -734,18 +779,35 @@ def main():
         e_d = s64.get("Eta")[3:-3, 3:-3]
         wet = (s64.get("MASK")[3:-3, 3:-3] > 0)
         rms = float(np.sqrt(np.mean((e_m - e_d)[wet] ** 2)))
-        mask_mis = int(np.sum(sm.get("MASK") != s64.get("MASK")))
+        mask_m, mask_d = sm.get("MASK"), s64.get("MASK")
+        mask_mis = int(np.sum(mask_m != mask_d))
+        # where the MASK differs: interior or ghost cells, and how far the
+        # FP64 run's total depth eta + h is from the wet/dry threshold there
+        mis = mask_m != mask_d
+        ghost = np.ones_like(mis)
+        ghost[3:-3, 3:-3] = False
+        hd = np.asarray(s64.get("Eta")) + np.asarray(s64.get("Depth"))
+        mask_detail = {"interior": int((mis & ~ghost).sum()), "ghost": int((mis & ghost).sum()),
+                       "abs_total_depth_m_percentiles": (
+                           {q: float(np.percentile(np.abs(hd[mis]), float(q))) for q in ("50", "90", "100")}
+                           if mis.any() else None)}
         res64 = {"value": aggregate_rate(cells, K, ws, ms64), "ms_per_step": ms64 / K, "dtype": "f64",
                  "step_roofline_frac_hbm": STEP_BYTES["fp64"] * cells / (ms64 / K * 1e-3) / 1e9 / hbm,
                  "eta_rms_mixed_vs_fp64_m": rms, "mask_mismatch_cells": mask_mis,
+                 "mask_mismatch_detail": mask_detail,
                  "time_mixed_s": sm.scalar("TIME"), "time_fp64_s": s64.scalar("TIME"),
                  "status": r64["status"]}
         prof64 = {} if args.no_kernel_profile else kernel_profile(
             s64, 8, cells, (params["Mglob"] + 1) * params["Nglob"], params["Mglob"] * (params["Nglob"] + 1), hbm)
         res64["kernels"] = {k: round(v["ms"], 4) for k, v in prof64.items()}
         s64.close()
+        # the stated eta error over a whole run: the 250 x 500 planar beach
+        # through its 300 s (rank 0 only)
+        if rank == 0:
+            res64["full_run_250x500"] = c1_full_run(fw)
     e2e_steps = min(K, 10)
-    e2e_dt, h2d, d2h = e2e_run(fw, sm, e2e_steps)
+    e2e_dt, h2d, d2h = e2e_run(fw, sm, e2e_steps, f32=True)
+    e2e64_dt, h2d64, d2h64 = e2e_run(fw, sm, e2e_steps, f32=False)
     link = link_rates(h2d // 5)
     # per-kernel timing last: some kernels update the state in place
     prof = {} if args.no_kernel_profile else kernel_profile(
@@ -773,7 +835,13 @@ def main():
                           "frac": STEP_BYTES["mixed"] * cells / step_s / 1e9 / hbm, "peak_kind": peak_kind},
         "e2e": {"value": cells * e2e_steps / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "what": "per step: Eta,U,V,Ubar,Vbar uploaded from pinned host memory (one fw_set_fields), fw_step, Eta,U,V read back (one fw_get_fields)",
+                "what": "per step: Eta,U,V,Ubar,Vbar uploaded as float host arrays (the reference's default "
+                        "REAL(SP) build) from pinned memory (one fw_set_fields_f32), fw_step, Eta,U,V read back "
+                        "(one fw_get_fields_f32)",
+                "double_host": {"value": cells * e2e_steps / e2e64_dt, "h2d_bytes_per_step": h2d64,
+                                "d2h_bytes_per_step": d2h64,
+                                "what": "the same with double host arrays (a -DDOUBLE_PRECISION host; "
+                                        "fw_set_fields / fw_get_fields)"},
                 # the transfers' share of a step against the pinned copy rates
                 # of this machine's host link
                 "transfer_ms_per_step": e2e_dt / e2e_steps * 1e3 - ms_mixed / K,

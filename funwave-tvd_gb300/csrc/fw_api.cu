@@ -152,7 +152,13 @@ int put_named(fw_ctx *c, const char *name, const void *host) {
         return put_field<double>(c, r, host);
     }
     if (!find_field<float>(c, name, r)) return FW_ERR_BAD_PARAM;
-    return put_field<float>(c, r, host);
+    int rc = put_field<float>(c, r, host);
+    if (rc == FW_OK && std::strcmp(name, "Depth") == 0) {
+        // the double copy of the total-depth tests (UPDATE_MASK)
+        FieldRef rd{c->ff.DepthD, 0, 0};
+        rc = put_field<double>(c, rd, host);
+    }
+    return rc;
 }
 
 void fill_float_constants(Grid &g) {
@@ -258,6 +264,7 @@ template <typename T> size_t carve(fw_ctx *c, char *base, bool assign) {
     f.rhs_y = (T *)take(plane * sizeof(T));
     double **df[] = {&f.ty, &f.tp, &f.tq, &f.tc};
     for (double **p : df) *p = (double *)take(plane * sizeof(double));
+    f.DepthD = sizeof(T) == sizeof(double) ? (double *)f.Depth : (double *)take(plane * sizeof(double));
     f.m9_dirty = (int *)take(sizeof(int));
     f.sw_p[0] = f.tp;
     f.sw_q[0] = f.tq;
@@ -857,6 +864,73 @@ int fw_set_field_f32(fw_ctx *c, const char *name, const float *host) {
     } else {
         e = cudaMemcpy2DAsync(r.ptr, (size_t)c->g.pitch * sizeof(float), host, (size_t)w * sizeof(float),
                               (size_t)w * sizeof(float), (size_t)h, cudaMemcpyHostToDevice, c->stream);
+        // the double Depth of the total-depth tests, widened from the floats
+        if (e == cudaSuccess && std::strcmp(name, "Depth") == 0) {
+            e = cudaMemcpyAsync(c->staging, host, (size_t)w * h * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+            if (e == cudaSuccess) convert_in_f32(c, (const float *)c->staging, c->ff.DepthD, w, h);
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return cuda_status(c, e);
+}
+
+// n fields to or from float host arrays at once.  The mixed build's fields
+// are floats in the same layout apart from the pitch: one 2-D copy per field
+// straight between the caller's array and the field, all on the step
+// stream, then one wait.  The FP64 build converts through the staging plane
+// field by field (fw_get_field_f32 / fw_set_field_f32).
+int fw_set_fields_f32(fw_ctx *c, int n, const char *const *names, const float *const *host) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    if (c->sticky_error) return FW_ERR_CUDA;
+    if (n < 1 || n > 16 || !names || !host) return FW_ERR_BAD_PARAM;
+    if (c->p.precision == FW_PREC_FP64) {
+        for (int k = 0; k < n; k++) {
+            const int rc = fw_set_field_f32(c, names[k], host[k]);
+            if (rc != FW_OK) return rc;
+        }
+        return FW_OK;
+    }
+    std::vector<FieldRef> refs((size_t)n);
+    for (int k = 0; k < n; k++)
+        if (!names[k] || !host[k] || !find_field<float>(c, names[k], refs[k]) || refs[k].is_mask)
+            return FW_ERR_BAD_PARAM;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < n && e == cudaSuccess; k++) {
+        if (std::strcmp(names[k], "Depth") == 0) {  // its double copy comes with it
+            const int rc = fw_set_field_f32(c, names[k], host[k]);
+            if (rc != FW_OK) return rc;
+            continue;
+        }
+        int w, h;
+        extent(c, refs[k].kind, w, h);
+        e = cudaMemcpy2DAsync(refs[k].ptr, (size_t)c->g.pitch * sizeof(float), host[k], (size_t)w * sizeof(float),
+                              (size_t)w * sizeof(float), (size_t)h, cudaMemcpyHostToDevice, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return cuda_status(c, e);
+}
+
+int fw_get_fields_f32(fw_ctx *c, int n, const char *const *names, float *const *host) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    if (c->sticky_error) return FW_ERR_CUDA;
+    if (n < 1 || n > 16 || !names || !host) return FW_ERR_BAD_PARAM;
+    if (c->p.precision == FW_PREC_FP64) {
+        for (int k = 0; k < n; k++) {
+            const int rc = fw_get_field_f32(c, names[k], host[k]);
+            if (rc != FW_OK) return rc;
+        }
+        return FW_OK;
+    }
+    std::vector<FieldRef> refs((size_t)n);
+    for (int k = 0; k < n; k++)
+        if (!names[k] || !host[k] || !find_field<float>(c, names[k], refs[k]) || refs[k].is_mask)
+            return FW_ERR_BAD_PARAM;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < n && e == cudaSuccess; k++) {
+        int w, h;
+        extent(c, refs[k].kind, w, h);
+        e = cudaMemcpy2DAsync(host[k], (size_t)w * sizeof(float), refs[k].ptr, (size_t)c->g.pitch * sizeof(float),
+                              (size_t)w * sizeof(float), (size_t)h, cudaMemcpyDeviceToHost, c->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return cuda_status(c, e);
@@ -1673,6 +1747,11 @@ int fw_set_fields(fw_ctx *c, int n, const char *const *names, const void *const 
                                   (size_t)w * sizeof(double), (size_t)h, cudaMemcpyDeviceToDevice, c->stream);
         else
             convert_in(c, buf + off[k], r.is_mask, r.ptr, w, h);
+        // the mixed build's double Depth of the total-depth tests
+        if (e == cudaSuccess && !fp64 && std::strcmp(names[k], "Depth") == 0)
+            e = cudaMemcpy2DAsync(c->ff.DepthD, (size_t)c->g.pitch * sizeof(double), buf + off[k],
+                                  (size_t)w * sizeof(double), (size_t)w * sizeof(double), (size_t)h,
+                                  cudaMemcpyDeviceToDevice, c->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_status(c, e);

@@ -90,6 +90,9 @@ struct Fields {
     uint8_t *MASK, *MASKn, *MASK9, *MASK_STRUC;
     T *rhs_x, *rhs_y;                 // tmp4 of GET_Eta_U_V_HU_HV
     double *ty, *tp, *tq, *tc;        // line-solver scratch
+    // Depth as the caller gave it, in double: the FP64 build's Depth itself;
+    // in the mixed build a copy that UPDATE_MASK's total-depth tests read
+    double *DepthD;
     double *sw_p[2], *sw_q[2], *sw_c[2];  // factorisation sweep scratch per direction (mixed)
     double *red;                      // reduced systems
     // mixed path: constant factorisation of the tridiagonal matrices, per

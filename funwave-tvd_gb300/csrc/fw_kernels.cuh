@@ -2260,6 +2260,26 @@ __global__ void k_nodisp_copy(Grid g, Fields<T> f) {
 // Depthy reset at old-dry cells, MASK9.  Launched over (Mloc+1) x (Nloc+1)
 // so that every face has a thread.
 // ---------------------------------------------------------------------------
+// The sign of eta + h, with h the Depth as given in double (the FP64
+// build's own Depth, the mixed build's double copy of it): +1 for
+// eta > -h, -1 for eta < -h, 0 for equality, as the double comparisons of
+// masks.F:107, 129 decide.  The mixed build decides in float where the
+// float sum's margin exceeds its rounding (about 2 ulps of the larger term,
+// plus the rounding of the stored float Depth), which gives the same sign,
+// and evaluates the rest in double: FP64 instructions run only at cells
+// within a few ulps of the threshold.
+__device__ __forceinline__ int wet_test(double eta, double, double hd) {
+    return eta > -hd ? 1 : (eta < -hd ? -1 : 0);
+}
+__device__ __forceinline__ int wet_test(float eta, float hf, double hd) {
+    const float s = eta + hf;
+    const float tol = 4.0e-7f * fmaxf(fabsf(eta), fabsf(hf)) + 1.0e-30f;
+    if (s > tol) return 1;
+    if (s < -tol) return -1;
+    const double e = (double)eta;
+    return e > -hd ? 1 : (e < -hd ? -1 : 0);
+}
+
 template <typename T>
 __device__ __forceinline__ bool in_mask_range(const Grid &g, int a, int b) {
     return a >= g.ib - 2 && a <= g.ie + 2 && b >= g.jb - 2 && b <= g.je + 2;
@@ -2269,19 +2289,20 @@ __device__ __forceinline__ int new_mask(const Grid &g, const Fields<T> &f, int a
     const size_t q = IDX(a, b);
     const int m = ro(f.MASK + (q));
     if (!in_mask_range<T>(g, a, b) || ro(f.MASK_STRUC + (q)) != 1) return m;
-    // total-depth tests: comparing the stored values in T is exact (a
-    // float widened to double compares the same), so no FP64 work is needed
+    // total-depth tests (masks.F:107, 129) of eta against Depth as given, in
+    // double (wet_test)
     const T eta = ro(f.Eta + (q));
+    const int side = wet_test(eta, ro(f.Depth + (q)), ro(f.DepthD + (q)));
     if (m < 1) {
         int r = m;
-        if (eta > -ro(f.Depth + (q))) r = 1;
+        if (side > 0) r = 1;
         if (ro(f.MASK + (IDX(a - 1, b))) == 1 && ro(f.Eta + (IDX(a - 1, b))) > eta) r = 1;
         if (ro(f.MASK + (IDX(a + 1, b))) == 1 && ro(f.Eta + (IDX(a + 1, b))) > eta) r = 1;
         if (ro(f.MASK + (IDX(a, b - 1))) == 1 && ro(f.Eta + (IDX(a, b - 1))) > eta) r = 1;
         if (ro(f.MASK + (IDX(a, b + 1))) == 1 && ro(f.Eta + (IDX(a, b + 1))) > eta) r = 1;
         return r;
     }
-    return (eta < -ro(f.Depth + (q))) ? 0 : m;
+    return (side < 0) ? 0 : m;
 }
 
 // one thread of UPDATE_MASK at (i, j) in 0..Mloc x 0..Nloc

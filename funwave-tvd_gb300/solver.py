@@ -255,6 +255,8 @@ def load_library(path=None):
     L.fw_output_begin.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(vp)]
     L.fw_set_fields.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(vp)]
     L.fw_get_fields.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(vp)]
+    L.fw_set_fields_f32.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(vp)]
+    L.fw_get_fields_f32.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(vp)]
     L.fw_output_wait.argtypes = [vp]
     L.fw_output_done.argtypes = [vp]
     L.fw_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(vp)]

@@ -125,6 +125,18 @@ MODULE FUNWAVE_GPU
       REAL(C_FLOAT), INTENT(IN) :: host(*)
     END FUNCTION
     ! names(k) = C_LOC of a NUL-terminated name, host(k) = C_LOC of its array
+    INTEGER(C_INT) FUNCTION fw_set_fields_f32(ctx, n, names, host) BIND(C, NAME="fw_set_fields_f32")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: ctx
+      INTEGER(C_INT), VALUE :: n
+      TYPE(C_PTR), INTENT(IN) :: names(*), host(*)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION fw_get_fields_f32(ctx, n, names, host) BIND(C, NAME="fw_get_fields_f32")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: ctx
+      INTEGER(C_INT), VALUE :: n
+      TYPE(C_PTR), INTENT(IN) :: names(*), host(*)
+    END FUNCTION
     INTEGER(C_INT) FUNCTION fw_set_fields(ctx, n, names, host) BIND(C, NAME="fw_set_fields")
       IMPORT :: C_INT, C_PTR
       TYPE(C_PTR), VALUE :: ctx

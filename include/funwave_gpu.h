@@ -147,6 +147,13 @@ int fw_set_field(fw_ctx *ctx, const char *name, const void *host);
  * depth and initial state once at start-up. */
 int fw_get_field_f32(fw_ctx *ctx, const char *name, float *host);
 int fw_set_field_f32(fw_ctx *ctx, const char *name, const float *host);
+/* n fields at once (n <= 16, names as above, no masks) to or from float
+ * host arrays, synchronous.  In a mixed context each field moves with one
+ * 2-D copy straight between the host array and the device field (with
+ * pinned host buffers, at the host link's rate, half the bytes of the
+ * double transfers); an FP64 context converts field by field. */
+int fw_set_fields_f32(fw_ctx *ctx, int n, const char *const *names, const float *const *host);
+int fw_get_fields_f32(fw_ctx *ctx, int n, const char *const *names, float *const *host);
 /* n fields at once (n <= 16; names and host layouts as above), synchronous.
  * fw_set_fields copies every plane to the device on a second stream and
  * converts each one as soon as it has arrived; fw_get_fields is

@@ -39,3 +39,38 @@ def test_f32_transfers(fw, precision):
         s.set_f32(name, a.astype(np.float32))
     assert s.step(2, check=False) == 0
     s.close()
+
+
+@pytest.mark.parametrize("precision", ["FP64", "MIXED"])
+def test_f32_multi_field_transfers(fw, precision):
+    """fw_set_fields_f32 / fw_get_fields_f32 move several fields at once and
+    equal the one-field calls; "Depth" among them keeps the mixed build's
+    double copy of the total-depth tests in step (the run goes on equally)."""
+    import ctypes
+    params, depth, _ = fw.cases.planar_beach(Mglob=70, Nglob=44, seed=6)
+    p = fw.with_defaults(params)
+    eta, u, v = fw.cases.random_state(70, 44, seed=7)
+    runs = []
+    for multi in (False, True):
+        s = fw.Solver(p, precision=precision)
+        s.init(depth, eta, u, v)
+        s.step(2)
+        names = ("Eta", "U", "Vbar", "Depth")
+        arrs = {n: np.asfortranarray(s.get_f32(n) * np.float32(1.0 + 1e-3)) for n in names}
+        if multi:
+            cn = (ctypes.c_char_p * 4)(*[n.encode() for n in names])
+            hp = (ctypes.c_void_p * 4)(*[arrs[n].ctypes.data for n in names])
+            assert s.L.fw_set_fields_f32(s.ctx, 4, cn, hp) == 0
+            outs = {n: np.zeros(s.shape(n), dtype=np.float32, order="F") for n in names}
+            op = (ctypes.c_void_p * 4)(*[outs[n].ctypes.data for n in names])
+            assert s.L.fw_get_fields_f32(s.ctx, 4, cn, op) == 0
+            for n in names:
+                assert np.array_equal(outs[n], s.get_f32(n)), n
+                assert np.array_equal(outs[n], arrs[n]), n
+        else:
+            for n in names:
+                s.set_f32(n, arrs[n])
+        assert s.step(3, check=False) == 0
+        runs.append(s.get("Eta"))
+        s.close()
+    assert np.array_equal(runs[0], runs[1])
