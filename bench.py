@@ -371,30 +371,16 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
     # inputs at float rounding; its distance from FP64 is what rounding
     # alone grows to by t_end through the run's threshold events (breaking
     # onsets, wet/dry), the floor for any path that stores floats
-    # FP64_F32STATE: FP64 arithmetic whose state is rounded to float after
-    # every step (a device round trip through fw_get/set_field_f32): what
-    # storing the state in float costs by t_end, whatever the arithmetic
-    import ctypes
-    rounded = ("Eta", "U", "V", "Ubar", "Vbar", "HU", "HV", "H", "AGE", "nu_break", "ETAT", "P", "Q")
-    for prec in ("MIXED", "FP64", "FP64_F32DEPTH", "FP64_F32STATE"):
+    for prec in ("MIXED", "FP64", "FP64_F32DEPTH"):
         s = fw.Solver(params, precision=prec[:4] if prec.startswith("FP64") else prec)
         s.init(depth.astype(np.float32).astype(np.float64) if prec == "FP64_F32DEPTH" else depth, phases=phases)
-        bufs = {k: np.zeros(s.shape(k), dtype=np.float32, order="F") for k in rounded} \
-            if prec == "FP64_F32STATE" else None
         n = 0
         ext, e0, e1 = cuda_timer(s)
         s.sync()
         e0.record(ext)
         while s.scalar("TIME") < t_end:
-            if bufs is None:
-                s.step(20)
-                n += 20
-                continue
-            s.step(1)
-            n += 1
-            for k, a in bufs.items():
-                assert s.L.fw_get_field_f32(s.ctx, k.encode(), a.ctypes.data) == 0
-                assert s.L.fw_set_field_f32(s.ctx, k.encode(), a.ctypes.data) == 0
+            s.step(20)
+            n += 20
         e1.record(ext)
         e1.synchronize()
         ms = e0.elapsed_time(e1)
@@ -409,13 +395,6 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
     floor = {"eta_rms_m": float(np.sqrt(np.mean((r["Eta"] - d["Eta"])[wet_r] ** 2))),
              "eta_max_abs_m": float(np.abs(r["Eta"] - d["Eta"])[wet_r].max()),
              "mask_mismatch_cells": int((r["MASK"] != d["MASK"]).sum()), "steps": r["steps"]}
-    f32s = out["FP64_F32STATE"]
-    wet_s = (f32s["MASK"] > 0) & (d["MASK"] > 0)
-    de2_s = ((f32s["Eta"] - d["Eta"]) ** 2) * wet_s
-    floor_state = {"eta_rms_m": float(np.sqrt(np.mean((f32s["Eta"] - d["Eta"])[wet_s] ** 2))),
-                   "eta_max_abs_m": float(np.abs(f32s["Eta"] - d["Eta"])[wet_s].max()),
-                   "share_in_breaking_zone": None, "mask_mismatch_cells": int((f32s["MASK"] != d["MASK"]).sum()),
-                   "rounded_fields": list(rounded), "steps": f32s["steps"]}
     cur_d = np.sqrt(d["Umean"] ** 2 + d["Vmean"] ** 2)
     du = np.sqrt((m["Umean"] - d["Umean"]) ** 2 + (m["Vmean"] - d["Vmean"]) ** 2)
     ru_m, ru_d = fw.max_runup(np.pad(m["HeightMax"], 3), depth), fw.max_runup(np.pad(d["HeightMax"], 3), depth)
@@ -432,7 +411,6 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
         zone = z
     de2 = ((m["Eta"] - d["Eta"]) ** 2) * wet
     quiet = wet & ~zone
-    floor_state["share_in_breaking_zone"] = float(np.sum(de2_s[zone]) / max(np.sum(de2_s), 1e-300))
     ad = np.abs(m["Eta"] - d["Eta"])[wet]
     return {
         "metric": "mixed vs FP64 on the 4096x4096 barred beach", "grid": [size, size], "dx_m": 1.0,
@@ -452,7 +430,6 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
         "cell_steps_per_s_mixed": m["rate"], "cell_steps_per_s_fp64": d["rate"],
         "speedup_mixed_over_fp64": m["rate"] / d["rate"],
         "rounding_floor_fp64_from_float_depth": floor,
-        "float_state_floor_fp64_rounded_every_step": floor_state,
     }
 
 

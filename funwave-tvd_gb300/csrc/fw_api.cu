@@ -874,68 +874,6 @@ int fw_set_field_f32(fw_ctx *c, const char *name, const float *host) {
     return cuda_status(c, e);
 }
 
-// n fields to or from float host arrays at once.  The mixed build's fields
-// are floats in the same layout apart from the pitch: one 2-D copy per field
-// straight between the caller's array and the field, all on the step
-// stream, then one wait.  The FP64 build converts through the staging plane
-// field by field (fw_get_field_f32 / fw_set_field_f32).
-int fw_set_fields_f32(fw_ctx *c, int n, const char *const *names, const float *const *host) {
-    if (!c) return FW_ERR_BAD_PARAM;
-    if (c->sticky_error) return FW_ERR_CUDA;
-    if (n < 1 || n > 16 || !names || !host) return FW_ERR_BAD_PARAM;
-    if (c->p.precision == FW_PREC_FP64) {
-        for (int k = 0; k < n; k++) {
-            const int rc = fw_set_field_f32(c, names[k], host[k]);
-            if (rc != FW_OK) return rc;
-        }
-        return FW_OK;
-    }
-    std::vector<FieldRef> refs((size_t)n);
-    for (int k = 0; k < n; k++)
-        if (!names[k] || !host[k] || !find_field<float>(c, names[k], refs[k]) || refs[k].is_mask)
-            return FW_ERR_BAD_PARAM;
-    cudaError_t e = cudaSuccess;
-    for (int k = 0; k < n && e == cudaSuccess; k++) {
-        if (std::strcmp(names[k], "Depth") == 0) {  // its double copy comes with it
-            const int rc = fw_set_field_f32(c, names[k], host[k]);
-            if (rc != FW_OK) return rc;
-            continue;
-        }
-        int w, h;
-        extent(c, refs[k].kind, w, h);
-        e = cudaMemcpy2DAsync(refs[k].ptr, (size_t)c->g.pitch * sizeof(float), host[k], (size_t)w * sizeof(float),
-                              (size_t)w * sizeof(float), (size_t)h, cudaMemcpyHostToDevice, c->stream);
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    return cuda_status(c, e);
-}
-
-int fw_get_fields_f32(fw_ctx *c, int n, const char *const *names, float *const *host) {
-    if (!c) return FW_ERR_BAD_PARAM;
-    if (c->sticky_error) return FW_ERR_CUDA;
-    if (n < 1 || n > 16 || !names || !host) return FW_ERR_BAD_PARAM;
-    if (c->p.precision == FW_PREC_FP64) {
-        for (int k = 0; k < n; k++) {
-            const int rc = fw_get_field_f32(c, names[k], host[k]);
-            if (rc != FW_OK) return rc;
-        }
-        return FW_OK;
-    }
-    std::vector<FieldRef> refs((size_t)n);
-    for (int k = 0; k < n; k++)
-        if (!names[k] || !host[k] || !find_field<float>(c, names[k], refs[k]) || refs[k].is_mask)
-            return FW_ERR_BAD_PARAM;
-    cudaError_t e = cudaSuccess;
-    for (int k = 0; k < n && e == cudaSuccess; k++) {
-        int w, h;
-        extent(c, refs[k].kind, w, h);
-        e = cudaMemcpy2DAsync(host[k], (size_t)w * sizeof(float), refs[k].ptr, (size_t)c->g.pitch * sizeof(float),
-                              (size_t)w * sizeof(float), (size_t)h, cudaMemcpyDeviceToHost, c->stream);
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    return cuda_status(c, e);
-}
-
 int fw_get_points(fw_ctx *c, const char *name, int n, const int *I, const int *J, double *out) {
     int rc = check_ready(c);
     if (rc != FW_OK) return rc;
@@ -1764,6 +1702,120 @@ int fw_get_fields(fw_ctx *c, int n, const char *const *names, void *const *host)
     int rc = fw_output_begin(c, n, names, host);
     if (rc != FW_OK) return rc;
     return fw_output_wait(c);
+}
+
+// n fields to or from float host arrays at once.  The mixed build's fields
+// are floats in the host layout apart from the pitch: each plane crosses
+// the host link as one contiguous copy, on the second stream, into (or out
+// of) the device input buffer, and a device-side 2-D copy on the step
+// stream moves it to (or from) the pitched field, so the copies of one
+// plane overlap the device copies of the next.  The FP64 build converts
+// through the staging plane field by field (fw_get_field_f32 /
+// fw_set_field_f32).
+static int f32_planes(fw_ctx *c, int n, const char *const *names, std::vector<FieldRef> &refs,
+                      std::vector<size_t> &off) {
+    refs.assign((size_t)n, FieldRef{});
+    off.assign((size_t)n + 1, 0);
+    for (int k = 0; k < n; k++) {
+        if (!names[k] || !find_field<float>(c, names[k], refs[k]) || refs[k].is_mask) return FW_ERR_BAD_PARAM;
+        int w, h;
+        extent(c, refs[k].kind, w, h);
+        off[k + 1] = off[k] + ((size_t)w * h * sizeof(float) + 255) / 256 * 256;
+    }
+    int rc = ensure_out_stream(c);
+    if (rc != FW_OK) return rc;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < n && e == cudaSuccess; k++)
+        if (!c->in_ev[k]) e = cudaEventCreateWithFlags(&c->in_ev[k], cudaEventDisableTiming);
+    // the step stream may still use the buffer (an earlier call): it is
+    // idle after this wait
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    if (off[n] > c->in_cap) {
+        if (c->in_buf) cudaFree(c->in_buf);
+        c->in_buf = nullptr;
+        c->in_cap = 0;
+        if (cudaMalloc(&c->in_buf, off[n]) != cudaSuccess) {
+            cudaGetLastError();
+            return FW_ERR_OOM;
+        }
+        c->in_cap = off[n];
+    }
+    return FW_OK;
+}
+
+int fw_set_fields_f32(fw_ctx *c, int n, const char *const *names, const float *const *host) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    if (c->sticky_error) return FW_ERR_CUDA;
+    if (n < 1 || n > 16 || !names || !host) return FW_ERR_BAD_PARAM;
+    for (int k = 0; k < n; k++)
+        if (!host[k]) return FW_ERR_BAD_PARAM;
+    if (c->p.precision == FW_PREC_FP64) {
+        for (int k = 0; k < n; k++) {
+            const int rc = fw_set_field_f32(c, names[k], host[k]);
+            if (rc != FW_OK) return rc;
+        }
+        return FW_OK;
+    }
+    std::vector<FieldRef> refs;
+    std::vector<size_t> off;
+    int rc = f32_planes(c, n, names, refs, off);
+    if (rc != FW_OK) return rc;
+    char *buf = (char *)c->in_buf;
+    cudaError_t e = cudaEventRecord(c->out_ready, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->out_stream, c->out_ready, 0);
+    for (int k = 0; k < n && e == cudaSuccess; k++) {
+        int w, h;
+        extent(c, refs[k].kind, w, h);
+        e = cudaMemcpyAsync(buf + off[k], host[k], (size_t)w * h * sizeof(float), cudaMemcpyHostToDevice,
+                            c->out_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(c->in_ev[k], c->out_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->in_ev[k], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(refs[k].ptr, (size_t)c->g.pitch * sizeof(float), buf + off[k], (size_t)w * sizeof(float),
+                                  (size_t)w * sizeof(float), (size_t)h, cudaMemcpyDeviceToDevice, c->stream);
+        // the double Depth of the total-depth tests, widened from the floats
+        if (e == cudaSuccess && std::strcmp(names[k], "Depth") == 0)
+            convert_in_f32(c, (const float *)(buf + off[k]), c->ff.DepthD, w, h);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    return finish(c);
+}
+
+int fw_get_fields_f32(fw_ctx *c, int n, const char *const *names, float *const *host) {
+    if (!c) return FW_ERR_BAD_PARAM;
+    if (c->sticky_error) return FW_ERR_CUDA;
+    if (n < 1 || n > 16 || !names || !host) return FW_ERR_BAD_PARAM;
+    for (int k = 0; k < n; k++)
+        if (!host[k]) return FW_ERR_BAD_PARAM;
+    if (c->p.precision == FW_PREC_FP64) {
+        for (int k = 0; k < n; k++) {
+            const int rc = fw_get_field_f32(c, names[k], host[k]);
+            if (rc != FW_OK) return rc;
+        }
+        return FW_OK;
+    }
+    std::vector<FieldRef> refs;
+    std::vector<size_t> off;
+    int rc = f32_planes(c, n, names, refs, off);
+    if (rc != FW_OK) return rc;
+    char *buf = (char *)c->in_buf;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < n && e == cudaSuccess; k++) {
+        int w, h;
+        extent(c, refs[k].kind, w, h);
+        e = cudaMemcpy2DAsync(buf + off[k], (size_t)w * sizeof(float), refs[k].ptr, (size_t)c->g.pitch * sizeof(float),
+                              (size_t)w * sizeof(float), (size_t)h, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(c->in_ev[k], c->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->out_stream, c->in_ev[k], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(host[k], buf + off[k], (size_t)w * h * sizeof(float), cudaMemcpyDeviceToHost,
+                                c->out_stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->out_stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return cuda_status(c, e);
 }
 
 int fw_host_alloc(size_t bytes, void **ptr) {

@@ -2016,125 +2016,26 @@ __global__ void __launch_bounds__(128) k_sol_c(Grid g, Fields<T> f, LinePart lp)
     }
 }
 
-// The middle of a line solve, per chunk: the first solution x0 of the
-// chunk's rows from the reduced system, the compensated residual
-// d - T x0 of every row, and the second pass's sweep and reduced right-hand
-// sides over that residual.  A row's neighbours across the chunk ends are
-// the neighbouring chunks' end values, which are reduced-system unknowns,
-// so the chunk needs nothing from another thread.
-template <typename T, int DIR, bool PER, int M>
-__global__ void __launch_bounds__(128) k_sol_mid(Grid g, Fields<T> f, LinePart lp) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= lp.nlines * lp.P) return;
-    int l, ch;
-    chunk_of<DIR>(lp, t, l, ch);
-    const int L = lp.L, P = lp.P;
-    const int s = ch * lp.m;
-    const int e = (ch == P - 1) ? L - 1 : s + lp.m - 1;
-    const float *red0 = red_rhs<0>(f.red, lp) + (size_t)l * 2 * P;
-    const float xs = red0[2 * ch], xe = red0[2 * ch + 1];
-    // x0 just outside the chunk: the previous chunk's last row and the next
-    // chunk's first row (the cyclic ends wrap in periodic y)
-    float xlo = 0.0f, xhi = 0.0f;
-    if (ch > 0) xlo = red0[2 * ch - 1];
-    else if (PER) xlo = red0[2 * P - 1];
-    if (ch < P - 1) xhi = red0[2 * ch + 2];
-    else if (PER) xhi = red0[0];
+// compensated residual of the first solve on every interior cell
+template <typename T, int DIR, bool PER>
+__global__ void __launch_bounds__(256) k_resid(Grid g, Fields<T> f, LinePart lp) {
+    const int i = g.ib + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = g.jb + blockIdx.y * blockDim.y + threadIdx.y;
+    if (i > g.ie || j > g.je) return;
+    const size_t q = IDX(i, j);
+    const int k = DIR == 0 ? i - g.ib : j - g.jb;
+    const size_t st = DIR == 0 ? 1 : (size_t)g.pitch;
+    const float *x0 = (const float *)f.tp;
     const T *rhs = DIR == 0 ? f.rhs_x : f.rhs_y;
-    const float *it_ = f.fac_it[DIR], *A_ = f.fac_A[DIR], *lr_ = f.fac_lr[DIR], *cp_ = f.fac_cp[DIR];
-    const float *p_ = f.fac_p[DIR], *q_ = f.fac_q[DIR];
-    const float *ah_ = f.fac_ah[DIR], *al_ = f.fac_al[DIR], *chh = f.fac_ch[DIR], *cl_ = f.fac_cl[DIR];
-    float *ys = (float *)f.ty;
-    float *x0 = (float *)f.tp;
-    FacLine fl = fac_line(f.fac_red[DIR], lp, l);
-    float sc0 = 1.0f, sc1 = 1.0f;
-    if (PER) {
-        sc0 = 1.0f / (1.0f + fl.tail[0]);
-        sc1 = 1.0f / (1.0f + fl.tail[1]);
-    }
-    const size_t stride = DIR == 0 ? 1 : (size_t)g.pitch;
-    int i0, j0;
-    line_cell<DIR>(g, l, s, i0, j0);
-    const size_t q0 = IDX(i0, j0);
-    constexpr int MR = M > 2 ? M : 1;
-    if (M > 2 && e - s + 1 == M) {
-        float xv[MR], rv[MR];
-#pragma unroll
-        for (int k = 0; k < MR; k++) {
-            const size_t q = q0 + (size_t)k * stride;
-            xv[k] = (k == 0) ? xs : (k == MR - 1) ? xe : ys[q] - p_[q] * xs - q_[q] * xe;
-        }
-#pragma unroll
-        for (int k = 0; k < MR; k++) {
-            const size_t q = q0 + (size_t)k * stride;
-            x0[q] = xv[k];
-            const float d = (float)rhs[q] * it_[q];
-            const float xm = k > 0 ? xv[k - 1] : xlo, xp = k < MR - 1 ? xv[k + 1] : xhi;
-            float r = residual(d, xv[k], xm, xp, ah_[q], al_[q], chh[q], cl_[q]);
-            if (PER && s + k == 0) r *= sc0;
-            if (PER && s + k == L - 1) r *= sc1;
-            rv[k] = r;
-        }
-        float yv[MR];
-        float yp = 0.0f;
-#pragma unroll
-        for (int k = 1; k < MR - 1; k++) {
-            const size_t q = q0 + (size_t)k * stride;
-            yp = rv[k] * A_[q] - lr_[q] * yp;
-            yv[k] = yp;
-        }
-        float yn = 0.0f;
-#pragma unroll
-        for (int k = MR - 2; k >= 1; k--) {
-            const size_t q = q0 + (size_t)k * stride;
-            yn = yv[k] - cp_[q] * yn;
-            yv[k] = yn;
-        }
-#pragma unroll
-        for (int k = 1; k < MR - 1; k++) ys[q0 + (size_t)k * stride] = yv[k];
-        float *red1 = red_rhs<1>(f.red, lp) + ((size_t)l * 2 * P + 2 * ch);
-        red1[0] = rv[0] - fl.cs[ch] * yv[1];
-        red1[1] = rv[MR - 1] - fl.ae[ch] * yv[MR - 2];
-        return;
-    }
-    // any chunk length: x0 first (the residual reads neighbouring rows)
-    for (int k = s; k <= e; k++) {
-        const size_t q = q0 + (size_t)(k - s) * stride;
-        x0[q] = (k == s) ? xs : (k == e) ? xe : ys[q] - p_[q] * xs - q_[q] * xe;
-    }
-    auto rval = [&](int k) {
-        const size_t q = q0 + (size_t)(k - s) * stride;
-        const float d = (float)rhs[q] * it_[q];
-        const float xm = k > s ? x0[q - stride] : xlo, xp = k < e ? x0[q + stride] : xhi;
-        float r = residual(d, x0[q], xm, xp, ah_[q], al_[q], chh[q], cl_[q]);
-        if (PER && k == 0) r *= sc0;
-        if (PER && k == L - 1) r *= sc1;
-        return r;
-    };
-    const float rs = rval(s), re = rval(e);
-    float red_s = rs, red_e = re;
-    if (e - s >= 2) {
-        float yp = 0.0f;
-        for (int k = s + 1; k <= e - 1; k++) {
-            const size_t q = q0 + (size_t)(k - s) * stride;
-            yp = rval(k) * A_[q] - lr_[q] * yp;
-            ys[q] = yp;
-        }
-        float yn = 0.0f, y1 = 0.0f, yl = 0.0f;
-        for (int k = e - 1; k >= s + 1; k--) {
-            const size_t q = q0 + (size_t)(k - s) * stride;
-            const float yk = ys[q] - cp_[q] * yn;
-            ys[q] = yk;
-            yn = yk;
-            if (k == e - 1) yl = yk;
-            if (k == s + 1) y1 = yk;
-        }
-        red_s = rs - fl.cs[ch] * y1;
-        red_e = re - fl.ae[ch] * yl;
-    }
-    float *red1 = red_rhs<1>(f.red, lp) + ((size_t)l * 2 * P + 2 * ch);
-    red1[0] = red_s;
-    red1[1] = red_e;
+    const float d = (float)rhs[q] * f.fac_it[DIR][q];
+    // neighbours along the line; the cyclic ends wrap in periodic y
+    float xm = 0.0f, xp = 0.0f;
+    if (k > 0) xm = x0[q - st];
+    else if (PER) xm = x0[q + (size_t)(lp.L - 1) * st];
+    if (k < lp.L - 1) xp = x0[q + st];
+    else if (PER) xp = x0[q - (size_t)(lp.L - 1) * st];
+    ((float *)f.tq)[q] = residual(d, x0[q], xm, xp, f.fac_ah[DIR][q], f.fac_al[DIR][q], f.fac_ch[DIR][q],
+                                  f.fac_cl[DIR][q]);
 }
 
 // x lines, one block per line, everything unit-stride: load d, solve, form
@@ -2370,13 +2271,18 @@ __global__ void k_nodisp_copy(Grid g, Fields<T> f) {
 __device__ __forceinline__ int wet_test(double eta, double hf, const double *) {
     return eta > -hf ? 1 : (eta < -hf ? -1 : 0);
 }
+// the double comparison, out of line so that the float path of the callers
+// keeps its registers
+static __device__ __noinline__ int wet_test_double(float eta, const double *hdp) {
+    const double e = (double)eta, hd = *hdp;
+    return e > -hd ? 1 : (e < -hd ? -1 : 0);
+}
 __device__ __forceinline__ int wet_test(float eta, float hf, const double *hdp) {
     const float s = eta + hf;
     const float tol = 4.0e-7f * fmaxf(fabsf(eta), fabsf(hf)) + 1.0e-30f;
     if (s > tol) return 1;
     if (s < -tol) return -1;
-    const double e = (double)eta, hd = *hdp;  // the double depth only here
-    return e > -hd ? 1 : (e < -hd ? -1 : 0);
+    return wet_test_double(eta, hdp);  // the double depth only here
 }
 
 template <typename T>
@@ -3405,22 +3311,24 @@ static bool launch_tri(fw_ctx *c, const LinePart &lp, bool fac = true, bool clea
         const size_t sb = (size_t)16 * lp.P * sizeof(float);
         const unsigned ga = (unsigned)((nt + 127) / 128);
         // chunks of 16 rows (lines of 512 cells and more) walk in registers
-        // pass 0 sweep, reduced solve, [x0, residual, pass 1 sweep], reduced
-        // solve, x0 + correction
         if (lp.m == 16) {
             k_sol_a<T, DIR, PER, 0, 16><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
             k_sol_b<T, DIR, PER, 0><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
-            k_sol_mid<T, DIR, PER, 16><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_c<T, DIR, 0, 16><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_resid<T, DIR, PER><<<gi, B2D, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_a<T, DIR, PER, 1, 16><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
             k_sol_b<T, DIR, PER, 1><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
             k_sol_c<T, DIR, 1, 16><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         } else {
             k_sol_a<T, DIR, PER, 0, 0><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
             k_sol_b<T, DIR, PER, 0><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
-            k_sol_mid<T, DIR, PER, 0><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_c<T, DIR, 0, 0><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_resid<T, DIR, PER><<<gi, B2D, 0, c->stream>>>(g, c->F<T>(), lp);
+            k_sol_a<T, DIR, PER, 1, 0><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
             k_sol_b<T, DIR, PER, 1><<<lp.nlines, nb, sb, c->stream>>>(g, c->F<T>(), lp);
             k_sol_c<T, DIR, 1, 0><<<ga, 128, 0, c->stream>>>(g, c->F<T>(), lp);
         }
-        note(c, 5);
+        note(c, 7);
         return false;
     }
     if constexpr (sizeof(T) == sizeof(double)) {

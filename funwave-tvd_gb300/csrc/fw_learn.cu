@@ -206,11 +206,13 @@ __global__ void k_corr_input(fw::Grid g, fw::Fields<T> f, float *in) {
 }
 
 // sums over the wet interior cells: [0] the eta correction, [1] the count,
-// [2] max |correction| (bits of a non-negative double)
+// [2] max |correction|, [3] the largest amount by which a corrected total
+// depth would fall below MinDepth (bits of non-negative doubles); [4] the
+// decision of k_corr_apply (1 applied, 0 the plain step kept)
 template <typename T>
-__global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, double *sums) {
+__global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, float min_depth) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-    float se = 0.0f, sc = 0.0f, mx = 0.0f;
+    float se = 0.0f, sc = 0.0f, mx = 0.0f, dry = 0.0f;
     if (i < g.Mglob && j < g.Nglob) {
         const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
         const long long p = (long long)i + (long long)j * g.Mglob;
@@ -219,24 +221,41 @@ __global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, doubl
             se = out[p * NOUT] * inv;
             sc = 1.0f;
             mx = fmaxf(fabsf(out[p * NOUT]), fmaxf(fabsf(out[p * NOUT + 1]), fabsf(out[p * NOUT + 2]))) * inv;
+            dry = fmaxf(0.0f, min_depth - ((float)f.H[id] + se));
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
         se += __shfl_xor_sync(0xffffffffu, se, o);
         sc += __shfl_xor_sync(0xffffffffu, sc, o);
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        dry = fmaxf(dry, __shfl_xor_sync(0xffffffffu, dry, o));
     }
     if (((threadIdx.x + threadIdx.y * blockDim.x) & 31) == 0) {
         atomicAdd(&sums[0], (double)se);
         atomicAdd(&sums[1], (double)sc);
         atomicMax((unsigned long long *)&sums[2], (unsigned long long)__double_as_longlong((double)mx));
+        atomicMax((unsigned long long *)&sums[3], (unsigned long long)__double_as_longlong((double)dry));
     }
 }
 
+// Whether a correction is applied, the same on every thread from the sums:
+// no component above max_corr; a finite result; no wet cell pushed to or
+// below MinDepth (the correction would move the shoreline and so change the
+// volume through UPDATE_MASK); and a volume drift of the raw eta correction
+// (its mean, which the projection removes) of at most half of max_corr:
+// a network whose output rises or falls the whole water level is off its
+// training data.  Otherwise the plain step stands.
+__device__ __forceinline__ bool corr_ok(const double *sums, double max_corr) {
+    const double mean = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+    return sums[2] <= max_corr && sums[1] == sums[1] && mean == mean && !(sums[3] > 0.0) &&
+           fabs(mean) <= 0.5 * max_corr;
+}
+
 template <typename T>
-__global__ void k_corr_apply(fw::Grid g, fw::Fields<T> f, const float *out, const double *sums, double max_corr) {
-    // the fallback: a correction above max_corr anywhere leaves the plain step
-    if (!(sums[2] <= max_corr) || !(sums[1] == sums[1])) return;
+__global__ void k_corr_apply(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, double max_corr) {
+    const bool ok = corr_ok(sums, max_corr);
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) sums[4] = ok ? 1.0 : 0.0;
+    if (!ok) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mglob || j >= g.Nglob) return;
     const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
@@ -502,9 +521,9 @@ template <typename T> int correct_enqueue(fw_ctx *c, fw_net *n, double max_corr)
     k_corr_input<T><<<gr, b, 0, s>>>(g, f, n->corr_in);
     int rc = forward(n, n->corr_in, npix, 1, g.Nglob, g.Mglob, s);
     if (rc != FW_OK) return rc;
-    double *sums = n->loss;  // 3 doubles of scratch after the loss slot
-    if (cudaMemsetAsync(sums, 0, 4 * sizeof(double), s) != cudaSuccess) return FW_ERR_CUDA;
-    k_corr_sums<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1);
+    double *sums = n->loss;  // 5 doubles of scratch after the loss slot
+    if (cudaMemsetAsync(sums, 0, 6 * sizeof(double), s) != cudaSuccess) return FW_ERR_CUDA;
+    k_corr_sums<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, (float)c->p.min_depth);
     k_corr_apply<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, max_corr);
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
 }
@@ -520,13 +539,13 @@ template <typename T> int correct(fw_ctx *c, fw_net *n, double max_corr, int *ap
     double *sums = n->loss;
     if (applied) {
         // only a caller that asks waits for the decision
-        double h[4];
+        double h[6];
         int st = 0;
         cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return FW_ERR_CUDA;
         if (st != 0) return take_status(n, st, s);
-        *applied = (h[3] <= max_corr && h[2] == h[2]) ? 1 : 0;
+        *applied = h[5] == 1.0 ? 1 : 0;
     }
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
 }
@@ -572,7 +591,7 @@ int fw_net_create(unsigned long long seed, fw_net **out) {
     bool ok = cudaMalloc(&n->w, off * sizeof(float)) == cudaSuccess && cudaMalloc(&n->g, off * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&n->m, off * sizeof(float)) == cudaSuccess && cudaMalloc(&n->v, off * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&n->part, (size_t)WG_BLOCKS * (9 * HID * HID + HID) * sizeof(float)) == cudaSuccess &&
-              cudaMalloc(&n->loss, 4 * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&n->loss, 8 * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&n->status, sizeof(int)) == cudaSuccess;
     size_t ioff = 0;
     for (int i = 0; i < NL + 3; i++) {

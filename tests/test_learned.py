@@ -183,3 +183,57 @@ def test_training_reduces_held_out_error(fw):
     # the eta correction is projected to zero mean over wet cells: the
     # corrected run keeps the plain run's volume budget
     net.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["FP64", "MIXED"])
+def test_correction_fallback_checks(fw, precision):
+    """fw_correct keeps the plain step when a check fails: a correction above
+    max_corr, a volume drift (the raw eta correction's mean, which the
+    projection would remove) above half of max_corr, or a wet cell pushed to
+    or below MinDepth.  The output layer's weights are zero here, so the
+    correction is its bias: eta bias b_e and u bias b_u, in metres and m/s."""
+    import fw_net_oracle as ref
+    params, depth, _ = fw.cases.planar_beach(Mglob=64, Nglob=40, seed=2)
+    depth = np.array(depth)
+    depth[10:14, 5:9] = 0.03          # a patch of shallow wet cells (MinDepth 0.01 m)
+    p = fw.with_defaults(params)
+    net = fw.learned.Net(seed=3)
+    base = net.params()
+    co = ref.LAYERS[-1][1]
+    nlast = 9 * ref.LAYERS[-1][0] * co + co
+
+    def run(b_e, b_u, max_corr, shallow=True):
+        d = depth if shallow else np.maximum(depth, np.where(depth > 0, 0.2, depth))
+        s = fw.Solver(p, precision=precision)
+        s.init(d)
+        s.step(2)
+        w = base.copy()
+        w[-nlast:] = 0.0
+        w[-co:][0] = b_e * fw.learned.OUT_SCALE
+        w[-co:][1] = b_u * fw.learned.OUT_SCALE
+        net.set_params(w)
+        eta0, u0 = s.get("Eta"), s.get("U")
+        applied = net.correct(s, max_corr=max_corr)
+        eta1, u1 = s.get("Eta"), s.get("U")
+        wet = s.get("MASK") > 0
+        s.close()
+        return applied, eta0, eta1, u0, u1, wet
+
+    # size cap
+    a, e0, e1, u0, u1, _ = run(0.0, 0.3, 0.2)
+    assert not a and np.array_equal(e0, e1) and np.array_equal(u0, u1)
+    # volume drift: a uniform rise of 0.15 m against max_corr 0.2 m
+    a, e0, e1, u0, u1, _ = run(0.15, 0.0, 0.2)
+    assert not a and np.array_equal(e0, e1) and np.array_equal(u0, u1)
+    # a uniform fall of 0.04 m would dry the 0.03 m patch
+    a, e0, e1, u0, u1, _ = run(-0.04, 0.05, 0.2)
+    assert not a and np.array_equal(e0, e1) and np.array_equal(u0, u1)
+    # the same without shallow cells passes: the uniform eta part is
+    # projected away (volume kept) and u gets its 0.05 m/s
+    a, e0, e1, u0, u1, wet = run(-0.04, 0.05, 0.2, shallow=False)
+    assert a
+    assert float(np.abs((e1 - e0)[wet]).max()) <= 1e-6
+    du = (u1 - u0)[3:-3, 3:-3][wet[3:-3, 3:-3]]
+    assert np.allclose(du, 0.05, rtol=0, atol=1e-6)
+    net.close()
