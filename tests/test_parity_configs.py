@@ -84,3 +84,16 @@ def test_shoal_crop_50_steps(fw, oracle_mod, where):
     _run_and_compare(s, o, 50, 25)
     s.close()
     o.close()
+
+
+def test_shoal_full_size_3_steps(fw, oracle_mod):
+    """The 2048 x 2048 shoal workload itself (JON_2D 50 x 30 cos^2s from
+    rest, seed of the benchmark): three whole FP64 steps against the oracle
+    at full size (the oracle takes about 5 s a step on 16 cores)."""
+    p, depth, phases = fw.cases.shoal_jonswap(seed=2024)
+    assert (p["Mglob"], p["Nglob"]) == (2048, 2048)
+    s, o = make_pair(fw, oracle_mod, p, depth, None, phases)
+    _run_and_compare(s, o, 3, 3)
+    s.close()
+    o.close()
+
