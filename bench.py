@@ -477,6 +477,101 @@ def net_report(fw, size=1024, reps=20):
             "ms_train_iteration_batch8_128x128": ms_iter}
 
 
+def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coarse_steps=500, batch=8):
+    """The learned coarse-grid correction at the configuration's sizes: fine
+    runs on 2048 x 2048 cells at dx = 1 m, their coarse twins on 1024 x 1024
+    at dx = 2 m; n_traj seeded trajectories (planar, barred and shoal
+    bathymetries, JONSWAP Hs 0.5-2 m) of steps_per_traj coarse steps give
+    n_traj x steps_per_traj pairs (2000 by default), all made by the solver
+    and kept on the GPU; Adam; then on held-out seeds a rollout of
+    eval_coarse_steps against the restricted fine run and the run-up of
+    fine, plain coarse and corrected coarse runs."""
+    import numpy as np
+    import torch
+    L = fw.learned
+    avail_gb = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE") / 1e9
+    if avail_gb < 64:
+        return {"skipped": "only %.0f GB of host memory available (64 needed)" % avail_gb}
+
+    def dt_for(p, h):
+        return round(0.35 * p["DX"] / np.sqrt(9.81 * max(h, 1.0)), 4)
+
+    def hs(seed):
+        return float(0.5 + 1.5 * ((seed * 37) % 10) / 9.0)
+
+    def barred(seed):
+        p, d, ph, _ = fw.cases.barred_beach(2048, 2048, 1.0, seed=seed, wk_from_shore=300.0, nfreq=16, ntheta=4,
+                                            shore_from_east=120.0, Hmo=hs(seed), Sponge_west_width=60.0)
+        p["DT_fixed"] = dt_for(p, float(d.max()))
+        return (p, d, ph)
+
+    def planar(seed):
+        p, d, ph = fw.cases.ensemble_members(1, seed=seed, nfreq=16, ntheta=4,
+                                             cells_range=(2048 * 2048, 2048 * 2048))[0]
+        p["Hmo"] = min(p["Hmo"], 2.0)
+        p["DT_fixed"] = dt_for(p, float(d.max()))
+        return (p, d, ph)
+
+    def shoal(seed):
+        p, d, ph = fw.cases.shoal_jonswap(2048, 2048, dx=1.0, seed=seed, Nfreq=16, Ntheta=4, Hmo=hs(seed),
+                                          Xc_WK=150.0, Sponge_west_width=80.0)
+        p["DT_fixed"] = dt_for(p, float(d.max()))
+        return (p, d, ph)
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda")
+    kinds = [barred, planar, shoal]
+    train_cases = [kinds[k % 3](101 + k) for k in range(n_traj)]
+    t0 = time.perf_counter()
+    X, T, Wm = [], [], []
+    for c in train_cases:
+        x, t, w = L.make_pairs(c, steps_per_traj, every=1)
+        X.append(torch.from_numpy(x).to(dev))
+        T.append(torch.from_numpy(t).to(dev))
+        Wm.append(torch.from_numpy(w).to(dev))
+        del x, t, w
+    npairs = sum(a.shape[0] for a in X)
+    t_pairs = time.perf_counter() - t0
+    net = L.Net(seed=0)
+    t0 = time.perf_counter()
+    rng = np.random.default_rng(0)
+    sizes = np.array([a.shape[0] for a in X], dtype=float)
+    losses = []
+    for it in range(iters):
+        k = rng.choice(len(X), p=sizes / sizes.sum())
+        idx = torch.from_numpy(rng.choice(X[k].shape[0], size=batch, replace=False)).to(dev)
+        losses.append(net.loss_grad(X[k][idx].contiguous(), T[k][idx].contiguous(), Wm[k][idx].contiguous()))
+        net.adam(2e-3 * (0.5 ** (it / max(1, iters // 3))))
+    t_train = time.perf_counter() - t0
+    del X, T, Wm
+    torch.cuda.empty_cache()
+    evals = []
+    for name, c in (("barred_held_out", barred(909)), ("planar_held_out", planar(919)), ("shoal_held_out", shoal(929))):
+        xh, th, wh = L.make_pairs(c, 100, every=5)
+        e0, e1 = L.one_step_error(net, xh, th, wh)
+        del xh, th, wh
+        fine = L.fine_run(c, 2 * eval_coarse_steps)
+        plain, _ = L.rollout(c, eval_coarse_steps)
+        corr, applied = L.rollout(c, eval_coarse_steps, net=net)
+        f = L.restrict(fine["Eta"])
+        m = (plain["MASK"] > 0) & (corr["MASK"] > 0)
+
+        def ru(o):
+            return fw.max_runup(np.pad(o["HeightMax"], 3), o["depth"])
+
+        evals.append({"case": name, "one_step_error_ratio": e1 / e0 if e0 > 0 else None,
+                      "eta_rms_plain_m": float(np.sqrt(np.mean((plain["Eta"] - f)[m] ** 2))),
+                      "eta_rms_corrected_m": float(np.sqrt(np.mean((corr["Eta"] - f)[m] ** 2))),
+                      "max_runup_fine_m": ru(fine), "max_runup_plain_m": ru(plain),
+                      "max_runup_corrected_m": ru(corr), "corrections_applied": applied})
+    net.close()
+    return {"metric": "learned coarse-grid correction at full size", "grid_fine": [2048, 2048],
+            "grid_coarse": [1024, 1024], "pairs": npairs, "trajectories": n_traj, "pairs_s": t_pairs,
+            "train_iters": iters, "batch": batch, "train_s": t_train,
+            "loss_first_last": [float(np.mean(losses[:50])), float(np.mean(losses[-50:]))],
+            "held_out": evals}
+
+
 def learned_report(fw, iters=4000, eval_coarse_steps=500, unroll=1, every=2, scale=1, relax=(0.5, 0.25), nudge=None):
     """The learned coarse-grid correction, at reduced training scale: pairs
     (one coarse step of 2 x dx against two fine steps, restricted) from
@@ -728,6 +823,8 @@ def main():
     ap.add_argument("--learned-iters", type=int, default=4000, help="learned report: Adam iterations")
     ap.add_argument("--net-report", action="store_true",
                     help="time the correction network's forward pass and training iteration")
+    ap.add_argument("--learned-full", action="store_true",
+                    help="the learned correction trained on 2000 solver-generated pairs at 2048^2 / 1024^2")
     ap.add_argument("--learned-report", action="store_true",
                     help="only the learned coarse-grid correction report (training, held-out error, throughput)")
     ap.add_argument("--precision-report", action="store_true",
@@ -742,6 +839,9 @@ def main():
         return reference_arm(args, fw, params, depth, phases)
     if args.net_report:
         print(json.dumps(net_report(fw)), flush=True)
+        return 0
+    if args.learned_full:
+        print(json.dumps(learned_full_report(fw)), flush=True)
         return 0
     if args.learned_report:
         print(json.dumps(learned_report(fw, iters=args.learned_iters, unroll=args.learned_unroll,
