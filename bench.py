@@ -477,7 +477,7 @@ def net_report(fw, size=1024, reps=20):
             "ms_train_iteration_batch8_128x128": ms_iter}
 
 
-def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coarse_steps=500, batch=8):
+def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coarse_steps=2000, batch=8):
     """The learned coarse-grid correction at the configuration's sizes: fine
     runs on 2048 x 2048 cells at dx = 1 m, their coarse twins on 1024 x 1024
     at dx = 2 m; n_traj seeded trajectories (planar, barred and shoal
@@ -559,7 +559,9 @@ def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coar
         def ru(o):
             return fw.max_runup(np.pad(o["HeightMax"], 3), o["depth"])
 
-        evals.append({"case": name, "one_step_error_ratio": e1 / e0 if e0 > 0 else None,
+        evals.append({"case": name, "coarse_steps": eval_coarse_steps,
+                      "simulated_s": eval_coarse_steps * 2.0 * c[0]["DT_fixed"],
+                      "one_step_error_ratio": e1 / e0 if e0 > 0 else None,
                       "eta_rms_plain_m": float(np.sqrt(np.mean((plain["Eta"] - f)[m] ** 2))),
                       "eta_rms_corrected_m": float(np.sqrt(np.mean((corr["Eta"] - f)[m] ** 2))),
                       "max_runup_fine_m": ru(fine), "max_runup_plain_m": ru(plain),

@@ -601,6 +601,7 @@ int fw_create(const fw_params *p, fw_ctx **out) {
     g.track_hmin = p->track_hmin;
     g.track_roller = p->track_roller;
     g.track_rad = p->track_radiation && p->steady_time < 999999.0 ? 1 : 0;
+    g.brk_passes = 8;
     g.track_umax = p->track_umax;
     g.track_mfmax = p->track_mfmax;
     g.steady_time = p->steady_time;
@@ -929,6 +930,7 @@ int fw_get_scalar(fw_ctx *c, const char *name, double *v) {
     else if (!std::strcmp(name, "jhi")) *v = c->g.jhi + 1;
     else if (!std::strcmp(name, "pitch")) *v = c->g.pitch;
     else if (!std::strcmp(name, "WAIT_LIMIT")) *v = c->fmaps[0][0][0].wait_limit;
+    else if (!std::strcmp(name, "BREAK_PASSES")) *v = c->g.brk_passes;
     else return FW_ERR_BAD_PARAM;
     return FW_OK;
 }
@@ -938,6 +940,10 @@ int fw_set_scalar(fw_ctx *c, const char *name, double v) {
     if (!std::strcmp(name, "TIME") || !std::strcmp(name, "DT")) {
         const int slot = !std::strcmp(name, "TIME") ? S_TIME : S_DT;
         cudaError_t e = cudaMemcpyAsync(dsc_ptr(c) + slot, &v, sizeof(double), cudaMemcpyHostToDevice, c->stream);
+        // the mixed path's float copies of DT and 1/DT follow a set DT
+        const float fdt[2] = {(float)v, (float)(1.0 / v)};
+        if (e == cudaSuccess && slot == S_DT && c->p.precision != FW_PREC_FP64)
+            e = cudaMemcpyAsync(c->ff.fsc + FS_DT, fdt, sizeof(fdt), cudaMemcpyHostToDevice, c->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         return cuda_status(c, e);
     }
@@ -947,6 +953,9 @@ int fw_set_scalar(fw_ctx *c, const char *name, double v) {
         for (auto &by_dir : c->fmaps)
             for (auto &by_fy : by_dir)
                 for (auto &m : by_fy) m.wait_limit = (unsigned)v;
+    } else if (!std::strcmp(name, "BREAK_PASSES")) {
+        if (!(v >= 0.0 && v <= 1.0e6)) return FW_ERR_BAD_PARAM;
+        c->g.brk_passes = (int)v;
     } else if (!std::strcmp(name, "T_brk")) {
         c->g.T_brk = v;
         fill_float_constants(c->g);

@@ -31,6 +31,7 @@ struct Grid {
     int track_hmin, track_umax, track_mfmax, stats;  // statistics switches
     int track_roller;        // BREAKING's roller flux and undertow (ROLLER / UNDERTOW output)
     int track_rad;           // CALCULATE_MEAN's radiation-stress, momentum-flux, dissipation sums
+    int brk_passes;          // fixed-point passes of the breaking sweep before the level-ordered one
     double steady_time, t_intv_mean;
     double DX, DY;
     double gamma1, gamma2, gamma3, b1, b2, Beta_1, Beta_2;

@@ -2531,32 +2531,146 @@ __device__ __forceinline__ bool brk_neigh(const Grid &g, const Fields<T> &f, con
     return hit;
 }
 
-// Candidates of the sweep: iterate to the fixed point, then set nu.  One
-// block; every pass either turns at least one candidate from 0 to DT or
-// ends the loop, so it runs at most ncand+1 passes.
+// one candidate of the sweep: 0 -> DT when a neighbour before it carries
+// the age far enough (breaker.F:182-224)
+template <typename T>
+__device__ __forceinline__ bool brk_try(const Grid &g, const Fields<T> &f, volatile T *N, int code, T DT) {
+    const int i = code % g.pitch, j = code / g.pitch;
+    const size_t id = IDX(i, j);
+    if (N[id] != (T)0 || !brk_neigh(g, f, N, i, j, DT)) return false;
+    N[id] = DT;
+    return true;
+}
+
+// exclusive prefix sum over a 1024-thread block (wsum: 32 ints of shared
+// memory); returns this thread's prefix
+__device__ __forceinline__ int block_scan_1024(int x, int *wsum) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int inc = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += y;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const int w = wsum[lane];
+        int wi = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, wi, d);
+            if (lane >= d) wi += y;
+        }
+        wsum[lane] = wi - w;
+    }
+    __syncthreads();
+    const int r = wsum[warp] + inc - x;
+    __syncthreads();
+    return r;
+}
+
+// Candidates of the sweep, in one 1024-thread block, then nu.  The sweep
+// (j outer, i inner) lets a candidate read the new values of (i-1,j),
+// (i-1,j-1), (i,j-1), (i+1,j-1) (cells before it) and the old values of
+// the cells after it, so new values only flow forward and a candidate
+// turns from 0 to DT at most once.
+//  - Passes to the fixed point: every candidate tests its neighbours in
+//    parallel, and the pass repeats while any changed.  What a pass sets
+//    is also set by the sequential sweep (by induction over the passes),
+//    so the fixed point is its result.  A chain of k candidates that set
+//    one another takes k + 1 passes; most stages need two or three.
+//  - After g.brk_passes passes without the fixed point, the rest in one
+//    pass by level t = i + 2j: the cells a candidate reads new values of
+//    lie on levels t-1, t-3, t-2, t-1, the cells it reads old values of on
+//    levels above t.  The candidates are sorted by level (a histogram, its
+//    prefix sum and a scatter, into the line solver's tq and tp planes,
+//    which are free between the stage's line solve and the next) and the
+//    non-empty levels are worked in order, one barrier each.  Starting
+//    from any pass's state (a subset of the sweep's result) this gives the
+//    sweep's result, in time bounded by the candidates and the levels
+//    (at most Mglob + 2 Nglob + 7) whatever the breaking pattern.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_break_b(Grid g, Fields<T> f) {
     __shared__ int changed;
+    __shared__ int wsum[32];
+    __shared__ int lev_beg[1024], lev_end[1024];
+    __shared__ unsigned nonempty[32];
     const int n = *f.ncand;
     const T DT = DTV;
     volatile T *N = f.AGEn;
-    for (int pass = 0; pass <= n; pass++) {
+    bool done = false;
+    for (int pass = 0; pass < g.brk_passes && pass <= n; pass++) {
         if (threadIdx.x == 0) changed = 0;
         __syncthreads();
-        for (int c = threadIdx.x; c < n; c += blockDim.x) {
-            const int code = f.cand[c];
-            const int i = code % g.pitch, j = code / g.pitch;
-            const size_t id = IDX(i, j);
-            if (N[id] != (T)0) continue;
-            if (brk_neigh(g, f, N, i, j, DT)) {
-                N[id] = DT;
-                changed = 1;
-            }
-        }
+        for (int c = threadIdx.x; c < n; c += blockDim.x)
+            if (brk_try(g, f, N, f.cand[c], DT)) changed = 1;
         __syncthreads();
         const int ch = changed;
         __syncthreads();
-        if (!ch) break;
+        if (!ch) {
+            done = true;
+            break;
+        }
+    }
+    if (!done && n > 0) {
+        // levels of the candidate range Ibeg-1..Iend+1 x Jbeg-1..Jend+1
+        const int i0 = g.ib - 1, j0 = g.jb - 1;
+        const int nlev = (g.ie + 1 - i0) + 2 * (g.je + 1 - j0) + 1;
+        volatile int *off = reinterpret_cast<volatile int *>(f.tq);
+        int *off_a = reinterpret_cast<int *>(f.tq);
+        int *sorted = reinterpret_cast<int *>(f.tp);
+        auto level = [&](int code) { return (code % g.pitch - i0) + 2 * (code / g.pitch - j0); };
+        for (int t = threadIdx.x; t < nlev; t += 1024) off[t] = 0;
+        __syncthreads();
+        for (int c = threadIdx.x; c < n; c += 1024) atomicAdd(&off_a[level(f.cand[c])], 1);
+        __syncthreads();
+        // counts -> exclusive offsets: each thread takes a run of levels
+        const int per = (nlev + 1023) / 1024;
+        const int lo = min((int)threadIdx.x * per, nlev), hi = min(lo + per, nlev);
+        int sum = 0;
+        for (int t = lo; t < hi; t++) sum += off[t];
+        int acc = block_scan_1024(sum, wsum);
+        for (int t = lo; t < hi; t++) {
+            const int v = off[t];
+            off[t] = acc;
+            acc += v;
+        }
+        __syncthreads();
+        // scatter; afterwards off[t] is the end of level t
+        for (int c = threadIdx.x; c < n; c += 1024) {
+            const int code = f.cand[c];
+            sorted[atomicAdd(&off_a[level(code)], 1)] = code;
+        }
+        __syncthreads();
+        // the levels in order, 1024 at a time: each thread flags its level
+        // if non-empty, and all threads walk the same flags, so every
+        // thread reaches the same barriers
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        for (int t0 = 0; t0 < nlev; t0 += 1024) {
+            const int t = t0 + threadIdx.x;
+            int b = 0, e = 0;
+            if (t < nlev) {
+                e = off[t];
+                b = t == 0 ? 0 : off[t - 1];
+            }
+            lev_beg[threadIdx.x] = b;
+            lev_end[threadIdx.x] = e;
+            const unsigned m = __ballot_sync(0xffffffffu, e > b);
+            if (lane == 0) nonempty[warp] = m;
+            __syncthreads();
+            for (int w = 0; w < 32; w++) {
+                unsigned mw = nonempty[w];
+                while (mw) {
+                    const int k = w * 32 + __ffs(mw) - 1;
+                    mw &= mw - 1;
+                    for (int c = lev_beg[k] + threadIdx.x; c < lev_end[k]; c += 1024)
+                        brk_try(g, f, N, sorted[c], DT);
+                    __syncthreads();
+                }
+            }
+            __syncthreads();  // all have read the flags before the next chunk's
+        }
     }
     for (int c = threadIdx.x; c < n; c += blockDim.x) {
         const int code = f.cand[c];

@@ -181,7 +181,12 @@ int fw_get_points(fw_ctx *ctx, const char *name, int n, const int *I, const int 
  * (0 = the default, about 0.3-1 s).  A wait that runs out leaves the
  * block's fluxes NaN, and the step reports FW_ERR_NAN; the context stays
  * usable.  Lowering it makes that path run on purpose (a test of failure
- * reporting).  Setting it drops the captured step graphs. */
+ * reporting).  Setting it drops the captured step graphs.
+ * "BREAK_PASSES" (get and set) is not a reference quantity either: the
+ * parallel passes of BREAKING's candidate sweep (breaker.F:182-224) before
+ * the rest runs in one pass ordered by level i + 2j (default 8; 0 = the
+ * level-ordered pass only).  Every value gives the sweep's result; it only
+ * moves the time.  Setting it drops the captured step graphs. */
 int fw_get_scalar(fw_ctx *ctx, const char *name, double *value);
 int fw_set_scalar(fw_ctx *ctx, const char *name, double value);
 
