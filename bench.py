@@ -477,15 +477,18 @@ def net_report(fw, size=1024, reps=20):
             "ms_train_iteration_batch8_128x128": ms_iter}
 
 
-def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coarse_steps=2000, batch=8):
+def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coarse_steps=2000, batch=8,
+                        n_train=3):
     """The learned coarse-grid correction at the configuration's sizes: fine
     runs on 2048 x 2048 cells at dx = 1 m, their coarse twins on 1024 x 1024
     at dx = 2 m; n_traj seeded trajectories (planar, barred and shoal
     bathymetries, JONSWAP Hs 0.5-2 m) of steps_per_traj coarse steps give
     n_traj x steps_per_traj pairs (2000 by default), all made by the solver
-    and kept on the GPU; Adam; then on held-out seeds a rollout of
-    eval_coarse_steps against the restricted fine run and the run-up of
-    fine, plain coarse and corrected coarse runs."""
+    and kept on the GPU; n_train trainings with Adam, each from its own
+    initial weights and batch order; then on held-out seeds, per training,
+    the one-step error ratio, the eta RMS against the restricted fine run
+    after 500 and after eval_coarse_steps coarse steps, and the maximum
+    run-up of fine, plain coarse and corrected coarse runs."""
     import numpy as np
     import torch
     L = fw.learned
@@ -532,46 +535,65 @@ def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coar
         del x, t, w
     npairs = sum(a.shape[0] for a in X)
     t_pairs = time.perf_counter() - t0
-    net = L.Net(seed=0)
-    t0 = time.perf_counter()
-    rng = np.random.default_rng(0)
     sizes = np.array([a.shape[0] for a in X], dtype=float)
-    losses = []
-    for it in range(iters):
-        k = rng.choice(len(X), p=sizes / sizes.sum())
-        idx = torch.from_numpy(rng.choice(X[k].shape[0], size=batch, replace=False)).to(dev)
-        losses.append(net.loss_grad(X[k][idx].contiguous(), T[k][idx].contiguous(), Wm[k][idx].contiguous()))
-        net.adam(2e-3 * (0.5 ** (it / max(1, iters // 3))))
-    t_train = time.perf_counter() - t0
+    nets, t_train, losses = [], [], []
+    for tr in range(n_train):
+        # each training: its own initial weights and batch order
+        net = L.Net(seed=tr)
+        rng = np.random.default_rng(tr)
+        t0 = time.perf_counter()
+        lo = []
+        for it in range(iters):
+            k = rng.choice(len(X), p=sizes / sizes.sum())
+            idx = torch.from_numpy(rng.choice(X[k].shape[0], size=batch, replace=False)).to(dev)
+            lo.append(net.loss_grad(X[k][idx].contiguous(), T[k][idx].contiguous(), Wm[k][idx].contiguous()))
+            net.adam(2e-3 * (0.5 ** (it / max(1, iters // 3))))
+        t_train.append(time.perf_counter() - t0)
+        losses.append([float(np.mean(lo[:50])), float(np.mean(lo[-50:]))])
+        nets.append(net)
     del X, T, Wm
     torch.cuda.empty_cache()
+
+    def ru(o):
+        return fw.max_runup(np.pad(o["HeightMax"], 3), o["depth"])
+
+    def rms(a, ref, mask):
+        return float(np.sqrt(np.mean((a - ref)[mask] ** 2)))
+
+    n_short = min(500, eval_coarse_steps)
     evals = []
     for name, c in (("barred_held_out", barred(909)), ("planar_held_out", planar(919)), ("shoal_held_out", shoal(929))):
         xh, th, wh = L.make_pairs(c, 100, every=5)
-        e0, e1 = L.one_step_error(net, xh, th, wh)
+        ratios = []
+        for net in nets:
+            e0, e1 = L.one_step_error(net, xh, th, wh)
+            ratios.append(e1 / e0 if e0 > 0 else None)
         del xh, th, wh
-        fine = L.fine_run(c, 2 * eval_coarse_steps)
-        plain, _ = L.rollout(c, eval_coarse_steps)
-        corr, applied = L.rollout(c, eval_coarse_steps, net=net)
-        f = L.restrict(fine["Eta"])
-        m = (plain["MASK"] > 0) & (corr["MASK"] > 0)
-
-        def ru(o):
-            return fw.max_runup(np.pad(o["HeightMax"], 3), o["depth"])
-
-        evals.append({"case": name, "coarse_steps": eval_coarse_steps,
-                      "simulated_s": eval_coarse_steps * 2.0 * c[0]["DT_fixed"],
-                      "one_step_error_ratio": e1 / e0 if e0 > 0 else None,
-                      "eta_rms_plain_m": float(np.sqrt(np.mean((plain["Eta"] - f)[m] ** 2))),
-                      "eta_rms_corrected_m": float(np.sqrt(np.mean((corr["Eta"] - f)[m] ** 2))),
-                      "max_runup_fine_m": ru(fine), "max_runup_plain_m": ru(plain),
-                      "max_runup_corrected_m": ru(corr), "corrections_applied": applied})
-    net.close()
+        fine = L.fine_run(c, 2 * eval_coarse_steps, snaps=(2 * n_short,))
+        plain, _ = L.rollout(c, eval_coarse_steps, snaps=(n_short,))
+        f_short = L.restrict(fine["snaps"][2 * n_short][0])
+        f_long = L.restrict(fine["Eta"])
+        p_short = plain["snaps"][n_short]
+        ev = {"case": name, "coarse_steps": [n_short, eval_coarse_steps],
+              "simulated_s": [n_short * 2.0 * c[0]["DT_fixed"], eval_coarse_steps * 2.0 * c[0]["DT_fixed"]],
+              "one_step_error_ratio": ratios, "max_runup_fine_m": ru(fine), "max_runup_plain_m": ru(plain),
+              "trainings": []}
+        for net in nets:
+            corr, applied = L.rollout(c, eval_coarse_steps, net=net, snaps=(n_short,))
+            c_short = corr["snaps"][n_short]
+            m_short = (p_short[1] > 0) & (c_short[1] > 0)
+            m_long = (plain["MASK"] > 0) & (corr["MASK"] > 0)
+            ev["trainings"].append({
+                "eta_rms_plain_m": [rms(p_short[0], f_short, m_short), rms(plain["Eta"], f_long, m_long)],
+                "eta_rms_corrected_m": [rms(c_short[0], f_short, m_short), rms(corr["Eta"], f_long, m_long)],
+                "max_runup_corrected_m": ru(corr), "corrections_applied": applied})
+        evals.append(ev)
+    for net in nets:
+        net.close()
     return {"metric": "learned coarse-grid correction at full size", "grid_fine": [2048, 2048],
             "grid_coarse": [1024, 1024], "pairs": npairs, "trajectories": n_traj, "pairs_s": t_pairs,
-            "train_iters": iters, "batch": batch, "train_s": t_train,
-            "loss_first_last": [float(np.mean(losses[:50])), float(np.mean(losses[-50:]))],
-            "held_out": evals}
+            "train_iters": iters, "batch": batch, "trainings": n_train, "train_s": t_train,
+            "loss_first_last": losses, "held_out": evals}
 
 
 def learned_report(fw, iters=4000, eval_coarse_steps=500, unroll=1, every=2, scale=1, relax=(0.5, 0.25), nudge=None):

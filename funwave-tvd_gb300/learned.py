@@ -305,10 +305,11 @@ def one_step_error(net, x, t, w):
     return e0, e1
 
 
-def rollout(case, nsteps_c, net=None, precision="MIXED", max_corr=0.2):
+def rollout(case, nsteps_c, net=None, precision="MIXED", max_corr=0.2, snaps=()):
     """The coarse twin of case run for nsteps_c steps, with the network's
     correction after every step when net is given; returns (coarse solver
-    state dict of interior Eta, U, V, HeightMax; steps corrected)."""
+    state dict of interior Eta, U, V, HeightMax, and in "snaps" the interior
+    Eta and MASK after each step count of snaps; steps corrected)."""
     pf, depth, phases = case
     pc, depth_c = coarse_case(with_defaults(pf), depth)
     pc = with_defaults(pc)
@@ -316,25 +317,40 @@ def rollout(case, nsteps_c, net=None, precision="MIXED", max_corr=0.2):
     cs = Solver(pc, precision=precision)
     cs.init(depth_c, phases=phases)
     applied = 0
-    for _ in range(nsteps_c):
+    taken = {}
+    for k in range(nsteps_c):
         cs.step(1)
         if net is not None:
             applied += int(net.correct(cs, max_corr))
+        if k + 1 in snaps:
+            taken[k + 1] = (_interior(cs.get("Eta")), _interior(cs.get("MASK")))
     out = {n: _interior(cs.get(n)) for n in ("Eta", "U", "V", "HeightMax", "MASK")}
+    out["snaps"] = taken
     out["TIME"] = cs.scalar("TIME")
     out["depth"] = depth_c
     cs.close()
     return out, applied
 
 
-def fine_run(case, nsteps_f, precision="MIXED"):
+def fine_run(case, nsteps_f, precision="MIXED", snaps=()):
+    """The fine case run for nsteps_f steps; the state dict as rollout's,
+    "snaps" holding the interior Eta and MASK after each step count of
+    snaps."""
     pf, depth, phases = case
     pf = with_defaults(pf)
     pf["OUT_Hmax"] = True
     fs = Solver(pf, precision=precision)
     fs.init(depth, phases=phases)
-    fs.step(nsteps_f)
+    taken, done = {}, 0
+    for k in sorted(set(snaps) | {nsteps_f}):
+        if k > nsteps_f:
+            break
+        fs.step(k - done)
+        done = k
+        if k in snaps:
+            taken[k] = (_interior(fs.get("Eta")), _interior(fs.get("MASK")))
     out = {n: _interior(fs.get(n)) for n in ("Eta", "U", "V", "HeightMax", "MASK")}
+    out["snaps"] = taken
     out["TIME"] = fs.scalar("TIME")
     out["depth"] = depth
     fs.close()

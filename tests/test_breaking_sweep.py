@@ -92,7 +92,8 @@ def test_level_pass_alone_in_whole_steps(fw, oracle_mod, precision):
     """Graph-captured steps of a breaking beach with BREAK_PASSES = 0 give
     the state of the default bit for bit; FP64 also matches the oracle."""
     p, _, _ = fw.cases.planar_beach(Mglob=96, Nglob=50, seed=31)
-    p.update({"PERIODIC": False, "Cbrk1": 0.2, "Cbrk2": 0.1})
+    # low onset thresholds: breaking from the first steps, with candidates
+    p.update({"PERIODIC": False, "Cbrk1": 0.03, "Cbrk2": 0.015})
     depth = sloped_beach(96, 50, h0=3.0, h1=-0.8, seed=32)
     state = fw.cases.random_state(96, 50, seed=33, eta_amp=0.2, u_amp=0.3)
     out = {}
@@ -109,6 +110,6 @@ def test_level_pass_alone_in_whole_steps(fw, oracle_mod, precision):
                 assert maxrel(interior(s.get(name)), interior(o[name])) <= 1e-9, name
         s.close()
         o.close()
-    assert (out[8]["AGE"] > 0).any()
+    assert (out[8]["AGE"] > 0).sum() > 100
     for k in out[8]:
         assert np.array_equal(out[8][k], out[0][k]), k
