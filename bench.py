@@ -436,9 +436,10 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
 def net_report(fw, size=1024, reps=20):
     """The correction network alone, on a size x size coarse grid: the
     forward pass (packing, four tcgen05 convolutions) and one training
-    iteration (forward, loss, backward with tcgen05 data gradients and
-    CUDA-core weight gradients, Adam) on a batch of 8 tiles of 128 x 128,
-    CUDA events on the current stream after 3 warm-up calls.  Tensor work:
+    iteration (forward, loss, backward with tcgen05 data and weight
+    gradients, Adam) on a batch of 8 tiles of 128 x 128 and on a batch of 8
+    whole size x size grids (the full-size training's batch), CUDA events on
+    the current stream after 3 warm-up calls.  Tensor work:
     2 x 9 x (16*32 + 32*32 + 32*32 + 32*16) MACs a pixel in the forward pass
     (channels as padded for the tensor cores)."""
     import torch
@@ -456,25 +457,30 @@ def net_report(fw, size=1024, reps=20):
     e1.record()
     e1.synchronize()
     ms_fwd = e0.elapsed_time(e1) / reps
-    xb = torch.randn((8, 128, 128, 5), device="cuda", generator=g)
-    tb = torch.randn((8, 128, 128, 3), device="cuda", generator=g)
-    wb = torch.ones((8, 128, 128), device="cuda")
-    for _ in range(3):
-        net.loss_grad(xb, tb, wb)
-        net.adam(1e-4)
-    torch.cuda.synchronize()
-    e0.record()
-    for _ in range(reps):
-        net.loss_grad(xb, tb, wb)
-        net.adam(1e-4)
-    e1.record()
-    e1.synchronize()
-    ms_iter = e0.elapsed_time(e1) / reps
+    def train_ms(hw):
+        xb = torch.randn((8, hw, hw, 5), device="cuda", generator=g)
+        tb = torch.randn((8, hw, hw, 3), device="cuda", generator=g)
+        wb = torch.ones((8, hw, hw), device="cuda")
+        for _ in range(3):
+            net.loss_grad(xb, tb, wb)
+            net.adam(1e-4)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            net.loss_grad(xb, tb, wb)
+            net.adam(1e-4)
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_iter = train_ms(128)
+    ms_iter_full = train_ms(size)
     net.close()
     macs = 9 * (16 * 32 + 32 * 32 + 32 * 32 + 32 * 16)
     return {"metric": "correction network", "grid": [size, size], "ms_forward": ms_fwd,
             "forward_tflops_padded": 2.0 * macs * size * size / (ms_fwd * 1e-3) / 1e12,
-            "ms_train_iteration_batch8_128x128": ms_iter}
+            "ms_train_iteration_batch8_128x128": ms_iter,
+            "ms_train_iteration_batch8_%dx%d" % (size, size): ms_iter_full}
 
 
 def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coarse_steps=2000, batch=8,

@@ -14,13 +14,15 @@
 // -> 32 ReLU -> 3.  Weight index [k][ci][co] with k = (ky+1)*3 + (kx+1) for
 // the tap at (x+kx, y+ky).
 //
-// The forward convolutions and the data gradients of the backward pass run
-// on the tcgen05 tensor cores (fw_tc.cuh).  Their BF16 activations and
-// gradients are stored chunk-planar with a zero border (fwtc::act_idx); the
-// network's FP32 inputs and outputs are plain [pixel][channel].  The backward pass carries the
-// gradient of each hidden activation in BF16 with the ReLU mask already
+// The forward convolutions, the data gradients and the weight and bias
+// gradients of the backward pass run on the tcgen05 tensor cores
+// (fw_tc.cuh).  Their BF16 activations and gradients are stored
+// chunk-planar with a zero border (fwtc::act_idx); the network's FP32
+// inputs and outputs are plain [pixel][channel].  The backward pass carries
+// the gradient of each hidden activation in BF16 with the ReLU mask already
 // applied (dy * [act > 0]), as the tensor-core data-gradient kernel writes
-// it; the weight gradients reduce those BF16 values in FP32.
+// it; the weight gradients sum those BF16 values times the BF16 inputs in
+// FP32 (per CTA in TMEM, then over the CTAs).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -44,80 +46,15 @@ constexpr int HID = 32;
 constexpr int NOUT = 3;
 constexpr int LCIN[NL] = {CIN0, HID, HID, HID};
 constexpr int LCOUT[NL] = {HID, HID, HID, NOUT};
-constexpr int WG_BLOCKS = 304;  // wgrad partial blocks (2 per SM)
+constexpr long long WG_PART = 304LL * (9 * 32 * 32 + 32);  // floats of the weight-gradient partials
 
 typedef __nv_bfloat16 bf16;
-
-__device__ __forceinline__ float bf(bf16 v) { return __bfloat162float(v); }
 
 // BF16 of a float, round to nearest even
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     const uint32_t l = __bfloat16_as_ushort(__float2bfloat16(lo));
     const uint32_t h = __bfloat16_as_ushort(__float2bfloat16(hi));
     return l | (h << 16);
-}
-
-// weight and bias gradients.  A tile is a row segment of TPX pixels; its
-// three input rows (with one pixel of halo on each side, zero outside the
-// grid) and its masked BF16 dy are staged in shared memory, then every
-// thread adds its share of the 9*CIN*COUT + COUT entries over the tile.
-// Each of the WG_BLOCKS blocks walks many tiles and writes one partial;
-// k_wgrad_reduce adds the partials.  x and dy are padded chunk-planar
-// activations (fwtc::act_idx) with XCC and DYCC chunks (the first CIN and
-// COUT channels used).
-constexpr int TPX = 64;
-template <int CIN, int COUT, int XCC, int DYCC>
-__global__ void __launch_bounds__(256) k_conv_wgrad(const bf16 *__restrict__ x, const bf16 *__restrict__ dy,
-                                                    float *__restrict__ part, int B, int H, int W) {
-    constexpr int E = 9 * CIN * COUT + COUT;
-    constexpr int NE = (E + 255) / 256;
-    __shared__ float xs[3][TPX + 2][CIN];
-    __shared__ float dys[TPX][COUT];
-    float acc[NE];
-#pragma unroll
-    for (int r = 0; r < NE; r++) acc[r] = 0.0f;
-    const fwtc::ActGeom gx_{B, H, W, XCC}, gd_{B, H, W, DYCC};
-    const int tiles_x = (W + TPX - 1) / TPX;
-    const long long ntiles = (long long)B * H * tiles_x;
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int tx = (int)(tile % tiles_x);
-        const long long row = tile / tiles_x;  // b*H + y
-        const int py = (int)(row % H), pb = (int)(row / H);
-        const int x0 = tx * TPX;
-        __syncthreads();
-        for (int e = threadIdx.x; e < 3 * (TPX + 2) * CIN; e += blockDim.x) {
-            const int ci = e % CIN, c = (e / CIN) % (TPX + 2), r = e / (CIN * (TPX + 2));
-            const int gx = x0 + c - 1, gy = py + r - 1;
-            float v = 0.0f;
-            if (gx >= 0 && gx < W && gy >= 0 && gy < H) v = bf(x[8 * fwtc::act_idx(gx_, pb, gy, ci >> 3, gx) + (ci & 7)]);
-            xs[r][c][ci] = v;
-        }
-        for (int e = threadIdx.x; e < TPX * COUT; e += blockDim.x) {
-            const int co = e % COUT, t = e / COUT;
-            dys[t][co] = x0 + t < W ? bf(dy[8 * fwtc::act_idx(gd_, pb, py, co >> 3, x0 + t) + (co & 7)]) : 0.0f;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < NE; r++) {
-            const int e = threadIdx.x + r * 256;
-            if (e >= E) continue;
-            float s = 0.0f;
-            if (e < 9 * CIN * COUT) {
-                const int co = e % COUT, ci = (e / COUT) % CIN, k = e / (COUT * CIN);
-                const int kx = k % 3, ky = k / 3;  // 0..2: tap offset + 1
-                for (int t = 0; t < TPX; t++) s += xs[ky][t + kx][ci] * dys[t][co];
-            } else {
-                const int co = e - 9 * CIN * COUT;
-                for (int t = 0; t < TPX; t++) s += dys[t][co];
-            }
-            acc[r] += s;
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < NE; r++) {
-        const int e = threadIdx.x + r * 256;
-        if (e < E) part[(size_t)blockIdx.x * E + e] = acc[r];
-    }
 }
 
 __global__ void k_wgrad_reduce(const float *part, int nblocks, int E, float *gw, float *gb, int nw) {
@@ -414,20 +351,48 @@ bool conv_attrs_all() {
            conv_attr<4, 32, EPI_MASK_BF16, 0>();
 }
 
+// the weight-gradient kernels' shared-memory size, set once like conv_attr
+template <int CIN, int COUT, int XCC, int DYCC> bool wgrad_attr() {
+    static bool attr = false;
+    if (!attr) {
+        constexpr int CCU = (CIN + 7) / 8;
+        if (cudaFuncSetAttribute(fwtc::k_wgrad_tc<XCC, CCU, DYCC, CIN, COUT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 fwtc::WLayout<CCU, DYCC>::BYTES) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        attr = true;
+    }
+    return true;
+}
+
+bool wgrad_attrs_all() {
+    return wgrad_attr<HID, NOUT, HID / 8, GC3 / 8>() && wgrad_attr<HID, HID, HID / 8, HID / 8>() &&
+           wgrad_attr<CIN0, HID, XC0 / 8, HID / 8>();
+}
+
+// SMs of the current device (0 on error)
+int sm_count() {
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            nsm = 0;
+        }
+    }
+    return nsm;
+}
+
 template <int CINC, int N, int EPI, int NOUTF>
 int conv_tc(const bf16 *x, const bf16 *img, const float *bias, const bf16 *act, void *y, int B, int H, int W,
             int *status, unsigned wait_limit, cudaStream_t s) {
     using Lt = fwtc::Layout<CINC, N>;
     auto k = fwtc::k_conv_tc<CINC, N, EPI, NOUTF>;
     if (!conv_attr<CINC, N, EPI, NOUTF>()) return FW_ERR_CUDA;
-    static int nsm = 0;
-    if (!nsm) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
-            cudaGetLastError();
-            return FW_ERR_CUDA;
-        }
-    }
+    const int nsm = sm_count();
+    if (!nsm) return FW_ERR_CUDA;
     const long long ntiles = (long long)((W + fwtc::TPX - 1) / fwtc::TPX) * ((H + fwtc::TROWS - 1) / fwtc::TROWS) * B;
     const unsigned grid = (unsigned)std::min<long long>(ntiles, (long long)nsm * Lt::PER_SM);
     k<<<grid, 64 + 32 * fwtc::EPI_WARPS, Lt::BYTES, s>>>(x, img, bias, act, y, H, W, B, status,
@@ -448,7 +413,8 @@ int take_status(fw_net *n, int st, cudaStream_t s) {
 // the tensor-core kernels number their tiles in an int
 bool shape_ok(int B, int H, int W) {
     return B > 0 && H > 0 && W > 0 &&
-           (long long)((W + fwtc::TPX - 1) / fwtc::TPX) * ((H + fwtc::TROWS - 1) / fwtc::TROWS) * B < (1LL << 31);
+           (long long)((W + fwtc::TPX - 1) / fwtc::TPX) * ((H + fwtc::TROWS - 1) / fwtc::TROWS) * B < (1LL << 31) &&
+           (long long)((W + fwtc::WKT - 1) / fwtc::WKT) * H * B < (1LL << 31);
 }
 
 void pack_images(fw_net *n, cudaStream_t s) {
@@ -478,12 +444,24 @@ int forward(fw_net *n, const float *in, long long npix, int B, int H, int W, cud
     return rc;
 }
 
+// weight and bias gradients of layer l on the tensor cores
+// (fwtc::k_wgrad_tc): one partial per CTA, then k_wgrad_reduce adds them
 template <int CIN, int COUT, int XCC, int DYCC>
-void wgrad(fw_net *n, int l, const bf16 *x, const bf16 *dy, int B, int H, int W, cudaStream_t s) {
-    constexpr int E = 9 * CIN * COUT + COUT;
-    k_conv_wgrad<CIN, COUT, XCC, DYCC><<<WG_BLOCKS, 256, 0, s>>>(x, dy, n->part, B, H, W);
-    k_wgrad_reduce<<<nblk(E, 256), 256, 0, s>>>(n->part, WG_BLOCKS, E, n->g + n->woff[l], n->g + n->boff[l],
+int wgrad(fw_net *n, int l, const bf16 *x, const bf16 *dy, int B, int H, int W, cudaStream_t s) {
+    constexpr int CCU = (CIN + 7) / 8, E = 9 * CIN * COUT + COUT;
+    using Lw = fwtc::WLayout<CCU, DYCC>;
+    if (!wgrad_attr<CIN, COUT, XCC, DYCC>()) return FW_ERR_CUDA;
+    const int nsm = sm_count();
+    if (!nsm) return FW_ERR_CUDA;
+    const long long ntiles = (long long)((W + fwtc::WKT - 1) / fwtc::WKT) * H * B;
+    // the partial buffer holds WG_PART floats
+    const long long cap = WG_PART / E;
+    const unsigned grid = (unsigned)std::min<long long>(std::min<long long>(ntiles, (long long)nsm * Lw::PER_SM), cap);
+    fwtc::k_wgrad_tc<XCC, CCU, DYCC, CIN, COUT><<<grid, 192, Lw::BYTES, s>>>(x, dy, n->part, H, W, B, n->status,
+                                                                            n->wait_limit);
+    k_wgrad_reduce<<<nblk(E, 256), 256, 0, s>>>(n->part, (int)grid, E, n->g + n->woff[l], n->g + n->boff[l],
                                                  9 * CIN * COUT);
+    return FW_OK;
 }
 
 // the output gradient is in gout; the images are current (forward ran)
@@ -491,18 +469,20 @@ int backward(fw_net *n, int B, int H, int W, cudaStream_t s) {
     using namespace fwtc;
     const bf16 *im = n->img;
     bf16 *ga = n->gbuf[0], *gb = n->gbuf[1];
-    wgrad<HID, NOUT, HID / 8, GC3 / 8>(n, 3, n->act[3], n->gout, B, H, W, s);
+    int rc = wgrad<HID, NOUT, HID / 8, GC3 / 8>(n, 3, n->act[3], n->gout, B, H, W, s);
     // gradient of act[3] (the output of layer 2), masked by its ReLU
-    int rc = conv_tc<2, 32, EPI_MASK_BF16, 0>(n->gout, im + n->img_off[NL + 2], nullptr, n->act[3], ga, B, H, W,
+    if (rc == FW_OK)
+        rc = conv_tc<2, 32, EPI_MASK_BF16, 0>(n->gout, im + n->img_off[NL + 2], nullptr, n->act[3], ga, B, H, W,
                                               n->status, n->wait_limit, s);
     for (int l = 2; l >= 1 && rc == FW_OK; l--) {
-        wgrad<HID, HID, HID / 8, HID / 8>(n, l, n->act[l], ga, B, H, W, s);
-        rc = conv_tc<4, 32, EPI_MASK_BF16, 0>(ga, im + n->img_off[NL + l - 1], nullptr, n->act[l], gb, B, H, W,
-                                              n->status, n->wait_limit, s);
+        rc = wgrad<HID, HID, HID / 8, HID / 8>(n, l, n->act[l], ga, B, H, W, s);
+        if (rc == FW_OK)
+            rc = conv_tc<4, 32, EPI_MASK_BF16, 0>(ga, im + n->img_off[NL + l - 1], nullptr, n->act[l], gb, B, H, W,
+                                                  n->status, n->wait_limit, s);
         std::swap(ga, gb);
     }
+    if (rc == FW_OK) rc = wgrad<CIN0, HID, XC0 / 8, HID / 8>(n, 0, n->act[0], ga, B, H, W, s);
     if (rc != FW_OK) return rc;
-    wgrad<CIN0, HID, XC0 / 8, HID / 8>(n, 0, n->act[0], ga, B, H, W, s);
     k_zero_pad_grad<<<nblk(9 * CIN0 * HID, 256), 256, 0, s>>>(n->g + n->woff[0]);
     return FW_OK;
 }
@@ -590,7 +570,7 @@ int fw_net_create(unsigned long long seed, fw_net **out) {
     }
     bool ok = cudaMalloc(&n->w, off * sizeof(float)) == cudaSuccess && cudaMalloc(&n->g, off * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&n->m, off * sizeof(float)) == cudaSuccess && cudaMalloc(&n->v, off * sizeof(float)) == cudaSuccess &&
-              cudaMalloc(&n->part, (size_t)WG_BLOCKS * (9 * HID * HID + HID) * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&n->part, (size_t)WG_PART * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&n->loss, 8 * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&n->status, sizeof(int)) == cudaSuccess;
     size_t ioff = 0;
@@ -599,7 +579,7 @@ int fw_net_create(unsigned long long seed, fw_net **out) {
         ioff += img_elems(i);
     }
     ok = ok && cudaMalloc(&n->img, ioff * sizeof(bf16)) == cudaSuccess;
-    ok = ok && conv_attrs_all();
+    ok = ok && conv_attrs_all() && wgrad_attrs_all();
     ok = ok && cudaMemset(n->status, 0, sizeof(int)) == cudaSuccess;
     ok = ok && cudaMemcpy(n->w, h.data(), off * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
     ok = ok && cudaMemset(n->g, 0, off * sizeof(float)) == cudaSuccess && cudaMemset(n->m, 0, off * sizeof(float)) == cudaSuccess &&

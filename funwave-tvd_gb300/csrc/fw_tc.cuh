@@ -483,4 +483,274 @@ static __global__ void k_pack_wimg(const float *__restrict__ w, int cin, int cou
     img[e] = __float2bfloat16(v);
 }
 
+// ---------------------------------------------------------------------------
+// Weight and bias gradients on the tensor cores.  For a layer with input x
+// and (masked) output gradient dy,
+//     dW[t][ci][co] = sum_p x[p + tap t][ci] dy[p][co],   db[co] = sum_p dy[p][co],
+// a GEMM whose K is the pixels: D (M x N) += A (M x K) B (K x N) with the
+// rows of A the (tap, input channel) pairs, N the output channels and one
+// tile of WKT = 64 consecutive pixels of a grid row per step of K.
+//
+// A tile's A operand is staged "tap-planar": for each tap t and used input
+// chunk c one 8-channel plane of 64 pixels (1 KB) copied by one bulk copy
+// from the padded activation, shifted by the tap (rows y-1..y+1, pixels
+// x0-1.. x0+1 onwards); plane q = t * CCU + c holds rows 8q .. 8q + 7 of A.
+// A plane of ones after the 9 CCU tap planes makes a row of D the bias
+// gradient; the planes up to the next multiple of 16 are zero.  Both A and
+// B (dy, DYCC planes) are read MN-major (the channels contiguous in 16
+// bytes): a core matrix is 8 pixels x 16 bytes = 128 contiguous bytes,
+// consecutive planes 1 KB apart (the M / N direction) and consecutive
+// 8-pixel groups 128 bytes apart (K).  Each 16 A planes are one M = 128
+// MMA into their own TMEM accumulator of N columns; the accumulators add up
+// over all the tiles a CTA walks, and the epilogue writes them as one
+// partial per CTA (the weight layout [t][ci][co], then the bias).
+//
+// Warp 0 (one lane) loads, warp 1 zeroes the pixels past the grid row in a
+// partial tile and one lane issues the MMAs, warps 2-5 read the
+// accumulators once at the end.  Every wait is bounded as in k_conv_tc.
+// ---------------------------------------------------------------------------
+constexpr int WKT = 64;                  // pixels of a tile: four K steps of 16
+constexpr int WPLANE = WKT * 16;         // bytes of one staged plane
+constexpr int WNSTAGE = 3;
+
+template <int CCU, int DYCC> struct WLayout {
+    static constexpr int NQ = 9 * CCU;                   // tap planes
+    static constexpr int G = (NQ + 1 + 15) / 16;         // M = 128 groups (with the ones plane)
+    static constexpr int XP = 16 * G;                    // staged A planes
+    static constexpr int N = DYCC * 8;
+    static constexpr int STAGE = (XP + DYCC) * WPLANE;
+    static constexpr int LOAD = (NQ + DYCC) * WPLANE;    // bytes the copies of one tile bring
+    static constexpr int TMEM_COLS = G * N <= 32 ? 32 : (G * N <= 64 ? 64 : (G * N <= 128 ? 128 : 256));
+    static constexpr int NEED = WNSTAGE * STAGE + 8 * (2 * WNSTAGE + 1) + 8 + 1024;
+    static constexpr int PER_SM_SMEM = 233472 / (NEED + 1024);
+    static constexpr int PER_SM_TMEM = 512 / TMEM_COLS;
+    static constexpr int PER_SM = PER_SM_SMEM < PER_SM_TMEM ? PER_SM_SMEM : PER_SM_TMEM;
+    static constexpr int BYTES = NEED;
+};
+
+// XCC / DYCC: chunks of the stored x and dy; CCU: chunks of x used (CIN =
+// the layer's input channels, <= 8 CCU); COUT: output channels (<= N).
+// part: E = 9 CIN COUT + COUT floats per CTA.
+template <int XCC, int CCU, int DYCC, int CIN, int COUT>
+__global__ void __launch_bounds__(192, 1) k_wgrad_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ dy,
+                                                     float *__restrict__ part, int H, int W, int B, int *status,
+                                                     unsigned wait_limit) {
+    using L = WLayout<CCU, DYCC>;
+    constexpr int N = L::N, E = 9 * CIN * COUT + COUT;
+    static_assert(N == 16 || N == 32, "N of 16 or 32");
+    static_assert(CIN <= 8 * CCU && COUT <= N && CCU <= XCC, "channels");
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const uint32_t xs0 = smem_u32(smem);
+    const uint32_t bar = xs0 + WNSTAGE * L::STAGE;
+    auto full_bar = [&](int st) { return bar + 8u * st; };
+    auto empty_bar = [&](int st) { return bar + 8u * (WNSTAGE + st); };
+    const uint32_t done_bar = bar + 8u * (2 * WNSTAGE);
+    const uint32_t tptr = bar + 8u * (2 * WNSTAGE + 1);
+    volatile uint32_t *flag = reinterpret_cast<volatile uint32_t *>(smem + (tptr + 4u - xs0));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const ActGeom gx{B, H, W, XCC}, gd{B, H, W, DYCC};
+    const int tiles_x = (W + WKT - 1) / WKT;
+    const int ntiles = tiles_x * H * B;
+    const int ntl = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    auto tile_xyb = [&](int i, int &x0, int &y, int &b) {
+        const int t = (int)blockIdx.x + i * (int)gridDim.x;
+        x0 = (t % tiles_x) * WKT;
+        y = (t / tiles_x) % H;
+        b = t / (tiles_x * H);
+    };
+    auto fail = [&](int code) {
+        *flag = 1u;
+        atomicExch(status, code);
+    };
+
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < WNSTAGE; k++) {
+            mbar_init(full_bar(k), 1);
+            mbar_init(empty_bar(k), 1);
+        }
+        mbar_init(done_bar, 1);
+        *flag = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tptr),
+                     "r"((uint32_t)L::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // the ones plane and the zero planes of every stage, once: the copies
+    // never write them
+    {
+        constexpr int PER = (L::XP - L::NQ) * (WPLANE / 16);
+        for (int e = threadIdx.x; e < WNSTAGE * PER; e += blockDim.x) {
+            const int st = e / PER, r = e % PER;
+            const int q = L::NQ + r / (WPLANE / 16), px = r % (WPLANE / 16);
+            const uint32_t one2 = 0x3F803F80u;  // two BF16 ones
+            const uint4 v = q == L::NQ ? make_uint4(one2, one2, one2, one2) : make_uint4(0u, 0u, 0u, 0u);
+            *reinterpret_cast<uint4 *>(smem + st * L::STAGE + q * WPLANE + px * 16) = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    uint32_t tmem;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(tmem) : "r"(tptr) : "memory");
+
+    int last[WNSTAGE];
+#pragma unroll
+    for (int k = 0; k < WNSTAGE; k++) last[k] = -1;
+    int committed = -1;
+    bool done_sent = false;
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int i = 0; i < ntl; i++) {
+                const int st = i % WNSTAGE;
+                if (i >= WNSTAGE &&
+                    !mbar_wait_or_abort(empty_bar(st), (uint32_t)(((i / WNSTAGE) - 1) & 1), flag, wait_limit)) {
+                    if (*flag == 0u) fail(1);
+                    break;
+                }
+                int x0, y, b;
+                tile_xyb(i, x0, y, b);
+                mbar_expect_tx(full_bar(st), (uint32_t)L::LOAD);
+                const uint32_t xs = xs0 + st * L::STAGE;
+#pragma unroll 1
+                for (int t = 0; t < 9; t++) {
+                    const int ky = t / 3, kx = t % 3;
+#pragma unroll
+                    for (int c = 0; c < CCU; c++)
+                        bulk_load(xs + (t * CCU + c) * WPLANE, x + 8 * act_idx(gx, b, y - 1 + ky, c, x0 - 1 + kx),
+                                  (uint32_t)WPLANE, full_bar(st));
+                }
+#pragma unroll
+                for (int c = 0; c < DYCC; c++)
+                    bulk_load(xs + (L::XP + c) * WPLANE, dy + 8 * act_idx(gd, b, y, c, x0), (uint32_t)WPLANE,
+                              full_bar(st));
+#pragma unroll
+                for (int k = 0; k < WNSTAGE; k++)
+                    if (k == st) last[k] = i;
+            }
+        }
+    } else if (warp == 1) {
+        // MN-major A and B (instruction descriptor bits 15 and 16)
+        constexpr uint32_t idesc = idesc_bf16<128, N>() | (1u << 15) | (1u << 16);
+        bool ok = true;
+        for (int i = 0; i < ntl; i++) {
+            const int st = i % WNSTAGE;
+            int landed = 1;
+            if (lane == 0) landed = mbar_wait_or_abort(full_bar(st), (uint32_t)((i / WNSTAGE) & 1), flag, wait_limit);
+            landed = __shfl_sync(0xffffffffu, landed, 0);
+            if (!landed) {
+                if (lane == 0 && *flag == 0u) fail(1);
+                ok = false;
+                break;
+            }
+            int x0, y, b;
+            tile_xyb(i, x0, y, b);
+            const int valid = W - x0 < WKT ? W - x0 : WKT;
+            uint8_t *xsg = smem + st * L::STAGE;
+            if (valid < WKT) {
+                // pixels past the grid row: zero in every loaded plane, once
+                // every lane has seen the copies land (the phase is complete,
+                // so the first poll succeeds)
+                mbar_wait(full_bar(st), (uint32_t)((i / WNSTAGE) & 1), 64);
+                const int nz = WKT - valid;
+                for (int e = lane; e < (L::NQ + DYCC) * nz; e += 32) {
+                    const int qq = e / nz, px = valid + e % nz;
+                    const int plane = qq < L::NQ ? qq : L::XP + (qq - L::NQ);
+                    *reinterpret_cast<uint4 *>(xsg + plane * WPLANE + px * 16) = make_uint4(0u, 0u, 0u, 0u);
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            }
+            __syncwarp();
+            if (lane == 0) {
+                tc_fence_after();
+                const uint32_t xs = xs0 + st * L::STAGE;
+                // no swizzle: the stride between core matrices along M / N in
+                // the SBO field, along K in the LBO field
+                const uint64_t a_base = sdesc(xs, 128, WPLANE), b_base = sdesc(xs + L::XP * WPLANE, 128, WPLANE);
+#pragma unroll
+                for (int ks = 0; ks < WKT / 16; ks++)
+#pragma unroll
+                    for (int g = 0; g < L::G; g++)
+                        tc_mma(tmem + (uint32_t)(g * N), a_base + (uint64_t)((g * 16 * WPLANE + ks * 256) >> 4),
+                               b_base + (uint64_t)((ks * 256) >> 4), idesc, (i | ks) != 0 ? 1u : 0u);
+                tc_commit(empty_bar(st));
+            }
+            committed = i;
+            __syncwarp();
+        }
+        if (lane == 0 && ok && ntl > 0) {
+            tc_commit(done_bar);
+            done_sent = true;
+        }
+    } else {
+        const int q = warp & 3;  // TMEM lane quadrant
+        float *pp = part + (size_t)blockIdx.x * E;
+        // 1: the accumulators are final; 0: this CTA had no tile (zeros);
+        // 2: a wait gave up (nothing is written).  Decided by lane 0 for the
+        // warp, whose TMEM loads are warp-wide.
+        int st = 1;
+        if (lane == 0) {
+            if (ntl == 0) {
+                st = 0;
+            } else if (!mbar_wait_or_abort(done_bar, 0u, flag, wait_limit)) {
+                if (*flag == 0u) fail(2);
+                st = 2;
+            }
+        }
+        st = __shfl_sync(0xffffffffu, st, 0);
+        tc_fence_after();
+        const int row = q * 32 + lane;
+#pragma unroll 1
+        for (int g = 0; g < L::G && st != 2; g++) {
+            uint32_t v[N];
+            if (st == 1) {
+                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * N);
+                tc_ld16(ta, *reinterpret_cast<uint32_t(*)[16]>(&v[0]));
+                if constexpr (N == 32) tc_ld16(ta + 16, *reinterpret_cast<uint32_t(*)[16]>(&v[16]));
+                tc_wait_ld();
+            } else {
+#pragma unroll
+                for (int c = 0; c < N; c++) v[c] = 0u;
+            }
+            const int plane = g * 16 + row / 8, ch = row % 8;
+            if (plane < L::NQ) {
+                const int t = plane / CCU, ci = (plane % CCU) * 8 + ch;
+                if (ci < CIN) {
+#pragma unroll
+                    for (int co = 0; co < COUT; co++) pp[(t * CIN + ci) * COUT + co] = __uint_as_float(v[co]);
+                }
+            } else if (plane == L::NQ && ch == 0) {
+#pragma unroll
+                for (int co = 0; co < COUT; co++) pp[9 * CIN * COUT + co] = __uint_as_float(v[co]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    // after an abort, wait (bounded, full limit) for this block's own copies
+    // and MMAs before its TMEM and shared memory are given up
+    if (*flag != 0u) {
+        if (warp == 0 && lane == 0) {
+#pragma unroll
+            for (int k = 0; k < WNSTAGE; k++)
+                if (last[k] >= 0) mbar_wait(full_bar(k), (uint32_t)((last[k] / WNSTAGE) & 1));
+        }
+        if (warp == 1 && lane == 0 && committed >= 0) {
+            mbar_wait(empty_bar(committed % WNSTAGE), (uint32_t)((committed / WNSTAGE) & 1));
+            if (done_sent) mbar_wait(done_bar, 0u);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)L::TMEM_COLS)
+                     : "memory");
+    }
+}
+
 }  // namespace fwtc
