@@ -5,17 +5,17 @@
 // tcgen05.mma tile), N = the output channels (16 or 32), K = 9 taps x the
 // input channels.  A CTA computes TROWS rows of 128 pixels:
 //
-//   1. one thread issues (TROWS + 2) x CINC bulk copies (cp.async.bulk),
+//   1. the lanes of one warp issue (TROWS + 2) x CINC bulk copies (cp.async.bulk),
 //      one contiguous 130-pixel run per staged row and 8-channel chunk of
 //      the padded activation (below), completing on an mbarrier (with the
 //      first tile, one bulk copy of the packed BF16 weight image too);
-//   2. the same thread issues TROWS x 9 x CINC/2 tcgen05.mma (kind::f16,
-//      BF16 x BF16 -> FP32) into TMEM, one 128 x N accumulator per output
-//      row, and commits them to a second mbarrier;
-//   3. the four warps read their 32 TMEM lanes (= pixels) back with
+//   2. one thread of a second warp issues TROWS x 9 x CINC/2 tcgen05.mma
+//      (kind::f16, BF16 x BF16 -> FP32) into TMEM, one 128 x N accumulator
+//      per output row, and commits them to a second mbarrier;
+//   3. the epilogue warps read their 32 TMEM lanes (= pixels) back with
 //      tcgen05.ld and apply the epilogue (bias + ReLU -> BF16, bias ->
 //      FP32, or the backward ReLU mask -> BF16).
-// CTAs are persistent and warp-specialised (a TMA warp, an MMA warp, four
+// CTAs are persistent and warp-specialised (a TMA warp, an MMA warp, eight
 // epilogue warps) with NSTAGE input stages and two TMEM accumulators, so
 // loads, MMAs and epilogues of successive tiles overlap.
 //
@@ -189,7 +189,7 @@ __device__ __forceinline__ float hi_bf(uint32_t w) { return __uint_as_float(w & 
 // Persistent, warp-specialised CTAs of 320 threads, each walking the tiles
 // t = blockIdx.x, + gridDim.x, ... (a tile: TROWS output rows x 128 pixels
 // of one image):
-//   warp 0 (one lane)   TMA producer: tile i's halo into input stage
+//   warp 0              TMA producer: tile i's halo into input stage
 //                       i % NSTAGE once the MMAs of tile i - NSTAGE have
 //                       released it (the weight image with tile 0);
 //   warp 1              allocates TMEM; one lane issues tile i's MMAs into
@@ -297,29 +297,35 @@ __global__ void __launch_bounds__(320, 1) k_conv_tc(const bf16 *__restrict__ x, 
     for (int k = 0; k < NSTAGE; k++) last[k] = -1;
     int committed = -1;
     if (warp == 0) {
-        if (lane == 0) {
-            for (int i = 0; i < ntl; i++) {
-                const int st = i % NSTAGE;
-                if (i >= NSTAGE && !mbar_wait_or_abort(empty_bar(st), (uint32_t)(((i / NSTAGE) - 1) & 1), flag, wait_limit)) {
+        // lane 0 waits for the stage and sets the bytes to expect, then the
+        // warp's lanes issue the tile's copies, one each
+        for (int i = 0; i < ntl; i++) {
+            const int st = i % NSTAGE;
+            int go = 1;
+            if (lane == 0) {
+                if (i >= NSTAGE &&
+                    !mbar_wait_or_abort(empty_bar(st), (uint32_t)(((i / NSTAGE) - 1) & 1), flag, wait_limit)) {
                     if (*flag == 0u) fail(1);
-                    break;
+                    go = 0;
+                } else {
+                    mbar_expect_tx(full_bar(st), (uint32_t)(L::X_BYTES + (i == 0 ? L::W_BYTES : 0)));
                 }
-                int x0, y0, b;
-                tile_xyb(i, x0, y0, b);
-                mbar_expect_tx(full_bar(st), (uint32_t)(L::X_BYTES + (i == 0 ? L::W_BYTES : 0)));
-                const uint32_t xs = xs0 + st * L::X_BYTES;
-                // staged row rr, chunk c: pixels x0-1 .. x0+128 of image row y0-1+rr
-#pragma unroll 1
-                for (int rr = 0; rr < TROWS + 2; rr++)
-#pragma unroll
-                    for (int c = 0; c < CINC; c++)
-                        bulk_load(xs + (rr * CINC + c) * ROWB, x + 8 * act_idx(gin, b, y0 - 1 + rr, c, x0 - 1),
-                                  (uint32_t)ROWB, full_bar(st));
-                if (i == 0) bulk_load(ws, wimg, (uint32_t)L::W_BYTES, full_bar(0));
-#pragma unroll
-                for (int k = 0; k < NSTAGE; k++)
-                    if (k == st) last[k] = i;
             }
+            go = __shfl_sync(0xffffffffu, go, 0);
+            if (!go) break;
+            int x0, y0, b;
+            tile_xyb(i, x0, y0, b);
+            const uint32_t xs = xs0 + st * L::X_BYTES;
+            // staged row rr, chunk c: pixels x0-1 .. x0+128 of image row y0-1+rr
+            for (int e = lane; e < (TROWS + 2) * CINC; e += 32) {
+                const int rr = e / CINC, c = e % CINC;
+                bulk_load(xs + e * ROWB, x + 8 * act_idx(gin, b, y0 - 1 + rr, c, x0 - 1), (uint32_t)ROWB,
+                          full_bar(st));
+            }
+            if (i == 0 && lane == 31) bulk_load(ws, wimg, (uint32_t)L::W_BYTES, full_bar(0));
+#pragma unroll
+            for (int k = 0; k < NSTAGE; k++)
+                if (k == st) last[k] = i;
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -505,7 +511,7 @@ static __global__ void k_pack_wimg(const float *__restrict__ w, int cin, int cou
 // over all the tiles a CTA walks, and the epilogue writes them as one
 // partial per CTA (the weight layout [t][ci][co], then the bias).
 //
-// Warp 0 (one lane) loads, warp 1 zeroes the pixels past the grid row in a
+// Warp 0 loads (one copy per lane), warp 1 zeroes the pixels past the grid row in a
 // partial tile and one lane issues the MMAs, warps 2-5 read the
 // accumulators once at the end.  Every wait is bounded as in k_conv_tc.
 // ---------------------------------------------------------------------------
@@ -604,34 +610,39 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const bf16 *__restrict__ x,
     int committed = -1;
     bool done_sent = false;
     if (warp == 0) {
-        if (lane == 0) {
-            for (int i = 0; i < ntl; i++) {
-                const int st = i % WNSTAGE;
+        // lane 0 waits for the stage and sets the bytes to expect, then the
+        // warp's lanes issue the tile's copies, one or two each
+        for (int i = 0; i < ntl; i++) {
+            const int st = i % WNSTAGE;
+            int go = 1;
+            if (lane == 0) {
                 if (i >= WNSTAGE &&
                     !mbar_wait_or_abort(empty_bar(st), (uint32_t)(((i / WNSTAGE) - 1) & 1), flag, wait_limit)) {
                     if (*flag == 0u) fail(1);
-                    break;
+                    go = 0;
+                } else {
+                    mbar_expect_tx(full_bar(st), (uint32_t)L::LOAD);
                 }
-                int x0, y, b;
-                tile_xyb(i, x0, y, b);
-                mbar_expect_tx(full_bar(st), (uint32_t)L::LOAD);
-                const uint32_t xs = xs0 + st * L::STAGE;
-#pragma unroll 1
-                for (int t = 0; t < 9; t++) {
-                    const int ky = t / 3, kx = t % 3;
-#pragma unroll
-                    for (int c = 0; c < CCU; c++)
-                        bulk_load(xs + (t * CCU + c) * WPLANE, x + 8 * act_idx(gx, b, y - 1 + ky, c, x0 - 1 + kx),
-                                  (uint32_t)WPLANE, full_bar(st));
-                }
-#pragma unroll
-                for (int c = 0; c < DYCC; c++)
+            }
+            go = __shfl_sync(0xffffffffu, go, 0);
+            if (!go) break;
+            int x0, y, b;
+            tile_xyb(i, x0, y, b);
+            const uint32_t xs = xs0 + st * L::STAGE;
+            for (int e = lane; e < L::NQ + DYCC; e += 32) {
+                if (e < L::NQ) {
+                    const int t = e / CCU, c = e % CCU, ky = t / 3, kx = t % 3;
+                    bulk_load(xs + e * WPLANE, x + 8 * act_idx(gx, b, y - 1 + ky, c, x0 - 1 + kx), (uint32_t)WPLANE,
+                              full_bar(st));
+                } else {
+                    const int c = e - L::NQ;
                     bulk_load(xs + (L::XP + c) * WPLANE, dy + 8 * act_idx(gd, b, y, c, x0), (uint32_t)WPLANE,
                               full_bar(st));
-#pragma unroll
-                for (int k = 0; k < WNSTAGE; k++)
-                    if (k == st) last[k] = i;
+                }
             }
+#pragma unroll
+            for (int k = 0; k < WNSTAGE; k++)
+                if (k == st) last[k] = i;
         }
     } else if (warp == 1) {
         // MN-major A and B (instruction descriptor bits 15 and 16)
