@@ -592,7 +592,8 @@ def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coar
             ev["trainings"].append({
                 "eta_rms_plain_m": [rms(p_short[0], f_short, m_short), rms(plain["Eta"], f_long, m_long)],
                 "eta_rms_corrected_m": [rms(c_short[0], f_short, m_short), rms(corr["Eta"], f_long, m_long)],
-                "max_runup_corrected_m": ru(corr), "corrections_applied": applied})
+                "max_runup_corrected_m": ru(corr), "corrections_applied": applied,
+                "rejected_by": corr["rejected"]})
         evals.append(ev)
     for net in nets:
         net.close()

@@ -142,9 +142,12 @@ __global__ void k_corr_input(fw::Grid g, fw::Fields<T> f, float *in) {
     in[p * NIN + 4] = f.MASK[id] ? 1.0f : 0.0f;
 }
 
-// sums over the wet interior cells: [0] the eta correction, [1] the count,
-// [2] max |correction|, [3] the largest amount by which a corrected total
-// depth would fall below MinDepth (bits of non-negative doubles); [4] the
+// The correction acts on the interior cells whose 3 x 3 neighbourhood is
+// wet (MASK9 = 1, masks.F): not on the cells at the shoreline, where the
+// wet/dry switch is a threshold the network does not see.
+// Sums over those cells: [0] the eta correction, [1] the count, [2] max
+// |correction|, [3] the largest amount by which a corrected total depth
+// would fall below MinDepth (bits of non-negative doubles); [4] the
 // decision of k_corr_apply (1 applied, 0 the plain step kept)
 template <typename T>
 __global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, float min_depth) {
@@ -153,7 +156,7 @@ __global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, doubl
     if (i < g.Mglob && j < g.Nglob) {
         const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
         const long long p = (long long)i + (long long)j * g.Mglob;
-        if (f.MASK[id]) {
+        if (f.MASK9[id]) {
             const float inv = (float)(1.0 / FW_NET_OUT_SCALE);
             se = out[p * NOUT] * inv;
             sc = 1.0f;
@@ -196,7 +199,7 @@ __global__ void k_corr_apply(fw::Grid g, fw::Fields<T> f, const float *out, doub
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mglob || j >= g.Nglob) return;
     const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
-    if (!f.MASK[id]) return;
+    if (!f.MASK9[id]) return;
     const long long p = (long long)i + (long long)j * g.Mglob;
     const double inv = 1.0 / FW_NET_OUT_SCALE;
     const double mean = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
@@ -249,6 +252,10 @@ struct fw_net {
     float *part = nullptr;
     double *loss = nullptr;
     float *corr_in = nullptr;   // fw_correct's input tensor
+    // the checks of the last fw_correct that reported its decision: mean
+    // raw eta correction, cells corrected, max |correction|, MinDepth
+    // violation, decision
+    double last_check[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     // fw_correct_run's graph of two (step + correction) pairs and what it was
     // captured with
     cudaGraphExec_t cexec = nullptr;
@@ -526,6 +533,8 @@ template <typename T> int correct(fw_ctx *c, fw_net *n, double max_corr, int *ap
         if (cudaStreamSynchronize(s) != cudaSuccess) return FW_ERR_CUDA;
         if (st != 0) return take_status(n, st, s);
         *applied = h[5] == 1.0 ? 1 : 0;
+        for (int k = 0; k < 5; k++) n->last_check[k] = h[k + 1];
+        n->last_check[0] = h[2] > 0.0 ? h[1] / h[2] : 0.0;  // the mean, not the sum
     }
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
 }
@@ -743,6 +752,12 @@ int fw_correct_run(fw_ctx *c, fw_net *n, int nsteps, double max_corr, int *statu
     if (cudaMemcpy(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FW_ERR_CUDA;
     if (st != 0) return take_status(n, st, c->stream);
     return rc;
+}
+
+int fw_net_last_check(fw_net *n, double *out) {
+    if (!n || !out) return FW_ERR_BAD_PARAM;
+    for (int k = 0; k < 5; k++) out[k] = n->last_check[k];
+    return FW_OK;
 }
 
 int fw_correct(fw_ctx *c, fw_net *n, double max_corr, int *applied) {

@@ -45,6 +45,7 @@ def _bind(L):
     L.fw_net_set_wait_limit.argtypes = [vp, ctypes.c_uint]
     L.fw_correct.argtypes = [vp, vp, ctypes.c_double, ctypes.POINTER(ip)]
     L.fw_correct_run.argtypes = [vp, vp, ip, ctypes.c_double, ctypes.POINTER(ip)]
+    L.fw_net_last_check.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     return L
 
 
@@ -122,6 +123,14 @@ class Net:
         ap = ctypes.c_int()
         self._ck(self.L.fw_correct(solver.ctx, self.h, float(max_corr), ctypes.byref(ap)), "fw_correct")
         return bool(ap.value)
+
+    def last_check(self):
+        """The checks of the last correct() that waited (fw_net_last_check):
+        mean raw eta correction, cells corrected, max |correction|, MinDepth
+        violation, applied."""
+        out = (ctypes.c_double * 5)()
+        self._ck(self.L.fw_net_last_check(self.h, out), "fw_net_last_check")
+        return {"mean_eta": out[0], "cells": out[1], "max_abs": out[2], "dry_m": out[3], "applied": out[4] == 1.0}
 
     def correct_run(self, solver, nsteps, max_corr=0.2):
         """nsteps of (step + correction) on the solver through fw_correct_run:
@@ -308,8 +317,9 @@ def one_step_error(net, x, t, w):
 def rollout(case, nsteps_c, net=None, precision="MIXED", max_corr=0.2, snaps=()):
     """The coarse twin of case run for nsteps_c steps, with the network's
     correction after every step when net is given; returns (coarse solver
-    state dict of interior Eta, U, V, HeightMax, and in "snaps" the interior
-    Eta and MASK after each step count of snaps; steps corrected)."""
+    state dict of interior Eta, U, V, HeightMax, in "snaps" the interior Eta
+    and MASK after each step count of snaps and in "rejected" the steps whose
+    correction each check rejected; steps corrected)."""
     pf, depth, phases = case
     pc, depth_c = coarse_case(with_defaults(pf), depth)
     pc = with_defaults(pc)
@@ -318,14 +328,25 @@ def rollout(case, nsteps_c, net=None, precision="MIXED", max_corr=0.2, snaps=())
     cs.init(depth_c, phases=phases)
     applied = 0
     taken = {}
+    # steps whose correction each check rejected (several may reject one)
+    rejected = {"size": 0, "drift": 0, "shore": 0, "nonfinite": 0}
     for k in range(nsteps_c):
         cs.step(1)
         if net is not None:
-            applied += int(net.correct(cs, max_corr))
+            ok = net.correct(cs, max_corr)
+            applied += int(ok)
+            if not ok:
+                c = net.last_check()
+                finite = all(np.isfinite([c["mean_eta"], c["max_abs"]]))
+                rejected["nonfinite"] += int(not finite)
+                rejected["size"] += int(finite and c["max_abs"] > max_corr)
+                rejected["drift"] += int(finite and abs(c["mean_eta"]) > 0.5 * max_corr)
+                rejected["shore"] += int(c["dry_m"] > 0.0)
         if k + 1 in snaps:
             taken[k + 1] = (_interior(cs.get("Eta")), _interior(cs.get("MASK")))
     out = {n: _interior(cs.get(n)) for n in ("Eta", "U", "V", "HeightMax", "MASK")}
     out["snaps"] = taken
+    out["rejected"] = rejected
     out["TIME"] = cs.scalar("TIME")
     out["depth"] = depth_c
     cs.close()

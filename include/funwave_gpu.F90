@@ -289,6 +289,11 @@ MODULE FUNWAVE_GPU
       REAL(C_DOUBLE), VALUE :: max_corr
       TYPE(C_PTR), VALUE :: applied               ! C_LOC of an INTEGER or C_NULL_PTR
     END FUNCTION
+    INTEGER(C_INT) FUNCTION fw_net_last_check(net, out) BIND(C, NAME="fw_net_last_check")
+      IMPORT :: C_INT, C_PTR, C_DOUBLE
+      TYPE(C_PTR), VALUE :: net
+      REAL(C_DOUBLE), INTENT(OUT) :: out(5)
+    END FUNCTION
     INTEGER(C_INT) FUNCTION fw_correct_run(ctx, net, nsteps, max_corr, status) BIND(C, NAME="fw_correct_run")
       IMPORT :: C_INT, C_PTR, C_DOUBLE
       TYPE(C_PTR), VALUE :: ctx, net

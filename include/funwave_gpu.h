@@ -262,15 +262,23 @@ int fw_net_adam(fw_net *net, float lr, float beta1, float beta2, float eps, void
  * applied, fw_correct_run) returns FW_ERR_TIMEOUT and clears it.  Lowering
  * the limit makes that path run on purpose (a test of failure reporting). */
 int fw_net_set_wait_limit(fw_net *net, unsigned polls);
-/* Apply the network to a context's current state: the eta correction is
- * projected to zero mean over the wet interior cells (so the volume is
- * unchanged), then eta, u, v (and H, HU, HV, Ubar, Vbar to first order) are
- * corrected on wet cells.  The correction is skipped (*applied = 0) when any
- * |correction| exceeds max_corr (the network's input is then outside what it
- * was trained on); the plain step stands.  The decision is made on the
- * device: with applied == NULL the call only enqueues work on the context's
- * stream; with applied given it waits and reports the decision. */
+/* Apply the network to a context's current state.  The correction acts on
+ * the interior cells whose 3 x 3 neighbourhood is wet (MASK9 = 1), not at
+ * the shoreline: the eta correction is projected to zero mean over those
+ * cells (so the volume is unchanged), then eta, u, v (and H, HU, HV, Ubar,
+ * Vbar to first order) are corrected there.  The plain step stands
+ * (*applied = 0) when any |correction| exceeds max_corr, when a value is not
+ * finite, when the raw eta correction's mean (the uniform rise or fall the
+ * projection removes) exceeds max_corr / 2, or when a corrected total depth
+ * would reach MinDepth.  The decision is made on the device: with applied
+ * == NULL the call only enqueues work on the context's stream; with applied
+ * given it waits and reports the decision. */
 int fw_correct(fw_ctx *ctx, fw_net *net, double max_corr, int *applied);
+/* The checks of the last fw_correct that was given applied: out[0] the raw
+ * eta correction's mean, out[1] the cells it acts on, out[2] the largest
+ * |correction| (m, m/s), out[3] the largest amount (m) by which a corrected
+ * total depth would fall below MinDepth, out[4] 1 if applied else 0. */
+int fw_net_last_check(fw_net *net, double *out);
 /* nsteps of (fw_step + fw_correct without waiting) on a coarse run, two
  * pairs per replay of one captured CUDA graph; status as fw_step's.  The
  * graph is captured again when the run, its buffer state, its launch

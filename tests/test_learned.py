@@ -191,8 +191,10 @@ def test_correction_fallback_checks(fw, precision):
     """fw_correct keeps the plain step when a check fails: a correction above
     max_corr, a volume drift (the raw eta correction's mean, which the
     projection would remove) above half of max_corr, or a wet cell pushed to
-    or below MinDepth.  The output layer's weights are zero here, so the
-    correction is its bias: eta bias b_e and u bias b_u, in metres and m/s."""
+    or below MinDepth; fw_net_last_check reports the checked values.  A
+    correction acts only on cells whose 3 x 3 neighbourhood is wet (MASK9).
+    The output layer's weights are zero here, so the correction is its bias:
+    eta bias b_e and u bias b_u, in metres and m/s."""
     import fw_net_oracle as ref
     params, depth, _ = fw.cases.planar_beach(Mglob=64, Nglob=40, seed=2)
     depth = np.array(depth)
@@ -216,24 +218,31 @@ def test_correction_fallback_checks(fw, precision):
         eta0, u0 = s.get("Eta"), s.get("U")
         applied = net.correct(s, max_corr=max_corr)
         eta1, u1 = s.get("Eta"), s.get("U")
-        wet = s.get("MASK") > 0
+        wet9 = s.get("MASK9") > 0
         s.close()
-        return applied, eta0, eta1, u0, u1, wet
+        return applied, eta0, eta1, u0, u1, wet9, net.last_check()
 
     # size cap
-    a, e0, e1, u0, u1, _ = run(0.0, 0.3, 0.2)
+    a, e0, e1, u0, u1, _, c = run(0.0, 0.3, 0.2)
     assert not a and np.array_equal(e0, e1) and np.array_equal(u0, u1)
+    assert not c["applied"] and abs(c["max_abs"] - 0.3) < 1e-6 and c["dry_m"] == 0.0
     # volume drift: a uniform rise of 0.15 m against max_corr 0.2 m
-    a, e0, e1, u0, u1, _ = run(0.15, 0.0, 0.2)
+    a, e0, e1, u0, u1, _, c = run(0.15, 0.0, 0.2)
     assert not a and np.array_equal(e0, e1) and np.array_equal(u0, u1)
+    assert abs(c["mean_eta"] - 0.15) < 1e-6
     # a uniform fall of 0.04 m would dry the 0.03 m patch
-    a, e0, e1, u0, u1, _ = run(-0.04, 0.05, 0.2)
+    a, e0, e1, u0, u1, _, c = run(-0.04, 0.05, 0.2)
     assert not a and np.array_equal(e0, e1) and np.array_equal(u0, u1)
+    assert abs(c["dry_m"] - 0.02) < 1e-3
     # the same without shallow cells passes: the uniform eta part is
-    # projected away (volume kept) and u gets its 0.05 m/s
-    a, e0, e1, u0, u1, wet = run(-0.04, 0.05, 0.2, shallow=False)
-    assert a
-    assert float(np.abs((e1 - e0)[wet]).max()) <= 1e-6
-    du = (u1 - u0)[3:-3, 3:-3][wet[3:-3, 3:-3]]
-    assert np.allclose(du, 0.05, rtol=0, atol=1e-6)
+    # projected away (volume kept) and u gets its 0.05 m/s on the cells
+    # whose neighbourhood is wet, nothing at the shoreline
+    a, e0, e1, u0, u1, wet9, c = run(-0.04, 0.05, 0.2, shallow=False)
+    assert a and c["applied"] and c["cells"] == float(wet9[3:-3, 3:-3].sum())
+    assert float(np.abs(e1 - e0).max()) <= 1e-6
+    du = (u1 - u0)[3:-3, 3:-3]
+    m9 = wet9[3:-3, 3:-3]
+    assert m9.any() and (~m9).any()
+    assert np.allclose(du[m9], 0.05, rtol=0, atol=1e-6)
+    assert np.array_equal(du[~m9], np.zeros_like(du[~m9]))
     net.close()
