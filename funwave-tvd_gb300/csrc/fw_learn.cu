@@ -143,8 +143,16 @@ __global__ void k_corr_input(fw::Grid g, fw::Fields<T> f, float *in) {
 }
 
 // The correction acts on the interior cells whose 3 x 3 neighbourhood is
-// wet (MASK9 = 1, masks.F): not on the cells at the shoreline, where the
-// wet/dry switch is a threshold the network does not see.
+// wet (MASK of the cell and its eight neighbours): not on the cells at the
+// shoreline, where the wet/dry switch is a threshold the network does not
+// see.  (MASK9 is not this test: with VISCOSITY_BREAKING it is 1 on every
+// interior cell, dry ones included.)
+template <typename T> __device__ __forceinline__ bool wet3x3(const fw::Grid &g, const fw::Fields<T> &f, size_t id) {
+    const uint8_t *m = f.MASK;
+    const size_t p = (size_t)g.pitch;
+    return m[id - p - 1] & m[id - p] & m[id - p + 1] & m[id - 1] & m[id] & m[id + 1] & m[id + p - 1] & m[id + p] &
+           m[id + p + 1];
+}
 // Sums over those cells: [0] the eta correction, [1] the count, [2] max
 // |correction|, [3] the largest amount by which a corrected total depth
 // would fall below MinDepth (bits of non-negative doubles); [4] the
@@ -156,7 +164,7 @@ __global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, doubl
     if (i < g.Mglob && j < g.Nglob) {
         const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
         const long long p = (long long)i + (long long)j * g.Mglob;
-        if (f.MASK9[id]) {
+        if (wet3x3(g, f, id)) {
             const float inv = (float)(1.0 / FW_NET_OUT_SCALE);
             se = out[p * NOUT] * inv;
             sc = 1.0f;
@@ -199,7 +207,7 @@ __global__ void k_corr_apply(fw::Grid g, fw::Fields<T> f, const float *out, doub
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mglob || j >= g.Nglob) return;
     const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
-    if (!f.MASK9[id]) return;
+    if (!wet3x3(g, f, id)) return;
     const long long p = (long long)i + (long long)j * g.Mglob;
     const double inv = 1.0 / FW_NET_OUT_SCALE;
     const double mean = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;

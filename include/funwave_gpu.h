@@ -263,8 +263,9 @@ int fw_net_adam(fw_net *net, float lr, float beta1, float beta2, float eps, void
  * the limit makes that path run on purpose (a test of failure reporting). */
 int fw_net_set_wait_limit(fw_net *net, unsigned polls);
 /* Apply the network to a context's current state.  The correction acts on
- * the interior cells whose 3 x 3 neighbourhood is wet (MASK9 = 1), not at
- * the shoreline: the eta correction is projected to zero mean over those
+ * the interior cells whose 3 x 3 neighbourhood is wet (MASK = 1 on the cell
+ * and its eight neighbours), not at the shoreline: the eta correction is
+ * projected to zero mean over those
  * cells (so the volume is unchanged), then eta, u, v (and H, HU, HV, Ubar,
  * Vbar to first order) are corrected there.  The plain step stands
  * (*applied = 0) when any |correction| exceeds max_corr, when a value is not

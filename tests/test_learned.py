@@ -192,7 +192,7 @@ def test_correction_fallback_checks(fw, precision):
     max_corr, a volume drift (the raw eta correction's mean, which the
     projection would remove) above half of max_corr, or a wet cell pushed to
     or below MinDepth; fw_net_last_check reports the checked values.  A
-    correction acts only on cells whose 3 x 3 neighbourhood is wet (MASK9).
+    correction acts only on cells whose 3 x 3 neighbourhood is wet.
     The output layer's weights are zero here, so the correction is its bias:
     eta bias b_e and u bias b_u, in metres and m/s."""
     import fw_net_oracle as ref
@@ -218,7 +218,10 @@ def test_correction_fallback_checks(fw, precision):
         eta0, u0 = s.get("Eta"), s.get("U")
         applied = net.correct(s, max_corr=max_corr)
         eta1, u1 = s.get("Eta"), s.get("U")
-        wet9 = s.get("MASK9") > 0
+        m = s.get("MASK") > 0
+        wet9 = np.zeros_like(m)
+        wet9[1:-1, 1:-1] = np.all([m[1 + a:m.shape[0] - 1 + a, 1 + b:m.shape[1] - 1 + b]
+                                   for a in (-1, 0, 1) for b in (-1, 0, 1)], axis=0)
         s.close()
         return applied, eta0, eta1, u0, u1, wet9, net.last_check()
 
