@@ -199,6 +199,7 @@ def test_correction_fallback_checks(fw, precision):
     params, depth, _ = fw.cases.planar_beach(Mglob=64, Nglob=40, seed=2)
     depth = np.array(depth)
     depth[10:14, 5:9] = 0.03          # a patch of shallow wet cells (MinDepth 0.01 m)
+    depth[52:, 28:] = -0.5            # an island: land and a shoreline
     p = fw.with_defaults(params)
     net = fw.learned.Net(seed=3)
     base = net.params()
