@@ -1753,6 +1753,89 @@ static int f32_planes(fw_ctx *c, int n, const char *const *names, std::vector<Fi
     return FW_OK;
 }
 
+// Float host arrays that the GPU can address (page-locked memory: the
+// caller's fw_host_alloc or cudaHostAlloc buffers) are read and written in
+// place by one kernel per call, whose loads and stores cross the host link
+// from every SM at once, and which scatters to (or gathers from) the pitched
+// fields itself: no copy engine, no staging plane.  Other host arrays take
+// the copy path below.
+struct HostPlanes {
+    float *host[16];   // the host arrays, through their device addresses
+    float *dev[16];    // the pitched fields
+    double *devd[16];  // set in: the double copy of Depth of the total-depth tests, else null
+    int w[16], h[16];
+    int pitch;
+};
+
+static __global__ void k_host_in_f32(HostPlanes hp) {
+    const int k = blockIdx.y, w = hp.w[k], h = hp.h[k];
+    const float *src = hp.host[k];
+    float *dst = hp.dev[k];
+    double *dd = hp.devd[k];
+    const long long n = (long long)w * h;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % w), j = (int)(e / w);
+        const float v = src[e];
+        const size_t q = (size_t)i + (size_t)j * hp.pitch;
+        dst[q] = v;
+        if (dd) dd[q] = (double)v;
+    }
+}
+
+static __global__ void k_host_out_f32(HostPlanes hp) {
+    const int k = blockIdx.y, w = hp.w[k], h = hp.h[k];
+    float *dst = hp.host[k];
+    const float *src = hp.dev[k];
+    const long long n = (long long)w * h;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % w), j = (int)(e / w);
+        dst[e] = src[(size_t)i + (size_t)j * hp.pitch];
+    }
+}
+
+// the device addresses of n page-locked host arrays; false if any is not
+static bool host_views(int n, const void *const *host, float **dev) {
+    for (int k = 0; k < n; k++) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, host[k]) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+        dev[k] = (float *)a.devicePointer;
+    }
+    return true;
+}
+
+// the mixed build's fields of n names for the direct path
+static bool host_planes(fw_ctx *c, int n, const char *const *names, const void *const *host, bool in,
+                        HostPlanes &hp) {
+    if (!host_views(n, host, hp.host)) return false;
+    for (int k = 0; k < n; k++) {
+        FieldRef r;
+        if (!names[k] || !find_field<float>(c, names[k], r) || r.is_mask) return false;
+        hp.dev[k] = (float *)r.ptr;
+        hp.devd[k] = in && std::strcmp(names[k], "Depth") == 0 ? c->ff.DepthD : nullptr;
+        extent(c, r.kind, hp.w[k], hp.h[k]);
+    }
+    hp.pitch = c->g.pitch;
+    return true;
+}
+
+static int host_planes_run(fw_ctx *c, int n, HostPlanes &hp, bool in) {
+    int dev = 0, nsm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    const dim3 grid((unsigned)std::max(1, 4 * nsm / n), (unsigned)n);
+    if (in) k_host_in_f32<<<grid, 512, 0, c->stream>>>(hp);
+    else k_host_out_f32<<<grid, 512, 0, c->stream>>>(hp);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_status(c, e);
+    return in ? finish(c) : FW_OK;
+}
+
 int fw_set_fields_f32(fw_ctx *c, int n, const char *const *names, const float *const *host) {
     if (!c) return FW_ERR_BAD_PARAM;
     if (c->sticky_error) return FW_ERR_CUDA;
@@ -1766,6 +1849,8 @@ int fw_set_fields_f32(fw_ctx *c, int n, const char *const *names, const float *c
         }
         return FW_OK;
     }
+    HostPlanes hp;
+    if (host_planes(c, n, names, (const void *const *)host, true, hp)) return host_planes_run(c, n, hp, true);
     std::vector<FieldRef> refs;
     std::vector<size_t> off;
     int rc = f32_planes(c, n, names, refs, off);
@@ -1805,6 +1890,8 @@ int fw_get_fields_f32(fw_ctx *c, int n, const char *const *names, float *const *
         }
         return FW_OK;
     }
+    HostPlanes hp;
+    if (host_planes(c, n, names, (const void *const *)host, false, hp)) return host_planes_run(c, n, hp, false);
     std::vector<FieldRef> refs;
     std::vector<size_t> off;
     int rc = f32_planes(c, n, names, refs, off);

@@ -494,38 +494,42 @@ static __global__ void k_pack_wimg(const float *__restrict__ w, int cin, int cou
 // and (masked) output gradient dy,
 //     dW[t][ci][co] = sum_p x[p + tap t][ci] dy[p][co],   db[co] = sum_p dy[p][co],
 // a GEMM whose K is the pixels: D (M x N) += A (M x K) B (K x N) with the
-// rows of A the (tap, input channel) pairs, N the output channels and one
-// tile of WKT = 64 consecutive pixels of a grid row per step of K.
+// rows of A (tap, input channel) pairs, N the output channels and one tile
+// of WKT = 64 consecutive pixels of a grid row per step of K.
 //
-// A tile's A operand is staged "tap-planar": for each tap t and used input
-// chunk c one 8-channel plane of 64 pixels (1 KB) copied by one bulk copy
-// from the padded activation, shifted by the tap (rows y-1..y+1, pixels
-// x0-1.. x0+1 onwards); plane q = t * CCU + c holds rows 8q .. 8q + 7 of A.
-// A plane of ones after the 9 CCU tap planes makes a row of D the bias
-// gradient; the planes up to the next multiple of 16 are zero.  Both A and
-// B (dy, DYCC planes) are read MN-major (the channels contiguous in 16
-// bytes): a core matrix is 8 pixels x 16 bytes = 128 contiguous bytes,
-// consecutive planes 1 KB apart (the M / N direction) and consecutive
-// 8-pixel groups 128 bytes apart (K).  Each 16 A planes are one M = 128
-// MMA into their own TMEM accumulator of N columns; the accumulators add up
-// over all the tiles a CTA walks, and the epilogue writes them as one
-// partial per CTA (the weight layout [t][ci][co], then the bias).
+// A tile stages, for each of the rows y-1, y, y+1 and each used 8-channel
+// chunk c of x, one run of 66 pixels (x0-1 .. x0+64) of the padded
+// activation: plane q = ky * CCU + c, 1056 bytes, one bulk copy each.  A
+// plane of ones follows the 3 CCU row planes (its row of D is the bias
+// gradient) and zero planes fill up to 16.  Both operands are read MN-major
+// (the 8 channels of a pixel are the contiguous 16 bytes): a core matrix is
+// 8 pixels x 16 bytes = 128 contiguous bytes, consecutive planes are 1056
+// bytes apart (the M direction, SBO) and consecutive 8-pixel groups 128
+// bytes apart (K, LBO).  The taps of one x offset kx are then the 16 planes
+// read from a start address kx * 16 bytes on: three M = 128 MMAs per K step
+// (kx = 0, 1, 2), each into its own TMEM accumulator of N columns, whose row
+// 8q + ch is tap (q / CCU) * 3 + kx, input channel (q % CCU) * 8 + ch.  B is
+// dy, DYCC planes of 64 pixels.  The accumulators add up over all the tiles
+// a CTA walks, and the epilogue writes them as one partial per CTA (the
+// weight layout [t][ci][co], then the bias).
 //
-// Warp 0 loads (one copy per lane), warp 1 zeroes the pixels past the grid row in a
-// partial tile and one lane issues the MMAs, warps 2-5 read the
+// Warp 0 loads (one copy per lane), warp 1 zeroes the pixels past the grid
+// row in a partial tile and one lane issues the MMAs, warps 2-5 read the
 // accumulators once at the end.  Every wait is bounded as in k_conv_tc.
 // ---------------------------------------------------------------------------
 constexpr int WKT = 64;                  // pixels of a tile: four K steps of 16
-constexpr int WPLANE = WKT * 16;         // bytes of one staged plane
-constexpr int WNSTAGE = 3;
+constexpr int WPLANE = WKT * 16;         // bytes of one staged dy plane
+constexpr int WXPLANE = (WKT + 2) * 16;  // bytes of one staged x plane (one halo pixel each side)
+constexpr int WNSTAGE = 4;
 
 template <int CCU, int DYCC> struct WLayout {
-    static constexpr int NQ = 9 * CCU;                   // tap planes
-    static constexpr int G = (NQ + 1 + 15) / 16;         // M = 128 groups (with the ones plane)
-    static constexpr int XP = 16 * G;                    // staged A planes
+    static constexpr int NQ = 3 * CCU;                   // row planes of x
+    static_assert(NQ + 1 <= 16, "the row planes and the ones plane fill one M = 128 group");
+    static constexpr int G = 3;                          // M = 128 groups: one per x offset of the taps
     static constexpr int N = DYCC * 8;
-    static constexpr int STAGE = (XP + DYCC) * WPLANE;
-    static constexpr int LOAD = (NQ + DYCC) * WPLANE;    // bytes the copies of one tile bring
+    static constexpr int DYOFF = 16 * WXPLANE;           // dy planes after the 16 x planes
+    static constexpr int STAGE = DYOFF + DYCC * WPLANE;
+    static constexpr int LOAD = NQ * WXPLANE + DYCC * WPLANE;  // bytes the copies of one tile bring
     static constexpr int TMEM_COLS = G * N <= 32 ? 32 : (G * N <= 64 ? 64 : (G * N <= 128 ? 128 : 256));
     static constexpr int NEED = WNSTAGE * STAGE + 8 * (2 * WNSTAGE + 1) + 8 + 1024;
     static constexpr int PER_SM_SMEM = 233472 / (NEED + 1024);
@@ -538,9 +542,9 @@ template <int CCU, int DYCC> struct WLayout {
 // the layer's input channels, <= 8 CCU); COUT: output channels (<= N).
 // part: E = 9 CIN COUT + COUT floats per CTA.
 template <int XCC, int CCU, int DYCC, int CIN, int COUT>
-__global__ void __launch_bounds__(192, 1) k_wgrad_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ dy,
-                                                     float *__restrict__ part, int H, int W, int B, int *status,
-                                                     unsigned wait_limit) {
+__global__ void __launch_bounds__(192) k_wgrad_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ dy,
+                                                  float *__restrict__ part, int H, int W, int B, int *status,
+                                                  unsigned wait_limit) {
     using L = WLayout<CCU, DYCC>;
     constexpr int N = L::N, E = 9 * CIN * COUT + COUT;
     static_assert(N == 16 || N == 32, "N of 16 or 32");
@@ -588,13 +592,13 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const bf16 *__restrict__ x,
     // the ones plane and the zero planes of every stage, once: the copies
     // never write them
     {
-        constexpr int PER = (L::XP - L::NQ) * (WPLANE / 16);
+        constexpr int PX = WXPLANE / 16, PER = (16 - L::NQ) * PX;
         for (int e = threadIdx.x; e < WNSTAGE * PER; e += blockDim.x) {
             const int st = e / PER, r = e % PER;
-            const int q = L::NQ + r / (WPLANE / 16), px = r % (WPLANE / 16);
+            const int q = L::NQ + r / PX, px = r % PX;
             const uint32_t one2 = 0x3F803F80u;  // two BF16 ones
             const uint4 v = q == L::NQ ? make_uint4(one2, one2, one2, one2) : make_uint4(0u, 0u, 0u, 0u);
-            *reinterpret_cast<uint4 *>(smem + st * L::STAGE + q * WPLANE + px * 16) = v;
+            *reinterpret_cast<uint4 *>(smem + st * L::STAGE + q * WXPLANE + px * 16) = v;
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -611,7 +615,7 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const bf16 *__restrict__ x,
     bool done_sent = false;
     if (warp == 0) {
         // lane 0 waits for the stage and sets the bytes to expect, then the
-        // warp's lanes issue the tile's copies, one or two each
+        // warp's lanes issue the tile's copies, one each
         for (int i = 0; i < ntl; i++) {
             const int st = i % WNSTAGE;
             int go = 1;
@@ -629,16 +633,14 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const bf16 *__restrict__ x,
             int x0, y, b;
             tile_xyb(i, x0, y, b);
             const uint32_t xs = xs0 + st * L::STAGE;
-            for (int e = lane; e < L::NQ + DYCC; e += 32) {
-                if (e < L::NQ) {
-                    const int t = e / CCU, c = e % CCU, ky = t / 3, kx = t % 3;
-                    bulk_load(xs + e * WPLANE, x + 8 * act_idx(gx, b, y - 1 + ky, c, x0 - 1 + kx), (uint32_t)WPLANE,
-                              full_bar(st));
-                } else {
-                    const int c = e - L::NQ;
-                    bulk_load(xs + (L::XP + c) * WPLANE, dy + 8 * act_idx(gd, b, y, c, x0), (uint32_t)WPLANE,
-                              full_bar(st));
-                }
+            if (lane < L::NQ) {
+                const int ky = lane / CCU, c = lane % CCU;
+                bulk_load(xs + lane * WXPLANE, x + 8 * act_idx(gx, b, y - 1 + ky, c, x0 - 1), (uint32_t)WXPLANE,
+                          full_bar(st));
+            } else if (lane < L::NQ + DYCC) {
+                const int c = lane - L::NQ;
+                bulk_load(xs + L::DYOFF + c * WPLANE, dy + 8 * act_idx(gd, b, y, c, x0), (uint32_t)WPLANE,
+                          full_bar(st));
             }
 #pragma unroll
             for (int k = 0; k < WNSTAGE; k++)
@@ -663,15 +665,17 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const bf16 *__restrict__ x,
             const int valid = W - x0 < WKT ? W - x0 : WKT;
             uint8_t *xsg = smem + st * L::STAGE;
             if (valid < WKT) {
-                // pixels past the grid row: zero in every loaded plane, once
-                // every lane has seen the copies land (the phase is complete,
-                // so the first poll succeeds)
+                // past the grid row: dy pixels valid.. and x pixels valid+2..
+                // (staged pixel s is grid pixel x0 - 1 + s; pixel W is the
+                // zero border) are zeroed, once every lane has seen the copies
+                // land (the phase is complete, so the first poll succeeds)
                 mbar_wait(full_bar(st), (uint32_t)((i / WNSTAGE) & 1), 64);
                 const int nz = WKT - valid;
                 for (int e = lane; e < (L::NQ + DYCC) * nz; e += 32) {
-                    const int qq = e / nz, px = valid + e % nz;
-                    const int plane = qq < L::NQ ? qq : L::XP + (qq - L::NQ);
-                    *reinterpret_cast<uint4 *>(xsg + plane * WPLANE + px * 16) = make_uint4(0u, 0u, 0u, 0u);
+                    const int qq = e / nz, r = e % nz;
+                    const int off = qq < L::NQ ? qq * WXPLANE + (valid + 2 + r) * 16
+                                               : L::DYOFF + (qq - L::NQ) * WPLANE + (valid + r) * 16;
+                    *reinterpret_cast<uint4 *>(xsg + off) = make_uint4(0u, 0u, 0u, 0u);
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             }
@@ -681,12 +685,12 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const bf16 *__restrict__ x,
                 const uint32_t xs = xs0 + st * L::STAGE;
                 // no swizzle: the stride between core matrices along M / N in
                 // the SBO field, along K in the LBO field
-                const uint64_t a_base = sdesc(xs, 128, WPLANE), b_base = sdesc(xs + L::XP * WPLANE, 128, WPLANE);
+                const uint64_t a_base = sdesc(xs, 128, WXPLANE), b_base = sdesc(xs + L::DYOFF, 128, WPLANE);
 #pragma unroll
                 for (int ks = 0; ks < WKT / 16; ks++)
 #pragma unroll
-                    for (int g = 0; g < L::G; g++)
-                        tc_mma(tmem + (uint32_t)(g * N), a_base + (uint64_t)((g * 16 * WPLANE + ks * 256) >> 4),
+                    for (int kx = 0; kx < 3; kx++)
+                        tc_mma(tmem + (uint32_t)(kx * N), a_base + (uint64_t)((kx * 16 + ks * 256) >> 4),
                                b_base + (uint64_t)((ks * 256) >> 4), idesc, (i | ks) != 0 ? 1u : 0u);
                 tc_commit(empty_bar(st));
             }
@@ -716,10 +720,10 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const bf16 *__restrict__ x,
         tc_fence_after();
         const int row = q * 32 + lane;
 #pragma unroll 1
-        for (int g = 0; g < L::G && st != 2; g++) {
+        for (int kx = 0; kx < 3 && st != 2; kx++) {
             uint32_t v[N];
             if (st == 1) {
-                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * N);
+                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(kx * N);
                 tc_ld16(ta, *reinterpret_cast<uint32_t(*)[16]>(&v[0]));
                 if constexpr (N == 32) tc_ld16(ta + 16, *reinterpret_cast<uint32_t(*)[16]>(&v[16]));
                 tc_wait_ld();
@@ -727,14 +731,14 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const bf16 *__restrict__ x,
 #pragma unroll
                 for (int c = 0; c < N; c++) v[c] = 0u;
             }
-            const int plane = g * 16 + row / 8, ch = row % 8;
+            const int plane = row / 8, ch = row % 8;
             if (plane < L::NQ) {
-                const int t = plane / CCU, ci = (plane % CCU) * 8 + ch;
+                const int t = (plane / CCU) * 3 + kx, ci = (plane % CCU) * 8 + ch;
                 if (ci < CIN) {
 #pragma unroll
                     for (int co = 0; co < COUT; co++) pp[(t * CIN + ci) * COUT + co] = __uint_as_float(v[co]);
                 }
-            } else if (plane == L::NQ && ch == 0) {
+            } else if (plane == L::NQ && kx == 0 && ch == 0) {
 #pragma unroll
                 for (int co = 0; co < COUT; co++) pp[9 * CIN * COUT + co] = __uint_as_float(v[co]);
             }

@@ -45,23 +45,37 @@ def test_f32_transfers(fw, precision):
 def test_f32_multi_field_transfers(fw, precision):
     """fw_set_fields_f32 / fw_get_fields_f32 move several fields at once and
     equal the one-field calls; "Depth" among them keeps the mixed build's
-    double copy of the total-depth tests in step (the run goes on equally)."""
+    double copy of the total-depth tests in step (the run goes on equally).
+    Pageable host arrays take the copy path; page-locked ones are read and
+    written in place by the transfer kernels (mixed build): both equal."""
     import ctypes
+    torch = pytest.importorskip("torch")
     params, depth, _ = fw.cases.planar_beach(Mglob=70, Nglob=44, seed=6)
     p = fw.with_defaults(params)
     eta, u, v = fw.cases.random_state(70, 44, seed=7)
+
+    def host_array(shape, pinned):
+        if not pinned:
+            return np.zeros(shape, dtype=np.float32, order="F")
+        # a Fortran-ordered view of page-locked memory
+        return torch.zeros((shape[1], shape[0]), dtype=torch.float32, pin_memory=True).numpy().T
+
     runs = []
-    for multi in (False, True):
+    for mode in ("single", "pageable", "pinned"):
+        multi, pinned = mode != "single", mode == "pinned"
         s = fw.Solver(p, precision=precision)
         s.init(depth, eta, u, v)
         s.step(2)
         names = ("Eta", "U", "Vbar", "Depth")
-        arrs = {n: np.asfortranarray(s.get_f32(n) * np.float32(1.0 + 1e-3)) for n in names}
+        arrs = {}
+        for n in names:
+            arrs[n] = host_array(s.shape(n), pinned)
+            arrs[n][...] = s.get_f32(n) * np.float32(1.0 + 1e-3)
         if multi:
             cn = (ctypes.c_char_p * 4)(*[n.encode() for n in names])
             hp = (ctypes.c_void_p * 4)(*[arrs[n].ctypes.data for n in names])
             assert s.L.fw_set_fields_f32(s.ctx, 4, cn, hp) == 0
-            outs = {n: np.zeros(s.shape(n), dtype=np.float32, order="F") for n in names}
+            outs = {n: host_array(s.shape(n), pinned) for n in names}
             op = (ctypes.c_void_p * 4)(*[outs[n].ctypes.data for n in names])
             assert s.L.fw_get_fields_f32(s.ctx, 4, cn, op) == 0
             for n in names:
@@ -74,3 +88,4 @@ def test_f32_multi_field_transfers(fw, precision):
         runs.append(s.get("Eta"))
         s.close()
     assert np.array_equal(runs[0], runs[1])
+    assert np.array_equal(runs[0], runs[2])
