@@ -276,7 +276,7 @@ def link_rates(nbytes, reps=10):
     return out
 
 
-def ensemble_bench(fw, pg, ws, n=512, K=10, W=2, run_seconds=300.0, autotune=True):
+def ensemble_bench(fw, pg, ws, n=512, K=100, W=2, run_seconds=300.0, autotune=True):
     """The 512-run ensemble (planar beaches of uneven size, slope, depth and
     JONSWAP forcing; 1.5e8 cells in all): every member steps concurrently,
     as one parent CUDA graph per two steps (fw_ensemble_run; the headline)
