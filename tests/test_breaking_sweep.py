@@ -9,8 +9,8 @@ link; here DT = 1 s on 20 m of water (crossing time 1/14 s per cell) makes
 every candidate carry the age on, and chains run across the grid.  Each
 BREAK_PASSES value (0: the level-ordered pass alone; 1, 3, 8: both; a
 million: passes alone) must give the oracle's sequential sweep bit for bit.
-Whole mixed and FP64 steps with the level-ordered pass alone give the same
-state as with the default.
+The mixed build's sweep breaks the same cells.  Whole mixed and FP64 steps
+with the level-ordered pass alone give the same state as with the default.
 """
 import numpy as np
 import pytest
@@ -83,6 +83,32 @@ def test_long_chains_match_oracle(fw, oracle_mod, passes):
     s.wave_breaking()
     o.call("wave_breaking")
     assert np.array_equal(_ring(s.get("AGE")), _ring(o["AGE"]))
+    s.close()
+    o.close()
+
+
+@pytest.mark.parametrize("passes", [0, 8])
+def test_long_chains_mixed(fw, oracle_mod, passes):
+    """The same sweep in the mixed build: the float tests decide as the
+    oracle's double ones on these well-separated values, so the same cells
+    break, with ages equal to float rounding.  It also checks that a DT set
+    from the host reaches the mixed build's float copy."""
+    params, depth, _ = fw.cases.planar_beach(Mglob=96, Nglob=64, seed=61)
+    s, o = make_pair(fw, oracle_mod, params, depth, precision="MIXED")
+    fields = _fields(s.Mloc, s.Nloc, s.scalar("T_brk"), seed=62)
+    for name, a in fields.items():
+        s.set(name, a)
+        o[name][:] = a
+    s.set_scalar("DT", 1.0)
+    o.set_scalar("DT", 1.0)
+    s.set_scalar("BREAK_PASSES", passes)
+    s.wave_breaking()
+    o.call("wave_breaking")
+    a, b = _ring(s.get("AGE")), _ring(o["AGE"])
+    assert ((b == 1.0).sum()) > 2000
+    assert np.array_equal(a > 0, b > 0)
+    assert np.array_equal(a == 1.0, b == 1.0)
+    assert np.allclose(a, b, rtol=1e-6, atol=0.0)
     s.close()
     o.close()
 
