@@ -433,6 +433,27 @@ def precision_report(fw, size=4096, t_end=33.0, t_steady=12.0, t_mean=20.0):
     }
 
 
+def fp64_only(fw, size, K, W):
+    """The FP64 path alone on the size x size shoal workload: W warm-up
+    steps, then K steps timed with CUDA events on the library's stream."""
+    import torch
+    torch.cuda.set_device(0)
+    params, depth, phases = fw.cases.shoal_jonswap(Mglob=size, Nglob=size, seed=2024)
+    s = fw.Solver(fw.with_defaults(params), precision="FP64")
+    s.init(depth, phases=phases)
+    s.step(W)
+    ext, e0, e1 = cuda_timer(s)
+    s.sync()
+    e0.record(ext)
+    st = s.step(K, check=False)
+    e1.record(ext)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / max(K, 1)
+    s.close()
+    return {"metric": "FP64 cell-steps/s", "value": size * size / (ms * 1e-3), "unit": "cell-steps/s",
+            "ms_per_step": ms, "steps": K, "warmup": W, "grid": [size, size], "status": st}
+
+
 def net_report(fw, size=1024, reps=20):
     """The correction network alone, on a size x size coarse grid: the
     forward pass (packing, four tcgen05 convolutions) and one training
@@ -862,6 +883,8 @@ def main():
                     help="only the 4096x4096 barred-beach mixed-vs-FP64 report (about 10 GPU minutes)")
     ap.add_argument("--no-kernel-profile", action="store_true",
                     help="skip the per-kernel timing (e.g. for an ncu launch list of the stepping only)")
+    ap.add_argument("--fp64-only", action="store_true",
+                    help="only the FP64 path on the --size workload: --warmup then --steps steps (e.g. for ncu)")
     args = ap.parse_args()
     fw = __graft_entry__.load_package()
     params, depth, phases = fw.cases.shoal_jonswap(Mglob=args.size, Nglob=args.size, seed=2024)
@@ -870,6 +893,9 @@ def main():
         return reference_arm(args, fw, params, depth, phases)
     if args.net_report:
         print(json.dumps(net_report(fw)), flush=True)
+        return 0
+    if args.fp64_only:
+        print(json.dumps(fp64_only(fw, args.size, args.steps, args.warmup)), flush=True)
         return 0
     if args.learned_full:
         print(json.dumps(learned_full_report(fw)), flush=True)
