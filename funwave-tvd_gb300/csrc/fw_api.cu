@@ -931,7 +931,6 @@ int fw_get_scalar(fw_ctx *c, const char *name, double *v) {
     else if (!std::strcmp(name, "pitch")) *v = c->g.pitch;
     else if (!std::strcmp(name, "WAIT_LIMIT")) *v = c->fmaps[0][0][0].wait_limit;
     else if (!std::strcmp(name, "BREAK_PASSES")) *v = c->g.brk_passes;
-    else if (!std::strcmp(name, "FUSED_UPDATE")) *v = c->fused_update;
     else return FW_ERR_BAD_PARAM;
     return FW_OK;
 }
@@ -957,9 +956,6 @@ int fw_set_scalar(fw_ctx *c, const char *name, double v) {
     } else if (!std::strcmp(name, "BREAK_PASSES")) {
         if (!(v >= 0.0 && v <= 1.0e6)) return FW_ERR_BAD_PARAM;
         c->g.brk_passes = (int)v;
-    } else if (!std::strcmp(name, "FUSED_UPDATE")) {
-        if (v != 0.0 && v != 1.0) return FW_ERR_BAD_PARAM;
-        c->fused_update = (int)v;
     } else if (!std::strcmp(name, "T_brk")) {
         c->g.T_brk = v;
         fill_float_constants(c->g);

@@ -209,7 +209,6 @@ struct fw_ctx {
     void *staging = nullptr;     // one host-layout plane for field transfers
     size_t arena_bytes = 0;
     int ncand_cap = 0;
-    int fused_update = 1;        // mixed steps: FLUXES folded into the update (k_flux_update); FUSED_UPDATE
     long long launches = 0;
     int initialized = 0;
     int sticky_error = 0;        // first CUDA error seen by a launcher

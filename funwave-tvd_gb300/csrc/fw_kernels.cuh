@@ -460,74 +460,6 @@ __device__ __forceinline__ void ho_lr(T vm1, T v0, T d0, T d1, T d2, T &L, T &R)
     }
 }
 
-// One face of direction DIR from the limited left and right values of U, V,
-// HU, HV, Eta, U4, V4 (Lv, Rv): the face fluxes, the Zhou wave speeds, HLL
-// and BOUNDARY_CONDITION's wall and dry-cell rules (last write wins).  Dd:
-// Depthx / Depthy at the face; m9: MASK9 at the face's cell (MASK9u of
-// fluxes.F:1333 never differs for the faces computed); pos: the face's
-// index along DIR; mL, mR: MASK of the cells pos-1 and pos.
-template <typename T, int DIR>
-__device__ __forceinline__ void face_flux(const Grid &g, const T (&Lv)[7], const T (&Rv)[7], T Dd, T m9, int pos,
-                                          int mL, int mR, T &Pm, T &Nm, T &Tm) {
-    const T g1 = GC(gamma1), g3 = GC(gamma3);
-    const int lo = DIR == 0 ? g.ib : g.jb, hi = DIR == 0 ? g.ie : g.je;
-    const T UL = Lv[0], UR = Rv[0], VL = Lv[1], VR = Rv[1], HUL = Lv[2], HUR = Rv[2];
-    const T HVL = Lv[3], HVR = Rv[3], EL = Lv[4], ER = Rv[4];
-    const T U4L = Lv[5], U4R = Rv[5], V4L = Lv[6], V4R = Rv[6];
-    const T HL = EL + Dd, HR = ER + Dd;
-    const T nL = DIR == 0 ? UL : VL, nR = DIR == 0 ? UR : VR;
-    const T tL = DIR == 0 ? VL : UL, tR = DIR == 0 ? VR : UR;
-    const T n4L = DIR == 0 ? U4L : V4L, n4R = DIR == 0 ? U4R : V4R;
-    const T t4L = DIR == 0 ? V4L : U4L, t4R = DIR == 0 ? V4R : U4R;
-    const T qnL = DIR == 0 ? HUL : HVL, qnR = DIR == 0 ? HUR : HVR;  // HU for x, HV for y
-    const T qtL = DIR == 0 ? HVL : HUL, qtR = DIR == 0 ? HVR : HUR;
-    // mass flux PL/QL, normal momentum flux FxL/GyL, tangential GxL/FyL
-    const T ML = qnL + g1 * m9 * HL * n4L;
-    const T MR = qnR + g1 * m9 * HR * n4R;
-    const T NL = g3 * ML * (nL + g1 * m9 * n4L) + (T)0.5 * (T)GRAV * ((EL) * (EL)*g3 + (T)2 * (EL) * (Dd));
-    const T NR = g3 * MR * (nR + g1 * m9 * n4R) + (T)0.5 * (T)GRAV * ((ER) * (ER)*g3 + (T)2 * (ER) * (Dd));
-    T TL, TR;
-    if (DIR == 0) {
-        TL = HL * (nL + g1 * m9 * n4L) * (tL + g1 * m9 * t4L) * g3;
-        TR = HR * (nR + g1 * m9 * n4R) * (tR + g1 * m9 * t4R) * g3;
-    } else {
-        TL = HL * (tL + g1 * m9 * t4L) * (nL + g1 * m9 * n4L) * g3;
-        TR = HR * (tR + g1 * m9 * t4R) * (nR + g1 * m9 * n4R) * g3;
-    }
-    // WAVE_SPEED (Zhou et al. 2001)
-    const T SQR_PHI_L = fsqrt((T)GRAV * fabs_(HL));
-    const T SQR_PHI_R = fsqrt((T)GRAV * fabs_(HR));
-    const T SQR_PHI_S = (T)0.5 * (SQR_PHI_L + SQR_PHI_R) + (T)0.25 * (nL - nR);
-    const T U_S = (T)0.5 * (nL + nR) + SQR_PHI_L - SQR_PHI_R;
-    const T SL = tmin(nL - SQR_PHI_L, U_S - SQR_PHI_S);
-    const T SR = tmax(nR + SQR_PHI_R, U_S + SQR_PHI_S);
-    Pm = hll(SL, SR, ML, MR, EL, ER);
-    Nm = hll(SL, SR, NL, NR, qnL, qnR);
-    Tm = hll(SL, SR, TL, TR, qtL, qtR);
-    // BOUNDARY_CONDITION: walls, then the dry-cell loop (last write wins)
-    const bool wall_on = DIR == 0 || !g.periodic;
-    if (wall_on && pos == lo) {
-        Pm = (T)0;
-        Nm = press(ER, Dd, g3);
-        Tm = (T)0;
-    }
-    if (wall_on && pos == hi + 1) {
-        Pm = (T)0;
-        Nm = press(EL, Dd, g3);
-        Tm = (T)0;
-    }
-    if (mL < 1) {
-        Pm = (T)0;
-        Nm = (pos - 1 != hi) ? press(ER, Dd, g3) * m2r<T>(mR) : (T)0;
-        Tm = (T)0;
-    }
-    if (mR < 1) {
-        Pm = (T)0;
-        Nm = (pos != lo) ? press(EL, Dd, g3) * m2r<T>(mL) : (T)0;
-        Tm = (T)0;
-    }
-}
-
 // Faces of direction DIR (0: x-faces, 1: y-faces).  A tile is 32 x FY
 // faces, FY/8 per thread (by default 32 x 8 x-faces and 32 x 32 y-faces,
 // so that the three-cell halo along y is shared by 32 faces; 32 x 16 in
@@ -591,6 +523,7 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
         }
     }
     __syncthreads();
+    const T g1 = GC(gamma1), g3 = GC(gamma3);
     for (int r = 0; r < TL::FPT; r++) {
     const int i = i0 + tx;
     const int j = j0 + ty + r * BY;
@@ -615,13 +548,67 @@ __global__ void __launch_bounds__(256) k_flux(Grid g, Fields<T> f) {
         ho_lr(ro(src[vv] + (cm)), ro(src[vv] + (fid)), din[vv][line][kf - 1], din[vv][line][kf], din[vv][line][kf + 1], Lv[vv],
               Rv[vv]);
     }
+    const T UL = Lv[0], UR = Rv[0], VL = Lv[1], VR = Rv[1], HUL = Lv[2], HUR = Rv[2];
+    const T HVL = Lv[3], HVR = Rv[3], EL = Lv[4], ER = Rv[4];
+    const T U4L = Lv[5], U4R = Rv[5], V4L = Lv[6], V4R = Rv[6];
     const T Dd = DIR == 0 ? ro(f.Depthx + (fid)) : ro(f.Depthy + (fid));
+    const T HL = EL + Dd, HR = ER + Dd;
     // MASK9u(Mloc1,:) = MASK9(Mloc,:) (fluxes.F:1333); the faces computed
     // here never reach that column
     const T m9 = m2r<T>(ro(f.MASK9 + (fid)));
+    const T nL = DIR == 0 ? UL : VL, nR = DIR == 0 ? UR : VR;
+    const T tL = DIR == 0 ? VL : UL, tR = DIR == 0 ? VR : UR;
+    const T n4L = DIR == 0 ? U4L : V4L, n4R = DIR == 0 ? U4R : V4R;
+    const T t4L = DIR == 0 ? V4L : U4L, t4R = DIR == 0 ? V4R : U4R;
+    const T qnL = DIR == 0 ? HUL : HVL, qnR = DIR == 0 ? HUR : HVR;  // HU for x, HV for y
+    const T qtL = DIR == 0 ? HVL : HUL, qtR = DIR == 0 ? HVR : HUR;
+    // mass flux PL/QL, normal momentum flux FxL/GyL, tangential GxL/FyL
+    const T ML = qnL + g1 * m9 * HL * n4L;
+    const T MR = qnR + g1 * m9 * HR * n4R;
+    const T NL = g3 * ML * (nL + g1 * m9 * n4L) + (T)0.5 * (T)GRAV * ((EL) * (EL)*g3 + (T)2 * (EL) * (Dd));
+    const T NR = g3 * MR * (nR + g1 * m9 * n4R) + (T)0.5 * (T)GRAV * ((ER) * (ER)*g3 + (T)2 * (ER) * (Dd));
+    T TL, TR;
+    if (DIR == 0) {
+        TL = HL * (nL + g1 * m9 * n4L) * (tL + g1 * m9 * t4L) * g3;
+        TR = HR * (nR + g1 * m9 * n4R) * (tR + g1 * m9 * t4R) * g3;
+    } else {
+        TL = HL * (tL + g1 * m9 * t4L) * (nL + g1 * m9 * n4L) * g3;
+        TR = HR * (tR + g1 * m9 * t4R) * (nR + g1 * m9 * n4R) * g3;
+    }
+    // WAVE_SPEED (Zhou et al. 2001)
+    const T SQR_PHI_L = fsqrt((T)GRAV * fabs_(HL));
+    const T SQR_PHI_R = fsqrt((T)GRAV * fabs_(HR));
+    const T SQR_PHI_S = (T)0.5 * (SQR_PHI_L + SQR_PHI_R) + (T)0.25 * (nL - nR);
+    const T U_S = (T)0.5 * (nL + nR) + SQR_PHI_L - SQR_PHI_R;
+    const T SL = tmin(nL - SQR_PHI_L, U_S - SQR_PHI_S);
+    const T SR = tmax(nR + SQR_PHI_R, U_S + SQR_PHI_S);
+    T Pm = hll(SL, SR, ML, MR, EL, ER);
+    T Nm = hll(SL, SR, NL, NR, qnL, qnR);
+    T Tm = hll(SL, SR, TL, TR, qtL, qtR);
+    // BOUNDARY_CONDITION: walls, then the dry-cell loop (last write wins)
+    const int pos = DIR == 0 ? i : j;
+    const bool wall_on = DIR == 0 || !g.periodic;
+    if (wall_on && pos == lo) {
+        Pm = (T)0;
+        Nm = press(ER, Dd, g3);
+        Tm = (T)0;
+    }
+    if (wall_on && pos == hi + 1) {
+        Pm = (T)0;
+        Nm = press(EL, Dd, g3);
+        Tm = (T)0;
+    }
     const int mL = ro(f.MASK + (cm)), mR = ro(f.MASK + (fid));  // cells pos-1 and pos
-    T Pm, Nm, Tm;
-    face_flux<T, DIR>(g, Lv, Rv, Dd, m9, DIR == 0 ? i : j, mL, mR, Pm, Nm, Tm);
+    if (mL < 1) {
+        Pm = (T)0;
+        Nm = (pos - 1 != hi) ? press(ER, Dd, g3) * m2r<T>(mR) : (T)0;
+        Tm = (T)0;
+    }
+    if (mR < 1) {
+        Pm = (T)0;
+        Nm = (pos != lo) ? press(EL, Dd, g3) * m2r<T>(mL) : (T)0;
+        Tm = (T)0;
+    }
     if (DIR == 0) {
         f.P[fid] = Pm;
         f.Fx[fid] = Nm;
@@ -710,6 +697,7 @@ __global__ void __launch_bounds__(256) k_flux_tma(Grid g, Fields<T> f, const __g
         }
     }
     __syncthreads();
+    const T g1 = GC(gamma1), g3 = GC(gamma3);
     for (int r = 0; r < TL::FPT; r++) {
     const int i = i0 + tx;
     const int j = j0 + ty + r * BY;
@@ -735,12 +723,68 @@ __global__ void __launch_bounds__(256) k_flux_tma(Grid g, Fields<T> f, const __g
               FLD(vv, DIR == 0 ? line : own + 3, DIR == 0 ? own + 3 : line + 3), din[vv][line][kf - 1],
               din[vv][line][kf], din[vv][line][kf + 1], Lv[vv], Rv[vv]);
     }
+    const T UL = Lv[0], UR = Rv[0], VL = Lv[1], VR = Rv[1], HUL = Lv[2], HUR = Rv[2];
+    const T HVL = Lv[3], HVR = Rv[3], EL = Lv[4], ER = Rv[4];
+    const T U4L = Lv[5], U4R = Rv[5], V4L = Lv[6], V4R = Rv[6];
     const T Dd = DIR == 0 ? ro(f.Depthx + (fid)) : ro(f.Depthy + (fid));
+    const T HL = EL + Dd, HR = ER + Dd;
+    // MASK9u(Mloc1,:) = MASK9(Mloc,:) (fluxes.F:1333); the faces computed
+    // here never reach that column
     const T m9 = m2r<T>(ro(f.MASK9 + (fid)));
+    const T nL = DIR == 0 ? UL : VL, nR = DIR == 0 ? UR : VR;
+    const T tL = DIR == 0 ? VL : UL, tR = DIR == 0 ? VR : UR;
+    const T n4L = DIR == 0 ? U4L : V4L, n4R = DIR == 0 ? U4R : V4R;
+    const T t4L = DIR == 0 ? V4L : U4L, t4R = DIR == 0 ? V4R : U4R;
+    const T qnL = DIR == 0 ? HUL : HVL, qnR = DIR == 0 ? HUR : HVR;  // HU for x, HV for y
+    const T qtL = DIR == 0 ? HVL : HUL, qtR = DIR == 0 ? HVR : HUR;
+    // mass flux PL/QL, normal momentum flux FxL/GyL, tangential GxL/FyL
+    const T ML = qnL + g1 * m9 * HL * n4L;
+    const T MR = qnR + g1 * m9 * HR * n4R;
+    const T NL = g3 * ML * (nL + g1 * m9 * n4L) + (T)0.5 * (T)GRAV * ((EL) * (EL)*g3 + (T)2 * (EL) * (Dd));
+    const T NR = g3 * MR * (nR + g1 * m9 * n4R) + (T)0.5 * (T)GRAV * ((ER) * (ER)*g3 + (T)2 * (ER) * (Dd));
+    T TL, TR;
+    if (DIR == 0) {
+        TL = HL * (nL + g1 * m9 * n4L) * (tL + g1 * m9 * t4L) * g3;
+        TR = HR * (nR + g1 * m9 * n4R) * (tR + g1 * m9 * t4R) * g3;
+    } else {
+        TL = HL * (tL + g1 * m9 * t4L) * (nL + g1 * m9 * n4L) * g3;
+        TR = HR * (tR + g1 * m9 * t4R) * (nR + g1 * m9 * n4R) * g3;
+    }
+    // WAVE_SPEED (Zhou et al. 2001)
+    const T SQR_PHI_L = fsqrt((T)GRAV * fabs_(HL));
+    const T SQR_PHI_R = fsqrt((T)GRAV * fabs_(HR));
+    const T SQR_PHI_S = (T)0.5 * (SQR_PHI_L + SQR_PHI_R) + (T)0.25 * (nL - nR);
+    const T U_S = (T)0.5 * (nL + nR) + SQR_PHI_L - SQR_PHI_R;
+    const T SL = tmin(nL - SQR_PHI_L, U_S - SQR_PHI_S);
+    const T SR = tmax(nR + SQR_PHI_R, U_S + SQR_PHI_S);
+    T Pm = hll(SL, SR, ML, MR, EL, ER);
+    T Nm = hll(SL, SR, NL, NR, qnL, qnR);
+    T Tm = hll(SL, SR, TL, TR, qtL, qtR);
+    // BOUNDARY_CONDITION: walls, then the dry-cell loop (last write wins)
+    const int pos = DIR == 0 ? i : j;
+    const bool wall_on = DIR == 0 || !g.periodic;
+    if (wall_on && pos == lo) {
+        Pm = (T)0;
+        Nm = press(ER, Dd, g3);
+        Tm = (T)0;
+    }
+    if (wall_on && pos == hi + 1) {
+        Pm = (T)0;
+        Nm = press(EL, Dd, g3);
+        Tm = (T)0;
+    }
     const int mL = MSK(DIR == 0 ? line : own + 2, DIR == 0 ? own + 2 : line + 3);  // cell pos-1
     const int mR = MSK(DIR == 0 ? line : own + 3, DIR == 0 ? own + 3 : line + 3);  // cell pos
-    T Pm, Nm, Tm;
-    face_flux<T, DIR>(g, Lv, Rv, Dd, m9, DIR == 0 ? i : j, mL, mR, Pm, Nm, Tm);
+    if (mL < 1) {
+        Pm = (T)0;
+        Nm = (pos - 1 != hi) ? press(ER, Dd, g3) * m2r<T>(mR) : (T)0;
+        Tm = (T)0;
+    }
+    if (mR < 1) {
+        Pm = (T)0;
+        Nm = (pos != lo) ? press(EL, Dd, g3) * m2r<T>(mL) : (T)0;
+        Tm = (T)0;
+    }
     if (!staged) {  // the tile never arrived: poison the fluxes (the step reports NaN)
         Pm = Nm = Tm = fnan<T>();
     }
@@ -762,21 +806,6 @@ __global__ void __launch_bounds__(256) k_flux_tma(Grid g, Fields<T> f, const __g
 
 #undef FLD
 #undef MSK
-
-// The face fluxes a cell's update reads: P, Fx, Gx at its x-faces i and
-// i+1 (0, 1) and Q, Fy, Gy at its y-faces j and j+1.  GlobalFaces reads the
-// arrays the flux kernels wrote; k_flux_update passes the values it keeps in
-// shared memory.
-template <typename T> struct GlobalFaces {
-    const Fields<T> &f;
-    size_t id, ie, in;
-    __device__ __forceinline__ T P(int k) const { return ro(f.P + (k ? ie : id)); }
-    __device__ __forceinline__ T Q(int k) const { return ro(f.Q + (k ? in : id)); }
-    __device__ __forceinline__ T Fx(int k) const { return ro(f.Fx + (k ? ie : id)); }
-    __device__ __forceinline__ T Fy(int k) const { return ro(f.Fy + (k ? in : id)); }
-    __device__ __forceinline__ T Gx(int k) const { return ro(f.Gx + (k ? ie : id)); }
-    __device__ __forceinline__ T Gy(int k) const { return ro(f.Gy + (k ? in : id)); }
-};
 
 // ---------------------------------------------------------------------------
 // SourceTerms (sources.F:56-548) at one interior cell, with the wavemaker
@@ -826,9 +855,9 @@ __device__ __forceinline__ T wavemaker_mass(const Grid &g, const Fields<T> &f, i
 
 // SourceTerms at one cell; BX, BY get BreakSourceX/Y (sources.F:428-456),
 // zero without viscosity breaking
-template <typename T, typename FA>
-__device__ __forceinline__ void source_terms_b(const Grid &g, const Fields<T> &f, int i, int j, T wm, const FA &fa,
-                                               T &SX, T &SY, T &BX, T &BY) {
+template <typename T>
+__device__ __forceinline__ void source_terms_b(const Grid &g, const Fields<T> &f, int i, int j, T wm, T &SX,
+                                               T &SY, T &BX, T &BY) {
     BX = (T)0;
     BY = (T)0;
     constexpr bool EXACT = sizeof(T) == sizeof(double);
@@ -847,7 +876,7 @@ __device__ __forceinline__ void source_terms_b(const Grid &g, const Fields<T> &f
     const T Hm = tmax(f.H[id], mdf);
     const T Eta = f.Eta[id];
     const T U4 = ro(f.U4 + (id)), V4 = ro(f.V4 + (id));
-    const T dPQ = OX(fa.P(1) - fa.P(0)) + OY(fa.Q(1) - fa.Q(0));
+    const T dPQ = OX(ro(f.P + (ie_)) - ro(f.P + (id))) + OY(ro(f.Q + (in_)) - ro(f.Q + (id)));
     const T FrcInsX = -ro(f.Cd + (id)) * U * spd;
     T sx = OX((T)GRAV * (Eta)) * (ro(f.Depthx + (ie_)) - ro(f.Depthx + (id))) * mk + FrcInsX +
            g1 * m9 * Hm *
@@ -899,8 +928,7 @@ template <typename T>
 __device__ __forceinline__ void source_terms(const Grid &g, const Fields<T> &f, int i, int j, T wm, T &SX,
                                              T &SY) {
     T bx, by;
-    const GlobalFaces<T> fa{f, IDX(i, j), IDX(i + 1, j), IDX(i, j + 1)};
-    source_terms_b(g, f, i, j, wm, fa, SX, SY, bx, by);
+    source_terms_b(g, f, i, j, wm, SX, SY, bx, by);
 }
 
 // SourceTerms alone (materialises SourceX, SourceY, WaveMaker_Mass)
@@ -925,14 +953,17 @@ __global__ void __launch_bounds__(256) k_sources(Grid g, Fields<T> f) {
 // with the stage's starting H (etauv_solver.F:94-101), Wsurf = R1
 // (etauv_solver.F:247) and BreakSourceX/Y.
 // ---------------------------------------------------------------------------
-// the update of one interior cell from its face fluxes (fa); the new eta
-// goes to eta_out (f.Eta, or a scratch plane while other tiles still read
-// f.Eta)
-template <typename T, bool RAD, typename FA>
-__device__ __forceinline__ void update_cell(const Grid &g, const Fields<T> &f, int i, int j, T al, T be,
-                                            const FA &fa, T *eta_out) {
+template <typename T, bool RAD = false>
+__global__ void __launch_bounds__(256, sizeof(T) == sizeof(float) ? 4 : 3) k_update(Grid g, Fields<T> f, T al, T be) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.Mloc || j >= g.Nloc) return;
     const size_t id = IDX(i, j);
     const T g3 = GC(gamma3);
+    if (i < g.ib || i > g.ie || j < g.jb || j > g.je) {
+        f.H[id] = f.Eta[id] * g3 + ro(f.Depth + (id));  // H = Eta*Gamma3+Depth on all cells
+        return;
+    }
     if constexpr (sizeof(T) == sizeof(float)) {
         // the right-hand sides' inputs (rows j-1..j+1 of U, V, Depth, the
         // masks), read after this kernel's stores
@@ -952,11 +983,12 @@ __device__ __forceinline__ void update_cell(const Grid &g, const Fields<T> &f, i
     const double TIME = f.dsc[S_TIME];
     const T wm = wavemaker_mass(g, f, i, j, TIME);
     T SX, SY, BX, BY;
-    source_terms_b(g, f, i, j, wm, fa, SX, SY, BX, BY);
+    source_terms_b(g, f, i, j, wm, SX, SY, BX, BY);
 
+    const size_t ie_ = IDX(i + 1, j), in_ = IDX(i, j + 1);
     constexpr bool EXACT = sizeof(T) == sizeof(double);
     const T cdx = EXACT ? (T)1 / DX : GC(rdx), cdy = EXACT ? (T)1 / DY : GC(rdy);
-    T R1 = -cdx * (fa.P(1) * (T)1 + fa.P(0) * (T)-1) - cdy * (fa.Q(1) * (T)1 + fa.Q(0) * (T)-1);
+    T R1 = -cdx * (ro(f.P + (ie_)) * (T)1 + ro(f.P + (id)) * (T)-1) - cdy * (ro(f.Q + (in_)) * (T)1 + ro(f.Q + (id)) * (T)-1);
     if (g.wavemaker != FW_WK_NONE) {
         const T xmk = i2r<T>(i - g.ib) * DX, ymk = i2r<T>(j - g.jb) * DY;
         if (fabs_(xmk - GC(xc_wk)) < GC(width_wk) && fabs_(ymk - GC(yc_wk)) < GC(ywidth_wk) / (T)2)
@@ -964,7 +996,7 @@ __device__ __forceinline__ void update_cell(const Grid &g, const Fields<T> &f, i
     }
     if constexpr (RAD) {
         const size_t PL = (size_t)g.pitch * (size_t)(g.Nloc + 1);
-        const T pc = (T)0.5 * (fa.P(1) + fa.P(0)), qc = (T)0.5 * (fa.Q(1) + fa.Q(0));
+        const T pc = (T)0.5 * (ro(f.P + (ie_)) + ro(f.P + (id))), qc = (T)0.5 * (ro(f.Q + (in_)) + ro(f.Q + (id)));
         const T hm = tmax(f.H[id], GC(min_depth_frc));  // H before this stage's update
         f.rad[RP_PC * PL + id] = pc;
         f.rad[RP_QC * PL + id] = qc;
@@ -979,11 +1011,11 @@ __device__ __forceinline__ void update_cell(const Grid &g, const Fields<T> &f, i
         if (eta < GC(trough)) eta = GC(trough);
         if (eta > GC(crest)) eta = GC(crest);
     }
-    const T R2 = -cdx * (fa.Fx(1) * (T)1 + fa.Fx(0) * (T)-1) - cdy * (fa.Fy(1) * (T)1 + fa.Fy(0) * (T)-1) + SX;
+    const T R2 = -cdx * (ro(f.Fx + (ie_)) * (T)1 + ro(f.Fx + (id)) * (T)-1) - cdy * (ro(f.Fy + (in_)) * (T)1 + ro(f.Fy + (id)) * (T)-1) + SX;
     const T ubar = al * ro(f.Ubar0 + (id)) + be * (f.Ubar[id] + DT * R2);
-    const T R3 = -cdx * (fa.Gx(1) * (T)1 + fa.Gx(0) * (T)-1) - cdy * (fa.Gy(1) * (T)1 + fa.Gy(0) * (T)-1) + SY;
+    const T R3 = -cdx * (ro(f.Gx + (ie_)) * (T)1 + ro(f.Gx + (id)) * (T)-1) - cdy * (ro(f.Gy + (in_)) * (T)1 + ro(f.Gy + (id)) * (T)-1) + SY;
     const T vbar = al * ro(f.Vbar0 + (id)) + be * (f.Vbar[id] + DT * R3);
-    eta_out[id] = eta;
+    f.Eta[id] = eta;
     f.Ubar[id] = ubar;
     f.Vbar[id] = vbar;
     const T H = eta * g3 + ro(f.Depth + (id));
@@ -1031,192 +1063,6 @@ __device__ __forceinline__ void update_cell(const Grid &g, const Fields<T> &f, i
         f.rhs_x[id] = ubar * mk * rH + fg * (g.f_hb1 * dep * dep * Vxy - g.f_b2 * dep * DVxy);
         f.rhs_y[id] = vbar * mk * rH + fg * (g.f_hb1 * dep * dep * Uxy - g.f_b2 * dep * DUxy);
     }
-}
-
-template <typename T, bool RAD = false>
-__global__ void __launch_bounds__(256, sizeof(T) == sizeof(float) ? 4 : 3) k_update(Grid g, Fields<T> f, T al, T be) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.Mloc || j >= g.Nloc) return;
-    const size_t id = IDX(i, j);
-    if (i < g.ib || i > g.ie || j < g.jb || j > g.je) {
-        f.H[id] = f.Eta[id] * GC(gamma3) + ro(f.Depth + (id));  // H = Eta*Gamma3+Depth on all cells
-        return;
-    }
-    const GlobalFaces<T> fa{f, id, IDX(i + 1, j), IDX(i, j + 1)};
-    update_cell<T, RAD>(g, f, i, j, al, be, fa, f.Eta);
-}
-
-// ---------------------------------------------------------------------------
-// FLUXES and ESTIMATE_HUV's update in one kernel (the mixed path): a tile of
-// TX x TY interior cells stages U V HU HV Eta U4 V4 and MASK with a
-// three-cell halo in shared memory, computes Din along x and along y, the
-// (TX+1) x TY x-faces and TX x (TY+1) y-faces the tile's cells need (the
-// same arithmetic as k_flux), keeps their six fluxes in shared memory, and
-// updates its cells from them (update_cell).  P and Q, which the next
-// stage's CAL_DISPERSION reads, go to global memory (each face written by
-// the tile that owns its cell, the last face by the last tile); Fx, Fy, Gx,
-// Gy are never stored.  Other tiles read a tile's cells as their halo while
-// it updates them, so the new eta goes to a scratch plane (the line
-// solver's tc, free until the solves), which k_eta_commit copies into Eta;
-// it also sets the ghost ring's H = Eta*Gamma3 + Depth.  The fluxes are
-// those of k_flux and k_flux_tma, and the update that of k_update.
-// ---------------------------------------------------------------------------
-struct FUTile {
-    static constexpr int TX = 32, TY = 8;              // cells of a tile (one per thread)
-    static constexpr int SW = TX + 6, SH = TY + 6;     // staged cells with the halo
-    static constexpr int NPX = TX + 3, NPY = TY + 3;   // Din positions along x (per row), along y (per column)
-    static constexpr int NPYP = NPY + 2;               // odd stride of the y Din rows
-};
-
-template <typename T> struct SmemFaces {
-    const T (*fx)[FUTile::TY][FUTile::TX + 1];  // [P, Fx, Gx][row][face]
-    const T (*fy)[FUTile::TY + 1][FUTile::TX];  // [Q, Gy, Fy][face][column]
-    int tx, ty;
-    __device__ __forceinline__ T P(int k) const { return fx[0][ty][tx + k]; }
-    __device__ __forceinline__ T Fx(int k) const { return fx[1][ty][tx + k]; }
-    __device__ __forceinline__ T Gx(int k) const { return fx[2][ty][tx + k]; }
-    __device__ __forceinline__ T Q(int k) const { return fy[0][ty + k][tx]; }
-    __device__ __forceinline__ T Gy(int k) const { return fy[1][ty + k][tx]; }
-    __device__ __forceinline__ T Fy(int k) const { return fy[2][ty + k][tx]; }
-};
-
-template <typename T, bool RAD>
-__global__ void __launch_bounds__(256, 3) k_flux_update(Grid g, Fields<T> f, T al, T be) {
-    using U = FUTile;
-    constexpr int TX = U::TX, TY = U::TY, SW = U::SW, SH = U::SH, NPX = U::NPX, NPY = U::NPY, NPYP = U::NPYP;
-    __shared__ T st[7][SH][SW];
-    __shared__ uint8_t sm[SH][SW + 2];
-    __shared__ T dnx[7][TY][NPX];
-    __shared__ T dny[7][TX][NPYP];
-    __shared__ T fx[3][TY][TX + 1];
-    __shared__ T fy[3][TY + 1][TX];
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + ty * TX;
-    const int i0 = g.ib + blockIdx.x * TX, j0 = g.jb + blockIdx.y * TY;
-    const int nvar = g.dispersion ? 7 : 5;
-    const T *src[7] = {f.U, f.V, f.HU, f.HV, f.Eta, f.U4, f.V4};
-    // the staged cells i0-3 .. i0+TX+2 x j0-3 .. j0+TY+2 (zero outside the arrays)
-    for (int e = tid; e < SH * SW; e += TX * TY) {
-        const int r = e / SW, cc = e % SW;
-        const int ci = i0 - 3 + cc, cj = j0 - 3 + r;
-        const bool in = ci < g.Mloc && cj < g.Nloc;
-        const size_t q = in ? IDX(ci, cj) : 0;
-#pragma unroll
-        for (int v = 0; v < 7; v++) st[v][r][cc] = (in && v < nvar) ? ro(src[v] + q) : (T)0;
-        sm[r][cc] = in ? ro(f.MASK + q) : (uint8_t)0;
-    }
-    __syncthreads();
-    // Din along x: row ln, position k is the cell p = i0 - 1 + k (cells
-    // p-2 .. p+1 are staged columns k .. k+3 of row ln + 3)
-    for (int it = tid; it < TY * NPX; it += TX * TY) {
-        const int ln = it / NPX, k = it % NPX;
-        const int p = i0 - 1 + k, cj = j0 + ln;
-        if (cj <= g.je && p >= g.ib - 1 && p <= g.ie + 2) {
-            int m[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) m[q] = sm[ln + 3][k + q];
-#pragma unroll
-            for (int v = 0; v < 7; v++) {
-                if (v < nvar) {
-                    T w[4];
-#pragma unroll
-                    for (int q = 0; q < 4; q++) w[q] = st[v][ln + 3][k + q];
-                    dnx[v][ln][k] = ho_din(w, m);
-                }
-            }
-        }
-    }
-    // Din along y: column ln, position k is the cell p = j0 - 1 + k (staged
-    // rows k .. k+3 of column ln + 3)
-    for (int it = tid; it < TX * NPY; it += TX * TY) {
-        const int ln = it % TX, k = it / TX;
-        const int p = j0 - 1 + k, ci = i0 + ln;
-        if (ci <= g.ie && p >= g.jb - 1 && p <= g.je + 2) {
-            int m[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) m[q] = sm[k + q][ln + 3];
-#pragma unroll
-            for (int v = 0; v < 7; v++) {
-                if (v < nvar) {
-                    T w[4];
-#pragma unroll
-                    for (int q = 0; q < 4; q++) w[q] = st[v][k + q][ln + 3];
-                    dny[v][ln][k] = ho_din(w, m);
-                }
-            }
-        }
-    }
-    __syncthreads();
-    // x-faces i0 .. i0+TX of rows j0 .. j0+TY-1
-    for (int it = tid; it < TY * (TX + 1); it += TX * TY) {
-        const int line = it / (TX + 1), own = it % (TX + 1);
-        const int i = i0 + own, j = j0 + line;
-        if (i > g.ie + 1 || j > g.je) continue;
-        const int fid = i + j * g.pitch;
-        T Lv[7], Rv[7];
-#pragma unroll
-        for (int v = 0; v < 7; v++) {
-            if (v >= nvar) {
-                Lv[v] = (T)0;
-                Rv[v] = (T)0;
-                continue;
-            }
-            ho_lr(st[v][line + 3][own + 2], st[v][line + 3][own + 3], dnx[v][line][own], dnx[v][line][own + 1],
-                  dnx[v][line][own + 2], Lv[v], Rv[v]);
-        }
-        const T Dd = ro(f.Depthx + (fid));
-        const T m9 = m2r<T>(ro(f.MASK9 + (fid)));
-        T Pm, Nm, Tm;
-        face_flux<T, 0>(g, Lv, Rv, Dd, m9, i, sm[line + 3][own + 2], sm[line + 3][own + 3], Pm, Nm, Tm);
-        fx[0][line][own] = Pm;
-        fx[1][line][own] = Nm;
-        fx[2][line][own] = Tm;
-        if (own < TX || i == g.ie + 1) f.P[fid] = Pm;
-    }
-    // y-faces j0 .. j0+TY of columns i0 .. i0+TX-1
-    for (int it = tid; it < (TY + 1) * TX; it += TX * TY) {
-        const int own = it / TX, line = it % TX;
-        const int i = i0 + line, j = j0 + own;
-        if (i > g.ie || j > g.je + 1) continue;
-        const int fid = i + j * g.pitch;
-        T Lv[7], Rv[7];
-#pragma unroll
-        for (int v = 0; v < 7; v++) {
-            if (v >= nvar) {
-                Lv[v] = (T)0;
-                Rv[v] = (T)0;
-                continue;
-            }
-            ho_lr(st[v][own + 2][line + 3], st[v][own + 3][line + 3], dny[v][line][own], dny[v][line][own + 1],
-                  dny[v][line][own + 2], Lv[v], Rv[v]);
-        }
-        const T Dd = ro(f.Depthy + (fid));
-        const T m9 = m2r<T>(ro(f.MASK9 + (fid)));
-        T Pm, Nm, Tm;
-        face_flux<T, 1>(g, Lv, Rv, Dd, m9, j, sm[own + 2][line + 3], sm[own + 3][line + 3], Pm, Nm, Tm);
-        fy[0][own][line] = Pm;
-        fy[1][own][line] = Nm;
-        fy[2][own][line] = Tm;
-        if (own < TY || j == g.je + 1) f.Q[fid] = Pm;
-    }
-    __syncthreads();
-    const int i = i0 + tx, j = j0 + ty;
-    if (i > g.ie || j > g.je) return;
-    const SmemFaces<T> fa{fx, fy, tx, ty};
-    update_cell<T, RAD>(g, f, i, j, al, be, fa, reinterpret_cast<T *>(f.tc));
-}
-
-// after k_flux_update: the new eta of the interior from the scratch plane
-// into Eta, and H = Eta*Gamma3 + Depth on the ghost ring (k_update's ghost
-// cells)
-template <typename T>
-__global__ void __launch_bounds__(256) k_eta_commit(Grid g, Fields<T> f) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.Mloc || j >= g.Nloc) return;
-    const size_t id = IDX(i, j);
-    if (i < g.ib || i > g.ie || j < g.jb || j > g.je) f.H[id] = f.Eta[id] * GC(gamma3) + ro(f.Depth + (id));
-    else f.Eta[id] = reinterpret_cast<const T *>(f.tc)[id];
 }
 
 // ---------------------------------------------------------------------------
@@ -3618,8 +3464,7 @@ static bool launch_tri(fw_ctx *c, const LinePart &lp, bool fac = true, bool clea
 
 // ESTIMATE_HUV; with_post = false leaves the GET_Eta_U_V_HU_HV tail (k_post)
 // to the fused kernel of the stage
-// fused: FLUXES and the update in one kernel (k_flux_update, mixed path)
-template <typename T> static void launch_estimate_huv_opt(fw_ctx *c, int istage, bool with_post, bool fused = false) {
+template <typename T> static void launch_estimate_huv_opt(fw_ctx *c, int istage, bool with_post) {
     const Grid &g = c->g;
     static const double AL[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0};
     static const double BE[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
@@ -3627,26 +3472,13 @@ template <typename T> static void launch_estimate_huv_opt(fw_ctx *c, int istage,
     // stage 2 too: with PERIODIC, EXCHANGE leaves the x-ghost values of the
     // previous exchange in the ghost corners (bc.F:735-740), so the last
     // stage's corners hold the second stage's values
-    const bool rad = istage >= 2 && g.track_rad;
-    if constexpr (sizeof(T) == sizeof(float)) {
-        if (fused) {
-            const dim3 b(FUTile::TX, FUTile::TY);
-            const dim3 gr((g.Mglob + FUTile::TX - 1) / FUTile::TX, (g.Nglob + FUTile::TY - 1) / FUTile::TY);
-            if (rad) k_flux_update<T, true><<<gr, b, 0, c->stream>>>(g, c->F<T>(), al, be);
-            else k_flux_update<T, false><<<gr, b, 0, c->stream>>>(g, c->F<T>(), al, be);
-            k_eta_commit<T><<<grid2(g.Mloc, g.Nloc, B2D), B2D, 0, c->stream>>>(g, c->F<T>());
-            note(c, 2);
-        }
-    }
-    if (!fused) {
-        if (rad)
-            k_update<T, true><<<grid2(g.Mloc, g.Nloc, c->blk(TK_UPDATE)), c->blk(TK_UPDATE), 0, c->stream>>>(
-                g, c->F<T>(), al, be);
-        else
-            k_update<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_UPDATE)), c->blk(TK_UPDATE), 0, c->stream>>>(g, c->F<T>(),
-                                                                                                         al, be);
-        note(c);
-    }
+    if (istage >= 2 && g.track_rad)
+        k_update<T, true><<<grid2(g.Mloc, g.Nloc, c->blk(TK_UPDATE)), c->blk(TK_UPDATE), 0, c->stream>>>(
+            g, c->F<T>(), al, be);
+    else
+        k_update<T><<<grid2(g.Mloc, g.Nloc, c->blk(TK_UPDATE)), c->blk(TK_UPDATE), 0, c->stream>>>(g, c->F<T>(), al,
+                                                                                                     be);
+    note(c);
     if (g.dispersion) {
         if (sizeof(T) == sizeof(float) && c->factored) {
             // factor both directions (when MASK9 changed) in one launch each,
@@ -3768,13 +3600,11 @@ template <typename T> void launch_end_step(fw_ctx *c) {
 template <typename T> void launch_stage(fw_ctx *c, int istage) {
     const Grid &g = c->g;
     if (g.dispersion) launch_dispersion<T>(c);
-    // mixed steps with the fused tail below fold FLUXES into the update
-    const bool fused = sizeof(T) == sizeof(float) && c->fused_update && g.dispersion && g.show_breaking;
-    if (!fused) launch_fluxes<T>(c);
+    launch_fluxes<T>(c);
     if (g.dispersion && g.show_breaking) {
         // GET_Eta_U_V_HU_HV tail + UPDATE_MASK + BREAKING (parallel part)
         // in one kernel, then the breaking sweep's candidates
-        launch_estimate_huv_opt<T>(c, istage, false, fused);
+        launch_estimate_huv_opt<T>(c, istage, false);
         k_post_mask_break<T><<<grid2(g.Mloc + 1, g.Nloc + 1, c->blk(TK_PMB)), c->blk(TK_PMB), 0, c->stream>>>(g, c->F<T>());
         note(c);
         auto &F = c->F<T>();

@@ -186,12 +186,7 @@ int fw_get_points(fw_ctx *ctx, const char *name, int n, const int *I, const int 
  * parallel passes of BREAKING's candidate sweep (breaker.F:182-224) before
  * the rest runs in one pass ordered by level i + 2j (default 8; 0 = the
  * level-ordered pass only).  Every value gives the sweep's result; it only
- * moves the time.  Setting it drops the captured step graphs.
- * "FUSED_UPDATE" (get and set, 1 or 0; not a reference quantity): whether a
- * mixed context's steps compute FLUXES inside the update kernel (default 1)
- * or with the separate flux kernels.  Both give the same state; the fused
- * steps do not store Fx, Fy, Gx, Gy, which fw_fluxes still does.  Setting
- * it drops the captured step graphs. */
+ * moves the time.  Setting it drops the captured step graphs. */
 int fw_get_scalar(fw_ctx *ctx, const char *name, double *value);
 int fw_set_scalar(fw_ctx *ctx, const char *name, double value);
 

@@ -2,21 +2,18 @@
 counterpart.  Every candidate shape must compute the same values bit for bit
 (the tuned kernels are per-cell or per-face), the tuning must leave a run's
 state as it found it, and shapes outside the compiled candidates are
-refused.  The mixed steps' fused flux and update kernel (FUSED_UPDATE, the
-default) gives the state of the separate flux kernels bit for bit."""
+refused."""
 import numpy as np
 import pytest
 
 FIELDS = ("Eta", "U", "V", "HU", "HV", "Ubar", "Vbar", "MASK", "MASK9", "AGE")
 
 
-def _run(fw, precision, nsteps, tuning=None, autotune_after=None, fused=None):
+def _run(fw, precision, nsteps, tuning=None, autotune_after=None):
     # 200 x 72 cells: no tile or block shape divides the grid evenly
     p, d, _ = fw.cases.planar_beach(Mglob=200, Nglob=72, seed=4)
     s = fw.Solver(fw.with_defaults(p), precision=precision)
     s.init(d)
-    if fused is not None:
-        s.set_scalar("FUSED_UPDATE", fused)
     if tuning is not None:
         s.set_tuning(tuning)
     if autotune_after is None:
@@ -59,9 +56,7 @@ def test_every_launch_shape_computes_the_same(fw, precision):
          "flux_x": 8, "flux_y": 32 if precision == "MIXED" else 8, "flux_x_tma": 1, "flux_y_tma": 1},
     ]
     for t in alts:
-        # the mixed steps with the separate flux kernels, whose shapes are
-        # tuned, against the default fused steps (k_flux_update)
-        out = _run(fw, precision, 24, tuning=t, fused=0)
+        out = _run(fw, precision, 24, tuning=t)
         assert out["tuning"] == dict({"flux_x_tma": 0, "flux_y_tma": 0}, **t)
         _same(out, ref)
 

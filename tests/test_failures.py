@@ -27,8 +27,6 @@ def _case(fw, precision, tma=False):
     s = fw.Solver(p, precision=precision)
     s.init(depth, eta, u, v)
     if tma:
-        # the steps with the separate, TMA-staged flux kernels
-        s.set_scalar("FUSED_UPDATE", 0)
         t = s.tuning()
         t.update({"flux_x": 8, "flux_y": 16, "flux_x_tma": 1, "flux_y_tma": 1})
         s.set_tuning(t)
