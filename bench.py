@@ -290,7 +290,7 @@ def ensemble_bench(fw, pg, ws, n=512, K=100, W=2, run_seconds=300.0, autotune=Tr
     ens = fw.Ensemble(members, precision="MIXED", autotune=autotune, single_launch=True)
     t_init = time.perf_counter() - t0
     t0 = time.perf_counter()
-    ens.step(W)  # builds the parent graph
+    ens.step(W, check=False)  # builds the parent graph
     t_graph = time.perf_counter() - t0
     barrier(pg)
     t0 = time.perf_counter()
@@ -298,7 +298,7 @@ def ensemble_bench(fw, pg, ws, n=512, K=100, W=2, run_seconds=300.0, autotune=Tr
     wall = max_over_ranks(time.perf_counter() - t0, pg)
     barrier(pg)
     handle, ens.handle = ens.handle, None  # the same members, round robin
-    ens.step(W)
+    ens.step(W, check=False)
     barrier(pg)
     t0 = time.perf_counter()
     ens.step(K, check=False)

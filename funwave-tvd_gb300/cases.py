@@ -109,9 +109,11 @@ def ensemble_members(n=512, seed=0, nfreq=24, ntheta=8, cells_range=(128 * 256, 
     """n planar-beach runs drawn from one seeded stream: interior cells log-
     uniform in cells_range with the cross-shore/alongshore aspect log-uniform
     in [1/2, 2], dx uniform in [1, 4] m, slope uniform in [1/50, 1/10],
-    offshore depth uniform in [5, 20] m, JON_2D Hs uniform in [0.5, 3] m and
-    Tp uniform in [6, 14] s (gamma 3.3, cos^2s spreading s = 10, nfreq x
-    ntheta components, phases from the stream).  Depth is
+    offshore depth uniform in [5, 20] m, JON_2D Hs uniform in [0.5, 3] m but at
+    most 0.15 of the depth at the wavemaker (higher waves make the internal
+    wavemaker's source region blow up, in the reference's algorithm as
+    here), and Tp uniform in [6, 14] s (gamma 3.3, cos^2s spreading s = 10,
+    nfreq x ntheta components, phases from the stream).  Depth is
     min(h0, slope * (x_shore - x)) with the shoreline at 85 % of the domain,
     so every run has dry land; the wavemaker sits at 20 % and a west sponge
     covers 10 %.  Returns a list of (params, depth, phases)."""
@@ -126,10 +128,11 @@ def ensemble_members(n=512, seed=0, nfreq=24, ntheta=8, cells_range=(128 * 256, 
         dx = float(rng.uniform(1.0, 4.0))
         slope = float(rng.uniform(1.0 / 50.0, 1.0 / 10.0))
         h0 = float(rng.uniform(5.0, 20.0))
-        hs = float(rng.uniform(0.5, 3.0))
+        x_shore = 0.85 * M * dx
+        dep_wk = float(min(h0, slope * (x_shore - 0.2 * M * dx)))
+        hs = float(rng.uniform(0.5, max(0.5, min(3.0, 0.15 * dep_wk))))
         tp = float(rng.uniform(6.0, 14.0))
         x = (np.arange(M) + 0.5) * dx
-        x_shore = 0.85 * M * dx
         h = np.minimum(h0, slope * (x_shore - x))
         depth = np.asfortranarray(np.repeat(h[:, None], N, axis=1))
         phases = np.asfortranarray(rng.uniform(0.0, 2.0 * np.pi, size=(nfreq, ntheta)))
@@ -137,7 +140,7 @@ def ensemble_members(n=512, seed=0, nfreq=24, ntheta=8, cells_range=(128 * 256, 
             "Mglob": M, "Nglob": N, "DX": dx, "DY": dx, "PERIODIC": False, "WAVEMAKER": "JON_2D",
             "Hmo": hs, "FreqPeak": 1.0 / tp, "FreqMin": 0.5 / tp, "FreqMax": 3.0 / tp, "GammaTMA": 3.3,
             "Nfreq": nfreq, "Ntheta": ntheta, "ThetaPeak": 0.0, "SPREADING": "COS2S", "SPREADING_S": 10.0,
-            "DEP_WK": float(min(h0, slope * (x_shore - 0.2 * M * dx))), "Xc_WK": 0.2 * M * dx,
+            "DEP_WK": dep_wk, "Xc_WK": 0.2 * M * dx,
             "Delta_WK": 0.5, "Time_ramp": 1.0, "DIRECT_SPONGE": True, "Sponge_west_width": 0.1 * M * dx,
             "DISPERSION": True, "VISCOSITY_BREAKING": True, "SHOW_BREAKING": True, "CFL": 0.5,
             "MinDepth": 0.01, "MinDepthFrc": 0.1,
