@@ -88,14 +88,17 @@ class Tile:
 
 
 def _exchange(dist, send, recv, torch):
-    """Post every receive and send (peer, tag, array), wait for all."""
-    reqs, bufs = [], []
+    """Post every receive and send (peer, tag, array), wait for all.  The
+    send buffers are held until the waits end."""
+    reqs, bufs, outs = [], [], []
     for peer, tag, shape in recv:
         b = torch.empty(shape, dtype=torch.float64)
         bufs.append(b)
         reqs.append(dist.irecv(b, src=peer, tag=tag))
     for peer, tag, arr in send:
-        reqs.append(dist.isend(torch.from_numpy(np.ascontiguousarray(arr)), dst=peer, tag=tag))
+        t = torch.from_numpy(np.ascontiguousarray(arr, dtype=np.float64))
+        outs.append(t)
+        reqs.append(dist.isend(t, dst=peer, tag=tag))
     for r in reqs:
         r.wait()
     return [b.numpy() for b in bufs]
