@@ -143,33 +143,28 @@ __global__ void k_corr_input(fw::Grid g, fw::Fields<T> f, float *in) {
 }
 
 // The correction acts on the interior cells whose 3 x 3 neighbourhood is
-// wet (MASK of the cell and its eight neighbours) and whose total depth H is
-// at least h_min = 1.5 max_corr + MinDepth: not at the shoreline, where the
-// wet/dry switch is a threshold the network does not see, and only where
-// no accepted correction (at most max_corr, less a mean of at most
-// max_corr / 2) can empty the cell.  (MASK9 is not the wet test: with
-// VISCOSITY_BREAKING it is 1 on every interior cell, dry ones included.)
-template <typename T>
-__device__ __forceinline__ bool corr_cell(const fw::Grid &g, const fw::Fields<T> &f, size_t id, float h_min) {
+// wet (MASK of the cell and its eight neighbours): not on the cells at the
+// shoreline, where the wet/dry switch is a threshold the network does not
+// see.  (MASK9 is not this test: with VISCOSITY_BREAKING it is 1 on every
+// interior cell, dry ones included.)
+template <typename T> __device__ __forceinline__ bool wet3x3(const fw::Grid &g, const fw::Fields<T> &f, size_t id) {
     const uint8_t *m = f.MASK;
     const size_t p = (size_t)g.pitch;
-    return (m[id - p - 1] & m[id - p] & m[id - p + 1] & m[id - 1] & m[id] & m[id + 1] & m[id + p - 1] & m[id + p] &
-            m[id + p + 1]) &&
-           (float)f.H[id] >= h_min;
+    return m[id - p - 1] & m[id - p] & m[id - p + 1] & m[id - 1] & m[id] & m[id + 1] & m[id + p - 1] & m[id + p] &
+           m[id + p + 1];
 }
 // Sums over those cells: [0] the eta correction, [1] the count, [2] max
 // |correction|, [3] the largest amount by which a corrected total depth
 // would fall below MinDepth (bits of non-negative doubles); [4] the
 // decision of k_corr_apply (1 applied, 0 the plain step kept)
 template <typename T>
-__global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, float min_depth,
-                            float h_min) {
+__global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, float min_depth) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     float se = 0.0f, sc = 0.0f, mx = 0.0f, dry = 0.0f;
     if (i < g.Mglob && j < g.Nglob) {
         const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
         const long long p = (long long)i + (long long)j * g.Mglob;
-        if (corr_cell(g, f, id, h_min)) {
+        if (wet3x3(g, f, id)) {
             const float inv = (float)(1.0 / FW_NET_OUT_SCALE);
             se = out[p * NOUT] * inv;
             sc = 1.0f;
@@ -205,15 +200,14 @@ __device__ __forceinline__ bool corr_ok(const double *sums, double max_corr) {
 }
 
 template <typename T>
-__global__ void k_corr_apply(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, double max_corr,
-                             float h_min) {
+__global__ void k_corr_apply(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, double max_corr) {
     const bool ok = corr_ok(sums, max_corr);
     if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) sums[4] = ok ? 1.0 : 0.0;
     if (!ok) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mglob || j >= g.Nglob) return;
     const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
-    if (!corr_cell(g, f, id, h_min)) return;
+    if (!wet3x3(g, f, id)) return;
     const long long p = (long long)i + (long long)j * g.Mglob;
     const double inv = 1.0 / FW_NET_OUT_SCALE;
     const double mean = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
@@ -524,9 +518,8 @@ template <typename T> int correct_enqueue(fw_ctx *c, fw_net *n, double max_corr)
     if (rc != FW_OK) return rc;
     double *sums = n->loss;  // 5 doubles of scratch after the loss slot
     if (cudaMemsetAsync(sums, 0, 6 * sizeof(double), s) != cudaSuccess) return FW_ERR_CUDA;
-    const float h_min = (float)(1.5 * max_corr + c->p.min_depth);
-    k_corr_sums<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, (float)c->p.min_depth, h_min);
-    k_corr_apply<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, max_corr, h_min);
+    k_corr_sums<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, (float)c->p.min_depth);
+    k_corr_apply<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, max_corr);
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
 }
 

@@ -264,8 +264,7 @@ int fw_net_adam(fw_net *net, float lr, float beta1, float beta2, float eps, void
 int fw_net_set_wait_limit(fw_net *net, unsigned polls);
 /* Apply the network to a context's current state.  The correction acts on
  * the interior cells whose 3 x 3 neighbourhood is wet (MASK = 1 on the cell
- * and its eight neighbours) and whose total depth is at least
- * 1.5 max_corr + MinDepth, not at the shoreline: the eta correction is
+ * and its eight neighbours), not at the shoreline: the eta correction is
  * projected to zero mean over those
  * cells (so the volume is unchanged), then eta, u, v (and H, HU, HV, Ubar,
  * Vbar to first order) are corrected there.  The plain step stands
