@@ -505,7 +505,7 @@ def net_report(fw, size=1024, reps=20):
 
 
 def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coarse_steps=2000, batch=8,
-                        n_train=3):
+                        n_train=3, bands=(1, 2)):
     """The learned coarse-grid correction at the configuration's sizes: fine
     runs on 2048 x 2048 cells at dx = 1 m, their coarse twins on 1024 x 1024
     at dx = 2 m; n_traj seeded trajectories (planar, barred and shoal
@@ -515,7 +515,8 @@ def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coar
     initial weights and batch order; then on held-out seeds, per training,
     the one-step error ratio, the eta RMS against the restricted fine run
     after 500 and after eval_coarse_steps coarse steps, and the maximum
-    run-up of fine, plain coarse and corrected coarse runs."""
+    run-up of fine, plain coarse and corrected coarse runs, for each shore
+    band of the correction in bands (fw_net_set_shore_band)."""
     import numpy as np
     import torch
     L = fw.learned
@@ -606,15 +607,20 @@ def learned_full_report(fw, n_traj=10, steps_per_traj=200, iters=4000, eval_coar
               "one_step_error_ratio": ratios, "max_runup_fine_m": ru(fine), "max_runup_plain_m": ru(plain),
               "trainings": []}
         for net in nets:
-            corr, applied = L.rollout(c, eval_coarse_steps, net=net, snaps=(n_short,))
-            c_short = corr["snaps"][n_short]
-            m_short = (p_short[1] > 0) & (c_short[1] > 0)
-            m_long = (plain["MASK"] > 0) & (corr["MASK"] > 0)
-            ev["trainings"].append({
-                "eta_rms_plain_m": [rms(p_short[0], f_short, m_short), rms(plain["Eta"], f_long, m_long)],
-                "eta_rms_corrected_m": [rms(c_short[0], f_short, m_short), rms(corr["Eta"], f_long, m_long)],
-                "max_runup_corrected_m": ru(corr), "corrections_applied": applied,
-                "rejected_by": corr["rejected"]})
+            tr = {}
+            for band in bands:
+                net.set_shore_band(band)
+                corr, applied = L.rollout(c, eval_coarse_steps, net=net, snaps=(n_short,))
+                c_short = corr["snaps"][n_short]
+                m_short = (p_short[1] > 0) & (c_short[1] > 0)
+                m_long = (plain["MASK"] > 0) & (corr["MASK"] > 0)
+                tr["band_%d" % band] = {
+                    "eta_rms_plain_m": [rms(p_short[0], f_short, m_short), rms(plain["Eta"], f_long, m_long)],
+                    "eta_rms_corrected_m": [rms(c_short[0], f_short, m_short), rms(corr["Eta"], f_long, m_long)],
+                    "max_runup_corrected_m": ru(corr), "corrections_applied": applied,
+                    "rejected_by": corr["rejected"]}
+            net.set_shore_band(1)
+            ev["trainings"].append(tr)
         evals.append(ev)
     for net in nets:
         net.close()

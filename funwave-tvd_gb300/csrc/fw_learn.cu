@@ -142,29 +142,34 @@ __global__ void k_corr_input(fw::Grid g, fw::Fields<T> f, float *in) {
     in[p * NIN + 4] = f.MASK[id] ? 1.0f : 0.0f;
 }
 
-// The correction acts on the interior cells whose 3 x 3 neighbourhood is
-// wet (MASK of the cell and its eight neighbours): not on the cells at the
-// shoreline, where the wet/dry switch is a threshold the network does not
-// see.  (MASK9 is not this test: with VISCOSITY_BREAKING it is 1 on every
-// interior cell, dry ones included.)
-template <typename T> __device__ __forceinline__ bool wet3x3(const fw::Grid &g, const fw::Fields<T> &f, size_t id) {
+// The correction acts on the interior cells whose neighbourhood of
+// (2 band + 1) x (2 band + 1) cells is wet (MASK; band 1 by default, at
+// most the ghost width 3; 0: every wet cell): not at the shoreline, where
+// the wet/dry switch is a threshold the network does not see.  (MASK9 is
+// not this test: with VISCOSITY_BREAKING it is 1 on every interior cell,
+// dry ones included.)
+template <typename T>
+__device__ __forceinline__ bool wet_band(const fw::Grid &g, const fw::Fields<T> &f, size_t id, int band) {
     const uint8_t *m = f.MASK;
-    const size_t p = (size_t)g.pitch;
-    return m[id - p - 1] & m[id - p] & m[id - p + 1] & m[id - 1] & m[id] & m[id + 1] & m[id + p - 1] & m[id + p] &
-           m[id + p + 1];
+    const long long p = g.pitch;
+    for (int b = -band; b <= band; b++)
+        for (int a = -band; a <= band; a++)
+            if (!m[(long long)id + a + b * p]) return false;
+    return true;
 }
 // Sums over those cells: [0] the eta correction, [1] the count, [2] max
 // |correction|, [3] the largest amount by which a corrected total depth
 // would fall below MinDepth (bits of non-negative doubles); [4] the
 // decision of k_corr_apply (1 applied, 0 the plain step kept)
 template <typename T>
-__global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, float min_depth) {
+__global__ void k_corr_sums(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, float min_depth,
+                            int band) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     float se = 0.0f, sc = 0.0f, mx = 0.0f, dry = 0.0f;
     if (i < g.Mglob && j < g.Nglob) {
         const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
         const long long p = (long long)i + (long long)j * g.Mglob;
-        if (wet3x3(g, f, id)) {
+        if (wet_band(g, f, id, band)) {
             const float inv = (float)(1.0 / FW_NET_OUT_SCALE);
             se = out[p * NOUT] * inv;
             sc = 1.0f;
@@ -200,14 +205,15 @@ __device__ __forceinline__ bool corr_ok(const double *sums, double max_corr) {
 }
 
 template <typename T>
-__global__ void k_corr_apply(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, double max_corr) {
+__global__ void k_corr_apply(fw::Grid g, fw::Fields<T> f, const float *out, double *sums, double max_corr,
+                             int band) {
     const bool ok = corr_ok(sums, max_corr);
     if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) sums[4] = ok ? 1.0 : 0.0;
     if (!ok) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Mglob || j >= g.Nglob) return;
     const size_t id = (size_t)(i + g.ib) + (size_t)(j + g.jb) * g.pitch;
-    if (!wet3x3(g, f, id)) return;
+    if (!wet_band(g, f, id, band)) return;
     const long long p = (long long)i + (long long)j * g.Mglob;
     const double inv = 1.0 / FW_NET_OUT_SCALE;
     const double mean = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
@@ -264,6 +270,7 @@ struct fw_net {
     // raw eta correction, cells corrected, max |correction|, MinDepth
     // violation, decision
     double last_check[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    int shore_band = 1;         // fw_correct acts where the (2 band + 1)^2 neighbourhood is wet
     // fw_correct_run's graph of two (step + correction) pairs and what it was
     // captured with
     cudaGraphExec_t cexec = nullptr;
@@ -518,8 +525,8 @@ template <typename T> int correct_enqueue(fw_ctx *c, fw_net *n, double max_corr)
     if (rc != FW_OK) return rc;
     double *sums = n->loss;  // 5 doubles of scratch after the loss slot
     if (cudaMemsetAsync(sums, 0, 6 * sizeof(double), s) != cudaSuccess) return FW_ERR_CUDA;
-    k_corr_sums<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, (float)c->p.min_depth);
-    k_corr_apply<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, max_corr);
+    k_corr_sums<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, (float)c->p.min_depth, n->shore_band);
+    k_corr_apply<T><<<gr, b, 0, s>>>(g, f, n->out, sums + 1, max_corr, n->shore_band);
     return cudaGetLastError() == cudaSuccess ? FW_OK : FW_ERR_CUDA;
 }
 
@@ -607,6 +614,17 @@ int fw_net_create(unsigned long long seed, fw_net **out) {
         return FW_ERR_OOM;
     }
     *out = n;
+    return FW_OK;
+}
+
+int fw_net_set_shore_band(fw_net *n, int cells) {
+    if (!n || cells < 0 || cells > 3) return FW_ERR_BAD_PARAM;
+    n->shore_band = cells;
+    // fw_correct_run's graph holds the old band
+    if (n->cexec) {
+        cudaGraphExecDestroy(n->cexec);
+        n->cexec = nullptr;
+    }
     return FW_OK;
 }
 

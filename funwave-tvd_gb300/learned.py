@@ -46,6 +46,7 @@ def _bind(L):
     L.fw_correct.argtypes = [vp, vp, ctypes.c_double, ctypes.POINTER(ip)]
     L.fw_correct_run.argtypes = [vp, vp, ip, ctypes.c_double, ctypes.POINTER(ip)]
     L.fw_net_last_check.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+    L.fw_net_set_shore_band.argtypes = [vp, ip]
     return L
 
 
@@ -123,6 +124,11 @@ class Net:
         ap = ctypes.c_int()
         self._ck(self.L.fw_correct(solver.ctx, self.h, float(max_corr), ctypes.byref(ap)), "fw_correct")
         return bool(ap.value)
+
+    def set_shore_band(self, cells=1):
+        """fw_net_set_shore_band: correct only where the (2 cells + 1)^2
+        neighbourhood is wet (0: every wet cell)."""
+        self._ck(self.L.fw_net_set_shore_band(self.h, int(cells)), "fw_net_set_shore_band")
 
     def last_check(self):
         """The checks of the last correct() that waited (fw_net_last_check):

@@ -294,6 +294,11 @@ MODULE FUNWAVE_GPU
       TYPE(C_PTR), VALUE :: net
       REAL(C_DOUBLE), INTENT(OUT) :: out(5)
     END FUNCTION
+    INTEGER(C_INT) FUNCTION fw_net_set_shore_band(net, cells) BIND(C, NAME="fw_net_set_shore_band")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: net
+      INTEGER(C_INT), VALUE :: cells
+    END FUNCTION
     INTEGER(C_INT) FUNCTION fw_correct_run(ctx, net, nsteps, max_corr, status) BIND(C, NAME="fw_correct_run")
       IMPORT :: C_INT, C_PTR, C_DOUBLE
       TYPE(C_PTR), VALUE :: ctx, net

@@ -264,8 +264,8 @@ int fw_net_adam(fw_net *net, float lr, float beta1, float beta2, float eps, void
 int fw_net_set_wait_limit(fw_net *net, unsigned polls);
 /* Apply the network to a context's current state.  The correction acts on
  * the interior cells whose 3 x 3 neighbourhood is wet (MASK = 1 on the cell
- * and its eight neighbours), not at the shoreline: the eta correction is
- * projected to zero mean over those
+ * and its eight neighbours; fw_net_set_shore_band changes the width), not
+ * at the shoreline: the eta correction is projected to zero mean over those
  * cells (so the volume is unchanged), then eta, u, v (and H, HU, HV, Ubar,
  * Vbar to first order) are corrected there.  The plain step stands
  * (*applied = 0) when any |correction| exceeds max_corr, when a value is not
@@ -280,6 +280,9 @@ int fw_correct(fw_ctx *ctx, fw_net *net, double max_corr, int *applied);
  * |correction| (m, m/s), out[3] the largest amount (m) by which a corrected
  * total depth would fall below MinDepth, out[4] 1 if applied else 0. */
 int fw_net_last_check(fw_net *net, double *out);
+/* The cells fw_correct acts on: those whose (2 cells + 1) x (2 cells + 1)
+ * neighbourhood is wet; cells 0..3 (default 1; 0: every wet cell). */
+int fw_net_set_shore_band(fw_net *net, int cells);
 /* nsteps of (fw_step + fw_correct without waiting) on a coarse run, two
  * pairs per replay of one captured CUDA graph; status as fw_step's.  The
  * graph is captured again when the run, its buffer state, its launch

@@ -192,7 +192,8 @@ def test_correction_fallback_checks(fw, precision):
     max_corr, a volume drift (the raw eta correction's mean, which the
     projection would remove) above half of max_corr, or a wet cell pushed to
     or below MinDepth; fw_net_last_check reports the checked values.  A
-    correction acts only on cells whose 3 x 3 neighbourhood is wet.
+    correction acts only on cells whose 3 x 3 neighbourhood is wet (5 x 5
+    with fw_net_set_shore_band(2), every wet cell with 0).
     The output layer's weights are zero here, so the correction is its bias:
     eta bias b_e and u bias b_u, in metres and m/s."""
     import fw_net_oracle as ref
@@ -206,7 +207,7 @@ def test_correction_fallback_checks(fw, precision):
     co = ref.LAYERS[-1][1]
     nlast = 9 * ref.LAYERS[-1][0] * co + co
 
-    def run(b_e, b_u, max_corr, shallow=True):
+    def run(b_e, b_u, max_corr, shallow=True, band=1):
         d = depth if shallow else np.maximum(depth, np.where(depth > 0, 0.2, depth))
         s = fw.Solver(p, precision=precision)
         s.init(d)
@@ -217,12 +218,15 @@ def test_correction_fallback_checks(fw, precision):
         w[-co:][1] = b_u * fw.learned.OUT_SCALE
         net.set_params(w)
         eta0, u0 = s.get("Eta"), s.get("U")
+        net.set_shore_band(band)
         applied = net.correct(s, max_corr=max_corr)
         eta1, u1 = s.get("Eta"), s.get("U")
         m = s.get("MASK") > 0
+        k = band
         wet9 = np.zeros_like(m)
-        wet9[1:-1, 1:-1] = np.all([m[1 + a:m.shape[0] - 1 + a, 1 + b:m.shape[1] - 1 + b]
-                                   for a in (-1, 0, 1) for b in (-1, 0, 1)], axis=0)
+        wet9[k:m.shape[0] - k, k:m.shape[1] - k] = np.all(
+            [m[k + a:m.shape[0] - k + a, k + b:m.shape[1] - k + b] for a in range(-k, k + 1) for b in range(-k, k + 1)],
+            axis=0)
         s.close()
         return applied, eta0, eta1, u0, u1, wet9, net.last_check()
 
@@ -240,13 +244,17 @@ def test_correction_fallback_checks(fw, precision):
     assert abs(c["dry_m"] - 0.02) < 1e-3
     # the same without shallow cells passes: the uniform eta part is
     # projected away (volume kept) and u gets its 0.05 m/s on the cells
-    # whose neighbourhood is wet, nothing at the shoreline
-    a, e0, e1, u0, u1, wet9, c = run(-0.04, 0.05, 0.2, shallow=False)
-    assert a and c["applied"] and c["cells"] == float(wet9[3:-3, 3:-3].sum())
-    assert float(np.abs(e1 - e0).max()) <= 1e-6
-    du = (u1 - u0)[3:-3, 3:-3]
-    m9 = wet9[3:-3, 3:-3]
-    assert m9.any() and (~m9).any()
-    assert np.allclose(du[m9], 0.05, rtol=0, atol=1e-6)
-    assert np.array_equal(du[~m9], np.zeros_like(du[~m9]))
+    # whose neighbourhood is wet, nothing at the shoreline; with a band of 2
+    # cells the 5 x 5 neighbourhood, with 0 every wet cell
+    for band in (1, 2, 0):
+        a, e0, e1, u0, u1, wet9, c = run(-0.04, 0.05, 0.2, shallow=False, band=band)
+        assert a and c["applied"] and c["cells"] == float(wet9[3:-3, 3:-3].sum())
+        assert float(np.abs(e1 - e0).max()) <= 1e-6
+        du = (u1 - u0)[3:-3, 3:-3]
+        m9 = wet9[3:-3, 3:-3]
+        assert m9.any() and (~m9).any()
+        assert np.allclose(du[m9], 0.05, rtol=0, atol=1e-6)
+        assert np.array_equal(du[~m9], np.zeros_like(du[~m9]))
+    with pytest.raises(fw.FwError):
+        net.set_shore_band(4)
     net.close()
