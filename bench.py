@@ -878,7 +878,7 @@ def main():
                     help="learned report: pairs along one coarse run nudged by this fraction toward the fine run")
     ap.add_argument("--learned-scale", type=int, default=1,
                     help="learned report: multiple of the 8 training cases")
-    ap.add_argument("--learned-iters", type=int, default=4000, help="learned report: Adam iterations")
+    ap.add_argument("--learned-iters", type=int, default=4000, help="learned reports: Adam iterations")
     ap.add_argument("--net-report", action="store_true",
                     help="time the correction network's forward pass and training iteration")
     ap.add_argument("--learned-full", action="store_true",
@@ -904,7 +904,7 @@ def main():
         print(json.dumps(fp64_only(fw, args.size, args.steps, args.warmup)), flush=True)
         return 0
     if args.learned_full:
-        print(json.dumps(learned_full_report(fw)), flush=True)
+        print(json.dumps(learned_full_report(fw, iters=args.learned_iters)), flush=True)
         return 0
     if args.learned_report:
         print(json.dumps(learned_report(fw, iters=args.learned_iters, unroll=args.learned_unroll,
