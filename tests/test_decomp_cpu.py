@@ -91,7 +91,7 @@ def _work(rank, ws, port, q, case):
 
 
 @pytest.mark.parametrize("case", [(23, 17, 2, 2, False), (30, 13, 3, 1, False), (12, 26, 1, 2, True),
-                                  (19, 21, 2, 2, True)])
+                                  (19, 21, 2, 2, True), (25, 20, 3, 2, True)])
 def test_decomposed_exchange_steps(case):
     torch = pytest.importorskip("torch")
     M, N, px, py, _ = case
