@@ -16,6 +16,15 @@ def test_member_distribution(fw):
         assert 1.0 <= p["DX"] <= 4.0 and 0.5 <= p["Hmo"] <= 3.0 and 6.0 <= 1.0 / p["FreqPeak"] <= 14.0
         assert d.shape == (p["Mglob"], p["Nglob"]) and (d < 0).any() and d.max() <= 20.0
         assert ph.shape == (p["Nfreq"], p["Ntheta"])
+    # the wave height stays within 0.15 of the depth at the wavemaker (or at
+    # the 0.5 m floor), the bound that keeps the wavemaker's source region
+    # stable in the reference's algorithm
+    hs = np.array([p["Hmo"] for p, _, _ in m])
+    dep = np.array([p["DEP_WK"] for p, _, _ in m])
+    assert (hs <= np.maximum(0.5, 0.15 * dep) + 1e-12).all()
+    # the same seed gives the same members
+    m2 = fw.cases.ensemble_members(8, seed=1)
+    assert all(a[0] == b[0] and np.array_equal(a[1], b[1]) for a, b in zip(m[:8], m2))
 
 
 def test_max_runup_measure(fw):
