@@ -18,8 +18,8 @@ multi-GPU run.  It holds:
   - trid_x_pipelined / trid_y_pipelined: the reference's pipelined Thomas,
     which performs the serial sweep's operations in the serial order, so
     its result equals trid_serial bit for bit;
-  - trid_x_partitioned: the reduced-system (partitioned) solve a GPU
-    decomposition would use instead: each rank reduces its segment of a
+  - trid_x_partitioned / trid_y_partitioned: the reduced-system
+    (partitioned) solve a GPU decomposition would use instead: each rank reduces its segment of a
     line to two boundary unknowns, the ranks exchange those rows, and each
     rank recovers its segment; equal to the serial solve to rounding.
 Arrays are numpy (Mloc, Nloc) with index (i, j), i the x direction, as
@@ -255,12 +255,25 @@ def trid_x_partitioned(tile, a, c, d):
     segment to the rows of its first and last unknowns, all ranks of the
     row gather those rows, solve the reduced system of 2 P unknowns per
     line, and recover their segments."""
+    row = [ix * tile.py + tile.jy for ix in range(tile.px)]  # the ranks sharing these lines, west to east
+    return _partitioned(tile, a, c, d, row, 30)
+
+
+def trid_y_partitioned(tile, a, c, d):
+    """The y lines (non-periodic) by the reduced system over this tile's
+    column of ranks, south to north."""
+    col = [tile.ix * tile.py + jy for jy in range(tile.py)]
+    return _partitioned(tile, a.T, c.T, d.T, col, 40).T
+
+
+def _partitioned(tile, a, c, d, row, tag0):
+    """The reduced-system solve of the lines along axis 0 of this rank's
+    segments, over the ranks of row (in line order)."""
     import torch
     import torch.distributed as dist
     y, v, w = _segment_parts(a, c, d)
     L, n = y.shape
     mine = np.stack([y[0], v[0], w[0], y[L - 1], v[L - 1], w[L - 1]])  # (6, n)
-    row = [ix * tile.py + tile.jy for ix in range(tile.px)]  # the ranks sharing these lines, west to east
     parts = []
     for r in row:
         if r == tile.rank:
@@ -268,8 +281,8 @@ def trid_x_partitioned(tile, a, c, d):
         else:
             parts.append(None)
     # every rank of the row sends its rows to every other one
-    send = [(r, 30 + tile.rank, mine) for r in row if r != tile.rank]
-    recv = [(r, 30 + r, (6, n)) for r in row if r != tile.rank]
+    send = [(r, tag0 + tile.rank, mine) for r in row if r != tile.rank]
+    recv = [(r, tag0 + r, (6, n)) for r in row if r != tile.rank]
     got = _exchange(dist, send, recv, torch)
     k = 0
     for i, r in enumerate(row):

@@ -84,6 +84,8 @@ def _work(rank, ws, port, q, case):
         ys = D.trid_serial(ay.T, cy.T, dy.T).T
         yp = D.trid_y_pipelined(t, ay[i0:i1, j0:j1], cy[i0:i1, j0:j1], dy[i0:i1, j0:j1])
         out["trid_y_pipelined"] = bool(np.array_equal(yp, ys[i0:i1, j0:j1]))
+        yr = D.trid_y_partitioned(t, ay[i0:i1, j0:j1], cy[i0:i1, j0:j1], dy[i0:i1, j0:j1])
+        out["trid_y_partitioned"] = float(np.abs(yr - ys[i0:i1, j0:j1]).max())
         dist.destroy_process_group()
         q.put((rank, out))
     except Exception as e:  # report to the parent instead of hanging it
@@ -110,7 +112,7 @@ def test_decomposed_exchange_steps(case):
         assert "error" not in r, (rank, r)
         assert r["halo"] and r["min"], (rank, r)
         assert r["trid_x_pipelined"] and r["trid_y_pipelined"], (rank, r)
-        assert r["trid_x_partitioned"] <= 1e-13, (rank, r)
+        assert r["trid_x_partitioned"] <= 1e-13 and r["trid_y_partitioned"] <= 1e-13, (rank, r)
 
 
 def test_block_ranges_cover_the_grid():
